@@ -1,0 +1,264 @@
+/*
+ * lpg.h — C ABI of the GB300 per-tick agent step for laser-polio models.
+ *
+ * The reference (laser_polio, pure Python + numba) has no native ABI: its
+ * per-tick path is the SEIR_ABM tick loop (laser_polio/model.py:246-282)
+ * calling each component's step() and log() over host numpy columns.  The
+ * entry points below are what those component classes call instead; each
+ * comment names the reference code it replaces.  Everything crosses this
+ * boundary as plain pointers and sizes: no torch, no CUDA types.
+ *
+ * Conventions
+ *   - Every function returns LPG_OK (0) or a negative lpg_status.  The text
+ *     of the last error is available from lpg_last_error().
+ *   - One handle holds one or more simulations ("replicates") that advance
+ *     in lockstep on one GPU and one CUDA stream.  A handle is not
+ *     thread-safe; calls on one handle must be serialized.
+ *   - Agent columns are passed in the reference's slot order
+ *     (LaserFrame index order, laser_polio/model.py:139-172), length
+ *     `capacity`.  Pointers may be host or device memory (CUDA unified
+ *     addressing decides); NULL means "column absent, use the reference's
+ *     default".
+ *   - Result arrays are int32, row-major [nt][n_nodes] or
+ *     [nt][n_nodes][n_strains], exactly the shapes of sim.results
+ *     (laser_polio/model.py:548-559, 1216, 1267-1272, 1601-1602, 1898-1917,
+ *     2086-2092).
+ */
+#ifndef LPG_H
+#define LPG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LPG_ABI_VERSION 1
+#define LPG_MAX_STRAINS 4
+#define LPG_MAX_SIA_PER_DAY 8
+
+typedef enum {
+  LPG_OK = 0,
+  LPG_ERR_ARG = -1,      /* bad argument (sizes, pointers, parameter ranges) */
+  LPG_ERR_CAPACITY = -2, /* births exceed capacity (LaserFrame.add, model.py:1719) */
+  LPG_ERR_NODE = -3,     /* node id outside [0, n_nodes) */
+  LPG_ERR_TIMEOUT = -4,  /* a bounded device loop gave up */
+  LPG_ERR_CUDA = -5,     /* CUDA runtime error */
+  LPG_ERR_STATE = -6,    /* call out of order (e.g. step before start) */
+  LPG_ERR_NOMEM = -7,    /* device allocation failed */
+  LPG_ERR_INTERNAL = -8  /* an internal consistency check failed */
+} lpg_status;
+
+/* Component mask: which of the five reference components are present
+ * (SEIR_ABM.components, laser_polio/model.py:209-244). */
+enum {
+  LPG_COMP_VD = 1,  /* VitalDynamics_ABM  model.py:1521-1765 */
+  LPG_COMP_DS = 2,  /* DiseaseState_ABM   model.py:505-812   */
+  LPG_COMP_RI = 4,  /* RI_ABM             model.py:1858-1992 */
+  LPG_COMP_SIA = 8, /* SIA_ABM            model.py:2063-2163 */
+  LPG_COMP_TX = 16  /* Transmission_ABM   model.py:1152-1491 */
+};
+
+/* A Distribution (laser_polio/distributions.py:17-102): kind is one of
+ * LPG_DIST_* in the engine headers: 0 constant(value), 1 exponential(scale),
+ * 2 gamma(shape, scale), 3 lognormal(mean, sigma), 4 normal(mean, std),
+ * 5 poisson(lam), 6 uniform(min, max), 7 lognormal_int(mean, sigma). */
+typedef struct {
+  int32_t kind;
+  double p1, p2;
+} lpg_dist;
+
+/* One SIA campaign (SIA_ABM.step, model.py:2099-2156), already resolved to
+ * the tick on which the reference would run it. */
+typedef struct {
+  int32_t tick;
+  int32_t strain;           /* vaccine strain (model.py:2115-2120) */
+  int32_t min_age, max_age; /* inclusive window in days (model.py:2042) */
+  double efficacy;          /* pars.vx_efficacy[vaccinetype] */
+  const uint8_t* node_mask; /* [n_nodes], nonzero = node targeted */
+} lpg_sia_event;
+
+/* One seed_schedule entry (DiseaseState_ABM.step, model.py:759-786). */
+typedef struct {
+  int32_t tick;
+  int32_t node;
+  int32_t is_count; /* 1: value is a head count; 0: value is a prevalence fraction */
+  double value;
+} lpg_seed_event;
+
+/* Everything one simulation needs besides its agent columns.  All pointers
+ * are host pointers and are copied by lpg_create. */
+typedef struct {
+  int32_t n_nodes;
+  int32_t n_strains; /* len(pars.strain_ids), <= LPG_MAX_STRAINS */
+  int32_t nt;        /* pars.dur + 1 */
+  int64_t count;     /* people.count at the start */
+  int64_t capacity;  /* people.capacity */
+  uint64_t seed;     /* keys the counter-based draws */
+  uint32_t components;
+  int32_t stop_if_no_cases;
+
+  /* VitalDynamics_ABM */
+  int32_t vd_step;               /* pars.step_size_VitalDynamics_ABM */
+  const double* birth_rate;      /* [n_nodes] cbr / 365000 (model.py:1669-1675) */
+  const int64_t* km_cumdeaths;   /* cumulative deaths by age-year (utils.py:795-816) */
+  int32_t km_len;                /* entries in km_cumdeaths */
+  int32_t km_max_year;           /* max_year of predict_age_at_death */
+
+  /* DiseaseState_ABM */
+  float p_paralysis;
+  const lpg_seed_event* seeds;
+  int32_t n_seeds;
+  lpg_dist dur_inf;              /* used to redraw timers of seeded agents */
+
+  /* RI_ABM */
+  int32_t ri_step;               /* pars.step_size_RI_ABM */
+  int32_t ri_enabled;            /* 0 when pars.vx_prob_ri is None */
+  int32_t ri_strain;             /* model.py:1934-1940 */
+  const double* vx_prob_ri;      /* [n_nodes] */
+  const double* vx_prob_ipv;     /* [n_nodes] */
+
+  /* SIA_ABM */
+  const lpg_sia_event* sia;
+  int32_t n_sia;
+  const float* vx_prob_sia;      /* [n_nodes] float32 (model.py:2109) */
+
+  /* Transmission_ABM */
+  const double* strain_r0_scalars; /* [n_strains] */
+  const double* network;           /* [n_nodes][n_nodes], network[i][j] = flow i->j */
+  const double* r0_scalars;        /* [n_nodes] */
+  const double* seasonality;       /* [nt] get_seasonality at each tick (utils.py:616-625) */
+  double zero_inflation;           /* pars.node_seeding_zero_inflation */
+  int32_t nb_r;                    /* max(1, round(pars.node_seeding_dispersion)) */
+
+  /* results present before the first tick */
+  const int32_t* pop0;             /* [n_nodes] results.pop[0] (model.py:559) */
+  const int32_t* R_preseed;        /* [nt][n_nodes] added into results.R, or NULL */
+} lpg_sim_desc;
+
+/* Agent columns (LaserFrame properties), reference slot order, length
+ * capacity.  Element types are those of the reference. */
+typedef struct {
+  int8_t* disease_state;         /* model.py:144 */
+  int8_t* strain;                /* model.py:151 */
+  int8_t* exposure_timer;        /* model.py:571 */
+  int8_t* infection_timer;       /* model.py:572 */
+  int8_t* paralysis_timer;       /* model.py:573 */
+  int8_t* potentially_paralyzed; /* model.py:146 */
+  int8_t* paralyzed;             /* model.py:149 */
+  int8_t* ipv_protected;         /* model.py:150 */
+  uint8_t* chronically_missed;   /* model.py:153 */
+  int16_t* node_id;              /* model.py:161 */
+  int16_t* ri_timer;             /* model.py:1891 */
+  float* acq_risk_multiplier;    /* model.py:1201 */
+  float* daily_infectivity;      /* model.py:1204 */
+  int32_t* date_of_birth;        /* model.py:1550 */
+  int32_t* date_of_death;        /* model.py:1603 */
+} lpg_columns;
+
+/* Result arrays to fill; NULL entries are skipped. */
+typedef struct {
+  int32_t* S;
+  int32_t* E;
+  int32_t* I;
+  int32_t* R;
+  int32_t* E_by_strain;
+  int32_t* I_by_strain;
+  int32_t* potentially_paralyzed;
+  int32_t* paralyzed;
+  int32_t* new_potentially_paralyzed;
+  int32_t* new_paralyzed;
+  int32_t* pop;
+  int32_t* births;
+  int32_t* deaths;
+  int32_t* new_exposed;
+  int32_t* new_exposed_by_strain;
+  int32_t* ri_vaccinated;
+  int32_t* ri_protected;
+  int32_t* ri_new_exposed_by_strain;
+  int32_t* ipv_vaccinated;
+  int32_t* sia_vaccinated;
+  int32_t* sia_protected;
+  int32_t* sia_new_exposed_by_strain;
+} lpg_results_view;
+
+typedef struct {
+  int32_t t;       /* next tick to run (SEIR_ABM.t) */
+  int32_t stopped; /* early stop fired (SEIR_ABM.should_stop) */
+  int64_t count;   /* people.count */
+  int32_t error;   /* sticky device-side error (lpg_status), 0 if none */
+} lpg_sim_state;
+
+/* Per-kernel device time accumulated while profiling is on. */
+typedef struct {
+  int32_t n_kernels;
+  const char* names[16];
+  double total_ms[16];
+  int64_t launches[16];
+} lpg_profile;
+
+typedef struct lpg_handle lpg_handle;
+
+/* Library version and the name of the device code it carries. */
+int lpg_version(void);
+
+/* Create a handle for n_sims simulations on CUDA device `device`.
+ * Replaces SEIR_ABM.__init__ + the components setter as far as the device
+ * state is concerned (model.py:101-175, 209-244). */
+int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t device, lpg_handle** out);
+
+/* Bind the starting agent columns of simulation `sim` (copied; the caller
+ * keeps ownership).  Replaces the implicit sharing of sim.people columns
+ * between components (model.py:1288-1298). */
+int lpg_bind_columns(lpg_handle* h, int32_t sim, const lpg_columns* cols);
+
+/* Lay the bound columns out on the device and log tick 0
+ * (SEIR_ABM.run at tick 0: log_results(0), model.py:253-256;
+ * Transmission_ABM.log, model.py:1461-1487). */
+int lpg_start(lpg_handle* h);
+
+/* Advance every simulation by up to n_ticks ticks: for each tick the
+ * components' step() in default_run_order then log(t)
+ * (model.py:257-271; pars.py:99).  A simulation stops at nt or at its
+ * early-stop tick.  Asynchronous: returns once the work is queued. */
+int lpg_step(lpg_handle* h, int32_t n_ticks);
+
+/* Wait for queued work; reports a sticky device-side error if one was set. */
+int lpg_sync(lpg_handle* h);
+
+int lpg_get_state(lpg_handle* h, int32_t sim, lpg_sim_state* out);
+
+/* Copy results of `sim` into caller arrays (sim.results.*). */
+int lpg_read_results(lpg_handle* h, int32_t sim, const lpg_results_view* out);
+
+/* Copy the current agent columns of `sim` back in reference slot order
+ * (slots [0, count) are written; slots past count are left untouched). */
+int lpg_read_columns(lpg_handle* h, int32_t sim, const lpg_columns* out);
+
+/* Diagnostic: recount every node total and selection weight from the agent
+ * columns and compare with the running totals the engine maintains.
+ * LPG_ERR_INTERNAL on any difference. */
+int lpg_check_invariants(lpg_handle* h);
+
+/* Use CUDA graphs for lpg_step (default on).  Off = plain launches. */
+int lpg_set_graphs(lpg_handle* h, int32_t enable);
+
+/* Per-kernel CUDA-event timing of lpg_step (forces plain launches). */
+int lpg_set_profiling(lpg_handle* h, int32_t enable);
+int lpg_read_profile(lpg_handle* h, lpg_profile* out);
+
+/* The CUDA stream the handle launches on, as an opaque pointer. */
+void* lpg_cuda_stream(lpg_handle* h);
+
+/* Number of kernel launches the handle has issued (graph replays count
+ * every kernel node). */
+int64_t lpg_kernel_launches(lpg_handle* h);
+
+const char* lpg_last_error(const lpg_handle* h);
+void lpg_destroy(lpg_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LPG_H */

@@ -1,0 +1,210 @@
+"""ctypes mirror of include/lpg.h.
+
+These structures are the only thing that crosses the C boundary: plain
+integers, doubles and pointers.  They are shared by the engine binding
+(``engine.py``) and by anything else that speaks the same ABI.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+LPG_MAX_STRAINS = 4
+LPG_MAX_SIA_PER_DAY = 8
+
+LPG_OK = 0
+STATUS_NAMES = {
+    0: "LPG_OK",
+    -1: "LPG_ERR_ARG",
+    -2: "LPG_ERR_CAPACITY",
+    -3: "LPG_ERR_NODE",
+    -4: "LPG_ERR_TIMEOUT",
+    -5: "LPG_ERR_CUDA",
+    -6: "LPG_ERR_STATE",
+    -7: "LPG_ERR_NOMEM",
+    -8: "LPG_ERR_INTERNAL",
+}
+
+COMP_VD, COMP_DS, COMP_RI, COMP_SIA, COMP_TX = 1, 2, 4, 8, 16
+COMPONENT_BITS = {
+    "VitalDynamics_ABM": COMP_VD,
+    "DiseaseState_ABM": COMP_DS,
+    "RI_ABM": COMP_RI,
+    "SIA_ABM": COMP_SIA,
+    "Transmission_ABM": COMP_TX,
+}
+
+DIST_KINDS = {
+    "constant": 0,
+    "exponential": 1,
+    "gamma": 2,
+    "lognormal": 3,
+    "normal": 4,
+    "poisson": 5,
+    "uniform": 6,
+    "lognormal_int": 7,
+}
+
+P_i8 = C.POINTER(C.c_int8)
+P_u8 = C.POINTER(C.c_uint8)
+P_i16 = C.POINTER(C.c_int16)
+P_i32 = C.POINTER(C.c_int32)
+P_i64 = C.POINTER(C.c_int64)
+P_f32 = C.POINTER(C.c_float)
+P_f64 = C.POINTER(C.c_double)
+
+
+class lpg_dist(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("p1", C.c_double), ("p2", C.c_double)]
+
+
+class lpg_sia_event(C.Structure):
+    _fields_ = [
+        ("tick", C.c_int32),
+        ("strain", C.c_int32),
+        ("min_age", C.c_int32),
+        ("max_age", C.c_int32),
+        ("efficacy", C.c_double),
+        ("node_mask", P_u8),
+    ]
+
+
+class lpg_seed_event(C.Structure):
+    _fields_ = [("tick", C.c_int32), ("node", C.c_int32), ("is_count", C.c_int32), ("value", C.c_double)]
+
+
+class lpg_sim_desc(C.Structure):
+    _fields_ = [
+        ("n_nodes", C.c_int32),
+        ("n_strains", C.c_int32),
+        ("nt", C.c_int32),
+        ("count", C.c_int64),
+        ("capacity", C.c_int64),
+        ("seed", C.c_uint64),
+        ("components", C.c_uint32),
+        ("stop_if_no_cases", C.c_int32),
+        ("vd_step", C.c_int32),
+        ("birth_rate", P_f64),
+        ("km_cumdeaths", P_i64),
+        ("km_len", C.c_int32),
+        ("km_max_year", C.c_int32),
+        ("p_paralysis", C.c_float),
+        ("seeds", C.POINTER(lpg_seed_event)),
+        ("n_seeds", C.c_int32),
+        ("dur_inf", lpg_dist),
+        ("ri_step", C.c_int32),
+        ("ri_enabled", C.c_int32),
+        ("ri_strain", C.c_int32),
+        ("vx_prob_ri", P_f64),
+        ("vx_prob_ipv", P_f64),
+        ("sia", C.POINTER(lpg_sia_event)),
+        ("n_sia", C.c_int32),
+        ("vx_prob_sia", P_f32),
+        ("strain_r0_scalars", P_f64),
+        ("network", P_f64),
+        ("r0_scalars", P_f64),
+        ("seasonality", P_f64),
+        ("zero_inflation", C.c_double),
+        ("nb_r", C.c_int32),
+        ("pop0", P_i32),
+        ("R_preseed", P_i32),
+    ]
+
+
+COLUMN_FIELDS = [
+    ("disease_state", P_i8, np.int8),
+    ("strain", P_i8, np.int8),
+    ("exposure_timer", P_i8, np.int8),
+    ("infection_timer", P_i8, np.int8),
+    ("paralysis_timer", P_i8, np.int8),
+    ("potentially_paralyzed", P_i8, np.int8),
+    ("paralyzed", P_i8, np.int8),
+    ("ipv_protected", P_i8, np.int8),
+    ("chronically_missed", P_u8, np.uint8),
+    ("node_id", P_i16, np.int16),
+    ("ri_timer", P_i16, np.int16),
+    ("acq_risk_multiplier", P_f32, np.float32),
+    ("daily_infectivity", P_f32, np.float32),
+    ("date_of_birth", P_i32, np.int32),
+    ("date_of_death", P_i32, np.int32),
+]
+
+
+class lpg_columns(C.Structure):
+    _fields_ = [(name, ptype) for name, ptype, _ in COLUMN_FIELDS]
+
+
+RESULT_FIELDS = [
+    ("S", False),
+    ("E", False),
+    ("I", False),
+    ("R", False),
+    ("E_by_strain", True),
+    ("I_by_strain", True),
+    ("potentially_paralyzed", False),
+    ("paralyzed", False),
+    ("new_potentially_paralyzed", False),
+    ("new_paralyzed", False),
+    ("pop", False),
+    ("births", False),
+    ("deaths", False),
+    ("new_exposed", False),
+    ("new_exposed_by_strain", True),
+    ("ri_vaccinated", False),
+    ("ri_protected", False),
+    ("ri_new_exposed_by_strain", True),
+    ("ipv_vaccinated", False),
+    ("sia_vaccinated", False),
+    ("sia_protected", False),
+    ("sia_new_exposed_by_strain", True),
+]
+
+
+class lpg_results_view(C.Structure):
+    _fields_ = [(name, P_i32) for name, _ in RESULT_FIELDS]
+
+
+class lpg_sim_state(C.Structure):
+    _fields_ = [("t", C.c_int32), ("stopped", C.c_int32), ("count", C.c_int64), ("error", C.c_int32)]
+
+
+class lpg_profile(C.Structure):
+    _fields_ = [
+        ("n_kernels", C.c_int32),
+        ("names", C.c_char_p * 16),
+        ("total_ms", C.c_double * 16),
+        ("launches", C.c_int64 * 16),
+    ]
+
+
+def ptr(arr, ctype):
+    """Pointer to the first element of a contiguous numpy array (or NULL)."""
+    if arr is None:
+        return None
+    assert arr.flags["C_CONTIGUOUS"], "arrays crossing the C ABI must be contiguous"
+    return arr.ctypes.data_as(ctype)
+
+
+def make_columns(cols: dict) -> lpg_columns:
+    """Build an lpg_columns from a dict name -> numpy array (missing = NULL)."""
+    out = lpg_columns()
+    for name, ptype, dtype in COLUMN_FIELDS:
+        arr = cols.get(name)
+        if arr is not None:
+            if arr.dtype != dtype:
+                raise TypeError(f"column {name} must be {np.dtype(dtype).name}, got {arr.dtype}")
+            setattr(out, name, ptr(arr, ptype))
+    return out
+
+
+def make_results_view(res: dict) -> lpg_results_view:
+    out = lpg_results_view()
+    for name, _ in RESULT_FIELDS:
+        arr = res.get(name)
+        if arr is not None:
+            if arr.dtype != np.int32:
+                raise TypeError(f"result {name} must be int32")
+            setattr(out, name, ptr(arr, P_i32))
+    return out

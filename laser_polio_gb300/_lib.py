@@ -1,0 +1,146 @@
+"""Loader and thin wrapper of the CUDA engine library (liblpg.so).
+
+The library is built in-tree by ``laser_polio_gb300.build``.  There is no
+fallback: if the library is missing or no CUDA device is present, creating
+a handle raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+from . import _abi
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "liblpg.so"
+_lib = None
+
+# the C entry points and their signatures, as declared in include/lpg.h
+SIGNATURES = {
+    "lpg_version": (C.c_int, []),
+    "lpg_create": (C.c_int, [C.POINTER(_abi.lpg_sim_desc), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "lpg_bind_columns": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(_abi.lpg_columns)]),
+    "lpg_start": (C.c_int, [C.c_void_p]),
+    "lpg_step": (C.c_int, [C.c_void_p, C.c_int32]),
+    "lpg_sync": (C.c_int, [C.c_void_p]),
+    "lpg_get_state": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(_abi.lpg_sim_state)]),
+    "lpg_read_results": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(_abi.lpg_results_view)]),
+    "lpg_read_columns": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(_abi.lpg_columns)]),
+    "lpg_check_invariants": (C.c_int, [C.c_void_p]),
+    "lpg_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
+    "lpg_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
+    "lpg_read_profile": (C.c_int, [C.c_void_p, C.POINTER(_abi.lpg_profile)]),
+    "lpg_cuda_stream": (C.c_void_p, [C.c_void_p]),
+    "lpg_kernel_launches": (C.c_int64, [C.c_void_p]),
+    "lpg_last_error": (C.c_char_p, [C.c_void_p]),
+    "lpg_destroy": (None, [C.c_void_p]),
+}
+
+
+def load(path: os.PathLike | None = None):
+    """Load liblpg.so (building it first if the sources are newer)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path is not None else LIB_PATH
+    if path is None:
+        from . import build as _build
+
+        try:
+            _build.build()
+        except (OSError, FileNotFoundError) as exc:  # nvcc absent: use a prebuilt library if there is one
+            if not p.exists():
+                raise RuntimeError(f"CUDA engine library {p} is missing and could not be built: {exc}") from exc
+    if not p.exists():
+        raise RuntimeError(f"CUDA engine library {p} is missing; run laser_polio_gb300.build")
+    lib = C.CDLL(str(p))
+    for name, (restype, argtypes) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class LpgError(RuntimeError):
+    def __init__(self, code, msg):
+        self.code = code
+        super().__init__(f"{_abi.STATUS_NAMES.get(code, code)}: {msg}")
+
+
+class Handle:
+    """One lpg_handle: simulations that advance together on one GPU."""
+
+    def __init__(self, descs, device: int = 0):
+        self.lib = load()
+        arr = (_abi.lpg_sim_desc * len(descs))(*descs)
+        self._descs = arr
+        h = C.c_void_p()
+        rc = self.lib.lpg_create(arr, len(descs), int(device), C.byref(h))
+        self.h = h
+        self._check(rc)
+
+    def _check(self, rc):
+        if rc != 0:
+            msg = self.lib.lpg_last_error(self.h).decode() if self.h else ""
+            if rc == -2:
+                raise ValueError(msg)
+            raise LpgError(rc, msg)
+
+    def bind_columns(self, sim: int, cols: dict):
+        self._check(self.lib.lpg_bind_columns(self.h, sim, C.byref(_abi.make_columns(cols))))
+
+    def start(self):
+        self._check(self.lib.lpg_start(self.h))
+
+    def step(self, n_ticks: int):
+        self._check(self.lib.lpg_step(self.h, int(n_ticks)))
+
+    def sync(self):
+        self._check(self.lib.lpg_sync(self.h))
+
+    def state(self, sim: int = 0) -> _abi.lpg_sim_state:
+        st = _abi.lpg_sim_state()
+        self._check(self.lib.lpg_get_state(self.h, sim, C.byref(st)))
+        if st.error:
+            self.sync()
+        return st
+
+    def read_results(self, sim: int, res: dict):
+        self._check(self.lib.lpg_read_results(self.h, sim, C.byref(_abi.make_results_view(res))))
+
+    def read_columns(self, sim: int, cols: dict):
+        self._check(self.lib.lpg_read_columns(self.h, sim, C.byref(_abi.make_columns(cols))))
+
+    def check_invariants(self):
+        self._check(self.lib.lpg_check_invariants(self.h))
+
+    def set_graphs(self, on: bool):
+        self._check(self.lib.lpg_set_graphs(self.h, int(bool(on))))
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.lpg_set_profiling(self.h, int(bool(on))))
+
+    def profile(self) -> dict:
+        p = _abi.lpg_profile()
+        self._check(self.lib.lpg_read_profile(self.h, C.byref(p)))
+        return {p.names[k].decode(): (p.total_ms[k], p.launches[k]) for k in range(p.n_kernels)}
+
+    def cuda_stream(self) -> int:
+        return self.lib.lpg_cuda_stream(self.h) or 0
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.lpg_kernel_launches(self.h))
+
+    def close(self):
+        if self.h:
+            self.lib.lpg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,185 @@
+/*
+ * lpg_detmath.h — deterministic double-precision elementary functions.
+ *
+ * Every function here is built from IEEE-754 operations that are correctly
+ * rounded on every target this project compiles for (add, sub, mul, div,
+ * sqrt, floor, and exact power-of-two scaling), evaluated in a fixed order.
+ * Compiled with contraction disabled (gcc -ffp-contract=off, nvcc
+ * --fmad=false) the same input gives the same bits on x86-64, aarch64 and
+ * sm_103a.  That is what lets the CUDA engine and the CPU oracle consume one
+ * counter-based random stream and agree bit for bit on every integer draw
+ * that depends on an exp() or a log() (Poisson counts, gamma variates,
+ * probabilities of exposure).
+ *
+ * Methods (all textbook mathematics, coefficients derived from first
+ * principles, not taken from any vendor library):
+ *   exp    Cody–Waite reduction x = k ln2 + r with a two-part ln2
+ *          (high part with 33 significant bits so k*hi is exact), then the
+ *          Taylor series of e^r to degree 14 (|r| <= ln2/2, truncation error
+ *          below 1e-18 relative), then exact scaling by 2^k.
+ *   expm1  the same Taylor series without its constant term when
+ *          |x| < ln2/2 (full relative precision for tiny rates), else exp-1.
+ *   log    x = m 2^e with m in [sqrt(1/2), sqrt(2)), log m = 2 atanh(s),
+ *          s = (m-1)/(m+1), |s| <= 0.1716, atanh series to s^25.
+ *   lfact  log(k!) exactly from the double k! for k < 20, else Stirling's
+ *          series for log Gamma(k+1) to the x^-7 term.
+ * Accuracy is a few ulp; the tests compare against numpy.
+ */
+#ifndef LPG_DETMATH_H
+#define LPG_DETMATH_H
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define LPG_HD __host__ __device__ __forceinline__
+#else
+#define LPG_HD static inline
+#endif
+
+#if !defined(__CUDACC__)
+#include <math.h>
+#include <string.h>
+#endif
+
+/* ln 2 split: LN2_HI = ln2 rounded to double with its low 20 mantissa bits
+ * cleared; LN2_LO = ln2 - LN2_HI rounded to double. */
+#define LPG_LN2_HI 0x1.62e42fef00000p-1
+#define LPG_LN2_LO 0x1.473de6af278edp-34
+#define LPG_INV_LN2 0x1.71547652b82fep+0
+#define LPG_SQRT2 0x1.6a09e667f3bcdp+0
+#define LPG_HALF_LOG_2PI 0x1.d67f1c864beb5p-1
+
+LPG_HD uint64_t lpg_dbits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t u;
+  memcpy(&u, &x, sizeof u);
+  return u;
+#endif
+}
+
+LPG_HD double lpg_bitsd(uint64_t u) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  memcpy(&x, &u, sizeof x);
+  return x;
+#endif
+}
+
+/* 2^k for -1022 <= k <= 1023, built from the exponent field. */
+LPG_HD double lpg_pow2i(int k) { return lpg_bitsd((uint64_t)(k + 1023) << 52); }
+
+/* p * 2^k, exact whenever the result is a normal double. */
+LPG_HD double lpg_scale2(double p, int k) {
+  if (k > 1023) return (p * lpg_pow2i(1023)) * lpg_pow2i(k - 1023);
+  if (k < -1022) return (p * lpg_pow2i(k + 600)) * lpg_pow2i(-600);
+  return p * lpg_pow2i(k);
+}
+
+/* Horner evaluation of sum_{n=0}^{14} r^n / n! (coefficients are the
+ * correctly rounded reciprocals of the exact double factorials). */
+LPG_HD double lpg_exp_series(double r) {
+  double p = 1.0 / 87178291200.0;            /* 1/14! */
+  p = p * r + 1.0 / 6227020800.0;            /* 1/13! */
+  p = p * r + 1.0 / 479001600.0;             /* 1/12! */
+  p = p * r + 1.0 / 39916800.0;              /* 1/11! */
+  p = p * r + 1.0 / 3628800.0;               /* 1/10! */
+  p = p * r + 1.0 / 362880.0;                /* 1/9!  */
+  p = p * r + 1.0 / 40320.0;                 /* 1/8!  */
+  p = p * r + 1.0 / 5040.0;                  /* 1/7!  */
+  p = p * r + 1.0 / 720.0;                   /* 1/6!  */
+  p = p * r + 1.0 / 120.0;                   /* 1/5!  */
+  p = p * r + 1.0 / 24.0;                    /* 1/4!  */
+  p = p * r + 1.0 / 6.0;                     /* 1/3!  */
+  p = p * r + 0.5;                           /* 1/2!  */
+  p = p * r + 1.0;                           /* 1/1!  */
+  p = p * r + 1.0;                           /* 1/0!  */
+  return p;
+}
+
+/* sum_{n=1}^{16} r^n / n! — the series of e^r - 1 without its constant. */
+LPG_HD double lpg_expm1_series(double r) {
+  double p = 1.0 / 20922789888000.0;         /* 1/16! */
+  p = p * r + 1.0 / 1307674368000.0;         /* 1/15! */
+  p = p * r + 1.0 / 87178291200.0;
+  p = p * r + 1.0 / 6227020800.0;
+  p = p * r + 1.0 / 479001600.0;
+  p = p * r + 1.0 / 39916800.0;
+  p = p * r + 1.0 / 3628800.0;
+  p = p * r + 1.0 / 362880.0;
+  p = p * r + 1.0 / 40320.0;
+  p = p * r + 1.0 / 5040.0;
+  p = p * r + 1.0 / 720.0;
+  p = p * r + 1.0 / 120.0;
+  p = p * r + 1.0 / 24.0;
+  p = p * r + 1.0 / 6.0;
+  p = p * r + 0.5;
+  p = p * r + 1.0;
+  return p * r;
+}
+
+LPG_HD double lpg_exp(double x) {
+  if (x != x) return x;
+  if (x > 709.782712893384) return lpg_bitsd(0x7ff0000000000000ULL);
+  if (x < -745.2) return 0.0;
+  double kd = floor(x * LPG_INV_LN2 + 0.5);
+  double r = (x - kd * LPG_LN2_HI) - kd * LPG_LN2_LO;
+  return lpg_scale2(lpg_exp_series(r), (int)kd);
+}
+
+LPG_HD double lpg_expm1(double x) {
+  if (x != x) return x;
+  if (x > -0.3465 && x < 0.3465) return lpg_expm1_series(x);
+  if (x < -40.0) return -1.0;
+  return lpg_exp(x) - 1.0;
+}
+
+LPG_HD double lpg_log(double x) {
+  if (x != x) return x;
+  if (x <= 0.0) return x == 0.0 ? -lpg_bitsd(0x7ff0000000000000ULL) : lpg_bitsd(0x7ff8000000000000ULL);
+  if (x == lpg_bitsd(0x7ff0000000000000ULL)) return x;
+  int eadj = 0;
+  if (x < 0x1.0p-1022) { x = x * 0x1.0p54; eadj = -54; }
+  uint64_t b = lpg_dbits(x);
+  int e = (int)((b >> 52) & 0x7ff) - 1023 + eadj;
+  double m = lpg_bitsd((b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL); /* [1,2) */
+  if (m > LPG_SQRT2) { m = m * 0.5; e += 1; }
+  double s = (m - 1.0) / (m + 1.0);
+  double s2 = s * s;
+  double q = 1.0 / 25.0;
+  q = q * s2 + 1.0 / 23.0;
+  q = q * s2 + 1.0 / 21.0;
+  q = q * s2 + 1.0 / 19.0;
+  q = q * s2 + 1.0 / 17.0;
+  q = q * s2 + 1.0 / 15.0;
+  q = q * s2 + 1.0 / 13.0;
+  q = q * s2 + 1.0 / 11.0;
+  q = q * s2 + 1.0 / 9.0;
+  q = q * s2 + 1.0 / 7.0;
+  q = q * s2 + 1.0 / 5.0;
+  q = q * s2 + 1.0 / 3.0;
+  q = q * s2 + 1.0;
+  double lm = 2.0 * s * q;
+  double ed = (double)e;
+  return ed * LPG_LN2_HI + (ed * LPG_LN2_LO + lm);
+}
+
+/* log(k!) for integer k >= 0. */
+LPG_HD double lpg_lfact(int64_t k) {
+  if (k < 2) return 0.0;
+  if (k < 20) {
+    double f = 1.0;
+    for (int64_t i = 2; i <= k; ++i) f = f * (double)i; /* exact below 2^53 */
+    return lpg_log(f);
+  }
+  double x = (double)(k + 1);
+  double ix = 1.0 / x;
+  double ix2 = ix * ix;
+  double corr = ix * (1.0 / 12.0 - ix2 * (1.0 / 360.0 - ix2 * (1.0 / 1260.0 - ix2 * (1.0 / 1680.0))));
+  return (x - 0.5) * lpg_log(x) - x + LPG_HALF_LOG_2PI + corr;
+}
+
+#endif /* LPG_DETMATH_H */

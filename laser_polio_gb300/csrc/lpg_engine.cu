@@ -1,0 +1,1023 @@
+/*
+ * lpg_engine.cu — host side of the C ABI in include/lpg.h.
+ *
+ * Owns the device state of a handle (one or more simulations on one GPU),
+ * lays the reference-ordered agent columns out node-major on the device,
+ * and launches the per-tick kernel sequence of lpg_kernels.cuh, captured
+ * once in a CUDA graph and replayed per tick.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lpg.h"
+#include "lpg_kernels.cuh"
+
+namespace {
+
+const char* kKernelNames[] = {"k_begin", "k_newborns", "k_sweep_a", "k_seed", "k_sweep_b", "k_node_tx", "k_select", "k_end"};
+constexpr int kNumTickKernels = 8;
+constexpr int kTicksPerGraph = 8;
+
+/* Reference-ordered columns of one simulation on the device. */
+struct Staging {
+  int8_t *ds = nullptr, *strain = nullptr, *et = nullptr, *it = nullptr, *pt = nullptr, *pp = nullptr, *par = nullptr,
+         *ipv = nullptr;
+  uint8_t* cm = nullptr;
+  int16_t *node = nullptr, *ri = nullptr;
+  float *risk = nullptr, *inf = nullptr;
+  int32_t *dob = nullptr, *dod = nullptr;
+  bool bound = false;
+};
+
+struct SimHost {
+  lpg_sim_desc d;
+  std::vector<double> birth_rate, p_ri, p_ipv, strain_scal, net, rowsum, r0s, seas;
+  std::vector<float> p_sia;
+  std::vector<int64_t> km;
+  std::vector<lpg_seed_event> seeds;
+  std::vector<lpg_sia_event> sia;
+  std::vector<std::vector<uint8_t>> sia_masks;
+  std::vector<int32_t> pop0, Rpre;
+  Staging stg;
+  int64_t res_elems = 0;
+};
+
+}  // namespace
+
+struct lpg_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<SimHost> sims;
+  std::vector<DevRep> hreps;
+  DevWorld W{};
+  std::vector<void*> allocs;
+  bool started = false;
+  std::string err;
+  bool use_graphs = true;
+  cudaGraphExec_t graph = nullptr;
+  bool graph_failed = false;
+  bool profiling = false;
+  double prof_ms[kNumTickKernels] = {0};
+  int64_t prof_n[kNumTickKernels] = {0};
+  std::vector<cudaEvent_t> ev_pool;
+  int64_t launches = 0;
+  int sm_count = 0;
+  int sweep_blocks = 0;
+  int select_blocks = 0;
+};
+
+static int fail(lpg_handle* h, int code, const char* fmt, ...) {
+  if (h) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    h->err = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                                       \
+  do {                                                                                                 \
+    cudaError_t e_ = (call);                                                                           \
+    if (e_ != cudaSuccess) return fail(h, LPG_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                       __FILE__, __LINE__);                                            \
+  } while (0)
+
+template <typename T>
+static int dalloc(lpg_handle* h, T** p, size_t n) {
+  size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess) return fail(h, LPG_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+  h->allocs.push_back((void*)*p);
+  return 0;
+}
+
+template <typename T>
+static int dupload(lpg_handle* h, T** p, const std::vector<T>& v) {
+  int rc = dalloc(h, p, v.size());
+  if (rc) return rc;
+  if (!v.empty()) CK(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+  return 0;
+}
+
+static void dfree_one(lpg_handle* h, void* p) {
+  if (!p) return;
+  cudaFree(p);
+  auto it = std::find(h->allocs.begin(), h->allocs.end(), p);
+  if (it != h->allocs.end()) h->allocs.erase(it);
+}
+
+__global__ void k_fill_f32(float* p, int64_t n, float v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+/* Node histogram of slots [0, count), node-id range check and sortedness. */
+__global__ void k_hist(const int16_t* node, int64_t count, int n_nodes, unsigned long long* cnt, int* flags) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+    int v = node[i];
+    if (v < 0 || v >= n_nodes) {
+      atomicOr(&flags[0], 1);
+      continue;
+    }
+    atomicAdd(&cnt[v], 1ULL);
+    if (i + 1 < count && node[i + 1] < v) atomicOr(&flags[1], 1);
+  }
+}
+
+struct ScatterArgs {
+  Staging s;
+  int64_t count;
+  const int32_t* node_chunk0; /* first chunk id of each local node */
+  const int64_t* node_first;  /* first slot of each node (sorted input) */
+  const int32_t* rank;        /* rank within node (unsorted input), or null */
+};
+
+__global__ void k_scatter(DevWorld W, ScatterArgs a) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += (int64_t)gridDim.x * blockDim.x) {
+    int n = a.s.node[i];
+    int64_t rk = a.rank ? (int64_t)a.rank[i] : i - a.node_first[n];
+    int64_t pos = (int64_t)(a.node_chunk0[n] + rk / LPG_CHUNK) * LPG_CHUNK + rk % LPG_CHUNK;
+    W.ds[pos] = a.s.ds[i];
+    W.strain[pos] = a.s.strain[i];
+    W.et[pos] = a.s.et[i];
+    W.it[pos] = a.s.it[i];
+    W.pt[pos] = a.s.pt[i];
+    W.pp[pos] = a.s.pp[i];
+    W.par[pos] = a.s.par[i];
+    W.ipv[pos] = a.s.ipv[i];
+    W.cm[pos] = a.s.cm[i];
+    W.ri[pos] = a.s.ri[i];
+    W.risk[pos] = a.s.risk[i];
+    W.inf[pos] = a.s.inf[i];
+    W.dob[pos] = a.s.dob[i];
+    W.dod[pos] = a.s.dod[i];
+    W.ref[pos] = (uint32_t)i;
+  }
+}
+
+/* Positions of one simulation back to reference order. */
+__global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used, int32_t node_base) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (int64_t)used * LPG_CHUNK;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    int64_t cid = chunk_base + q / LPG_CHUNK;
+    int o = (int)(q % LPG_CHUNK);
+    if (o >= W.chunk_fill[cid]) continue;
+    int64_t pos = cid * LPG_CHUNK + o;
+    uint32_t i = W.ref[pos];
+    s.ds[i] = W.ds[pos];
+    s.strain[i] = W.strain[pos];
+    s.et[i] = W.et[pos];
+    s.it[i] = W.it[pos];
+    s.pt[i] = W.pt[pos];
+    s.pp[i] = W.pp[pos];
+    s.par[i] = W.par[pos];
+    s.ipv[i] = W.ipv[pos];
+    s.cm[i] = W.cm[pos];
+    s.node[i] = (int16_t)(W.chunk_node[cid] - node_base);
+    s.ri[i] = W.ri[pos];
+    s.risk[i] = W.risk[pos];
+    s.inf[i] = W.inf[pos];
+    s.dob[i] = W.dob[pos];
+    s.dod[i] = W.dod[pos];
+  }
+}
+
+__global__ void k_cmp_counts(DevWorld W, const int32_t* tot, const uint64_t* sw, const uint64_t* bb,
+                             const uint64_t* cw, const uint64_t* subw, int* bad) {
+  int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid < W.G) {
+    for (int k = 0; k < TT_N; ++k)
+      if (tot[(int64_t)k * W.G + gid] != W.tot[(int64_t)k * W.G + gid]) atomicOr(bad, 1);
+    if (sw[gid] != W.sw[gid]) atomicOr(bad, 2);
+    for (int k = 0; k < LPG_MAX_STRAINS; ++k)
+      if (bb[(int64_t)k * W.G + gid] != W.bb[(int64_t)k * W.G + gid]) atomicOr(bad, 4);
+  }
+  for (int r = 0; r < W.n_reps; ++r) {
+    const DevRep* rp = &W.reps[r];
+    for (int64_t q = gid; q < rp->used_chunks; q += (int64_t)gridDim.x * blockDim.x) {
+      int64_t cid = rp->chunk_base + q;
+      if (cw[cid] != W.chunk_w[cid]) atomicOr(bad, 8);
+      for (int s = 0; s < LPG_NSUB; ++s)
+        if (subw[cid * LPG_NSUB + s] != W.sub_w[cid * LPG_NSUB + s]) atomicOr(bad, 16);
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+extern "C" int lpg_version(void) { return LPG_ABI_VERSION; }
+
+extern "C" const char* lpg_last_error(const lpg_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+extern "C" void* lpg_cuda_stream(lpg_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+extern "C" int64_t lpg_kernel_launches(lpg_handle* h) { return h ? h->launches : 0; }
+
+static const int res_wide[RS_N] = {0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 1, 0, 0, 0, 1};
+
+extern "C" int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t device, lpg_handle** out) {
+  if (!out) return LPG_ERR_ARG;
+  *out = nullptr;
+  if (!sims || n_sims < 1 || n_sims > 1024) return LPG_ERR_ARG;
+  lpg_handle* h = new lpg_handle();
+  *out = h;
+  h->device = device;
+  for (int r = 0; r < n_sims; ++r) {
+    const lpg_sim_desc& d = sims[r];
+    if (d.n_nodes < 1 || d.n_nodes > 32767) return fail(h, LPG_ERR_ARG, "sim %d: n_nodes %d out of range", r, d.n_nodes);
+    if (d.n_strains < 1 || d.n_strains > LPG_MAX_STRAINS)
+      return fail(h, LPG_ERR_ARG, "sim %d: n_strains %d out of range [1, %d]", r, d.n_strains, LPG_MAX_STRAINS);
+    if (d.nt < 1) return fail(h, LPG_ERR_ARG, "sim %d: nt must be >= 1", r);
+    if (d.count < 0 || d.capacity < d.count || d.capacity >= (int64_t)0xFFFFFFF0LL)
+      return fail(h, LPG_ERR_ARG, "sim %d: count %lld / capacity %lld invalid", r, (long long)d.count, (long long)d.capacity);
+    if (d.vd_step < 1 || d.ri_step < 1) return fail(h, LPG_ERR_ARG, "sim %d: step sizes must be >= 1", r);
+    if (!d.pop0) return fail(h, LPG_ERR_ARG, "sim %d: pop0 is required", r);
+    if ((d.components & LPG_COMP_TX) && (!d.network || !d.seasonality || !d.strain_r0_scalars || !d.r0_scalars))
+      return fail(h, LPG_ERR_ARG, "sim %d: transmission needs network, seasonality and scalars", r);
+    if (d.km_len < 1 || !d.km_cumdeaths) return fail(h, LPG_ERR_ARG, "sim %d: km table required", r);
+    SimHost s;
+    s.d = d;
+    const size_t n = (size_t)d.n_nodes;
+    auto vec = [&](const double* p, size_t k, double dflt) {
+      std::vector<double> v(k, dflt);
+      if (p) std::copy(p, p + k, v.begin());
+      return v;
+    };
+    s.birth_rate = vec(d.birth_rate, n, 0.0);
+    s.p_ri = vec(d.vx_prob_ri, n, 0.0);
+    s.p_ipv = vec(d.vx_prob_ipv, n, 0.0);
+    s.strain_scal = vec(d.strain_r0_scalars, (size_t)d.n_strains, 1.0);
+    s.net = vec(d.network, n * n, 0.0);
+    s.r0s = vec(d.r0_scalars, n, 1.0);
+    s.seas = vec(d.seasonality, (size_t)d.nt, 1.0);
+    s.rowsum.assign(n, 0.0);
+    for (size_t i = 0; i < n; ++i) {
+      double acc = 0.0;
+      for (size_t j = 0; j < n; ++j) acc = acc + s.net[i * n + j];
+      s.rowsum[i] = acc;
+    }
+    s.p_sia.assign(n, 0.0f);
+    if (d.vx_prob_sia) std::copy(d.vx_prob_sia, d.vx_prob_sia + n, s.p_sia.begin());
+    s.km.assign(d.km_cumdeaths, d.km_cumdeaths + d.km_len);
+    for (int k = 0; k < d.n_seeds; ++k) {
+      lpg_seed_event e = d.seeds[k];
+      if (e.node < 0 || e.node >= d.n_nodes) return fail(h, LPG_ERR_NODE, "sim %d: seed event node %d out of range", r, e.node);
+      s.seeds.push_back(e);
+    }
+    std::vector<int32_t> per_tick(d.nt, 0);
+    for (int k = 0; k < d.n_sia; ++k) {
+      lpg_sia_event e = d.sia[k];
+      if (e.tick < 0 || e.tick >= d.nt) continue;
+      if (e.strain < 0 || e.strain >= d.n_strains) return fail(h, LPG_ERR_ARG, "sim %d: SIA strain out of range", r);
+      if (++per_tick[e.tick] > LPG_MAX_SIA_PER_DAY)
+        return fail(h, LPG_ERR_ARG, "sim %d: more than %d SIA events on tick %d", r, LPG_MAX_SIA_PER_DAY, e.tick);
+      s.sia.push_back(e);
+      s.sia_masks.emplace_back(e.node_mask, e.node_mask + n);
+    }
+    if (d.ri_strain < 0 || d.ri_strain >= d.n_strains) return fail(h, LPG_ERR_ARG, "sim %d: RI strain out of range", r);
+    s.pop0.assign(d.pop0, d.pop0 + n);
+    if (d.R_preseed) s.Rpre.assign(d.R_preseed, d.R_preseed + (size_t)d.nt * n);
+    h->sims.push_back(std::move(s));
+  }
+  CK(cudaSetDevice(device));
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  CK(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device));
+  return LPG_OK;
+}
+
+static int alloc_staging(lpg_handle* h, Staging& s, int64_t cap) {
+  int rc = 0;
+  rc |= dalloc(h, &s.ds, cap);
+  rc |= dalloc(h, &s.strain, cap);
+  rc |= dalloc(h, &s.et, cap);
+  rc |= dalloc(h, &s.it, cap);
+  rc |= dalloc(h, &s.pt, cap);
+  rc |= dalloc(h, &s.pp, cap);
+  rc |= dalloc(h, &s.par, cap);
+  rc |= dalloc(h, &s.ipv, cap);
+  rc |= dalloc(h, &s.cm, cap);
+  rc |= dalloc(h, &s.node, cap);
+  rc |= dalloc(h, &s.ri, cap);
+  rc |= dalloc(h, &s.risk, cap);
+  rc |= dalloc(h, &s.inf, cap);
+  rc |= dalloc(h, &s.dob, cap);
+  rc |= dalloc(h, &s.dod, cap);
+  return rc ? LPG_ERR_NOMEM : 0;
+}
+
+static void free_staging(lpg_handle* h, Staging& s) {
+  void* ps[] = {s.ds, s.strain, s.et, s.it, s.pt, s.pp, s.par, s.ipv, s.cm, s.node, s.ri, s.risk, s.inf, s.dob, s.dod};
+  for (void* p : ps) dfree_one(h, p);
+  s = Staging();
+}
+
+extern "C" int lpg_bind_columns(lpg_handle* h, int32_t sim, const lpg_columns* c) {
+  if (!h || !c || sim < 0 || sim >= (int)h->sims.size()) return LPG_ERR_ARG;
+  if (h->started) return fail(h, LPG_ERR_STATE, "columns must be bound before lpg_start");
+  SimHost& s = h->sims[sim];
+  const int64_t cap = s.d.capacity;
+  CK(cudaSetDevice(h->device));
+  if (!s.stg.bound) {
+    int rc = alloc_staging(h, s.stg, cap);
+    if (rc) return rc;
+  }
+  Staging& g = s.stg;
+  cudaStream_t st = h->stream;
+#define COPY_OR(dst, src, esz, memv)                                                   \
+  if (src) {                                                                           \
+    CK(cudaMemcpyAsync(dst, src, (size_t)cap * (esz), cudaMemcpyDefault, st));          \
+  } else {                                                                             \
+    CK(cudaMemsetAsync(dst, memv, (size_t)cap * (esz), st));                            \
+  }
+  COPY_OR(g.ds, c->disease_state, 1, 0xff);
+  COPY_OR(g.strain, c->strain, 1, 0);
+  COPY_OR(g.et, c->exposure_timer, 1, 0);
+  COPY_OR(g.it, c->infection_timer, 1, 0);
+  COPY_OR(g.pt, c->paralysis_timer, 1, 0);
+  COPY_OR(g.pp, c->potentially_paralyzed, 1, 0xff);
+  COPY_OR(g.par, c->paralyzed, 1, 0);
+  COPY_OR(g.ipv, c->ipv_protected, 1, 0);
+  COPY_OR(g.cm, c->chronically_missed, 1, 0);
+  COPY_OR(g.node, c->node_id, 2, 0xff);
+  COPY_OR(g.ri, c->ri_timer, 2, 0xff);
+  COPY_OR(g.dob, c->date_of_birth, 4, 0xff);
+  COPY_OR(g.dod, c->date_of_death, 4, 0);
+#undef COPY_OR
+  if (c->acq_risk_multiplier) {
+    CK(cudaMemcpyAsync(g.risk, c->acq_risk_multiplier, (size_t)cap * 4, cudaMemcpyDefault, st));
+  } else {
+    k_fill_f32<<<256, 256, 0, st>>>(g.risk, cap, 1.0f);
+  }
+  if (c->daily_infectivity) {
+    CK(cudaMemcpyAsync(g.inf, c->daily_infectivity, (size_t)cap * 4, cudaMemcpyDefault, st));
+  } else {
+    k_fill_f32<<<256, 256, 0, st>>>(g.inf, cap, 1.0f);
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  g.bound = true;
+  return LPG_OK;
+}
+
+static int launch_tick(lpg_handle* h, bool capture);
+
+extern "C" int lpg_start(lpg_handle* h) {
+  if (!h) return LPG_ERR_ARG;
+  if (h->started) return LPG_OK;
+  CK(cudaSetDevice(h->device));
+  cudaStream_t st = h->stream;
+  const int R = (int)h->sims.size();
+  for (int r = 0; r < R; ++r)
+    if (!h->sims[r].stg.bound) return fail(h, LPG_ERR_STATE, "sim %d has no bound columns", r);
+
+  /* 1. node counts, id range and sortedness per simulation */
+  std::vector<std::vector<int64_t>> counts(R);
+  std::vector<int> sorted(R, 1);
+  unsigned long long* dcnt = nullptr;
+  int* dflags = nullptr;
+  int maxn = 0;
+  for (auto& s : h->sims) maxn = std::max(maxn, s.d.n_nodes);
+  if (dalloc(h, &dcnt, maxn) || dalloc(h, &dflags, 2)) return LPG_ERR_NOMEM;
+  for (int r = 0; r < R; ++r) {
+    SimHost& s = h->sims[r];
+    CK(cudaMemsetAsync(dcnt, 0, sizeof(unsigned long long) * maxn, st));
+    CK(cudaMemsetAsync(dflags, 0, sizeof(int) * 2, st));
+    if (s.d.count > 0) k_hist<<<1024, 256, 0, st>>>(s.stg.node, s.d.count, s.d.n_nodes, dcnt, dflags);
+    CK(cudaGetLastError());
+    std::vector<unsigned long long> hc(s.d.n_nodes);
+    int hf[2];
+    CK(cudaMemcpyAsync(hc.data(), dcnt, sizeof(unsigned long long) * s.d.n_nodes, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hf, dflags, sizeof hf, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (hf[0]) return fail(h, LPG_ERR_NODE, "sim %d: node_id outside [0, %d) among the first %lld slots", r, s.d.n_nodes,
+                           (long long)s.d.count);
+    sorted[r] = !hf[1];
+    counts[r].assign(hc.begin(), hc.end());
+  }
+  dfree_one(h, dcnt);
+  dfree_one(h, dflags);
+
+  /* 2. chunk layout */
+  std::vector<DevRep>& hr = h->hreps;
+  hr.assign(R, DevRep{});
+  int32_t chunk_total = 0, G = 0, csr_total = 0;
+  std::vector<std::vector<int32_t>> node_chunk0(R), csr_start(R), chunk_fill_init(R);
+  for (int r = 0; r < R; ++r) {
+    SimHost& s = h->sims[r];
+    const int n = s.d.n_nodes;
+    DevRep& d = hr[r];
+    d.node_base = G;
+    d.chunk_base = chunk_total;
+    d.csr_base = csr_total;
+    node_chunk0[r].resize(n);
+    csr_start[r].resize(n + 1);
+    int32_t used = 0;
+    for (int i = 0; i < n; ++i) {
+      int64_t cnt = counts[r][i];
+      int32_t k = (int32_t)std::max<int64_t>(1, (cnt + LPG_CHUNK - 1) / LPG_CHUNK);
+      node_chunk0[r][i] = d.chunk_base + used;
+      csr_start[r][i] = used;
+      for (int32_t q = 0; q < k; ++q) {
+        int64_t f = cnt - (int64_t)q * LPG_CHUNK;
+        chunk_fill_init[r].push_back((int32_t)std::max<int64_t>(0, std::min<int64_t>(f, LPG_CHUNK)));
+      }
+      used += k;
+    }
+    csr_start[r][n] = used;
+    int64_t reserve = (s.d.capacity - s.d.count + LPG_CHUNK - 1) / LPG_CHUNK + n;
+    d.used_chunks = used;
+    d.chunk_cap = (int32_t)(used + reserve);
+    chunk_total += d.chunk_cap;
+    G += n;
+    csr_total += n + 1;
+  }
+  if ((int64_t)chunk_total * LPG_CHUNK >= (int64_t)0xFFFFFFF0LL)
+    return fail(h, LPG_ERR_ARG, "device layout needs more than 2^32 positions");
+
+  /* 3. allocations */
+  DevWorld& W = h->W;
+  W.n_reps = R;
+  W.G = G;
+  W.total_chunks = chunk_total;
+  const int64_t P = (int64_t)chunk_total * LPG_CHUNK;
+  int rc = 0;
+  rc |= dalloc(h, &W.ds, P);
+  rc |= dalloc(h, &W.strain, P);
+  rc |= dalloc(h, &W.et, P);
+  rc |= dalloc(h, &W.it, P);
+  rc |= dalloc(h, &W.pt, P);
+  rc |= dalloc(h, &W.pp, P);
+  rc |= dalloc(h, &W.par, P);
+  rc |= dalloc(h, &W.ipv, P);
+  rc |= dalloc(h, &W.cm, P);
+  rc |= dalloc(h, &W.ri, P);
+  rc |= dalloc(h, &W.risk, P);
+  rc |= dalloc(h, &W.inf, P);
+  rc |= dalloc(h, &W.dob, P);
+  rc |= dalloc(h, &W.dod, P);
+  rc |= dalloc(h, &W.ref, P);
+  rc |= dalloc(h, &W.chunk_node, chunk_total);
+  rc |= dalloc(h, &W.chunk_fill, chunk_total);
+  rc |= dalloc(h, &W.chunk_nbt, chunk_total);
+  rc |= dalloc(h, &W.chunk_nbo, chunk_total);
+  rc |= dalloc(h, &W.chunk_w, chunk_total);
+  rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
+  rc |= dalloc(h, &W.cpref, chunk_total);
+  rc |= dalloc(h, &W.node_chunks[0], chunk_total);
+  rc |= dalloc(h, &W.node_chunks[1], chunk_total);
+  rc |= dalloc(h, &W.node_chunk_start[0], csr_total);
+  rc |= dalloc(h, &W.node_chunk_start[1], csr_total);
+  rc |= dalloc(h, &W.node_rep, G);
+  rc |= dalloc(h, &W.node_count, G);
+  rc |= dalloc(h, &W.ev, (size_t)EV_N * G);
+  rc |= dalloc(h, &W.tot, (size_t)TT_N * G);
+  rc |= dalloc(h, &W.sw, G);
+  rc |= dalloc(h, &W.bb, (size_t)LPG_MAX_STRAINS * G);
+  rc |= dalloc(h, &W.nb_end, G);
+  rc |= dalloc(h, &W.nb_li0, G);
+  rc |= dalloc(h, &W.prob, (size_t)LPG_MAX_STRAINS * G);
+  rc |= dalloc(h, &W.size, G);
+  rc |= dalloc(h, &W.uniq, G);
+  rc |= dalloc(h, &W.ksel, G);
+  rc |= dalloc(h, &W.tgt_off, G + 1);
+  int64_t hits = 0;
+  for (auto& s : h->sims) hits += s.d.capacity;
+  W.hits_cap = hits;
+  rc |= dalloc(h, &W.hits, hits);
+  rc |= dalloc(h, &W.bar_count, 1);
+  rc |= dalloc(h, &W.bar_gen, 1);
+  rc |= dalloc(h, &W.abort_flag, 1);
+  rc |= dalloc(h, &W.reps, R);
+  if (rc) return LPG_ERR_NOMEM;
+  CK(cudaMemsetAsync(W.ds, 0xff, P, st));
+  CK(cudaMemsetAsync(W.ref, 0xff, P * 4, st));
+  CK(cudaMemsetAsync(W.chunk_node, 0xff, sizeof(int32_t) * chunk_total, st));
+  CK(cudaMemsetAsync(W.chunk_fill, 0, sizeof(int32_t) * chunk_total, st));
+  CK(cudaMemsetAsync(W.chunk_nbt, 0xff, sizeof(int32_t) * chunk_total, st));
+  CK(cudaMemsetAsync(W.chunk_nbo, 0, sizeof(int32_t) * chunk_total, st));
+  CK(cudaMemsetAsync(W.ev, 0, sizeof(int32_t) * EV_N * G, st));
+  CK(cudaMemsetAsync(W.tot, 0, sizeof(int32_t) * TT_N * G, st));
+  CK(cudaMemsetAsync(W.sw, 0, sizeof(uint64_t) * G, st));
+  CK(cudaMemsetAsync(W.bb, 0, sizeof(uint64_t) * LPG_MAX_STRAINS * G, st));
+  CK(cudaMemsetAsync(W.size, 0, sizeof(int64_t) * G, st));
+  CK(cudaMemsetAsync(W.uniq, 0, sizeof(int64_t) * G, st));
+  CK(cudaMemsetAsync(W.bar_count, 0, 4, st));
+  CK(cudaMemsetAsync(W.bar_gen, 0, 4, st));
+  CK(cudaMemsetAsync(W.abort_flag, 0, 4, st));
+
+  /* 4. per-simulation static data, results, pools, chunk tables */
+  std::vector<int32_t> h_node_rep(G), h_chunk_node(chunk_total, -1), h_chunk_fill(chunk_total, 0), h_csr(chunk_total, 0),
+      h_start(csr_total, 0);
+  std::vector<int64_t> h_node_count(G);
+  for (int r = 0; r < R; ++r) {
+    SimHost& s = h->sims[r];
+    const lpg_sim_desc& d = s.d;
+    DevRep& rp = hr[r];
+    const int n = d.n_nodes;
+    rp.n_nodes = n;
+    rp.ns = d.n_strains;
+    rp.nt = d.nt;
+    rp.comps = (int32_t)d.components;
+    rp.stop_if = d.stop_if_no_cases;
+    rp.vd_step = d.vd_step;
+    rp.ri_step = d.ri_step;
+    rp.ri_enabled = d.ri_enabled;
+    rp.ri_strain = d.ri_strain;
+    rp.km_len = d.km_len;
+    rp.km_max_year = d.km_max_year;
+    rp.nb_r = d.nb_r;
+    rp.count0 = d.count;
+    rp.capacity = d.capacity;
+    rp.seed = d.seed;
+    rp.p_par = d.p_paralysis;
+    rp.zi = d.zero_inflation;
+    rp.dur_kind = d.dur_inf.kind;
+    rp.dur_p1 = d.dur_inf.p1;
+    rp.dur_p2 = d.dur_inf.p2;
+    rp.t = 0;
+    rp.stopped = 0;
+    rp.stop_at = 0x7fffffff;
+    rp.error = 0;
+    rp.count = d.count;
+    rp.csr_cur = 0;
+    rp.started = 0;
+    double* dp;
+    float* fp;
+    int64_t* ip;
+    if (dupload(h, &dp, s.birth_rate)) return LPG_ERR_NOMEM;
+    rp.birth_rate = dp;
+    if (dupload(h, &dp, s.p_ri)) return LPG_ERR_NOMEM;
+    rp.p_ri = dp;
+    if (dupload(h, &dp, s.p_ipv)) return LPG_ERR_NOMEM;
+    rp.p_ipv = dp;
+    if (dupload(h, &dp, s.strain_scal)) return LPG_ERR_NOMEM;
+    rp.strain_scal = dp;
+    if (dupload(h, &dp, s.net)) return LPG_ERR_NOMEM;
+    rp.net = dp;
+    if (dupload(h, &dp, s.rowsum)) return LPG_ERR_NOMEM;
+    rp.rowsum = dp;
+    if (dupload(h, &dp, s.r0s)) return LPG_ERR_NOMEM;
+    rp.r0s = dp;
+    if (dupload(h, &dp, s.seas)) return LPG_ERR_NOMEM;
+    rp.seas = dp;
+    if (dupload(h, &fp, s.p_sia)) return LPG_ERR_NOMEM;
+    rp.p_sia = fp;
+    if (dupload(h, &ip, s.km)) return LPG_ERR_NOMEM;
+    rp.km = ip;
+    /* per-tick SIA and seed tables, events in schedule order */
+    std::vector<int32_t> sfirst(d.nt, 0), scnt(d.nt, 0), dfirst(d.nt, 0), dcnt_(d.nt, 0);
+    std::vector<uint8_t> future(d.nt, 0);
+    std::vector<DevSia> hsia;
+    std::vector<uint8_t*> masks;
+    for (int tt = 0; tt < d.nt; ++tt) {
+      sfirst[tt] = (int32_t)hsia.size();
+      for (size_t k = 0; k < s.sia.size(); ++k) {
+        if (s.sia[k].tick != tt) continue;
+        uint8_t* m;
+        if (dupload(h, &m, s.sia_masks[k])) return LPG_ERR_NOMEM;
+        DevSia e{s.sia[k].tick, s.sia[k].strain, s.sia[k].min_age, s.sia[k].max_age, s.sia[k].efficacy, m};
+        hsia.push_back(e);
+        scnt[tt] += 1;
+      }
+    }
+    std::vector<DevSeed> hseed;
+    for (int tt = 0; tt < d.nt; ++tt) {
+      dfirst[tt] = (int32_t)hseed.size();
+      for (size_t k = 0; k < s.seeds.size(); ++k) {
+        if (s.seeds[k].tick != tt) continue;
+        DevSeed e{s.seeds[k].tick, s.seeds[k].node, s.seeds[k].is_count, (int32_t)k, s.seeds[k].value};
+        hseed.push_back(e);
+        dcnt_[tt] += 1;
+      }
+    }
+    for (int tt = 0; tt < d.nt; ++tt)
+      for (auto& e : s.seeds)
+        if (e.tick > tt) future[tt] = 1;
+    int32_t* i32;
+    uint8_t* u8;
+    if (dupload(h, &i32, sfirst)) return LPG_ERR_NOMEM;
+    rp.sia_first = i32;
+    if (dupload(h, &i32, scnt)) return LPG_ERR_NOMEM;
+    rp.sia_cnt = i32;
+    if (dupload(h, &i32, dfirst)) return LPG_ERR_NOMEM;
+    rp.seed_first = i32;
+    if (dupload(h, &i32, dcnt_)) return LPG_ERR_NOMEM;
+    rp.seed_cnt = i32;
+    if (dupload(h, &u8, future)) return LPG_ERR_NOMEM;
+    rp.future_seed = u8;
+    DevSia* ds_;
+    DevSeed* dd_;
+    if (dupload(h, &ds_, hsia)) return LPG_ERR_NOMEM;
+    rp.sia = ds_;
+    if (dupload(h, &dd_, hseed)) return LPG_ERR_NOMEM;
+    rp.seeds = dd_;
+    /* results */
+    int64_t off = 0;
+    for (int k = 0; k < RS_N; ++k) {
+      rp.res_off[k] = off;
+      off += (int64_t)d.nt * n * (res_wide[k] ? d.n_strains : 1);
+    }
+    s.res_elems = off;
+    if (dalloc(h, &rp.res, off)) return LPG_ERR_NOMEM;
+    CK(cudaMemsetAsync(rp.res, 0, sizeof(int32_t) * off, st));
+    CK(cudaMemcpyAsync(rp.res + rp.res_off[RS_POP], s.pop0.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    if (!s.Rpre.empty())
+      CK(cudaMemcpyAsync(rp.res + rp.res_off[RS_R], s.Rpre.data(), sizeof(int32_t) * s.Rpre.size(), cudaMemcpyHostToDevice, st));
+    /* unborn pool: reference slots [count, capacity) */
+    const int64_t np = std::max<int64_t>(d.capacity - d.count, 1);
+    rc = 0;
+    rc |= dalloc(h, &rp.pl_et, np);
+    rc |= dalloc(h, &rp.pl_it, np);
+    rc |= dalloc(h, &rp.pl_pt, np);
+    rc |= dalloc(h, &rp.pl_strain, np);
+    rc |= dalloc(h, &rp.pl_pp, np);
+    rc |= dalloc(h, &rp.pl_par, np);
+    rc |= dalloc(h, &rp.pl_ipv, np);
+    rc |= dalloc(h, &rp.pl_cm, np);
+    rc |= dalloc(h, &rp.pl_ri, np);
+    rc |= dalloc(h, &rp.pl_risk, np);
+    rc |= dalloc(h, &rp.pl_inf, np);
+    if (rc) return LPG_ERR_NOMEM;
+    const int64_t pc = d.capacity - d.count;
+    if (pc > 0) {
+      Staging& g = s.stg;
+      const int64_t c0 = d.count;
+      CK(cudaMemcpyAsync(rp.pl_et, g.et + c0, pc, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_it, g.it + c0, pc, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_pt, g.pt + c0, pc, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_strain, g.strain + c0, pc, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_pp, g.pp + c0, pc, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_par, g.par + c0, pc, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_ipv, g.ipv + c0, pc, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_cm, g.cm + c0, pc, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_ri, g.ri + c0, pc * 2, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_risk, g.risk + c0, pc * 4, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(rp.pl_inf, g.inf + c0, pc * 4, cudaMemcpyDeviceToDevice, st));
+    }
+    /* chunk tables */
+    int32_t c = 0;
+    for (int i = 0; i < n; ++i) {
+      h_node_rep[rp.node_base + i] = r;
+      h_node_count[rp.node_base + i] = counts[r][i];
+      h_start[rp.csr_base + i] = csr_start[r][i];
+      for (int32_t k = csr_start[r][i]; k < csr_start[r][i + 1]; ++k, ++c) {
+        h_chunk_node[rp.chunk_base + c] = rp.node_base + i;
+        h_chunk_fill[rp.chunk_base + c] = chunk_fill_init[r][c];
+        h_csr[rp.chunk_base + k] = rp.chunk_base + c;
+      }
+    }
+    h_start[rp.csr_base + n] = csr_start[r][n];
+  }
+  CK(cudaMemcpyAsync(W.node_rep, h_node_rep.data(), sizeof(int32_t) * G, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(W.node_count, h_node_count.data(), sizeof(int64_t) * G, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(W.chunk_node, h_chunk_node.data(), sizeof(int32_t) * chunk_total, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(W.chunk_fill, h_chunk_fill.data(), sizeof(int32_t) * chunk_total, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(W.node_chunks[0], h_csr.data(), sizeof(int32_t) * chunk_total, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(W.node_chunk_start[0], h_start.data(), sizeof(int32_t) * csr_total, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(W.reps, hr.data(), sizeof(DevRep) * R, cudaMemcpyHostToDevice, st));
+
+  /* 5. scatter the reference-ordered columns into the node-major layout */
+  for (int r = 0; r < R; ++r) {
+    SimHost& s = h->sims[r];
+    const int n = s.d.n_nodes;
+    int32_t* d_nc0;
+    int64_t* d_first;
+    std::vector<int64_t> first(n, 0);
+    for (int i = 1; i < n; ++i) first[i] = first[i - 1] + counts[r][i - 1];
+    if (dupload(h, &d_nc0, node_chunk0[r])) return LPG_ERR_NOMEM;
+    if (dupload(h, &d_first, first)) return LPG_ERR_NOMEM;
+    int32_t* d_rank = nullptr;
+    if (!sorted[r] && s.d.count > 0) {
+      /* stable rank of each slot within its node, from the host copy */
+      std::vector<int16_t> nodes(s.d.count);
+      CK(cudaMemcpyAsync(nodes.data(), s.stg.node, sizeof(int16_t) * s.d.count, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      std::vector<int32_t> rank(s.d.count), next(n, 0);
+      for (int64_t i = 0; i < s.d.count; ++i) rank[i] = next[nodes[i]]++;
+      if (dupload(h, &d_rank, rank)) return LPG_ERR_NOMEM;
+      CK(cudaStreamSynchronize(st));
+    }
+    ScatterArgs a{s.stg, s.d.count, d_nc0, d_first, d_rank};
+    if (s.d.count > 0) k_scatter<<<2048, 256, 0, st>>>(W, a);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    dfree_one(h, d_nc0);
+    dfree_one(h, d_first);
+    dfree_one(h, d_rank);
+    free_staging(h, s.stg);
+  }
+
+  /* 6. running totals and selection weights from a full count, then tick 0 */
+  k_count<<<std::max(1, h->sm_count * 4), LPG_SWEEP_THREADS, 0, st>>>(W, W.tot, W.sw, W.bb, W.chunk_w, W.sub_w);
+  CK(cudaGetLastError());
+  for (int r = 0; r < R; ++r) {
+    hr[r].started = 1;
+    hr[r].cur_t = 0;
+    hr[r].active = 1;
+    hr[r].vd_tick = hr[r].ri_tick = hr[r].sia_n = hr[r].seed_n = 0;
+    hr[r].nb_total = 0;
+  }
+  CK(cudaMemcpyAsync(W.reps, hr.data(), sizeof(DevRep) * R, cudaMemcpyHostToDevice, st));
+  k_end<<<(G + 255) / 256, 256, 0, st>>>(W);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+
+  /* launch geometry */
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_THREADS, 0));
+  h->sweep_blocks = std::max(1, occ) * h->sm_count;
+  occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_select, 256, 0));
+  h->select_blocks = std::max(1, std::min(occ, 4)) * h->sm_count;
+  h->started = true;
+  return LPG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+static int launch_one(lpg_handle* h, int k, bool timed) {
+  cudaStream_t st = h->stream;
+  DevWorld& W = h->W;
+  const int R = W.n_reps, G = W.G;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (timed) {
+    e0 = h->ev_pool[2 * k];
+    e1 = h->ev_pool[2 * k + 1];
+    CK(cudaEventRecord(e0, st));
+  }
+  switch (k) {
+    case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
+    case 1: k_newborns<<<dim3(64, R), 256, 0, st>>>(W); break;
+    case 2: k_sweep<0><<<h->sweep_blocks, LPG_SWEEP_THREADS, 0, st>>>(W); break;
+    case 3: k_seed<<<R, 1024, 0, st>>>(W); break;
+    case 4: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_THREADS, 0, st>>>(W); break;
+    case 5: k_node_tx<<<(G + 127) / 128, 128, 0, st>>>(W); break;
+    case 6: {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(h->select_blocks);
+      cfg.blockDim = dim3(256);
+      cfg.dynamicSmemBytes = 0;
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeCooperative;
+      attr[0].val.cooperative = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      CK(cudaLaunchKernelEx(&cfg, k_select, W));
+      break;
+    }
+    case 7: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
+  }
+  CK(cudaGetLastError());
+  if (timed) CK(cudaEventRecord(e1, st));
+  return 0;
+}
+
+static int launch_tick(lpg_handle* h, bool capture) {
+  (void)capture;
+  for (int k = 0; k < kNumTickKernels; ++k) {
+    int rc = launch_one(h, k, false);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+static int build_graph(lpg_handle* h) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = 0;
+  for (int t = 0; t < kTicksPerGraph && !rc; ++t) rc = launch_tick(h, true);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (rc || e != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    h->graph_failed = true;
+    return 0;
+  }
+  e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    h->graph = nullptr;
+    h->graph_failed = true;
+  }
+  return 0;
+}
+
+extern "C" int lpg_step(lpg_handle* h, int32_t n_ticks) {
+  if (!h) return LPG_ERR_ARG;
+  if (!h->started) return fail(h, LPG_ERR_STATE, "lpg_step before lpg_start");
+  if (n_ticks <= 0) return LPG_OK;
+  CK(cudaSetDevice(h->device));
+  if (h->profiling) {
+    if (h->ev_pool.empty()) {
+      h->ev_pool.resize(2 * kNumTickKernels);
+      for (auto& e : h->ev_pool) CK(cudaEventCreate(&e));
+    }
+    for (int t = 0; t < n_ticks; ++t) {
+      for (int k = 0; k < kNumTickKernels; ++k) {
+        int rc = launch_one(h, k, true);
+        if (rc) return rc;
+      }
+      CK(cudaStreamSynchronize(h->stream));
+      for (int k = 0; k < kNumTickKernels; ++k) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, h->ev_pool[2 * k], h->ev_pool[2 * k + 1]));
+        h->prof_ms[k] += ms;
+        h->prof_n[k] += 1;
+      }
+      h->launches += kNumTickKernels;
+    }
+    return LPG_OK;
+  }
+  int left = n_ticks;
+  if (h->use_graphs && !h->graph_failed && n_ticks >= kTicksPerGraph) {
+    if (!h->graph) {
+      int rc = build_graph(h);
+      if (rc) return rc;
+    }
+    if (h->graph) {
+      while (left >= kTicksPerGraph) {
+        CK(cudaGraphLaunch(h->graph, h->stream));
+        h->launches += (int64_t)kTicksPerGraph * kNumTickKernels;
+        left -= kTicksPerGraph;
+      }
+    }
+  }
+  for (; left > 0; --left) {
+    int rc = launch_tick(h, false);
+    if (rc) return rc;
+    h->launches += kNumTickKernels;
+  }
+  return LPG_OK;
+}
+
+extern "C" int lpg_sync(lpg_handle* h) {
+  if (!h) return LPG_ERR_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  if (!h->started) return LPG_OK;
+  int32_t ab = 0;
+  CK(cudaMemcpy(&ab, h->W.abort_flag, 4, cudaMemcpyDeviceToHost));
+  if (ab) return fail(h, LPG_ERR_TIMEOUT, "a bounded grid barrier of the selection kernel timed out");
+  std::vector<DevRep> reps(h->W.n_reps);
+  CK(cudaMemcpy(reps.data(), h->W.reps, sizeof(DevRep) * reps.size(), cudaMemcpyDeviceToHost));
+  for (size_t r = 0; r < reps.size(); ++r) {
+    if (reps[r].error == LPG_ERR_CAPACITY)
+      return fail(h, LPG_ERR_CAPACITY, "sim %zu: births at tick %d exceed capacity %lld", r, reps[r].cur_t,
+                  (long long)reps[r].capacity);
+    if (reps[r].error) return fail(h, reps[r].error, "sim %zu: device error %d at tick %d", r, reps[r].error, reps[r].cur_t);
+  }
+  return LPG_OK;
+}
+
+extern "C" int lpg_get_state(lpg_handle* h, int32_t sim, lpg_sim_state* out) {
+  if (!h || !out || sim < 0 || sim >= (int)h->sims.size()) return LPG_ERR_ARG;
+  if (!h->started) {
+    out->t = 0;
+    out->stopped = 0;
+    out->count = h->sims[sim].d.count;
+    out->error = 0;
+    return LPG_OK;
+  }
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  DevRep r;
+  CK(cudaMemcpy(&r, h->W.reps + sim, sizeof(DevRep), cudaMemcpyDeviceToHost));
+  out->t = r.t;
+  out->stopped = r.stopped;
+  out->count = r.count;
+  out->error = r.error;
+  return LPG_OK;
+}
+
+extern "C" int lpg_read_results(lpg_handle* h, int32_t sim, const lpg_results_view* v) {
+  if (!h || !v || sim < 0 || sim >= (int)h->sims.size()) return LPG_ERR_ARG;
+  if (!h->started) return fail(h, LPG_ERR_STATE, "no results before lpg_start");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  DevRep r;
+  CK(cudaMemcpy(&r, h->W.reps + sim, sizeof(DevRep), cudaMemcpyDeviceToHost));
+  int32_t* const* outs = (int32_t* const*)v;
+  const lpg_sim_desc& d = h->sims[sim].d;
+  for (int k = 0; k < RS_N; ++k) {
+    if (!outs[k]) continue;
+    size_t n = (size_t)d.nt * d.n_nodes * (res_wide[k] ? d.n_strains : 1);
+    CK(cudaMemcpy(outs[k], r.res + r.res_off[k], n * sizeof(int32_t), cudaMemcpyDefault));
+  }
+  return LPG_OK;
+}
+
+extern "C" int lpg_read_columns(lpg_handle* h, int32_t sim, const lpg_columns* c) {
+  if (!h || !c || sim < 0 || sim >= (int)h->sims.size()) return LPG_ERR_ARG;
+  if (!h->started) return fail(h, LPG_ERR_STATE, "no columns before lpg_start");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  DevRep r;
+  CK(cudaMemcpy(&r, h->W.reps + sim, sizeof(DevRep), cudaMemcpyDeviceToHost));
+  Staging s;
+  int rc = alloc_staging(h, s, std::max<int64_t>(r.count, 1));
+  if (rc) return rc;
+  k_gather<<<2048, 256, 0, h->stream>>>(h->W, s, r.chunk_base, r.used_chunks, r.node_base);
+  CK(cudaGetLastError());
+  const size_t n = (size_t)r.count;
+#define OUT(dst, src, esz) \
+  if (dst) CK(cudaMemcpyAsync(dst, src, n * (esz), cudaMemcpyDefault, h->stream))
+  OUT(c->disease_state, s.ds, 1);
+  OUT(c->strain, s.strain, 1);
+  OUT(c->exposure_timer, s.et, 1);
+  OUT(c->infection_timer, s.it, 1);
+  OUT(c->paralysis_timer, s.pt, 1);
+  OUT(c->potentially_paralyzed, s.pp, 1);
+  OUT(c->paralyzed, s.par, 1);
+  OUT(c->ipv_protected, s.ipv, 1);
+  OUT(c->chronically_missed, s.cm, 1);
+  OUT(c->node_id, s.node, 2);
+  OUT(c->ri_timer, s.ri, 2);
+  OUT(c->acq_risk_multiplier, s.risk, 4);
+  OUT(c->daily_infectivity, s.inf, 4);
+  OUT(c->date_of_birth, s.dob, 4);
+  OUT(c->date_of_death, s.dod, 4);
+#undef OUT
+  CK(cudaStreamSynchronize(h->stream));
+  free_staging(h, s);
+  return LPG_OK;
+}
+
+/* Recount everything and compare with the running totals (diagnostic). */
+extern "C" int lpg_check_invariants(lpg_handle* h) {
+  if (!h || !h->started) return LPG_ERR_STATE;
+  CK(cudaSetDevice(h->device));
+  DevWorld& W = h->W;
+  const int G = W.G;
+  int32_t* tot;
+  uint64_t *sw, *bb, *cw, *subw;
+  int* bad;
+  if (dalloc(h, &tot, (size_t)TT_N * G) || dalloc(h, &sw, G) || dalloc(h, &bb, (size_t)LPG_MAX_STRAINS * G) ||
+      dalloc(h, &cw, W.total_chunks) || dalloc(h, &subw, (size_t)W.total_chunks * LPG_NSUB) || dalloc(h, &bad, 1))
+    return LPG_ERR_NOMEM;
+  cudaStream_t st = h->stream;
+  CK(cudaMemsetAsync(tot, 0, sizeof(int32_t) * TT_N * G, st));
+  CK(cudaMemsetAsync(sw, 0, sizeof(uint64_t) * G, st));
+  CK(cudaMemsetAsync(bb, 0, sizeof(uint64_t) * LPG_MAX_STRAINS * G, st));
+  CK(cudaMemsetAsync(cw, 0, sizeof(uint64_t) * W.total_chunks, st));
+  CK(cudaMemsetAsync(subw, 0, sizeof(uint64_t) * W.total_chunks * LPG_NSUB, st));
+  CK(cudaMemsetAsync(bad, 0, 4, st));
+  k_count<<<std::max(1, h->sm_count * 4), LPG_SWEEP_THREADS, 0, st>>>(W, tot, sw, bb, cw, subw);
+  k_cmp_counts<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, tot, sw, bb, cw, subw, bad);
+  CK(cudaGetLastError());
+  int hb = 0;
+  CK(cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  void* ps[] = {tot, sw, bb, cw, subw, bad};
+  for (void* p : ps) dfree_one(h, p);
+  if (hb) return fail(h, LPG_ERR_INTERNAL, "running totals differ from a recount (mask 0x%x)", hb);
+  return LPG_OK;
+}
+
+extern "C" int lpg_set_graphs(lpg_handle* h, int32_t enable) {
+  if (!h) return LPG_ERR_ARG;
+  h->use_graphs = enable != 0;
+  return LPG_OK;
+}
+
+extern "C" int lpg_set_profiling(lpg_handle* h, int32_t enable) {
+  if (!h) return LPG_ERR_ARG;
+  h->profiling = enable != 0;
+  if (h->profiling) {
+    for (int k = 0; k < kNumTickKernels; ++k) {
+      h->prof_ms[k] = 0;
+      h->prof_n[k] = 0;
+    }
+  }
+  return LPG_OK;
+}
+
+extern "C" int lpg_read_profile(lpg_handle* h, lpg_profile* out) {
+  if (!h || !out) return LPG_ERR_ARG;
+  out->n_kernels = kNumTickKernels;
+  for (int k = 0; k < kNumTickKernels; ++k) {
+    out->names[k] = kKernelNames[k];
+    out->total_ms[k] = h->prof_ms[k];
+    out->launches[k] = h->prof_n[k];
+  }
+  return LPG_OK;
+}
+
+extern "C" void lpg_destroy(lpg_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (auto e : h->ev_pool) cudaEventDestroy(e);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}

@@ -1,0 +1,188 @@
+/*
+ * lpg_engine.cuh — device data layout of the GB300 per-tick agent step.
+ *
+ * Layout.  The reference keeps agents in one append-only table in slot
+ * order (LaserFrame, laser_polio/model.py:139); within a node, agents appear
+ * in slot order, but nodes interleave once births append new runs
+ * (model.py:1730).  On the device the table is re-laid node-major: every
+ * node owns an ordered list of CHUNK-slot chunks, and a chunk holds agents of
+ * exactly one node, in the reference's slot order.  Births go to the tail of
+ * their node's list.  So
+ *   - the fused sweep processes whole chunks whose node is known up front
+ *     (no per-agent node id read, no segmented reductions: one set of node
+ *     counters per chunk);
+ *   - a node's susceptible CDF in slot order (model.py:1108) is the
+ *     concatenation of its chunks, indexed by per-chunk and per-SUB-slot
+ *     susceptible weight totals kept exact in integers;
+ *   - every column access is an aligned, coalesced vector access.
+ * ref_slot[pos] maps each position back to the reference slot, which keys
+ * all per-agent random draws and the copy back to the host.
+ *
+ * Aggregates.  Node totals the reference recounts every tick (count_SEIRP,
+ * model.py:869-929; tx_step_prep, :932-1007) are kept as running integer
+ * totals, updated by every transition that changes them (exact, so they
+ * equal a recount bit for bit).  Susceptible acquisition risk is summed in
+ * units of 2^-24, infectivity x strain scalar in units of 2^-32.
+ */
+#ifndef LPG_ENGINE_CUH
+#define LPG_ENGINE_CUH
+
+#include <stdint.h>
+
+#include "lpg.h"
+#include "lpg_rng.h"
+
+#define LPG_CHUNK 2048
+#define LPG_SUB 128
+#define LPG_NSUB (LPG_CHUNK / LPG_SUB)
+#define LPG_SWEEP_THREADS 256
+#define LPG_SPT (LPG_CHUNK / LPG_SWEEP_THREADS) /* slots per thread = 8 */
+
+/* per-tick event counters per node */
+enum {
+  EV_DEATHS = 0,
+  EV_BIRTHS = 1,
+  EV_NEWPOT = 2,
+  EV_NEWPAR = 3,
+  EV_RIVAC = 4,
+  EV_RIPROT = 5,
+  EV_IPVVAC = 6,
+  EV_SIAVAC0 = 7,
+  EV_SIAPROT0 = EV_SIAVAC0 + LPG_MAX_SIA_PER_DAY,
+  EV_TXNEW0 = EV_SIAPROT0 + LPG_MAX_SIA_PER_DAY,
+  EV_N = EV_TXNEW0 + LPG_MAX_STRAINS
+};
+
+/* running totals per node */
+enum {
+  TT_S = 0,
+  TT_R = 1,
+  TT_POTP = 2,
+  TT_P = 3,
+  TT_E0 = 4,
+  TT_I0 = TT_E0 + LPG_MAX_STRAINS,
+  TT_N = TT_I0 + LPG_MAX_STRAINS
+};
+
+/* results fields, in the order of lpg_results_view */
+enum {
+  RS_S, RS_E, RS_I, RS_R, RS_EBS, RS_IBS, RS_POTP, RS_P, RS_NEWPOTP, RS_NEWP, RS_POP, RS_BIRTHS, RS_DEATHS,
+  RS_NEWEXP, RS_NEWEXPBS, RS_RIVAC, RS_RIPROT, RS_RINEWEXPBS, RS_IPVVAC, RS_SIAVAC, RS_SIAPROT, RS_SIANEWEXPBS,
+  RS_N
+};
+
+typedef struct {
+  int32_t tick, strain, min_age, max_age;
+  double efficacy;
+  const uint8_t* mask; /* device, [n_nodes] */
+} DevSia;
+
+typedef struct {
+  int32_t tick, node, is_count, pad;
+  double value;
+} DevSeed;
+
+/* Per-simulation device record. */
+typedef struct {
+  /* static */
+  int32_t n_nodes, ns, nt, comps;
+  int32_t stop_if, vd_step, ri_step, ri_enabled;
+  int32_t ri_strain, km_len, km_max_year, nb_r;
+  int32_t node_base;  /* first global node id */
+  int32_t chunk_base; /* first chunk id */
+  int32_t chunk_cap;  /* chunks reserved */
+  int32_t csr_base;   /* offset of this sim's node_chunk_start entries (n_nodes + 1) */
+  int64_t count0, capacity;
+  uint64_t seed;
+  float p_par;
+  int32_t pad0;
+  double zi;
+  int32_t dur_kind;
+  int32_t pad1;
+  double dur_p1, dur_p2;
+  const double* birth_rate;
+  const double* p_ri;
+  const double* p_ipv;
+  const double* strain_scal;
+  const double* net;
+  const double* rowsum;
+  const double* r0s;
+  const double* seas;
+  const float* p_sia;
+  const int64_t* km;
+  const int32_t* sia_first; /* [nt] index into sia[] of the first event of the tick */
+  const int32_t* sia_cnt;   /* [nt] */
+  const DevSia* sia;
+  const int32_t* seed_first;
+  const int32_t* seed_cnt;
+  const DevSeed* seeds;
+  const uint8_t* future_seed; /* [nt] 1 if a seed event is scheduled after tick t */
+  int32_t* res;               /* results base */
+  int64_t res_off[RS_N];
+  /* unborn pool columns, indexed by reference slot - count0 */
+  int8_t *pl_et, *pl_it, *pl_pt, *pl_strain, *pl_pp, *pl_par, *pl_ipv;
+  uint8_t* pl_cm;
+  int16_t* pl_ri;
+  float *pl_risk, *pl_inf;
+  /* dynamic */
+  int32_t t;       /* next tick */
+  int32_t stopped; /* early stop happened */
+  int32_t stop_at; /* tick at which the stop rule fired, or INT32_MAX */
+  int32_t error;
+  int64_t count;
+  int32_t used_chunks;
+  int32_t csr_cur; /* which CSR buffer is current */
+  int32_t started;
+  /* per-tick, written by k_begin */
+  int32_t cur_t, active, vd_tick, ri_tick;
+  int32_t sia_n, sia_i0, seed_n, seed_i0;
+  int64_t nb_total, count_before;
+  int32_t any_demand, pad2;
+} DevRep;
+
+/* Global device state shared by the kernels of one handle. */
+typedef struct {
+  int32_t n_reps, G; /* replicates, global nodes */
+  int32_t total_chunks;
+  int32_t pad;
+  DevRep* reps;
+  /* per position */
+  int8_t *ds, *strain, *et, *it, *pt, *pp, *par, *ipv;
+  uint8_t* cm;
+  int16_t* ri;
+  float *risk, *inf;
+  int32_t *dob, *dod;
+  uint32_t* ref;
+  /* per chunk */
+  int32_t* chunk_node;
+  int32_t* chunk_fill;
+  int32_t* chunk_nbt; /* tick of the newborns written into the chunk */
+  int32_t* chunk_nbo; /* offset of the first of them */
+  uint64_t* chunk_w;  /* susceptible weight total */
+  uint64_t* sub_w;    /* [chunk][LPG_NSUB] */
+  uint64_t* cpref;    /* selection scratch, CSR order */
+  int32_t* node_chunks[2];
+  int32_t* node_chunk_start[2]; /* per sim: n_nodes + 1 entries at csr_base */
+  /* per global node */
+  int32_t* node_rep;
+  int64_t* node_count;
+  int32_t* ev;  /* [EV_N][G] */
+  int32_t* tot; /* [TT_N][G] */
+  uint64_t* sw; /* [G] */
+  uint64_t* bb; /* [LPG_MAX_STRAINS][G] */
+  int64_t* nb_end;
+  int64_t* nb_li0;
+  double* prob; /* [LPG_MAX_STRAINS][G] */
+  int64_t* size;
+  int64_t* uniq;
+  int64_t* ksel;
+  int64_t* tgt_off; /* [G + 1] */
+  uint32_t* hits;
+  int64_t hits_cap;
+  /* grid barrier of the cooperative selection kernel */
+  uint32_t* bar_count;
+  uint32_t* bar_gen;
+  int32_t* abort_flag;
+} DevWorld;
+
+#endif

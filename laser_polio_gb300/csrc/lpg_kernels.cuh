@@ -1,0 +1,1144 @@
+/*
+ * lpg_kernels.cuh — device kernels of the per-tick agent step.
+ *
+ * One tick is this fixed launch sequence (every kernel reads the tick and
+ * its flags from device memory, so the sequence is captured once in a CUDA
+ * graph and replayed):
+ *   k_begin      per simulation: stop rule (model.py:788-795), per-tick
+ *                counters, births per node (model.py:1711-1716) and their
+ *                chunk placement
+ *   k_newborns   newborn rows (model.py:1719-1730)
+ *   k_sweep<0>   fused sweep over every chunk: deaths (get_deaths,
+ *                model.py:1767-1781), disease progression and paralysis
+ *                (model.py:393-454), RI (fast_ri, :1784-1855) and SIA
+ *                (fast_sia, :1994-2060); on seed ticks RI/SIA wait for ...
+ *   k_seed       ... the seed schedule (model.py:759-786) and ...
+ *   k_sweep<1>   ... run after it
+ *   k_node_tx    per node: population (model.py:1751-1755), mixing,
+ *                seasonality, probabilities and exposure counts
+ *                (model.py:1327-1407)
+ *   k_select     cooperative: weighted selection rounds and strain
+ *                assignment (tx_infect_nb, model.py:1010-1149)
+ *   k_end        results rows of the tick (model.py:1461-1487 and the
+ *                result writes of every component)
+ */
+#ifndef LPG_KERNELS_CUH
+#define LPG_KERNELS_CUH
+
+#include <stdint.h>
+
+#include "lpg_engine.cuh"
+
+#define FULLMASK 0xffffffffu
+#define LPG_NONE 0xffffffffu
+#define LPG_MAX_ROUNDS 1000000
+#define LPG_SPIN_LIMIT (1LL << 25)
+
+/* ------------------------------------------------------------------------ */
+/* fixed-point weights (identical definitions in the oracle)                */
+__device__ __forceinline__ uint64_t fix_risk(float r) {
+  double d = (double)r * 16777216.0;
+  if (!(d > 0.0)) return 0;
+  if (d > 0x1.0p62) d = 0x1.0p62;
+  return (uint64_t)rint(d);
+}
+__device__ __forceinline__ uint64_t fix_beta(float inf, double scal) {
+  double d = ((double)inf * scal) * 4294967296.0;
+  if (!(d > 0.0)) return 0;
+  if (d > 0x1.0p62) d = 0x1.0p62;
+  return (uint64_t)rint(d);
+}
+__device__ __forceinline__ int8_t dec_i8(int8_t v) { return (int8_t)(uint8_t)((uint8_t)v - 1u); }
+__device__ __forceinline__ unsigned long long neg64(uint64_t w) { return (unsigned long long)(0ULL - w); }
+
+__device__ __forceinline__ int32_t* RES(const DevRep* rp, int k, int t) {
+  int wide = (k == RS_EBS || k == RS_IBS || k == RS_NEWEXPBS || k == RS_RINEWEXPBS || k == RS_SIANEWEXPBS);
+  return rp->res + rp->res_off[k] + (int64_t)t * rp->n_nodes * (wide ? rp->ns : 1);
+}
+
+/* Newborn lifespan: restates laser_core's KaplanMeierEstimator for age 0
+ * (model.py:1725).  Same arithmetic as the oracle's lpo_km_newborn. */
+__device__ int32_t km_newborn(const DevRep* rp, int32_t t, uint64_t slot) {
+  const int64_t* cum = rp->km;
+  int32_t top = rp->km_max_year < rp->km_len - 1 ? rp->km_max_year : rp->km_len - 1;
+  int64_t total = cum[top];
+  int32_t y = top;
+  if (total > 0) {
+    double u0 = lpg_u01(rp->seed, LPG_P_KM, t, slot, 0, 0);
+    int64_t draw = (int64_t)floor(u0 * (double)total);
+    int32_t lo = 0, hi = top;
+    while (lo < hi) {
+      int32_t mid = (lo + hi) >> 1;
+      if (cum[mid] > draw) hi = mid; else lo = mid + 1;
+    }
+    y = lo;
+  }
+  double u1 = lpg_u01(rp->seed, LPG_P_KM, t, slot, 0, 1);
+  return y * 365 + (int32_t)floor(u1 * 365.0);
+}
+
+/* Block-wide exclusive scan of one value per thread (blockDim multiple of 32). */
+__device__ int64_t block_excl_scan(int64_t v, int64_t* total) {
+  __shared__ int64_t ws[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int64_t y = __shfl_up_sync(FULLMASK, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int64_t s = lane < nw ? ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int64_t y = __shfl_up_sync(FULLMASK, s, o);
+      if (lane >= o) s += y;
+    }
+    ws[lane] = s;
+  }
+  __syncthreads();
+  int64_t incl = x + (wid > 0 ? ws[wid - 1] : 0);
+  *total = ws[nw - 1];
+  __syncthreads();
+  return incl - v;
+}
+
+/* ------------------------------------------------------------------------ */
+__global__ void k_begin(DevWorld W) {
+  DevRep* rp = &W.reps[blockIdx.x];
+  __shared__ int s_active, s_vd, s_t;
+  __shared__ unsigned long long s_sum;
+  if (threadIdx.x == 0) {
+    int t = rp->t;
+    int active = rp->started && !rp->error && !rp->stopped && t >= 1 && t < rp->nt;
+    rp->cur_t = t;
+    rp->active = active;
+    rp->vd_tick = active && (rp->comps & LPG_COMP_VD) && (t % rp->vd_step == 0);
+    rp->ri_tick = active && (rp->comps & LPG_COMP_RI) && rp->ri_enabled && (t % rp->ri_step == 0);
+    rp->sia_n = (active && (rp->comps & LPG_COMP_SIA)) ? rp->sia_cnt[t] : 0;
+    rp->sia_i0 = active ? rp->sia_first[t] : 0;
+    rp->seed_n = (active && (rp->comps & LPG_COMP_DS)) ? rp->seed_cnt[t] : 0;
+    rp->seed_i0 = active ? rp->seed_first[t] : 0;
+    rp->nb_total = 0;
+    rp->count_before = rp->count;
+    rp->any_demand = 0;
+    s_active = active;
+    s_vd = rp->vd_tick;
+    s_t = t;
+    s_sum = 0;
+  }
+  __syncthreads();
+  if (!s_active) return;
+  const int n = rp->n_nodes, nb = rp->node_base, t = s_t, G = W.G;
+  for (int k = 0; k < EV_N; ++k)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) W.ev[(int64_t)k * G + nb + i] = 0;
+
+  /* stop rule: evaluated on the E/I results of t-1 (model.py:788-795) */
+  if ((rp->comps & LPG_COMP_DS) && rp->stop_if) {
+    unsigned long long local = 0;
+    if (rp->comps & LPG_COMP_TX) {
+      const int32_t* E = RES(rp, RS_E, t - 1);
+      const int32_t* I = RES(rp, RS_I, t - 1);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) local += (unsigned long long)(E[i] > 0) + (I[i] > 0);
+    }
+    if (local) atomicAdd(&s_sum, local);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_sum == 0 && !rp->future_seed[t]) rp->stop_at = t;
+  }
+  if (!s_vd) return;
+
+  /* births per node: integer part + Bernoulli on the fraction (model.py:1711-1716) */
+  const int32_t* pop1 = RES(rp, RS_POP, t - 1);
+  int64_t carry_b = 0, carry_c = 0;
+  for (int base = 0; base < n; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    int64_t b = 0, newch = 0, li0 = 0;
+    if (i < n) {
+      int g = nb + i;
+      double expected = ((double)rp->vd_step * rp->birth_rate[i]) * (double)pop1[i];
+      int32_t bi = (int32_t)expected;
+      double frac = expected - (double)bi;
+      double u = lpg_u01(rp->seed, LPG_P_BIRTH, t, (uint64_t)i, 0, 0);
+      b = (int64_t)bi + (u < frac ? 1 : 0);
+      li0 = W.node_count[g];
+      int64_t c_old = li0 > 0 ? (li0 + LPG_CHUNK - 1) / LPG_CHUNK : 1;
+      int64_t c_new = li0 + b > 0 ? (li0 + b + LPG_CHUNK - 1) / LPG_CHUNK : 1;
+      newch = c_new - c_old;
+    }
+    int64_t tb, tc;
+    int64_t eb = block_excl_scan(b, &tb);
+    int64_t ec = block_excl_scan(newch, &tc);
+    if (i < n) {
+      int g = nb + i;
+      W.nb_end[g] = carry_b + eb + b;
+      W.nb_li0[g] = li0;
+      W.ev[(int64_t)EV_BIRTHS * G + g] = (int32_t)b;
+      W.ksel[g] = carry_c + ec; /* scratch: new chunks before this node */
+    }
+    carry_b += tb;
+    carry_c += tc;
+  }
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    s_ok = 1;
+    if (rp->count + carry_b > rp->capacity) {
+      rp->error = LPG_ERR_CAPACITY;
+      rp->active = 0;
+      s_ok = 0;
+    } else if (rp->used_chunks + carry_c > rp->chunk_cap) {
+      rp->error = LPG_ERR_INTERNAL;
+      rp->active = 0;
+      s_ok = 0;
+    }
+  }
+  __syncthreads();
+  if (!s_ok || carry_b == 0) return;
+
+  int cur = rp->csr_cur;
+  if (carry_c > 0) {
+    /* rebuild the node -> chunk lists into the other buffer */
+    int nw = 1 - cur;
+    const int32_t* so = W.node_chunk_start[cur] + rp->csr_base;
+    int32_t* sn = W.node_chunk_start[nw] + rp->csr_base;
+    const int32_t* lo_ = W.node_chunks[cur] + rp->chunk_base;
+    int32_t* ln = W.node_chunks[nw] + rp->chunk_base;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sn[i] = so[i] + (int32_t)W.ksel[nb + i];
+    if (threadIdx.x == 0) sn[n] = so[n] + (int32_t)carry_c;
+    __syncthreads();
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int i = wid; i < n; i += nwarp) {
+      int32_t a0 = so[i], a1 = so[i + 1], d0 = sn[i];
+      for (int k = lane; k < a1 - a0; k += 32) ln[d0 + k] = lo_[a0 + k];
+      int32_t added = (sn[i + 1] - sn[i]) - (a1 - a0);
+      for (int k = lane; k < added; k += 32) {
+        int32_t cid = rp->chunk_base + rp->used_chunks + (int32_t)W.ksel[nb + i] + k;
+        ln[d0 + (a1 - a0) + k] = cid;
+        W.chunk_node[cid] = nb + i;
+        W.chunk_fill[cid] = 0;
+        W.chunk_nbt[cid] = -1;
+        W.chunk_w[cid] = 0;
+        for (int s = 0; s < LPG_NSUB; ++s) W.sub_w[(int64_t)cid * LPG_NSUB + s] = 0;
+      }
+    }
+    __syncthreads();
+    cur = nw;
+  }
+  /* chunk fills and newborn markers */
+  const int32_t* st = W.node_chunk_start[cur] + rp->csr_base;
+  const int32_t* ls = W.node_chunks[cur] + rp->chunk_base;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    int g = nb + i;
+    int64_t b = W.ev[(int64_t)EV_BIRTHS * G + g];
+    if (b == 0) continue;
+    int64_t li0 = W.nb_li0[g], newc = li0 + b;
+    for (int64_t k = li0 / LPG_CHUNK; k <= (newc - 1) / LPG_CHUNK; ++k) {
+      int32_t cid = ls[st[i] + k];
+      int64_t f = newc - k * LPG_CHUNK;
+      W.chunk_fill[cid] = (int32_t)(f < LPG_CHUNK ? f : LPG_CHUNK);
+      W.chunk_nbt[cid] = t;
+      W.chunk_nbo[cid] = (k == li0 / LPG_CHUNK) ? (int32_t)(li0 % LPG_CHUNK) : 0;
+    }
+    W.node_count[g] = newc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    rp->csr_cur = cur;
+    rp->used_chunks += (int32_t)carry_c;
+    rp->count += carry_b;
+    rp->nb_total = carry_b;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+__global__ void k_newborns(DevWorld W) {
+  const DevRep* rp = &W.reps[blockIdx.y];
+  if (!rp->active || !rp->vd_tick || rp->nb_total == 0) return;
+  const int n = rp->n_nodes, nb = rp->node_base, t = rp->cur_t, G = W.G;
+  const int64_t total = rp->nb_total;
+  const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+  const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (W.nb_end[nb + mid] > j) hi = mid; else lo = mid + 1;
+    }
+    int g = nb + lo;
+    int64_t bstart = W.nb_end[g] - W.ev[(int64_t)EV_BIRTHS * G + g];
+    int64_t li = W.nb_li0[g] + (j - bstart);
+    int32_t cid = ls[st[lo] + li / LPG_CHUNK];
+    int64_t off = li % LPG_CHUNK;
+    int64_t pos = (int64_t)cid * LPG_CHUNK + off;
+    int64_t ref = rp->count_before + j;
+    int64_t q = ref - rp->count0;
+    W.et[pos] = rp->pl_et[q];
+    W.it[pos] = rp->pl_it[q];
+    W.pt[pos] = rp->pl_pt[q];
+    W.strain[pos] = rp->pl_strain[q];
+    int8_t pp = rp->pl_pp[q], par = rp->pl_par[q];
+    W.pp[pos] = pp;
+    W.par[pos] = par;
+    W.ipv[pos] = rp->pl_ipv[q];
+    W.cm[pos] = rp->pl_cm[q];
+    W.ri[pos] = rp->pl_ri[q];
+    float risk = rp->pl_risk[q];
+    W.risk[pos] = risk;
+    W.inf[pos] = rp->pl_inf[q];
+    W.dob[pos] = t;
+    W.dod[pos] = t + km_newborn(rp, t, (uint64_t)ref);
+    W.ref[pos] = (uint32_t)ref;
+    W.ds[pos] = 0;
+    uint64_t w = fix_risk(risk);
+    atomicAdd(&W.tot[(int64_t)TT_S * G + g], 1);
+    if (w) {
+      atomicAdd((unsigned long long*)&W.sw[g], (unsigned long long)w);
+      atomicAdd((unsigned long long*)&W.chunk_w[cid], (unsigned long long)w);
+      atomicAdd((unsigned long long*)&W.sub_w[(int64_t)cid * LPG_NSUB + off / LPG_SUB], (unsigned long long)w);
+    }
+    if (pp == 1) atomicAdd(&W.tot[(int64_t)TT_POTP * G + g], 1);
+    if (par == 1) atomicAdd(&W.tot[(int64_t)TT_P * G + g], 1);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Shared-memory node counters of one sweep CTA, flushed on node change. */
+struct SweepSmem {
+  int32_t ev[EV_N];
+  int32_t tot[TT_N];
+  unsigned long long sw;
+  unsigned long long bb[LPG_MAX_STRAINS];
+};
+
+__device__ __forceinline__ void sweep_flush(SweepSmem& S, DevWorld& W, int g) {
+  __syncthreads();
+  if (g >= 0) {
+    int k = threadIdx.x;
+    if (k < EV_N) {
+      int32_t v = S.ev[k];
+      if (v) atomicAdd(&W.ev[(int64_t)k * W.G + g], v);
+    } else if (k < EV_N + TT_N) {
+      int32_t v = S.tot[k - EV_N];
+      if (v) atomicAdd(&W.tot[(int64_t)(k - EV_N) * W.G + g], v);
+    } else if (k == EV_N + TT_N) {
+      if (S.sw) atomicAdd((unsigned long long*)&W.sw[g], S.sw);
+    } else if (k < EV_N + TT_N + 1 + LPG_MAX_STRAINS) {
+      int s = k - EV_N - TT_N - 1;
+      if (S.bb[s]) atomicAdd((unsigned long long*)&W.bb[(int64_t)s * W.G + g], S.bb[s]);
+    }
+  }
+  __syncthreads();
+  int k = threadIdx.x;
+  if (k < EV_N) S.ev[k] = 0;
+  else if (k < EV_N + TT_N) S.tot[k - EV_N] = 0;
+  else if (k == EV_N + TT_N) S.sw = 0;
+  else if (k < EV_N + TT_N + 1 + LPG_MAX_STRAINS) S.bb[k - EV_N - TT_N - 1] = 0;
+  __syncthreads();
+}
+
+/* An agent leaves S: node, chunk and sub-block weights drop by its risk. */
+__device__ __forceinline__ void s_exit(SweepSmem& S, DevWorld& W, int64_t pos, int64_t cid) {
+  uint64_t w = fix_risk(W.risk[pos]);
+  atomicAdd(&S.tot[TT_S], -1);
+  if (w) {
+    atomicAdd(&S.sw, neg64(w));
+    atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
+    atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
+  }
+}
+
+__device__ __forceinline__ bool any_ei(uint64_t x) {
+  uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+  uint32_t m = __vcmpltu4(__vsub4(lo, 0x01010101u), 0x02020202u) | __vcmpltu4(__vsub4(hi, 0x01010101u), 0x02020202u);
+  return m != 0;
+}
+
+/* Fused sweep.  PHASE 0 does deaths and disease progression, plus RI/SIA
+ * unless a seed event falls on the tick; PHASE 1 does RI/SIA on seed ticks. */
+template <int PHASE>
+__global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
+  __shared__ SweepSmem S;
+  __shared__ int32_t s_off[1025];
+  __shared__ int32_t s_nreps;
+  const int R = W.n_reps;
+  if (threadIdx.x == 0) {
+    int32_t acc = 0;
+    for (int r = 0; r < R && r < 1024; ++r) {
+      s_off[r] = acc;
+      const DevRep* rp = &W.reps[r];
+      int work = rp->active;
+      if (PHASE == 1) work = work && rp->seed_n > 0 && (rp->ri_tick || rp->sia_n > 0);
+      acc += work ? rp->used_chunks : 0;
+    }
+    s_off[R < 1024 ? R : 1024] = acc;
+    s_nreps = R < 1024 ? R : 1024;
+  }
+  {
+    int k = threadIdx.x;
+    if (k < EV_N) S.ev[k] = 0;
+    else if (k < EV_N + TT_N) S.tot[k - EV_N] = 0;
+    else if (k == EV_N + TT_N) S.sw = 0;
+    else if (k < EV_N + TT_N + 1 + LPG_MAX_STRAINS) S.bb[k - EV_N - TT_N - 1] = 0;
+  }
+  __syncthreads();
+  const int32_t total = s_off[s_nreps];
+  if (total == 0) return;
+  const int32_t per = (total + gridDim.x - 1) / gridDim.x;
+  const int32_t w0 = blockIdx.x * per;
+  const int32_t w1 = min(w0 + per, total);
+  int cur_g = -1;
+  const int o = threadIdx.x * LPG_SPT;
+
+  for (int32_t w = w0; w < w1; ++w) {
+    int lo = 0, hi = s_nreps - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (s_off[mid] <= w) lo = mid; else hi = mid - 1;
+    }
+    const DevRep* rp = &W.reps[lo];
+    const int64_t cid = rp->chunk_base + (w - s_off[lo]);
+    const int g = W.chunk_node[cid];
+    if (g != cur_g) {
+      sweep_flush(S, W, cur_g);
+      cur_g = g;
+    }
+    const int t = rp->cur_t;
+    const int ni = g - rp->node_base;
+    const int do_vd = PHASE == 0 && rp->vd_tick;
+    const int do_ds = PHASE == 0 && (rp->comps & LPG_COMP_DS);
+    const int late = (PHASE == 0) == (rp->seed_n == 0);
+    const int do_ri = late && rp->ri_tick;
+    const int nsia = late ? rp->sia_n : 0;
+    const int fill = W.chunk_fill[cid];
+    if (o >= fill) continue;
+    const int nbo = (W.chunk_nbt[cid] == t) ? W.chunk_nbo[cid] : LPG_CHUNK;
+    const int64_t pos0 = cid * LPG_CHUNK + o;
+    const uint64_t st8 = *reinterpret_cast<const uint64_t*>(W.ds + pos0);
+    const bool need = do_vd || do_ri || nsia > 0 || (do_ds && any_ei(st8));
+    if (!need) continue;
+
+    /* dense per-tick columns, loaded only on the ticks that need them */
+    int32_t dod[LPG_SPT], dob[LPG_SPT];
+    int16_t rit[LPG_SPT];
+    uint8_t cmv[LPG_SPT];
+    if (do_vd) {
+      int4 a = *reinterpret_cast<const int4*>(W.dod + pos0);
+      int4 b = *reinterpret_cast<const int4*>(W.dod + pos0 + 4);
+      dod[0] = a.x; dod[1] = a.y; dod[2] = a.z; dod[3] = a.w;
+      dod[4] = b.x; dod[5] = b.y; dod[6] = b.z; dod[7] = b.w;
+    }
+    if (do_ri || nsia) {
+      uint64_t c8 = *reinterpret_cast<const uint64_t*>(W.cm + pos0);
+#pragma unroll
+      for (int j = 0; j < LPG_SPT; ++j) cmv[j] = (uint8_t)(c8 >> (8 * j));
+    }
+    if (do_ri) {
+      int4 a = *reinterpret_cast<const int4*>(W.ri + pos0);
+      const int16_t* pa = reinterpret_cast<const int16_t*>(&a);
+#pragma unroll
+      for (int j = 0; j < LPG_SPT; ++j) rit[j] = pa[j];
+    }
+    if (nsia) {
+      int4 a = *reinterpret_cast<const int4*>(W.dob + pos0);
+      int4 b = *reinterpret_cast<const int4*>(W.dob + pos0 + 4);
+      dob[0] = a.x; dob[1] = a.y; dob[2] = a.z; dob[3] = a.w;
+      dob[4] = b.x; dob[5] = b.y; dob[6] = b.z; dob[7] = b.w;
+    }
+    uint64_t out8 = st8;
+    bool ri_dirty = false;
+    const int nvalid = min(LPG_SPT, fill - o);
+    for (int j = 0; j < nvalid; ++j) {
+      const int64_t pos = pos0 + j;
+      int8_t s = (int8_t)(st8 >> (8 * j));
+      const int8_t s_in = s;
+      int st = -1; /* strain, loaded on demand */
+      /* -- deaths (get_deaths) -------------------------------------------- */
+      if (do_vd && s >= 0 && (o + j) < nbo && dod[j] <= t) {
+        atomicAdd(&S.ev[EV_DEATHS], 1);
+        if (s == 0) {
+          s_exit(S, W, pos, cid);
+        } else if (s == 1 || s == 2) {
+          st = W.strain[pos];
+          if (s == 1) {
+            atomicAdd(&S.tot[TT_E0 + st], -1);
+          } else {
+            atomicAdd(&S.tot[TT_I0 + st], -1);
+            uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+            if (bw) atomicAdd(&S.bb[st], neg64(bw));
+          }
+        } else if (s == 3) {
+          atomicAdd(&S.tot[TT_R], -1);
+        }
+        if (W.pp[pos] == 1) atomicAdd(&S.tot[TT_POTP], -1);
+        if (W.par[pos] == 1) atomicAdd(&S.tot[TT_P], -1);
+        s = -1;
+      }
+      /* -- disease progression (disease_state_step_kernel) ------------------ */
+      if (do_ds) {
+        if (s == 1) {
+          int8_t e = W.et[pos];
+          if (st < 0) st = W.strain[pos];
+          if (e <= 0) {
+            s = 2;
+            atomicAdd(&S.tot[TT_E0 + st], -1);
+            atomicAdd(&S.tot[TT_I0 + st], 1);
+            uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+            if (bw) atomicAdd(&S.bb[st], (unsigned long long)bw);
+          }
+          W.et[pos] = dec_i8(e);
+        }
+        if (s == 2) {
+          int8_t i = W.it[pos];
+          if (st < 0) st = W.strain[pos];
+          if (i <= 0) {
+            s = 3;
+            atomicAdd(&S.tot[TT_I0 + st], -1);
+            atomicAdd(&S.tot[TT_R], 1);
+            uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+            if (bw) atomicAdd(&S.bb[st], neg64(bw));
+          }
+          W.it[pos] = dec_i8(i);
+          if (st == 0) {
+            int8_t p = W.pt[pos];
+            if (p <= 0 && W.pp[pos] == -1) {
+              if (W.ipv[pos] == 0) {
+                W.pp[pos] = 1;
+                atomicAdd(&S.tot[TT_POTP], 1);
+                atomicAdd(&S.ev[EV_NEWPOT], 1);
+                if (lpg_u01(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < (double)rp->p_par) {
+                  W.par[pos] = 1;
+                  atomicAdd(&S.tot[TT_P], 1);
+                  atomicAdd(&S.ev[EV_NEWPAR], 1);
+                }
+              } else {
+                W.pp[pos] = 0;
+              }
+            }
+            W.pt[pos] = dec_i8(p);
+          }
+        }
+      }
+      /* -- routine immunisation (fast_ri) ------------------------------------ */
+      if (do_ri && s >= 0 && cmv[j] != 1) {
+        int32_t timer = (int32_t)rit[j] - rp->ri_step;
+        rit[j] = (int16_t)(uint16_t)(uint32_t)timer;
+        ri_dirty = true;
+        bool eligible = false;
+        if (t == rp->ri_step) eligible = timer <= 0 && timer >= -rp->ri_step;
+        else if (t > rp->ri_step) eligible = timer <= 0 && timer > -rp->ri_step;
+        if (eligible) {
+          uint32_t ref = W.ref[pos];
+          if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 0) < rp->p_ri[ni]) {
+            atomicAdd(&S.ev[EV_RIVAC], 1);
+            if (s == 0) {
+              s = 1;
+              W.strain[pos] = (int8_t)rp->ri_strain;
+              st = rp->ri_strain;
+              atomicAdd(&S.ev[EV_RIPROT], 1);
+              s_exit(S, W, pos, cid);
+              atomicAdd(&S.tot[TT_E0 + rp->ri_strain], 1);
+            }
+          }
+          if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 1) < rp->p_ipv[ni]) {
+            atomicAdd(&S.ev[EV_IPVVAC], 1);
+            W.ipv[pos] = 1;
+          }
+        }
+      }
+      /* -- SIA campaigns of the day (fast_sia) ------------------------------- */
+      for (int k = 0; k < nsia; ++k) {
+        if (s < 0 || cmv[j] == 1) break;
+        const DevSia& ev = rp->sia[rp->sia_i0 + k];
+        int64_t age = (int64_t)t - (int64_t)dob[j];
+        if (!(ev.min_age <= age && age <= ev.max_age)) continue;
+        if (ev.mask[ni] == 0) continue;
+        double r = lpg_u01(rp->seed, LPG_P_SIA, t, W.ref[pos], 0, (uint64_t)k);
+        double p = (double)rp->p_sia[ni];
+        if (r < p) {
+          atomicAdd(&S.ev[EV_SIAVAC0 + k], 1);
+          if (s == 0 && r < p * ev.efficacy) {
+            s = 1;
+            W.strain[pos] = (int8_t)ev.strain;
+            st = ev.strain;
+            atomicAdd(&S.ev[EV_SIAPROT0 + k], 1);
+            s_exit(S, W, pos, cid);
+            atomicAdd(&S.tot[TT_E0 + ev.strain], 1);
+          }
+        }
+      }
+      if (s != s_in) {
+        out8 = (out8 & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)s << (8 * j));
+      }
+    }
+    if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
+    if (ri_dirty) {
+      int4 a;
+      int16_t* pa = reinterpret_cast<int16_t*>(&a);
+      const int4 old = *reinterpret_cast<const int4*>(W.ri + pos0);
+      const int16_t* po = reinterpret_cast<const int16_t*>(&old);
+#pragma unroll
+      for (int j = 0; j < LPG_SPT; ++j) pa[j] = (j < nvalid) ? rit[j] : po[j];
+      *reinterpret_cast<int4*>(W.ri + pos0) = a;
+    }
+  }
+  sweep_flush(S, W, cur_g);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Seed schedule: one CTA per simulation, events of the tick in order. */
+__global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
+  const DevRep* rp = &W.reps[blockIdx.x];
+  if (!rp->active || rp->seed_n == 0) return;
+  const int t = rp->cur_t, nb = rp->node_base, G = W.G;
+  const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+  const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
+  __shared__ unsigned long long s_cnt;
+  __shared__ unsigned int hist[256];
+  __shared__ uint64_t s_prefix;
+  __shared__ int64_t s_need;
+  __shared__ unsigned long long s_ties;
+  __shared__ int s_ntie;
+  __shared__ uint32_t s_tie_ref[64];
+  __shared__ int64_t s_tie_pos[64];
+  for (int e = rp->seed_i0; e < rp->seed_i0 + rp->seed_n; ++e) {
+    const DevSeed ev = rp->seeds[e];
+    const int ni = ev.node;
+    if (ni < 0 || ni >= rp->n_nodes) continue;
+    const int g = nb + ni;
+    const int64_t nslots = W.node_count[g];
+    const int32_t c0 = st[ni];
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    unsigned long long local = 0;
+    for (int64_t li = threadIdx.x; li < nslots; li += blockDim.x) {
+      int64_t pos = (int64_t)ls[c0 + li / LPG_CHUNK] * LPG_CHUNK + li % LPG_CHUNK;
+      local += W.ds[pos] >= 0;
+    }
+    atomicAdd(&s_cnt, local);
+    __syncthreads();
+    const int64_t N = (int64_t)s_cnt;
+    int64_t nseed = ev.is_count ? (int64_t)ev.value : (int64_t)((double)N * ev.value);
+    if (ev.is_count && nseed > N) nseed = N;
+    if (nseed <= 0) {
+      __syncthreads();
+      continue;
+    }
+    /* radix select of the nseed-th smallest key among the candidates */
+    if (threadIdx.x == 0) {
+      s_prefix = 0;
+      s_need = nseed;
+    }
+    __syncthreads();
+    const bool all = nseed >= N;
+    if (!all) {
+      for (int shift = 56; shift >= 0; shift -= 8) {
+        for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+        __syncthreads();
+        const uint64_t hmask = shift == 56 ? 0ULL : (~0ULL << (shift + 8));
+        const uint64_t pre = s_prefix;
+        for (int64_t li = threadIdx.x; li < nslots; li += blockDim.x) {
+          int64_t pos = (int64_t)ls[c0 + li / LPG_CHUNK] * LPG_CHUNK + li % LPG_CHUNK;
+          if (W.ds[pos] < 0) continue;
+          uint64_t key = lpg_raw(rp->seed, LPG_P_SEEDPICK, t, W.ref[pos], (uint64_t)ev.pad, 0);
+          if ((key & hmask) == (pre & hmask)) atomicAdd(&hist[(key >> shift) & 255], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          int64_t need = s_need, cum = 0;
+          int b = 0;
+          for (; b < 256; ++b) {
+            if (cum + hist[b] >= need) break;
+            cum += hist[b];
+          }
+          s_prefix = pre | ((uint64_t)b << shift);
+          s_need = need - cum;
+        }
+        __syncthreads();
+      }
+    }
+    const uint64_t kstar = s_prefix;
+    const int64_t need_ties = s_need;
+    /* ties on the threshold key: keep the lowest reference slots */
+    if (threadIdx.x == 0) {
+      s_ties = 0;
+      s_ntie = 0;
+    }
+    __syncthreads();
+    if (!all) {
+      for (int64_t li = threadIdx.x; li < nslots; li += blockDim.x) {
+        int64_t pos = (int64_t)ls[c0 + li / LPG_CHUNK] * LPG_CHUNK + li % LPG_CHUNK;
+        if (W.ds[pos] < 0) continue;
+        uint64_t key = lpg_raw(rp->seed, LPG_P_SEEDPICK, t, W.ref[pos], (uint64_t)ev.pad, 0);
+        if (key == kstar) {
+          unsigned long long k = atomicAdd(&s_ties, 1ULL);
+          if (k < 64) {
+            s_tie_ref[k] = W.ref[pos];
+            s_tie_pos[k] = pos;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !all) {
+      int nt_ = (int)(s_ties < 64 ? s_ties : 64);
+      if (s_ties > 64) W.reps[blockIdx.x].error = LPG_ERR_INTERNAL;
+      /* order the ties by reference slot (insertion sort, at most 64) */
+      for (int a = 1; a < nt_; ++a) {
+        uint32_t rk = s_tie_ref[a];
+        int64_t pk = s_tie_pos[a];
+        int b = a - 1;
+        while (b >= 0 && s_tie_ref[b] > rk) {
+          s_tie_ref[b + 1] = s_tie_ref[b];
+          s_tie_pos[b + 1] = s_tie_pos[b];
+          --b;
+        }
+        s_tie_ref[b + 1] = rk;
+        s_tie_pos[b + 1] = pk;
+      }
+      s_ntie = (int)(need_ties < nt_ ? need_ties : nt_);
+    }
+    __syncthreads();
+    /* apply: state 2 regardless of state; redraw non-positive infection timers */
+    for (int64_t li = threadIdx.x; li < nslots + 64; li += blockDim.x) {
+      int64_t pos;
+      if (li < nslots) {
+        pos = (int64_t)ls[c0 + li / LPG_CHUNK] * LPG_CHUNK + li % LPG_CHUNK;
+        int8_t s = W.ds[pos];
+        if (s < 0) continue;
+        if (!all) {
+          uint64_t key = lpg_raw(rp->seed, LPG_P_SEEDPICK, t, W.ref[pos], (uint64_t)ev.pad, 0);
+          if (!(key < kstar)) continue;
+        }
+      } else {
+        int k = (int)(li - nslots);
+        if (all || k >= s_ntie) continue;
+        pos = s_tie_pos[k];
+      }
+      int8_t s = W.ds[pos];
+      int sti = W.strain[pos];
+      const int64_t cid = pos / LPG_CHUNK;
+      if (s != 2) {
+        uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[sti]);
+        if (s == 0) {
+          uint64_t w = fix_risk(W.risk[pos]);
+          atomicAdd(&W.tot[(int64_t)TT_S * G + g], -1);
+          if (w) {
+            atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
+            atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
+            atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
+          }
+        } else if (s == 1) {
+          atomicAdd(&W.tot[(int64_t)(TT_E0 + sti) * G + g], -1);
+        } else if (s == 3) {
+          atomicAdd(&W.tot[(int64_t)TT_R * G + g], -1);
+        }
+        atomicAdd(&W.tot[(int64_t)(TT_I0 + sti) * G + g], 1);
+        if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)sti * G + g], (unsigned long long)bw);
+        W.ds[pos] = 2;
+      }
+      if (W.it[pos] <= 0) {
+        lpg_stream sm;
+        lpg_stream_init(&sm, rp->seed, LPG_P_SEEDTIMER, t, W.ref[pos], (uint64_t)ev.pad);
+        W.it[pos] = lpg_trunc_i8(lpg_dist_sample(&sm, rp->dur_kind, rp->dur_p1, rp->dur_p2));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Node-level force of infection and exposure counts; same arithmetic, in
+ * the same order, as the oracle's lpo_node_tx. */
+__global__ void k_node_tx(DevWorld W) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= W.G) return;
+  DevRep* rp = &W.reps[W.node_rep[g]];
+  if (!rp->active) return;
+  const int i = g - rp->node_base, n = rp->n_nodes, ns = rp->ns, t = rp->cur_t, G = W.G;
+  const int nb = rp->node_base;
+  int32_t pop_t = 0;
+  if (rp->comps & LPG_COMP_VD) {
+    const int32_t* pop1 = RES(rp, RS_POP, t - 1);
+    pop_t = pop1[i];
+    if (rp->vd_tick) pop_t = pop_t + W.ev[(int64_t)EV_BIRTHS * G + g] - W.ev[(int64_t)EV_DEATHS * G + g];
+    RES(rp, RS_POP, t)[i] = pop_t;
+  } else {
+    pop_t = RES(rp, RS_POP, t)[i];
+  }
+  W.size[g] = 0;
+  W.uniq[g] = 0;
+  if (!(rp->comps & LPG_COMP_TX)) return;
+  double p[LPG_MAX_STRAINS];
+  double total_p = 0.0;
+  int local_zero = 1;
+  const double rowsum = rp->rowsum[i];
+  for (int k = 0; k < ns; ++k) {
+    const uint64_t* Bk = W.bb + (int64_t)k * G + nb;
+    if (Bk[i] != 0) local_zero = 0;
+    double inc = 0.0;
+    for (int ii = 0; ii < n; ++ii) inc = inc + ((double)Bk[ii] * 0x1.0p-32) * rp->net[(int64_t)ii * n + i];
+    double bpre = (double)Bk[i] * 0x1.0p-32;
+    double beta = bpre + (inc - bpre * rowsum);
+    beta = (beta * rp->seas[t]) * rp->r0s[i];
+    double denom = (double)(pop_t > 1 ? pop_t : 1);
+    double rate = beta / denom;
+    double pk = -lpg_expm1(-rate);
+    if (!(pk > 0.0)) pk = 0.0;
+    p[k] = pk;
+    total_p = total_p + pk;
+  }
+  for (int k = 0; k < ns; ++k) W.prob[(int64_t)k * G + g] = p[k];
+  const double srisk = (double)W.sw[g] * 0x1.0p-24;
+  const double exposure = srisk * total_p;
+  int64_t total = 0;
+  lpg_stream sm;
+  lpg_stream_init(&sm, rp->seed, LPG_P_TXCOUNT, t, (uint64_t)i, 0);
+  if (!(exposure > 0.0)) {
+    total = 0;
+  } else if (local_zero) {
+    if (rp->zi >= 1.0) {
+      total = 0;
+    } else {
+      double mean = exposure / (1.0 - rp->zi);
+      double r = (double)rp->nb_r;
+      double pp = r / (r + mean);
+      double u = lpg_next(&sm);
+      total = (u < rp->zi) ? 0 : lpg_negbinom(&sm, r, pp);
+    }
+  } else {
+    total = lpg_poisson(&sm, exposure);
+  }
+  const int64_t sc = W.tot[(int64_t)TT_S * G + g];
+  const int64_t size = total < sc ? total : sc;
+  W.size[g] = size;
+  if (size > 0) rp->any_demand = 1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Software grid barrier for the cooperative selection kernel (all CTAs are
+ * co-resident by cooperative launch).  Every wait is bounded: on timeout the
+ * kernel raises abort_flag and all CTAs leave. */
+__device__ __forceinline__ bool grid_sync(DevWorld& W) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t* genp = W.bar_gen;
+    uint32_t gen = *genp;
+    __threadfence();
+    uint32_t arrived = atomicAdd(W.bar_count, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch(W.bar_count, 0u);
+      __threadfence();
+      atomicAdd(W.bar_gen, 1u);
+    } else {
+      long long it = 0;
+      while (*genp == gen) {
+        __nanosleep(64);
+        if (++it > LPG_SPIN_LIMIT) {
+          atomicExch(W.abort_flag, 1);
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile int32_t*)W.abort_flag == 0;
+}
+
+__device__ __forceinline__ int pick_strain(const double* p, int ns, double total_p, double r) {
+  double cum = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    cum = cum + p[k] / total_p;
+    if (r < cum) return k;
+  }
+  return 0;
+}
+
+__global__ void __launch_bounds__(256) k_select(DevWorld W) {
+  const int R = W.n_reps, G = W.G;
+  int any = 0;
+  for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
+  if (!any) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
+  const int64_t gwarp = gtid >> 5, nwarps = gsz >> 5;
+  __shared__ int64_t s_K;
+  for (int round = 0; round < LPG_MAX_ROUNDS; ++round) {
+    /* A1: remaining demand and chunk prefix of every node that still needs draws */
+    for (int64_t g = gwarp; g < G; g += nwarps) {
+      const DevRep* rp = &W.reps[W.node_rep[g]];
+      int64_t k = 0;
+      if (rp->active && (rp->comps & LPG_COMP_TX)) {
+        k = W.size[g] - W.uniq[g];
+        if (k < 0) k = 0;
+        if (W.sw[g] == 0) k = 0;
+      }
+      if (lane == 0) W.ksel[g] = k;
+      if (k > 0) {
+        const int i = (int)(g - rp->node_base);
+        const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+        const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
+        uint64_t* cp = W.cpref + rp->chunk_base;
+        uint64_t carry = 0;
+        for (int32_t a = st[i]; a < st[i + 1]; a += 32) {
+          int32_t idx = a + lane;
+          uint64_t v = idx < st[i + 1] ? W.chunk_w[ls[idx]] : 0;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            uint64_t y = __shfl_up_sync(FULLMASK, v, o);
+            if (lane >= o) v += y;
+          }
+          if (idx < st[i + 1]) cp[idx] = carry + v;
+          carry += __shfl_sync(FULLMASK, v, 31);
+        }
+      }
+    }
+    if (!grid_sync(W)) return;
+    /* A2: target offsets of all nodes */
+    if (blockIdx.x == 0) {
+      int64_t carry = 0;
+      for (int base = 0; base < G; base += blockDim.x) {
+        int g = base + threadIdx.x;
+        int64_t k = g < G ? W.ksel[g] : 0;
+        int64_t tot;
+        int64_t ex = block_excl_scan(k, &tot);
+        if (g < G) W.tgt_off[g] = carry + ex;
+        carry += tot;
+      }
+      if (threadIdx.x == 0) W.tgt_off[G] = carry;
+    }
+    if (!grid_sync(W)) return;
+    if (threadIdx.x == 0) s_K = W.tgt_off[G];
+    __syncthreads();
+    const int64_t K = s_K;
+    if (K == 0) break;
+    if (K > W.hits_cap) {
+      if (gtid == 0) W.reps[0].error = LPG_ERR_INTERNAL;
+      return;
+    }
+    /* B: locate every target in its node's frozen susceptible CDF */
+    for (int64_t q = gtid; q < K; q += gsz) {
+      int lo = 0, hi = G;
+      while (lo < hi) { /* first g with tgt_off[g] > q */
+        int mid = (lo + hi) >> 1;
+        if (W.tgt_off[mid] > q) hi = mid; else lo = mid + 1;
+      }
+      const int g = lo - 1;
+      const DevRep* rp = &W.reps[W.node_rep[g]];
+      const int i = g - rp->node_base;
+      const int64_t j = q - W.tgt_off[g];
+      uint64_t v = lpg_scale_target(lpg_u53(rp->seed, LPG_P_SELECT, rp->cur_t, (uint64_t)i, (uint64_t)round, (uint64_t)j), W.sw[g]);
+      const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+      const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
+      const uint64_t* cp = W.cpref + rp->chunk_base;
+      int32_t a = st[i], b = st[i + 1] - 1;
+      while (a < b) {
+        int32_t mid = (a + b) >> 1;
+        if (cp[mid] > v) b = mid; else a = mid + 1;
+      }
+      if (a > st[i]) v -= cp[a - 1];
+      const int64_t cid = ls[a];
+      int sb = 0;
+      for (; sb < LPG_NSUB; ++sb) {
+        uint64_t w = W.sub_w[cid * LPG_NSUB + sb];
+        if (w > v) break;
+        v -= w;
+      }
+      uint32_t hit = LPG_NONE;
+      if (sb < LPG_NSUB) {
+        const int64_t p0 = cid * LPG_CHUNK + (int64_t)sb * LPG_SUB;
+        for (int k = 0; k < LPG_SUB; ++k) {
+          if (W.ds[p0 + k] != 0) continue;
+          uint64_t w = fix_risk(W.risk[p0 + k]);
+          if (w > v) {
+            hit = (uint32_t)(p0 + k);
+            break;
+          }
+          v -= w;
+        }
+      }
+      if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
+      W.hits[q] = hit;
+    }
+    if (!grid_sync(W)) return;
+    /* C: first target to reach an agent exposes it; strain by relative FOI */
+    for (int64_t q = gtid; q < K; q += gsz) {
+      const uint32_t hit = W.hits[q];
+      if (hit == LPG_NONE) continue;
+      const int64_t pos = hit;
+      uint32_t* wp = reinterpret_cast<uint32_t*>(W.ds + (pos & ~3LL));
+      const int sh = (int)(pos & 3) * 8;
+      uint32_t old = *(volatile uint32_t*)wp;
+      bool won = false;
+      while (((old >> sh) & 0xffu) == 0) {
+        uint32_t nw = (old & ~(0xffu << sh)) | (1u << sh);
+        uint32_t prev = atomicCAS(wp, old, nw);
+        if (prev == old) {
+          won = true;
+          break;
+        }
+        old = prev;
+      }
+      if (!won) continue;
+      const int64_t cid = pos / LPG_CHUNK;
+      const int g = W.chunk_node[cid];
+      const DevRep* rp = &W.reps[W.node_rep[g]];
+      double p[LPG_MAX_STRAINS];
+      double totalp = 0.0;
+      for (int k = 0; k < rp->ns; ++k) {
+        p[k] = W.prob[(int64_t)k * G + g];
+        totalp = totalp + p[k];
+      }
+      double r = lpg_u01(rp->seed, LPG_P_STRAIN, rp->cur_t, W.ref[pos], 0, 0);
+      int s = pick_strain(p, rp->ns, totalp, r);
+      W.strain[pos] = (int8_t)s;
+      uint64_t w = fix_risk(W.risk[pos]);
+      atomicAdd(&W.tot[(int64_t)TT_S * G + g], -1);
+      atomicAdd(&W.tot[(int64_t)(TT_E0 + s) * G + g], 1);
+      atomicAdd(&W.ev[(int64_t)(EV_TXNEW0 + s) * G + g], 1);
+      atomicAdd((unsigned long long*)&W.uniq[g], 1ULL);
+      if (w) {
+        atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
+        atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
+        atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
+      }
+    }
+    if (!grid_sync(W)) return;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Results rows of the tick and the tick advance. */
+__global__ void k_end(DevWorld W) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= W.G) return;
+  DevRep* rp = &W.reps[W.node_rep[g]];
+  if (!rp->active) return;
+  const int i = g - rp->node_base, n = rp->n_nodes, ns = rp->ns, t = rp->cur_t, G = W.G;
+  const int32_t* ev = W.ev;
+#define EVv(k) ev[(int64_t)(k) * G + g]
+#define TTv(k) W.tot[(int64_t)(k) * G + g]
+  if (rp->comps & LPG_COMP_TX) {
+    int32_t e = 0, in = 0;
+    for (int k = 0; k < ns; ++k) {
+      int32_t ek = TTv(TT_E0 + k), ik = TTv(TT_I0 + k);
+      RES(rp, RS_EBS, t)[i * ns + k] = ek;
+      RES(rp, RS_IBS, t)[i * ns + k] = ik;
+      e += ek;
+      in += ik;
+    }
+    RES(rp, RS_S, t)[i] = TTv(TT_S);
+    RES(rp, RS_E, t)[i] = e;
+    RES(rp, RS_I, t)[i] = in;
+    RES(rp, RS_R, t)[i] += TTv(TT_R);
+    RES(rp, RS_POTP, t)[i] = TTv(TT_POTP);
+    RES(rp, RS_P, t)[i] = TTv(TT_P);
+  }
+  if (t >= 1) {
+    if (rp->comps & LPG_COMP_DS) {
+      RES(rp, RS_NEWPOTP, t)[i] = EVv(EV_NEWPOT);
+      RES(rp, RS_NEWP, t)[i] = EVv(EV_NEWPAR);
+    }
+    if (rp->vd_tick) {
+      RES(rp, RS_DEATHS, t)[i] = EVv(EV_DEATHS);
+      if (rp->nb_total > 0) RES(rp, RS_BIRTHS, t)[i] = EVv(EV_BIRTHS);
+    }
+    int32_t ne = 0;
+    int32_t nebs[LPG_MAX_STRAINS] = {0, 0, 0, 0};
+    if (rp->ri_tick) {
+      int32_t prot = EVv(EV_RIPROT);
+      RES(rp, RS_RIVAC, t)[i] = EVv(EV_RIVAC);
+      RES(rp, RS_RIPROT, t)[i] = prot;
+      RES(rp, RS_RINEWEXPBS, t)[i * ns + rp->ri_strain] = prot;
+      RES(rp, RS_IPVVAC, t)[i] = EVv(EV_IPVVAC);
+      ne += prot;
+      nebs[rp->ri_strain] += prot;
+    }
+    for (int k = 0; k < rp->sia_n; ++k) {
+      const DevSia& sv = rp->sia[rp->sia_i0 + k];
+      int32_t vac = EVv(EV_SIAVAC0 + k), prot = EVv(EV_SIAPROT0 + k);
+      RES(rp, RS_SIAVAC, t)[i] = vac;
+      RES(rp, RS_SIAPROT, t)[i] = prot;
+      RES(rp, RS_SIANEWEXPBS, t)[i * ns + sv.strain] += prot;
+      ne += prot;
+      nebs[sv.strain] += prot;
+    }
+    if (rp->comps & LPG_COMP_TX) {
+      for (int k = 0; k < ns; ++k) {
+        int32_t v = EVv(EV_TXNEW0 + k);
+        ne += v;
+        nebs[k] += v;
+      }
+    }
+    RES(rp, RS_NEWEXP, t)[i] += ne;
+    for (int k = 0; k < ns; ++k) RES(rp, RS_NEWEXPBS, t)[i * ns + k] += nebs[k];
+  }
+#undef EVv
+#undef TTv
+  if (i == 0) {
+    rp->t = t + 1;
+    if (rp->stop_at == t) rp->stopped = 1;
+  }
+  (void)n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Full recount of the running totals and selection weights (tick 0 and the
+ * invariant check).  One CTA per chunk. */
+__global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_count(DevWorld W, int32_t* tot_out, uint64_t* sw_out,
+                                                             uint64_t* bb_out, uint64_t* chunk_w_out,
+                                                             uint64_t* sub_w_out) {
+  __shared__ int32_t s_tot[TT_N];
+  __shared__ unsigned long long s_sw, s_bb[LPG_MAX_STRAINS], s_sub[LPG_NSUB];
+  for (int r = 0; r < W.n_reps; ++r) {
+    const DevRep* rp = &W.reps[r];
+    for (int32_t lc = blockIdx.x; lc < rp->used_chunks; lc += gridDim.x) {
+      const int64_t cid = rp->chunk_base + lc;
+      const int g = W.chunk_node[cid];
+      if (threadIdx.x < TT_N) s_tot[threadIdx.x] = 0;
+      if (threadIdx.x < LPG_NSUB) s_sub[threadIdx.x] = 0;
+      if (threadIdx.x < LPG_MAX_STRAINS) s_bb[threadIdx.x] = 0;
+      if (threadIdx.x == 0) s_sw = 0;
+      __syncthreads();
+      const int fill = W.chunk_fill[cid];
+      for (int o = threadIdx.x; o < fill; o += blockDim.x) {
+        const int64_t pos = cid * LPG_CHUNK + o;
+        const int8_t s = W.ds[pos];
+        if (s < 0) continue;
+        const int st = W.strain[pos];
+        if (s == 0) {
+          atomicAdd(&s_tot[TT_S], 1);
+          uint64_t w = fix_risk(W.risk[pos]);
+          if (w) {
+            atomicAdd(&s_sw, (unsigned long long)w);
+            atomicAdd(&s_sub[o / LPG_SUB], (unsigned long long)w);
+          }
+        } else if (s == 1) {
+          atomicAdd(&s_tot[TT_E0 + st], 1);
+        } else if (s == 2) {
+          atomicAdd(&s_tot[TT_I0 + st], 1);
+          uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd(&s_bb[st], (unsigned long long)bw);
+        } else if (s == 3) {
+          atomicAdd(&s_tot[TT_R], 1);
+        }
+        if (W.pp[pos] == 1) atomicAdd(&s_tot[TT_POTP], 1);
+        if (W.par[pos] == 1) atomicAdd(&s_tot[TT_P], 1);
+      }
+      __syncthreads();
+      if (threadIdx.x < TT_N && s_tot[threadIdx.x]) atomicAdd(&tot_out[(int64_t)threadIdx.x * W.G + g], s_tot[threadIdx.x]);
+      if (threadIdx.x < LPG_MAX_STRAINS && s_bb[threadIdx.x])
+        atomicAdd((unsigned long long*)&bb_out[(int64_t)threadIdx.x * W.G + g], s_bb[threadIdx.x]);
+      if (threadIdx.x < LPG_NSUB) sub_w_out[cid * LPG_NSUB + threadIdx.x] = s_sub[threadIdx.x];
+      if (threadIdx.x == 0) {
+        if (s_sw) atomicAdd((unsigned long long*)&sw_out[g], s_sw);
+        chunk_w_out[cid] = s_sw;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+#endif

@@ -1,0 +1,286 @@
+/*
+ * lpg_rng.h — the counter-based draw hook shared by the CUDA engine and the
+ * CPU oracle.
+ *
+ * The reference draws from numba's per-thread np.random state
+ * (laser_polio/model.py:446, :1712-1716, :1848, :1852, :2047, :1096,
+ * :1130, :1388-1405), which cannot be replayed on another machine or thread
+ * count.  Here every random number is a pure function of
+ *     (seed, purpose, tick, a, b, k)
+ * evaluated with Philox4x64-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
+ * numbers: as easy as 1, 2, 3", SC'11).  a/b identify the agent slot (in the
+ * reference's slot order) or the node, k is the position in that stream.
+ * Any thread, in any order, on either machine gets the same value, so the
+ * GPU and the oracle agree on every draw without sharing state.
+ *
+ * Samplers built on it (all published methods):
+ *   Poisson   inversion by sequential search for lam < 10; PTRS transformed
+ *             rejection (W. Hormann, "The transformed rejection method for
+ *             generating Poisson random variables", Insurance: Mathematics
+ *             and Economics 12, 1993) for lam >= 10.
+ *   normal    Marsaglia polar method.
+ *   gamma     Marsaglia & Tsang (ACM TOMS 26(3), 2000) for shape >= 1,
+ *             boosted by U^(1/a) for shape < 1.
+ *   neg. binomial  Poisson(Gamma(r, (1-p)/p)) — the gamma–Poisson mixture
+ *             numpy's negative_binomial uses.
+ * Rejection loops are bounded; the bound is never reached in practice and a
+ * deterministic fallback keeps both sides identical if it were.
+ */
+#ifndef LPG_RNG_H
+#define LPG_RNG_H
+
+#include "lpg_detmath.h"
+
+/* Purposes: the first counter word's high half. */
+enum {
+  LPG_P_PARALYSIS = 1,  /* a = slot                       */
+  LPG_P_RI = 2,         /* a = slot, k=0 OPV, k=1 IPV     */
+  LPG_P_SIA = 3,        /* a = slot, k = event of the day */
+  LPG_P_BIRTH = 4,      /* a = node                       */
+  LPG_P_KM = 5,         /* a = slot, k = 0,1,...          */
+  LPG_P_TXCOUNT = 6,    /* a = node, k = 0,1,...          */
+  LPG_P_SELECT = 7,     /* a = node, b = round, k = draw  */
+  LPG_P_STRAIN = 8,     /* a = slot                       */
+  LPG_P_SEEDPICK = 9,   /* a = slot, b = seed event       */
+  LPG_P_SEEDTIMER = 10  /* a = slot, b = seed event, k    */
+};
+
+#define LPG_PHILOX_M0 0xD2E7470EE14C6C93ULL
+#define LPG_PHILOX_M1 0xCA5A826395121157ULL
+#define LPG_PHILOX_W0 0x9E3779B97F4A7C15ULL
+#define LPG_PHILOX_W1 0xBB67AE8584CAA73BULL
+/* Second key word: a fixed tag so that streams of this project do not
+ * coincide with a plain Philox(seed) stream. */
+#define LPG_KEY_TAG 0x6C617365722D706FULL
+
+LPG_HD uint64_t lpg_mulhilo64(uint64_t a, uint64_t b, uint64_t* hi) {
+#if defined(__CUDA_ARCH__)
+  *hi = __umul64hi(a, b);
+  return a * b;
+#else
+  unsigned __int128 p = (unsigned __int128)a * (unsigned __int128)b;
+  *hi = (uint64_t)(p >> 64);
+  return (uint64_t)p;
+#endif
+}
+
+/* Philox4x64 with 10 rounds; ctr is replaced by the output block. */
+LPG_HD void lpg_philox4x64_10(uint64_t ctr[4], uint64_t k0, uint64_t k1) {
+  uint64_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int r = 0; r < 10; ++r) {
+    uint64_t hi0, hi1;
+    uint64_t lo0 = lpg_mulhilo64(LPG_PHILOX_M0, c0, &hi0);
+    uint64_t lo1 = lpg_mulhilo64(LPG_PHILOX_M1, c2, &hi1);
+    uint64_t n0 = hi1 ^ c1 ^ k0;
+    uint64_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += LPG_PHILOX_W0;
+    k1 += LPG_PHILOX_W1;
+  }
+  ctr[0] = c0;
+  ctr[1] = c1;
+  ctr[2] = c2;
+  ctr[3] = c3;
+}
+
+/* Raw 64-bit word k of stream (seed, purpose, tick, a, b). */
+LPG_HD uint64_t lpg_raw(uint64_t seed, uint32_t purpose, int32_t tick, uint64_t a, uint64_t b, uint64_t k) {
+  uint64_t c[4];
+  c[0] = a;
+  c[1] = b;
+  c[2] = ((uint64_t)purpose << 32) | (uint64_t)(uint32_t)tick;
+  c[3] = k >> 2;
+  lpg_philox4x64_10(c, seed, LPG_KEY_TAG);
+  return c[k & 3];
+}
+
+/* 53-bit integer and the matching uniform on [0, 1). */
+LPG_HD uint64_t lpg_u53(uint64_t seed, uint32_t purpose, int32_t tick, uint64_t a, uint64_t b, uint64_t k) {
+  return lpg_raw(seed, purpose, tick, a, b, k) >> 11;
+}
+
+LPG_HD double lpg_u01(uint64_t seed, uint32_t purpose, int32_t tick, uint64_t a, uint64_t b, uint64_t k) {
+  return (double)lpg_u53(seed, purpose, tick, a, b, k) * 0x1.0p-53;
+}
+
+/* floor(m * T / 2^53) for a 53-bit m: the CDF target of a uniform draw
+ * scaled to an integer total weight T (exact, 128-bit product). */
+LPG_HD uint64_t lpg_scale_target(uint64_t m53, uint64_t total) {
+  uint64_t hi;
+  uint64_t lo = lpg_mulhilo64(m53, total, &hi);
+  return (hi << 11) | (lo >> 53);
+}
+
+/* A sequential stream: draws k = 0, 1, 2, ... of one (purpose, tick, a, b). */
+typedef struct {
+  uint64_t seed, a, b;
+  uint32_t purpose;
+  int32_t tick;
+  uint64_t k;
+  uint64_t blk[4];
+  uint64_t blk_id;
+} lpg_stream;
+
+LPG_HD void lpg_stream_init(lpg_stream* s, uint64_t seed, uint32_t purpose, int32_t tick, uint64_t a, uint64_t b) {
+  s->seed = seed;
+  s->purpose = purpose;
+  s->tick = tick;
+  s->a = a;
+  s->b = b;
+  s->k = 0;
+  s->blk_id = ~(uint64_t)0;
+}
+
+LPG_HD double lpg_next(lpg_stream* s) {
+  uint64_t id = s->k >> 2;
+  if (id != s->blk_id) {
+    s->blk[0] = s->a;
+    s->blk[1] = s->b;
+    s->blk[2] = ((uint64_t)s->purpose << 32) | (uint64_t)(uint32_t)s->tick;
+    s->blk[3] = id;
+    lpg_philox4x64_10(s->blk, s->seed, LPG_KEY_TAG);
+    s->blk_id = id;
+  }
+  uint64_t w = s->blk[s->k & 3];
+  s->k += 1;
+  return (double)(w >> 11) * 0x1.0p-53;
+}
+
+#define LPG_MAX_REJECT 1000
+
+/* Standard normal, Marsaglia polar method. */
+LPG_HD double lpg_std_normal(lpg_stream* s) {
+  for (int it = 0; it < LPG_MAX_REJECT; ++it) {
+    double u = 2.0 * lpg_next(s) - 1.0;
+    double v = 2.0 * lpg_next(s) - 1.0;
+    double q = u * u + v * v;
+    if (q >= 1.0 || q == 0.0) continue;
+    return u * sqrt(-2.0 * lpg_log(q) / q);
+  }
+  return 0.0;
+}
+
+/* Gamma(shape a, scale 1). */
+LPG_HD double lpg_std_gamma(lpg_stream* s, double a) {
+  if (!(a > 0.0)) return 0.0;
+  double boost = 1.0;
+  if (a < 1.0) {
+    double u = lpg_next(s);
+    boost = lpg_exp(lpg_log(u) / a);
+    a = a + 1.0;
+  }
+  double d = a - 1.0 / 3.0;
+  double c = 1.0 / sqrt(9.0 * d);
+  for (int it = 0; it < LPG_MAX_REJECT; ++it) {
+    double x = lpg_std_normal(s);
+    double v = 1.0 + c * x;
+    if (v <= 0.0) continue;
+    v = v * v * v;
+    double u = lpg_next(s);
+    double x2 = x * x;
+    if (u < 1.0 - 0.0331 * (x2 * x2)) return d * v * boost;
+    if (lpg_log(u) < 0.5 * x2 + d * (1.0 - v + lpg_log(v))) return d * v * boost;
+  }
+  return d * boost;
+}
+
+/* Poisson(lam). */
+LPG_HD int64_t lpg_poisson(lpg_stream* s, double lam) {
+  if (!(lam > 0.0)) return 0;
+  if (lam < 10.0) {
+    double p = lpg_exp(-lam);
+    double f = p;
+    double u = lpg_next(s);
+    int64_t x = 0;
+    while (u > f && x < 1000) {
+      x += 1;
+      p = p * lam / (double)x;
+      f = f + p;
+    }
+    return x;
+  }
+  double slam = sqrt(lam);
+  double loglam = lpg_log(lam);
+  double b = 0.931 + 2.53 * slam;
+  double a = -0.059 + 0.02483 * b;
+  double invalpha = 1.1239 + 1.1328 / (b - 3.4);
+  double vr = 0.9277 - 3.6224 / (b - 2.0);
+  for (int it = 0; it < LPG_MAX_REJECT; ++it) {
+    double u = lpg_next(s) - 0.5;
+    double v = lpg_next(s);
+    double us = 0.5 - fabs(u);
+    double kd = floor((2.0 * a / us + b) * u + lam + 0.43);
+    if (us >= 0.07 && v <= vr) return (int64_t)kd;
+    if (kd < 0.0 || (us < 0.013 && v > us)) continue;
+    double lhs = lpg_log(v) + lpg_log(invalpha) - lpg_log(a / (us * us) + b);
+    double rhs = -lam + kd * loglam - lpg_lfact((int64_t)kd);
+    if (lhs <= rhs) return (int64_t)kd;
+  }
+  return (int64_t)floor(lam);
+}
+
+/* Negative binomial (number of failures before r successes, success
+ * probability p), as the gamma–Poisson mixture. */
+LPG_HD int64_t lpg_negbinom(lpg_stream* s, double r, double p) {
+  double y = lpg_std_gamma(s, r) * ((1.0 - p) / p);
+  return lpg_poisson(s, y);
+}
+
+/* Distribution kinds, mirroring laser_polio/distributions.py:17-102. */
+enum {
+  LPG_DIST_CONSTANT = 0,
+  LPG_DIST_EXPONENTIAL = 1,
+  LPG_DIST_GAMMA = 2,
+  LPG_DIST_LOGNORMAL = 3,   /* p1 = mean, p2 = sigma of the lognormal itself */
+  LPG_DIST_NORMAL = 4,
+  LPG_DIST_POISSON = 5,
+  LPG_DIST_UNIFORM = 6,     /* integer in [p1, p2) */
+  LPG_DIST_LOGNORMAL_INT = 7
+};
+
+LPG_HD double lpg_dist_sample(lpg_stream* s, int kind, double p1, double p2) {
+  switch (kind) {
+    case LPG_DIST_CONSTANT:
+      return p1;
+    case LPG_DIST_EXPONENTIAL:
+      return -p1 * lpg_log(1.0 - lpg_next(s));
+    case LPG_DIST_GAMMA:
+      return lpg_std_gamma(s, p1) * p2;
+    case LPG_DIST_LOGNORMAL:
+    case LPG_DIST_LOGNORMAL_INT: {
+      if (!(p1 > 0.0)) return 0.0;
+      double mu = lpg_log(p1 * p1 / sqrt(p2 * p2 + p1 * p1));
+      double sg = sqrt(lpg_log(p2 * p2 / (p1 * p1) + 1.0));
+      double v = lpg_exp(mu + sg * lpg_std_normal(s));
+      if (kind == LPG_DIST_LOGNORMAL_INT) v = floor(v + 0.5);
+      return v;
+    }
+    case LPG_DIST_NORMAL:
+      return p1 + p2 * lpg_std_normal(s);
+    case LPG_DIST_POISSON:
+      return (double)lpg_poisson(s, p1);
+    case LPG_DIST_UNIFORM: {
+      double span = p2 - p1;
+      return p1 + floor(lpg_next(s) * span);
+    }
+    default:
+      return 0.0;
+  }
+}
+
+/* Store a float draw into an int8 column the way numpy's unsafe cast does
+ * on both of this project's hosts: truncate toward zero, keep the low byte. */
+LPG_HD int8_t lpg_trunc_i8(double v) {
+  if (v != v) return 0;
+  if (v > 9.2e18 || v < -9.2e18) return 0;
+  int64_t w = (int64_t)v;
+  return (int8_t)(uint8_t)(uint64_t)w;
+}
+
+#endif /* LPG_RNG_H */

@@ -1,0 +1,148 @@
+"""ctypes wrapper of the C oracle (lpg_oracle.c).
+
+Test infrastructure (see oracle/__init__.py).  It takes exactly the same
+lpg_sim_desc / lpg_columns / lpg_results_view structures as the CUDA engine,
+so a test can hand one simulation description to both and compare.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from laser_polio_gb300 import _abi
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        L.lpo_create.restype = C.c_void_p
+        L.lpo_create.argtypes = [C.POINTER(_abi.lpg_sim_desc)]
+        L.lpo_destroy.argtypes = [C.c_void_p]
+        L.lpo_bind_columns.argtypes = [C.c_void_p, C.POINTER(_abi.lpg_columns)]
+        L.lpo_read_columns.argtypes = [C.c_void_p, C.POINTER(_abi.lpg_columns)]
+        L.lpo_read_results.argtypes = [C.c_void_p, C.POINTER(_abi.lpg_results_view)]
+        L.lpo_get_state.argtypes = [C.c_void_p, C.POINTER(_abi.lpg_sim_state)]
+        L.lpo_start.argtypes = [C.c_void_p]
+        L.lpo_step.argtypes = [C.c_void_p, C.c_int32]
+        L.lpo_last_error.restype = C.c_char_p
+        L.lpo_last_error.argtypes = [C.c_void_p]
+        L.lpo_philox.argtypes = [C.POINTER(C.c_uint64), C.c_uint64, C.c_uint64]
+        for name in ("lpo_exp", "lpo_expm1", "lpo_mlog"):
+            getattr(L, name).restype = C.c_double
+            getattr(L, name).argtypes = [C.c_double]
+        L.lpo_lfact.restype = C.c_double
+        L.lpo_lfact.argtypes = [C.c_int64]
+        L.lpo_poisson_many.argtypes = [C.c_uint64, C.c_double, C.c_int64, C.POINTER(C.c_int64)]
+        L.lpo_gamma_many.argtypes = [C.c_uint64, C.c_double, C.c_int64, C.POINTER(C.c_double)]
+        L.lpo_negbinom_many.argtypes = [C.c_uint64, C.c_double, C.c_double, C.c_int64, C.POINTER(C.c_int64)]
+        L.lpo_dist_many.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_double, C.c_int64, C.POINTER(C.c_double)]
+        L.lpo_km_newborn.restype = C.c_int32
+        L.lpo_km_newborn.argtypes = [C.POINTER(C.c_int64), C.c_int32, C.c_int32, C.c_uint64, C.c_int32, C.c_uint64]
+        L.lpo_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+class OracleSim:
+    """One simulation run by the CPU oracle, driven like the engine handle."""
+
+    def __init__(self, desc: _abi.lpg_sim_desc, keepalive=None):
+        self._keep = keepalive
+        self.desc = desc
+        self.h = lib().lpo_create(C.byref(desc))
+
+    def bind_columns(self, cols: dict):
+        lib().lpo_bind_columns(self.h, C.byref(_abi.make_columns(cols)))
+
+    def start(self):
+        lib().lpo_start(self.h)
+
+    def step(self, n_ticks: int):
+        rc = lib().lpo_step(self.h, int(n_ticks))
+        if rc != 0:
+            raise RuntimeError(f"oracle: {_abi.STATUS_NAMES.get(rc, rc)}: {lib().lpo_last_error(self.h).decode()}")
+
+    def state(self) -> _abi.lpg_sim_state:
+        st = _abi.lpg_sim_state()
+        lib().lpo_get_state(self.h, C.byref(st))
+        return st
+
+    def read_results(self, res: dict):
+        lib().lpo_read_results(self.h, C.byref(_abi.make_results_view(res)))
+
+    def read_columns(self, cols: dict):
+        lib().lpo_read_columns(self.h, C.byref(_abi.make_columns(cols)))
+
+    def close(self):
+        if self.h:
+            lib().lpo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def philox(ctr, key):
+    c = (C.c_uint64 * 4)(*[int(x) for x in ctr])
+    lib().lpo_philox(c, int(key[0]), int(key[1]))
+    return [int(x) for x in c]
+
+
+def det_exp(x):
+    return lib().lpo_exp(float(x))
+
+
+def det_expm1(x):
+    return lib().lpo_expm1(float(x))
+
+
+def det_log(x):
+    return lib().lpo_mlog(float(x))
+
+
+def det_lfact(k):
+    return lib().lpo_lfact(int(k))
+
+
+def poisson_many(seed, lam, n):
+    out = np.zeros(n, np.int64)
+    lib().lpo_poisson_many(seed, lam, n, out.ctypes.data_as(C.POINTER(C.c_int64)))
+    return out
+
+
+def gamma_many(seed, shape, n):
+    out = np.zeros(n, np.float64)
+    lib().lpo_gamma_many(seed, shape, n, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def negbinom_many(seed, r, p, n):
+    out = np.zeros(n, np.int64)
+    lib().lpo_negbinom_many(seed, r, p, n, out.ctypes.data_as(C.POINTER(C.c_int64)))
+    return out
+
+
+def dist_many(seed, kind, p1, p2, n):
+    out = np.zeros(n, np.float64)
+    lib().lpo_dist_many(seed, kind, p1, p2, n, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def km_newborn(cum, max_year, seed, t, slot):
+    cum = np.ascontiguousarray(cum, dtype=np.int64)
+    return lib().lpo_km_newborn(cum.ctypes.data_as(C.POINTER(C.c_int64)), len(cum), max_year, seed, t, slot)
+
+
+def num_threads():
+    return lib().lpo_num_threads()

@@ -1,0 +1,81 @@
+"""Run an SEIR_ABM built with laser_polio_gb300 on the CPU oracle.
+
+Test-only: it hands the same C-ABI description the engine would get
+(engine.build_sim_spec) to the oracle and copies the outcome back into the
+sim's host arrays, exactly where the engine's finish step would put it.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from laser_polio_gb300.engine import build_sim_spec
+from oracle.oracle import OracleSim
+
+
+def run_with_oracle(sim, n_ticks=None):
+    spec = build_sim_spec(sim)
+    o = OracleSim(spec.desc, keepalive=spec)
+    o.bind_columns(spec.columns)
+    o.start()
+    o.step(sim.nt - 1 if n_ticks is None else n_ticks)
+    st = o.state()
+    o.read_results(spec.results)
+    o.read_columns(spec.columns)
+    sim.people._set_count(st.count)
+    sim.t = st.t
+    sim.should_stop = bool(st.stopped)
+    o.close()
+    return sim
+
+
+def snapshot(sim):
+    """Copies of the spec's columns and results (for parity comparisons)."""
+    spec = build_sim_spec(sim)
+    cols = {k: v.copy() for k, v in spec.columns.items()}
+    res = {k: v.copy() for k, v in spec.results.items()}
+    return spec, cols, res
+
+
+def run_spec_oracle(spec, cols, res, n_ticks):
+    o = OracleSim(spec.desc, keepalive=spec)
+    o.bind_columns(cols)
+    o.start()
+    o.step(n_ticks)
+    st = o.state()
+    o.read_results(res)
+    o.read_columns(cols)
+    o.close()
+    return st
+
+
+def run_spec_gpu(spec, cols, res, n_ticks, graphs=True, check=False):
+    from laser_polio_gb300._lib import Handle
+
+    h = Handle([spec.desc])
+    h.set_graphs(graphs)
+    h.bind_columns(0, cols)
+    h.start()
+    if check:
+        for _ in range(n_ticks):
+            h.step(1)
+            h.check_invariants()
+    else:
+        h.step(n_ticks)
+    h.sync()
+    st = h.state(0)
+    h.read_results(0, res)
+    h.read_columns(0, cols)
+    h.close()
+    return st
+
+
+def assert_same(a: dict, b: dict, what: str, count=None):
+    for k in a:
+        x, y = a[k], b[k]
+        if count is not None and x.ndim == 1:
+            x, y = x[:count], y[:count]
+        if not np.array_equal(x, y):
+            idx = np.argwhere(x != y)
+            raise AssertionError(f"{what} '{k}' differs at {len(idx)} entries, first {idx[:5].tolist()}: "
+                                 f"{x[tuple(idx[0])]} vs {y[tuple(idx[0])]}")

@@ -1,0 +1,437 @@
+"""Known-answer tests of the reference, restated against this package.
+
+Each test builds the scenario of a reference test (file:line in its
+docstring) with the same pars and components, runs it on a backend, and
+asserts what the reference asserts.  Backends: the CPU oracle (always) and
+the CUDA engine (``-m gpu``).  These pin the oracle's semantics to the
+reference's own expectations; tests/test_parity_gpu.py then pins the engine
+to the oracle bit for bit.
+
+Two reference tests depend on which random numbers their seed happens to
+draw (an exposure on day 1 from a Poisson(~1) draw; no death among a few
+agents in two weeks).  The draw hook here is not numba's generator, so those
+tests fix a seed that gives the same situation for this draw hook; their
+expected vectors are unchanged.
+"""
+
+import numpy as np
+import pytest
+
+import laser_polio_gb300 as lp
+from laser_polio_gb300.core import PropertySet
+from oracle_backend import run_with_oracle
+
+BACKENDS = ["oracle", pytest.param("gpu", marks=pytest.mark.gpu)]
+
+
+def run(sim, backend):
+    if backend == "oracle":
+        return run_with_oracle(sim)
+    sim.run()
+    return sim
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_progression_without_transmission(backend):
+    """tests/test_diseasestate_abm.py:64-122: constant timers 1/1, everyone E."""
+    base = {
+        "start_date": lp.date("2020-01-01"),
+        "init_pop": np.array([1000, 500]),
+        "cbr": np.array([30, 25]),
+        "r0_scalars": np.array([0.5, 2.0]),
+        "init_immun": 0.0,
+        "init_prev": 0.0,
+        "dur_exp": lp.constant(value=1),
+        "dur_inf": lp.constant(value=1),
+        "p_paralysis": 1 / 2000,
+        "stop_if_no_cases": False,
+        "seed": 7,
+    }
+    expect = {1: (0, 1500, 0, 0), 2: (0, 0, 1500, 0), 3: (0, 0, 0, 1500)}
+    for dur, (ns, ne, ni, nr) in expect.items():
+        sim = lp.SEIR_ABM(PropertySet({**base, "dur": dur}))
+        sim.components = [lp.DiseaseState_ABM]
+        init_pop = 1500
+        assert np.all(sim.people.exposure_timer[:init_pop] == 1)
+        assert np.all(sim.people.infection_timer[:init_pop] == 1)
+        sim.people.disease_state[:init_pop] = 1
+        run(sim, backend)
+        ds = sim.people.disease_state
+        assert np.sum(ds == 0) == ns
+        assert np.sum(ds == 1) == ne
+        assert np.sum(ds == 2) == ni
+        assert np.sum(ds == 3) == nr
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_disease_timers_with_trans_explicit(backend):
+    """tests/test_diseasestate_abm.py:258-351: 2 agents, r0=999, timers 2/3/10,
+    exact S/E/I/R and new-potentially-paralyzed series for 31 ticks."""
+    dur_exp, dur_inf, t_to_paralysis = 2, 3, 10
+    pars = PropertySet(
+        {
+            "start_date": lp.date("2018-01-01"),
+            "dur": 30,
+            "init_pop": np.array([1, 1]),
+            "cbr": np.array([0, 0]),
+            "r0_scalars": np.array([1.0, 1.0]),
+            "init_immun": 0.0,
+            "init_prev": 1,
+            "dur_exp": lp.constant(value=dur_exp),
+            "dur_inf": lp.constant(value=dur_inf),
+            "t_to_paralysis": lp.constant(value=t_to_paralysis),
+            "p_paralysis": 1 / 2000,
+            "r0": 999,
+            "distances": np.array([[0, 1], [1, 0]]),
+            "stop_if_no_cases": False,
+            "individual_heterogeneity": False,
+            "seed": 131,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.DiseaseState_ABM, lp.Transmission_ABM, lp.VitalDynamics_ABM]
+    ds = sim.people.disease_state[: sim.people.count]
+    assert (np.sum(ds == 0), np.sum(ds == 1), np.sum(ds == 2), np.sum(ds == 3)) == (1, 0, 1, 0)
+    assert np.all(sim.people.exposure_timer == dur_exp)
+    assert np.all(sim.people.infection_timer == dur_inf)
+    assert np.all(sim.people.paralysis_timer >= sim.people.exposure_timer)
+    assert np.all(sim.people.paralysis_timer <= sim.people.infection_timer)
+    run(sim, backend)
+    n_s = sim.results.S.sum(axis=1)
+    n_e = sim.results.E.sum(axis=1)
+    n_i = sim.results.I.sum(axis=1)
+    n_r = sim.results.R.sum(axis=1)
+    n_npp = sim.results.new_potentially_paralyzed.sum(axis=1)
+    z = np.zeros(sim.pars.dur + 1, dtype=int)
+    s_exp, e_exp, i_exp, r_exp, p_exp = z.copy(), z.copy(), z.copy(), z.copy(), z.copy()
+    s_exp[0] = 1
+    e_exp[1 : 2 + dur_exp] = 1
+    i_exp[0 : dur_inf + 1] += 1
+    i_exp[2 + dur_exp : 2 + dur_exp + dur_inf] += 1
+    r_exp[1 + dur_inf :] += 1
+    r_exp[2 + dur_exp + dur_inf :] += 1
+    p_exp[1 + dur_inf] += 1
+    p_exp[2 + dur_exp + dur_inf] += 1
+    assert np.array_equal(n_s, s_exp)
+    assert np.array_equal(n_e, e_exp)
+    assert np.array_equal(n_i, i_exp)
+    assert np.array_equal(n_r, r_exp)
+    assert np.array_equal(n_npp, p_exp)
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_paralysis_progression_manual(backend):
+    """tests/test_diseasestate_abm.py:497-541: p_paralysis=1, IPV on half."""
+    pars = PropertySet(
+        {
+            "start_date": lp.date("2020-01-01"),
+            "dur": 3,
+            "init_pop": np.array([4, 4]),
+            "cbr": np.array([0]),
+            "r0_scalars": np.array([0.0]),
+            "init_immun": 0.0,
+            "init_prev": 0.0,
+            "dur_exp": lp.constant(value=1),
+            "dur_inf": lp.constant(value=1),
+            "p_paralysis": 1.0,
+            "stop_if_no_cases": False,
+            "seed": 3,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.DiseaseState_ABM, lp.Transmission_ABM]
+    sim.people.disease_state[:] = np.array([0, 0, 1, 1, 2, 2, 3, 3])
+    sim.people.paralysis_timer[:] = 1
+    protected = np.array([1, 3, 5, 7])
+    unprotected = np.setdiff1d(np.arange(sim.people.count), protected)
+    sim.people.ipv_protected[:] = 0
+    sim.people.ipv_protected[protected] = 1
+    run(sim, backend)
+    assert np.sum(sim.people.potentially_paralyzed[protected] <= 0) == 4
+    assert np.sum(sim.people.potentially_paralyzed[unprotected] > 0) == 2
+    assert np.sum(sim.people.paralyzed[protected] <= 0) == 4
+    assert np.sum(sim.people.paralyzed[unprotected] > 0) == 2
+    assert np.sum(sim.results.potentially_paralyzed[-1]) == 2
+    assert np.sum(sim.results.paralyzed[-1]) == 2
+
+
+def _interventions_sim(dur=30, init_pop=None, vx_prob_ri=0.5, vx_prob_ipv=0.75, cbr=None, r0=14, new_pars=None, seed=123):
+    """tests/test_interventions.py:8-35 (setup_sim)."""
+    init_pop = np.array([50000, 50000]) if init_pop is None else init_pop
+    cbr = np.array([30, 25]) if cbr is None else cbr
+    pars = PropertySet(
+        {
+            "dur": dur,
+            "init_pop": init_pop,
+            "cbr": cbr,
+            "init_immun": 0.0,
+            "init_prev": 0.0,
+            "r0": r0,
+            "dur_exp": lp.constant(value=2),
+            "dur_inf": lp.constant(value=1),
+            "vx_prob_ri": vx_prob_ri,
+            "vx_prob_ipv": vx_prob_ipv,
+            "stop_if_no_cases": False,
+            "seed": seed,
+            "strain_r0_scalars": {0: 1.0, 1: 0.0, 2: 0.0},
+        }
+    )
+    pars += new_pars if new_pars is not None else {}
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.RI_ABM, lp.SIA_ABM, lp.Transmission_ABM]
+    return sim
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_ri_no_effect_on_non_susceptibles(backend):
+    """tests/test_interventions.py:138-150."""
+    sim = _interventions_sim(init_pop=np.array([10, 10]), r0=0, vx_prob_ri=1.0, seed=124)
+    sim.people.ri_timer[:20] = 0
+    sim.people.disease_state[:5] = 1
+    sim.people.disease_state[5:10] = 2
+    sim.people.disease_state[10:15] = 3
+    run(sim, backend)
+    assert np.sum(sim.results.ri_vaccinated) == 20
+    assert np.sum(sim.results.new_exposed) == 5
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_ri_zero(backend):
+    """tests/test_interventions.py:65-90: no RI once the first cohort ages out;
+    zero probabilities give zero doses."""
+    sim = _interventions_sim(dur=365, cbr=np.array([0, 0]), vx_prob_ri=1.0, vx_prob_ipv=1.0, init_pop=np.array([5000, 5000]))
+    run(sim, backend)
+    assert np.sum(sim.results.ri_vaccinated[98 + 14 :]) == 0
+    assert np.sum(sim.results.ipv_vaccinated[98 + 14 :]) == 0
+    sim = _interventions_sim(dur=365, cbr=np.array([300, 250]), vx_prob_ri=0.0, vx_prob_ipv=0.0, init_pop=np.array([5000, 5000]))
+    run(sim, backend)
+    assert np.sum(sim.results.ri_vaccinated) == 0
+    assert np.sum(sim.results.ipv_vaccinated) == 0
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_sia_schedule(backend):
+    """tests/test_interventions.py:156-195: SIA on its date only, node 0 only,
+    56% of the vaccinated protected with nOPV2."""
+    sia_pars = {
+        "sia_schedule": [{"date": "2019-01-10", "nodes": [0], "age_range": (0, 5 * 365), "vaccinetype": "nOPV2"}],
+        "vx_prob_sia": [0.6, 0.8],
+    }
+    sim = _interventions_sim(vx_prob_ri=0, new_pars=sia_pars)
+    run(sim, backend)
+    n_vx_day10 = np.sum(sim.results.sia_vaccinated[9, :])
+    n_vx_rest = np.sum(sim.results.sia_vaccinated) - n_vx_day10
+    assert n_vx_day10 > 0
+    assert n_vx_rest == 0
+    assert sim.results.sia_vaccinated[9, 1] == 0
+    assert np.isclose(np.sum(sim.results.sia_protected), n_vx_day10 * 0.56, atol=100)
+    alive_in_node = (sim.people.node_id == 0) & (sim.people.disease_state >= 0)
+    age = sim.t - sim.people.date_of_birth[alive_in_node]
+    exp_vx = np.sum(age < 5 * 365) * sim.pars.vx_prob_sia[0]
+    assert np.isclose(n_vx_day10, exp_vx, atol=500)
+    n_exposed = np.sum(sim.results.new_exposed)
+    assert n_exposed > 0
+    assert n_exposed == np.sum(sim.results.sia_protected)
+    exposeds = sim.people.disease_state == 1
+    ages = sim.t - sim.people.date_of_birth[exposeds]
+    assert np.all(ages <= (5 * 365 + 22))
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_chronically_missed(backend):
+    """tests/test_interventions.py:198-223."""
+    sia_pars = {
+        "sia_schedule": [{"date": "2019-01-10", "nodes": [0, 1], "age_range": (0, 5 * 365), "vaccinetype": "perfect"}],
+        "vx_prob_sia": [1.0, 1.0],
+        "missed_frac": 0.2,
+    }
+    sim = _interventions_sim(vx_prob_ri=0, new_pars=sia_pars)
+    run(sim, backend)
+    missed = sim.people.chronically_missed[: sim.people.count]
+    assert np.isclose(np.sum(missed), sim.pars.init_pop.sum() * 0.2, atol=100)
+    eir = np.isin(sim.people.disease_state[: sim.people.count], [1, 2, 3])
+    assert not np.any(eir & missed.astype(bool))
+    age = sim.t - sim.people.date_of_birth[: sim.people.count]
+    exp_vx = np.sum(age < 5 * 365) * (1 - sim.pars.missed_frac)
+    assert np.isclose(np.sum(eir), exp_vx, atol=500)
+
+
+def _vd_sim(step_size=1, cbr=None, init_pop=None):
+    """tests/test_vital_dynamics.py:8-23."""
+    pars = PropertySet(
+        {
+            "start_date": lp.date("2020-01-01"),
+            "dur": 30,
+            "init_pop": np.array([10000, 5000]) if init_pop is None else init_pop,
+            "cbr": np.array([30, 25]) if cbr is None else cbr,
+            "step_size_VitalDynamics_ABM": step_size,
+            "stop_if_no_cases": False,
+            "seed": 11,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.Transmission_ABM]
+    return sim
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_births_generated(backend):
+    """tests/test_vital_dynamics.py:37-61."""
+    sim = _vd_sim(step_size=1)
+    initial = sim.people.count
+    run(sim, backend)
+    assert sim.people.count > initial
+    assert initial + sim.results.births.sum() - sim.results.deaths.sum() == np.sum(sim.people.disease_state > -1)
+    dobs = sim.people.date_of_birth[: sim.people.count]
+    dobs = dobs[dobs >= 0]
+    expected = np.bincount(dobs, minlength=sim.pars.dur + 1)
+    observed = np.sum(sim.results.births, axis=1)
+    expected[1] += expected[0]
+    observed[1] += observed[0]
+    assert np.array_equal(expected[1:], observed[1:])
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+@pytest.mark.parametrize("step_size", [1, 7])
+def test_deaths_occur(backend, step_size):
+    """tests/test_vital_dynamics.py:64-112 (step sizes 1 and 7)."""
+    sim = _vd_sim(step_size=step_size)
+    sim.people.date_of_death[:5] = 1
+    run(sim, backend)
+    assert np.all(sim.people.date_of_death[:5] == 1)
+    assert np.all(sim.people.disease_state[:5] == -1)
+    dods = sim.people.date_of_death[: sim.people.count]
+    expected = np.bincount(dods, minlength=sim.pars.dur + 1)[: sim.pars.dur + 1]
+    observed = np.sum(sim.results.deaths, axis=1)
+    expected[1] += expected[0]
+    observed[1] += observed[0]
+    if step_size == 1:
+        assert np.array_equal(expected[1:], observed[1:])
+    else:
+        expected[0] = observed[0] = 0
+        edges = np.arange(0, sim.pars.dur + 1, 7)
+        bins = np.digitize(np.arange(sim.pars.dur + 1), edges, right=True)
+        eb = np.bincount(bins, weights=expected)[: len(edges) - 1]
+        ob = np.bincount(bins, weights=observed)[: len(edges) - 1]
+        assert np.array_equal(eb, ob)
+    _, counts = np.unique(sim.people.disease_state[: np.sum(sim.pars.init_pop)], return_counts=True)
+    assert counts[0] == np.sum(sim.results.deaths)
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_age_progression_and_zero_birth_rate(backend):
+    """tests/test_vital_dynamics.py:116-146."""
+    sim = _vd_sim()
+    initial_ages = sim.t - sim.people.date_of_birth[: np.sum(sim.pars.init_pop)]
+    run(sim, backend)
+    end_ages = sim.t - sim.people.date_of_birth[: np.sum(sim.pars.init_pop)]
+    assert np.all(end_ages == initial_ages + sim.pars.dur + 1)
+    sim = _vd_sim(cbr=np.array([0, 0]), init_pop=np.array([1000, 500]))
+    initial = sim.people.count
+    run(sim, backend)
+    assert sim.people.count == initial
+
+
+def _strain_sim(dur=30, init_prev=None, vx_prob_sia=None, sia_schedule=None, r0=14, seed=123):
+    """tests/test_strain_transmission.py:10-55."""
+    pars = PropertySet(
+        {
+            "seed": seed,
+            "start_date": lp.date("2019-01-01"),
+            "dur": dur,
+            "init_pop": np.array([10000, 10000]),
+            "cbr": np.array([30, 25]),
+            "init_immun": np.array([0.0, 0.0]),
+            "init_prev": np.array([0.0, 0.0]) if init_prev is None else init_prev,
+            "r0": r0,
+            "r0_scalars": np.array([1.0, 1.0]),
+            "seasonal_amplitude": 0.0,
+            "seasonal_peak_doy": 180,
+            "distances": np.array([[0, 50], [50, 0]]),
+            "gravity_k": 0.5,
+            "max_migr_frac": 0.01,
+            "sia_schedule": sia_schedule,
+            "vx_prob_sia": vx_prob_sia,
+            "vx_prob_ri": None,
+            "stop_if_no_cases": False,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.DiseaseState_ABM, lp.Transmission_ABM, lp.VitalDynamics_ABM, lp.SIA_ABM]
+    return sim
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_strain_separation(backend):
+    """tests/test_strain_transmission.py:86-150 and :250-300: VDPV2 seeding
+    alone gives only strain 0; no seeding gives nothing; SIA in node 1 adds
+    only vaccine strains."""
+    sim = _strain_sim(dur=60, init_prev=np.array([0.01, 0.0]))
+    run(sim, backend)
+    eb, ib = sim.results.E_by_strain, sim.results.I_by_strain
+    assert eb[:, :, 0].sum() > 0 and ib[:, :, 0].sum() > 0
+    assert eb[:, :, 1:].sum() == 0 and ib[:, :, 1:].sum() == 0
+    assert sim.results.E.sum() == eb[:, :, 0].sum()
+
+    sim = _strain_sim(dur=60)
+    run(sim, backend)
+    assert sim.results.E_by_strain.sum() == 0 and sim.results.I_by_strain.sum() == 0
+
+    sia = [{"date": "2019-01-10", "nodes": [1], "age_range": (0, 5 * 365), "vaccinetype": "nOPV2"}]
+    sim = _strain_sim(dur=60, init_prev=np.array([0.01, 0.0]), vx_prob_sia=np.array([0.0, 0.8]), sia_schedule=sia)
+    run(sim, backend)
+    eb, ib = sim.results.E_by_strain, sim.results.I_by_strain
+    assert eb[:, :, 0].sum() > 0 and ib[:, :, 0].sum() > 0
+    assert eb[:, :, 1:].sum() > 0 and ib[:, :, 1:].sum() > 0
+    assert eb.sum() == eb[:, :, 0].sum() + eb[:, :, 1:].sum()
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_zero_transmission(backend):
+    """tests/test_transmission.py:99-113: r0 = 0 gives no new exposures."""
+    pars = PropertySet(
+        {
+            "start_date": lp.date("2020-01-01"),
+            "dur": 30,
+            "init_pop": np.array([10000, 5000]),
+            "cbr": np.array([30, 25]),
+            "init_immun": 0.0,
+            "init_prev": 0.05,
+            "r0": 0,
+            "stop_if_no_cases": False,
+            "seed": 5,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.Transmission_ABM]
+    run(sim, backend)
+    assert np.sum(sim.results.new_exposed) == 0
+
+
+def test_seasonality_reference_cases():
+    """tests/test_seasonality.py:28-126: peaks, amplitude to 1e-10, symmetry."""
+    import datetime as dt
+
+    dates = [dt.date(2024, 1, 1) + dt.timedelta(days=x) for x in range(364)]
+    for amp, peak in [(1.0, 180), (0.5, 90), (0.8, 270), (0.3, 0)]:
+        s = lp.utils.seasonality_table(dates, amp, peak)
+        assert abs(int(np.argmax(s)) - peak) <= 1
+    for amp, peak in [(1.0, 180), (0.5, 90), (0.2, 270)]:
+        s = lp.utils.seasonality_table(dates, amp, peak)
+        assert abs(s.min() - (1 - amp)) < 1e-10
+        assert abs(s.max() - (1 + amp)) < 1e-10
+    s = lp.utils.seasonality_table(dates, 1.0, 180)
+    k = int(np.argmax(s))
+    np.testing.assert_allclose(s[k - 30 : k], s[k : k + 30][::-1], rtol=1e-2)
+    np.testing.assert_allclose(lp.utils.seasonality_table(dates, 0.0, 180), 1.0, rtol=1e-10)
+
+    class MockSim:
+        pars = {"seasonal_amplitude": 0.4, "seasonal_peak_doy": 180}
+        datevec = dates
+        t = 100
+
+    assert lp.get_seasonality(MockSim()) == s_at(dates, 0.4, 180, 100)
+
+
+def s_at(dates, amp, peak, t):
+    return lp.utils.seasonality_table(dates, amp, peak)[t]
