@@ -1,0 +1,415 @@
+"""Benchmark: agent-ticks/s of the per-tick agent step at the Nigeria scale.
+
+Workload (one "step" = one tick of the full agent step: VitalDynamics,
+DiseaseState, RI, SIA and Transmission, with the SEIR log) over a synthetic
+774-node, 2.2e8-agent population (capacity +30%), seeded numpy draws with
+the distributions of the Nigeria-scale configuration.  agent-ticks = sum
+over the timed ticks of people.count (slots scanned, dead included, as the
+reference's loops do).
+
+  value     W untimed ticks, then K ticks timed with CUDA events on the
+            engine's stream, state resident in HBM (the agent table is far
+            larger than L2, so no flush is needed between ticks).
+  e2e       a full run through the C ABI from pinned host columns: upload,
+            layout, K ticks, read back results and columns.
+  roofline  per-kernel CUDA-event times from a second run of the same ticks
+            in profiling mode; the dominant kernel's algorithmic bytes per
+            launch / its mean launch time against the measured HBM peak.
+  cpu_baseline  the C/OpenMP oracle on the machine's cores over the first ticks
+            of the same population.
+
+python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+# survey: compulsory column bytes per agent-tick by tick type
+B_EVERY = 18.0  # state, node, strain, 3 timers, pp, paralyzed, ipv, risk, infectivity
+B_VD = 4.0  # date_of_death on VD ticks
+B_RI = 5.0  # ri_timer read + write, chronically_missed on RI ticks
+B_SIA = 5.0  # date_of_birth, chronically_missed on SIA days
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2548)
+    ap.add_argument("--warmup", type=int, default=7)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--agents", type=float, default=2.2e8)
+    ap.add_argument("--nodes", type=int, default=774)
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--cpu-seconds", type=float, default=25.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--out", default=None)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def tick_bytes(params, t):
+    """Survey's algorithmic bytes per agent for tick t."""
+    b = B_EVERY
+    if t % params["vd_step"] == 0:
+        b += B_VD
+    if params["ri_enabled"] and t % params["ri_step"] == 0:
+        b += B_RI
+    b += B_SIA * sum(1 for e in params["sia"] if e[0] == t)
+    return b
+
+
+def sweep_bytes(params, t):
+    """Columns the fused sweep must read for every agent slot on tick t:
+    the state byte always; date_of_death on VD ticks; chronically_missed and
+    ri_timer (read + write) on RI ticks; chronically_missed and date_of_birth
+    on SIA days.  Timers, strain, flags, risk and infectivity are read only
+    for the agents whose state needs them (sector-granular in practice)."""
+    b = 1.0
+    if t % params["vd_step"] == 0:
+        b += 4.0
+    if params["ri_enabled"] and t % params["ri_step"] == 0:
+        b += 1.0 + 2.0 + 2.0
+    if any(e[0] == t for e in params["sia"]):
+        b += 1.0 + 4.0
+    return b
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[3:7], strict=False):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def counts_per_tick(params, births):
+    """cnt[t] = people.count after tick t's births: the slots tick t scans."""
+    per_tick_births = births.sum(axis=1).astype(np.int64)
+    return params["count"] + np.cumsum(per_tick_births)
+
+
+def make_bundle(args, rank, pinned):
+    from laser_polio_gb300 import synthetic
+
+    alloc = None
+    if pinned:
+        import torch
+
+        def alloc(name, n, dtype):
+            t = torch.empty(n, dtype=getattr(torch, np.dtype(dtype).name), pin_memory=True)
+            return t.numpy()
+
+    return synthetic.bundle("nigeria", n_agents=int(args.agents), n_nodes=args.nodes, seed=args.seed + rank, alloc=alloc)
+
+
+def result_arrays(params):
+    from laser_polio_gb300 import _abi
+
+    nt, n, ns = params["nt"], params["n_nodes"], params["n_strains"]
+    return {name: np.zeros((nt, n, ns) if wide else (nt, n), np.int32) for name, wide in _abi.RESULT_FIELDS}
+
+
+def run_cpu_baseline(params, cols, warmup, steps, seconds):
+    """The oracle over the first ticks of the same population."""
+    from laser_polio_gb300.engine import make_desc
+    from oracle.oracle import OracleSim
+    from oracle.oracle import num_threads
+
+    d, keep = make_desc(params)
+    o = OracleSim(d, keepalive=keep)
+    o.bind_columns(cols)
+    o.start()
+    o.step(warmup)
+    done, agent_ticks = 0, 0
+    t0 = time.perf_counter()
+    while done < steps:
+        o.step(1)
+        done += 1
+        agent_ticks += o.state().count
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": agent_ticks / dt, "ticks": done, "seconds": dt, "cores": num_threads(), "warmup": warmup}
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    params, cols = make_bundle(args, 0, pinned=False)
+    warm = min(args.warmup, 2)
+    cpu = run_cpu_baseline(params, cols, warm, args.steps, args.cpu_seconds)
+    sample = (f"first {cpu['ticks']} ticks after {warm} untimed of the {params['count']:.3g}-agent, "
+              f"{params['n_nodes']}-node population ({cpu['seconds']:.1f} s)")
+    line = {
+        "impl": "reference",
+        "metric": "agent-ticks/s (774 nodes, 2.2e8 agents, full agent step)",
+        "value": cpu["value"],
+        "unit": "agent-ticks/s",
+        "n_gpus": ws,
+        "steps": cpu["ticks"],
+        "warmup": warm,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int8/int32 state, f64 node FOI",
+        "data": "synthetic (seeded numpy, Nigeria-scale shapes)",
+        "config": {"workload": "nigeria_like 774 nodes x 2.2e8 agents, capacity +30%, 2555-tick run",
+                   "agents": params["count"], "nodes": params["n_nodes"]},
+        "cpu_baseline": {"value": cpu["value"], "unit": "agent-ticks/s", "cores": cpu["cores"], "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": cpu["value"], "unit": "agent-ticks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = local
+    from laser_polio_gb300._lib import Handle
+    from laser_polio_gb300.engine import make_desc
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    params, cols = make_bundle(args, rank, pinned=True)
+    desc, keep = make_desc(params)
+    W, K = args.warmup, args.steps
+    nt = params["nt"]
+    if W + K > nt - 1:
+        K = max(1, nt - 1 - W)
+    col_bytes = sum(v.nbytes for v in cols.values())
+
+    # ---- end to end through the C ABI from pinned host columns --------------
+    e2e = None
+    if not args.no_e2e:
+        res = result_arrays(params)
+        out_cols = {k: np.empty_like(v) for k, v in cols.items()}
+        barrier()
+        t0 = time.perf_counter()
+        h = Handle([desc], device=dev)
+        h.bind_columns(0, cols)
+        h.start()
+        h.step(W + K)
+        h.sync()
+        h.read_results(0, res)
+        h.read_columns(0, out_cols)
+        barrier()
+        dt = time.perf_counter() - t0
+        h.close()
+        cnt = counts_per_tick(params, res["births"])
+        at = float(cnt[1 : W + K + 1].sum())
+        res_bytes = sum(v.nbytes for v in res.values())
+        e2e = {"value": at / dt, "unit": "agent-ticks/s", "h2d_bytes_per_step": int(col_bytes // (W + K)),
+               "d2h_bytes_per_step": int((res_bytes + col_bytes) // (W + K)), "seconds": dt, "ticks": W + K}
+        del out_cols
+
+    # ---- device-resident timed region ------------------------------------
+    h = Handle([desc], device=dev)
+    h.bind_columns(0, cols)
+    h.start()
+    h.step(W)
+    h.sync()
+    stream = torch.cuda.ExternalStream(h.cuda_stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    l0 = h.kernel_launches()
+    barrier()
+    with ClockSampler(dev) as clocks:
+        e0.record(stream)
+        h.step(K)
+        e1.record(stream)
+        h.sync()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    launches = h.kernel_launches() - l0
+    res = result_arrays(params)
+    h.read_results(0, res)
+    st = h.state(0)
+    h.close()
+    cnt = counts_per_tick(params, res["births"])
+    ticks = np.arange(W + 1, W + K + 1)
+    agent_ticks = float(cnt[ticks].sum())
+    ms_max = ms
+    at_total = agent_ticks
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+        a = torch.tensor([agent_ticks], device="cuda", dtype=torch.float64)
+        dist.all_reduce(a)
+        at_total = float(a.item())
+    value = at_total / (ms_max / 1e3)
+
+    # ---- per-kernel times (profiling mode, same ticks) --------------------
+    roof = None
+    prof = None
+    if not args.no_profile:
+        h = Handle([desc], device=dev)
+        h.bind_columns(0, cols)
+        h.start()
+        h.step(W)
+        h.sync()
+        h.set_profiling(True)
+        h.step(K)
+        h.sync()
+        prof = h.profile()
+        h.close()
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        which = "measured" if "hbm_gbs" in peaks else "fallback"
+        top = max(prof, key=lambda k: prof[k][0])
+        sweep_ms, sweep_n = prof["k_sweep_a"]
+        alg = sum(tick_bytes(params, t) * cnt[t] for t in ticks) / K
+        kern = sum(sweep_bytes(params, t) * cnt[t] for t in ticks) / K
+        per_launch_ms = sweep_ms / max(1, sweep_n)
+        roof = {
+            "kernel": "k_sweep_a",
+            "bound": "hbm",
+            "achieved": kern / (per_launch_ms / 1e3) / 1e9,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": kern / (per_launch_ms / 1e3) / 1e9 / peak,
+            "traffic": None,
+            "peak_source": which,
+            "alg_bytes_per_launch": kern,
+            "survey_bytes_per_launch": alg,
+            "survey_equiv_gbs": alg / (per_launch_ms / 1e3) / 1e9,
+            "mean_launch_ms": per_launch_ms,
+            "top_kernel": top,
+            "kernel_ms_per_tick": {k: v[0] / max(1, v[1]) for k, v in prof.items()},
+            "kernel_share": {k: v[0] / sum(x[0] for x in prof.values()) for k, v in prof.items()},
+        }
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        del h
+        cpu_res = run_cpu_baseline(params, cols, 0, 1000, args.cpu_seconds)
+        cpu = {"value": cpu_res["value"], "unit": "agent-ticks/s", "cores": cpu_res["cores"], "kind": "port",
+               "sample": f"oracle, first {cpu_res['ticks']} ticks of the same population ({cpu_res['seconds']:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": "agent-ticks/s (774 nodes, 2.2e8 agents, full agent step)",
+            "value": value,
+            "unit": "agent-ticks/s",
+            "n_gpus": ws,
+            "steps": K,
+            "warmup": W,
+            "ms_per_step": ms_max / K,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "int8/int32 state, f64 node FOI",
+            "data": "synthetic (seeded numpy, Nigeria-scale shapes)",
+            "config": {"workload": "nigeria_like 774 nodes x 2.2e8 agents, capacity +30%, ticks "
+                                   f"{W + 1}-{W + K} of a 2555-tick run",
+                       "agents": params["count"], "capacity": params["capacity"], "nodes": params["n_nodes"],
+                       "l2": "state columns larger than L2 (no flush needed)", "replicas": ws},
+            "e2e": e2e,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": launches,
+            "final_tick": st.t,
+            "new_exposed_total": int(res["new_exposed"].sum()),
+        }
+        print(json.dumps(line), flush=True)
+        if args.out:
+            Path(args.out).write_text(json.dumps(line, indent=1))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

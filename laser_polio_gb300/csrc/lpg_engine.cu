@@ -124,12 +124,16 @@ __global__ void k_fill_f32(float* p, int64_t n, float v) {
 __global__ void k_hist(const int16_t* node, int64_t count, int n_nodes, unsigned long long* cnt, int* flags) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
     int v = node[i];
+    const unsigned act = __activemask();
     if (v < 0 || v >= n_nodes) {
       atomicOr(&flags[0], 1);
-      continue;
+      v = -1;
+    } else if (i + 1 < count && node[i + 1] < v) {
+      atomicOr(&flags[1], 1);
     }
-    atomicAdd(&cnt[v], 1ULL);
-    if (i + 1 < count && node[i + 1] < v) atomicOr(&flags[1], 1);
+    /* one atomic per distinct node id in the warp */
+    const unsigned peers = __match_any_sync(act, v);
+    if (v >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&cnt[v], (unsigned long long)__popc(peers));
   }
 }
 

@@ -355,7 +355,203 @@ __device__ __forceinline__ bool any_ei(uint64_t x) {
 }
 
 /* Fused sweep.  PHASE 0 does deaths and disease progression, plus RI/SIA
- * unless a seed event falls on the tick; PHASE 1 does RI/SIA on seed ticks. */
+ * unless a seed event falls on the tick; PHASE 1 does RI/SIA on seed ticks.
+ * Each CTA owns a contiguous range of chunks (consecutive chunks mostly share
+ * a node, so node counters flush rarely) and prefetches the state bytes of
+ * LPG_SWEEP_UNROLL chunks before processing them, to keep enough bytes in
+ * flight per SM for HBM. */
+#define LPG_SWEEP_UNROLL 8
+
+struct ChunkCtx {
+  int64_t cid;
+  const DevRep* rp;
+  int g, fill, nbo;
+};
+
+template <int PHASE>
+__device__ __forceinline__ void sweep_chunk(SweepSmem& S, DevWorld& W, const ChunkCtx& cc, uint64_t st8) {
+  const DevRep* rp = cc.rp;
+  const int64_t cid = cc.cid;
+  const int o = threadIdx.x * LPG_SPT;
+  const int t = rp->cur_t;
+  const int ni = cc.g - rp->node_base;
+  const int do_vd = PHASE == 0 && rp->vd_tick;
+  const int do_ds = PHASE == 0 && (rp->comps & LPG_COMP_DS);
+  const int late = (PHASE == 0) == (rp->seed_n == 0);
+  const int do_ri = late && rp->ri_tick;
+  const int nsia = late ? rp->sia_n : 0;
+  const int fill = cc.fill;
+  if (o >= fill) return;
+  const bool need = do_vd || do_ri || nsia > 0 || (do_ds && any_ei(st8));
+  if (!need) return;
+  const int nbo = cc.nbo;
+  const int64_t pos0 = cid * LPG_CHUNK + o;
+
+  /* dense per-tick columns, loaded only on the ticks that need them */
+  int32_t dod[LPG_SPT], dob[LPG_SPT];
+  int16_t rit[LPG_SPT];
+  uint8_t cmv[LPG_SPT];
+  if (do_vd) {
+    int4 a = *reinterpret_cast<const int4*>(W.dod + pos0);
+    int4 b = *reinterpret_cast<const int4*>(W.dod + pos0 + 4);
+    dod[0] = a.x; dod[1] = a.y; dod[2] = a.z; dod[3] = a.w;
+    dod[4] = b.x; dod[5] = b.y; dod[6] = b.z; dod[7] = b.w;
+  }
+  if (do_ri || nsia) {
+    uint64_t c8 = *reinterpret_cast<const uint64_t*>(W.cm + pos0);
+#pragma unroll
+    for (int j = 0; j < LPG_SPT; ++j) cmv[j] = (uint8_t)(c8 >> (8 * j));
+  }
+  if (do_ri) {
+    int4 a = *reinterpret_cast<const int4*>(W.ri + pos0);
+    const int16_t* pa = reinterpret_cast<const int16_t*>(&a);
+#pragma unroll
+    for (int j = 0; j < LPG_SPT; ++j) rit[j] = pa[j];
+  }
+  if (nsia) {
+    int4 a = *reinterpret_cast<const int4*>(W.dob + pos0);
+    int4 b = *reinterpret_cast<const int4*>(W.dob + pos0 + 4);
+    dob[0] = a.x; dob[1] = a.y; dob[2] = a.z; dob[3] = a.w;
+    dob[4] = b.x; dob[5] = b.y; dob[6] = b.z; dob[7] = b.w;
+  }
+  uint64_t out8 = st8;
+  bool ri_dirty = false;
+  const int nvalid = min(LPG_SPT, fill - o);
+  for (int j = 0; j < nvalid; ++j) {
+    const int64_t pos = pos0 + j;
+    int8_t s = (int8_t)(st8 >> (8 * j));
+    const int8_t s_in = s;
+    int st = -1; /* strain, loaded on demand */
+    /* -- deaths (get_deaths) -------------------------------------------- */
+    if (do_vd && s >= 0 && (o + j) < nbo && dod[j] <= t) {
+      atomicAdd(&S.ev[EV_DEATHS], 1);
+      if (s == 0) {
+        s_exit(S, W, pos, cid);
+      } else if (s == 1 || s == 2) {
+        st = W.strain[pos];
+        if (s == 1) {
+          atomicAdd(&S.tot[TT_E0 + st], -1);
+        } else {
+          atomicAdd(&S.tot[TT_I0 + st], -1);
+          uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd(&S.bb[st], neg64(bw));
+        }
+      } else if (s == 3) {
+        atomicAdd(&S.tot[TT_R], -1);
+      }
+      if (W.pp[pos] == 1) atomicAdd(&S.tot[TT_POTP], -1);
+      if (W.par[pos] == 1) atomicAdd(&S.tot[TT_P], -1);
+      s = -1;
+    }
+    /* -- disease progression (disease_state_step_kernel) ------------------ */
+    if (do_ds) {
+      if (s == 1) {
+        int8_t e = W.et[pos];
+        if (st < 0) st = W.strain[pos];
+        if (e <= 0) {
+          s = 2;
+          atomicAdd(&S.tot[TT_E0 + st], -1);
+          atomicAdd(&S.tot[TT_I0 + st], 1);
+          uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd(&S.bb[st], (unsigned long long)bw);
+        }
+        W.et[pos] = dec_i8(e);
+      }
+      if (s == 2) {
+        int8_t i = W.it[pos];
+        if (st < 0) st = W.strain[pos];
+        if (i <= 0) {
+          s = 3;
+          atomicAdd(&S.tot[TT_I0 + st], -1);
+          atomicAdd(&S.tot[TT_R], 1);
+          uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd(&S.bb[st], neg64(bw));
+        }
+        W.it[pos] = dec_i8(i);
+        if (st == 0) {
+          int8_t p = W.pt[pos];
+          if (p <= 0 && W.pp[pos] == -1) {
+            if (W.ipv[pos] == 0) {
+              W.pp[pos] = 1;
+              atomicAdd(&S.tot[TT_POTP], 1);
+              atomicAdd(&S.ev[EV_NEWPOT], 1);
+              if (lpg_u01(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < (double)rp->p_par) {
+                W.par[pos] = 1;
+                atomicAdd(&S.tot[TT_P], 1);
+                atomicAdd(&S.ev[EV_NEWPAR], 1);
+              }
+            } else {
+              W.pp[pos] = 0;
+            }
+          }
+          W.pt[pos] = dec_i8(p);
+        }
+      }
+    }
+    /* -- routine immunisation (fast_ri) ------------------------------------ */
+    if (do_ri && s >= 0 && cmv[j] != 1) {
+      int32_t timer = (int32_t)rit[j] - rp->ri_step;
+      rit[j] = (int16_t)(uint16_t)(uint32_t)timer;
+      ri_dirty = true;
+      bool eligible = false;
+      if (t == rp->ri_step) eligible = timer <= 0 && timer >= -rp->ri_step;
+      else if (t > rp->ri_step) eligible = timer <= 0 && timer > -rp->ri_step;
+      if (eligible) {
+        uint32_t ref = W.ref[pos];
+        if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 0) < rp->p_ri[ni]) {
+          atomicAdd(&S.ev[EV_RIVAC], 1);
+          if (s == 0) {
+            s = 1;
+            W.strain[pos] = (int8_t)rp->ri_strain;
+            st = rp->ri_strain;
+            atomicAdd(&S.ev[EV_RIPROT], 1);
+            s_exit(S, W, pos, cid);
+            atomicAdd(&S.tot[TT_E0 + rp->ri_strain], 1);
+          }
+        }
+        if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 1) < rp->p_ipv[ni]) {
+          atomicAdd(&S.ev[EV_IPVVAC], 1);
+          W.ipv[pos] = 1;
+        }
+      }
+    }
+    /* -- SIA campaigns of the day (fast_sia) ------------------------------- */
+    for (int k = 0; k < nsia; ++k) {
+      if (s < 0 || cmv[j] == 1) break;
+      const DevSia& ev = rp->sia[rp->sia_i0 + k];
+      int64_t age = (int64_t)t - (int64_t)dob[j];
+      if (!(ev.min_age <= age && age <= ev.max_age)) continue;
+      if (ev.mask[ni] == 0) continue;
+      double r = lpg_u01(rp->seed, LPG_P_SIA, t, W.ref[pos], 0, (uint64_t)k);
+      double p = (double)rp->p_sia[ni];
+      if (r < p) {
+        atomicAdd(&S.ev[EV_SIAVAC0 + k], 1);
+        if (s == 0 && r < p * ev.efficacy) {
+          s = 1;
+          W.strain[pos] = (int8_t)ev.strain;
+          st = ev.strain;
+          atomicAdd(&S.ev[EV_SIAPROT0 + k], 1);
+          s_exit(S, W, pos, cid);
+          atomicAdd(&S.tot[TT_E0 + ev.strain], 1);
+        }
+      }
+    }
+    if (s != s_in) {
+      out8 = (out8 & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)s << (8 * j));
+    }
+  }
+  if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
+  if (ri_dirty) {
+    int4 a;
+    int16_t* pa = reinterpret_cast<int16_t*>(&a);
+    const int4 old = *reinterpret_cast<const int4*>(W.ri + pos0);
+    const int16_t* po = reinterpret_cast<const int16_t*>(&old);
+#pragma unroll
+    for (int j = 0; j < LPG_SPT; ++j) pa[j] = (j < nvalid) ? rit[j] : po[j];
+    *reinterpret_cast<int4*>(W.ri + pos0) = a;
+  }
+}
+
 template <int PHASE>
 __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
   __shared__ SweepSmem S;
@@ -390,196 +586,39 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
   int cur_g = -1;
   const int o = threadIdx.x * LPG_SPT;
 
-  for (int32_t w = w0; w < w1; ++w) {
-    int lo = 0, hi = s_nreps - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (s_off[mid] <= w) lo = mid; else hi = mid - 1;
-    }
-    const DevRep* rp = &W.reps[lo];
-    const int64_t cid = rp->chunk_base + (w - s_off[lo]);
-    const int g = W.chunk_node[cid];
-    if (g != cur_g) {
-      sweep_flush(S, W, cur_g);
-      cur_g = g;
-    }
-    const int t = rp->cur_t;
-    const int ni = g - rp->node_base;
-    const int do_vd = PHASE == 0 && rp->vd_tick;
-    const int do_ds = PHASE == 0 && (rp->comps & LPG_COMP_DS);
-    const int late = (PHASE == 0) == (rp->seed_n == 0);
-    const int do_ri = late && rp->ri_tick;
-    const int nsia = late ? rp->sia_n : 0;
-    const int fill = W.chunk_fill[cid];
-    if (o >= fill) continue;
-    const int nbo = (W.chunk_nbt[cid] == t) ? W.chunk_nbo[cid] : LPG_CHUNK;
-    const int64_t pos0 = cid * LPG_CHUNK + o;
-    const uint64_t st8 = *reinterpret_cast<const uint64_t*>(W.ds + pos0);
-    const bool need = do_vd || do_ri || nsia > 0 || (do_ds && any_ei(st8));
-    if (!need) continue;
-
-    /* dense per-tick columns, loaded only on the ticks that need them */
-    int32_t dod[LPG_SPT], dob[LPG_SPT];
-    int16_t rit[LPG_SPT];
-    uint8_t cmv[LPG_SPT];
-    if (do_vd) {
-      int4 a = *reinterpret_cast<const int4*>(W.dod + pos0);
-      int4 b = *reinterpret_cast<const int4*>(W.dod + pos0 + 4);
-      dod[0] = a.x; dod[1] = a.y; dod[2] = a.z; dod[3] = a.w;
-      dod[4] = b.x; dod[5] = b.y; dod[6] = b.z; dod[7] = b.w;
-    }
-    if (do_ri || nsia) {
-      uint64_t c8 = *reinterpret_cast<const uint64_t*>(W.cm + pos0);
+  for (int32_t wb = w0; wb < w1; wb += LPG_SWEEP_UNROLL) {
+    ChunkCtx cc[LPG_SWEEP_UNROLL];
+    uint64_t st8[LPG_SWEEP_UNROLL];
 #pragma unroll
-      for (int j = 0; j < LPG_SPT; ++j) cmv[j] = (uint8_t)(c8 >> (8 * j));
-    }
-    if (do_ri) {
-      int4 a = *reinterpret_cast<const int4*>(W.ri + pos0);
-      const int16_t* pa = reinterpret_cast<const int16_t*>(&a);
-#pragma unroll
-      for (int j = 0; j < LPG_SPT; ++j) rit[j] = pa[j];
-    }
-    if (nsia) {
-      int4 a = *reinterpret_cast<const int4*>(W.dob + pos0);
-      int4 b = *reinterpret_cast<const int4*>(W.dob + pos0 + 4);
-      dob[0] = a.x; dob[1] = a.y; dob[2] = a.z; dob[3] = a.w;
-      dob[4] = b.x; dob[5] = b.y; dob[6] = b.z; dob[7] = b.w;
-    }
-    uint64_t out8 = st8;
-    bool ri_dirty = false;
-    const int nvalid = min(LPG_SPT, fill - o);
-    for (int j = 0; j < nvalid; ++j) {
-      const int64_t pos = pos0 + j;
-      int8_t s = (int8_t)(st8 >> (8 * j));
-      const int8_t s_in = s;
-      int st = -1; /* strain, loaded on demand */
-      /* -- deaths (get_deaths) -------------------------------------------- */
-      if (do_vd && s >= 0 && (o + j) < nbo && dod[j] <= t) {
-        atomicAdd(&S.ev[EV_DEATHS], 1);
-        if (s == 0) {
-          s_exit(S, W, pos, cid);
-        } else if (s == 1 || s == 2) {
-          st = W.strain[pos];
-          if (s == 1) {
-            atomicAdd(&S.tot[TT_E0 + st], -1);
-          } else {
-            atomicAdd(&S.tot[TT_I0 + st], -1);
-            uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-            if (bw) atomicAdd(&S.bb[st], neg64(bw));
-          }
-        } else if (s == 3) {
-          atomicAdd(&S.tot[TT_R], -1);
+    for (int u = 0; u < LPG_SWEEP_UNROLL; ++u) {
+      const int32_t w = wb + u;
+      cc[u].fill = 0;
+      cc[u].g = -1;
+      st8[u] = ~0ULL;
+      if (w < w1) {
+        int lo = 0, hi = s_nreps - 1;
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (s_off[mid] <= w) lo = mid; else hi = mid - 1;
         }
-        if (W.pp[pos] == 1) atomicAdd(&S.tot[TT_POTP], -1);
-        if (W.par[pos] == 1) atomicAdd(&S.tot[TT_P], -1);
-        s = -1;
-      }
-      /* -- disease progression (disease_state_step_kernel) ------------------ */
-      if (do_ds) {
-        if (s == 1) {
-          int8_t e = W.et[pos];
-          if (st < 0) st = W.strain[pos];
-          if (e <= 0) {
-            s = 2;
-            atomicAdd(&S.tot[TT_E0 + st], -1);
-            atomicAdd(&S.tot[TT_I0 + st], 1);
-            uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-            if (bw) atomicAdd(&S.bb[st], (unsigned long long)bw);
-          }
-          W.et[pos] = dec_i8(e);
-        }
-        if (s == 2) {
-          int8_t i = W.it[pos];
-          if (st < 0) st = W.strain[pos];
-          if (i <= 0) {
-            s = 3;
-            atomicAdd(&S.tot[TT_I0 + st], -1);
-            atomicAdd(&S.tot[TT_R], 1);
-            uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-            if (bw) atomicAdd(&S.bb[st], neg64(bw));
-          }
-          W.it[pos] = dec_i8(i);
-          if (st == 0) {
-            int8_t p = W.pt[pos];
-            if (p <= 0 && W.pp[pos] == -1) {
-              if (W.ipv[pos] == 0) {
-                W.pp[pos] = 1;
-                atomicAdd(&S.tot[TT_POTP], 1);
-                atomicAdd(&S.ev[EV_NEWPOT], 1);
-                if (lpg_u01(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < (double)rp->p_par) {
-                  W.par[pos] = 1;
-                  atomicAdd(&S.tot[TT_P], 1);
-                  atomicAdd(&S.ev[EV_NEWPAR], 1);
-                }
-              } else {
-                W.pp[pos] = 0;
-              }
-            }
-            W.pt[pos] = dec_i8(p);
-          }
-        }
-      }
-      /* -- routine immunisation (fast_ri) ------------------------------------ */
-      if (do_ri && s >= 0 && cmv[j] != 1) {
-        int32_t timer = (int32_t)rit[j] - rp->ri_step;
-        rit[j] = (int16_t)(uint16_t)(uint32_t)timer;
-        ri_dirty = true;
-        bool eligible = false;
-        if (t == rp->ri_step) eligible = timer <= 0 && timer >= -rp->ri_step;
-        else if (t > rp->ri_step) eligible = timer <= 0 && timer > -rp->ri_step;
-        if (eligible) {
-          uint32_t ref = W.ref[pos];
-          if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 0) < rp->p_ri[ni]) {
-            atomicAdd(&S.ev[EV_RIVAC], 1);
-            if (s == 0) {
-              s = 1;
-              W.strain[pos] = (int8_t)rp->ri_strain;
-              st = rp->ri_strain;
-              atomicAdd(&S.ev[EV_RIPROT], 1);
-              s_exit(S, W, pos, cid);
-              atomicAdd(&S.tot[TT_E0 + rp->ri_strain], 1);
-            }
-          }
-          if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 1) < rp->p_ipv[ni]) {
-            atomicAdd(&S.ev[EV_IPVVAC], 1);
-            W.ipv[pos] = 1;
-          }
-        }
-      }
-      /* -- SIA campaigns of the day (fast_sia) ------------------------------- */
-      for (int k = 0; k < nsia; ++k) {
-        if (s < 0 || cmv[j] == 1) break;
-        const DevSia& ev = rp->sia[rp->sia_i0 + k];
-        int64_t age = (int64_t)t - (int64_t)dob[j];
-        if (!(ev.min_age <= age && age <= ev.max_age)) continue;
-        if (ev.mask[ni] == 0) continue;
-        double r = lpg_u01(rp->seed, LPG_P_SIA, t, W.ref[pos], 0, (uint64_t)k);
-        double p = (double)rp->p_sia[ni];
-        if (r < p) {
-          atomicAdd(&S.ev[EV_SIAVAC0 + k], 1);
-          if (s == 0 && r < p * ev.efficacy) {
-            s = 1;
-            W.strain[pos] = (int8_t)ev.strain;
-            st = ev.strain;
-            atomicAdd(&S.ev[EV_SIAPROT0 + k], 1);
-            s_exit(S, W, pos, cid);
-            atomicAdd(&S.tot[TT_E0 + ev.strain], 1);
-          }
-        }
-      }
-      if (s != s_in) {
-        out8 = (out8 & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)s << (8 * j));
+        const DevRep* rp = &W.reps[lo];
+        const int64_t cid = rp->chunk_base + (w - s_off[lo]);
+        cc[u].rp = rp;
+        cc[u].cid = cid;
+        cc[u].g = W.chunk_node[cid];
+        cc[u].fill = W.chunk_fill[cid];
+        cc[u].nbo = (W.chunk_nbt[cid] == rp->cur_t) ? W.chunk_nbo[cid] : LPG_CHUNK;
+        if (o < cc[u].fill) st8[u] = *reinterpret_cast<const uint64_t*>(W.ds + cid * LPG_CHUNK + o);
       }
     }
-    if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
-    if (ri_dirty) {
-      int4 a;
-      int16_t* pa = reinterpret_cast<int16_t*>(&a);
-      const int4 old = *reinterpret_cast<const int4*>(W.ri + pos0);
-      const int16_t* po = reinterpret_cast<const int16_t*>(&old);
-#pragma unroll
-      for (int j = 0; j < LPG_SPT; ++j) pa[j] = (j < nvalid) ? rit[j] : po[j];
-      *reinterpret_cast<int4*>(W.ri + pos0) = a;
+#pragma unroll 1
+    for (int u = 0; u < LPG_SWEEP_UNROLL; ++u) {
+      if (wb + u >= w1) break;
+      if (cc[u].g != cur_g) {
+        sweep_flush(S, W, cur_g);
+        cur_g = cc[u].g;
+      }
+      sweep_chunk<PHASE>(S, W, cc[u], st8[u]);
     }
   }
   sweep_flush(S, W, cur_g);

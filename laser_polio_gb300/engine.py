@@ -45,6 +45,82 @@ def _node_vector(value, n, dtype):
     return np.ascontiguousarray(np.broadcast_to(arr, (n,)), dtype=dtype)
 
 
+def make_desc(p: dict):
+    """An lpg_sim_desc from plain parameters.
+
+    Keys: n_nodes, n_strains, nt, count, capacity, seed, components (mask),
+    stop_if_no_cases, vd_step, birth_rate[n], km_cumdeaths, km_max_year,
+    p_paralysis, seeds [(tick, node, is_count, value)], dur_inf (kind, p1, p2),
+    ri_step, ri_enabled, ri_strain, vx_prob_ri[n], vx_prob_ipv[n],
+    sia [(tick, strain, min_age, max_age, efficacy, node_mask[n])],
+    vx_prob_sia[n], strain_r0_scalars[ns], network[n, n], r0_scalars[n],
+    seasonality[nt], zero_inflation, nb_r, pop0[n], R_preseed[nt, n] or None.
+    Returns (desc, keepalive list).
+    """
+    keep = []
+
+    def arr(a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        keep.append(a)
+        return a
+
+    n = int(p["n_nodes"])
+    d = _abi.lpg_sim_desc()
+    d.n_nodes = n
+    d.n_strains = int(p["n_strains"])
+    d.nt = int(p["nt"])
+    d.count = int(p["count"])
+    d.capacity = int(p["capacity"])
+    d.seed = int(p["seed"]) & 0xFFFFFFFFFFFFFFFF
+    d.components = int(p["components"])
+    d.stop_if_no_cases = int(p.get("stop_if_no_cases", 0))
+    d.vd_step = int(p.get("vd_step", 7))
+    d.birth_rate = _abi.ptr(arr(_node_vector(p.get("birth_rate", 0.0), n, np.float64), np.float64), _abi.P_f64)
+    km = arr(p["km_cumdeaths"], np.int64)
+    d.km_cumdeaths = _abi.ptr(km, _abi.P_i64)
+    d.km_len = len(km)
+    d.km_max_year = int(p.get("km_max_year", 100))
+    d.p_paralysis = float(np.float32(p.get("p_paralysis", 1 / 2000)))
+    seeds = list(p.get("seeds", []))
+    seed_arr = (_abi.lpg_seed_event * max(1, len(seeds)))()
+    for i, (t, node, is_count, value) in enumerate(seeds):
+        seed_arr[i].tick, seed_arr[i].node, seed_arr[i].is_count, seed_arr[i].value = int(t), int(node), int(is_count), float(value)
+    keep.append(seed_arr)
+    d.seeds = C.cast(seed_arr, C.POINTER(_abi.lpg_seed_event))
+    d.n_seeds = len(seeds)
+    kind, p1, p2 = p.get("dur_inf", (0, 1.0, 0.0))
+    d.dur_inf = _abi.lpg_dist(int(kind), float(p1), float(p2))
+    d.ri_step = int(p.get("ri_step", 14))
+    d.ri_enabled = int(p.get("ri_enabled", 0))
+    d.ri_strain = int(p.get("ri_strain", 1))
+    d.vx_prob_ri = _abi.ptr(arr(_node_vector(p.get("vx_prob_ri", 0.0), n, np.float64), np.float64), _abi.P_f64)
+    d.vx_prob_ipv = _abi.ptr(arr(_node_vector(p.get("vx_prob_ipv", 0.0), n, np.float64), np.float64), _abi.P_f64)
+    events = list(p.get("sia", []))
+    sia_arr = (_abi.lpg_sia_event * max(1, len(events)))()
+    for i, (t, st, lo, hi, eff, mask) in enumerate(events):
+        e = sia_arr[i]
+        e.tick, e.strain, e.min_age, e.max_age, e.efficacy = int(t), int(st), int(lo), int(hi), float(eff)
+        e.node_mask = _abi.ptr(arr(mask, np.uint8), _abi.P_u8)
+    keep.append(sia_arr)
+    d.sia = C.cast(sia_arr, C.POINTER(_abi.lpg_sia_event))
+    d.n_sia = len(events)
+    if events:
+        per_tick = np.bincount([int(e[0]) for e in events])
+        if per_tick.max() > _abi.LPG_MAX_SIA_PER_DAY:
+            raise ValueError(f"at most {_abi.LPG_MAX_SIA_PER_DAY} SIA events on one day are supported")
+    d.vx_prob_sia = _abi.ptr(arr(_node_vector(np.asarray(p.get("vx_prob_sia", 0.0), dtype=np.float32), n, np.float32), np.float32), _abi.P_f32)
+    d.strain_r0_scalars = _abi.ptr(arr(p["strain_r0_scalars"], np.float64), _abi.P_f64)
+    d.network = _abi.ptr(arr(p["network"], np.float64), _abi.P_f64)
+    d.r0_scalars = _abi.ptr(arr(_node_vector(np.asarray(p.get("r0_scalars", 1.0), dtype=np.float64), n, np.float64), np.float64), _abi.P_f64)
+    d.seasonality = _abi.ptr(arr(p["seasonality"], np.float64), _abi.P_f64)
+    d.zero_inflation = float(p.get("zero_inflation", 0.0))
+    d.nb_r = int(p.get("nb_r", 1000))
+    d.pop0 = _abi.ptr(arr(p["pop0"], np.int32), _abi.P_i32)
+    rp = p.get("R_preseed")
+    d.R_preseed = _abi.ptr(arr(rp, np.int32), _abi.P_i32) if rp is not None else None
+    return d, keep
+
+
 def build_sim_spec(sim) -> SimSpec:
     """Describe ``sim`` (an SEIR_ABM with drop-in components) for the C ABI."""
     pars = sim.pars
@@ -58,35 +134,20 @@ def build_sim_spec(sim) -> SimSpec:
     ns = len(pars.strain_ids)
     if ns > _abi.LPG_MAX_STRAINS:
         raise ValueError(f"at most {_abi.LPG_MAX_STRAINS} strains are supported, got {ns}")
-    keep = []
-
-    def arr(a, dtype):
-        a = np.ascontiguousarray(a, dtype=dtype)
-        keep.append(a)
-        return a
-
-    d = _abi.lpg_sim_desc()
-    d.n_nodes = n
-    d.n_strains = ns
-    d.nt = sim.nt
-    d.count = sim.people.count
-    d.capacity = sim.people.capacity
-    d.seed = int(pars.seed) & 0xFFFFFFFFFFFFFFFF
-    d.components = mask
-    d.stop_if_no_cases = int(bool(pars["stop_if_no_cases"]) and "DiseaseState_ABM" in inst)
+    p = {"n_nodes": n, "n_strains": ns, "nt": sim.nt, "count": sim.people.count, "capacity": sim.people.capacity,
+         "seed": int(pars.seed), "components": mask,
+         "stop_if_no_cases": int(bool(pars["stop_if_no_cases"]) and "DiseaseState_ABM" in inst)}
 
     vd = inst.get("VitalDynamics_ABM")
-    d.vd_step = int(pars.step_size_VitalDynamics_ABM)
-    d.birth_rate = _abi.ptr(arr(vd.birth_rate if vd is not None else np.zeros(n), np.float64), _abi.P_f64)
+    p["vd_step"] = int(pars.step_size_VitalDynamics_ABM)
+    p["birth_rate"] = vd.birth_rate if vd is not None else np.zeros(n)
     if vd is not None and getattr(vd, "death_estimator", None) is not None:
-        km = arr(vd.death_estimator.cumulative_deaths, np.int64)
+        p["km_cumdeaths"] = vd.death_estimator.cumulative_deaths
     else:
-        km = arr(lpu.create_cumulative_deaths(int(np.sum(pars.init_pop)), 100), np.int64)
-    d.km_cumdeaths = _abi.ptr(km, _abi.P_i64)
-    d.km_len = len(km)
-    d.km_max_year = 100
+        p["km_cumdeaths"] = lpu.create_cumulative_deaths(int(np.sum(pars.init_pop)), 100)
+    p["km_max_year"] = 100
 
-    d.p_paralysis = float(np.float32(pars.p_paralysis))
+    p["p_paralysis"] = pars.p_paralysis
     seeds = []
     ds = inst.get("DiseaseState_ABM")
     if ds is not None:
@@ -98,21 +159,14 @@ def build_sim_spec(sim) -> SimSpec:
                     seeds.append((int(t), int(node), 1, float(value)))
                 else:
                     raise ValueError(f"Unsupported seed value type: {type(value)}")
-    seed_arr = (_abi.lpg_seed_event * max(1, len(seeds)))()
-    for i, (t, node, is_count, value) in enumerate(seeds):
-        seed_arr[i].tick, seed_arr[i].node, seed_arr[i].is_count, seed_arr[i].value = t, node, is_count, value
-    keep.append(seed_arr)
-    d.seeds = C.cast(seed_arr, C.POINTER(_abi.lpg_seed_event))
-    d.n_seeds = len(seeds)
-    kind, p1, p2 = pars.dur_inf.spec()
-    d.dur_inf = _abi.lpg_dist(kind, p1, p2)
+    p["seeds"] = seeds
+    p["dur_inf"] = pars.dur_inf.spec()
 
-    d.ri_step = int(pars.step_size_RI_ABM)
-    d.ri_enabled = int(pars["vx_prob_ri"] is not None and "RI_ABM" in inst)
-    d.ri_strain = _vaccine_strain(getattr(pars, "ri_vaccine_type", "tOPV") if "ri_vaccine_type" in pars else "tOPV")
-    d.vx_prob_ri = _abi.ptr(arr(_node_vector(pars["vx_prob_ri"] if pars["vx_prob_ri"] is not None else 0.0, n, np.float64), np.float64), _abi.P_f64)
-    ipv = pars["vx_prob_ipv"] if pars["vx_prob_ipv"] is not None else 0.0
-    d.vx_prob_ipv = _abi.ptr(arr(_node_vector(ipv, n, np.float64), np.float64), _abi.P_f64)
+    p["ri_step"] = int(pars.step_size_RI_ABM)
+    p["ri_enabled"] = int(pars["vx_prob_ri"] is not None and "RI_ABM" in inst)
+    p["ri_strain"] = _vaccine_strain(pars["ri_vaccine_type"] if "ri_vaccine_type" in pars else "tOPV")
+    p["vx_prob_ri"] = pars["vx_prob_ri"] if pars["vx_prob_ri"] is not None else 0.0
+    p["vx_prob_ipv"] = pars["vx_prob_ipv"] if pars["vx_prob_ipv"] is not None else 0.0
 
     sia = inst.get("SIA_ABM")
     events = []
@@ -126,30 +180,17 @@ def build_sim_spec(sim) -> SimSpec:
             node_mask[ev["nodes"]] = 1
             min_age, max_age = ev["age_range"]
             vt = ev["vaccinetype"]
-            events.append((t, _vaccine_strain(vt), int(min_age), int(max_age), float(pars["vx_efficacy"][vt]), arr(node_mask, np.uint8)))
-    sia_arr = (_abi.lpg_sia_event * max(1, len(events)))()
-    for i, (t, st, lo, hi, eff, m) in enumerate(events):
-        e = sia_arr[i]
-        e.tick, e.strain, e.min_age, e.max_age, e.efficacy = t, st, lo, hi, eff
-        e.node_mask = _abi.ptr(m, _abi.P_u8)
-    keep.append(sia_arr)
-    d.sia = C.cast(sia_arr, C.POINTER(_abi.lpg_sia_event))
-    d.n_sia = len(events)
-    if events:
-        counts_per_tick = np.bincount([e[0] for e in events])
-        if counts_per_tick.max() > _abi.LPG_MAX_SIA_PER_DAY:
-            raise ValueError(f"at most {_abi.LPG_MAX_SIA_PER_DAY} SIA events on one day are supported")
-    vps = pars.vx_prob_sia if pars.vx_prob_sia is not None else np.zeros(n)
-    d.vx_prob_sia = _abi.ptr(arr(_node_vector(np.asarray(vps, dtype=np.float32), n, np.float32), np.float32), _abi.P_f32)
+            events.append((t, _vaccine_strain(vt), int(min_age), int(max_age), float(pars["vx_efficacy"][vt]), node_mask))
+    p["sia"] = events
+    p["vx_prob_sia"] = pars.vx_prob_sia if pars.vx_prob_sia is not None else 0.0
 
     tx = inst.get("Transmission_ABM")
-    d.strain_r0_scalars = _abi.ptr(arr(np.array(list(pars.strain_r0_scalars.values()), dtype=np.float64)[:ns], np.float64), _abi.P_f64)
-    net = tx.network if tx is not None else np.zeros((n, n))
-    d.network = _abi.ptr(arr(net, np.float64), _abi.P_f64)
-    d.r0_scalars = _abi.ptr(arr(_node_vector(np.asarray(pars.r0_scalars, dtype=np.float64), n, np.float64), np.float64), _abi.P_f64)
-    d.seasonality = _abi.ptr(arr(lpu.seasonality_table(sim.datevec, pars["seasonal_amplitude"], pars["seasonal_peak_doy"]), np.float64), _abi.P_f64)
-    d.zero_inflation = float(pars.node_seeding_zero_inflation)
-    d.nb_r = int(max(1, int(np.round(pars.node_seeding_dispersion))))
+    p["strain_r0_scalars"] = np.array(list(pars.strain_r0_scalars.values()), dtype=np.float64)[:ns]
+    p["network"] = tx.network if tx is not None else np.zeros((n, n))
+    p["r0_scalars"] = np.asarray(pars.r0_scalars, dtype=np.float64)
+    p["seasonality"] = lpu.seasonality_table(sim.datevec, pars["seasonal_amplitude"], pars["seasonal_peak_doy"])
+    p["zero_inflation"] = float(pars.node_seeding_zero_inflation)
+    p["nb_r"] = int(max(1, int(np.round(pars.node_seeding_dispersion))))
 
     results = {}
     for name, _ in _abi.RESULT_FIELDS:
@@ -157,13 +198,10 @@ def build_sim_spec(sim) -> SimSpec:
         if isinstance(a, np.ndarray) and a.dtype == np.int32:
             results[name] = a
     pop = results.get("pop")
-    pop0 = arr(pop[0] if pop is not None else np.asarray(pars.init_pop), np.int32)
-    d.pop0 = _abi.ptr(pop0, _abi.P_i32)
+    p["pop0"] = pop[0] if pop is not None else np.asarray(pars.init_pop)
     Rres = results.get("R")
-    if Rres is not None and np.any(Rres):
-        d.R_preseed = _abi.ptr(arr(Rres, np.int32), _abi.P_i32)
-    else:
-        d.R_preseed = None
+    p["R_preseed"] = Rres if (Rres is not None and np.any(Rres)) else None
+    d, keep = make_desc(p)
 
     columns = {}
     for name, _, dtype in _abi.COLUMN_FIELDS:

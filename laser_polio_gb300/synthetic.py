@@ -150,3 +150,188 @@ def nigeria_like(n_agents=2_000_000, n_nodes=774, dur=2555, seed=42):
     _age_immunity(sim, rng, immun)
     _seed_infections(sim, rng, 2, 10)
     return sim
+
+
+# ---------------------------------------------------------------------------
+# Full-size bundles: reference-ordered columns built directly (no per-agent
+# Python), in parallel chunks, optionally into caller-provided (e.g. pinned)
+# host buffers.  Same recipe as nigeria_like / zamfara_like.
+
+COLUMN_DTYPES = {
+    "disease_state": np.int8,
+    "strain": np.int8,
+    "exposure_timer": np.int8,
+    "infection_timer": np.int8,
+    "paralysis_timer": np.int8,
+    "potentially_paralyzed": np.int8,
+    "paralyzed": np.int8,
+    "ipv_protected": np.int8,
+    "chronically_missed": np.uint8,
+    "node_id": np.int16,
+    "ri_timer": np.int16,
+    "acq_risk_multiplier": np.float32,
+    "daily_infectivity": np.float32,
+    "date_of_birth": np.int32,
+    "date_of_death": np.int32,
+}
+
+
+def _km_ages(rng, cum, ages_days, max_year=100):
+    """Vectorised KM age at death (same rule as core.KaplanMeierEstimator)."""
+    top = min(int(max_year), len(cum) - 1)
+    years = np.minimum(ages_days // 365, top)
+    lower = np.where(years > 0, cum[np.maximum(years - 1, 0)], 0)
+    total = cum[top]
+    span = np.maximum(total - lower, 0)
+    draw = lower + np.floor(rng.random(len(ages_days)) * span).astype(np.int64)
+    y = np.searchsorted(cum[: top + 1], draw, side="right")
+    y = np.where(span > 0, np.maximum(y, years), top)
+    y = np.minimum(y, top)
+    lo = np.where(y == years, ages_days, y * 365)
+    hi = np.maximum((y + 1) * 365, lo + 1)
+    return (lo + np.floor(rng.random(len(ages_days)) * (hi - lo)).astype(np.int64)).astype(np.int32)
+
+
+def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capacity_factor=1.3, threads=None,
+           alloc=None):
+    """(make_desc parameters, reference-ordered columns) of a synthetic run.
+
+    kind 'nigeria' (defaults 2.2e8 agents, 774 nodes, 2555 ticks) or
+    'zamfara' (1e6 agents, 14 nodes, 365 ticks).  ``alloc(name, n, dtype)``
+    may supply the column buffers (pinned host memory for the end-to-end
+    measurement).
+    """
+    import concurrent.futures as cf
+    import datetime as dt
+
+    from scipy.special import ndtr
+
+    from .core import gravity
+    from .core import row_normalizer
+    from .engine import _vaccine_strain
+    from .utils import create_cumulative_deaths
+    from .utils import seasonality_table
+
+    if kind == "nigeria":
+        n_agents = int(2.2e8 if n_agents is None else n_agents)
+        n_nodes = 774 if n_nodes is None else n_nodes
+        dur = 2555 if dur is None else dur
+        mu, sg, side, cbr = np.log(2.8e5), 0.7, 1000.0, 37
+    else:
+        n_agents = int(1e6 if n_agents is None else n_agents)
+        n_nodes = 14 if n_nodes is None else n_nodes
+        dur = 365 if dur is None else dur
+        mu, sg, side, cbr = np.log(7e4), 0.6, 200.0, 35
+    rng = np.random.default_rng(seed)
+    pops = _node_pops(rng, n_nodes, mu, sg, n_agents)
+    count = int(pops.sum())
+    capacity = int(count * capacity_factor)
+    nt = dur + 1
+    r0 = 14.0
+    if kind == "nigeria":
+        immun = rng.uniform(0.4, 0.9, n_nodes)
+        p_ri = rng.beta(6, 4, n_nodes)
+        p_sia = rng.beta(8, 3, n_nodes)
+        sia = []
+        for k, t in enumerate(range(180, dur + 1, 180)):
+            mask = np.zeros(n_nodes, np.uint8)
+            mask[rng.choice(n_nodes, size=max(1, int(0.3 * n_nodes)), replace=False)] = 1
+            sia.append((t, _vaccine_strain("mOPV2" if k % 2 == 0 else "nOPV2"), 0, 5 * 365, 0.6, mask))
+    else:
+        immun = np.full(n_nodes, 0.8)
+        p_ri = np.full(n_nodes, 0.5)
+        p_sia = np.zeros(n_nodes)
+        sia = []
+    r0s = rng.lognormal(0.0, 0.3, n_nodes)
+    xy = rng.uniform(0, side, size=(n_nodes, 2))
+    dist = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
+    dist[dist == 0] = 1.0
+    np.fill_diagonal(dist, 0.0)
+    net = row_normalizer(gravity(pops, dist, 0.5, 1, 1, 2.0) / np.power(float(pops.sum()), 2.0), 0.2)
+    start = dt.date(2019, 1, 1)
+    datevec = [start + dt.timedelta(days=i) for i in range(nt)]
+    cum = create_cumulative_deaths(count, 100).astype(np.int64)
+    seed_nodes = rng.choice(n_nodes, size=2, replace=False)
+    params = {
+        "n_nodes": n_nodes, "n_strains": 3, "nt": nt, "count": count, "capacity": capacity, "seed": seed,
+        "components": 31, "stop_if_no_cases": 0, "vd_step": 7, "birth_rate": np.full(n_nodes, cbr / 365000.0),
+        "km_cumdeaths": cum, "km_max_year": 100, "p_paralysis": 1 / 2000, "seeds": [], "dur_inf": (2, 4.0, 6.0),
+        "ri_step": 14, "ri_enabled": 1, "ri_strain": 1, "vx_prob_ri": p_ri, "vx_prob_ipv": np.zeros(n_nodes),
+        "sia": sia, "vx_prob_sia": p_sia.astype(np.float32), "strain_r0_scalars": np.array([1.0, 0.25, 0.125]),
+        "network": net, "r0_scalars": r0s, "seasonality": seasonality_table(datevec, 0.4, 180),
+        "zero_inflation": 0.0, "nb_r": 1000, "pop0": pops.astype(np.int32), "R_preseed": None,
+    }
+
+    alloc = alloc or (lambda name, n, dtype: np.empty(n, dtype=dtype))
+    cols = {name: alloc(name, capacity, dt_) for name, dt_ in COLUMN_DTYPES.items()}
+    node_start = np.concatenate([[0], np.cumsum(pops)])
+    var = float(np.exp(0.8**2) - 1.0)
+    mu_ln = np.log(1.0 / np.sqrt(var + 1.0))
+    sigma_ln = np.sqrt(np.log(var + 1.0))
+    rho = 2.0 * np.sin(np.pi * 0.8 / 6)
+    scale_inf = r0 / 24.0
+    m_par, s_par = 12.5, 3.5
+    mu_p = np.log(m_par**2 / np.sqrt(s_par**2 + m_par**2))
+    sg_p = np.sqrt(np.log(s_par**2 / m_par**2 + 1))
+    trunc = 1.0 - np.exp(-80.0 / 20.0)
+    chunk = 1 << 22
+    spans = [(a, min(a + chunk, capacity)) for a in range(0, capacity, chunk)]
+    seqs = np.random.SeedSequence(seed).spawn(len(spans))
+
+    def fill(i):
+        a, b = spans[i]
+        g = np.random.default_rng(seqs[i])
+        n = b - a
+        et = np.clip(-np.log(g.random((3, n))).sum(0), 0, 127)
+        it = np.clip(-6.0 * np.log(g.random((4, n))).sum(0), 0, 127)
+        et8 = et.astype(np.int8)
+        it8 = it.astype(np.int8)
+        raw = np.exp(mu_p + sg_p * g.standard_normal(n)) - et8
+        cols["exposure_timer"][a:b] = et8
+        cols["infection_timer"][a:b] = it8
+        cols["paralysis_timer"][a:b] = np.clip(raw, 0, np.minimum(it8, 127)).astype(np.int8)
+        z1 = g.standard_normal(n)
+        z2 = rho * z1 + np.sqrt(1 - rho * rho) * g.standard_normal(n)
+        cols["acq_risk_multiplier"][a:b] = np.exp(mu_ln + sigma_ln * z1)
+        cols["daily_infectivity"][a:b] = -scale_inf * np.log(np.maximum(ndtr(-z2), 1e-300))
+        cols["strain"][a:b] = 0
+        cols["potentially_paralyzed"][a:b] = -1
+        cols["paralyzed"][a:b] = 0
+        cols["ipv_protected"][a:b] = 0
+        cols["chronically_missed"][a:b] = 0
+        live = max(0, min(b, count) - a)
+        ds = cols["disease_state"]
+        ds[a:b] = -1
+        cols["node_id"][a:b] = -1
+        cols["ri_timer"][a:b] = -1
+        cols["date_of_birth"][a:b] = -1
+        cols["date_of_death"][a:b] = 0
+        if live:
+            idx = np.arange(a, a + live)
+            node = (np.searchsorted(node_start, idx, side="right") - 1).astype(np.int16)
+            cols["node_id"][a : a + live] = node
+            age_y = -20.0 * np.log(1.0 - g.random(live) * trunc)
+            age = np.maximum(1, (age_y * 365.0).astype(np.int64))
+            cols["date_of_birth"][a : a + live] = -age
+            st = np.zeros(live, np.int8)
+            st[age > 15 * 365] = 3
+            young = age <= 15 * 365
+            st[young & (g.random(live) < immun[node])] = 3
+            ds[a : a + live] = st
+            cols["ri_timer"][a : a + live] = (-age + g.uniform(42, 98, live)).astype(np.int32).astype(np.int16)
+            cols["date_of_death"][a : a + live] = _km_ages(g, cum, age) - age
+
+    with cf.ThreadPoolExecutor(max_workers=threads or min(32, (os_cpu() or 4))) as ex:
+        list(ex.map(fill, range(len(spans))))
+    for nd in seed_nodes:
+        lo, hi = node_start[nd], node_start[nd + 1]
+        pick = rng.choice(np.arange(lo, hi), size=min(10, hi - lo), replace=False)
+        cols["disease_state"][pick] = 2
+        cols["strain"][pick] = 0
+    return params, cols
+
+
+def os_cpu():
+    import os
+
+    return os.cpu_count()
