@@ -38,7 +38,7 @@ struct Staging {
 
 struct SimHost {
   lpg_sim_desc d;
-  std::vector<double> birth_rate, p_ri, p_ipv, strain_scal, net, rowsum, r0s, seas;
+  std::vector<double> birth_rate, p_ri, p_ipv, strain_scal, net, net_t, rowsum, r0s, seas;
   std::vector<float> p_sia;
   std::vector<int64_t> km;
   std::vector<lpg_seed_event> seeds;
@@ -262,6 +262,9 @@ extern "C" int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t devi
     s.net = vec(d.network, n * n, 0.0);
     s.r0s = vec(d.r0_scalars, n, 1.0);
     s.seas = vec(d.seasonality, (size_t)d.nt, 1.0);
+    s.net_t.assign(n * n, 0.0);
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = 0; j < n; ++j) s.net_t[j * n + i] = s.net[i * n + j];
     s.rowsum.assign(n, 0.0);
     for (size_t i = 0; i < n; ++i) {
       double acc = 0.0;
@@ -566,6 +569,8 @@ extern "C" int lpg_start(lpg_handle* h) {
     rp.strain_scal = dp;
     if (dupload(h, &dp, s.net)) return LPG_ERR_NOMEM;
     rp.net = dp;
+    if (dupload(h, &dp, s.net_t)) return LPG_ERR_NOMEM;
+    rp.net_t = dp;
     if (dupload(h, &dp, s.rowsum)) return LPG_ERR_NOMEM;
     rp.rowsum = dp;
     if (dupload(h, &dp, s.r0s)) return LPG_ERR_NOMEM;
@@ -736,7 +741,9 @@ extern "C" int lpg_start(lpg_handle* h) {
 
   /* launch geometry */
   int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_THREADS, 0));
+  CK(cudaFuncSetAttribute(k_sweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
+  CK(cudaFuncSetAttribute(k_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM));
   h->sweep_blocks = std::max(1, occ) * h->sm_count;
   occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_select, 256, 0));
@@ -759,10 +766,10 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
   switch (k) {
     case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
     case 1: k_newborns<<<dim3(64, R), 256, 0, st>>>(W); break;
-    case 2: k_sweep<0><<<h->sweep_blocks, LPG_SWEEP_THREADS, 0, st>>>(W); break;
+    case 2: k_sweep<0><<<h->sweep_blocks, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM, st>>>(W); break;
     case 3: k_seed<<<R, 1024, 0, st>>>(W); break;
-    case 4: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_THREADS, 0, st>>>(W); break;
-    case 5: k_node_tx<<<(G + 127) / 128, 128, 0, st>>>(W); break;
+    case 4: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM, st>>>(W); break;
+    case 5: k_node_tx<<<(G * 32 + 255) / 256, 256, 0, st>>>(W); break;
     case 6: {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(h->select_blocks);

@@ -104,7 +104,8 @@ typedef struct {
   const double* p_ri;
   const double* p_ipv;
   const double* strain_scal;
-  const double* net;
+  const double* net;   /* network[i][j], row-major */
+  const double* net_t; /* transposed: net_t[j][i] = network[i][j] */
   const double* rowsum;
   const double* r0s;
   const double* seas;

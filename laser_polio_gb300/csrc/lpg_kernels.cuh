@@ -356,74 +356,108 @@ __device__ __forceinline__ bool any_ei(uint64_t x) {
 
 /* Fused sweep.  PHASE 0 does deaths and disease progression, plus RI/SIA
  * unless a seed event falls on the tick; PHASE 1 does RI/SIA on seed ticks.
+ *
  * Each CTA owns a contiguous range of chunks (consecutive chunks mostly share
- * a node, so node counters flush rarely) and prefetches the state bytes of
- * LPG_SWEEP_UNROLL chunks before processing them, to keep enough bytes in
- * flight per SM for HBM. */
-#define LPG_SWEEP_UNROLL 8
+ * a node, so node counters flush rarely).  The columns every agent needs are
+ * staged into shared memory with 1-D bulk copies (cp.async.bulk, completion
+ * on an mbarrier) through a ring of LPG_NST stages, issued LPG_NST stages
+ * ahead of the consumers: on plain ticks a stage holds the state bytes of up
+ * to LPG_PLAIN_GROUP chunks; on ticks with deaths, RI or SIA it holds one
+ * chunk's state plus the dense columns of that tick (date_of_death,
+ * ri_timer + chronically_missed, date_of_birth).  Columns needed only by
+ * E/I agents (timers, strain, flags, infectivity) are read from global
+ * memory for those agents alone.  Every mbarrier wait is bounded. */
+#define LPG_NST 4
+#define LPG_STAGE_BYTES (24 * 1024)
+#define LPG_PLAIN_GROUP (LPG_STAGE_BYTES / LPG_CHUNK)
+#define LPG_SWEEP_SMEM (LPG_NST * LPG_STAGE_BYTES)
+#define LPG_MBAR_SPIN (1LL << 24)
+/* dense stage layout (bytes) */
+#define OFF_DS 0
+#define OFF_DOD 2048
+#define OFF_RI (2048 + 8192)
+#define OFF_CM (2048 + 8192 + 4096)
+#define OFF_DOB (2048 + 8192 + 4096 + 2048)
 
-struct ChunkCtx {
-  int64_t cid;
-  const DevRep* rp;
-  int g, fill, nbo;
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+/* bounded wait; false on timeout */
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long it = 0; it < LPG_MBAR_SPIN; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (it > 64) __nanosleep(32);
+  }
+  return false;
+}
+
+struct SweepPlan {
+  int32_t total, nreps;
+  int32_t off[1025];   /* work-item offsets per simulation */
+  int32_t cbase[1024]; /* first chunk id per simulation */
+  uint8_t dense[1024]; /* 1 when the simulation's tick needs dense columns */
 };
 
+/* End of the stage that starts at work item w (same answer on every thread). */
+__device__ __forceinline__ int32_t stage_end(const SweepPlan& P, int32_t w, int32_t w1, int* r_out) {
+  int lo = 0, hi = P.nreps - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (P.off[mid] <= w) lo = mid; else hi = mid - 1;
+  }
+  *r_out = lo;
+  int32_t lim = min(w1, P.off[lo + 1]);
+  return P.dense[lo] ? w + 1 : min(lim, w + LPG_PLAIN_GROUP);
+}
+
+/* Per-agent phases of one 8-slot group, reading staged columns from smem. */
 template <int PHASE>
-__device__ __forceinline__ void sweep_chunk(SweepSmem& S, DevWorld& W, const ChunkCtx& cc, uint64_t st8) {
-  const DevRep* rp = cc.rp;
-  const int64_t cid = cc.cid;
-  const int o = threadIdx.x * LPG_SPT;
+__device__ __forceinline__ void sweep_slots(SweepSmem& S, DevWorld& W, const DevRep* rp, int64_t cid, int g, int fill,
+                                            int nbo, const uint8_t* stg, bool dense_layout, int o, uint64_t st8) {
   const int t = rp->cur_t;
-  const int ni = cc.g - rp->node_base;
+  const int ni = g - rp->node_base;
   const int do_vd = PHASE == 0 && rp->vd_tick;
   const int do_ds = PHASE == 0 && (rp->comps & LPG_COMP_DS);
   const int late = (PHASE == 0) == (rp->seed_n == 0);
   const int do_ri = late && rp->ri_tick;
   const int nsia = late ? rp->sia_n : 0;
-  const int fill = cc.fill;
-  if (o >= fill) return;
   const bool need = do_vd || do_ri || nsia > 0 || (do_ds && any_ei(st8));
   if (!need) return;
-  const int nbo = cc.nbo;
   const int64_t pos0 = cid * LPG_CHUNK + o;
-
-  /* dense per-tick columns, loaded only on the ticks that need them */
-  int32_t dod[LPG_SPT], dob[LPG_SPT];
-  int16_t rit[LPG_SPT];
-  uint8_t cmv[LPG_SPT];
-  if (do_vd) {
-    int4 a = *reinterpret_cast<const int4*>(W.dod + pos0);
-    int4 b = *reinterpret_cast<const int4*>(W.dod + pos0 + 4);
-    dod[0] = a.x; dod[1] = a.y; dod[2] = a.z; dod[3] = a.w;
-    dod[4] = b.x; dod[5] = b.y; dod[6] = b.z; dod[7] = b.w;
-  }
-  if (do_ri || nsia) {
-    uint64_t c8 = *reinterpret_cast<const uint64_t*>(W.cm + pos0);
-#pragma unroll
-    for (int j = 0; j < LPG_SPT; ++j) cmv[j] = (uint8_t)(c8 >> (8 * j));
-  }
-  if (do_ri) {
-    int4 a = *reinterpret_cast<const int4*>(W.ri + pos0);
-    const int16_t* pa = reinterpret_cast<const int16_t*>(&a);
-#pragma unroll
-    for (int j = 0; j < LPG_SPT; ++j) rit[j] = pa[j];
-  }
-  if (nsia) {
-    int4 a = *reinterpret_cast<const int4*>(W.dob + pos0);
-    int4 b = *reinterpret_cast<const int4*>(W.dob + pos0 + 4);
-    dob[0] = a.x; dob[1] = a.y; dob[2] = a.z; dob[3] = a.w;
-    dob[4] = b.x; dob[5] = b.y; dob[6] = b.z; dob[7] = b.w;
-  }
+  const int32_t* sdod = reinterpret_cast<const int32_t*>(stg + OFF_DOD);
+  int16_t* sri = const_cast<int16_t*>(reinterpret_cast<const int16_t*>(stg + OFF_RI));
+  const uint8_t* scm = stg + OFF_CM;
+  const int32_t* sdob = reinterpret_cast<const int32_t*>(stg + OFF_DOB);
+  (void)dense_layout;
   uint64_t out8 = st8;
   bool ri_dirty = false;
   const int nvalid = min(LPG_SPT, fill - o);
   for (int j = 0; j < nvalid; ++j) {
     const int64_t pos = pos0 + j;
+    const int q = o + j;
     int8_t s = (int8_t)(st8 >> (8 * j));
     const int8_t s_in = s;
-    int st = -1; /* strain, loaded on demand */
+    int st = -1;
     /* -- deaths (get_deaths) -------------------------------------------- */
-    if (do_vd && s >= 0 && (o + j) < nbo && dod[j] <= t) {
+    if (do_vd && s >= 0 && q < nbo && sdod[q] <= t) {
       atomicAdd(&S.ev[EV_DEATHS], 1);
       if (s == 0) {
         s_exit(S, W, pos, cid);
@@ -489,9 +523,9 @@ __device__ __forceinline__ void sweep_chunk(SweepSmem& S, DevWorld& W, const Chu
       }
     }
     /* -- routine immunisation (fast_ri) ------------------------------------ */
-    if (do_ri && s >= 0 && cmv[j] != 1) {
-      int32_t timer = (int32_t)rit[j] - rp->ri_step;
-      rit[j] = (int16_t)(uint16_t)(uint32_t)timer;
+    if (do_ri && s >= 0 && scm[q] != 1) {
+      int32_t timer = (int32_t)sri[q] - rp->ri_step;
+      sri[q] = (int16_t)(uint16_t)(uint32_t)timer;
       ri_dirty = true;
       bool eligible = false;
       if (t == rp->ri_step) eligible = timer <= 0 && timer >= -rp->ri_step;
@@ -503,7 +537,6 @@ __device__ __forceinline__ void sweep_chunk(SweepSmem& S, DevWorld& W, const Chu
           if (s == 0) {
             s = 1;
             W.strain[pos] = (int8_t)rp->ri_strain;
-            st = rp->ri_strain;
             atomicAdd(&S.ev[EV_RIPROT], 1);
             s_exit(S, W, pos, cid);
             atomicAdd(&S.tot[TT_E0 + rp->ri_strain], 1);
@@ -517,11 +550,11 @@ __device__ __forceinline__ void sweep_chunk(SweepSmem& S, DevWorld& W, const Chu
     }
     /* -- SIA campaigns of the day (fast_sia) ------------------------------- */
     for (int k = 0; k < nsia; ++k) {
-      if (s < 0 || cmv[j] == 1) break;
+      if (s < 0 || scm[q] == 1) break;
       const DevSia& ev = rp->sia[rp->sia_i0 + k];
-      int64_t age = (int64_t)t - (int64_t)dob[j];
-      if (!(ev.min_age <= age && age <= ev.max_age)) continue;
       if (ev.mask[ni] == 0) continue;
+      int64_t age = (int64_t)t - (int64_t)sdob[q];
+      if (!(ev.min_age <= age && age <= ev.max_age)) continue;
       double r = lpg_u01(rp->seed, LPG_P_SIA, t, W.ref[pos], 0, (uint64_t)k);
       double p = (double)rp->p_sia[ni];
       if (r < p) {
@@ -529,46 +562,44 @@ __device__ __forceinline__ void sweep_chunk(SweepSmem& S, DevWorld& W, const Chu
         if (s == 0 && r < p * ev.efficacy) {
           s = 1;
           W.strain[pos] = (int8_t)ev.strain;
-          st = ev.strain;
           atomicAdd(&S.ev[EV_SIAPROT0 + k], 1);
           s_exit(S, W, pos, cid);
           atomicAdd(&S.tot[TT_E0 + ev.strain], 1);
         }
       }
     }
-    if (s != s_in) {
-      out8 = (out8 & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)s << (8 * j));
-    }
+    if (s != s_in) out8 = (out8 & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)s << (8 * j));
   }
   if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
-  if (ri_dirty) {
-    int4 a;
-    int16_t* pa = reinterpret_cast<int16_t*>(&a);
-    const int4 old = *reinterpret_cast<const int4*>(W.ri + pos0);
-    const int16_t* po = reinterpret_cast<const int16_t*>(&old);
-#pragma unroll
-    for (int j = 0; j < LPG_SPT; ++j) pa[j] = (j < nvalid) ? rit[j] : po[j];
-    *reinterpret_cast<int4*>(W.ri + pos0) = a;
-  }
+  if (ri_dirty) *reinterpret_cast<int4*>(W.ri + pos0) = *reinterpret_cast<const int4*>(sri + o);
 }
 
 template <int PHASE>
 __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
+  extern __shared__ __align__(128) uint8_t sm_stage[];
   __shared__ SweepSmem S;
-  __shared__ int32_t s_off[1025];
-  __shared__ int32_t s_nreps;
-  const int R = W.n_reps;
+  __shared__ SweepPlan P;
+  __shared__ __align__(8) uint64_t full[LPG_NST];
+  __shared__ int s_abort;
+  const int R = W.n_reps < 1024 ? W.n_reps : 1024;
   if (threadIdx.x == 0) {
     int32_t acc = 0;
-    for (int r = 0; r < R && r < 1024; ++r) {
-      s_off[r] = acc;
+    for (int r = 0; r < R; ++r) {
+      P.off[r] = acc;
       const DevRep* rp = &W.reps[r];
       int work = rp->active;
       if (PHASE == 1) work = work && rp->seed_n > 0 && (rp->ri_tick || rp->sia_n > 0);
+      const int late = (PHASE == 0) == (rp->seed_n == 0);
+      P.cbase[r] = rp->chunk_base;
+      P.dense[r] = (PHASE == 0 && rp->vd_tick) || (late && (rp->ri_tick || rp->sia_n > 0));
       acc += work ? rp->used_chunks : 0;
     }
-    s_off[R < 1024 ? R : 1024] = acc;
-    s_nreps = R < 1024 ? R : 1024;
+    P.off[R] = acc;
+    P.total = acc;
+    P.nreps = R;
+    s_abort = 0;
+    for (int b = 0; b < LPG_NST; ++b) mbar_init(&full[b], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   {
     int k = threadIdx.x;
@@ -578,48 +609,95 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
     else if (k < EV_N + TT_N + 1 + LPG_MAX_STRAINS) S.bb[k - EV_N - TT_N - 1] = 0;
   }
   __syncthreads();
-  const int32_t total = s_off[s_nreps];
+  const int32_t total = P.total;
   if (total == 0) return;
   const int32_t per = (total + gridDim.x - 1) / gridDim.x;
   const int32_t w0 = blockIdx.x * per;
   const int32_t w1 = min(w0 + per, total);
+  if (w0 >= w1) return;
+
+  /* producer (thread 0): issue one stage starting at work item wp into buffer b */
+  int32_t wp = w0;
+  int issued = 0;
+  auto issue = [&](int b) {
+    int r;
+    const int32_t we = stage_end(P, wp, w1, &r);
+    const DevRep* rp = &W.reps[r];
+    const int64_t cid = P.cbase[r] + (wp - P.off[r]);
+    uint8_t* dst = sm_stage + (size_t)b * LPG_STAGE_BYTES;
+    uint32_t bytes = (uint32_t)(we - wp) * LPG_CHUNK;
+    if (P.dense[r]) {
+      const int late = (PHASE == 0) == (rp->seed_n == 0);
+      const bool vd = PHASE == 0 && rp->vd_tick;
+      const bool ri = late && rp->ri_tick;
+      const bool sia = late && rp->sia_n > 0;
+      bytes = LPG_CHUNK + (vd ? 4 * LPG_CHUNK : 0) + (ri ? 2 * LPG_CHUNK : 0) + ((ri || sia) ? LPG_CHUNK : 0) +
+              (sia ? 4 * LPG_CHUNK : 0);
+      mbar_expect_tx(&full[b], bytes);
+      bulk_g2s(dst + OFF_DS, W.ds + cid * LPG_CHUNK, LPG_CHUNK, &full[b]);
+      if (vd) bulk_g2s(dst + OFF_DOD, W.dod + cid * LPG_CHUNK, 4 * LPG_CHUNK, &full[b]);
+      if (ri) bulk_g2s(dst + OFF_RI, W.ri + cid * LPG_CHUNK, 2 * LPG_CHUNK, &full[b]);
+      if (ri || sia) bulk_g2s(dst + OFF_CM, W.cm + cid * LPG_CHUNK, LPG_CHUNK, &full[b]);
+      if (sia) bulk_g2s(dst + OFF_DOB, W.dob + cid * LPG_CHUNK, 4 * LPG_CHUNK, &full[b]);
+    } else {
+      mbar_expect_tx(&full[b], bytes);
+      bulk_g2s(dst, W.ds + cid * LPG_CHUNK, bytes, &full[b]);
+    }
+    wp = we;
+    ++issued;
+  };
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < LPG_NST && wp < w1; ++b) issue(b);
+  }
+
   int cur_g = -1;
   const int o = threadIdx.x * LPG_SPT;
-
-  for (int32_t wb = w0; wb < w1; wb += LPG_SWEEP_UNROLL) {
-    ChunkCtx cc[LPG_SWEEP_UNROLL];
-    uint64_t st8[LPG_SWEEP_UNROLL];
-#pragma unroll
-    for (int u = 0; u < LPG_SWEEP_UNROLL; ++u) {
-      const int32_t w = wb + u;
-      cc[u].fill = 0;
-      cc[u].g = -1;
-      st8[u] = ~0ULL;
-      if (w < w1) {
-        int lo = 0, hi = s_nreps - 1;
-        while (lo < hi) {
-          int mid = (lo + hi + 1) >> 1;
-          if (s_off[mid] <= w) lo = mid; else hi = mid - 1;
-        }
-        const DevRep* rp = &W.reps[lo];
-        const int64_t cid = rp->chunk_base + (w - s_off[lo]);
-        cc[u].rp = rp;
-        cc[u].cid = cid;
-        cc[u].g = W.chunk_node[cid];
-        cc[u].fill = W.chunk_fill[cid];
-        cc[u].nbo = (W.chunk_nbt[cid] == rp->cur_t) ? W.chunk_nbo[cid] : LPG_CHUNK;
-        if (o < cc[u].fill) st8[u] = *reinterpret_cast<const uint64_t*>(W.ds + cid * LPG_CHUNK + o);
-      }
-    }
-#pragma unroll 1
-    for (int u = 0; u < LPG_SWEEP_UNROLL; ++u) {
-      if (wb + u >= w1) break;
-      if (cc[u].g != cur_g) {
+  int32_t wc = w0;
+  for (int32_t i = 0; wc < w1; ++i) {
+    const int b = i % LPG_NST;
+    const uint32_t parity = (uint32_t)(i / LPG_NST) & 1u;
+    int r;
+    const int32_t we = stage_end(P, wc, w1, &r);
+    if (!mbar_wait(&full[b], parity)) atomicExch(&s_abort, 1);
+    __syncthreads();
+    if (s_abort) break;
+    const DevRep* rp = &W.reps[r];
+    const uint8_t* stg = sm_stage + (size_t)b * LPG_STAGE_BYTES;
+    const bool dense = P.dense[r];
+    for (int32_t w = wc; w < we; ++w) {
+      const int64_t cid = P.cbase[r] + (w - P.off[r]);
+      const int g = W.chunk_node[cid];
+      if (g != cur_g) {
         sweep_flush(S, W, cur_g);
-        cur_g = cc[u].g;
+        cur_g = g;
       }
-      sweep_chunk<PHASE>(S, W, cc[u], st8[u]);
+      const int fill = W.chunk_fill[cid];
+      if (o < fill) {
+        const int nbo = (W.chunk_nbt[cid] == rp->cur_t) ? W.chunk_nbo[cid] : LPG_CHUNK;
+        const uint8_t* cst = dense ? stg : stg + (size_t)(w - wc) * LPG_CHUNK;
+        const uint64_t st8 = *reinterpret_cast<const uint64_t*>(cst + o);
+        sweep_slots<PHASE>(S, W, rp, cid, g, fill, nbo, stg, dense, o, st8);
+      }
     }
+    wc = we;
+    __syncthreads();
+    if (threadIdx.x == 0 && wp < w1) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(b);
+    }
+  }
+  if (s_abort) {
+    /* leave no bulk copy in flight into this CTA's shared memory */
+    if (threadIdx.x == 0) {
+      W.reps[0].error = LPG_ERR_TIMEOUT;
+      for (int b = 0; b < LPG_NST; ++b) {
+        for (long long it = 0; it < LPG_MBAR_SPIN; ++it) {
+          if (mbar_try_wait(&full[b], 0) || mbar_try_wait(&full[b], 1)) break;
+        }
+      }
+    }
+    __syncthreads();
+    return;
   }
   sweep_flush(S, W, cur_g);
 }
@@ -788,9 +866,13 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
 
 /* ------------------------------------------------------------------------ */
 /* Node-level force of infection and exposure counts; same arithmetic, in
- * the same order, as the oracle's lpo_node_tx. */
+ * the same order, as the oracle's lpo_node_tx.  One warp per node: lane l
+ * accumulates the incoming infectivity of source nodes l, l+32, ... from the
+ * transposed network row (contiguous), then lane 0 adds the 32 partial sums
+ * in lane order. */
 __global__ void k_node_tx(DevWorld W) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (g >= W.G) return;
   DevRep* rp = &W.reps[W.node_rep[g]];
   if (!rp->active) return;
@@ -801,24 +883,37 @@ __global__ void k_node_tx(DevWorld W) {
     const int32_t* pop1 = RES(rp, RS_POP, t - 1);
     pop_t = pop1[i];
     if (rp->vd_tick) pop_t = pop_t + W.ev[(int64_t)EV_BIRTHS * G + g] - W.ev[(int64_t)EV_DEATHS * G + g];
-    RES(rp, RS_POP, t)[i] = pop_t;
+    if (lane == 0) RES(rp, RS_POP, t)[i] = pop_t;
   } else {
     pop_t = RES(rp, RS_POP, t)[i];
   }
-  W.size[g] = 0;
-  W.uniq[g] = 0;
+  if (lane == 0) {
+    W.size[g] = 0;
+    W.uniq[g] = 0;
+  }
   if (!(rp->comps & LPG_COMP_TX)) return;
+  const double* nrow = rp->net_t + (int64_t)i * n; /* nrow[ii] = network[ii][i] */
+  double part[LPG_MAX_STRAINS] = {0.0, 0.0, 0.0, 0.0};
+  for (int ii = lane; ii < n; ii += 32) {
+    const double w = nrow[ii];
+    for (int k = 0; k < ns; ++k) part[k] = part[k] + ((double)W.bb[(int64_t)k * G + nb + ii] * 0x1.0p-32) * w;
+  }
+  double inc[LPG_MAX_STRAINS];
+  for (int k = 0; k < ns; ++k) {
+    double acc = 0.0;
+    for (int l = 0; l < 32; ++l) acc = acc + __shfl_sync(FULLMASK, part[k], l);
+    inc[k] = acc;
+  }
+  if (lane != 0) return;
   double p[LPG_MAX_STRAINS];
   double total_p = 0.0;
   int local_zero = 1;
   const double rowsum = rp->rowsum[i];
   for (int k = 0; k < ns; ++k) {
-    const uint64_t* Bk = W.bb + (int64_t)k * G + nb;
-    if (Bk[i] != 0) local_zero = 0;
-    double inc = 0.0;
-    for (int ii = 0; ii < n; ++ii) inc = inc + ((double)Bk[ii] * 0x1.0p-32) * rp->net[(int64_t)ii * n + i];
-    double bpre = (double)Bk[i] * 0x1.0p-32;
-    double beta = bpre + (inc - bpre * rowsum);
+    const uint64_t bk = W.bb[(int64_t)k * G + g];
+    if (bk != 0) local_zero = 0;
+    double bpre = (double)bk * 0x1.0p-32;
+    double beta = bpre + (inc[k] - bpre * rowsum);
     beta = (beta * rp->seas[t]) * rp->r0s[i];
     double denom = (double)(pop_t > 1 ? pop_t : 1);
     double rate = beta / denom;
@@ -979,23 +1074,40 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
       }
       if (a > st[i]) v -= cp[a - 1];
       const int64_t cid = ls[a];
-      int sb = 0;
-      for (; sb < LPG_NSUB; ++sb) {
-        uint64_t w = W.sub_w[cid * LPG_NSUB + sb];
-        if (w > v) break;
-        v -= w;
+      /* sub-block: the 16 totals in one round trip */
+      uint64_t swv[LPG_NSUB];
+#pragma unroll
+      for (int k = 0; k < LPG_NSUB; ++k) swv[k] = W.sub_w[cid * LPG_NSUB + k];
+      int sb = LPG_NSUB;
+#pragma unroll
+      for (int k = 0; k < LPG_NSUB; ++k) {
+        if (sb == LPG_NSUB) {
+          if (swv[k] > v) sb = k;
+          else v -= swv[k];
+        }
       }
       uint32_t hit = LPG_NONE;
       if (sb < LPG_NSUB) {
+        /* slots: 128 state bytes as 8 x 16 B, then risks 32 at a time */
         const int64_t p0 = cid * LPG_CHUNK + (int64_t)sb * LPG_SUB;
-        for (int k = 0; k < LPG_SUB; ++k) {
-          if (W.ds[p0 + k] != 0) continue;
-          uint64_t w = fix_risk(W.risk[p0 + k]);
-          if (w > v) {
-            hit = (uint32_t)(p0 + k);
-            break;
+        uint4 sv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) sv[k] = reinterpret_cast<const uint4*>(W.ds + p0)[k];
+        for (int grp = 0; grp < 4 && hit == LPG_NONE; ++grp) {
+          float4 rv[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) rv[k] = reinterpret_cast<const float4*>(W.risk + p0 + grp * 32)[k];
+          const uint32_t* sw32 = reinterpret_cast<const uint32_t*>(&sv[grp * 2]);
+#pragma unroll
+          for (int k = 0; k < 32; ++k) {
+            if (hit != LPG_NONE) break;
+            const uint32_t sbyte = (sw32[k >> 2] >> (8 * (k & 3))) & 0xffu;
+            if (sbyte != 0) continue;
+            const float rk = reinterpret_cast<const float*>(rv)[k];
+            const uint64_t w = fix_risk(rk);
+            if (w > v) hit = (uint32_t)(p0 + grp * 32 + k);
+            else v -= w;
           }
-          v -= w;
         }
       }
       if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;

@@ -603,8 +603,14 @@ void lpo_node_tx(int n, int ns, const uint64_t* B, const uint64_t* SW, const int
     int local_zero = 1;
     for (int k = 0; k < ns; ++k) {
       if (B[(size_t)nd * ns + k] != 0) local_zero = 0;
+      /* incoming infectivity sum_i beta_i N[i][nd], associated as 32
+       * interleaved partial sums (i = l, l+32, ...) added in lane order */
       double inc = 0.0;
-      for (int i = 0; i < n; ++i) inc = inc + ((double)B[(size_t)i * ns + k] * 0x1.0p-32) * net[(size_t)i * n + nd];
+      for (int l = 0; l < 32; ++l) {
+        double part = 0.0;
+        for (int i = l; i < n; i += 32) part = part + ((double)B[(size_t)i * ns + k] * 0x1.0p-32) * net[(size_t)i * n + nd];
+        inc = inc + part;
+      }
       double rowsum = 0.0;
       for (int j = 0; j < n; ++j) rowsum = rowsum + net[(size_t)nd * n + j];
       double bpre = (double)B[(size_t)nd * ns + k] * 0x1.0p-32;
