@@ -21,8 +21,8 @@
 
 namespace {
 
-const char* kKernelNames[] = {"k_begin", "k_newborns", "k_sweep_a", "k_seed", "k_sweep_b", "k_node_tx", "k_select", "k_end"};
-constexpr int kNumTickKernels = 8;
+const char* kKernelNames[] = {"k_begin", "k_newborns", "k_sweep_a", "k_dsq", "k_seed", "k_sweep_b", "k_node_tx", "k_select", "k_end"};
+constexpr int kNumTickKernels = 9;
 constexpr int kTicksPerGraph = 8;
 
 /* Reference-ordered columns of one simulation on the device. */
@@ -64,8 +64,8 @@ struct lpg_handle {
   cudaGraphExec_t graph = nullptr;
   bool graph_failed = false;
   bool profiling = false;
-  double prof_ms[kNumTickKernels] = {0};
-  int64_t prof_n[kNumTickKernels] = {0};
+  double prof_ms[16] = {0};
+  int64_t prof_n[16] = {0};
   std::vector<cudaEvent_t> ev_pool;
   int64_t launches = 0;
   int sm_count = 0;
@@ -174,7 +174,8 @@ __global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used
        q += (int64_t)gridDim.x * blockDim.x) {
     int64_t cid = chunk_base + q / LPG_CHUNK;
     int o = (int)(q % LPG_CHUNK);
-    if (o >= W.chunk_fill[cid]) continue;
+    const int4 meta = W.cmeta[cid];
+    if (o >= meta.y) continue;
     int64_t pos = cid * LPG_CHUNK + o;
     uint32_t i = W.ref[pos];
     s.ds[i] = W.ds[pos];
@@ -186,7 +187,7 @@ __global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used
     s.par[i] = W.par[pos];
     s.ipv[i] = W.ipv[pos];
     s.cm[i] = W.cm[pos];
-    s.node[i] = (int16_t)(W.chunk_node[cid] - node_base);
+    s.node[i] = (int16_t)(meta.x - node_base);
     s.ri[i] = W.ri[pos];
     s.risk[i] = W.risk[pos];
     s.inf[i] = W.inf[pos];
@@ -230,7 +231,7 @@ static const int res_wide[RS_N] = {0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 
 extern "C" int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t device, lpg_handle** out) {
   if (!out) return LPG_ERR_ARG;
   *out = nullptr;
-  if (!sims || n_sims < 1 || n_sims > 1024) return LPG_ERR_ARG;
+  if (!sims || n_sims < 1 || n_sims > LPG_MAX_REPS) return LPG_ERR_ARG;
   lpg_handle* h = new lpg_handle();
   *out = h;
   h->device = device;
@@ -471,10 +472,8 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.dob, P);
   rc |= dalloc(h, &W.dod, P);
   rc |= dalloc(h, &W.ref, P);
-  rc |= dalloc(h, &W.chunk_node, chunk_total);
-  rc |= dalloc(h, &W.chunk_fill, chunk_total);
-  rc |= dalloc(h, &W.chunk_nbt, chunk_total);
-  rc |= dalloc(h, &W.chunk_nbo, chunk_total);
+  rc |= dalloc(h, &W.cmeta, chunk_total);
+  rc |= dalloc(h, &W.dsq_n, 1);
   rc |= dalloc(h, &W.chunk_w, chunk_total);
   rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.cpref, chunk_total);
@@ -506,10 +505,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   if (rc) return LPG_ERR_NOMEM;
   CK(cudaMemsetAsync(W.ds, 0xff, P, st));
   CK(cudaMemsetAsync(W.ref, 0xff, P * 4, st));
-  CK(cudaMemsetAsync(W.chunk_node, 0xff, sizeof(int32_t) * chunk_total, st));
-  CK(cudaMemsetAsync(W.chunk_fill, 0, sizeof(int32_t) * chunk_total, st));
-  CK(cudaMemsetAsync(W.chunk_nbt, 0xff, sizeof(int32_t) * chunk_total, st));
-  CK(cudaMemsetAsync(W.chunk_nbo, 0, sizeof(int32_t) * chunk_total, st));
+  CK(cudaMemsetAsync(W.dsq_n, 0, 4, st));
   CK(cudaMemsetAsync(W.ev, 0, sizeof(int32_t) * EV_N * G, st));
   CK(cudaMemsetAsync(W.tot, 0, sizeof(int32_t) * TT_N * G, st));
   CK(cudaMemsetAsync(W.sw, 0, sizeof(uint64_t) * G, st));
@@ -521,7 +517,8 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaMemsetAsync(W.abort_flag, 0, 4, st));
 
   /* 4. per-simulation static data, results, pools, chunk tables */
-  std::vector<int32_t> h_node_rep(G), h_chunk_node(chunk_total, -1), h_chunk_fill(chunk_total, 0), h_csr(chunk_total, 0),
+  std::vector<int4> h_meta(chunk_total, make_int4(-1, 0, -1, 0));
+  std::vector<int32_t> h_node_rep(G), h_csr(chunk_total, 0),
       h_start(csr_total, 0);
   std::vector<int64_t> h_node_count(G);
   for (int r = 0; r < R; ++r) {
@@ -678,8 +675,7 @@ extern "C" int lpg_start(lpg_handle* h) {
       h_node_count[rp.node_base + i] = counts[r][i];
       h_start[rp.csr_base + i] = csr_start[r][i];
       for (int32_t k = csr_start[r][i]; k < csr_start[r][i + 1]; ++k, ++c) {
-        h_chunk_node[rp.chunk_base + c] = rp.node_base + i;
-        h_chunk_fill[rp.chunk_base + c] = chunk_fill_init[r][c];
+        h_meta[rp.chunk_base + c] = make_int4(rp.node_base + i, chunk_fill_init[r][c], -1, 0);
         h_csr[rp.chunk_base + k] = rp.chunk_base + c;
       }
     }
@@ -687,8 +683,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   }
   CK(cudaMemcpyAsync(W.node_rep, h_node_rep.data(), sizeof(int32_t) * G, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(W.node_count, h_node_count.data(), sizeof(int64_t) * G, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(W.chunk_node, h_chunk_node.data(), sizeof(int32_t) * chunk_total, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(W.chunk_fill, h_chunk_fill.data(), sizeof(int32_t) * chunk_total, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(W.cmeta, h_meta.data(), sizeof(int4) * chunk_total, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(W.node_chunks[0], h_csr.data(), sizeof(int32_t) * chunk_total, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(W.node_chunk_start[0], h_start.data(), sizeof(int32_t) * csr_total, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(W.reps, hr.data(), sizeof(DevRep) * R, cudaMemcpyHostToDevice, st));
@@ -765,12 +760,13 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
   }
   switch (k) {
     case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
-    case 1: k_newborns<<<dim3(64, R), 256, 0, st>>>(W); break;
+    case 1: k_newborns<<<dim3(h->sm_count * 2, R), 256, 0, st>>>(W); break;
     case 2: k_sweep<0><<<h->sweep_blocks, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 3: k_seed<<<R, 1024, 0, st>>>(W); break;
-    case 4: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 5: k_node_tx<<<(G * 32 + 255) / 256, 256, 0, st>>>(W); break;
-    case 6: {
+    case 3: k_dsq<<<h->sm_count * 8, 256, 0, st>>>(W); break;
+    case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
+    case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM, st>>>(W); break;
+    case 6: k_node_tx<<<(G * 32 + 255) / 256, 256, 0, st>>>(W); break;
+    case 7: {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(h->select_blocks);
       cfg.blockDim = dim3(256);
@@ -784,7 +780,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
       CK(cudaLaunchKernelEx(&cfg, k_select, W));
       break;
     }
-    case 7: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
+    case 8: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
   }
   CK(cudaGetLastError());
   if (timed) CK(cudaEventRecord(e1, st));

@@ -37,6 +37,7 @@
 #define LPG_NSUB (LPG_CHUNK / LPG_SUB)
 #define LPG_SWEEP_THREADS 256
 #define LPG_SPT (LPG_CHUNK / LPG_SWEEP_THREADS) /* slots per thread = 8 */
+#define LPG_MAX_REPS 256
 
 /* per-tick event counters per node */
 enum {
@@ -155,10 +156,7 @@ typedef struct {
   int32_t *dob, *dod;
   uint32_t* ref;
   /* per chunk */
-  int32_t* chunk_node;
-  int32_t* chunk_fill;
-  int32_t* chunk_nbt; /* tick of the newborns written into the chunk */
-  int32_t* chunk_nbo; /* offset of the first of them */
+  int4* cmeta; /* per chunk: x node, y fill, z tick of the newborns written into it, w offset of the first */
   uint64_t* chunk_w;  /* susceptible weight total */
   uint64_t* sub_w;    /* [chunk][LPG_NSUB] */
   uint64_t* cpref;    /* selection scratch, CSR order */
@@ -178,8 +176,9 @@ typedef struct {
   int64_t* uniq;
   int64_t* ksel;
   int64_t* tgt_off; /* [G + 1] */
-  uint32_t* hits;
+  uint32_t* hits; /* selection targets; also the queue of E/I positions of the tick */
   int64_t hits_cap;
+  uint32_t* dsq_n; /* entries in that queue */
   /* grid barrier of the cooperative selection kernel */
   uint32_t* bar_count;
   uint32_t* bar_gen;

@@ -8,12 +8,13 @@
  *                counters, births per node (model.py:1711-1716) and their
  *                chunk placement
  *   k_newborns   newborn rows (model.py:1719-1730)
- *   k_sweep<0>   fused sweep over every chunk: deaths (get_deaths,
- *                model.py:1767-1781), disease progression and paralysis
- *                (model.py:393-454), RI (fast_ri, :1784-1855) and SIA
- *                (fast_sia, :1994-2060); on seed ticks RI/SIA wait for ...
- *   k_seed       ... the seed schedule (model.py:759-786) and ...
- *   k_sweep<1>   ... run after it
+ *   k_sweep<0>   sweep over every chunk: deaths (get_deaths,
+ *                model.py:1767-1781) and the queue of agents in E or I
+ *   k_dsq        disease progression and paralysis of the queued agents
+ *                (model.py:393-454)
+ *   k_seed       the seed schedule (model.py:759-786)
+ *   k_sweep<1>   RI (fast_ri, :1784-1855) and SIA (fast_sia, :1994-2060)
+ *                on the ticks that have them
  *   k_node_tx    per node: population (model.py:1751-1755), mixing,
  *                seasonality, probabilities and exposure counts
  *                (model.py:1327-1407)
@@ -110,6 +111,7 @@ __global__ void k_begin(DevWorld W) {
   DevRep* rp = &W.reps[blockIdx.x];
   __shared__ int s_active, s_vd, s_t;
   __shared__ unsigned long long s_sum;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *W.dsq_n = 0;
   if (threadIdx.x == 0) {
     int t = rp->t;
     int active = rp->started && !rp->error && !rp->stopped && t >= 1 && t < rp->nt;
@@ -215,9 +217,7 @@ __global__ void k_begin(DevWorld W) {
       for (int k = lane; k < added; k += 32) {
         int32_t cid = rp->chunk_base + rp->used_chunks + (int32_t)W.ksel[nb + i] + k;
         ln[d0 + (a1 - a0) + k] = cid;
-        W.chunk_node[cid] = nb + i;
-        W.chunk_fill[cid] = 0;
-        W.chunk_nbt[cid] = -1;
+        W.cmeta[cid] = make_int4(nb + i, 0, -1, 0);
         W.chunk_w[cid] = 0;
         for (int s = 0; s < LPG_NSUB; ++s) W.sub_w[(int64_t)cid * LPG_NSUB + s] = 0;
       }
@@ -236,9 +236,8 @@ __global__ void k_begin(DevWorld W) {
     for (int64_t k = li0 / LPG_CHUNK; k <= (newc - 1) / LPG_CHUNK; ++k) {
       int32_t cid = ls[st[i] + k];
       int64_t f = newc - k * LPG_CHUNK;
-      W.chunk_fill[cid] = (int32_t)(f < LPG_CHUNK ? f : LPG_CHUNK);
-      W.chunk_nbt[cid] = t;
-      W.chunk_nbo[cid] = (k == li0 / LPG_CHUNK) ? (int32_t)(li0 % LPG_CHUNK) : 0;
+      W.cmeta[cid] = make_int4(nb + i, (int32_t)(f < LPG_CHUNK ? f : LPG_CHUNK), t,
+                               (k == li0 / LPG_CHUNK) ? (int32_t)(li0 % LPG_CHUNK) : 0);
     }
     W.node_count[g] = newc;
   }
@@ -354,25 +353,32 @@ __device__ __forceinline__ bool any_ei(uint64_t x) {
   return m != 0;
 }
 
-/* Fused sweep.  PHASE 0 does deaths and disease progression, plus RI/SIA
- * unless a seed event falls on the tick; PHASE 1 does RI/SIA on seed ticks.
+/* Fused sweep over every agent slot, in two launches per tick.
+ *   PHASE 0: deaths (get_deaths, model.py:1767-1781) on VD ticks, and the
+ *            queue of agents in E or I for disease progression (k_dsq).
+ *   PHASE 1: routine immunisation (fast_ri, model.py:1784-1855) and SIA
+ *            campaigns (fast_sia, :1994-2060), on the ticks that have them,
+ *            after progression and the seed schedule as in default_run_order.
  *
  * Each CTA owns a contiguous range of chunks (consecutive chunks mostly share
- * a node, so node counters flush rarely).  The columns every agent needs are
- * staged into shared memory with 1-D bulk copies (cp.async.bulk, completion
- * on an mbarrier) through a ring of LPG_NST stages, issued LPG_NST stages
- * ahead of the consumers: on plain ticks a stage holds the state bytes of up
- * to LPG_PLAIN_GROUP chunks; on ticks with deaths, RI or SIA it holds one
- * chunk's state plus the dense columns of that tick (date_of_death,
- * ri_timer + chronically_missed, date_of_birth).  Columns needed only by
- * E/I agents (timers, strain, flags, infectivity) are read from global
- * memory for those agents alone.  Every mbarrier wait is bounded. */
+ * a node, so node counters flush rarely).  Chunk metadata and the columns
+ * every agent needs are staged into shared memory with 1-D bulk copies
+ * (cp.async.bulk, completion on an mbarrier) through a ring of LPG_NST
+ * stages issued ahead of the consumers: on ticks without dense work a stage
+ * holds up to LPG_PLAIN_GROUP chunks' state bytes; otherwise one chunk's
+ * state plus the dense columns of the tick (date_of_death; ri_timer and
+ * chronically_missed; date_of_birth).  The producer reads only shared
+ * memory.  Each thread handles 8 consecutive slots: masks are computed from
+ * vector shared-memory loads, and only the slots with an event take the
+ * scalar path.  Every mbarrier wait is bounded. */
 #define LPG_NST 4
-#define LPG_STAGE_BYTES (24 * 1024)
-#define LPG_PLAIN_GROUP (LPG_STAGE_BYTES / LPG_CHUNK)
+#define LPG_META_BYTES 256
+#define LPG_COL_BYTES (24 * 1024)
+#define LPG_STAGE_BYTES (LPG_META_BYTES + LPG_COL_BYTES)
+#define LPG_PLAIN_GROUP (LPG_COL_BYTES / LPG_CHUNK)
 #define LPG_SWEEP_SMEM (LPG_NST * LPG_STAGE_BYTES)
 #define LPG_MBAR_SPIN (1LL << 24)
-/* dense stage layout (bytes) */
+/* dense stage layout (bytes after the metadata block) */
 #define OFF_DS 0
 #define OFF_DOD 2048
 #define OFF_RI (2048 + 8192)
@@ -409,11 +415,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+/* per-simulation flags of the launch, cached in shared memory */
+enum { SF_WORK = 1, SF_DENSE = 2, SF_VD = 4, SF_DS = 8, SF_RI = 16, SF_SIA = 32 };
+
 struct SweepPlan {
   int32_t total, nreps;
-  int32_t off[1025];   /* work-item offsets per simulation */
-  int32_t cbase[1024]; /* first chunk id per simulation */
-  uint8_t dense[1024]; /* 1 when the simulation's tick needs dense columns */
+  int32_t off[LPG_MAX_REPS + 1]; /* work-item offsets per simulation */
+  int32_t cbase[LPG_MAX_REPS];   /* first chunk id per simulation */
+  int32_t tick[LPG_MAX_REPS];
+  uint8_t flags[LPG_MAX_REPS];
 };
 
 /* End of the stage that starts at work item w (same answer on every thread). */
@@ -424,50 +434,90 @@ __device__ __forceinline__ int32_t stage_end(const SweepPlan& P, int32_t w, int3
     if (P.off[mid] <= w) lo = mid; else hi = mid - 1;
   }
   *r_out = lo;
-  int32_t lim = min(w1, P.off[lo + 1]);
-  return P.dense[lo] ? w + 1 : min(lim, w + LPG_PLAIN_GROUP);
+  const int32_t lim = min(w1, P.off[lo + 1]);
+  return (P.flags[lo] & SF_DENSE) ? w + 1 : min(lim, w + LPG_PLAIN_GROUP);
 }
 
-/* Per-agent phases of one 8-slot group, reading staged columns from smem. */
-template <int PHASE>
-__device__ __forceinline__ void sweep_slots(SweepSmem& S, DevWorld& W, const DevRep* rp, int64_t cid, int g, int fill,
-                                            int nbo, const uint8_t* stg, bool dense_layout, int o, uint64_t st8) {
-  const int t = rp->cur_t;
-  const int ni = g - rp->node_base;
-  const int do_vd = PHASE == 0 && rp->vd_tick;
-  const int do_ds = PHASE == 0 && (rp->comps & LPG_COMP_DS);
-  const int late = (PHASE == 0) == (rp->seed_n == 0);
-  const int do_ri = late && rp->ri_tick;
-  const int nsia = late ? rp->sia_n : 0;
-  const bool need = do_vd || do_ri || nsia > 0 || (do_ds && any_ei(st8));
-  if (!need) return;
+/* Byte mask (bit j for byte j) of the bytes of x equal to 1 or 2. */
+__device__ __forceinline__ uint32_t ei_bits(uint64_t x) {
+  uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+  uint32_t a = __vcmpltu4(__vsub4(lo, 0x01010101u), 0x02020202u);
+  uint32_t b = __vcmpltu4(__vsub4(hi, 0x01010101u), 0x02020202u);
+  uint32_t m = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    m |= ((a >> (8 * j + 7)) & 1u) << j;
+    m |= ((b >> (8 * j + 7)) & 1u) << (j + 4);
+  }
+  return m;
+}
+/* Byte mask of the non-negative (alive) bytes of x. */
+__device__ __forceinline__ uint32_t alive_bits(uint64_t x) {
+  uint32_t m = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) m |= ((uint32_t)((x >> (8 * j + 7)) & 1u) ^ 1u) << j;
+  return m;
+}
+__device__ __forceinline__ uint64_t set_byte(uint64_t x, int j, int8_t v) {
+  return (x & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)v << (8 * j));
+}
+
+/* Append the positions of the set bits of m (slots pos0 + j) to the E/I
+ * queue: one atomic per warp.  Called by all 32 lanes. */
+__device__ __forceinline__ void dsq_append(DevWorld& W, uint32_t m, int64_t pos0) {
+  if (__ballot_sync(FULLMASK, m != 0) == 0) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t c = __popc(m);
+  uint32_t x = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(FULLMASK, x, o);
+    if (lane >= o) x += y;
+  }
+  const uint32_t tot = __shfl_sync(FULLMASK, x, 31);
+  uint32_t base = 0;
+  if (lane == 31) base = atomicAdd(W.dsq_n, tot);
+  base = __shfl_sync(FULLMASK, base, 31);
+  uint32_t at = base + x - c;
+  while (m) {
+    const int j = __ffs(m) - 1;
+    m &= m - 1;
+    W.hits[at++] = (uint32_t)(pos0 + j);
+  }
+}
+
+/* One thread's 8 slots (pos0 .. pos0+7), PHASE 0: deaths; returns the mask
+ * of slots in E or I after them (the agents progression must visit). */
+__device__ __forceinline__ uint32_t sweep_slots_a(SweepSmem& S, DevWorld& W, const DevRep* rp, uint8_t fl, int t,
+                                              int64_t cid, int nbo, int o, uint64_t st8, const uint8_t* cols,
+                                              uint32_t valid) {
   const int64_t pos0 = cid * LPG_CHUNK + o;
-  const int32_t* sdod = reinterpret_cast<const int32_t*>(stg + OFF_DOD);
-  int16_t* sri = const_cast<int16_t*>(reinterpret_cast<const int16_t*>(stg + OFF_RI));
-  const uint8_t* scm = stg + OFF_CM;
-  const int32_t* sdob = reinterpret_cast<const int32_t*>(stg + OFF_DOB);
-  (void)dense_layout;
+  uint32_t alive = alive_bits(st8) & valid;
+  uint32_t ei = ei_bits(st8) & valid;
   uint64_t out8 = st8;
-  bool ri_dirty = false;
-  const int nvalid = min(LPG_SPT, fill - o);
-  for (int j = 0; j < nvalid; ++j) {
-    const int64_t pos = pos0 + j;
-    const int q = o + j;
-    int8_t s = (int8_t)(st8 >> (8 * j));
-    const int8_t s_in = s;
-    int st = -1;
-    /* -- deaths (get_deaths) -------------------------------------------- */
-    if (do_vd && s >= 0 && q < nbo && sdod[q] <= t) {
+  if (fl & SF_VD) {
+    const int4* d4 = reinterpret_cast<const int4*>(cols + OFF_DOD) + (o >> 2);
+    const int4 a = d4[0], b = d4[1];
+    const int32_t dd[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    uint32_t dead = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) dead |= (uint32_t)(dd[j] <= t && (o + j) < nbo) << j;
+    dead &= alive;
+    while (dead) {
+      const int j = __ffs(dead) - 1;
+      dead &= dead - 1;
+      const int64_t pos = pos0 + j;
+      const int8_t s = (int8_t)(st8 >> (8 * j));
       atomicAdd(&S.ev[EV_DEATHS], 1);
       if (s == 0) {
         s_exit(S, W, pos, cid);
       } else if (s == 1 || s == 2) {
-        st = W.strain[pos];
+        const int st = W.strain[pos];
         if (s == 1) {
           atomicAdd(&S.tot[TT_E0 + st], -1);
         } else {
           atomicAdd(&S.tot[TT_I0 + st], -1);
-          uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
           if (bw) atomicAdd(&S.bb[st], neg64(bw));
         }
       } else if (s == 3) {
@@ -475,103 +525,98 @@ __device__ __forceinline__ void sweep_slots(SweepSmem& S, DevWorld& W, const Dev
       }
       if (W.pp[pos] == 1) atomicAdd(&S.tot[TT_POTP], -1);
       if (W.par[pos] == 1) atomicAdd(&S.tot[TT_P], -1);
-      s = -1;
+      out8 = set_byte(out8, j, -1);
+      ei &= ~(1u << j);
     }
-    /* -- disease progression (disease_state_step_kernel) ------------------ */
-    if (do_ds) {
-      if (s == 1) {
-        int8_t e = W.et[pos];
-        if (st < 0) st = W.strain[pos];
-        if (e <= 0) {
-          s = 2;
-          atomicAdd(&S.tot[TT_E0 + st], -1);
-          atomicAdd(&S.tot[TT_I0 + st], 1);
-          uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-          if (bw) atomicAdd(&S.bb[st], (unsigned long long)bw);
-        }
-        W.et[pos] = dec_i8(e);
-      }
-      if (s == 2) {
-        int8_t i = W.it[pos];
-        if (st < 0) st = W.strain[pos];
-        if (i <= 0) {
-          s = 3;
-          atomicAdd(&S.tot[TT_I0 + st], -1);
-          atomicAdd(&S.tot[TT_R], 1);
-          uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-          if (bw) atomicAdd(&S.bb[st], neg64(bw));
-        }
-        W.it[pos] = dec_i8(i);
-        if (st == 0) {
-          int8_t p = W.pt[pos];
-          if (p <= 0 && W.pp[pos] == -1) {
-            if (W.ipv[pos] == 0) {
-              W.pp[pos] = 1;
-              atomicAdd(&S.tot[TT_POTP], 1);
-              atomicAdd(&S.ev[EV_NEWPOT], 1);
-              if (lpg_u01(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < (double)rp->p_par) {
-                W.par[pos] = 1;
-                atomicAdd(&S.tot[TT_P], 1);
-                atomicAdd(&S.ev[EV_NEWPAR], 1);
-              }
-            } else {
-              W.pp[pos] = 0;
-            }
-          }
-          W.pt[pos] = dec_i8(p);
-        }
-      }
+    if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
+  }
+  return ei;
+}
+
+/* One thread's 8 slots, PHASE 1: RI then the SIA campaigns of the day. */
+__device__ __forceinline__ void sweep_slots_b(SweepSmem& S, DevWorld& W, const DevRep* rp, uint8_t fl, int t,
+                                              int64_t cid, int ni, int o, uint64_t st8, const uint8_t* cols,
+                                              uint32_t valid) {
+  const int64_t pos0 = cid * LPG_CHUNK + o;
+  uint32_t alive = alive_bits(st8) & valid;
+  const uint64_t c8 = *reinterpret_cast<const uint64_t*>(cols + OFF_CM + o);
+  uint32_t reach = alive;
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    if (((c8 >> (8 * j)) & 0xffu) == 1u) reach &= ~(1u << j);
+  uint64_t out8 = st8;
+  if ((fl & SF_RI) && reach) {
+    int4 rv = *reinterpret_cast<const int4*>(cols + OFF_RI + 2 * o);
+    int16_t* r16 = reinterpret_cast<int16_t*>(&rv);
+    const int step = rp->ri_step;
+    uint32_t elig = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      if (!((reach >> j) & 1u)) continue;
+      const int32_t timer = (int32_t)r16[j] - step;
+      r16[j] = (int16_t)(uint16_t)(uint32_t)timer;
+      bool e = false;
+      if (t == step) e = timer <= 0 && timer >= -step;
+      else if (t > step) e = timer <= 0 && timer > -step;
+      elig |= (uint32_t)e << j;
     }
-    /* -- routine immunisation (fast_ri) ------------------------------------ */
-    if (do_ri && s >= 0 && scm[q] != 1) {
-      int32_t timer = (int32_t)sri[q] - rp->ri_step;
-      sri[q] = (int16_t)(uint16_t)(uint32_t)timer;
-      ri_dirty = true;
-      bool eligible = false;
-      if (t == rp->ri_step) eligible = timer <= 0 && timer >= -rp->ri_step;
-      else if (t > rp->ri_step) eligible = timer <= 0 && timer > -rp->ri_step;
-      if (eligible) {
-        uint32_t ref = W.ref[pos];
-        if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 0) < rp->p_ri[ni]) {
-          atomicAdd(&S.ev[EV_RIVAC], 1);
-          if (s == 0) {
-            s = 1;
-            W.strain[pos] = (int8_t)rp->ri_strain;
-            atomicAdd(&S.ev[EV_RIPROT], 1);
-            s_exit(S, W, pos, cid);
-            atomicAdd(&S.tot[TT_E0 + rp->ri_strain], 1);
-          }
-        }
-        if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 1) < rp->p_ipv[ni]) {
-          atomicAdd(&S.ev[EV_IPVVAC], 1);
-          W.ipv[pos] = 1;
+    *reinterpret_cast<int4*>(W.ri + pos0) = rv;
+    while (elig) {
+      const int j = __ffs(elig) - 1;
+      elig &= elig - 1;
+      const int64_t pos = pos0 + j;
+      const uint32_t ref = W.ref[pos];
+      const int8_t s = (int8_t)(out8 >> (8 * j));
+      if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 0) < rp->p_ri[ni]) {
+        atomicAdd(&S.ev[EV_RIVAC], 1);
+        if (s == 0) {
+          out8 = set_byte(out8, j, 1);
+          W.strain[pos] = (int8_t)rp->ri_strain;
+          atomicAdd(&S.ev[EV_RIPROT], 1);
+          s_exit(S, W, pos, cid);
+          atomicAdd(&S.tot[TT_E0 + rp->ri_strain], 1);
         }
       }
+      if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 1) < rp->p_ipv[ni]) {
+        atomicAdd(&S.ev[EV_IPVVAC], 1);
+        W.ipv[pos] = 1;
+      }
     }
-    /* -- SIA campaigns of the day (fast_sia) ------------------------------- */
-    for (int k = 0; k < nsia; ++k) {
-      if (s < 0 || scm[q] == 1) break;
+  }
+  if ((fl & SF_SIA) && reach) {
+    const int4* d4 = reinterpret_cast<const int4*>(cols + OFF_DOB) + (o >> 2);
+    const int4 a = d4[0], b = d4[1];
+    const int32_t db[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    for (int k = 0; k < rp->sia_n; ++k) {
       const DevSia& ev = rp->sia[rp->sia_i0 + k];
       if (ev.mask[ni] == 0) continue;
-      int64_t age = (int64_t)t - (int64_t)sdob[q];
-      if (!(ev.min_age <= age && age <= ev.max_age)) continue;
-      double r = lpg_u01(rp->seed, LPG_P_SIA, t, W.ref[pos], 0, (uint64_t)k);
-      double p = (double)rp->p_sia[ni];
-      if (r < p) {
-        atomicAdd(&S.ev[EV_SIAVAC0 + k], 1);
-        if (s == 0 && r < p * ev.efficacy) {
-          s = 1;
-          W.strain[pos] = (int8_t)ev.strain;
-          atomicAdd(&S.ev[EV_SIAPROT0 + k], 1);
-          s_exit(S, W, pos, cid);
-          atomicAdd(&S.tot[TT_E0 + ev.strain], 1);
+      uint32_t in = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int64_t age = (int64_t)t - (int64_t)db[j];
+        in |= (uint32_t)(ev.min_age <= age && age <= ev.max_age) << j;
+      }
+      in &= reach;
+      const double p = (double)rp->p_sia[ni];
+      while (in) {
+        const int j = __ffs(in) - 1;
+        in &= in - 1;
+        const int64_t pos = pos0 + j;
+        const double r = lpg_u01(rp->seed, LPG_P_SIA, t, W.ref[pos], 0, (uint64_t)k);
+        if (r < p) {
+          atomicAdd(&S.ev[EV_SIAVAC0 + k], 1);
+          if ((int8_t)(out8 >> (8 * j)) == 0 && r < p * ev.efficacy) {
+            out8 = set_byte(out8, j, 1);
+            W.strain[pos] = (int8_t)ev.strain;
+            atomicAdd(&S.ev[EV_SIAPROT0 + k], 1);
+            s_exit(S, W, pos, cid);
+            atomicAdd(&S.tot[TT_E0 + ev.strain], 1);
+          }
         }
       }
     }
-    if (s != s_in) out8 = (out8 & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)s << (8 * j));
   }
   if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
-  if (ri_dirty) *reinterpret_cast<int4*>(W.ri + pos0) = *reinterpret_cast<const int4*>(sri + o);
 }
 
 template <int PHASE>
@@ -581,18 +626,28 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
   __shared__ SweepPlan P;
   __shared__ __align__(8) uint64_t full[LPG_NST];
   __shared__ int s_abort;
-  const int R = W.n_reps < 1024 ? W.n_reps : 1024;
+  const int R = W.n_reps < LPG_MAX_REPS ? W.n_reps : LPG_MAX_REPS;
   if (threadIdx.x == 0) {
     int32_t acc = 0;
     for (int r = 0; r < R; ++r) {
       P.off[r] = acc;
       const DevRep* rp = &W.reps[r];
-      int work = rp->active;
-      if (PHASE == 1) work = work && rp->seed_n > 0 && (rp->ri_tick || rp->sia_n > 0);
-      const int late = (PHASE == 0) == (rp->seed_n == 0);
+      uint8_t f = 0;
+      if (rp->active) {
+        if (PHASE == 0) {
+          if (rp->vd_tick) f |= SF_VD | SF_DENSE;
+          if (rp->comps & LPG_COMP_DS) f |= SF_DS;
+          if (f) f |= SF_WORK;
+        } else {
+          if (rp->ri_tick) f |= SF_RI;
+          if (rp->sia_n > 0) f |= SF_SIA;
+          if (f) f |= SF_WORK | SF_DENSE;
+        }
+      }
+      P.flags[r] = f;
       P.cbase[r] = rp->chunk_base;
-      P.dense[r] = (PHASE == 0 && rp->vd_tick) || (late && (rp->ri_tick || rp->sia_n > 0));
-      acc += work ? rp->used_chunks : 0;
+      P.tick[r] = rp->cur_t;
+      acc += (f & SF_WORK) ? rp->used_chunks : 0;
     }
     P.off[R] = acc;
     P.total = acc;
@@ -616,35 +671,35 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
   const int32_t w1 = min(w0 + per, total);
   if (w0 >= w1) return;
 
-  /* producer (thread 0): issue one stage starting at work item wp into buffer b */
+  /* producer (thread 0): the stage starting at work item wp into buffer b */
   int32_t wp = w0;
-  int issued = 0;
   auto issue = [&](int b) {
     int r;
     const int32_t we = stage_end(P, wp, w1, &r);
-    const DevRep* rp = &W.reps[r];
+    const uint8_t f = P.flags[r];
     const int64_t cid = P.cbase[r] + (wp - P.off[r]);
+    const int nc = we - wp;
     uint8_t* dst = sm_stage + (size_t)b * LPG_STAGE_BYTES;
-    uint32_t bytes = (uint32_t)(we - wp) * LPG_CHUNK;
-    if (P.dense[r]) {
-      const int late = (PHASE == 0) == (rp->seed_n == 0);
-      const bool vd = PHASE == 0 && rp->vd_tick;
-      const bool ri = late && rp->ri_tick;
-      const bool sia = late && rp->sia_n > 0;
-      bytes = LPG_CHUNK + (vd ? 4 * LPG_CHUNK : 0) + (ri ? 2 * LPG_CHUNK : 0) + ((ri || sia) ? LPG_CHUNK : 0) +
-              (sia ? 4 * LPG_CHUNK : 0);
-      mbar_expect_tx(&full[b], bytes);
-      bulk_g2s(dst + OFF_DS, W.ds + cid * LPG_CHUNK, LPG_CHUNK, &full[b]);
-      if (vd) bulk_g2s(dst + OFF_DOD, W.dod + cid * LPG_CHUNK, 4 * LPG_CHUNK, &full[b]);
-      if (ri) bulk_g2s(dst + OFF_RI, W.ri + cid * LPG_CHUNK, 2 * LPG_CHUNK, &full[b]);
-      if (ri || sia) bulk_g2s(dst + OFF_CM, W.cm + cid * LPG_CHUNK, LPG_CHUNK, &full[b]);
-      if (sia) bulk_g2s(dst + OFF_DOB, W.dob + cid * LPG_CHUNK, 4 * LPG_CHUNK, &full[b]);
+    uint8_t* cols = dst + LPG_META_BYTES;
+    uint32_t bytes = (uint32_t)nc * 16u;
+    if (f & SF_DENSE) {
+      bytes += LPG_CHUNK + ((f & SF_VD) ? 4 * LPG_CHUNK : 0) + ((f & SF_RI) ? 2 * LPG_CHUNK : 0) +
+               ((f & (SF_RI | SF_SIA)) ? LPG_CHUNK : 0) + ((f & SF_SIA) ? 4 * LPG_CHUNK : 0);
     } else {
-      mbar_expect_tx(&full[b], bytes);
-      bulk_g2s(dst, W.ds + cid * LPG_CHUNK, bytes, &full[b]);
+      bytes += (uint32_t)nc * LPG_CHUNK;
+    }
+    mbar_expect_tx(&full[b], bytes);
+    bulk_g2s(dst, W.cmeta + cid, (uint32_t)nc * 16u, &full[b]);
+    if (f & SF_DENSE) {
+      bulk_g2s(cols + OFF_DS, W.ds + cid * LPG_CHUNK, LPG_CHUNK, &full[b]);
+      if (f & SF_VD) bulk_g2s(cols + OFF_DOD, W.dod + cid * LPG_CHUNK, 4 * LPG_CHUNK, &full[b]);
+      if (f & SF_RI) bulk_g2s(cols + OFF_RI, W.ri + cid * LPG_CHUNK, 2 * LPG_CHUNK, &full[b]);
+      if (f & (SF_RI | SF_SIA)) bulk_g2s(cols + OFF_CM, W.cm + cid * LPG_CHUNK, LPG_CHUNK, &full[b]);
+      if (f & SF_SIA) bulk_g2s(cols + OFF_DOB, W.dob + cid * LPG_CHUNK, 4 * LPG_CHUNK, &full[b]);
+    } else {
+      bulk_g2s(cols, W.ds + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
     }
     wp = we;
-    ++issued;
   };
   if (threadIdx.x == 0) {
     for (int b = 0; b < LPG_NST && wp < w1; ++b) issue(b);
@@ -662,22 +717,37 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
     __syncthreads();
     if (s_abort) break;
     const DevRep* rp = &W.reps[r];
+    const uint8_t fl = P.flags[r];
+    const int t = P.tick[r];
     const uint8_t* stg = sm_stage + (size_t)b * LPG_STAGE_BYTES;
-    const bool dense = P.dense[r];
+    const int4* meta = reinterpret_cast<const int4*>(stg);
+    const uint8_t* cols = stg + LPG_META_BYTES;
     for (int32_t w = wc; w < we; ++w) {
-      const int64_t cid = P.cbase[r] + (w - P.off[r]);
-      const int g = W.chunk_node[cid];
+      const int4 m = meta[w - wc];
+      const int g = m.x;
       if (g != cur_g) {
         sweep_flush(S, W, cur_g);
         cur_g = g;
       }
-      const int fill = W.chunk_fill[cid];
+      const int fill = m.y;
+      const int64_t cid = P.cbase[r] + (w - P.off[r]);
+      uint32_t qm = 0;
       if (o < fill) {
-        const int nbo = (W.chunk_nbt[cid] == rp->cur_t) ? W.chunk_nbo[cid] : LPG_CHUNK;
-        const uint8_t* cst = dense ? stg : stg + (size_t)(w - wc) * LPG_CHUNK;
+        const uint32_t valid = fill - o >= 8 ? 0xffu : ((1u << (fill - o)) - 1u);
+        const uint8_t* cst = (fl & SF_DENSE) ? cols + OFF_DS : cols + (size_t)(w - wc) * LPG_CHUNK;
         const uint64_t st8 = *reinterpret_cast<const uint64_t*>(cst + o);
-        sweep_slots<PHASE>(S, W, rp, cid, g, fill, nbo, stg, dense, o, st8);
+        if (PHASE == 0) {
+          if (fl & SF_VD) {
+            const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
+            qm = sweep_slots_a(S, W, rp, fl, t, cid, nbo, o, st8, cols, valid);
+          } else {
+            qm = ei_bits(st8) & valid;
+          }
+        } else {
+          sweep_slots_b(S, W, rp, fl, t, cid, g - rp->node_base, o, st8, cols, valid);
+        }
       }
+      if (PHASE == 0 && (fl & SF_DS)) dsq_append(W, qm, cid * LPG_CHUNK + o);
     }
     wc = we;
     __syncthreads();
@@ -700,6 +770,88 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
     return;
   }
   sweep_flush(S, W, cur_g);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Disease progression (disease_state_step_kernel, model.py:393-454) of the
+ * agents queued by k_sweep<0>, one thread per agent.  Node counters are
+ * aggregated across the warp's lanes that share a node before the atomics. */
+__device__ __forceinline__ void warp_add(int32_t* p, unsigned peers, int32_t v) {
+  const int32_t tot = __reduce_add_sync(peers, v);
+  if ((threadIdx.x & 31) == __ffs(peers) - 1 && tot) atomicAdd(p, tot);
+}
+
+__global__ void __launch_bounds__(256) k_dsq(DevWorld W) {
+  const uint32_t n = *W.dsq_n;
+  const int64_t G = W.G;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t q = base + threadIdx.x;
+    const bool on = q < n;
+    int g = -1, st = 0;
+    int32_t dE = 0, dI = 0, dR = 0, dPP = 0, dP = 0, nPP = 0, nP = 0;
+    int64_t pos = 0;
+    if (on) {
+      pos = W.hits[q];
+      const int64_t cid = pos / LPG_CHUNK;
+      g = W.cmeta[cid].x;
+      const DevRep* rp = &W.reps[W.node_rep[g]];
+      const int t = rp->cur_t;
+      int8_t s = W.ds[pos];
+      st = W.strain[pos];
+      if (s == 1) {
+        const int8_t e = W.et[pos];
+        if (e <= 0) {
+          s = 2;
+          dE -= 1;
+          dI += 1;
+          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], (unsigned long long)bw);
+        }
+        W.et[pos] = dec_i8(e);
+      }
+      if (s == 2) {
+        const int8_t i = W.it[pos];
+        if (i <= 0) {
+          s = 3;
+          dI -= 1;
+          dR += 1;
+          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
+        }
+        W.it[pos] = dec_i8(i);
+        if (st == 0) {
+          const int8_t p = W.pt[pos];
+          if (p <= 0 && W.pp[pos] == -1) {
+            if (W.ipv[pos] == 0) {
+              W.pp[pos] = 1;
+              dPP += 1;
+              nPP += 1;
+              if (lpg_u01(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < (double)rp->p_par) {
+                W.par[pos] = 1;
+                dP += 1;
+                nP += 1;
+              }
+            } else {
+              W.pp[pos] = 0;
+            }
+          }
+          W.pt[pos] = dec_i8(p);
+        }
+      }
+      W.ds[pos] = s;
+    }
+    const unsigned act = __ballot_sync(FULLMASK, on);
+    if (!on) continue;
+    const unsigned by_node = __match_any_sync(act, g);
+    warp_add(&W.tot[(int64_t)TT_R * G + g], by_node, dR);
+    warp_add(&W.tot[(int64_t)TT_POTP * G + g], by_node, dPP);
+    warp_add(&W.tot[(int64_t)TT_P * G + g], by_node, dP);
+    warp_add(&W.ev[(int64_t)EV_NEWPOT * G + g], by_node, nPP);
+    warp_add(&W.ev[(int64_t)EV_NEWPAR * G + g], by_node, nP);
+    const unsigned by_ns = __match_any_sync(act, g * LPG_MAX_STRAINS + st);
+    warp_add(&W.tot[(int64_t)(TT_E0 + st) * G + g], by_ns, dE);
+    warp_add(&W.tot[(int64_t)(TT_I0 + st) * G + g], by_ns, dI);
+  }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -894,9 +1046,23 @@ __global__ void k_node_tx(DevWorld W) {
   if (!(rp->comps & LPG_COMP_TX)) return;
   const double* nrow = rp->net_t + (int64_t)i * n; /* nrow[ii] = network[ii][i] */
   double part[LPG_MAX_STRAINS] = {0.0, 0.0, 0.0, 0.0};
-  for (int ii = lane; ii < n; ii += 32) {
-    const double w = nrow[ii];
-    for (int k = 0; k < ns; ++k) part[k] = part[k] + ((double)W.bb[(int64_t)k * G + nb + ii] * 0x1.0p-32) * w;
+  for (int ii0 = lane; ii0 < n; ii0 += 128) {
+    double wv[4];
+    uint64_t bv[4][LPG_MAX_STRAINS];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int ii = ii0 + 32 * u;
+      wv[u] = ii < n ? nrow[ii] : 0.0;
+#pragma unroll
+      for (int k = 0; k < LPG_MAX_STRAINS; ++k) bv[u][k] = (ii < n && k < ns) ? W.bb[(int64_t)k * G + nb + ii] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (ii0 + 32 * u >= n) break;
+#pragma unroll
+      for (int k = 0; k < LPG_MAX_STRAINS; ++k)
+        if (k < ns) part[k] = part[k] + ((double)bv[u][k] * 0x1.0p-32) * wv[u];
+    }
   }
   double inc[LPG_MAX_STRAINS];
   for (int k = 0; k < ns; ++k) {
@@ -1134,7 +1300,7 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
       }
       if (!won) continue;
       const int64_t cid = pos / LPG_CHUNK;
-      const int g = W.chunk_node[cid];
+      const int g = W.cmeta[cid].x;
       const DevRep* rp = &W.reps[W.node_rep[g]];
       double p[LPG_MAX_STRAINS];
       double totalp = 0.0;
@@ -1247,13 +1413,14 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_count(DevWorld W, int32_t
     const DevRep* rp = &W.reps[r];
     for (int32_t lc = blockIdx.x; lc < rp->used_chunks; lc += gridDim.x) {
       const int64_t cid = rp->chunk_base + lc;
-      const int g = W.chunk_node[cid];
+      const int4 meta = W.cmeta[cid];
+      const int g = meta.x;
       if (threadIdx.x < TT_N) s_tot[threadIdx.x] = 0;
       if (threadIdx.x < LPG_NSUB) s_sub[threadIdx.x] = 0;
       if (threadIdx.x < LPG_MAX_STRAINS) s_bb[threadIdx.x] = 0;
       if (threadIdx.x == 0) s_sw = 0;
       __syncthreads();
-      const int fill = W.chunk_fill[cid];
+      const int fill = meta.y;
       for (int o = threadIdx.x; o < fill; o += blockDim.x) {
         const int64_t pos = cid * LPG_CHUNK + o;
         const int8_t s = W.ds[pos];
