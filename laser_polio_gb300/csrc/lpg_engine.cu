@@ -473,7 +473,8 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.dod, P);
   rc |= dalloc(h, &W.ref, P);
   rc |= dalloc(h, &W.cmeta, chunk_total);
-  rc |= dalloc(h, &W.dsq_n, 1);
+  rc |= dalloc(h, &W.dsq_cnt, 1024);
+  rc |= dalloc(h, &W.dsq_first, 1024);
   rc |= dalloc(h, &W.chunk_w, chunk_total);
   rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.cpref, chunk_total);
@@ -494,8 +495,9 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.uniq, G);
   rc |= dalloc(h, &W.ksel, G);
   rc |= dalloc(h, &W.tgt_off, G + 1);
-  int64_t hits = 0;
-  for (auto& s : h->sims) hits += s.d.capacity;
+  /* selection targets (at most the susceptibles) and the E/I queue slabs
+   * (at most one entry per position) share this buffer */
+  int64_t hits = (int64_t)chunk_total * LPG_CHUNK;
   W.hits_cap = hits;
   rc |= dalloc(h, &W.hits, hits);
   rc |= dalloc(h, &W.bar_count, 1);
@@ -505,7 +507,8 @@ extern "C" int lpg_start(lpg_handle* h) {
   if (rc) return LPG_ERR_NOMEM;
   CK(cudaMemsetAsync(W.ds, 0xff, P, st));
   CK(cudaMemsetAsync(W.ref, 0xff, P * 4, st));
-  CK(cudaMemsetAsync(W.dsq_n, 0, 4, st));
+  CK(cudaMemsetAsync(W.dsq_cnt, 0, 4 * 1024, st));
+  CK(cudaMemsetAsync(W.dsq_first, 0, 4 * 1024, st));
   CK(cudaMemsetAsync(W.ev, 0, sizeof(int32_t) * EV_N * G, st));
   CK(cudaMemsetAsync(W.tot, 0, sizeof(int32_t) * TT_N * G, st));
   CK(cudaMemsetAsync(W.sw, 0, sizeof(uint64_t) * G, st));
@@ -739,7 +742,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaFuncSetAttribute(k_sweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
   CK(cudaFuncSetAttribute(k_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM));
-  h->sweep_blocks = std::max(1, occ) * h->sm_count;
+  h->sweep_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
   occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_select, 256, 0));
   h->select_blocks = std::max(1, std::min(occ, 4)) * h->sm_count;
@@ -762,7 +765,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
     case 1: k_newborns<<<dim3(h->sm_count * 2, R), 256, 0, st>>>(W); break;
     case 2: k_sweep<0><<<h->sweep_blocks, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 3: k_dsq<<<h->sm_count * 8, 256, 0, st>>>(W); break;
+    case 3: k_dsq<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
     case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
     case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM, st>>>(W); break;
     case 6: k_node_tx<<<(G * 32 + 255) / 256, 256, 0, st>>>(W); break;

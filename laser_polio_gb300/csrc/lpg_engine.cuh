@@ -178,7 +178,8 @@ typedef struct {
   int64_t* tgt_off; /* [G + 1] */
   uint32_t* hits; /* selection targets; also the queue of E/I positions of the tick */
   int64_t hits_cap;
-  uint32_t* dsq_n; /* entries in that queue */
+  uint32_t* dsq_cnt;  /* per k_sweep<0> CTA: entries in its slab of that queue */
+  int32_t* dsq_first; /* per k_sweep<0> CTA: its first work item (slab offset / CHUNK) */
   /* grid barrier of the cooperative selection kernel */
   uint32_t* bar_count;
   uint32_t* bar_gen;

@@ -111,7 +111,6 @@ __global__ void k_begin(DevWorld W) {
   DevRep* rp = &W.reps[blockIdx.x];
   __shared__ int s_active, s_vd, s_t;
   __shared__ unsigned long long s_sum;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *W.dsq_n = 0;
   if (threadIdx.x == 0) {
     int t = rp->t;
     int active = rp->started && !rp->error && !rp->stopped && t >= 1 && t < rp->nt;
@@ -378,12 +377,6 @@ __device__ __forceinline__ bool any_ei(uint64_t x) {
 #define LPG_PLAIN_GROUP (LPG_COL_BYTES / LPG_CHUNK)
 #define LPG_SWEEP_SMEM (LPG_NST * LPG_STAGE_BYTES)
 #define LPG_MBAR_SPIN (1LL << 24)
-/* dense stage layout (bytes after the metadata block) */
-#define OFF_DS 0
-#define OFF_DOD 2048
-#define OFF_RI (2048 + 8192)
-#define OFF_CM (2048 + 8192 + 4096)
-#define OFF_DOB (2048 + 8192 + 4096 + 2048)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -426,6 +419,36 @@ struct SweepPlan {
   uint8_t flags[LPG_MAX_REPS];
 };
 
+/* Staged bytes per chunk for a simulation's flags: state always, plus the
+ * dense columns of the tick. */
+__device__ __forceinline__ int chunk_bytes(uint8_t f) {
+  return LPG_CHUNK + ((f & SF_VD) ? 4 * LPG_CHUNK : 0) + ((f & SF_RI) ? 2 * LPG_CHUNK : 0) +
+         ((f & (SF_RI | SF_SIA)) ? LPG_CHUNK : 0) + ((f & SF_SIA) ? 4 * LPG_CHUNK : 0);
+}
+/* Chunks per stage (k consecutive chunks: each column is one contiguous copy). */
+__device__ __forceinline__ int stage_chunks(uint8_t f) {
+  const int k = LPG_COL_BYTES / chunk_bytes(f);
+  return k < LPG_PLAIN_GROUP ? k : LPG_PLAIN_GROUP;
+}
+/* Column offsets inside a stage of k chunks. */
+struct StageLayout {
+  int ds, dod, ri, cm, dob;
+};
+__device__ __forceinline__ StageLayout stage_layout(uint8_t f, int k) {
+  StageLayout L;
+  int off = 0;
+  L.ds = off;
+  off += k * LPG_CHUNK;
+  L.dod = off;
+  if (f & SF_VD) off += k * 4 * LPG_CHUNK;
+  L.ri = off;
+  if (f & SF_RI) off += k * 2 * LPG_CHUNK;
+  L.cm = off;
+  if (f & (SF_RI | SF_SIA)) off += k * LPG_CHUNK;
+  L.dob = off;
+  return L;
+}
+
 /* End of the stage that starts at work item w (same answer on every thread). */
 __device__ __forceinline__ int32_t stage_end(const SweepPlan& P, int32_t w, int32_t w1, int* r_out) {
   int lo = 0, hi = P.nreps - 1;
@@ -435,7 +458,7 @@ __device__ __forceinline__ int32_t stage_end(const SweepPlan& P, int32_t w, int3
   }
   *r_out = lo;
   const int32_t lim = min(w1, P.off[lo + 1]);
-  return (P.flags[lo] & SF_DENSE) ? w + 1 : min(lim, w + LPG_PLAIN_GROUP);
+  return min(lim, w + stage_chunks(P.flags[lo]));
 }
 
 /* Byte mask (bit j for byte j) of the bytes of x equal to 1 or 2. */
@@ -462,9 +485,10 @@ __device__ __forceinline__ uint64_t set_byte(uint64_t x, int j, int8_t v) {
   return (x & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)v << (8 * j));
 }
 
-/* Append the positions of the set bits of m (slots pos0 + j) to the E/I
- * queue: one atomic per warp.  Called by all 32 lanes. */
-__device__ __forceinline__ void dsq_append(DevWorld& W, uint32_t m, int64_t pos0) {
+/* Append the positions of the set bits of m (slots pos0 + j) to this CTA's
+ * slab of the E/I queue: one shared-memory atomic per warp.  Called by all 32
+ * lanes. */
+__device__ __forceinline__ void dsq_append(uint32_t* slab, uint32_t* s_cnt, uint32_t m, int64_t pos0) {
   if (__ballot_sync(FULLMASK, m != 0) == 0) return;
   const int lane = threadIdx.x & 31;
   const uint32_t c = __popc(m);
@@ -476,13 +500,13 @@ __device__ __forceinline__ void dsq_append(DevWorld& W, uint32_t m, int64_t pos0
   }
   const uint32_t tot = __shfl_sync(FULLMASK, x, 31);
   uint32_t base = 0;
-  if (lane == 31) base = atomicAdd(W.dsq_n, tot);
+  if (lane == 31) base = atomicAdd(s_cnt, tot);
   base = __shfl_sync(FULLMASK, base, 31);
   uint32_t at = base + x - c;
   while (m) {
     const int j = __ffs(m) - 1;
     m &= m - 1;
-    W.hits[at++] = (uint32_t)(pos0 + j);
+    slab[at++] = (uint32_t)(pos0 + j);
   }
 }
 
@@ -490,13 +514,13 @@ __device__ __forceinline__ void dsq_append(DevWorld& W, uint32_t m, int64_t pos0
  * of slots in E or I after them (the agents progression must visit). */
 __device__ __forceinline__ uint32_t sweep_slots_a(SweepSmem& S, DevWorld& W, const DevRep* rp, uint8_t fl, int t,
                                               int64_t cid, int nbo, int o, uint64_t st8, const uint8_t* cols,
-                                              uint32_t valid) {
+                                              const StageLayout& L, int kk, uint32_t valid) {
   const int64_t pos0 = cid * LPG_CHUNK + o;
   uint32_t alive = alive_bits(st8) & valid;
   uint32_t ei = ei_bits(st8) & valid;
   uint64_t out8 = st8;
   if (fl & SF_VD) {
-    const int4* d4 = reinterpret_cast<const int4*>(cols + OFF_DOD) + (o >> 2);
+    const int4* d4 = reinterpret_cast<const int4*>(cols + L.dod + kk * 4 * LPG_CHUNK) + (o >> 2);
     const int4 a = d4[0], b = d4[1];
     const int32_t dd[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     uint32_t dead = 0;
@@ -536,17 +560,17 @@ __device__ __forceinline__ uint32_t sweep_slots_a(SweepSmem& S, DevWorld& W, con
 /* One thread's 8 slots, PHASE 1: RI then the SIA campaigns of the day. */
 __device__ __forceinline__ void sweep_slots_b(SweepSmem& S, DevWorld& W, const DevRep* rp, uint8_t fl, int t,
                                               int64_t cid, int ni, int o, uint64_t st8, const uint8_t* cols,
-                                              uint32_t valid) {
+                                              const StageLayout& L, int kk, uint32_t valid) {
   const int64_t pos0 = cid * LPG_CHUNK + o;
   uint32_t alive = alive_bits(st8) & valid;
-  const uint64_t c8 = *reinterpret_cast<const uint64_t*>(cols + OFF_CM + o);
+  const uint64_t c8 = *reinterpret_cast<const uint64_t*>(cols + L.cm + kk * LPG_CHUNK + o);
   uint32_t reach = alive;
 #pragma unroll
   for (int j = 0; j < 8; ++j)
     if (((c8 >> (8 * j)) & 0xffu) == 1u) reach &= ~(1u << j);
   uint64_t out8 = st8;
   if ((fl & SF_RI) && reach) {
-    int4 rv = *reinterpret_cast<const int4*>(cols + OFF_RI + 2 * o);
+    int4 rv = *reinterpret_cast<const int4*>(cols + L.ri + kk * 2 * LPG_CHUNK + 2 * o);
     int16_t* r16 = reinterpret_cast<int16_t*>(&rv);
     const int step = rp->ri_step;
     uint32_t elig = 0;
@@ -584,7 +608,7 @@ __device__ __forceinline__ void sweep_slots_b(SweepSmem& S, DevWorld& W, const D
     }
   }
   if ((fl & SF_SIA) && reach) {
-    const int4* d4 = reinterpret_cast<const int4*>(cols + OFF_DOB) + (o >> 2);
+    const int4* d4 = reinterpret_cast<const int4*>(cols + L.dob + kk * 4 * LPG_CHUNK) + (o >> 2);
     const int4 a = d4[0], b = d4[1];
     const int32_t db[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     for (int k = 0; k < rp->sia_n; ++k) {
@@ -625,7 +649,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
   __shared__ SweepSmem S;
   __shared__ SweepPlan P;
   __shared__ __align__(8) uint64_t full[LPG_NST];
-  __shared__ int s_abort;
+  __shared__ uint32_t s_qcnt;
   const int R = W.n_reps < LPG_MAX_REPS ? W.n_reps : LPG_MAX_REPS;
   if (threadIdx.x == 0) {
     int32_t acc = 0;
@@ -652,7 +676,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
     P.off[R] = acc;
     P.total = acc;
     P.nreps = R;
-    s_abort = 0;
+    s_qcnt = 0;
     for (int b = 0; b < LPG_NST; ++b) mbar_init(&full[b], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -665,111 +689,115 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
   }
   __syncthreads();
   const int32_t total = P.total;
-  if (total == 0) return;
   const int32_t per = (total + gridDim.x - 1) / gridDim.x;
-  const int32_t w0 = blockIdx.x * per;
+  const int32_t w0 = min((int32_t)blockIdx.x * per, total);
   const int32_t w1 = min(w0 + per, total);
-  if (w0 >= w1) return;
-
-  /* producer (thread 0): the stage starting at work item wp into buffer b */
-  int32_t wp = w0;
-  auto issue = [&](int b) {
-    int r;
-    const int32_t we = stage_end(P, wp, w1, &r);
-    const uint8_t f = P.flags[r];
-    const int64_t cid = P.cbase[r] + (wp - P.off[r]);
-    const int nc = we - wp;
-    uint8_t* dst = sm_stage + (size_t)b * LPG_STAGE_BYTES;
-    uint8_t* cols = dst + LPG_META_BYTES;
-    uint32_t bytes = (uint32_t)nc * 16u;
-    if (f & SF_DENSE) {
-      bytes += LPG_CHUNK + ((f & SF_VD) ? 4 * LPG_CHUNK : 0) + ((f & SF_RI) ? 2 * LPG_CHUNK : 0) +
-               ((f & (SF_RI | SF_SIA)) ? LPG_CHUNK : 0) + ((f & SF_SIA) ? 4 * LPG_CHUNK : 0);
-    } else {
-      bytes += (uint32_t)nc * LPG_CHUNK;
-    }
-    mbar_expect_tx(&full[b], bytes);
-    bulk_g2s(dst, W.cmeta + cid, (uint32_t)nc * 16u, &full[b]);
-    if (f & SF_DENSE) {
-      bulk_g2s(cols + OFF_DS, W.ds + cid * LPG_CHUNK, LPG_CHUNK, &full[b]);
-      if (f & SF_VD) bulk_g2s(cols + OFF_DOD, W.dod + cid * LPG_CHUNK, 4 * LPG_CHUNK, &full[b]);
-      if (f & SF_RI) bulk_g2s(cols + OFF_RI, W.ri + cid * LPG_CHUNK, 2 * LPG_CHUNK, &full[b]);
-      if (f & (SF_RI | SF_SIA)) bulk_g2s(cols + OFF_CM, W.cm + cid * LPG_CHUNK, LPG_CHUNK, &full[b]);
-      if (f & SF_SIA) bulk_g2s(cols + OFF_DOB, W.dob + cid * LPG_CHUNK, 4 * LPG_CHUNK, &full[b]);
-    } else {
-      bulk_g2s(cols, W.ds + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
-    }
-    wp = we;
-  };
-  if (threadIdx.x == 0) {
-    for (int b = 0; b < LPG_NST && wp < w1; ++b) issue(b);
-  }
-
-  int cur_g = -1;
-  const int o = threadIdx.x * LPG_SPT;
-  int32_t wc = w0;
-  for (int32_t i = 0; wc < w1; ++i) {
-    const int b = i % LPG_NST;
-    const uint32_t parity = (uint32_t)(i / LPG_NST) & 1u;
-    int r;
-    const int32_t we = stage_end(P, wc, w1, &r);
-    if (!mbar_wait(&full[b], parity)) atomicExch(&s_abort, 1);
-    __syncthreads();
-    if (s_abort) break;
-    const DevRep* rp = &W.reps[r];
-    const uint8_t fl = P.flags[r];
-    const int t = P.tick[r];
-    const uint8_t* stg = sm_stage + (size_t)b * LPG_STAGE_BYTES;
-    const int4* meta = reinterpret_cast<const int4*>(stg);
-    const uint8_t* cols = stg + LPG_META_BYTES;
-    for (int32_t w = wc; w < we; ++w) {
-      const int4 m = meta[w - wc];
-      const int g = m.x;
-      if (g != cur_g) {
-        sweep_flush(S, W, cur_g);
-        cur_g = g;
-      }
-      const int fill = m.y;
-      const int64_t cid = P.cbase[r] + (w - P.off[r]);
-      uint32_t qm = 0;
-      if (o < fill) {
-        const uint32_t valid = fill - o >= 8 ? 0xffu : ((1u << (fill - o)) - 1u);
-        const uint8_t* cst = (fl & SF_DENSE) ? cols + OFF_DS : cols + (size_t)(w - wc) * LPG_CHUNK;
-        const uint64_t st8 = *reinterpret_cast<const uint64_t*>(cst + o);
-        if (PHASE == 0) {
-          if (fl & SF_VD) {
-            const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
-            qm = sweep_slots_a(S, W, rp, fl, t, cid, nbo, o, st8, cols, valid);
-          } else {
-            qm = ei_bits(st8) & valid;
-          }
-        } else {
-          sweep_slots_b(S, W, rp, fl, t, cid, g - rp->node_base, o, st8, cols, valid);
-        }
-      }
-      if (PHASE == 0 && (fl & SF_DS)) dsq_append(W, qm, cid * LPG_CHUNK + o);
-    }
-    wc = we;
-    __syncthreads();
-    if (threadIdx.x == 0 && wp < w1) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(b);
-    }
-  }
-  if (s_abort) {
-    /* leave no bulk copy in flight into this CTA's shared memory */
+  /* this CTA's slab of the E/I queue starts at its first position */
+  uint32_t* slab = W.hits + (int64_t)w0 * LPG_CHUNK;
+  if (w0 < w1) {
+    /* producer (thread 0): the stage starting at work item wp into buffer b */
+    int32_t wp = w0;
+    auto issue = [&](int b) {
+      int r;
+      const int32_t we = stage_end(P, wp, w1, &r);
+      const uint8_t f = P.flags[r];
+      const int64_t cid = P.cbase[r] + (wp - P.off[r]);
+      const int nc = we - wp;
+      const StageLayout L = stage_layout(f, nc);
+      uint8_t* dst = sm_stage + (size_t)b * LPG_STAGE_BYTES;
+      uint8_t* cols = dst + LPG_META_BYTES;
+      const uint32_t bytes = (uint32_t)nc * 16u + (uint32_t)nc * (uint32_t)chunk_bytes(f);
+      mbar_expect_tx(&full[b], bytes);
+      bulk_g2s(dst, W.cmeta + cid, (uint32_t)nc * 16u, &full[b]);
+      bulk_g2s(cols + L.ds, W.ds + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
+      if (f & SF_VD) bulk_g2s(cols + L.dod, W.dod + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
+      if (f & SF_RI) bulk_g2s(cols + L.ri, W.ri + cid * LPG_CHUNK, (uint32_t)nc * 2 * LPG_CHUNK, &full[b]);
+      if (f & (SF_RI | SF_SIA)) bulk_g2s(cols + L.cm, W.cm + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
+      if (f & SF_SIA) bulk_g2s(cols + L.dob, W.dob + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
+      wp = we;
+    };
     if (threadIdx.x == 0) {
-      W.reps[0].error = LPG_ERR_TIMEOUT;
-      for (int b = 0; b < LPG_NST; ++b) {
-        for (long long it = 0; it < LPG_MBAR_SPIN; ++it) {
-          if (mbar_try_wait(&full[b], 0) || mbar_try_wait(&full[b], 1)) break;
+      for (int b = 0; b < LPG_NST && wp < w1; ++b) issue(b);
+    }
+
+    int cur_g = -1;
+    bool aborted = false;
+    const int o = threadIdx.x * LPG_SPT;
+    int32_t wc = w0;
+    for (int32_t i = 0; wc < w1; ++i) {
+      const int b = i % LPG_NST;
+      const uint32_t parity = (uint32_t)(i / LPG_NST) & 1u;
+      int r;
+      const int32_t we = stage_end(P, wc, w1, &r);
+      /* every thread acquires the stage; the CTA agrees on success */
+      const bool ok = __syncthreads_and(mbar_wait(&full[b], parity));
+      if (ok) {
+        const DevRep* rp = &W.reps[r];
+        const uint8_t fl = P.flags[r];
+        const int t = P.tick[r];
+        const uint8_t* stg = sm_stage + (size_t)b * LPG_STAGE_BYTES;
+        const int4* meta = reinterpret_cast<const int4*>(stg);
+        const uint8_t* cols = stg + LPG_META_BYTES;
+        const StageLayout L = stage_layout(fl, we - wc);
+        for (int32_t w = wc; w < we; ++w) {
+          const int kk = w - wc;
+          const int4 m = meta[kk];
+          const int g = m.x;
+          if (g != cur_g) {
+            sweep_flush(S, W, cur_g);
+            cur_g = g;
+          }
+          const int fill = m.y;
+          const int64_t cid = P.cbase[r] + (w - P.off[r]);
+          uint32_t qm = 0;
+          if (o < fill) {
+            const uint32_t valid = fill - o >= 8 ? 0xffu : ((1u << (fill - o)) - 1u);
+            const uint64_t st8 = *reinterpret_cast<const uint64_t*>(cols + L.ds + kk * LPG_CHUNK + o);
+            if (PHASE == 0) {
+              if (fl & SF_VD) {
+                const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
+                qm = sweep_slots_a(S, W, rp, fl, t, cid, nbo, o, st8, cols, L, kk, valid);
+              } else {
+                qm = ei_bits(st8) & valid;
+              }
+            } else {
+              sweep_slots_b(S, W, rp, fl, t, cid, g - rp->node_base, o, st8, cols, L, kk, valid);
+            }
+          }
+          if (PHASE == 0 && (fl & SF_DS)) dsq_append(slab, &s_qcnt, qm, cid * LPG_CHUNK + o);
         }
       }
+      wc = we;
+      if (!ok) {
+        aborted = true;
+        break;
+      }
+      /* all reads of buffer b are done before it is refilled */
+      __syncthreads();
+      if (threadIdx.x == 0 && wp < w1) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(b);
+      }
     }
-    __syncthreads();
-    return;
+    if (aborted) {
+      /* leave no bulk copy in flight into this CTA's shared memory */
+      if (threadIdx.x == 0) {
+        W.reps[0].error = LPG_ERR_TIMEOUT;
+        for (int b = 0; b < LPG_NST; ++b) {
+          for (long long it = 0; it < LPG_MBAR_SPIN; ++it) {
+            if (mbar_try_wait(&full[b], 0) || mbar_try_wait(&full[b], 1)) break;
+          }
+        }
+      }
+      __syncthreads();
+    } else {
+      sweep_flush(S, W, cur_g);
+    }
   }
-  sweep_flush(S, W, cur_g);
+  if (PHASE == 0 && threadIdx.x == 0) {
+    W.dsq_cnt[blockIdx.x] = s_qcnt;
+    W.dsq_first[blockIdx.x] = w0;
+  }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -781,8 +809,19 @@ __device__ __forceinline__ void warp_add(int32_t* p, unsigned peers, int32_t v) 
   if ((threadIdx.x & 31) == __ffs(peers) - 1 && tot) atomicAdd(p, tot);
 }
 
-__global__ void __launch_bounds__(256) k_dsq(DevWorld W) {
-  const uint32_t n = *W.dsq_n;
+__global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
+  /* the queue is one slab per CTA of k_sweep<0>: prefix of their counts */
+  __shared__ uint32_t s_pre[1025];
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (int b = 0; b < nslabs; ++b) {
+      s_pre[b] = acc;
+      acc += W.dsq_cnt[b];
+    }
+    s_pre[nslabs] = acc;
+  }
+  __syncthreads();
+  const uint32_t n = s_pre[nslabs];
   const int64_t G = W.G;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t q = base + threadIdx.x;
@@ -791,7 +830,12 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W) {
     int32_t dE = 0, dI = 0, dR = 0, dPP = 0, dP = 0, nPP = 0, nP = 0;
     int64_t pos = 0;
     if (on) {
-      pos = W.hits[q];
+      int lo = 0, hi = nslabs - 1; /* slab holding entry q */
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (s_pre[mid] <= q) lo = mid; else hi = mid - 1;
+      }
+      pos = W.hits[(int64_t)W.dsq_first[lo] * LPG_CHUNK + (q - s_pre[lo])];
       const int64_t cid = pos / LPG_CHUNK;
       g = W.cmeta[cid].x;
       const DevRep* rp = &W.reps[W.node_rep[g]];
