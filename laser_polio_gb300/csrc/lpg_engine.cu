@@ -21,8 +21,8 @@
 
 namespace {
 
-const char* kKernelNames[] = {"k_begin", "k_newborns", "k_sweep_a", "k_dsq", "k_seed", "k_sweep_b", "k_node_tx", "k_select", "k_end"};
-constexpr int kNumTickKernels = 9;
+const char* kKernelNames[] = {"k_begin", "k_newborns", "k_sweep_a", "k_dsq", "k_seed", "k_sweep_b", "k_beta", "k_node_tx", "k_select", "k_end"};
+constexpr int kNumTickKernels = 10;
 constexpr int kTicksPerGraph = 8;
 
 /* Reference-ordered columns of one simulation on the device. */
@@ -225,6 +225,14 @@ extern "C" const char* lpg_last_error(const lpg_handle* h) { return h ? h->err.c
 extern "C" void* lpg_cuda_stream(lpg_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 extern "C" int64_t lpg_kernel_launches(lpg_handle* h) { return h ? h->launches : 0; }
+
+/* Integer threshold T with  u < p  <=>  m < T  for u = m * 2^-53, m a 53-bit
+ * integer: T = ceil(p * 2^53) clamped to [0, 2^53] (p * 2^53 is exact). */
+static uint64_t u53_threshold(double p) {
+  if (!(p > 0.0)) return 0;
+  if (p >= 1.0) return 1ULL << 53;
+  return (uint64_t)std::ceil(p * 9007199254740992.0);
+}
 
 static const int res_wide[RS_N] = {0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 1, 0, 0, 0, 1};
 
@@ -491,6 +499,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.nb_end, G);
   rc |= dalloc(h, &W.nb_li0, G);
   rc |= dalloc(h, &W.prob, (size_t)LPG_MAX_STRAINS * G);
+  rc |= dalloc(h, &W.beta, (size_t)LPG_MAX_STRAINS * G);
   rc |= dalloc(h, &W.size, G);
   rc |= dalloc(h, &W.uniq, G);
   rc |= dalloc(h, &W.ksel, G);
@@ -579,6 +588,19 @@ extern "C" int lpg_start(lpg_handle* h) {
     rp.seas = dp;
     if (dupload(h, &fp, s.p_sia)) return LPG_ERR_NOMEM;
     rp.p_sia = fp;
+    {
+      std::vector<uint64_t> tri(n), tipv(n);
+      for (int i = 0; i < n; ++i) {
+        tri[i] = u53_threshold(s.p_ri[i]);
+        tipv[i] = u53_threshold(s.p_ipv[i]);
+      }
+      uint64_t* up;
+      if (dupload(h, &up, tri)) return LPG_ERR_NOMEM;
+      rp.thr_ri = up;
+      if (dupload(h, &up, tipv)) return LPG_ERR_NOMEM;
+      rp.thr_ipv = up;
+      rp.thr_par = u53_threshold((double)d.p_paralysis);
+    }
     if (dupload(h, &ip, s.km)) return LPG_ERR_NOMEM;
     rp.km = ip;
     /* per-tick SIA and seed tables, events in schedule order */
@@ -592,7 +614,15 @@ extern "C" int lpg_start(lpg_handle* h) {
         if (s.sia[k].tick != tt) continue;
         uint8_t* m;
         if (dupload(h, &m, s.sia_masks[k])) return LPG_ERR_NOMEM;
-        DevSia e{s.sia[k].tick, s.sia[k].strain, s.sia[k].min_age, s.sia[k].max_age, s.sia[k].efficacy, m};
+        std::vector<uint64_t> tv(n), tp(n);
+        for (int i = 0; i < n; ++i) {
+          const double pv = (double)s.p_sia[i];
+          tv[i] = u53_threshold(pv);
+          tp[i] = u53_threshold(pv * s.sia[k].efficacy);
+        }
+        uint64_t *dtv, *dtp;
+        if (dupload(h, &dtv, tv) || dupload(h, &dtp, tp)) return LPG_ERR_NOMEM;
+        DevSia e{s.sia[k].tick, s.sia[k].strain, s.sia[k].min_age, s.sia[k].max_age, s.sia[k].efficacy, m, dtv, dtp};
         hsia.push_back(e);
         scnt[tt] += 1;
       }
@@ -741,11 +771,11 @@ extern "C" int lpg_start(lpg_handle* h) {
   int occ = 0;
   CK(cudaFuncSetAttribute(k_sweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
   CK(cudaFuncSetAttribute(k_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM));
   h->sweep_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
   occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_select, 256, 0));
-  h->select_blocks = std::max(1, std::min(occ, 4)) * h->sm_count;
+  h->select_blocks = std::max(1, std::min(occ, 2)) * h->sm_count;
   h->started = true;
   return LPG_OK;
 }
@@ -764,12 +794,13 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
   switch (k) {
     case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
     case 1: k_newborns<<<dim3(h->sm_count * 2, R), 256, 0, st>>>(W); break;
-    case 2: k_sweep<0><<<h->sweep_blocks, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM, st>>>(W); break;
+    case 2: k_sweep<0><<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
     case 3: k_dsq<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
     case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
-    case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_THREADS, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 6: k_node_tx<<<(G * 32 + 255) / 256, 256, 0, st>>>(W); break;
-    case 7: {
+    case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
+    case 6: k_beta<<<(LPG_MAX_STRAINS * G + 255) / 256, 256, 0, st>>>(W); break;
+    case 7: k_node_tx<<<(G * 32 + 63) / 64, 64, 0, st>>>(W); break;
+    case 8: {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(h->select_blocks);
       cfg.blockDim = dim3(256);
@@ -783,7 +814,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
       CK(cudaLaunchKernelEx(&cfg, k_select, W));
       break;
     }
-    case 8: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
+    case 9: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
   }
   CK(cudaGetLastError());
   if (timed) CK(cudaEventRecord(e1, st));

@@ -38,6 +38,8 @@
 #define LPG_SWEEP_THREADS 256
 #define LPG_SPT (LPG_CHUNK / LPG_SWEEP_THREADS) /* slots per thread = 8 */
 #define LPG_MAX_REPS 256
+#define LPG_SWEEP_CONSUMERS 256
+#define LPG_SWEEP_BLOCK (LPG_SWEEP_CONSUMERS + 32)
 
 /* per-tick event counters per node */
 enum {
@@ -75,7 +77,9 @@ enum {
 typedef struct {
   int32_t tick, strain, min_age, max_age;
   double efficacy;
-  const uint8_t* mask; /* device, [n_nodes] */
+  const uint8_t* mask;     /* device, [n_nodes] */
+  const uint64_t* thr_vac; /* [n_nodes] u < p            <=> u53 < thr_vac  */
+  const uint64_t* thr_pro; /* [n_nodes] u < p * efficacy <=> u53 < thr_pro  */
 } DevSia;
 
 typedef struct {
@@ -97,6 +101,9 @@ typedef struct {
   uint64_t seed;
   float p_par;
   int32_t pad0;
+  uint64_t thr_par;        /* u < p_paralysis <=> u53 < thr_par */
+  const uint64_t* thr_ri;  /* [n_nodes] */
+  const uint64_t* thr_ipv; /* [n_nodes] */
   double zi;
   int32_t dur_kind;
   int32_t pad1;
@@ -172,6 +179,7 @@ typedef struct {
   int64_t* nb_end;
   int64_t* nb_li0;
   double* prob; /* [LPG_MAX_STRAINS][G] */
+  double* beta; /* [LPG_MAX_STRAINS][G] node infectivity before mixing, as double */
   int64_t* size;
   int64_t* uniq;
   int64_t* ksel;

@@ -300,58 +300,6 @@ __global__ void k_newborns(DevWorld W) {
   }
 }
 
-/* ------------------------------------------------------------------------ */
-/* Shared-memory node counters of one sweep CTA, flushed on node change. */
-struct SweepSmem {
-  int32_t ev[EV_N];
-  int32_t tot[TT_N];
-  unsigned long long sw;
-  unsigned long long bb[LPG_MAX_STRAINS];
-};
-
-__device__ __forceinline__ void sweep_flush(SweepSmem& S, DevWorld& W, int g) {
-  __syncthreads();
-  if (g >= 0) {
-    int k = threadIdx.x;
-    if (k < EV_N) {
-      int32_t v = S.ev[k];
-      if (v) atomicAdd(&W.ev[(int64_t)k * W.G + g], v);
-    } else if (k < EV_N + TT_N) {
-      int32_t v = S.tot[k - EV_N];
-      if (v) atomicAdd(&W.tot[(int64_t)(k - EV_N) * W.G + g], v);
-    } else if (k == EV_N + TT_N) {
-      if (S.sw) atomicAdd((unsigned long long*)&W.sw[g], S.sw);
-    } else if (k < EV_N + TT_N + 1 + LPG_MAX_STRAINS) {
-      int s = k - EV_N - TT_N - 1;
-      if (S.bb[s]) atomicAdd((unsigned long long*)&W.bb[(int64_t)s * W.G + g], S.bb[s]);
-    }
-  }
-  __syncthreads();
-  int k = threadIdx.x;
-  if (k < EV_N) S.ev[k] = 0;
-  else if (k < EV_N + TT_N) S.tot[k - EV_N] = 0;
-  else if (k == EV_N + TT_N) S.sw = 0;
-  else if (k < EV_N + TT_N + 1 + LPG_MAX_STRAINS) S.bb[k - EV_N - TT_N - 1] = 0;
-  __syncthreads();
-}
-
-/* An agent leaves S: node, chunk and sub-block weights drop by its risk. */
-__device__ __forceinline__ void s_exit(SweepSmem& S, DevWorld& W, int64_t pos, int64_t cid) {
-  uint64_t w = fix_risk(W.risk[pos]);
-  atomicAdd(&S.tot[TT_S], -1);
-  if (w) {
-    atomicAdd(&S.sw, neg64(w));
-    atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
-    atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
-  }
-}
-
-__device__ __forceinline__ bool any_ei(uint64_t x) {
-  uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
-  uint32_t m = __vcmpltu4(__vsub4(lo, 0x01010101u), 0x02020202u) | __vcmpltu4(__vsub4(hi, 0x01010101u), 0x02020202u);
-  return m != 0;
-}
-
 /* Fused sweep over every agent slot, in two launches per tick.
  *   PHASE 0: deaths (get_deaths, model.py:1767-1781) on VD ticks, and the
  *            queue of agents in E or I for disease progression (k_dsq).
@@ -359,17 +307,20 @@ __device__ __forceinline__ bool any_ei(uint64_t x) {
  *            campaigns (fast_sia, :1994-2060), on the ticks that have them,
  *            after progression and the seed schedule as in default_run_order.
  *
- * Each CTA owns a contiguous range of chunks (consecutive chunks mostly share
- * a node, so node counters flush rarely).  Chunk metadata and the columns
- * every agent needs are staged into shared memory with 1-D bulk copies
- * (cp.async.bulk, completion on an mbarrier) through a ring of LPG_NST
- * stages issued ahead of the consumers: on ticks without dense work a stage
- * holds up to LPG_PLAIN_GROUP chunks' state bytes; otherwise one chunk's
- * state plus the dense columns of the tick (date_of_death; ri_timer and
- * chronically_missed; date_of_birth).  The producer reads only shared
- * memory.  Each thread handles 8 consecutive slots: masks are computed from
- * vector shared-memory loads, and only the slots with an event take the
- * scalar path.  Every mbarrier wait is bounded. */
+ * Warp-specialised pipeline.  Each CTA owns a contiguous range of chunks.
+ * One producer warp stages chunk metadata and the columns every agent needs
+ * into shared memory with 1-D bulk copies (cp.async.bulk; completion on a
+ * "full" mbarrier), through a ring of LPG_NST stages; eight consumer warps
+ * process a stage and release it on an "empty" mbarrier.  A stage holds k
+ * consecutive chunks, k = as many as fit in LPG_COL_BYTES given the tick's
+ * columns: state bytes always; date_of_death on VD ticks; ri_timer and
+ * chronically_missed on RI ticks; chronically_missed and date_of_birth on
+ * SIA days.  A warp processes one chunk at a time (every lane the same
+ * chunk, so the same node): its events go to per-warp shared counters,
+ * flushed to the node totals with one global atomic per counter after the
+ * chunk.  There is no CTA-wide barrier in the steady state.  Every mbarrier
+ * wait is bounded; on a timeout the kernel raises an error, stops issuing,
+ * waits (bounded) for the copies it issued and returns. */
 #define LPG_NST 4
 #define LPG_META_BYTES 256
 #define LPG_COL_BYTES (24 * 1024)
@@ -384,6 +335,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
@@ -419,8 +373,7 @@ struct SweepPlan {
   uint8_t flags[LPG_MAX_REPS];
 };
 
-/* Staged bytes per chunk for a simulation's flags: state always, plus the
- * dense columns of the tick. */
+/* Staged bytes per chunk for a simulation's flags. */
 __device__ __forceinline__ int chunk_bytes(uint8_t f) {
   return LPG_CHUNK + ((f & SF_VD) ? 4 * LPG_CHUNK : 0) + ((f & SF_RI) ? 2 * LPG_CHUNK : 0) +
          ((f & (SF_RI | SF_SIA)) ? LPG_CHUNK : 0) + ((f & SF_SIA) ? 4 * LPG_CHUNK : 0);
@@ -430,7 +383,6 @@ __device__ __forceinline__ int stage_chunks(uint8_t f) {
   const int k = LPG_COL_BYTES / chunk_bytes(f);
   return k < LPG_PLAIN_GROUP ? k : LPG_PLAIN_GROUP;
 }
-/* Column offsets inside a stage of k chunks. */
 struct StageLayout {
   int ds, dod, ri, cm, dob;
 };
@@ -487,7 +439,7 @@ __device__ __forceinline__ uint64_t set_byte(uint64_t x, int j, int8_t v) {
 
 /* Append the positions of the set bits of m (slots pos0 + j) to this CTA's
  * slab of the E/I queue: one shared-memory atomic per warp.  Called by all 32
- * lanes. */
+ * lanes of the warp. */
 __device__ __forceinline__ void dsq_append(uint32_t* slab, uint32_t* s_cnt, uint32_t m, int64_t pos0) {
   if (__ballot_sync(FULLMASK, m != 0) == 0) return;
   const int lane = threadIdx.x & 31;
@@ -510,67 +462,118 @@ __device__ __forceinline__ void dsq_append(uint32_t* slab, uint32_t* s_cnt, uint
   }
 }
 
-/* One thread's 8 slots (pos0 .. pos0+7), PHASE 0: deaths; returns the mask
- * of slots in E or I after them (the agents progression must visit). */
-__device__ __forceinline__ uint32_t sweep_slots_a(SweepSmem& S, DevWorld& W, const DevRep* rp, uint8_t fl, int t,
-                                              int64_t cid, int nbo, int o, uint64_t st8, const uint8_t* cols,
-                                              const StageLayout& L, int kk, uint32_t valid) {
+/* Per-warp node counters of the sweep (every lane works on the same chunk). */
+struct WarpCount {
+  int32_t ev[EV_N];
+  int32_t tot[TT_N];
+  unsigned long long sw;
+  unsigned long long bb[LPG_MAX_STRAINS];
+};
+
+/* The warp's counters into the node totals (after each chunk with events). */
+__device__ __forceinline__ void warp_flush(WarpCount& C, DevWorld& W, int g) {
+  __syncwarp();
+  const int lane = threadIdx.x & 31;
+  for (int k = lane; k < EV_N; k += 32) {
+    const int32_t v = C.ev[k];
+    if (v) {
+      atomicAdd(&W.ev[(int64_t)k * W.G + g], v);
+      C.ev[k] = 0;
+    }
+  }
+  if (lane < TT_N) {
+    const int32_t v = C.tot[lane];
+    if (v) {
+      atomicAdd(&W.tot[(int64_t)lane * W.G + g], v);
+      C.tot[lane] = 0;
+    }
+  }
+  if (lane == TT_N) {
+    if (C.sw) atomicAdd((unsigned long long*)&W.sw[g], C.sw);
+    C.sw = 0;
+  }
+  if (lane > TT_N && lane <= TT_N + LPG_MAX_STRAINS) {
+    const int s = lane - TT_N - 1;
+    if (C.bb[s]) atomicAdd((unsigned long long*)&W.bb[(int64_t)s * W.G + g], C.bb[s]);
+    C.bb[s] = 0;
+  }
+  __syncwarp();
+}
+
+/* An agent leaves S: node, chunk and sub-block weights drop by its risk. */
+__device__ __forceinline__ void s_exit_w(WarpCount& C, DevWorld& W, int64_t pos, int64_t cid) {
+  const uint64_t w = fix_risk(W.risk[pos]);
+  atomicAdd(&C.tot[TT_S], -1);
+  if (w) {
+    atomicAdd(&C.sw, neg64(w));
+    atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
+    atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
+  }
+}
+
+/* One thread's 8 slots (pos0 .. pos0+7), PHASE 0 on VD ticks: deaths;
+ * returns the mask of slots in E or I after them. */
+__device__ __forceinline__ uint32_t sweep_slots_a(WarpCount& C, DevWorld& W, const DevRep* rp, int t, int64_t cid,
+                                              int nbo, int o, uint64_t st8, const int32_t* sdod, uint32_t valid,
+                                              bool& ev_any) {
   const int64_t pos0 = cid * LPG_CHUNK + o;
-  uint32_t alive = alive_bits(st8) & valid;
+  const uint32_t alive = alive_bits(st8) & valid;
   uint32_t ei = ei_bits(st8) & valid;
   uint64_t out8 = st8;
-  if (fl & SF_VD) {
-    const int4* d4 = reinterpret_cast<const int4*>(cols + L.dod + kk * 4 * LPG_CHUNK) + (o >> 2);
-    const int4 a = d4[0], b = d4[1];
-    const int32_t dd[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-    uint32_t dead = 0;
+  const int4* d4 = reinterpret_cast<const int4*>(sdod + o);
+  const int4 a = d4[0], b = d4[1];
+  const int32_t dd[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+  uint32_t dead = 0;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) dead |= (uint32_t)(dd[j] <= t && (o + j) < nbo) << j;
-    dead &= alive;
-    while (dead) {
-      const int j = __ffs(dead) - 1;
-      dead &= dead - 1;
-      const int64_t pos = pos0 + j;
-      const int8_t s = (int8_t)(st8 >> (8 * j));
-      atomicAdd(&S.ev[EV_DEATHS], 1);
-      if (s == 0) {
-        s_exit(S, W, pos, cid);
-      } else if (s == 1 || s == 2) {
-        const int st = W.strain[pos];
-        if (s == 1) {
-          atomicAdd(&S.tot[TT_E0 + st], -1);
-        } else {
-          atomicAdd(&S.tot[TT_I0 + st], -1);
-          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-          if (bw) atomicAdd(&S.bb[st], neg64(bw));
-        }
-      } else if (s == 3) {
-        atomicAdd(&S.tot[TT_R], -1);
+  for (int j = 0; j < 8; ++j) dead |= (uint32_t)(dd[j] <= t && (o + j) < nbo) << j;
+  dead &= alive;
+  if (dead) ev_any = true;
+  while (dead) {
+    const int j = __ffs(dead) - 1;
+    dead &= dead - 1;
+    const int64_t pos = pos0 + j;
+    const int8_t s = (int8_t)(st8 >> (8 * j));
+    atomicAdd(&C.ev[EV_DEATHS], 1);
+    if (s == 0) {
+      s_exit_w(C, W, pos, cid);
+    } else if (s == 1 || s == 2) {
+      const int st = W.strain[pos];
+      if (s == 1) {
+        atomicAdd(&C.tot[TT_E0 + st], -1);
+      } else {
+        atomicAdd(&C.tot[TT_I0 + st], -1);
+        const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+        if (bw) atomicAdd(&C.bb[st], neg64(bw));
       }
-      if (W.pp[pos] == 1) atomicAdd(&S.tot[TT_POTP], -1);
-      if (W.par[pos] == 1) atomicAdd(&S.tot[TT_P], -1);
-      out8 = set_byte(out8, j, -1);
-      ei &= ~(1u << j);
+    } else if (s == 3) {
+      atomicAdd(&C.tot[TT_R], -1);
     }
-    if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
+    if (W.pp[pos] == 1) atomicAdd(&C.tot[TT_POTP], -1);
+    if (W.par[pos] == 1) atomicAdd(&C.tot[TT_P], -1);
+    out8 = set_byte(out8, j, -1);
+    ei &= ~(1u << j);
   }
+  if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
   return ei;
 }
 
-/* One thread's 8 slots, PHASE 1: RI then the SIA campaigns of the day. */
-__device__ __forceinline__ void sweep_slots_b(SweepSmem& S, DevWorld& W, const DevRep* rp, uint8_t fl, int t,
-                                              int64_t cid, int ni, int o, uint64_t st8, const uint8_t* cols,
-                                              const StageLayout& L, int kk, uint32_t valid) {
+/* One thread's 8 slots, PHASE 1: RI then the SIA campaigns of the day.
+ * Probability tests are integer compares of the 53-bit draw with the
+ * precomputed thresholds (identical outcomes to the double compares). */
+__device__ __forceinline__ void sweep_slots_b(WarpCount& C, DevWorld& W, const DevRep* rp, uint8_t fl, int t,
+                                              int64_t cid, int ni, int o, uint64_t st8, const uint8_t* scm,
+                                              const int16_t* sri, const int32_t* sdob, uint32_t valid, bool& ev_any) {
   const int64_t pos0 = cid * LPG_CHUNK + o;
-  uint32_t alive = alive_bits(st8) & valid;
-  const uint64_t c8 = *reinterpret_cast<const uint64_t*>(cols + L.cm + kk * LPG_CHUNK + o);
+  const uint32_t alive = alive_bits(st8) & valid;
+  const uint64_t c8 = *reinterpret_cast<const uint64_t*>(scm + o);
   uint32_t reach = alive;
 #pragma unroll
   for (int j = 0; j < 8; ++j)
     if (((c8 >> (8 * j)) & 0xffu) == 1u) reach &= ~(1u << j);
+  if (!reach) return;
   uint64_t out8 = st8;
-  if ((fl & SF_RI) && reach) {
-    int4 rv = *reinterpret_cast<const int4*>(cols + L.ri + kk * 2 * LPG_CHUNK + 2 * o);
+  if (fl & SF_RI) {
+    int4 rv = *reinterpret_cast<const int4*>(sri + o);
     int16_t* r16 = reinterpret_cast<int16_t*>(&rv);
     const int step = rp->ri_step;
     uint32_t elig = 0;
@@ -585,30 +588,32 @@ __device__ __forceinline__ void sweep_slots_b(SweepSmem& S, DevWorld& W, const D
       elig |= (uint32_t)e << j;
     }
     *reinterpret_cast<int4*>(W.ri + pos0) = rv;
+    if (elig) ev_any = true;
+    const uint64_t thr_ri = rp->thr_ri[ni], thr_ipv = rp->thr_ipv[ni];
     while (elig) {
       const int j = __ffs(elig) - 1;
       elig &= elig - 1;
       const int64_t pos = pos0 + j;
       const uint32_t ref = W.ref[pos];
       const int8_t s = (int8_t)(out8 >> (8 * j));
-      if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 0) < rp->p_ri[ni]) {
-        atomicAdd(&S.ev[EV_RIVAC], 1);
+      if (lpg_u53(rp->seed, LPG_P_RI, t, ref, 0, 0) < thr_ri) {
+        atomicAdd(&C.ev[EV_RIVAC], 1);
         if (s == 0) {
           out8 = set_byte(out8, j, 1);
           W.strain[pos] = (int8_t)rp->ri_strain;
-          atomicAdd(&S.ev[EV_RIPROT], 1);
-          s_exit(S, W, pos, cid);
-          atomicAdd(&S.tot[TT_E0 + rp->ri_strain], 1);
+          atomicAdd(&C.ev[EV_RIPROT], 1);
+          s_exit_w(C, W, pos, cid);
+          atomicAdd(&C.tot[TT_E0 + rp->ri_strain], 1);
         }
       }
-      if (lpg_u01(rp->seed, LPG_P_RI, t, ref, 0, 1) < rp->p_ipv[ni]) {
-        atomicAdd(&S.ev[EV_IPVVAC], 1);
+      if (lpg_u53(rp->seed, LPG_P_RI, t, ref, 0, 1) < thr_ipv) {
+        atomicAdd(&C.ev[EV_IPVVAC], 1);
         W.ipv[pos] = 1;
       }
     }
   }
-  if ((fl & SF_SIA) && reach) {
-    const int4* d4 = reinterpret_cast<const int4*>(cols + L.dob + kk * 4 * LPG_CHUNK) + (o >> 2);
+  if (fl & SF_SIA) {
+    const int4* d4 = reinterpret_cast<const int4*>(sdob + o);
     const int4 a = d4[0], b = d4[1];
     const int32_t db[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     for (int k = 0; k < rp->sia_n; ++k) {
@@ -621,20 +626,21 @@ __device__ __forceinline__ void sweep_slots_b(SweepSmem& S, DevWorld& W, const D
         in |= (uint32_t)(ev.min_age <= age && age <= ev.max_age) << j;
       }
       in &= reach;
-      const double p = (double)rp->p_sia[ni];
+      if (in) ev_any = true;
+      const uint64_t tv = ev.thr_vac[ni], tp = ev.thr_pro[ni];
       while (in) {
         const int j = __ffs(in) - 1;
         in &= in - 1;
         const int64_t pos = pos0 + j;
-        const double r = lpg_u01(rp->seed, LPG_P_SIA, t, W.ref[pos], 0, (uint64_t)k);
-        if (r < p) {
-          atomicAdd(&S.ev[EV_SIAVAC0 + k], 1);
-          if ((int8_t)(out8 >> (8 * j)) == 0 && r < p * ev.efficacy) {
+        const uint64_t r = lpg_u53(rp->seed, LPG_P_SIA, t, W.ref[pos], 0, (uint64_t)k);
+        if (r < tv) {
+          atomicAdd(&C.ev[EV_SIAVAC0 + k], 1);
+          if ((int8_t)(out8 >> (8 * j)) == 0 && r < tp) {
             out8 = set_byte(out8, j, 1);
             W.strain[pos] = (int8_t)ev.strain;
-            atomicAdd(&S.ev[EV_SIAPROT0 + k], 1);
-            s_exit(S, W, pos, cid);
-            atomicAdd(&S.tot[TT_E0 + ev.strain], 1);
+            atomicAdd(&C.ev[EV_SIAPROT0 + k], 1);
+            s_exit_w(C, W, pos, cid);
+            atomicAdd(&C.tot[TT_E0 + ev.strain], 1);
           }
         }
       }
@@ -644,12 +650,15 @@ __device__ __forceinline__ void sweep_slots_b(SweepSmem& S, DevWorld& W, const D
 }
 
 template <int PHASE>
-__global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
+__global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   extern __shared__ __align__(128) uint8_t sm_stage[];
-  __shared__ SweepSmem S;
   __shared__ SweepPlan P;
   __shared__ __align__(8) uint64_t full[LPG_NST];
+  __shared__ __align__(8) uint64_t empty[LPG_NST];
+  __shared__ WarpCount WC[LPG_SWEEP_CONSUMERS / 32];
   __shared__ uint32_t s_qcnt;
+  __shared__ int32_t s_issued;
+  __shared__ volatile int s_abort;
   const int R = W.n_reps < LPG_MAX_REPS ? W.n_reps : LPG_MAX_REPS;
   if (threadIdx.x == 0) {
     int32_t acc = 0;
@@ -677,51 +686,62 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
     P.total = acc;
     P.nreps = R;
     s_qcnt = 0;
-    for (int b = 0; b < LPG_NST; ++b) mbar_init(&full[b], 1);
+    s_issued = 0;
+    s_abort = 0;
+    for (int b = 0; b < LPG_NST; ++b) {
+      mbar_init(&full[b], 1);
+      mbar_init(&empty[b], LPG_SWEEP_CONSUMERS);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   {
-    int k = threadIdx.x;
-    if (k < EV_N) S.ev[k] = 0;
-    else if (k < EV_N + TT_N) S.tot[k - EV_N] = 0;
-    else if (k == EV_N + TT_N) S.sw = 0;
-    else if (k < EV_N + TT_N + 1 + LPG_MAX_STRAINS) S.bb[k - EV_N - TT_N - 1] = 0;
+    int32_t* z = reinterpret_cast<int32_t*>(WC);
+    for (int k = threadIdx.x; k < (int)(sizeof(WC) / 4); k += blockDim.x) z[k] = 0;
   }
   __syncthreads();
   const int32_t total = P.total;
   const int32_t per = (total + gridDim.x - 1) / gridDim.x;
   const int32_t w0 = min((int32_t)blockIdx.x * per, total);
   const int32_t w1 = min(w0 + per, total);
-  /* this CTA's slab of the E/I queue starts at its first position */
   uint32_t* slab = W.hits + (int64_t)w0 * LPG_CHUNK;
-  if (w0 < w1) {
-    /* producer (thread 0): the stage starting at work item wp into buffer b */
-    int32_t wp = w0;
-    auto issue = [&](int b) {
-      int r;
-      const int32_t we = stage_end(P, wp, w1, &r);
-      const uint8_t f = P.flags[r];
-      const int64_t cid = P.cbase[r] + (wp - P.off[r]);
-      const int nc = we - wp;
-      const StageLayout L = stage_layout(f, nc);
-      uint8_t* dst = sm_stage + (size_t)b * LPG_STAGE_BYTES;
-      uint8_t* cols = dst + LPG_META_BYTES;
-      const uint32_t bytes = (uint32_t)nc * 16u + (uint32_t)nc * (uint32_t)chunk_bytes(f);
-      mbar_expect_tx(&full[b], bytes);
-      bulk_g2s(dst, W.cmeta + cid, (uint32_t)nc * 16u, &full[b]);
-      bulk_g2s(cols + L.ds, W.ds + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
-      if (f & SF_VD) bulk_g2s(cols + L.dod, W.dod + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
-      if (f & SF_RI) bulk_g2s(cols + L.ri, W.ri + cid * LPG_CHUNK, (uint32_t)nc * 2 * LPG_CHUNK, &full[b]);
-      if (f & (SF_RI | SF_SIA)) bulk_g2s(cols + L.cm, W.cm + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
-      if (f & SF_SIA) bulk_g2s(cols + L.dob, W.dob + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
-      wp = we;
-    };
-    if (threadIdx.x == 0) {
-      for (int b = 0; b < LPG_NST && wp < w1; ++b) issue(b);
-    }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    int cur_g = -1;
-    bool aborted = false;
+  if (warp == LPG_SWEEP_CONSUMERS / 32) {
+    /* ---- producer warp: one lane issues the stages ---- */
+    if (lane == 0 && w0 < w1) {
+      int32_t wp = w0;
+      int32_t i = 0;
+      for (; wp < w1; ++i) {
+        const int b = i % LPG_NST;
+        if (i >= LPG_NST && !mbar_wait(&empty[b], (uint32_t)((i / LPG_NST) - 1) & 1u)) {
+          s_abort = 1;
+          break;
+        }
+        if (s_abort) break;
+        int r;
+        const int32_t we = stage_end(P, wp, w1, &r);
+        const uint8_t f = P.flags[r];
+        const int64_t cid = P.cbase[r] + (wp - P.off[r]);
+        const int nc = we - wp;
+        const StageLayout L = stage_layout(f, nc);
+        uint8_t* dst = sm_stage + (size_t)b * LPG_STAGE_BYTES;
+        uint8_t* cols = dst + LPG_META_BYTES;
+        const uint32_t bytes = (uint32_t)nc * 16u + (uint32_t)nc * (uint32_t)chunk_bytes(f);
+        if (i >= LPG_NST) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&full[b], bytes);
+        bulk_g2s(dst, W.cmeta + cid, (uint32_t)nc * 16u, &full[b]);
+        bulk_g2s(cols + L.ds, W.ds + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
+        if (f & SF_VD) bulk_g2s(cols + L.dod, W.dod + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
+        if (f & SF_RI) bulk_g2s(cols + L.ri, W.ri + cid * LPG_CHUNK, (uint32_t)nc * 2 * LPG_CHUNK, &full[b]);
+        if (f & (SF_RI | SF_SIA)) bulk_g2s(cols + L.cm, W.cm + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
+        if (f & SF_SIA) bulk_g2s(cols + L.dob, W.dob + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
+        wp = we;
+      }
+      s_issued = i;
+    }
+  } else if (w0 < w1) {
+    /* ---- consumer warps ---- */
+    WarpCount& C = WC[warp];
     const int o = threadIdx.x * LPG_SPT;
     int32_t wc = w0;
     for (int32_t i = 0; wc < w1; ++i) {
@@ -729,69 +749,60 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_sweep(DevWorld W) {
       const uint32_t parity = (uint32_t)(i / LPG_NST) & 1u;
       int r;
       const int32_t we = stage_end(P, wc, w1, &r);
-      /* every thread acquires the stage; the CTA agrees on success */
-      const bool ok = __syncthreads_and(mbar_wait(&full[b], parity));
-      if (ok) {
-        const DevRep* rp = &W.reps[r];
-        const uint8_t fl = P.flags[r];
-        const int t = P.tick[r];
-        const uint8_t* stg = sm_stage + (size_t)b * LPG_STAGE_BYTES;
-        const int4* meta = reinterpret_cast<const int4*>(stg);
-        const uint8_t* cols = stg + LPG_META_BYTES;
-        const StageLayout L = stage_layout(fl, we - wc);
-        for (int32_t w = wc; w < we; ++w) {
-          const int kk = w - wc;
-          const int4 m = meta[kk];
-          const int g = m.x;
-          if (g != cur_g) {
-            sweep_flush(S, W, cur_g);
-            cur_g = g;
-          }
-          const int fill = m.y;
-          const int64_t cid = P.cbase[r] + (w - P.off[r]);
-          uint32_t qm = 0;
-          if (o < fill) {
-            const uint32_t valid = fill - o >= 8 ? 0xffu : ((1u << (fill - o)) - 1u);
-            const uint64_t st8 = *reinterpret_cast<const uint64_t*>(cols + L.ds + kk * LPG_CHUNK + o);
-            if (PHASE == 0) {
-              if (fl & SF_VD) {
-                const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
-                qm = sweep_slots_a(S, W, rp, fl, t, cid, nbo, o, st8, cols, L, kk, valid);
-              } else {
-                qm = ei_bits(st8) & valid;
-              }
-            } else {
-              sweep_slots_b(S, W, rp, fl, t, cid, g - rp->node_base, o, st8, cols, L, kk, valid);
-            }
-          }
-          if (PHASE == 0 && (fl & SF_DS)) dsq_append(slab, &s_qcnt, qm, cid * LPG_CHUNK + o);
-        }
-      }
-      wc = we;
+      bool ok = !s_abort && mbar_wait(&full[b], parity);
+      ok = __all_sync(FULLMASK, ok);
       if (!ok) {
-        aborted = true;
+        s_abort = 1;
         break;
       }
-      /* all reads of buffer b are done before it is refilled */
-      __syncthreads();
-      if (threadIdx.x == 0 && wp < w1) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        issue(b);
-      }
-    }
-    if (aborted) {
-      /* leave no bulk copy in flight into this CTA's shared memory */
-      if (threadIdx.x == 0) {
-        W.reps[0].error = LPG_ERR_TIMEOUT;
-        for (int b = 0; b < LPG_NST; ++b) {
-          for (long long it = 0; it < LPG_MBAR_SPIN; ++it) {
-            if (mbar_try_wait(&full[b], 0) || mbar_try_wait(&full[b], 1)) break;
+      const DevRep* rp = &W.reps[r];
+      const uint8_t fl = P.flags[r];
+      const int t = P.tick[r];
+      const uint8_t* stg = sm_stage + (size_t)b * LPG_STAGE_BYTES;
+      const int4* meta = reinterpret_cast<const int4*>(stg);
+      const uint8_t* cols = stg + LPG_META_BYTES;
+      const StageLayout L = stage_layout(fl, we - wc);
+      for (int32_t w = wc; w < we; ++w) {
+        const int kk = w - wc;
+        const int4 m = meta[kk];
+        const int g = m.x;
+        const int fill = m.y;
+        const int64_t cid = P.cbase[r] + (w - P.off[r]);
+        uint32_t qm = 0;
+        bool ev_any = false;
+        if (o < fill) {
+          const uint32_t valid = fill - o >= 8 ? 0xffu : ((1u << (fill - o)) - 1u);
+          const uint64_t st8 = *reinterpret_cast<const uint64_t*>(cols + L.ds + kk * LPG_CHUNK + o);
+          if (PHASE == 0) {
+            if (fl & SF_VD) {
+              const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
+              qm = sweep_slots_a(C, W, rp, t, cid, nbo, o, st8,
+                                 reinterpret_cast<const int32_t*>(cols + L.dod + kk * 4 * LPG_CHUNK), valid, ev_any);
+            } else {
+              qm = ei_bits(st8) & valid;
+            }
+          } else {
+            sweep_slots_b(C, W, rp, fl, t, cid, g - rp->node_base, o, st8, cols + L.cm + kk * LPG_CHUNK,
+                          reinterpret_cast<const int16_t*>(cols + L.ri + kk * 2 * LPG_CHUNK),
+                          reinterpret_cast<const int32_t*>(cols + L.dob + kk * 4 * LPG_CHUNK), valid, ev_any);
           }
         }
+        if (PHASE == 0 && (fl & SF_DS)) dsq_append(slab, &s_qcnt, qm, cid * LPG_CHUNK + o);
+        if (__any_sync(FULLMASK, ev_any)) warp_flush(C, W, g);
       }
-      __syncthreads();
-    } else {
-      sweep_flush(S, W, cur_g);
+      mbar_arrive(&empty[b]);
+      wc = we;
+    }
+  }
+  __syncthreads();
+  if (s_abort && threadIdx.x == LPG_SWEEP_CONSUMERS) {
+    /* leave no bulk copy in flight into this CTA's shared memory */
+    W.reps[0].error = LPG_ERR_TIMEOUT;
+    const int32_t n = s_issued;
+    for (int b = 0; b < LPG_NST; ++b) {
+      int32_t last = -1;
+      for (int32_t j = b; j < n; j += LPG_NST) last = j;
+      if (last >= 0) mbar_wait(&full[b], (uint32_t)(last / LPG_NST) & 1u);
     }
   }
   if (PHASE == 0 && threadIdx.x == 0) {
@@ -870,7 +881,7 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
               W.pp[pos] = 1;
               dPP += 1;
               nPP += 1;
-              if (lpg_u01(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < (double)rp->p_par) {
+              if (lpg_u53(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < rp->thr_par) {
                 W.par[pos] = 1;
                 dP += 1;
                 nP += 1;
@@ -1066,6 +1077,14 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
  * accumulates the incoming infectivity of source nodes l, l+32, ... from the
  * transposed network row (contiguous), then lane 0 adds the 32 partial sums
  * in lane order. */
+/* Node infectivity before mixing as doubles, (double)B * 2^-32: converted
+ * once per node and strain (FP64 throughput is scarce on this part). */
+__global__ void k_beta(DevWorld W) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (int64_t)LPG_MAX_STRAINS * W.G) return;
+  W.beta[q] = (double)W.bb[q] * 0x1.0p-32;
+}
+
 __global__ void k_node_tx(DevWorld W) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -1092,20 +1111,20 @@ __global__ void k_node_tx(DevWorld W) {
   double part[LPG_MAX_STRAINS] = {0.0, 0.0, 0.0, 0.0};
   for (int ii0 = lane; ii0 < n; ii0 += 128) {
     double wv[4];
-    uint64_t bv[4][LPG_MAX_STRAINS];
+    double bv[4][LPG_MAX_STRAINS];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int ii = ii0 + 32 * u;
       wv[u] = ii < n ? nrow[ii] : 0.0;
 #pragma unroll
-      for (int k = 0; k < LPG_MAX_STRAINS; ++k) bv[u][k] = (ii < n && k < ns) ? W.bb[(int64_t)k * G + nb + ii] : 0;
+      for (int k = 0; k < LPG_MAX_STRAINS; ++k) bv[u][k] = (ii < n && k < ns) ? W.beta[(int64_t)k * G + nb + ii] : 0.0;
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (ii0 + 32 * u >= n) break;
 #pragma unroll
       for (int k = 0; k < LPG_MAX_STRAINS; ++k)
-        if (k < ns) part[k] = part[k] + ((double)bv[u][k] * 0x1.0p-32) * wv[u];
+        if (k < ns) part[k] = part[k] + bv[u][k] * wv[u];
     }
   }
   double inc[LPG_MAX_STRAINS];
@@ -1120,9 +1139,8 @@ __global__ void k_node_tx(DevWorld W) {
   int local_zero = 1;
   const double rowsum = rp->rowsum[i];
   for (int k = 0; k < ns; ++k) {
-    const uint64_t bk = W.bb[(int64_t)k * G + g];
-    if (bk != 0) local_zero = 0;
-    double bpre = (double)bk * 0x1.0p-32;
+    if (W.bb[(int64_t)k * G + g] != 0) local_zero = 0;
+    double bpre = W.beta[(int64_t)k * G + g];
     double beta = bpre + (inc[k] - bpre * rowsum);
     beta = (beta * rp->seas[t]) * rp->r0s[i];
     double denom = (double)(pop_t > 1 ? pop_t : 1);
@@ -1240,8 +1258,9 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
       }
     }
     if (!grid_sync(W)) return;
-    /* A2: target offsets of all nodes */
-    if (blockIdx.x == 0) {
+    /* A2: target offsets of all nodes; every CTA computes (and writes) the
+     * same values, so no further grid barrier is needed */
+    {
       int64_t carry = 0;
       for (int base = 0; base < G; base += blockDim.x) {
         int g = base + threadIdx.x;
@@ -1251,11 +1270,12 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
         if (g < G) W.tgt_off[g] = carry + ex;
         carry += tot;
       }
-      if (threadIdx.x == 0) W.tgt_off[G] = carry;
+      if (threadIdx.x == 0) {
+        W.tgt_off[G] = carry;
+        s_K = carry;
+      }
+      __syncthreads();
     }
-    if (!grid_sync(W)) return;
-    if (threadIdx.x == 0) s_K = W.tgt_off[G];
-    __syncthreads();
     const int64_t K = s_K;
     if (K == 0) break;
     if (K > W.hits_cap) {
