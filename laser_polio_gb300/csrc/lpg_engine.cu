@@ -21,7 +21,7 @@
 
 namespace {
 
-const char* kKernelNames[] = {"k_begin", "k_newborns", "k_sweep_a", "k_dsq", "k_seed", "k_sweep_b", "k_beta", "k_node_tx", "k_select", "k_end"};
+const char* kKernelNames[] = {"k_begin", "k_newborns", "k_sweep_a", "k_dsq", "k_seed", "k_sweep_b", "k_evb", "k_node_tx", "k_select", "k_end"};
 constexpr int kNumTickKernels = 10;
 constexpr int kTicksPerGraph = 8;
 
@@ -38,7 +38,8 @@ struct Staging {
 
 struct SimHost {
   lpg_sim_desc d;
-  std::vector<double> birth_rate, p_ri, p_ipv, strain_scal, net, net_t, rowsum, r0s, seas;
+  std::vector<double> birth_rate, p_ri, p_ipv, strain_scal, net, rowsum, r0s, seas;
+  std::vector<uint64_t> netq_t;
   std::vector<float> p_sia;
   std::vector<int64_t> km;
   std::vector<lpg_seed_event> seeds;
@@ -271,9 +272,15 @@ extern "C" int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t devi
     s.net = vec(d.network, n * n, 0.0);
     s.r0s = vec(d.r0_scalars, n, 1.0);
     s.seas = vec(d.seasonality, (size_t)d.nt, 1.0);
-    s.net_t.assign(n * n, 0.0);
+    s.netq_t.assign(n * n, 0);
     for (size_t i = 0; i < n; ++i)
-      for (size_t j = 0; j < n; ++j) s.net_t[j * n + i] = s.net[i * n + j];
+      for (size_t j = 0; j < n; ++j) {
+        const double w = s.net[i * n + j];
+        uint64_t q = 0;
+        if (w >= 4.0) q = 0xFFFFFFFFFFFFFFFFULL;
+        else if (w > 0.0) q = (uint64_t)std::nearbyint(w * 0x1.0p62);
+        s.netq_t[j * n + i] = q;
+      }
     s.rowsum.assign(n, 0.0);
     for (size_t i = 0; i < n; ++i) {
       double acc = 0.0;
@@ -481,8 +488,9 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.dod, P);
   rc |= dalloc(h, &W.ref, P);
   rc |= dalloc(h, &W.cmeta, chunk_total);
-  rc |= dalloc(h, &W.dsq_cnt, 1024);
-  rc |= dalloc(h, &W.dsq_first, 1024);
+  rc |= dalloc(h, &W.qcnt, 2048);
+  rc |= dalloc(h, &W.qfirst, 2048);
+  rc |= dalloc(h, &W.evq, (size_t)chunk_total * LPG_CHUNK);
   rc |= dalloc(h, &W.chunk_w, chunk_total);
   rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.cpref, chunk_total);
@@ -499,7 +507,6 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.nb_end, G);
   rc |= dalloc(h, &W.nb_li0, G);
   rc |= dalloc(h, &W.prob, (size_t)LPG_MAX_STRAINS * G);
-  rc |= dalloc(h, &W.beta, (size_t)LPG_MAX_STRAINS * G);
   rc |= dalloc(h, &W.size, G);
   rc |= dalloc(h, &W.uniq, G);
   rc |= dalloc(h, &W.ksel, G);
@@ -516,8 +523,8 @@ extern "C" int lpg_start(lpg_handle* h) {
   if (rc) return LPG_ERR_NOMEM;
   CK(cudaMemsetAsync(W.ds, 0xff, P, st));
   CK(cudaMemsetAsync(W.ref, 0xff, P * 4, st));
-  CK(cudaMemsetAsync(W.dsq_cnt, 0, 4 * 1024, st));
-  CK(cudaMemsetAsync(W.dsq_first, 0, 4 * 1024, st));
+  CK(cudaMemsetAsync(W.qcnt, 0, 4 * 2048, st));
+  CK(cudaMemsetAsync(W.qfirst, 0, 4 * 2048, st));
   CK(cudaMemsetAsync(W.ev, 0, sizeof(int32_t) * EV_N * G, st));
   CK(cudaMemsetAsync(W.tot, 0, sizeof(int32_t) * TT_N * G, st));
   CK(cudaMemsetAsync(W.sw, 0, sizeof(uint64_t) * G, st));
@@ -578,8 +585,11 @@ extern "C" int lpg_start(lpg_handle* h) {
     rp.strain_scal = dp;
     if (dupload(h, &dp, s.net)) return LPG_ERR_NOMEM;
     rp.net = dp;
-    if (dupload(h, &dp, s.net_t)) return LPG_ERR_NOMEM;
-    rp.net_t = dp;
+    {
+      uint64_t* qp;
+      if (dupload(h, &qp, s.netq_t)) return LPG_ERR_NOMEM;
+      rp.netq_t = qp;
+    }
     if (dupload(h, &dp, s.rowsum)) return LPG_ERR_NOMEM;
     rp.rowsum = dp;
     if (dupload(h, &dp, s.r0s)) return LPG_ERR_NOMEM;
@@ -798,7 +808,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 3: k_dsq<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
     case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
     case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 6: k_beta<<<(LPG_MAX_STRAINS * G + 255) / 256, 256, 0, st>>>(W); break;
+    case 6: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
     case 7: k_node_tx<<<(G * 32 + 63) / 64, 64, 0, st>>>(W); break;
     case 8: {
       cudaLaunchConfig_t cfg = {};

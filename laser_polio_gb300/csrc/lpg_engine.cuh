@@ -113,7 +113,7 @@ typedef struct {
   const double* p_ipv;
   const double* strain_scal;
   const double* net;   /* network[i][j], row-major */
-  const double* net_t; /* transposed: net_t[j][i] = network[i][j] */
+  const uint64_t* netq_t; /* transposed, quantised: netq_t[j][i] = network[i][j] in units of 2^-62 */
   const double* rowsum;
   const double* r0s;
   const double* seas;
@@ -179,15 +179,15 @@ typedef struct {
   int64_t* nb_end;
   int64_t* nb_li0;
   double* prob; /* [LPG_MAX_STRAINS][G] */
-  double* beta; /* [LPG_MAX_STRAINS][G] node infectivity before mixing, as double */
   int64_t* size;
   int64_t* uniq;
   int64_t* ksel;
   int64_t* tgt_off; /* [G + 1] */
-  uint32_t* hits; /* selection targets; also the queue of E/I positions of the tick */
+  uint32_t* hits; /* selection targets */
   int64_t hits_cap;
-  uint32_t* dsq_cnt;  /* per k_sweep<0> CTA: entries in its slab of that queue */
-  int32_t* dsq_first; /* per k_sweep<0> CTA: its first work item (slab offset / CHUNK) */
+  uint64_t* evq;     /* event queues of the sweeps: one slab per sweep CTA */
+  uint32_t* qcnt;    /* [2][1024] entries per slab (k_sweep<0>, k_sweep<1>) */
+  int32_t* qfirst;   /* [2][1024] first work item of the slab's CTA */
   /* grid barrier of the cooperative selection kernel */
   uint32_t* bar_count;
   uint32_t* bar_gen;

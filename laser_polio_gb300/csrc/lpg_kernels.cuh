@@ -8,13 +8,15 @@
  *                counters, births per node (model.py:1711-1716) and their
  *                chunk placement
  *   k_newborns   newborn rows (model.py:1719-1730)
- *   k_sweep<0>   sweep over every chunk: deaths (get_deaths,
+ *   k_sweep<0>   streaming sweep over every chunk: deaths (get_deaths,
  *                model.py:1767-1781) and the queue of agents in E or I
- *   k_dsq        disease progression and paralysis of the queued agents
- *                (model.py:393-454)
+ *   k_dsq        death bookkeeping and disease progression and paralysis of
+ *                the queued agents (model.py:393-454)
  *   k_seed       the seed schedule (model.py:759-786)
- *   k_sweep<1>   RI (fast_ri, :1784-1855) and SIA (fast_sia, :1994-2060)
- *                on the ticks that have them
+ *   k_sweep<1>   streaming sweep on RI/SIA ticks: the RI countdown and the
+ *                queue of agents that RI (fast_ri, :1784-1855) or today's
+ *                SIA campaigns (fast_sia, :1994-2060) reach
+ *   k_evb        their draws and exposures
  *   k_node_tx    per node: population (model.py:1751-1755), mixing,
  *                seasonality, probabilities and exposure counts
  *                (model.py:1327-1407)
@@ -437,14 +439,21 @@ __device__ __forceinline__ uint64_t set_byte(uint64_t x, int j, int8_t v) {
   return (x & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)v << (8 * j));
 }
 
-/* Append the positions of the set bits of m (slots pos0 + j) to this CTA's
- * slab of the E/I queue: one shared-memory atomic per warp.  Called by all 32
- * lanes of the warp. */
-__device__ __forceinline__ void dsq_append(uint32_t* slab, uint32_t* s_cnt, uint32_t m, int64_t pos0) {
-  if (__ballot_sync(FULLMASK, m != 0) == 0) return;
+/* Queue entries of the sweeps (u64): bits 0-31 position, bits 32-47 kind or
+ * event flags, bits 48-55 the state byte before the sweep (deaths). */
+#define QA_DS 1u
+#define QA_DEATH 2u
+#define QB_RI 1u /* bit 0: RI-eligible; bit 1 + k: candidate of SIA event k */
+
+__device__ __forceinline__ uint64_t q_entry(int64_t pos, uint32_t kind, uint32_t old_state) {
+  return (uint64_t)(uint32_t)pos | ((uint64_t)(kind & 0xffffu) << 32) | ((uint64_t)(old_state & 0xffu) << 48);
+}
+
+/* Reserve n entries of this CTA's slab for each lane (warp scan + one shared
+ * atomic per warp); returns the lane's first index.  All 32 lanes call. */
+__device__ __forceinline__ uint32_t slab_reserve(uint32_t* s_cnt, uint32_t n) {
   const int lane = threadIdx.x & 31;
-  const uint32_t c = __popc(m);
-  uint32_t x = c;
+  uint32_t x = n;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     uint32_t y = __shfl_up_sync(FULLMASK, x, o);
@@ -452,201 +461,100 @@ __device__ __forceinline__ void dsq_append(uint32_t* slab, uint32_t* s_cnt, uint
   }
   const uint32_t tot = __shfl_sync(FULLMASK, x, 31);
   uint32_t base = 0;
-  if (lane == 31) base = atomicAdd(s_cnt, tot);
+  if (lane == 31 && tot) base = atomicAdd(s_cnt, tot);
   base = __shfl_sync(FULLMASK, base, 31);
-  uint32_t at = base + x - c;
-  while (m) {
-    const int j = __ffs(m) - 1;
-    m &= m - 1;
-    slab[at++] = (uint32_t)(pos0 + j);
-  }
+  return base + x - n;
 }
 
-/* Per-warp node counters of the sweep (every lane works on the same chunk). */
-struct WarpCount {
-  int32_t ev[EV_N];
-  int32_t tot[TT_N];
-  unsigned long long sw;
-  unsigned long long bb[LPG_MAX_STRAINS];
-};
-
-/* The warp's counters into the node totals (after each chunk with events). */
-__device__ __forceinline__ void warp_flush(WarpCount& C, DevWorld& W, int g) {
-  __syncwarp();
-  const int lane = threadIdx.x & 31;
-  for (int k = lane; k < EV_N; k += 32) {
-    const int32_t v = C.ev[k];
-    if (v) {
-      atomicAdd(&W.ev[(int64_t)k * W.G + g], v);
-      C.ev[k] = 0;
-    }
-  }
-  if (lane < TT_N) {
-    const int32_t v = C.tot[lane];
-    if (v) {
-      atomicAdd(&W.tot[(int64_t)lane * W.G + g], v);
-      C.tot[lane] = 0;
-    }
-  }
-  if (lane == TT_N) {
-    if (C.sw) atomicAdd((unsigned long long*)&W.sw[g], C.sw);
-    C.sw = 0;
-  }
-  if (lane > TT_N && lane <= TT_N + LPG_MAX_STRAINS) {
-    const int s = lane - TT_N - 1;
-    if (C.bb[s]) atomicAdd((unsigned long long*)&W.bb[(int64_t)s * W.G + g], C.bb[s]);
-    C.bb[s] = 0;
-  }
-  __syncwarp();
-}
-
-/* An agent leaves S: node, chunk and sub-block weights drop by its risk. */
-__device__ __forceinline__ void s_exit_w(WarpCount& C, DevWorld& W, int64_t pos, int64_t cid) {
-  const uint64_t w = fix_risk(W.risk[pos]);
-  atomicAdd(&C.tot[TT_S], -1);
-  if (w) {
-    atomicAdd(&C.sw, neg64(w));
-    atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
-    atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
-  }
-}
-
-/* One thread's 8 slots (pos0 .. pos0+7), PHASE 0 on VD ticks: deaths;
- * returns the mask of slots in E or I after them. */
-__device__ __forceinline__ uint32_t sweep_slots_a(WarpCount& C, DevWorld& W, const DevRep* rp, int t, int64_t cid,
-                                              int nbo, int o, uint64_t st8, const int32_t* sdod, uint32_t valid,
-                                              bool& ev_any) {
-  const int64_t pos0 = cid * LPG_CHUNK + o;
-  const uint32_t alive = alive_bits(st8) & valid;
-  uint32_t ei = ei_bits(st8) & valid;
-  uint64_t out8 = st8;
-  const int4* d4 = reinterpret_cast<const int4*>(sdod + o);
-  const int4 a = d4[0], b = d4[1];
-  const int32_t dd[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-  uint32_t dead = 0;
+/* PHASE 0, one thread's 8 slots: deaths are written here (state -1) and
+ * queued with their old state for the bookkeeping; agents in E or I that
+ * survive are queued for progression. */
+__device__ __forceinline__ void sweep_a8(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, bool on, bool vd, int t,
+                                         int64_t pos0, int nbo, int o, uint64_t st8, const int32_t* sdod,
+                                         uint32_t valid) {
+  uint32_t ei = 0, dead = 0;
+  if (on) {
+    ei = ei_bits(st8) & valid;
+    if (vd) {
+      const uint32_t alive = alive_bits(st8) & valid;
+      const int4* d4 = reinterpret_cast<const int4*>(sdod + o);
+      const int4 a = d4[0], b = d4[1];
+      const int32_t dd[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 #pragma unroll
-  for (int j = 0; j < 8; ++j) dead |= (uint32_t)(dd[j] <= t && (o + j) < nbo) << j;
-  dead &= alive;
-  if (dead) ev_any = true;
-  while (dead) {
-    const int j = __ffs(dead) - 1;
-    dead &= dead - 1;
-    const int64_t pos = pos0 + j;
-    const int8_t s = (int8_t)(st8 >> (8 * j));
-    atomicAdd(&C.ev[EV_DEATHS], 1);
-    if (s == 0) {
-      s_exit_w(C, W, pos, cid);
-    } else if (s == 1 || s == 2) {
-      const int st = W.strain[pos];
-      if (s == 1) {
-        atomicAdd(&C.tot[TT_E0 + st], -1);
-      } else {
-        atomicAdd(&C.tot[TT_I0 + st], -1);
-        const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-        if (bw) atomicAdd(&C.bb[st], neg64(bw));
-      }
-    } else if (s == 3) {
-      atomicAdd(&C.tot[TT_R], -1);
-    }
-    if (W.pp[pos] == 1) atomicAdd(&C.tot[TT_POTP], -1);
-    if (W.par[pos] == 1) atomicAdd(&C.tot[TT_P], -1);
-    out8 = set_byte(out8, j, -1);
-    ei &= ~(1u << j);
-  }
-  if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
-  return ei;
-}
-
-/* One thread's 8 slots, PHASE 1: RI then the SIA campaigns of the day.
- * Probability tests are integer compares of the 53-bit draw with the
- * precomputed thresholds (identical outcomes to the double compares). */
-__device__ __forceinline__ void sweep_slots_b(WarpCount& C, DevWorld& W, const DevRep* rp, uint8_t fl, int t,
-                                              int64_t cid, int ni, int o, uint64_t st8, const uint8_t* scm,
-                                              const int16_t* sri, const int32_t* sdob, uint32_t valid, bool& ev_any) {
-  const int64_t pos0 = cid * LPG_CHUNK + o;
-  const uint32_t alive = alive_bits(st8) & valid;
-  const uint64_t c8 = *reinterpret_cast<const uint64_t*>(scm + o);
-  uint32_t reach = alive;
+      for (int j = 0; j < 8; ++j) dead |= (uint32_t)(dd[j] <= t && (o + j) < nbo) << j;
+      dead &= alive;
+      if (dead) {
+        uint64_t out8 = st8;
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
-    if (((c8 >> (8 * j)) & 0xffu) == 1u) reach &= ~(1u << j);
-  if (!reach) return;
-  uint64_t out8 = st8;
-  if (fl & SF_RI) {
-    int4 rv = *reinterpret_cast<const int4*>(sri + o);
-    int16_t* r16 = reinterpret_cast<int16_t*>(&rv);
-    const int step = rp->ri_step;
-    uint32_t elig = 0;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      if (!((reach >> j) & 1u)) continue;
-      const int32_t timer = (int32_t)r16[j] - step;
-      r16[j] = (int16_t)(uint16_t)(uint32_t)timer;
-      bool e = false;
-      if (t == step) e = timer <= 0 && timer >= -step;
-      else if (t > step) e = timer <= 0 && timer > -step;
-      elig |= (uint32_t)e << j;
-    }
-    *reinterpret_cast<int4*>(W.ri + pos0) = rv;
-    if (elig) ev_any = true;
-    const uint64_t thr_ri = rp->thr_ri[ni], thr_ipv = rp->thr_ipv[ni];
-    while (elig) {
-      const int j = __ffs(elig) - 1;
-      elig &= elig - 1;
-      const int64_t pos = pos0 + j;
-      const uint32_t ref = W.ref[pos];
-      const int8_t s = (int8_t)(out8 >> (8 * j));
-      if (lpg_u53(rp->seed, LPG_P_RI, t, ref, 0, 0) < thr_ri) {
-        atomicAdd(&C.ev[EV_RIVAC], 1);
-        if (s == 0) {
-          out8 = set_byte(out8, j, 1);
-          W.strain[pos] = (int8_t)rp->ri_strain;
-          atomicAdd(&C.ev[EV_RIPROT], 1);
-          s_exit_w(C, W, pos, cid);
-          atomicAdd(&C.tot[TT_E0 + rp->ri_strain], 1);
-        }
-      }
-      if (lpg_u53(rp->seed, LPG_P_RI, t, ref, 0, 1) < thr_ipv) {
-        atomicAdd(&C.ev[EV_IPVVAC], 1);
-        W.ipv[pos] = 1;
+        for (int j = 0; j < 8; ++j)
+          if ((dead >> j) & 1u) out8 |= 0xffULL << (8 * j);
+        *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
+        ei &= ~dead;
       }
     }
   }
-  if (fl & SF_SIA) {
-    const int4* d4 = reinterpret_cast<const int4*>(sdob + o);
-    const int4 a = d4[0], b = d4[1];
-    const int32_t db[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-    for (int k = 0; k < rp->sia_n; ++k) {
-      const DevSia& ev = rp->sia[rp->sia_i0 + k];
-      if (ev.mask[ni] == 0) continue;
-      uint32_t in = 0;
+  if (__ballot_sync(FULLMASK, (ei | dead) != 0) == 0) return;
+  uint32_t at = slab_reserve(s_cnt, __popc(ei) + __popc(dead));
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if ((ei >> j) & 1u) slab[at++] = q_entry(pos0 + j, QA_DS, 0);
+    if ((dead >> j) & 1u) slab[at++] = q_entry(pos0 + j, QA_DEATH, (uint32_t)(st8 >> (8 * j)));
+  }
+}
+
+/* PHASE 1, one thread's 8 slots: the RI timer countdown (dense) and the
+ * masks of the agents that RI or today's SIA campaigns reach; those are
+ * queued with their event flags. */
+__device__ __forceinline__ void sweep_b8(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, bool on, const DevRep* rp,
+                                         uint8_t fl, int t, int ni, int64_t pos0, int o, uint64_t st8,
+                                         const uint8_t* scm, const int16_t* sri, const int32_t* sdob,
+                                         uint32_t valid) {
+  uint32_t f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  uint32_t any = 0;
+  if (on) {
+    uint32_t reach = alive_bits(st8) & valid;
+    const uint64_t c8 = *reinterpret_cast<const uint64_t*>(scm + o);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (((c8 >> (8 * j)) & 0xffu) == 1u) reach &= ~(1u << j);
+    if (reach && (fl & SF_RI)) {
+      int4 rv = *reinterpret_cast<const int4*>(sri + o);
+      int16_t* r16 = reinterpret_cast<int16_t*>(&rv);
+      const int step = rp->ri_step;
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const int64_t age = (int64_t)t - (int64_t)db[j];
-        in |= (uint32_t)(ev.min_age <= age && age <= ev.max_age) << j;
+        if (!((reach >> j) & 1u)) continue;
+        const int32_t timer = (int32_t)r16[j] - step;
+        r16[j] = (int16_t)(uint16_t)(uint32_t)timer;
+        bool e = false;
+        if (t == step) e = timer <= 0 && timer >= -step;
+        else if (t > step) e = timer <= 0 && timer > -step;
+        f[j] |= e ? QB_RI : 0u;
       }
-      in &= reach;
-      if (in) ev_any = true;
-      const uint64_t tv = ev.thr_vac[ni], tp = ev.thr_pro[ni];
-      while (in) {
-        const int j = __ffs(in) - 1;
-        in &= in - 1;
-        const int64_t pos = pos0 + j;
-        const uint64_t r = lpg_u53(rp->seed, LPG_P_SIA, t, W.ref[pos], 0, (uint64_t)k);
-        if (r < tv) {
-          atomicAdd(&C.ev[EV_SIAVAC0 + k], 1);
-          if ((int8_t)(out8 >> (8 * j)) == 0 && r < tp) {
-            out8 = set_byte(out8, j, 1);
-            W.strain[pos] = (int8_t)ev.strain;
-            atomicAdd(&C.ev[EV_SIAPROT0 + k], 1);
-            s_exit_w(C, W, pos, cid);
-            atomicAdd(&C.tot[TT_E0 + ev.strain], 1);
-          }
+      *reinterpret_cast<int4*>(W.ri + pos0) = rv;
+    }
+    if (reach && (fl & SF_SIA)) {
+      const int4* d4 = reinterpret_cast<const int4*>(sdob + o);
+      const int4 a = d4[0], b = d4[1];
+      const int32_t db[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+      for (int k = 0; k < rp->sia_n; ++k) {
+        const DevSia& ev = rp->sia[rp->sia_i0 + k];
+        if (ev.mask[ni] == 0) continue;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int64_t age = (int64_t)t - (int64_t)db[j];
+          if (((reach >> j) & 1u) && ev.min_age <= age && age <= ev.max_age) f[j] |= 2u << k;
         }
       }
     }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) any += f[j] != 0;
   }
-  if (out8 != st8) *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
+  if (__ballot_sync(FULLMASK, any != 0) == 0) return;
+  uint32_t at = slab_reserve(s_cnt, any);
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    if (f[j]) slab[at++] = q_entry(pos0 + j, f[j], 0);
 }
 
 template <int PHASE>
@@ -655,7 +563,6 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   __shared__ SweepPlan P;
   __shared__ __align__(8) uint64_t full[LPG_NST];
   __shared__ __align__(8) uint64_t empty[LPG_NST];
-  __shared__ WarpCount WC[LPG_SWEEP_CONSUMERS / 32];
   __shared__ uint32_t s_qcnt;
   __shared__ int32_t s_issued;
   __shared__ volatile int s_abort;
@@ -694,16 +601,12 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  {
-    int32_t* z = reinterpret_cast<int32_t*>(WC);
-    for (int k = threadIdx.x; k < (int)(sizeof(WC) / 4); k += blockDim.x) z[k] = 0;
-  }
   __syncthreads();
   const int32_t total = P.total;
   const int32_t per = (total + gridDim.x - 1) / gridDim.x;
   const int32_t w0 = min((int32_t)blockIdx.x * per, total);
   const int32_t w1 = min(w0 + per, total);
-  uint32_t* slab = W.hits + (int64_t)w0 * LPG_CHUNK;
+  uint64_t* slab = W.evq + (int64_t)w0 * LPG_CHUNK;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (warp == LPG_SWEEP_CONSUMERS / 32) {
@@ -741,7 +644,6 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
     }
   } else if (w0 < w1) {
     /* ---- consumer warps ---- */
-    WarpCount& C = WC[warp];
     const int o = threadIdx.x * LPG_SPT;
     int32_t wc = w0;
     for (int32_t i = 0; wc < w1; ++i) {
@@ -765,30 +667,23 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       for (int32_t w = wc; w < we; ++w) {
         const int kk = w - wc;
         const int4 m = meta[kk];
-        const int g = m.x;
         const int fill = m.y;
         const int64_t cid = P.cbase[r] + (w - P.off[r]);
-        uint32_t qm = 0;
-        bool ev_any = false;
-        if (o < fill) {
-          const uint32_t valid = fill - o >= 8 ? 0xffu : ((1u << (fill - o)) - 1u);
-          const uint64_t st8 = *reinterpret_cast<const uint64_t*>(cols + L.ds + kk * LPG_CHUNK + o);
-          if (PHASE == 0) {
-            if (fl & SF_VD) {
-              const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
-              qm = sweep_slots_a(C, W, rp, t, cid, nbo, o, st8,
-                                 reinterpret_cast<const int32_t*>(cols + L.dod + kk * 4 * LPG_CHUNK), valid, ev_any);
-            } else {
-              qm = ei_bits(st8) & valid;
-            }
-          } else {
-            sweep_slots_b(C, W, rp, fl, t, cid, g - rp->node_base, o, st8, cols + L.cm + kk * LPG_CHUNK,
-                          reinterpret_cast<const int16_t*>(cols + L.ri + kk * 2 * LPG_CHUNK),
-                          reinterpret_cast<const int32_t*>(cols + L.dob + kk * 4 * LPG_CHUNK), valid, ev_any);
+        const int64_t pos0 = cid * LPG_CHUNK + o;
+        const bool on = o < fill;
+        const uint32_t valid = !on ? 0u : (fill - o >= 8 ? 0xffu : ((1u << (fill - o)) - 1u));
+        const uint64_t st8 = on ? *reinterpret_cast<const uint64_t*>(cols + L.ds + kk * LPG_CHUNK + o) : ~0ULL;
+        if (PHASE == 0) {
+          if (fl & SF_DS || fl & SF_VD) {
+            const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
+            sweep_a8(W, slab, &s_qcnt, on, (fl & SF_VD) != 0, t, pos0, nbo, o, st8,
+                     reinterpret_cast<const int32_t*>(cols + L.dod + kk * 4 * LPG_CHUNK), valid);
           }
+        } else {
+          sweep_b8(W, slab, &s_qcnt, on, rp, fl, t, m.x - rp->node_base, pos0, o, st8, cols + L.cm + kk * LPG_CHUNK,
+                   reinterpret_cast<const int16_t*>(cols + L.ri + kk * 2 * LPG_CHUNK),
+                   reinterpret_cast<const int32_t*>(cols + L.dob + kk * 4 * LPG_CHUNK), valid);
         }
-        if (PHASE == 0 && (fl & SF_DS)) dsq_append(slab, &s_qcnt, qm, cid * LPG_CHUNK + o);
-        if (__any_sync(FULLMASK, ev_any)) warp_flush(C, W, g);
       }
       mbar_arrive(&empty[b]);
       wc = we;
@@ -805,99 +700,141 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       if (last >= 0) mbar_wait(&full[b], (uint32_t)(last / LPG_NST) & 1u);
     }
   }
-  if (PHASE == 0 && threadIdx.x == 0) {
-    W.dsq_cnt[blockIdx.x] = s_qcnt;
-    W.dsq_first[blockIdx.x] = w0;
+  if (threadIdx.x == 0) {
+    W.qcnt[PHASE * 1024 + blockIdx.x] = s_qcnt;
+    W.qfirst[PHASE * 1024 + blockIdx.x] = w0;
   }
 }
 
 /* ------------------------------------------------------------------------ */
-/* Disease progression (disease_state_step_kernel, model.py:393-454) of the
- * agents queued by k_sweep<0>, one thread per agent.  Node counters are
- * aggregated across the warp's lanes that share a node before the atomics. */
+/* Queue kernels: one thread per queued agent.  The queue is one slab per CTA
+ * of the sweep; entries of a warp mostly belong to one node, so node counters
+ * are summed across the lanes that share a node before the global atomics. */
 __device__ __forceinline__ void warp_add(int32_t* p, unsigned peers, int32_t v) {
   const int32_t tot = __reduce_add_sync(peers, v);
   if ((threadIdx.x & 31) == __ffs(peers) - 1 && tot) atomicAdd(p, tot);
 }
 
-__global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
-  /* the queue is one slab per CTA of k_sweep<0>: prefix of their counts */
-  __shared__ uint32_t s_pre[1025];
-  if (threadIdx.x == 0) {
-    uint32_t acc = 0;
-    for (int b = 0; b < nslabs; ++b) {
-      s_pre[b] = acc;
-      acc += W.dsq_cnt[b];
-    }
-    s_pre[nslabs] = acc;
+/* Entry q of the queue of sweep PHASE (prefix of the slab sizes in s_pre). */
+__device__ __forceinline__ uint64_t q_get(const DevWorld& W, int phase, const uint32_t* s_pre, int nslabs, uint32_t q) {
+  int lo = 0, hi = nslabs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (s_pre[mid] <= q) lo = mid; else hi = mid - 1;
   }
+  return W.evq[(int64_t)W.qfirst[phase * 1024 + lo] * LPG_CHUNK + (q - s_pre[lo])];
+}
+
+__device__ __forceinline__ uint32_t q_prefix(const DevWorld& W, int phase, uint32_t* s_pre, int nslabs) {
+  int64_t carry = 0;
+  for (int base = 0; base < nslabs; base += blockDim.x) {
+    const int b = base + threadIdx.x;
+    const int64_t v = b < nslabs ? W.qcnt[phase * 1024 + b] : 0;
+    int64_t tot;
+    const int64_t ex = block_excl_scan(v, &tot);
+    if (b < nslabs) s_pre[b] = (uint32_t)(carry + ex);
+    carry += tot;
+  }
+  if (threadIdx.x == 0) s_pre[nslabs] = (uint32_t)carry;
   __syncthreads();
-  const uint32_t n = s_pre[nslabs];
+  return s_pre[nslabs];
+}
+
+/* Queue of k_sweep<0>: deaths (bookkeeping of get_deaths, model.py:1767-1781)
+ * and disease progression (disease_state_step_kernel, model.py:393-454). */
+__global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
+  __shared__ uint32_t s_pre[1025];
+  const uint32_t n = q_prefix(W, 0, s_pre, nslabs);
   const int64_t G = W.G;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t q = base + threadIdx.x;
     const bool on = q < n;
     int g = -1, st = 0;
-    int32_t dE = 0, dI = 0, dR = 0, dPP = 0, dP = 0, nPP = 0, nP = 0;
-    int64_t pos = 0;
+    int32_t dS = 0, dE = 0, dI = 0, dR = 0, dPP = 0, dP = 0, nPP = 0, nP = 0, nDead = 0;
     if (on) {
-      int lo = 0, hi = nslabs - 1; /* slab holding entry q */
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (s_pre[mid] <= q) lo = mid; else hi = mid - 1;
-      }
-      pos = W.hits[(int64_t)W.dsq_first[lo] * LPG_CHUNK + (q - s_pre[lo])];
+      const uint64_t e = q_get(W, 0, s_pre, nslabs, q);
+      const int64_t pos = (int64_t)(uint32_t)e;
+      const uint32_t kind = (uint32_t)(e >> 32) & 0xffffu;
       const int64_t cid = pos / LPG_CHUNK;
       g = W.cmeta[cid].x;
       const DevRep* rp = &W.reps[W.node_rep[g]];
       const int t = rp->cur_t;
-      int8_t s = W.ds[pos];
-      st = W.strain[pos];
-      if (s == 1) {
-        const int8_t e = W.et[pos];
-        if (e <= 0) {
-          s = 2;
-          dE -= 1;
-          dI += 1;
-          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], (unsigned long long)bw);
-        }
-        W.et[pos] = dec_i8(e);
-      }
-      if (s == 2) {
-        const int8_t i = W.it[pos];
-        if (i <= 0) {
-          s = 3;
-          dI -= 1;
-          dR += 1;
-          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
-        }
-        W.it[pos] = dec_i8(i);
-        if (st == 0) {
-          const int8_t p = W.pt[pos];
-          if (p <= 0 && W.pp[pos] == -1) {
-            if (W.ipv[pos] == 0) {
-              W.pp[pos] = 1;
-              dPP += 1;
-              nPP += 1;
-              if (lpg_u53(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < rp->thr_par) {
-                W.par[pos] = 1;
-                dP += 1;
-                nP += 1;
-              }
-            } else {
-              W.pp[pos] = 0;
-            }
+      if (kind == QA_DEATH) {
+        const int8_t s = (int8_t)(uint8_t)(e >> 48);
+        nDead = 1;
+        if (s == 0) {
+          dS = -1;
+          const uint64_t w = fix_risk(W.risk[pos]);
+          if (w) {
+            atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
+            atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
+            atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
           }
-          W.pt[pos] = dec_i8(p);
+        } else if (s == 1 || s == 2) {
+          st = W.strain[pos];
+          if (s == 1) {
+            dE = -1;
+          } else {
+            dI = -1;
+            const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+            if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
+          }
+        } else if (s == 3) {
+          dR = -1;
         }
+        if (W.pp[pos] == 1) dPP -= 1;
+        if (W.par[pos] == 1) dP -= 1;
+      } else {
+        int8_t s = W.ds[pos];
+        st = W.strain[pos];
+        if (s == 1) {
+          const int8_t ex = W.et[pos];
+          if (ex <= 0) {
+            s = 2;
+            dE -= 1;
+            dI += 1;
+            const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+            if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], (unsigned long long)bw);
+          }
+          W.et[pos] = dec_i8(ex);
+        }
+        if (s == 2) {
+          const int8_t i = W.it[pos];
+          if (i <= 0) {
+            s = 3;
+            dI -= 1;
+            dR += 1;
+            const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+            if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
+          }
+          W.it[pos] = dec_i8(i);
+          if (st == 0) {
+            const int8_t p = W.pt[pos];
+            if (p <= 0 && W.pp[pos] == -1) {
+              if (W.ipv[pos] == 0) {
+                W.pp[pos] = 1;
+                dPP += 1;
+                nPP += 1;
+                if (lpg_u53(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < rp->thr_par) {
+                  W.par[pos] = 1;
+                  dP += 1;
+                  nP += 1;
+                }
+              } else {
+                W.pp[pos] = 0;
+              }
+            }
+            W.pt[pos] = dec_i8(p);
+          }
+        }
+        W.ds[pos] = s;
       }
-      W.ds[pos] = s;
     }
     const unsigned act = __ballot_sync(FULLMASK, on);
     if (!on) continue;
     const unsigned by_node = __match_any_sync(act, g);
+    warp_add(&W.ev[(int64_t)EV_DEATHS * G + g], by_node, nDead);
+    warp_add(&W.tot[(int64_t)TT_S * G + g], by_node, dS);
     warp_add(&W.tot[(int64_t)TT_R * G + g], by_node, dR);
     warp_add(&W.tot[(int64_t)TT_POTP * G + g], by_node, dPP);
     warp_add(&W.tot[(int64_t)TT_P * G + g], by_node, dP);
@@ -906,6 +843,99 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
     const unsigned by_ns = __match_any_sync(act, g * LPG_MAX_STRAINS + st);
     warp_add(&W.tot[(int64_t)(TT_E0 + st) * G + g], by_ns, dE);
     warp_add(&W.tot[(int64_t)(TT_I0 + st) * G + g], by_ns, dI);
+  }
+}
+
+/* Queue of k_sweep<1>: the draws of RI (fast_ri, model.py:1845-1854) and of
+ * the SIA campaigns of the day (fast_sia, :2047-2059), in that order per
+ * agent.  Probability tests are integer compares of the 53-bit draw with
+ * precomputed thresholds (same outcome as the double compares). */
+__global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
+  __shared__ uint32_t s_pre[1025];
+  const uint32_t n = q_prefix(W, 1, s_pre, nslabs);
+  const int64_t G = W.G;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t q = base + threadIdx.x;
+    const bool on = q < n;
+    int g = -1;
+    int32_t rivac = 0, riprot = 0, ipvvac = 0, dS = 0;
+    int32_t dE[LPG_MAX_STRAINS] = {0, 0, 0, 0};
+    int32_t sv[LPG_MAX_SIA_PER_DAY] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int32_t sp[LPG_MAX_SIA_PER_DAY] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int nsia = 0;
+    if (on) {
+      const uint64_t e = q_get(W, 1, s_pre, nslabs, q);
+      const int64_t pos = (int64_t)(uint32_t)e;
+      const uint32_t fl = (uint32_t)(e >> 32) & 0xffffu;
+      const int64_t cid = pos / LPG_CHUNK;
+      g = W.cmeta[cid].x;
+      const DevRep* rp = &W.reps[W.node_rep[g]];
+      const int t = rp->cur_t, ni = g - rp->node_base;
+      const uint32_t ref = W.ref[pos];
+      int8_t s = W.ds[pos];
+      const int8_t s_in = s;
+      bool exposed = false;
+      if (fl & QB_RI) {
+        if (lpg_u53(rp->seed, LPG_P_RI, t, ref, 0, 0) < rp->thr_ri[ni]) {
+          rivac = 1;
+          if (s == 0) {
+            s = 1;
+            W.strain[pos] = (int8_t)rp->ri_strain;
+            riprot = 1;
+            dE[rp->ri_strain] += 1;
+            exposed = true;
+          }
+        }
+        if (lpg_u53(rp->seed, LPG_P_RI, t, ref, 0, 1) < rp->thr_ipv[ni]) {
+          ipvvac = 1;
+          W.ipv[pos] = 1;
+        }
+      }
+      nsia = rp->sia_n;
+#pragma unroll
+      for (int k = 0; k < LPG_MAX_SIA_PER_DAY; ++k) {
+        if (k >= nsia) break;
+        if (!((fl >> (1 + k)) & 1u)) continue;
+        const DevSia& ev = rp->sia[rp->sia_i0 + k];
+        const uint64_t r = lpg_u53(rp->seed, LPG_P_SIA, t, ref, 0, (uint64_t)k);
+        if (r < ev.thr_vac[ni]) {
+          sv[k] = 1;
+          if (s == 0 && r < ev.thr_pro[ni]) {
+            s = 1;
+            W.strain[pos] = (int8_t)ev.strain;
+            sp[k] = 1;
+            dE[ev.strain] += 1;
+            exposed = true;
+          }
+        }
+      }
+      if (exposed) {
+        dS = -1;
+        const uint64_t w = fix_risk(W.risk[pos]);
+        if (w) {
+          atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
+          atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
+          atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
+        }
+      }
+      if (s != s_in) W.ds[pos] = s;
+    }
+    const unsigned act = __ballot_sync(FULLMASK, on);
+    if (!on) continue;
+    const unsigned by_node = __match_any_sync(act, g);
+    warp_add(&W.ev[(int64_t)EV_RIVAC * G + g], by_node, rivac);
+    warp_add(&W.ev[(int64_t)EV_RIPROT * G + g], by_node, riprot);
+    warp_add(&W.ev[(int64_t)EV_IPVVAC * G + g], by_node, ipvvac);
+    warp_add(&W.tot[(int64_t)TT_S * G + g], by_node, dS);
+#pragma unroll
+    for (int k = 0; k < LPG_MAX_STRAINS; ++k) warp_add(&W.tot[(int64_t)(TT_E0 + k) * G + g], by_node, dE[k]);
+    const int ns_max = __reduce_max_sync(by_node, nsia);
+#pragma unroll
+    for (int k = 0; k < LPG_MAX_SIA_PER_DAY; ++k) {
+      if (k >= ns_max) break;
+      warp_add(&W.ev[(int64_t)(EV_SIAVAC0 + k) * G + g], by_node, sv[k]);
+      warp_add(&W.ev[(int64_t)(EV_SIAPROT0 + k) * G + g], by_node, sp[k]);
+    }
   }
 }
 
@@ -1077,14 +1107,11 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
  * accumulates the incoming infectivity of source nodes l, l+32, ... from the
  * transposed network row (contiguous), then lane 0 adds the 32 partial sums
  * in lane order. */
-/* Node infectivity before mixing as doubles, (double)B * 2^-32: converted
- * once per node and strain (FP64 throughput is scarce on this part). */
-__global__ void k_beta(DevWorld W) {
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= (int64_t)LPG_MAX_STRAINS * W.G) return;
-  W.beta[q] = (double)W.bb[q] * 0x1.0p-32;
-}
-
+/* Node-level force of infection and exposure counts (model.py:1327-1407);
+ * the same arithmetic, in the same order, as the oracle's lpo_node_tx.
+ * One warp per node.  Incoming infectivity sum_i B_i N[i][n] is exact
+ * integer arithmetic: B in units of 2^-32 times the network weight in units
+ * of 2^-62 (transposed row, contiguous), 128-bit sums, one conversion. */
 __global__ void k_node_tx(DevWorld W) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -1107,31 +1134,36 @@ __global__ void k_node_tx(DevWorld W) {
     W.uniq[g] = 0;
   }
   if (!(rp->comps & LPG_COMP_TX)) return;
-  const double* nrow = rp->net_t + (int64_t)i * n; /* nrow[ii] = network[ii][i] */
-  double part[LPG_MAX_STRAINS] = {0.0, 0.0, 0.0, 0.0};
+  const uint64_t* qrow = rp->netq_t + (int64_t)i * n; /* qrow[ii] = network[ii][i] in 2^-62 */
+  unsigned __int128 part[LPG_MAX_STRAINS] = {0, 0, 0, 0};
   for (int ii0 = lane; ii0 < n; ii0 += 128) {
-    double wv[4];
-    double bv[4][LPG_MAX_STRAINS];
+    uint64_t wv[4];
+    uint64_t bv[4][LPG_MAX_STRAINS];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int ii = ii0 + 32 * u;
-      wv[u] = ii < n ? nrow[ii] : 0.0;
+      wv[u] = ii < n ? qrow[ii] : 0;
 #pragma unroll
-      for (int k = 0; k < LPG_MAX_STRAINS; ++k) bv[u][k] = (ii < n && k < ns) ? W.beta[(int64_t)k * G + nb + ii] : 0.0;
+      for (int k = 0; k < LPG_MAX_STRAINS; ++k) bv[u][k] = (ii < n && k < ns) ? W.bb[(int64_t)k * G + nb + ii] : 0;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      if (ii0 + 32 * u >= n) break;
+    for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int k = 0; k < LPG_MAX_STRAINS; ++k)
-        if (k < ns) part[k] = part[k] + bv[u][k] * wv[u];
-    }
+      for (int k = 0; k < LPG_MAX_STRAINS; ++k) part[k] += (unsigned __int128)bv[u][k] * wv[u];
   }
   double inc[LPG_MAX_STRAINS];
-  for (int k = 0; k < ns; ++k) {
-    double acc = 0.0;
-    for (int l = 0; l < 32; ++l) acc = acc + __shfl_sync(FULLMASK, part[k], l);
-    inc[k] = acc;
+#pragma unroll
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+    uint64_t lo = (uint64_t)part[k], hi = (uint64_t)(part[k] >> 64);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const uint64_t olo = __shfl_down_sync(FULLMASK, lo, off);
+      const uint64_t ohi = __shfl_down_sync(FULLMASK, hi, off);
+      const uint64_t nlo = lo + olo;
+      hi = hi + ohi + (nlo < lo ? 1 : 0);
+      lo = nlo;
+    }
+    inc[k] = ((double)hi * 0x1.0p64 + (double)lo) * 0x1.0p-94;
   }
   if (lane != 0) return;
   double p[LPG_MAX_STRAINS];
@@ -1139,8 +1171,9 @@ __global__ void k_node_tx(DevWorld W) {
   int local_zero = 1;
   const double rowsum = rp->rowsum[i];
   for (int k = 0; k < ns; ++k) {
-    if (W.bb[(int64_t)k * G + g] != 0) local_zero = 0;
-    double bpre = W.beta[(int64_t)k * G + g];
+    const uint64_t bk = W.bb[(int64_t)k * G + g];
+    if (bk != 0) local_zero = 0;
+    const double bpre = (double)bk * 0x1.0p-32;
     double beta = bpre + (inc[k] - bpre * rowsum);
     beta = (beta * rp->seas[t]) * rp->r0s[i];
     double denom = (double)(pop_t > 1 ? pop_t : 1);

@@ -592,6 +592,13 @@ static void lpo_sia(lpo_sim* s, int32_t t) {
 }
 
 /* ---------------------------------------------------------------------- */
+/* Network weight in units of 2^-62 (saturating at 4). */
+static inline uint64_t lpo_netq(double w) {
+  if (!(w > 0.0)) return 0;
+  if (w >= 4.0) return 0xFFFFFFFFFFFFFFFFULL;
+  return (uint64_t)nearbyint(w * 0x1.0p62);
+}
+
 /* Node-level force of infection and exposure counts
  * (model.py:1327-1407), restated in the order the engine evaluates it. */
 void lpo_node_tx(int n, int ns, const uint64_t* B, const uint64_t* SW, const int32_t* Scount, const double* net,
@@ -603,14 +610,12 @@ void lpo_node_tx(int n, int ns, const uint64_t* B, const uint64_t* SW, const int
     int local_zero = 1;
     for (int k = 0; k < ns; ++k) {
       if (B[(size_t)nd * ns + k] != 0) local_zero = 0;
-      /* incoming infectivity sum_i beta_i N[i][nd], associated as 32
-       * interleaved partial sums (i = l, l+32, ...) added in lane order */
-      double inc = 0.0;
-      for (int l = 0; l < 32; ++l) {
-        double part = 0.0;
-        for (int i = l; i < n; i += 32) part = part + ((double)B[(size_t)i * ns + k] * 0x1.0p-32) * net[(size_t)i * n + nd];
-        inc = inc + part;
-      }
+      /* incoming infectivity sum_i beta_i N[i][nd], exact: B (units 2^-32)
+       * times the network weight quantised to units of 2^-62, summed in 128
+       * bits, converted once */
+      unsigned __int128 acc = 0;
+      for (int i = 0; i < n; ++i) acc += (unsigned __int128)B[(size_t)i * ns + k] * (unsigned __int128)lpo_netq(net[(size_t)i * n + nd]);
+      double inc = ((double)(uint64_t)(acc >> 64) * 0x1.0p64 + (double)(uint64_t)acc) * 0x1.0p-94;
       double rowsum = 0.0;
       for (int j = 0; j < n; ++j) rowsum = rowsum + net[(size_t)nd * n + j];
       double bpre = (double)B[(size_t)nd * ns + k] * 0x1.0p-32;
