@@ -469,12 +469,12 @@ __device__ __forceinline__ uint32_t slab_reserve(uint32_t* s_cnt, uint32_t n) {
 /* PHASE 0, one thread's 8 slots: deaths are written here (state -1) and
  * queued with their old state for the bookkeeping; agents in E or I that
  * survive are queued for progression. */
-__device__ __forceinline__ void sweep_a8(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, bool on, bool vd, int t,
-                                         int64_t pos0, int nbo, int o, uint64_t st8, const int32_t* sdod,
+__device__ __forceinline__ void sweep_a8(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, bool on, bool vd, bool ds,
+                                         int t, int64_t pos0, int nbo, int o, uint64_t st8, const int32_t* sdod,
                                          uint32_t valid) {
   uint32_t ei = 0, dead = 0;
   if (on) {
-    ei = ei_bits(st8) & valid;
+    ei = ds ? (ei_bits(st8) & valid) : 0u;
     if (vd) {
       const uint32_t alive = alive_bits(st8) & valid;
       const int4* d4 = reinterpret_cast<const int4*>(sdod + o);
@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
         if (PHASE == 0) {
           if (fl & SF_DS || fl & SF_VD) {
             const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
-            sweep_a8(W, slab, &s_qcnt, on, (fl & SF_VD) != 0, t, pos0, nbo, o, st8,
+            sweep_a8(W, slab, &s_qcnt, on, (fl & SF_VD) != 0, (fl & SF_DS) != 0, t, pos0, nbo, o, st8,
                      reinterpret_cast<const int32_t*>(cols + L.dod + kk * 4 * LPG_CHUNK), valid);
           }
         } else {
