@@ -809,7 +809,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
     case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
     case 6: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
-    case 7: k_node_tx<<<(G * 32 + 63) / 64, 64, 0, st>>>(W); break;
+    case 7: k_node_tx<<<G, 256, 0, st>>>(W); break;
     case 8: {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(h->select_blocks);

@@ -466,95 +466,158 @@ __device__ __forceinline__ uint32_t slab_reserve(uint32_t* s_cnt, uint32_t n) {
   return base + x - n;
 }
 
-/* PHASE 0, one thread's 8 slots: deaths are written here (state -1) and
- * queued with their old state for the bookkeeping; agents in E or I that
- * survive are queued for progression. */
-__device__ __forceinline__ void sweep_a8(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, bool on, bool vd, bool ds,
-                                         int t, int64_t pos0, int nbo, int o, uint64_t st8, const int32_t* sdod,
-                                         uint32_t valid) {
+/* PHASE 0, one thread's 16 slots (pos0 .. pos0+15; sv the state bytes,
+ * sdod the dates of death in shared memory or null): deaths are written
+ * here (state -1) and queued with their old state for the bookkeeping;
+ * agents in E or I that survive are queued for progression. */
+__device__ __forceinline__ void sweep_a16(uint64_t* slab, uint32_t* s_cnt, DevWorld& W, bool on, bool ds, int t,
+                                          int64_t pos0, int off, int nbo, uint4 sv, const int32_t* sdod) {
   uint32_t ei = 0, dead = 0;
   if (on) {
-    ei = ds ? (ei_bits(st8) & valid) : 0u;
-    if (vd) {
-      const uint32_t alive = alive_bits(st8) & valid;
-      const int4* d4 = reinterpret_cast<const int4*>(sdod + o);
-      const int4 a = d4[0], b = d4[1];
-      const int32_t dd[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    const uint32_t wv[4] = {sv.x, sv.y, sv.z, sv.w};
+    uint32_t eiw[4];
+    uint32_t any_ei = 0;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) dead |= (uint32_t)(dd[j] <= t && (o + j) < nbo) << j;
-      dead &= alive;
-      if (dead) {
-        uint64_t out8 = st8;
+    for (int q = 0; q < 4; ++q) {
+      eiw[q] = __vcmpltu4(__vsub4(wv[q], 0x01010101u), 0x02020202u);
+      any_ei |= eiw[q];
+    }
+    if (ds && any_ei) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-          if ((dead >> j) & 1u) out8 |= 0xffULL << (8 * j);
-        *reinterpret_cast<uint64_t*>(W.ds + pos0) = out8;
-        ei &= ~dead;
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ei |= ((eiw[q] >> (8 * j + 7)) & 1u) << (4 * q + j);
+    }
+    if (sdod) {
+      const int4* d4 = reinterpret_cast<const int4*>(sdod + off);
+      int32_t mn = 0x7fffffff;
+      int4 dq[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        dq[q] = d4[q];
+        mn = min(mn, min(min(dq[q].x, dq[q].y), min(dq[q].z, dq[q].w)));
+      }
+      if (mn <= t) { /* rare: somebody's date of death has come */
+        uint32_t alive = 0, due = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int32_t dd[4] = {dq[q].x, dq[q].y, dq[q].z, dq[q].w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int k = 4 * q + j;
+            alive |= (((wv[q] >> (8 * j + 7)) & 1u) ^ 1u) << k;
+            due |= (uint32_t)(dd[j] <= t && (off + k) < nbo) << k;
+          }
+        }
+        dead = alive & due;
+        if (dead) {
+          uint4 out = sv;
+          uint32_t* ow = reinterpret_cast<uint32_t*>(&out);
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            if ((dead >> k) & 1u) ow[k >> 2] |= 0xffu << (8 * (k & 3));
+          *reinterpret_cast<uint4*>(W.ds + pos0) = out;
+          ei &= ~dead;
+        }
       }
     }
   }
   if (__ballot_sync(FULLMASK, (ei | dead) != 0) == 0) return;
   uint32_t at = slab_reserve(s_cnt, __popc(ei) + __popc(dead));
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    if ((ei >> j) & 1u) slab[at++] = q_entry(pos0 + j, QA_DS, 0);
-    if ((dead >> j) & 1u) slab[at++] = q_entry(pos0 + j, QA_DEATH, (uint32_t)(st8 >> (8 * j)));
+  const uint32_t wv2[4] = {sv.x, sv.y, sv.z, sv.w};
+  uint32_t m = ei | dead;
+  while (m) {
+    const int k = __ffs(m) - 1;
+    m &= m - 1;
+    const bool is_dead = (dead >> k) & 1u;
+    slab[at++] = q_entry(pos0 + k, is_dead ? QA_DEATH : QA_DS, is_dead ? (wv2[k >> 2] >> (8 * (k & 3))) : 0u);
   }
 }
 
-/* PHASE 1, one thread's 8 slots: the RI timer countdown (dense) and the
- * masks of the agents that RI or today's SIA campaigns reach; those are
- * queued with their event flags. */
-__device__ __forceinline__ void sweep_b8(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, bool on, const DevRep* rp,
-                                         uint8_t fl, int t, int ni, int64_t pos0, int o, uint64_t st8,
-                                         const uint8_t* scm, const int16_t* sri, const int32_t* sdob,
-                                         uint32_t valid) {
-  uint32_t f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  uint32_t any = 0;
+/* PHASE 1, one thread's 16 slots: the RI countdown and the masks of agents
+ * that RI or today's SIA campaigns reach (queued with their event flags).
+ * The countdown is packed 16-bit arithmetic: the stored value wraps like
+ * the reference's int16 store, and eligibility  -step <(=) old - step <= 0
+ * is a range test on the old value. */
+__device__ __forceinline__ void sweep_b16(uint64_t* slab, uint32_t* s_cnt, DevWorld& W, bool on, const DevRep* rp,
+                                          uint8_t fl, int t, int ni, int64_t pos0, int off, uint4 sv,
+                                          const uint8_t* scm, const int16_t* sri, const int32_t* sdob) {
+  uint32_t fri = 0;
+  uint32_t fsia[LPG_MAX_SIA_PER_DAY] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int nsia_used = 0;
   if (on) {
-    uint32_t reach = alive_bits(st8) & valid;
-    const uint64_t c8 = *reinterpret_cast<const uint64_t*>(scm + o);
+    const uint32_t wv[4] = {sv.x, sv.y, sv.z, sv.w};
+    const uint4 cv = *reinterpret_cast<const uint4*>(scm + off);
+    const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+    /* per-byte 0xff where the agent is alive (state >= 0) and not chronically missed */
+    uint32_t reachw[4];
+    uint32_t any_reach = 0;
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
-      if (((c8 >> (8 * j)) & 0xffu) == 1u) reach &= ~(1u << j);
-    if (reach && (fl & SF_RI)) {
-      int4 rv = *reinterpret_cast<const int4*>(sri + o);
-      int16_t* r16 = reinterpret_cast<int16_t*>(&rv);
-      const int step = rp->ri_step;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        if (!((reach >> j) & 1u)) continue;
-        const int32_t timer = (int32_t)r16[j] - step;
-        r16[j] = (int16_t)(uint16_t)(uint32_t)timer;
-        bool e = false;
-        if (t == step) e = timer <= 0 && timer >= -step;
-        else if (t > step) e = timer <= 0 && timer > -step;
-        f[j] |= e ? QB_RI : 0u;
-      }
-      *reinterpret_cast<int4*>(W.ri + pos0) = rv;
+    for (int q = 0; q < 4; ++q) {
+      /* alive: sign bit clear, i.e. (byte ^ 0x80) >= 0x80 unsigned */
+      const uint32_t missed = __vcmpeq4(cw[q], 0x01010101u);
+      reachw[q] = __vcmpgeu4(wv[q] ^ 0x80808080u, 0x80808080u) & ~missed;
+      any_reach |= reachw[q];
     }
-    if (reach && (fl & SF_SIA)) {
-      const int4* d4 = reinterpret_cast<const int4*>(sdob + o);
-      const int4 a = d4[0], b = d4[1];
-      const int32_t db[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-      for (int k = 0; k < rp->sia_n; ++k) {
+    if (any_reach && (fl & SF_RI)) {
+      const int step = rp->ri_step;
+      const uint32_t step2 = ((uint32_t)step & 0xffffu) * 0x00010001u;
+      uint4 r4[2];
+      r4[0] = *reinterpret_cast<const uint4*>(sri + off);
+      r4[1] = *reinterpret_cast<const uint4*>(sri + off + 8);
+      uint32_t* rw = reinterpret_cast<uint32_t*>(r4);
+      const uint32_t lo2 = t == step ? 0x00000000u : 0x00010001u; /* eligible: lo <= old <= step */
+      const uint32_t hi2 = step2;
+#pragma unroll
+      for (int h = 0; h < 8; ++h) {
+        /* 16-bit lanes of slots 2h, 2h+1: byte masks of the reach word */
+        const uint32_t rb = reachw[h >> 1] >> (16 * (h & 1));
+        const uint32_t m2 = ((rb & 0xffu) ? 0x0000ffffu : 0u) | ((rb & 0xff00u) ? 0xffff0000u : 0u);
+        const uint32_t old = rw[h];
+        const uint32_t nw = __vsub2(old, step2);
+        const uint32_t el = __vcmpges2(old, lo2) & __vcmples2(old, hi2) & m2;
+        rw[h] = (nw & m2) | (old & ~m2);
+        fri |= ((el & 1u) << (2 * h)) | (((el >> 16) & 1u) << (2 * h + 1));
+      }
+      *reinterpret_cast<uint4*>(W.ri + pos0) = r4[0];
+      *reinterpret_cast<uint4*>(W.ri + pos0 + 8) = r4[1];
+    }
+    if (any_reach && (fl & SF_SIA)) {
+      const int4* d4 = reinterpret_cast<const int4*>(sdob + off);
+      int4 dq[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dq[q] = d4[q];
+      nsia_used = rp->sia_n;
+      for (int k = 0; k < nsia_used && k < LPG_MAX_SIA_PER_DAY; ++k) {
         const DevSia& ev = rp->sia[rp->sia_i0 + k];
         if (ev.mask[ni] == 0) continue;
+        /* age window  min <= t - dob <= max  <=>  t - max <= dob <= t - min */
+        const int64_t lo64 = (int64_t)t - ev.max_age, hi64 = (int64_t)t - ev.min_age;
+        uint32_t mk = 0;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int64_t age = (int64_t)t - (int64_t)db[j];
-          if (((reach >> j) & 1u) && ev.min_age <= age && age <= ev.max_age) f[j] |= 2u << k;
+        for (int q = 0; q < 4; ++q) {
+          const int32_t dd[4] = {dq[q].x, dq[q].y, dq[q].z, dq[q].w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            mk |= (uint32_t)(((reachw[q] >> (8 * j)) & 1u) && (int64_t)dd[j] >= lo64 && (int64_t)dd[j] <= hi64) << (4 * q + j);
         }
+        fsia[k] = mk;
       }
     }
-#pragma unroll
-    for (int j = 0; j < 8; ++j) any += f[j] != 0;
   }
-  if (__ballot_sync(FULLMASK, any != 0) == 0) return;
-  uint32_t at = slab_reserve(s_cnt, any);
+  uint32_t any = fri;
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
-    if (f[j]) slab[at++] = q_entry(pos0 + j, f[j], 0);
+  for (int k = 0; k < LPG_MAX_SIA_PER_DAY; ++k) any |= fsia[k];
+  if (__ballot_sync(FULLMASK, any != 0) == 0) return;
+  uint32_t at = slab_reserve(s_cnt, __popc(any));
+  while (any) {
+    const int j = __ffs(any) - 1;
+    any &= any - 1;
+    uint32_t f = (fri >> j) & 1u;
+#pragma unroll
+    for (int k = 0; k < LPG_MAX_SIA_PER_DAY; ++k) f |= ((fsia[k] >> j) & 1u) << (1 + k);
+    slab[at++] = q_entry(pos0 + j, f, 0);
+  }
 }
 
 template <int PHASE>
@@ -643,8 +706,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       s_issued = i;
     }
   } else if (w0 < w1) {
-    /* ---- consumer warps ---- */
-    const int o = threadIdx.x * LPG_SPT;
+    /* ---- consumer warps: 16-slot groups of the stage, 256 groups per pass ---- */
     int32_t wc = w0;
     for (int32_t i = 0; wc < w1; ++i) {
       const int b = i % LPG_NST;
@@ -663,26 +725,32 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       const uint8_t* stg = sm_stage + (size_t)b * LPG_STAGE_BYTES;
       const int4* meta = reinterpret_cast<const int4*>(stg);
       const uint8_t* cols = stg + LPG_META_BYTES;
-      const StageLayout L = stage_layout(fl, we - wc);
-      for (int32_t w = wc; w < we; ++w) {
-        const int kk = w - wc;
-        const int4 m = meta[kk];
-        const int fill = m.y;
-        const int64_t cid = P.cbase[r] + (w - P.off[r]);
-        const int64_t pos0 = cid * LPG_CHUNK + o;
-        const bool on = o < fill;
-        const uint32_t valid = !on ? 0u : (fill - o >= 8 ? 0xffu : ((1u << (fill - o)) - 1u));
-        const uint64_t st8 = on ? *reinterpret_cast<const uint64_t*>(cols + L.ds + kk * LPG_CHUNK + o) : ~0ULL;
+      const int nc = we - wc;
+      const StageLayout L = stage_layout(fl, nc);
+      const int ngroups = nc * (LPG_CHUNK / 16);
+      for (int gb = 0; gb < ngroups; gb += LPG_SWEEP_CONSUMERS) {
+        const int gi = gb + threadIdx.x;
+        const bool on = gi < ngroups;
+        const int kk = on ? gi / (LPG_CHUNK / 16) : 0;
+        const int off = on ? (gi % (LPG_CHUNK / 16)) * 16 : 0;
+        const int64_t cid = P.cbase[r] + (wc + kk - P.off[r]);
+        const int64_t pos0 = cid * LPG_CHUNK + off;
+        /* slots past a chunk's fill hold state -1 (never alive), so they drop
+         * out of every test below without a fill check */
+        const uint4 sv = on ? *reinterpret_cast<const uint4*>(cols + L.ds + kk * LPG_CHUNK + off)
+                            : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
         if (PHASE == 0) {
-          if (fl & SF_DS || fl & SF_VD) {
+          if (fl & (SF_DS | SF_VD)) {
+            const int4 m = meta[kk];
             const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
-            sweep_a8(W, slab, &s_qcnt, on, (fl & SF_VD) != 0, (fl & SF_DS) != 0, t, pos0, nbo, o, st8,
-                     reinterpret_cast<const int32_t*>(cols + L.dod + kk * 4 * LPG_CHUNK), valid);
+            sweep_a16(slab, &s_qcnt, W, on, (fl & SF_DS) != 0, t, pos0, off, nbo, sv,
+                      (fl & SF_VD) ? reinterpret_cast<const int32_t*>(cols + L.dod + kk * 4 * LPG_CHUNK) : nullptr);
           }
         } else {
-          sweep_b8(W, slab, &s_qcnt, on, rp, fl, t, m.x - rp->node_base, pos0, o, st8, cols + L.cm + kk * LPG_CHUNK,
-                   reinterpret_cast<const int16_t*>(cols + L.ri + kk * 2 * LPG_CHUNK),
-                   reinterpret_cast<const int32_t*>(cols + L.dob + kk * 4 * LPG_CHUNK), valid);
+          const int ni = meta[kk].x - rp->node_base;
+          sweep_b16(slab, &s_qcnt, W, on, rp, fl, t, ni, pos0, off, sv, cols + L.cm + kk * LPG_CHUNK,
+                    reinterpret_cast<const int16_t*>(cols + L.ri + kk * 2 * LPG_CHUNK),
+                    reinterpret_cast<const int32_t*>(cols + L.dob + kk * 4 * LPG_CHUNK));
         }
       }
       mbar_arrive(&empty[b]);
@@ -1109,12 +1177,14 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
  * in lane order. */
 /* Node-level force of infection and exposure counts (model.py:1327-1407);
  * the same arithmetic, in the same order, as the oracle's lpo_node_tx.
- * One warp per node.  Incoming infectivity sum_i B_i N[i][n] is exact
+ * One CTA per node.  Incoming infectivity sum_i B_i N[i][n] is exact
  * integer arithmetic: B in units of 2^-32 times the network weight in units
- * of 2^-62 (transposed row, contiguous), 128-bit sums, one conversion. */
-__global__ void k_node_tx(DevWorld W) {
-  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+ * of 2^-62 (transposed row, contiguous), 128-bit sums, one conversion; an
+ * exact sum does not depend on how the threads split it. */
+__global__ void __launch_bounds__(256) k_node_tx(DevWorld W) {
+  const int g = blockIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ uint64_t s_lo[8][LPG_MAX_STRAINS], s_hi[8][LPG_MAX_STRAINS];
   if (g >= W.G) return;
   DevRep* rp = &W.reps[W.node_rep[g]];
   if (!rp->active) return;
@@ -1125,33 +1195,24 @@ __global__ void k_node_tx(DevWorld W) {
     const int32_t* pop1 = RES(rp, RS_POP, t - 1);
     pop_t = pop1[i];
     if (rp->vd_tick) pop_t = pop_t + W.ev[(int64_t)EV_BIRTHS * G + g] - W.ev[(int64_t)EV_DEATHS * G + g];
-    if (lane == 0) RES(rp, RS_POP, t)[i] = pop_t;
+    if (threadIdx.x == 0) RES(rp, RS_POP, t)[i] = pop_t;
   } else {
     pop_t = RES(rp, RS_POP, t)[i];
   }
-  if (lane == 0) {
+  if (threadIdx.x == 0) {
     W.size[g] = 0;
     W.uniq[g] = 0;
   }
   if (!(rp->comps & LPG_COMP_TX)) return;
   const uint64_t* qrow = rp->netq_t + (int64_t)i * n; /* qrow[ii] = network[ii][i] in 2^-62 */
   unsigned __int128 part[LPG_MAX_STRAINS] = {0, 0, 0, 0};
-  for (int ii0 = lane; ii0 < n; ii0 += 128) {
-    uint64_t wv[4];
-    uint64_t bv[4][LPG_MAX_STRAINS];
+  for (int ii = threadIdx.x; ii < n; ii += blockDim.x) {
+    const uint64_t w = qrow[ii];
+    if (!w) continue;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int ii = ii0 + 32 * u;
-      wv[u] = ii < n ? qrow[ii] : 0;
-#pragma unroll
-      for (int k = 0; k < LPG_MAX_STRAINS; ++k) bv[u][k] = (ii < n && k < ns) ? W.bb[(int64_t)k * G + nb + ii] : 0;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int k = 0; k < LPG_MAX_STRAINS; ++k) part[k] += (unsigned __int128)bv[u][k] * wv[u];
+    for (int k = 0; k < LPG_MAX_STRAINS; ++k)
+      if (k < ns) part[k] += (unsigned __int128)W.bb[(int64_t)k * G + nb + ii] * w;
   }
-  double inc[LPG_MAX_STRAINS];
 #pragma unroll
   for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
     uint64_t lo = (uint64_t)part[k], hi = (uint64_t)(part[k] >> 64);
@@ -1163,9 +1224,23 @@ __global__ void k_node_tx(DevWorld W) {
       hi = hi + ohi + (nlo < lo ? 1 : 0);
       lo = nlo;
     }
+    if (lane == 0) {
+      s_lo[wid][k] = lo;
+      s_hi[wid][k] = hi;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double inc[LPG_MAX_STRAINS];
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+    uint64_t lo = 0, hi = 0;
+    for (int w8 = 0; w8 < (int)(blockDim.x >> 5); ++w8) {
+      const uint64_t nlo = lo + s_lo[w8][k];
+      hi = hi + s_hi[w8][k] + (nlo < lo ? 1 : 0);
+      lo = nlo;
+    }
     inc[k] = ((double)hi * 0x1.0p64 + (double)lo) * 0x1.0p-94;
   }
-  if (lane != 0) return;
   double p[LPG_MAX_STRAINS];
   double total_p = 0.0;
   int local_zero = 1;
@@ -1250,6 +1325,103 @@ __device__ __forceinline__ int pick_strain(const double* p, int ns, double total
   return 0;
 }
 
+/* Locate target v (< the node's remaining susceptible weight) in node g's
+ * frozen CDF: chunk by binary search of the chunk prefix cp, sub-block by
+ * its 16 totals, slot by the 128 state bytes and risks.  LPG_NONE if the
+ * weights are inconsistent (an internal error). */
+__device__ __forceinline__ uint32_t locate(const DevWorld& W, const int32_t* ls, const uint64_t* cp, int32_t a,
+                                           int32_t b, uint64_t v) {
+  int32_t lo = a, hi = b - 1;
+  while (lo < hi) {
+    int32_t mid = (lo + hi) >> 1;
+    if (cp[mid] > v) hi = mid; else lo = mid + 1;
+  }
+  if (lo > a) v -= cp[lo - 1];
+  const int64_t cid = ls[lo];
+  uint64_t swv[LPG_NSUB];
+#pragma unroll
+  for (int k = 0; k < LPG_NSUB; ++k) swv[k] = __ldcg(&W.sub_w[cid * LPG_NSUB + k]);
+  int sb = LPG_NSUB;
+#pragma unroll
+  for (int k = 0; k < LPG_NSUB; ++k) {
+    if (sb == LPG_NSUB) {
+      if (swv[k] > v) sb = k;
+      else v -= swv[k];
+    }
+  }
+  uint32_t hit = LPG_NONE;
+  if (sb < LPG_NSUB) {
+    const int64_t p0 = cid * LPG_CHUNK + (int64_t)sb * LPG_SUB;
+    uint4 sv[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sv[k] = __ldcg(reinterpret_cast<const uint4*>(W.ds + p0) + k);
+    for (int grp = 0; grp < 4 && hit == LPG_NONE; ++grp) {
+      float4 rv[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) rv[k] = reinterpret_cast<const float4*>(W.risk + p0 + grp * 32)[k];
+      const uint32_t* sw32 = reinterpret_cast<const uint32_t*>(&sv[grp * 2]);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        if (hit != LPG_NONE) break;
+        const uint32_t sbyte = (sw32[k >> 2] >> (8 * (k & 3))) & 0xffu;
+        if (sbyte != 0) continue;
+        const uint64_t w = fix_risk(reinterpret_cast<const float*>(rv)[k]);
+        if (w > v) hit = (uint32_t)(p0 + grp * 32 + k);
+        else v -= w;
+      }
+    }
+  }
+  return hit;
+}
+
+/* The first agent of a target to claim it (state 0 -> 1) exposes it: strain
+ * by relative FOI (model.py:1127-1145) and every susceptible total. */
+__device__ __forceinline__ void claim(DevWorld& W, uint32_t hit) {
+  const int64_t pos = hit;
+  uint32_t* wp = reinterpret_cast<uint32_t*>(W.ds + (pos & ~3LL));
+  const int sh = (int)(pos & 3) * 8;
+  uint32_t old = *(volatile uint32_t*)wp;
+  bool won = false;
+  while (((old >> sh) & 0xffu) == 0) {
+    const uint32_t nw = (old & ~(0xffu << sh)) | (1u << sh);
+    const uint32_t prev = atomicCAS(wp, old, nw);
+    if (prev == old) {
+      won = true;
+      break;
+    }
+    old = prev;
+  }
+  if (!won) return;
+  const int G = W.G;
+  const int64_t cid = pos / LPG_CHUNK;
+  const int g = W.cmeta[cid].x;
+  const DevRep* rp = &W.reps[W.node_rep[g]];
+  double p[LPG_MAX_STRAINS];
+  double totalp = 0.0;
+  for (int k = 0; k < rp->ns; ++k) {
+    p[k] = W.prob[(int64_t)k * G + g];
+    totalp = totalp + p[k];
+  }
+  const double r = lpg_u01(rp->seed, LPG_P_STRAIN, rp->cur_t, W.ref[pos], 0, 0);
+  const int s = pick_strain(p, rp->ns, totalp, r);
+  W.strain[pos] = (int8_t)s;
+  const uint64_t w = fix_risk(W.risk[pos]);
+  atomicAdd(&W.tot[(int64_t)TT_S * G + g], -1);
+  atomicAdd(&W.tot[(int64_t)(TT_E0 + s) * G + g], 1);
+  atomicAdd(&W.ev[(int64_t)(EV_TXNEW0 + s) * G + g], 1);
+  atomicAdd((unsigned long long*)&W.uniq[g], 1ULL);
+  if (w) {
+    atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
+    atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
+    atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
+  }
+}
+
+/* Weighted selection without replacement (tx_infect_nb, model.py:1066-1147).
+ * Round 0 runs over all nodes at once (three grid barriers); the few
+ * collisions left after it are redrawn per node by one CTA in later rounds,
+ * with CTA barriers only.  Round r of node n draws the (n, r, j) uniforms
+ * of the oracle, so the CDF targets are the same whatever runs them. */
 __global__ void __launch_bounds__(256) k_select(DevWorld W) {
   const int R = W.n_reps, G = W.G;
   int any = 0;
@@ -1260,166 +1432,130 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
   const int64_t gwarp = gtid >> 5, nwarps = gsz >> 5;
   __shared__ int64_t s_K;
-  for (int round = 0; round < LPG_MAX_ROUNDS; ++round) {
-    /* A1: remaining demand and chunk prefix of every node that still needs draws */
-    for (int64_t g = gwarp; g < G; g += nwarps) {
-      const DevRep* rp = &W.reps[W.node_rep[g]];
-      int64_t k = 0;
-      if (rp->active && (rp->comps & LPG_COMP_TX)) {
-        k = W.size[g] - W.uniq[g];
-        if (k < 0) k = 0;
-        if (W.sw[g] == 0) k = 0;
-      }
-      if (lane == 0) W.ksel[g] = k;
-      if (k > 0) {
-        const int i = (int)(g - rp->node_base);
-        const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
-        const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
-        uint64_t* cp = W.cpref + rp->chunk_base;
-        uint64_t carry = 0;
-        for (int32_t a = st[i]; a < st[i + 1]; a += 32) {
-          int32_t idx = a + lane;
-          uint64_t v = idx < st[i + 1] ? W.chunk_w[ls[idx]] : 0;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            uint64_t y = __shfl_up_sync(FULLMASK, v, o);
-            if (lane >= o) v += y;
-          }
-          if (idx < st[i + 1]) cp[idx] = carry + v;
-          carry += __shfl_sync(FULLMASK, v, 31);
-        }
-      }
+
+  /* ---- round 0, all nodes ---- */
+  for (int64_t g = gwarp; g < G; g += nwarps) {
+    const DevRep* rp = &W.reps[W.node_rep[g]];
+    int64_t k = 0;
+    if (rp->active && (rp->comps & LPG_COMP_TX)) {
+      k = W.size[g] - W.uniq[g];
+      if (k < 0) k = 0;
+      if (W.sw[g] == 0) k = 0;
     }
-    if (!grid_sync(W)) return;
-    /* A2: target offsets of all nodes; every CTA computes (and writes) the
-     * same values, so no further grid barrier is needed */
-    {
-      int64_t carry = 0;
-      for (int base = 0; base < G; base += blockDim.x) {
-        int g = base + threadIdx.x;
-        int64_t k = g < G ? W.ksel[g] : 0;
-        int64_t tot;
-        int64_t ex = block_excl_scan(k, &tot);
-        if (g < G) W.tgt_off[g] = carry + ex;
-        carry += tot;
-      }
-      if (threadIdx.x == 0) {
-        W.tgt_off[G] = carry;
-        s_K = carry;
-      }
-      __syncthreads();
-    }
-    const int64_t K = s_K;
-    if (K == 0) break;
-    if (K > W.hits_cap) {
-      if (gtid == 0) W.reps[0].error = LPG_ERR_INTERNAL;
-      return;
-    }
-    /* B: locate every target in its node's frozen susceptible CDF */
-    for (int64_t q = gtid; q < K; q += gsz) {
-      int lo = 0, hi = G;
-      while (lo < hi) { /* first g with tgt_off[g] > q */
-        int mid = (lo + hi) >> 1;
-        if (W.tgt_off[mid] > q) hi = mid; else lo = mid + 1;
-      }
-      const int g = lo - 1;
-      const DevRep* rp = &W.reps[W.node_rep[g]];
-      const int i = g - rp->node_base;
-      const int64_t j = q - W.tgt_off[g];
-      uint64_t v = lpg_scale_target(lpg_u53(rp->seed, LPG_P_SELECT, rp->cur_t, (uint64_t)i, (uint64_t)round, (uint64_t)j), W.sw[g]);
+    if (lane == 0) W.ksel[g] = k;
+    if (k > 0) {
+      const int i = (int)(g - rp->node_base);
       const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
       const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
-      const uint64_t* cp = W.cpref + rp->chunk_base;
-      int32_t a = st[i], b = st[i + 1] - 1;
-      while (a < b) {
-        int32_t mid = (a + b) >> 1;
-        if (cp[mid] > v) b = mid; else a = mid + 1;
-      }
-      if (a > st[i]) v -= cp[a - 1];
-      const int64_t cid = ls[a];
-      /* sub-block: the 16 totals in one round trip */
-      uint64_t swv[LPG_NSUB];
+      uint64_t* cp = W.cpref + rp->chunk_base;
+      uint64_t carry = 0;
+      for (int32_t a = st[i]; a < st[i + 1]; a += 32) {
+        int32_t idx = a + lane;
+        uint64_t v = idx < st[i + 1] ? __ldcg(&W.chunk_w[ls[idx]]) : 0;
 #pragma unroll
-      for (int k = 0; k < LPG_NSUB; ++k) swv[k] = W.sub_w[cid * LPG_NSUB + k];
-      int sb = LPG_NSUB;
-#pragma unroll
-      for (int k = 0; k < LPG_NSUB; ++k) {
-        if (sb == LPG_NSUB) {
-          if (swv[k] > v) sb = k;
-          else v -= swv[k];
+        for (int o = 1; o < 32; o <<= 1) {
+          uint64_t y = __shfl_up_sync(FULLMASK, v, o);
+          if (lane >= o) v += y;
         }
-      }
-      uint32_t hit = LPG_NONE;
-      if (sb < LPG_NSUB) {
-        /* slots: 128 state bytes as 8 x 16 B, then risks 32 at a time */
-        const int64_t p0 = cid * LPG_CHUNK + (int64_t)sb * LPG_SUB;
-        uint4 sv[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) sv[k] = reinterpret_cast<const uint4*>(W.ds + p0)[k];
-        for (int grp = 0; grp < 4 && hit == LPG_NONE; ++grp) {
-          float4 rv[8];
-#pragma unroll
-          for (int k = 0; k < 8; ++k) rv[k] = reinterpret_cast<const float4*>(W.risk + p0 + grp * 32)[k];
-          const uint32_t* sw32 = reinterpret_cast<const uint32_t*>(&sv[grp * 2]);
-#pragma unroll
-          for (int k = 0; k < 32; ++k) {
-            if (hit != LPG_NONE) break;
-            const uint32_t sbyte = (sw32[k >> 2] >> (8 * (k & 3))) & 0xffu;
-            if (sbyte != 0) continue;
-            const float rk = reinterpret_cast<const float*>(rv)[k];
-            const uint64_t w = fix_risk(rk);
-            if (w > v) hit = (uint32_t)(p0 + grp * 32 + k);
-            else v -= w;
-          }
-        }
-      }
-      if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
-      W.hits[q] = hit;
-    }
-    if (!grid_sync(W)) return;
-    /* C: first target to reach an agent exposes it; strain by relative FOI */
-    for (int64_t q = gtid; q < K; q += gsz) {
-      const uint32_t hit = W.hits[q];
-      if (hit == LPG_NONE) continue;
-      const int64_t pos = hit;
-      uint32_t* wp = reinterpret_cast<uint32_t*>(W.ds + (pos & ~3LL));
-      const int sh = (int)(pos & 3) * 8;
-      uint32_t old = *(volatile uint32_t*)wp;
-      bool won = false;
-      while (((old >> sh) & 0xffu) == 0) {
-        uint32_t nw = (old & ~(0xffu << sh)) | (1u << sh);
-        uint32_t prev = atomicCAS(wp, old, nw);
-        if (prev == old) {
-          won = true;
-          break;
-        }
-        old = prev;
-      }
-      if (!won) continue;
-      const int64_t cid = pos / LPG_CHUNK;
-      const int g = W.cmeta[cid].x;
-      const DevRep* rp = &W.reps[W.node_rep[g]];
-      double p[LPG_MAX_STRAINS];
-      double totalp = 0.0;
-      for (int k = 0; k < rp->ns; ++k) {
-        p[k] = W.prob[(int64_t)k * G + g];
-        totalp = totalp + p[k];
-      }
-      double r = lpg_u01(rp->seed, LPG_P_STRAIN, rp->cur_t, W.ref[pos], 0, 0);
-      int s = pick_strain(p, rp->ns, totalp, r);
-      W.strain[pos] = (int8_t)s;
-      uint64_t w = fix_risk(W.risk[pos]);
-      atomicAdd(&W.tot[(int64_t)TT_S * G + g], -1);
-      atomicAdd(&W.tot[(int64_t)(TT_E0 + s) * G + g], 1);
-      atomicAdd(&W.ev[(int64_t)(EV_TXNEW0 + s) * G + g], 1);
-      atomicAdd((unsigned long long*)&W.uniq[g], 1ULL);
-      if (w) {
-        atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
-        atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
-        atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
+        if (idx < st[i + 1]) cp[idx] = carry + v;
+        carry += __shfl_sync(FULLMASK, v, 31);
       }
     }
-    if (!grid_sync(W)) return;
+  }
+  if (!grid_sync(W)) return;
+  {
+    /* target offsets of all nodes; every CTA computes the same values */
+    int64_t carry = 0;
+    for (int base = 0; base < G; base += blockDim.x) {
+      int g = base + threadIdx.x;
+      int64_t k = g < G ? W.ksel[g] : 0;
+      int64_t tot;
+      int64_t ex = block_excl_scan(k, &tot);
+      if (g < G) W.tgt_off[g] = carry + ex;
+      carry += tot;
+    }
+    if (threadIdx.x == 0) {
+      W.tgt_off[G] = carry;
+      s_K = carry;
+    }
+    __syncthreads();
+  }
+  const int64_t K = s_K;
+  if (K > W.hits_cap) {
+    if (gtid == 0) W.reps[0].error = LPG_ERR_INTERNAL;
+    return;
+  }
+  for (int64_t q = gtid; q < K; q += gsz) {
+    int lo = 0, hi = G;
+    while (lo < hi) { /* first g with tgt_off[g] > q */
+      int mid = (lo + hi) >> 1;
+      if (W.tgt_off[mid] > q) hi = mid; else lo = mid + 1;
+    }
+    const int g = lo - 1;
+    const DevRep* rp = &W.reps[W.node_rep[g]];
+    const int i = g - rp->node_base;
+    const int64_t j = q - W.tgt_off[g];
+    const uint64_t v = lpg_scale_target(lpg_u53(rp->seed, LPG_P_SELECT, rp->cur_t, (uint64_t)i, 0, (uint64_t)j), W.sw[g]);
+    const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+    const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
+    const uint32_t hit = locate(W, ls, W.cpref + rp->chunk_base, st[i], st[i + 1], v);
+    if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
+    W.hits[q] = hit;
+  }
+  if (!grid_sync(W)) return;
+  for (int64_t q = gtid; q < K; q += gsz) {
+    const uint32_t hit = W.hits[q];
+    if (hit != LPG_NONE) claim(W, hit);
+  }
+  if (!grid_sync(W)) return;
+
+  /* ---- later rounds: one CTA per node that still needs agents ---- */
+  __shared__ int64_t s_k;
+  __shared__ uint64_t s_T;
+  for (int g = blockIdx.x; g < G; g += gridDim.x) {
+    const DevRep* rp = &W.reps[W.node_rep[g]];
+    if (!rp->active || !(rp->comps & LPG_COMP_TX)) continue;
+    const int i = g - rp->node_base;
+    const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+    const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
+    uint64_t* cp = W.cpref + rp->chunk_base;
+    /* this node's region of the target buffer: its own positions */
+    uint32_t* hits = W.hits + (int64_t)(rp->chunk_base + st[i]) * LPG_CHUNK;
+    for (int round = 1; round < LPG_MAX_ROUNDS; ++round) {
+      if (threadIdx.x == 0) {
+        const int64_t k = __ldcg(&W.size[g]) - (int64_t)__ldcg((const unsigned long long*)&W.uniq[g]);
+        s_T = __ldcg(&W.sw[g]);
+        s_k = (k > 0 && s_T > 0) ? k : 0;
+      }
+      __syncthreads();
+      const int64_t k = s_k;
+      const uint64_t T = s_T;
+      if (k == 0) break;
+      /* chunk prefix of the node (CTA scan) */
+      uint64_t carry = 0;
+      for (int32_t a = st[i]; a < st[i + 1]; a += blockDim.x) {
+        const int32_t idx = a + threadIdx.x;
+        const int64_t v = idx < st[i + 1] ? (int64_t)__ldcg(&W.chunk_w[ls[idx]]) : 0;
+        int64_t tot;
+        const int64_t ex = block_excl_scan(v, &tot);
+        if (idx < st[i + 1]) cp[idx] = carry + (uint64_t)ex + (uint64_t)v;
+        carry += (uint64_t)tot;
+      }
+      __syncthreads();
+      for (int64_t j = threadIdx.x; j < k; j += blockDim.x) {
+        const uint64_t v = lpg_scale_target(lpg_u53(rp->seed, LPG_P_SELECT, rp->cur_t, (uint64_t)i, (uint64_t)round, (uint64_t)j), T);
+        const uint32_t hit = locate(W, ls, cp, st[i], st[i + 1], v);
+        if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
+        hits[j] = hit;
+      }
+      __syncthreads();
+      for (int64_t j = threadIdx.x; j < k; j += blockDim.x) {
+        const uint32_t hit = hits[j];
+        if (hit != LPG_NONE) claim(W, hit);
+      }
+      __threadfence_block();
+      __syncthreads();
+    }
   }
 }
 
