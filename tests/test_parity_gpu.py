@@ -159,3 +159,31 @@ def test_capacity_error_is_raised():
         setattr(sim.people, name, np.ascontiguousarray(getattr(sim.people, name)[: sim.people.capacity]))
     with pytest.raises(ValueError):
         sim.run()
+
+
+def test_parity_heavy_collisions():
+    """Demand close to the susceptible count: many selection rounds per node."""
+    pars = PropertySet(
+        {
+            "seed": 77,
+            "start_date": lp.date("2019-01-01"),
+            "dur": 40,
+            "init_pop": np.array([3000, 1500, 800]),
+            "cbr": np.array([30, 30, 30]),
+            "init_immun": [0.0, 0.2, 0.0],
+            "init_prev": [30, 10, 5],
+            "r0": 200,
+            "risk_mult_var": 9.0,
+            "r0_scalars": np.array([1.0, 1.5, 0.7]),
+            "distances": np.array([[0, 10, 30], [10, 0, 15], [30, 15, 0]]),
+            "migration_method": "gravity",
+            "gravity_k": 0.5,
+            "max_migr_frac": 0.3,
+            "stop_if_no_cases": False,
+            "verbose": 0,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.Transmission_ABM]
+    res, st = parity(sim, check=True, graphs=False)
+    assert res["new_exposed"].sum() > 2000
