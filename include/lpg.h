@@ -257,6 +257,29 @@ int64_t lpg_kernel_launches(lpg_handle* h);
 const char* lpg_last_error(const lpg_handle* h);
 void lpg_destroy(lpg_handle* h);
 
+/* ---------------------------------------------------------------------- */
+/* Standalone ops over plain device columns (no handle).  Asynchronous on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) on the
+ * current device.  Errors: a negative lpg_status; the text from
+ * lpg_op_last_error() (per host thread). */
+
+#define LPG_COUNT_SEIRP_MAX_NODES 4096
+
+/* count_SEIRP (laser_polio/model.py:869-899, kernel :902-929): per-node
+ * counts of slots [0, n_people) with disease_state >= 0 — S, E, I, R
+ * [n_nodes]; E_by_strain, I_by_strain [n_nodes][n_strains];
+ * potentially_paralyzed == 1 as POTP, paralyzed == 1 as P [n_nodes].
+ * Columns and outputs are device pointers; outputs are overwritten.  Slots
+ * with a node id outside [0, n_nodes), or E/I slots with a strain outside
+ * [0, n_strains), are not counted; their number goes to *n_invalid (device
+ * int64, may be NULL).  Scratch: cudaMallocAsync on `stream`. */
+int lpg_count_seirp(const int16_t* node_id, const int8_t* disease_state, const int8_t* strain,
+                    const int8_t* potentially_paralyzed, const int8_t* paralyzed, int32_t n_nodes, int32_t n_strains,
+                    int64_t n_people, int32_t* S, int32_t* E, int32_t* I, int32_t* R, int32_t* E_by_strain,
+                    int32_t* I_by_strain, int32_t* POTP, int32_t* P, int64_t* n_invalid, void* stream);
+
+const char* lpg_op_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

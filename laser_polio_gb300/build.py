@@ -1,6 +1,9 @@
 """Build the CUDA engine (liblpg.so) in-tree for sm_103a with nvcc.
 
     python -m laser_polio_gb300.build
+
+Each translation unit compiles to an object in parallel; one nvcc call
+links them into the shared library.
 """
 
 from __future__ import annotations
@@ -14,10 +17,11 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build" / "liblpg.so"
-SOURCES = [CSRC / "lpg_engine.cu"]
+SOURCES = [CSRC / "lpg_engine.cu", CSRC / "lpg_ops.cu"]
 DEPS = SOURCES + [CSRC / "lpg_kernels.cuh", CSRC / "lpg_engine.cuh", CSRC / "lpg_rng.h", CSRC / "lpg_detmath.h",
                   ROOT / "include" / "lpg.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-math-errno"]
 
 
 def nvcc() -> str:
@@ -30,16 +34,25 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if OUT.exists() and OUT.stat().st_mtime >= newest and not force:
         return OUT
     OUT.parent.mkdir(parents=True, exist_ok=True)
-    tmp = OUT.with_suffix(f".{os.getpid()}.tmp")
-    cmd = [
-        nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-shared",
-        "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-math-errno",
-        f"-I{ROOT / 'include'}", f"-I{CSRC}",
-        *[str(s) for s in SOURCES], "-o", str(tmp),
-    ]
-    if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    subprocess.run(cmd, check=True)
+    tag = os.getpid()
+    objs = [OUT.parent / f"{s.stem}.{tag}.o" for s in SOURCES]
+    procs = []
+    for src, obj in zip(SOURCES, objs):
+        cmd = [nvcc(), ARCH, *FLAGS, f"-I{ROOT / 'include'}", f"-I{CSRC}", "-c", str(src), "-o", str(obj)]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        procs.append((cmd, subprocess.Popen(cmd)))
+    failed = [cmd for cmd, p in procs if p.wait() != 0]
+    if failed:
+        for obj in objs:
+            obj.unlink(missing_ok=True)
+        raise subprocess.CalledProcessError(1, failed[0])
+    tmp = OUT.with_suffix(f".{tag}.tmp")
+    try:
+        subprocess.run([nvcc(), ARCH, "-shared", *[str(o) for o in objs], "-o", str(tmp)], check=True)
+    finally:
+        for obj in objs:
+            obj.unlink(missing_ok=True)
     os.replace(tmp, OUT)
     return OUT
 

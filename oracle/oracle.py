@@ -146,3 +146,40 @@ def km_newborn(cum, max_year, seed, t, slot):
 
 def num_threads():
     return lib().lpo_num_threads()
+
+
+def count_seirp(node_id, disease_state, strain, potentially_paralyzed, paralyzed, n_nodes, n_strains, n_people):
+    """count_SEIRP (laser_polio/model.py:869-899, kernel :902-929) in numpy.
+
+    Returns (S, E, I, R, E_by_strain, I_by_strain, POTP, P, n_invalid).  The
+    reference indexes out of bounds for a node id outside [0, n_nodes) or an
+    E/I strain outside [0, n_strains); such slots are skipped here and
+    counted in n_invalid.
+    """
+    n = int(n_people)
+    nd = np.asarray(node_id[:n]).astype(np.int64)
+    ds = np.asarray(disease_state[:n]).astype(np.int8)
+    st = np.asarray(strain[:n]).astype(np.int64)
+    pp = np.asarray(potentially_paralyzed[:n]).astype(np.int8)
+    pa = np.asarray(paralyzed[:n]).astype(np.int8)
+    G, ns = int(n_nodes), int(n_strains)
+    alive = ds >= 0
+    node_ok = (nd >= 0) & (nd < G)
+    ei = (ds == 1) | (ds == 2)
+    strain_ok = (st >= 0) & (st < ns)
+    live = alive & node_ok
+    n_invalid = int(np.count_nonzero(alive & ~node_ok) + np.count_nonzero(live & ei & ~strain_ok))
+
+    def count(mask):
+        return np.bincount(nd[live & mask], minlength=G).astype(np.int32)
+
+    S = count(ds == 0)
+    R = count(ds == 3)
+    POTP = count(pp == 1)
+    P = count(pa == 1)
+    Ebs = np.zeros((G, ns), dtype=np.int32)
+    Ibs = np.zeros((G, ns), dtype=np.int32)
+    for k in range(ns):
+        Ebs[:, k] = count((ds == 1) & (st == k))
+        Ibs[:, k] = count((ds == 2) & (st == k))
+    return S, Ebs.sum(axis=1).astype(np.int32), Ibs.sum(axis=1).astype(np.int32), R, Ebs, Ibs, POTP, P, n_invalid
