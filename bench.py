@@ -225,7 +225,8 @@ def reference_arm(args):
         "vs_baseline": None,
         "dtype": "int8/int32 state, f64 node FOI",
         "data": "synthetic (seeded numpy, Nigeria-scale shapes)",
-        "config": {"workload": "nigeria_like 774 nodes x 2.2e8 agents, capacity +30%, 2555-tick run",
+        "config": {"workload": f"nigeria_like {params['n_nodes']} nodes x {params['count']:.3g} agents, "
+                               "capacity +30%, 2555-tick run",
                    "agents": params["count"], "nodes": params["n_nodes"]},
         "cpu_baseline": {"value": cpu["value"], "unit": "agent-ticks/s", "cores": cpu["cores"], "kind": "port",
                          "sample": sample},
@@ -390,8 +391,8 @@ def main():
             "vs_baseline": None,
             "dtype": "int8/int32 state, f64 node FOI",
             "data": "synthetic (seeded numpy, Nigeria-scale shapes)",
-            "config": {"workload": "nigeria_like 774 nodes x 2.2e8 agents, capacity +30%, ticks "
-                                   f"{W + 1}-{W + K} of a 2555-tick run",
+            "config": {"workload": f"nigeria_like {params['n_nodes']} nodes x {params['count']:.3g} agents, "
+                                   f"capacity +30%, ticks {W + 1}-{W + K} of a 2555-tick run",
                        "agents": params["count"], "capacity": params["capacity"], "nodes": params["n_nodes"],
                        "l2": "state columns larger than L2 (no flush needed)", "replicas": ws},
             "e2e": e2e,
