@@ -278,6 +278,27 @@ int lpg_count_seirp(const int16_t* node_id, const int8_t* disease_state, const i
                     int64_t n_people, int32_t* S, int32_t* E, int32_t* I, int32_t* R, int32_t* E_by_strain,
                     int32_t* I_by_strain, int32_t* POTP, int32_t* P, int64_t* n_invalid, void* stream);
 
+/* lpg_count_seirp without any device allocation, for callers that cannot
+ * allocate device memory at call time (a process whose device memory is
+ * claimed by its own caching pool; a loop that must not stall the device,
+ * which cudaFree does).  No counterpart in the reference (its count_SEIRP
+ * allocates numpy tables on every call).  Same arguments and results as
+ * lpg_count_seirp; n_nodes is limited the same way (LPG_COUNT_SEIRP_MAX_NODES),
+ * and a histogram larger than the static scratch is rejected with
+ * LPG_ERR_ARG.
+ *   - Scratch: a file-scope device array of LPG_COUNT_SEIRP_STATIC_WORDS
+ *     int32 words (4 MiB) per device; nothing in it needs to start at zero.
+ *   - The first call on each device looks up the array's device address with
+ *     that device current; make that first call before any stream capture.
+ *   - All calls on a device share the array: calls whose kernels overlap on
+ *     the GPU race and may return wrong counts.  Serialize them (one stream). */
+#define LPG_COUNT_SEIRP_STATIC_WORDS (1 << 20)
+int lpg_count_seirp_static(const int16_t* node_id, const int8_t* disease_state, const int8_t* strain,
+                           const int8_t* potentially_paralyzed, const int8_t* paralyzed, int32_t n_nodes,
+                           int32_t n_strains, int64_t n_people, int32_t* S, int32_t* E, int32_t* I, int32_t* R,
+                           int32_t* E_by_strain, int32_t* I_by_strain, int32_t* POTP, int32_t* P,
+                           int64_t* n_invalid, void* stream);
+
 const char* lpg_op_last_error(void);
 
 #ifdef __cplusplus

@@ -36,6 +36,7 @@ SIGNATURES = {
     "lpg_last_error": (C.c_char_p, [C.c_void_p]),
     "lpg_destroy": (None, [C.c_void_p]),
     "lpg_count_seirp": (C.c_int, [C.c_void_p] * 5 + [C.c_int32, C.c_int32, C.c_int64] + [C.c_void_p] * 10),
+    "lpg_count_seirp_static": (C.c_int, [C.c_void_p] * 5 + [C.c_int32, C.c_int32, C.c_int64] + [C.c_void_p] * 10),
     "lpg_op_last_error": (C.c_char_p, []),
 }
 

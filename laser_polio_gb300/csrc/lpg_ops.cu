@@ -13,7 +13,10 @@
  * not depend on the grid.  No global atomics, and the outputs are written
  * (not accumulated): the caller need not clear them.
  *
- * Scratch: one slice per CTA, from cudaMallocAsync on the caller's stream.
+ * Two entry points share these kernels:
+ *   lpg_count_seirp         scratch from cudaMallocAsync on the caller's stream;
+ *   lpg_count_seirp_static  scratch in a file-scope __device__ array, for
+ *                           callers that cannot allocate device memory.
  */
 #include <cuda_runtime.h>
 #include <stdarg.h>
@@ -223,12 +226,14 @@ __global__ void __launch_bounds__(SEIRP_THREADS) k_seirp_reduce(SeirpIn a, Seirp
 }
 
 /* ------------------------------------------------------------------------ */
-/* Per-device setup: SM count, and the dynamic
+/* Per-device setup shared by both entry points: SM count, and the dynamic
  * shared memory opt-in of the partial kernels (up to SEIRP_FIELDS_MAX x
  * LPG_COUNT_SEIRP_MAX_NODES + 1 words). */
 struct SeirpDev {
   bool ready;
   int sms;
+  bool static_ready;
+  int32_t* static_scratch; /* device address of g_seirp_scratch on this device */
 };
 static SeirpDev g_dev[SEIRP_MAX_DEVICES];
 static std::mutex g_dev_mu;
@@ -259,7 +264,8 @@ struct SeirpLaunch {
   int dev;
 };
 
-/* Argument checks; fills the launch record with the grid. */
+/* Argument checks shared by both entry points; fills the launch record with
+ * the grid the allocating entry point uses. */
 static int seirp_prepare(SeirpLaunch& L, const int16_t* node_id, const int8_t* disease_state, const int8_t* strain,
                          const int8_t* potentially_paralyzed, const int8_t* paralyzed, int32_t n_nodes,
                          int32_t n_strains, int64_t n_people, int32_t* S, int32_t* E, int32_t* I, int32_t* R,
@@ -325,4 +331,64 @@ extern "C" int lpg_count_seirp(const int16_t* node_id, const int8_t* disease_sta
   if (rc) return rc;
   if (e != cudaSuccess) return op_fail(LPG_ERR_CUDA, "count_SEIRP scratch free: %s", cudaGetErrorString(e));
   return LPG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The no-allocation variant.  Its scratch is this file-scope array, one per
+ * device that loads the library: LPG_COUNT_SEIRP_STATIC_WORDS int32 words
+ * (4 MiB).  It exists for callers that cannot allocate device memory at call
+ * time: a host process whose device memory is already claimed by its own
+ * caching pool (a framework allocator that reserved the free memory, so a
+ * second allocator fails with out-of-memory), and a loop that must not
+ * stall the device (cudaFree synchronizes the whole device, and a
+ * stream-ordered pool may have to grow).
+ *
+ * Nothing in the array needs to start at zero: every launch writes each
+ * histogram slice in full before the reduce kernel reads it.  The grid is
+ * shrunk so that nblk slices fit; the largest slice (4096 nodes, 4 strains)
+ * still leaves room for 21 CTAs.
+ *
+ * All calls on one device share the array, so two calls whose kernels
+ * overlap on the GPU (different streams, or different host threads without
+ * ordering between their streams) race on it and may return wrong counts.
+ * Serialize them, e.g. by issuing them on one stream. */
+static __device__ __align__(256) int32_t g_seirp_scratch[LPG_COUNT_SEIRP_STATIC_WORDS];
+
+/* The first call on each device takes the device address of
+ * g_seirp_scratch with that device current (the call's current device);
+ * later calls reuse it.  That first call per device should come before any
+ * stream capture begins. */
+static int seirp_static_setup(int dev, int32_t** out) {
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  SeirpDev& d = g_dev[dev];
+  if (!d.static_ready) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_seirp_scratch);
+    if (e != cudaSuccess || !p)
+      return op_fail(LPG_ERR_CUDA, "count_SEIRP static scratch address: %s", cudaGetErrorString(e));
+    d.static_scratch = (int32_t*)p;
+    d.static_ready = true;
+  }
+  *out = d.static_scratch;
+  return LPG_OK;
+}
+
+extern "C" int lpg_count_seirp_static(const int16_t* node_id, const int8_t* disease_state, const int8_t* strain,
+                                      const int8_t* potentially_paralyzed, const int8_t* paralyzed, int32_t n_nodes,
+                                      int32_t n_strains, int64_t n_people, int32_t* S, int32_t* E, int32_t* I,
+                                      int32_t* R, int32_t* E_by_strain, int32_t* I_by_strain, int32_t* POTP,
+                                      int32_t* P, int64_t* n_invalid, void* stream) {
+  SeirpLaunch L;
+  int rc = seirp_prepare(L, node_id, disease_state, strain, potentially_paralyzed, paralyzed, n_nodes, n_strains,
+                         n_people, S, E, I, R, E_by_strain, I_by_strain, POTP, P, n_invalid, stream);
+  if (rc) return rc;
+  const int64_t slice = (int64_t)L.in.F * n_nodes + 1;
+  if (slice > LPG_COUNT_SEIRP_STATIC_WORDS)
+    return op_fail(LPG_ERR_ARG, "count_SEIRP_static: %lld histogram words exceed the static scratch of %d",
+                   (long long)slice, LPG_COUNT_SEIRP_STATIC_WORDS);
+  L.nblk = (int)std::min<int64_t>(L.nblk, LPG_COUNT_SEIRP_STATIC_WORDS / slice);
+  int32_t* part = nullptr;
+  rc = seirp_static_setup(L.dev, &part);
+  if (rc) return rc;
+  return seirp_launch(L, part);
 }
