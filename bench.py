@@ -37,7 +37,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-# survey: compulsory column bytes per agent-tick by tick type
+# column bytes the reference's per-tick loops read per agent-tick, each column once, by tick type
 B_EVERY = 18.0  # state, node, strain, 3 timers, pp, paralyzed, ipv, risk, infectivity
 B_VD = 4.0  # date_of_death on VD ticks
 B_RI = 5.0  # ri_timer read + write, chronically_missed on RI ticks
@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--batch", type=int, default=0,
+                    help="instead: R calibration replicates (730 ticks) batched in one handle vs run one by one")
     return ap.parse_args()
 
 
@@ -69,7 +71,11 @@ def dist_env():
 
 
 def tick_bytes(params, t):
-    """Survey's algorithmic bytes per agent for tick t."""
+    """Bytes per agent slot on tick t of every column the reference's loops
+    read that tick, each counted once (state, node, strain, three timers,
+    paralysis flags, IPV flag, risk, infectivity; date of death on VD ticks;
+    RI timer and chronically-missed flag on RI ticks; date of birth and the
+    flag on SIA days)."""
     b = B_EVERY
     if t % params["vd_step"] == 0:
         b += B_VD
@@ -79,20 +85,29 @@ def tick_bytes(params, t):
     return b
 
 
-def sweep_bytes(params, t):
-    """Columns the fused sweep must read for every agent slot on tick t:
-    the state byte always; date_of_death on VD ticks; chronically_missed and
-    ri_timer (read + write) on RI ticks; chronically_missed and date_of_birth
-    on SIA days.  Timers, strain, flags, risk and infectivity are read only
-    for the agents whose state needs them (sector-granular in practice)."""
-    b = 1.0
-    if t % params["vd_step"] == 0:
-        b += 4.0
-    if params["ri_enabled"] and t % params["ri_step"] == 0:
-        b += 1.0 + 2.0 + 2.0
-    if any(e[0] == t for e in params["sia"]):
-        b += 1.0 + 4.0
-    return b
+def sweep_a_bytes(params, t):
+    """Column bytes k_sweep<0> must read per agent slot on tick t: the state
+    byte always, date_of_death on VD ticks.  Timers, strain, flags, risk and
+    infectivity are read only for the agents whose state needs them (by the
+    queue kernels)."""
+    return 1.0 + (4.0 if t % params["vd_step"] == 0 else 0.0)
+
+
+def sweep_b_bytes(params, t):
+    """Column bytes k_sweep<1> moves per agent slot on tick t (0 when it has
+    nothing to do): state, chronically_missed, ri_timer read and write on RI
+    ticks; state, chronically_missed, date_of_birth on SIA days."""
+    ri = bool(params["ri_enabled"]) and t % params["ri_step"] == 0
+    sia = any(e[0] == t for e in params["sia"])
+    if not (ri or sia):
+        return 0.0
+    return 1.0 + 1.0 + (4.0 if ri else 0.0) + (4.0 if sia else 0.0)
+
+
+# DRAM bytes per slot that ncu measured for k_sweep<0> (dram__bytes_read.sum +
+# dram__bytes_write.sum over the launch / slots scanned) on a 5.1e7-agent
+# population: plain ticks and VD ticks (profiles/k_sweep_dram_nigeria_5e7.md).
+NCU_SWEEP_A_BYTES_PER_SLOT = {"plain": 1.0006, "vd": 4.987}
 
 
 class ClockSampler:
@@ -235,10 +250,93 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def batch_arm(args):
+    """R calibration replicates (node counts from {14, 44, 120, 300}, 1e6-2e7
+    agents each, per-replicate R0 / seasonality / gravity k, 730 ticks): the
+    same ticks timed once with all replicates in one handle (one launch
+    sequence per tick) and once as R plain runs one after another.  Both
+    arms time only the device ticks (CUDA events on the handle's stream)."""
+    import torch
+
+    from laser_polio_gb300 import synthetic
+    from laser_polio_gb300._lib import Handle
+    from laser_polio_gb300.engine import make_desc
+
+    t_gen = time.perf_counter()
+    specs = synthetic.replicate_specs(args.batch, seed=args.seed, dur=730)
+    bundles = [synthetic.bundle(**sp) for sp in specs]
+    t_gen = time.perf_counter() - t_gen
+    descs = [make_desc(p) for p, _ in bundles]
+    nt = bundles[0][0]["nt"]
+    W = args.warmup
+    K = min(args.steps, nt - 1 - W)
+
+    def timed(idx):
+        h = Handle([descs[i][0] for i in idx])
+        for j, i in enumerate(idx):
+            h.bind_columns(j, bundles[i][1])
+        h.start()
+        h.step(W)
+        h.sync()
+        stream = torch.cuda.ExternalStream(h.cuda_stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        h.step(K)
+        e1.record(stream)
+        h.sync()
+        ms = e0.elapsed_time(e1)
+        at = 0.0
+        for j, i in enumerate(idx):
+            res = result_arrays(bundles[i][0])
+            h.read_results(j, res)
+            cnt = counts_per_tick(bundles[i][0], res["births"])
+            at += float(cnt[W + 1 : W + K + 1].sum())
+        launches = h.kernel_launches()
+        h.close()
+        return ms, at, launches
+
+    with ClockSampler(0) as clocks:
+        ms_b, at_b, _ = timed(list(range(len(bundles))))
+    ms_s, at_s = 0.0, 0.0
+    for i in range(len(bundles)):
+        ms, at, _ = timed([i])
+        ms_s += ms
+        at_s += at
+    assert at_s == at_b
+    line = {
+        "metric": f"agent-ticks/s, {len(bundles)}-replicate calibration batch",
+        "value": at_b / (ms_b / 1e3),
+        "unit": "agent-ticks/s",
+        "n_gpus": 1,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": ms_b / K,
+        "higher_is_better": True,
+        "data": "synthetic (seeded numpy, calibration-batch shapes)",
+        "config": {"workload": f"{len(bundles)} replicates, nodes in {{14, 44, 120, 300}}, "
+                               f"{sum(p['count'] for p, _ in bundles):.3g} agents in total, "
+                               f"ticks {W + 1}-{W + K} of 730",
+                   "agents": [p["count"] for p, _ in bundles], "nodes": [p["n_nodes"] for p, _ in bundles]},
+        "sequential": {"value": at_s / (ms_s / 1e3), "ms_total": ms_s},
+        "batched_ms_total": ms_b,
+        "speedup_vs_sequential": ms_s / ms_b,
+        "clocks": clocks.summary(),
+        "generation_s": t_gen,
+    }
+    print(json.dumps(line), flush=True)
+    if args.out:
+        Path(args.out).write_text(json.dumps(line, indent=1))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.batch:
+        batch_arm(args)
         return
     import torch
 
@@ -350,7 +448,11 @@ def main():
         top = max(prof, key=lambda k: prof[k][0])
         sweep_ms, sweep_n = prof["k_sweep_a"]
         alg = sum(tick_bytes(params, t) * cnt[t] for t in ticks) / K
-        kern = sum(sweep_bytes(params, t) * cnt[t] for t in ticks) / K
+        kern = sum(sweep_a_bytes(params, t) * cnt[t] for t in ticks) / K
+        traffic = sum(NCU_SWEEP_A_BYTES_PER_SLOT["vd" if t % params["vd_step"] == 0 else "plain"] * cnt[t]
+                      for t in ticks) / K
+        b_ticks = [t for t in ticks if sweep_b_bytes(params, t) > 0]
+        kern_b = sum(sweep_b_bytes(params, t) * cnt[t] for t in b_ticks) / max(1, len(b_ticks))
         per_launch_ms = sweep_ms / max(1, sweep_n)
         roof = {
             "kernel": "k_sweep_a",
@@ -359,12 +461,15 @@ def main():
             "peak": peak,
             "unit": "GB/s",
             "frac": kern / (per_launch_ms / 1e3) / 1e9 / peak,
-            "traffic": None,
+            "traffic": traffic,
+            "traffic_source": "ncu DRAM bytes per slot of k_sweep<0> on plain and VD ticks (5.1e7 agents), "
+                              "times the slots of each timed launch",
             "peak_source": which,
             "alg_bytes_per_launch": kern,
-            "survey_bytes_per_launch": alg,
-            "survey_equiv_gbs": alg / (per_launch_ms / 1e3) / 1e9,
+            "reference_column_bytes_per_launch": alg,
+            "reference_column_equiv_gbs": alg / (per_launch_ms / 1e3) / 1e9,
             "mean_launch_ms": per_launch_ms,
+            "k_sweep_b": {"alg_bytes_per_active_launch": kern_b, "active_launches": len(b_ticks)},
             "top_kernel": top,
             "kernel_ms_per_tick": {k: v[0] / max(1, v[1]) for k, v in prof.items()},
             "kernel_share": {k: v[0] / sum(x[0] for x in prof.values()) for k, v in prof.items()},

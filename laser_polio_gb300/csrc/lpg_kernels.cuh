@@ -317,12 +317,13 @@ __global__ void k_newborns(DevWorld W) {
  * consecutive chunks, k = as many as fit in LPG_COL_BYTES given the tick's
  * columns: state bytes always; date_of_death on VD ticks; ri_timer and
  * chronically_missed on RI ticks; chronically_missed and date_of_birth on
- * SIA days.  A warp processes one chunk at a time (every lane the same
- * chunk, so the same node): its events go to per-warp shared counters,
- * flushed to the node totals with one global atomic per counter after the
- * chunk.  There is no CTA-wide barrier in the steady state.  Every mbarrier
- * wait is bounded; on a timeout the kernel raises an error, stops issuing,
- * waits (bounded) for the copies it issued and returns. */
+ * SIA days.  Each consumer thread tests 16 slots at a time with SIMD byte
+ * compares and appends the agents that need work to its CTA's queue slab;
+ * on ticks that stage only state bytes, a warp whose 512 slots hold no
+ * agent in E or I moves on after one vote.  Each consumer warp releases a
+ * stage with one arrival.  There is no CTA-wide barrier in the steady state.
+ * Every mbarrier wait is bounded; on a timeout the kernel raises an error,
+ * stops issuing, waits (bounded) for the copies it issued and returns. */
 #define LPG_NST 4
 #define LPG_META_BYTES 256
 #define LPG_COL_BYTES (24 * 1024)
@@ -330,6 +331,16 @@ __global__ void k_newborns(DevWorld W) {
 #define LPG_PLAIN_GROUP (LPG_COL_BYTES / LPG_CHUNK)
 #define LPG_SWEEP_SMEM (LPG_NST * LPG_STAGE_BYTES)
 #define LPG_MBAR_SPIN (1LL << 24)
+#define LPG_DIRECT_UNROLL 8
+
+/* 16-byte global load that bypasses L1 allocation (streamed once). */
+__device__ __forceinline__ uint4 ldg_stream16(const void* p) {
+  uint4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p));
+  return v;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -369,6 +380,7 @@ enum { SF_WORK = 1, SF_DENSE = 2, SF_VD = 4, SF_DS = 8, SF_RI = 16, SF_SIA = 32 
 
 struct SweepPlan {
   int32_t total, nreps;
+  int32_t direct; /* PHASE 0 with state bytes only for every simulation: no staging */
   int32_t off[LPG_MAX_REPS + 1]; /* work-item offsets per simulation */
   int32_t cbase[LPG_MAX_REPS];   /* first chunk id per simulation */
   int32_t tick[LPG_MAX_REPS];
@@ -655,12 +667,16 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
     P.off[R] = acc;
     P.total = acc;
     P.nreps = R;
+    int direct = PHASE == 0;
+    for (int r = 0; r < R; ++r)
+      if ((P.flags[r] & SF_WORK) && (P.flags[r] & (SF_DS | SF_VD)) != SF_DS) direct = 0;
+    P.direct = direct;
     s_qcnt = 0;
     s_issued = 0;
     s_abort = 0;
     for (int b = 0; b < LPG_NST; ++b) {
       mbar_init(&full[b], 1);
-      mbar_init(&empty[b], LPG_SWEEP_CONSUMERS);
+      mbar_init(&empty[b], LPG_SWEEP_CONSUMERS / 32);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -672,7 +688,47 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   uint64_t* slab = W.evq + (int64_t)w0 * LPG_CHUNK;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  if (warp == LPG_SWEEP_CONSUMERS / 32) {
+  if (PHASE == 0 && P.direct) {
+    /* Only state bytes to read: every warp streams them straight from global
+     * memory, LPG_DIRECT_UNROLL 16-byte loads in flight per thread, and
+     * queues the agents in E or I.  A simulation's work items map to
+     * consecutive chunks, so each simulation's share of [w0, w1) is one
+     * contiguous byte range. */
+    int32_t w = w0;
+    while (w < w1) {
+      int r;
+      (void)stage_end(P, w, w1, &r);
+      const int32_t we = min(w1, P.off[r + 1]);
+      const int64_t lo = (P.cbase[r] + (int64_t)(w - P.off[r])) * LPG_CHUNK;
+      const int64_t nbytes = (int64_t)(we - w) * LPG_CHUNK;
+      const int t = P.tick[r];
+      const uint8_t* base = reinterpret_cast<const uint8_t*>(W.ds) + lo;
+      const int64_t step = (int64_t)LPG_SWEEP_BLOCK * 16 * LPG_DIRECT_UNROLL;
+      for (int64_t ob = 0; ob < nbytes; ob += step) {
+        uint4 v[LPG_DIRECT_UNROLL];
+        uint32_t e = 0;
+#pragma unroll
+        for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
+          const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
+          v[u] = o < nbytes ? ldg_stream16(base + o) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+        }
+#pragma unroll
+        for (int u = 0; u < LPG_DIRECT_UNROLL; ++u)
+          e |= __vcmpltu4(__vsub4(v[u].x, 0x01010101u), 0x02020202u) |
+               __vcmpltu4(__vsub4(v[u].y, 0x01010101u), 0x02020202u) |
+               __vcmpltu4(__vsub4(v[u].z, 0x01010101u), 0x02020202u) |
+               __vcmpltu4(__vsub4(v[u].w, 0x01010101u), 0x02020202u);
+        if (__ballot_sync(FULLMASK, e != 0) == 0) continue;
+#pragma unroll
+        for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
+          const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
+          sweep_a16(slab, &s_qcnt, W, o < nbytes, true, t, lo + o, (int)(o & (LPG_CHUNK - 1)), LPG_CHUNK, v[u],
+                    nullptr);
+        }
+      }
+      w = we;
+    }
+  } else if (warp == LPG_SWEEP_CONSUMERS / 32) {
     /* ---- producer warp: one lane issues the stages ---- */
     if (lane == 0 && w0 < w1) {
       int32_t wp = w0;
@@ -728,6 +784,37 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       const int nc = we - wc;
       const StageLayout L = stage_layout(fl, nc);
       const int ngroups = nc * (LPG_CHUNK / 16);
+      if (PHASE == 0 && (fl & (SF_DS | SF_VD)) == SF_DS) {
+        /* state bytes only: queue the agents in E or I.  Two 16-slot groups
+         * per thread per pass; a warp with none in either skips the rest. */
+        const uint8_t* dsb = cols + L.ds;
+        const int nbytes = nc * LPG_CHUNK;
+        const int64_t pos_base = (P.cbase[r] + (int64_t)(wc - P.off[r])) * LPG_CHUNK;
+        for (int ob = 0; ob < nbytes; ob += 2 * LPG_SWEEP_CONSUMERS * 16) {
+          const int oa = ob + threadIdx.x * 16, oc = oa + LPG_SWEEP_CONSUMERS * 16;
+          const uint4 none = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+          const uint4 va = oa < nbytes ? *reinterpret_cast<const uint4*>(dsb + oa) : none;
+          const uint4 vc = oc < nbytes ? *reinterpret_cast<const uint4*>(dsb + oc) : none;
+          const uint32_t ea = __vcmpltu4(__vsub4(va.x, 0x01010101u), 0x02020202u) |
+                              __vcmpltu4(__vsub4(va.y, 0x01010101u), 0x02020202u) |
+                              __vcmpltu4(__vsub4(va.z, 0x01010101u), 0x02020202u) |
+                              __vcmpltu4(__vsub4(va.w, 0x01010101u), 0x02020202u);
+          const uint32_t ec = __vcmpltu4(__vsub4(vc.x, 0x01010101u), 0x02020202u) |
+                              __vcmpltu4(__vsub4(vc.y, 0x01010101u), 0x02020202u) |
+                              __vcmpltu4(__vsub4(vc.z, 0x01010101u), 0x02020202u) |
+                              __vcmpltu4(__vsub4(vc.w, 0x01010101u), 0x02020202u);
+          const unsigned vote = __ballot_sync(FULLMASK, ea != 0) | __ballot_sync(FULLMASK, ec != 0);
+          if (vote == 0) continue;
+          sweep_a16(slab, &s_qcnt, W, oa < nbytes, true, t, pos_base + oa, oa & (LPG_CHUNK - 1), LPG_CHUNK, va,
+                    nullptr);
+          sweep_a16(slab, &s_qcnt, W, oc < nbytes, true, t, pos_base + oc, oc & (LPG_CHUNK - 1), LPG_CHUNK, vc,
+                    nullptr);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[b]);
+        wc = we;
+        continue;
+      }
       for (int gb = 0; gb < ngroups; gb += LPG_SWEEP_CONSUMERS) {
         const int gi = gb + threadIdx.x;
         const bool on = gi < ngroups;
@@ -753,7 +840,8 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
                     reinterpret_cast<const int32_t*>(cols + L.dob + kk * 4 * LPG_CHUNK));
         }
       }
-      mbar_arrive(&empty[b]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[b]);
       wc = we;
     }
   }

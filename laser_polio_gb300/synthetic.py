@@ -19,11 +19,13 @@ distributions:
                  lognormal(ln 2.8e5, 0.7), under-15 immunity U(0.4, 0.9) per
                  node, three strains, RI coverage beta(6, 4), an SIA every
                  180 d over 30% of nodes (ages 0-5 y, coverage beta(8, 3),
-                 efficacy 0.6), CBR 37, 2555 ticks.  Its columns are built on
-                 the host for moderate sizes and by ``device_columns`` on the
-                 GPU for the full size.
+                 efficacy 0.6), CBR 37, 2555 ticks.
 
 Both return a fully initialised SEIR_ABM with the five drop-in components.
+For the full sizes, ``bundle`` builds the same recipe directly as
+reference-ordered column arrays (no SEIR_ABM, no per-agent Python), in
+parallel chunks on the host; ``replicate_specs`` draws the per-replicate
+settings of a calibration batch (64 replicates of 1e6-2e7 agents, 730 ticks).
 """
 
 from __future__ import annotations
@@ -193,13 +195,15 @@ def _km_ages(rng, cum, ages_days, max_year=100):
 
 
 def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capacity_factor=1.3, threads=None,
-           alloc=None):
+           alloc=None, r0=14.0, amp=0.4, peak=180, gravity_k=0.5):
     """(make_desc parameters, reference-ordered columns) of a synthetic run.
 
     kind 'nigeria' (defaults 2.2e8 agents, 774 nodes, 2555 ticks) or
     'zamfara' (1e6 agents, 14 nodes, 365 ticks).  ``alloc(name, n, dtype)``
     may supply the column buffers (pinned host memory for the end-to-end
-    measurement).
+    measurement).  r0, amp, peak and gravity_k are the replicate-level
+    parameters a calibration varies (R0, seasonal amplitude and peak day,
+    gravity k).
     """
     import concurrent.futures as cf
     import datetime as dt
@@ -227,7 +231,7 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
     count = int(pops.sum())
     capacity = int(count * capacity_factor)
     nt = dur + 1
-    r0 = 14.0
+    r0 = float(r0)
     if kind == "nigeria":
         immun = rng.uniform(0.4, 0.9, n_nodes)
         p_ri = rng.beta(6, 4, n_nodes)
@@ -247,7 +251,7 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
     dist = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
     dist[dist == 0] = 1.0
     np.fill_diagonal(dist, 0.0)
-    net = row_normalizer(gravity(pops, dist, 0.5, 1, 1, 2.0) / np.power(float(pops.sum()), 2.0), 0.2)
+    net = row_normalizer(gravity(pops, dist, float(gravity_k), 1, 1, 2.0) / np.power(float(pops.sum()), 2.0), 0.2)
     start = dt.date(2019, 1, 1)
     datevec = [start + dt.timedelta(days=i) for i in range(nt)]
     cum = create_cumulative_deaths(count, 100).astype(np.int64)
@@ -258,7 +262,7 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
         "km_cumdeaths": cum, "km_max_year": 100, "p_paralysis": 1 / 2000, "seeds": [], "dur_inf": (2, 4.0, 6.0),
         "ri_step": 14, "ri_enabled": 1, "ri_strain": 1, "vx_prob_ri": p_ri, "vx_prob_ipv": np.zeros(n_nodes),
         "sia": sia, "vx_prob_sia": p_sia.astype(np.float32), "strain_r0_scalars": np.array([1.0, 0.25, 0.125]),
-        "network": net, "r0_scalars": r0s, "seasonality": seasonality_table(datevec, 0.4, 180),
+        "network": net, "r0_scalars": r0s, "seasonality": seasonality_table(datevec, float(amp), int(peak)),
         "zero_inflation": 0.0, "nb_r": 1000, "pop0": pops.astype(np.int32), "R_preseed": None,
     }
 
@@ -329,6 +333,28 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
         cols["disease_state"][pick] = 2
         cols["strain"][pick] = 0
     return params, cols
+
+
+def replicate_specs(n=64, seed=42, dur=730):
+    """Per-replicate settings of a calibration batch: node counts from
+    {14, 44, 120, 300}, agents log-uniform in [1e6, 2e7] (about 4e8 in total
+    for 64), R0 ~ U(8, 20), seasonal amplitude ~ U(0.1, 0.6), peak day
+    ~ U(0, 364), gravity k ~ lognormal(ln 0.5, 0.5), seeds seed + r."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(n):
+        out.append({
+            "kind": "zamfara",
+            "n_nodes": int(rng.choice([14, 44, 120, 300])),
+            "n_agents": int(np.exp(rng.uniform(np.log(1e6), np.log(2e7)))),
+            "dur": dur,
+            "seed": seed + r,
+            "r0": float(rng.uniform(8, 20)),
+            "amp": float(rng.uniform(0.1, 0.6)),
+            "peak": int(rng.integers(0, 365)),
+            "gravity_k": float(rng.lognormal(np.log(0.5), 0.5)),
+        })
+    return out
 
 
 def os_cpu():

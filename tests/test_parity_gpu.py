@@ -187,3 +187,33 @@ def test_parity_heavy_collisions():
     sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.Transmission_ABM]
     res, st = parity(sim, check=True, graphs=False)
     assert res["new_exposed"].sum() > 2000
+
+
+def test_parity_batched_replicates():
+    """Replicates of different sizes, node counts, durations and components
+    in one handle: each equals its own oracle run."""
+    from laser_polio_gb300._lib import Handle
+
+    sims = [
+        synthetic.zamfara_like(n_agents=80_000, dur=90, seed=1),
+        synthetic.nigeria_like(n_agents=150_000, n_nodes=44, dur=120, seed=2),
+        _busy_sim(seed=8, dur=70, stop=True),
+        synthetic.zamfara_like(n_agents=30_000, dur=150, seed=3, n_nodes=5),
+    ]
+    snaps_o = [snapshot(s) for s in sims]
+    snaps_g = [snapshot(s) for s in sims]
+    states_o = [run_spec_oracle(spec, cols, res, s.nt - 1) for s, (spec, cols, res) in zip(sims, snaps_o)]
+    h = Handle([spec.desc for spec, _, _ in snaps_g])
+    for i, (_, cols, _) in enumerate(snaps_g):
+        h.bind_columns(i, cols)
+    h.start()
+    h.step(max(s.nt for s in sims) - 1)
+    h.sync()
+    for i, ((_, cols_o, res_o), (_, cols_g, res_g), so) in enumerate(zip(snaps_o, snaps_g, states_o)):
+        sg = h.state(i)
+        assert (sg.t, sg.stopped, sg.count, sg.error) == (so.t, so.stopped, so.count, so.error), i
+        h.read_results(i, res_g)
+        h.read_columns(i, cols_g)
+        assert_same(res_o, res_g, f"replicate {i} result")
+        assert_same(cols_o, cols_g, f"replicate {i} column", count=so.count)
+    h.close()
