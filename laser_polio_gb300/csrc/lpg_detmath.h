@@ -182,4 +182,39 @@ LPG_HD double lpg_lfact(int64_t k) {
   return (x - 0.5) * lpg_log(x) - x + LPG_HALF_LOG_2PI + corr;
 }
 
+/* rint(r * 2^24) as an unsigned integer, clamped to [0, 2^62], for a float
+ * r (0 for r <= 0 and NaN) — the fixed-point susceptibility weight — from
+ * the bits of r alone, with integer operations only.  r * 2^24 is exact in
+ * double, so this equals the double-precision definition
+ * (d = (double)r * 2^24; !(d > 0) -> 0; min(d, 2^62); rint(d)) bit for bit:
+ * for r = M * 2^(E - 150) (M the 24-bit significand, E the biased exponent)
+ * the product is M * 2^(E - 126), a left shift for E >= 126 and otherwise a
+ * right shift rounded half to even. */
+LPG_HD uint64_t lpg_fix_risk_bits(float r) {
+  union {
+    float f;
+    uint32_t u;
+  } c;
+  c.f = r;
+  const uint32_t u = c.u;
+  if (u & 0x80000000u) return 0; /* negative (or -0, negative NaN) */
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint32_t frac = u & 0x7fffffu;
+  if (e == 0xffu) return frac ? 0 : ((uint64_t)1 << 62); /* NaN -> 0, +inf -> clamp */
+  if (e == 0) return 0;                                   /* zero or subnormal: below 2^-126 * 2^24 < 1/2 */
+  const uint64_t m = (uint64_t)(frac | 0x800000u);
+  if (e >= 126) {
+    const uint32_t sh = e - 126;
+    if (sh >= 39) return (uint64_t)1 << 62; /* m * 2^sh >= 2^62 */
+    const uint64_t v = m << sh;
+    return v > ((uint64_t)1 << 62) ? ((uint64_t)1 << 62) : v;
+  }
+  const uint32_t s = 126 - e; /* 1 .. 125 */
+  if (s > 24) return 0;       /* m * 2^-s < 1/2 */
+  const uint64_t q = m >> s;
+  const uint64_t rem = m & (((uint64_t)1 << s) - 1);
+  const uint64_t half = (uint64_t)1 << (s - 1);
+  return q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+}
+
 #endif /* LPG_DETMATH_H */

@@ -494,6 +494,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.chunk_w, chunk_total);
   rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.cpref, chunk_total);
+  rc |= dalloc(h, &W.sel_part, 1024);
   rc |= dalloc(h, &W.node_chunks[0], chunk_total);
   rc |= dalloc(h, &W.node_chunks[1], chunk_total);
   rc |= dalloc(h, &W.node_chunk_start[0], csr_total);
@@ -511,6 +512,12 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.uniq, G);
   rc |= dalloc(h, &W.ksel, G);
   rc |= dalloc(h, &W.tgt_off, G + 1);
+  {
+    uint8_t* si = nullptr;
+    rc |= dalloc(h, &si, (size_t)G * sizeof(SelInfo));
+    W.sel_info = si;
+  }
+  rc |= dalloc(h, &W.sel_base, G);
   /* selection targets (at most the susceptibles) and the E/I queue slabs
    * (at most one entry per position) share this buffer */
   int64_t hits = (int64_t)chunk_total * LPG_CHUNK;
@@ -785,7 +792,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   h->sweep_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
   occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_select, 256, 0));
-  h->select_blocks = std::max(1, std::min(occ, 2)) * h->sm_count;
+  h->select_blocks = std::min(1024, std::max(1, std::min(occ, 2)) * h->sm_count);
   h->started = true;
   return LPG_OK;
 }

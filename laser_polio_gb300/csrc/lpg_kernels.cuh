@@ -39,12 +39,7 @@
 
 /* ------------------------------------------------------------------------ */
 /* fixed-point weights (identical definitions in the oracle)                */
-__device__ __forceinline__ uint64_t fix_risk(float r) {
-  double d = (double)r * 16777216.0;
-  if (!(d > 0.0)) return 0;
-  if (d > 0x1.0p62) d = 0x1.0p62;
-  return (uint64_t)rint(d);
-}
+__device__ __forceinline__ uint64_t fix_risk(float r) { return lpg_fix_risk_bits(r); }
 __device__ __forceinline__ uint64_t fix_beta(float inf, double scal) {
   double d = ((double)inf * scal) * 4294967296.0;
   if (!(d > 0.0)) return 0;
@@ -1404,28 +1399,31 @@ __device__ __forceinline__ bool grid_sync(DevWorld& W) {
   return *(volatile int32_t*)W.abort_flag == 0;
 }
 
-__device__ __forceinline__ int pick_strain(const double* p, int ns, double total_p, double r) {
-  double cum = 0.0;
-  for (int k = 0; k < ns; ++k) {
-    cum = cum + p[k] / total_p;
-    if (r < cum) return k;
+/* Weight of entry x of the concatenated CSR chunk lists (x = chunk_base of
+ * a simulation + position in its list; 0 past the end of a list).  With
+ * first_g: the global node whose list starts at x, else -1. */
+__device__ __forceinline__ uint64_t csr_chunk_weight(const DevWorld& W, int64_t x, int* first_g = nullptr) {
+  int lo = 0, hi = W.n_reps - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (W.reps[mid].chunk_base <= x) lo = mid; else hi = mid - 1;
   }
-  return 0;
+  const DevRep* rp = &W.reps[lo];
+  const int64_t j = x - rp->chunk_base;
+  const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+  if (j < 0 || j >= st[rp->n_nodes]) return 0;
+  const int32_t cid = W.node_chunks[rp->csr_cur][rp->chunk_base + j];
+  if (first_g) {
+    const int g = W.cmeta[cid].x;
+    if (st[g - rp->node_base] == j) *first_g = g;
+  }
+  return __ldcg(&W.chunk_w[cid]);
 }
 
-/* Locate target v (< the node's remaining susceptible weight) in node g's
- * frozen CDF: chunk by binary search of the chunk prefix cp, sub-block by
- * its 16 totals, slot by the 128 state bytes and risks.  LPG_NONE if the
- * weights are inconsistent (an internal error). */
-__device__ __forceinline__ uint32_t locate(const DevWorld& W, const int32_t* ls, const uint64_t* cp, int32_t a,
-                                           int32_t b, uint64_t v) {
-  int32_t lo = a, hi = b - 1;
-  while (lo < hi) {
-    int32_t mid = (lo + hi) >> 1;
-    if (cp[mid] > v) hi = mid; else lo = mid + 1;
-  }
-  if (lo > a) v -= cp[lo - 1];
-  const int64_t cid = ls[lo];
+/* Slot of target v inside chunk cid (v < the chunk's remaining weight):
+ * sub-block by its 16 totals, slot by the 128 state bytes and risks.
+ * LPG_NONE if the weights are inconsistent (an internal error). */
+__device__ __forceinline__ uint32_t locate_in_chunk(const DevWorld& W, int64_t cid, uint64_t v) {
   uint64_t swv[LPG_NSUB];
 #pragma unroll
   for (int k = 0; k < LPG_NSUB; ++k) swv[k] = __ldcg(&W.sub_w[cid * LPG_NSUB + k]);
@@ -1462,9 +1460,183 @@ __device__ __forceinline__ uint32_t locate(const DevWorld& W, const int32_t* ls,
   return hit;
 }
 
-/* The first agent of a target to claim it (state 0 -> 1) exposes it: strain
- * by relative FOI (model.py:1127-1145) and every susceptible total. */
-__device__ __forceinline__ void claim(DevWorld& W, uint32_t hit) {
+/* Locate target v (< the node's remaining susceptible weight) in the node's
+ * frozen CDF.  cp holds n chunk prefixes of the node's chunk list ls (n
+ * entries); the node's own prefix of entry j is cp[j] - base.  First chunk
+ * whose prefix exceeds v (searchsorted side='right', model.py:1118), then
+ * the slot inside it. */
+__device__ __forceinline__ uint32_t locate(const DevWorld& W, const int32_t* ls, const uint64_t* cp, int32_t n,
+                                           uint64_t v, uint64_t base) {
+  int32_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int32_t mid = (lo + hi) >> 1;
+    if (cp[mid] - base > v) hi = mid; else lo = mid + 1;
+  }
+  if (lo > 0) v -= cp[lo - 1] - base;
+  return locate_in_chunk(W, ls[lo], v);
+}
+
+/* A team of T lanes (T a power of two <= 32, aligned in its warp) that
+ * locates one target together. */
+struct Team {
+  unsigned mask; /* the team's lanes */
+  int T, l, lane0;
+};
+__device__ __forceinline__ Team make_team(int T) {
+  Team t;
+  const int lane = threadIdx.x & 31;
+  t.T = T;
+  t.l = lane & (T - 1);
+  t.lane0 = lane & ~(T - 1);
+  t.mask = T == 32 ? FULLMASK : (((1u << T) - 1u) << t.lane0);
+  return t;
+}
+__device__ __forceinline__ unsigned team_ballot(const Team& tm, bool p) {
+  return tm.T == 32 ? __ballot_sync(tm.mask, p) : (__ballot_sync(tm.mask, p) >> tm.lane0) & ((1u << tm.T) - 1u);
+}
+__device__ __forceinline__ uint64_t team_incl_scan(const Team& tm, uint64_t x) {
+  for (int o = 1; o < tm.T; o <<= 1) {
+    const uint64_t y = __shfl_up_sync(tm.mask, x, o, tm.T);
+    if (tm.l >= o) x += y;
+  }
+  return x;
+}
+
+/* locate() by a team: the same answer, with a (T+1)-ary search of the chunk
+ * prefix and, for T >= 4, the sub-block totals and the 128 slots split over
+ * the lanes (each lane a contiguous run; a team scan finds the lane that
+ * holds the target).  Every lane of the team returns the hit. */
+__device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& tm, const int32_t* ls,
+                                                const uint64_t* cp, int32_t n, uint64_t v, uint64_t base) {
+  const int T = tm.T;
+  int32_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int32_t m = hi - lo;
+    const int32_t p = lo + (int32_t)(((int64_t)(tm.l + 1) * m) / (T + 1));
+    const unsigned b = team_ballot(tm, cp[p] - base > v);
+    const int c = __ffs(b) - 1; /* first probe above v; probes ascend with the lane */
+    if (c < 0) {
+      lo = lo + (int32_t)(((int64_t)T * m) / (T + 1)) + 1;
+    } else {
+      const int32_t pc = lo + (int32_t)(((int64_t)(c + 1) * m) / (T + 1));
+      if (c > 0) lo = lo + (int32_t)(((int64_t)c * m) / (T + 1)) + 1;
+      hi = pc;
+    }
+  }
+  if (lo > 0) v -= cp[lo - 1] - base;
+  const int64_t cid = ls[lo];
+  if (T < 4) {
+    const uint32_t h = tm.l == 0 ? locate_in_chunk(W, cid, v) : 0u;
+    return __shfl_sync(tm.mask, h, 0, T);
+  }
+  /* sub-block: lanes l < min(T, 16) hold 16 / min(T, 16) consecutive totals */
+  const int TS = T < LPG_NSUB ? T : LPG_NSUB;
+  const int per = LPG_NSUB / TS;
+  uint64_t sw[LPG_NSUB];
+  uint64_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < LPG_NSUB; ++k) {
+    sw[k] = 0;
+    if (k < per && tm.l < TS) {
+      sw[k] = __ldcg(&W.sub_w[cid * LPG_NSUB + tm.l * per + k]);
+      sum += sw[k];
+    }
+  }
+  uint64_t incl = team_incl_scan(tm, sum);
+  uint64_t excl = incl - sum;
+  unsigned own = team_ballot(tm, sum > 0 && excl <= v && v < incl);
+  if (own == 0) return LPG_NONE;
+  int ol = __ffs(own) - 1;
+  int sb = -1;
+  uint64_t vl = v - excl;
+  if (tm.l == ol) {
+#pragma unroll
+    for (int k = 0; k < LPG_NSUB; ++k) {
+      if (sb < 0 && k < per) {
+        if (sw[k] > vl) sb = tm.l * per + k;
+        else vl -= sw[k];
+      }
+    }
+  }
+  sb = __shfl_sync(tm.mask, sb, ol, T);
+  vl = __shfl_sync(tm.mask, vl, ol, T);
+  if (sb < 0) return LPG_NONE;
+  /* slots: lane l holds L = 128 / T consecutive slots */
+  const int L = LPG_SUB / T;
+  const int64_t s0 = cid * LPG_CHUNK + (int64_t)sb * LPG_SUB + (int64_t)tm.l * L;
+  uint32_t dw[8];
+  float4 rv[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (k < L / 4) {
+      dw[k] = __ldcg(reinterpret_cast<const uint32_t*>(W.ds + s0) + k);
+      rv[k] = reinterpret_cast<const float4*>(W.risk + s0)[k];
+    } else {
+      dw[k] = 0xffffffffu;
+      rv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  uint64_t wsum = 0;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    if (k < L && ((dw[k >> 2] >> (8 * (k & 3))) & 0xffu) == 0)
+      wsum += fix_risk(reinterpret_cast<const float*>(rv)[k]);
+  }
+  incl = team_incl_scan(tm, wsum);
+  excl = incl - wsum;
+  own = team_ballot(tm, wsum > 0 && excl <= vl && vl < incl);
+  if (own == 0) return LPG_NONE;
+  ol = __ffs(own) - 1;
+  uint32_t hit = LPG_NONE;
+  if (tm.l == ol) {
+    uint64_t r = vl - excl;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      if (hit == LPG_NONE && k < L && ((dw[k >> 2] >> (8 * (k & 3))) & 0xffu) == 0) {
+        const uint64_t w = fix_risk(reinterpret_cast<const float*>(rv)[k]);
+        if (w > r) hit = (uint32_t)(s0 + k);
+        else r -= w;
+      }
+    }
+  }
+  return __shfl_sync(tm.mask, hit, ol, T);
+}
+
+/* Per-node record of one selection step, written once per tick so that a
+ * target needs one load to find everything about its node. */
+struct SelInfo {
+  uint64_t seed;
+  uint64_t T;        /* remaining susceptible weight */
+  double cum[LPG_MAX_STRAINS]; /* cumulative relative FOI (model.py:1127-1135) */
+  int32_t a;         /* first entry of the node's chunk list in the concatenated lists */
+  int32_t n;         /* its chunks */
+  int32_t i;         /* node index in its simulation */
+  int32_t t;         /* tick */
+  int32_t ns;
+  int32_t pad;
+};
+
+#define LPG_SEL_OFFS 2048 /* target offsets kept in shared memory when G < this */
+
+/* Cumulative relative FOI that the strain draw compares against
+ * (model.py:1127-1135), formed with the same operations in the same order. */
+__device__ __forceinline__ void sel_strain_cum(const DevWorld& W, const DevRep* rp, int g, double* cum) {
+  double p[LPG_MAX_STRAINS];
+  double totalp = 0.0;
+  for (int k = 0; k < rp->ns; ++k) {
+    p[k] = W.prob[(int64_t)k * W.G + g];
+    totalp = totalp + p[k];
+  }
+  double c = 0.0;
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+    if (k < rp->ns) c = c + p[k] / totalp;
+    cum[k] = c;
+  }
+}
+
+/* The first target to claim an agent (state 0 -> 1) exposes it: strain by
+ * relative FOI (model.py:1127-1145) and every susceptible total. */
+__device__ __forceinline__ void claim(DevWorld& W, uint32_t hit, int g, const SelInfo& N) {
   const int64_t pos = hit;
   uint32_t* wp = reinterpret_cast<uint32_t*>(W.ds + (pos & ~3LL));
   const int sh = (int)(pos & 3) * 8;
@@ -1482,16 +1654,13 @@ __device__ __forceinline__ void claim(DevWorld& W, uint32_t hit) {
   if (!won) return;
   const int G = W.G;
   const int64_t cid = pos / LPG_CHUNK;
-  const int g = W.cmeta[cid].x;
-  const DevRep* rp = &W.reps[W.node_rep[g]];
-  double p[LPG_MAX_STRAINS];
-  double totalp = 0.0;
-  for (int k = 0; k < rp->ns; ++k) {
-    p[k] = W.prob[(int64_t)k * G + g];
-    totalp = totalp + p[k];
-  }
-  const double r = lpg_u01(rp->seed, LPG_P_STRAIN, rp->cur_t, W.ref[pos], 0, 0);
-  const int s = pick_strain(p, rp->ns, totalp, r);
+  const double r = lpg_u01(N.seed, LPG_P_STRAIN, N.t, W.ref[pos], 0, 0);
+  int s = 0;
+  for (int k = 0; k < N.ns; ++k)
+    if (r < N.cum[k]) {
+      s = k;
+      break;
+    }
   W.strain[pos] = (int8_t)s;
   const uint64_t w = fix_risk(W.risk[pos]);
   atomicAdd(&W.tot[(int64_t)TT_S * G + g], -1);
@@ -1505,141 +1674,240 @@ __device__ __forceinline__ void claim(DevWorld& W, uint32_t hit) {
   }
 }
 
+/* Node of target q: the last g with off[g] <= q. */
+__device__ __forceinline__ int sel_node_of(const int64_t* off, int G, int64_t q) {
+  int lo = 0, hi = G;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] > q) hi = mid; else lo = mid + 1;
+  }
+  return lo - 1;
+}
+
 /* Weighted selection without replacement (tx_infect_nb, model.py:1066-1147).
- * Round 0 runs over all nodes at once (three grid barriers); the few
- * collisions left after it are redrawn per node by one CTA in later rounds,
- * with CTA barriers only.  Round r of node n draws the (n, r, j) uniforms
- * of the oracle, so the CDF targets are the same whatever runs them. */
+ * Round 0 runs over all nodes at once (four grid barriers): demand and the
+ * per-node record, the prefix of chunk weights over every chunk list, target
+ * offsets (kept in shared memory by every CTA), then every target is
+ * located and then claimed, targets going round-robin over the CTAs.  The
+ * few collisions left after round 0 are redrawn per node by one CTA in later
+ * rounds, with CTA barriers only.  Round r of node n draws the (n, r, j)
+ * uniforms of the oracle, so the CDF targets are the same whatever runs
+ * them. */
 __global__ void __launch_bounds__(256) k_select(DevWorld W) {
   const int R = W.n_reps, G = W.G;
   int any = 0;
   for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
   if (!any) return;
-  const int lane = threadIdx.x & 31;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
-  const int64_t gwarp = gtid >> 5, nwarps = gsz >> 5;
+  SelInfo* info = reinterpret_cast<SelInfo*>(W.sel_info);
   __shared__ int64_t s_K;
+  __shared__ int64_t s_off[LPG_SEL_OFFS];
+  const bool offs_in_smem = G < LPG_SEL_OFFS;
 
   /* ---- round 0, all nodes ---- */
-  for (int64_t g = gwarp; g < G; g += nwarps) {
+  for (int64_t g = gtid; g < G; g += gsz) {
     const DevRep* rp = &W.reps[W.node_rep[g]];
     int64_t k = 0;
+    const uint64_t T = W.sw[g];
     if (rp->active && (rp->comps & LPG_COMP_TX)) {
       k = W.size[g] - W.uniq[g];
       if (k < 0) k = 0;
-      if (W.sw[g] == 0) k = 0;
+      if (T == 0) k = 0;
     }
-    if (lane == 0) W.ksel[g] = k;
+    W.ksel[g] = k;
     if (k > 0) {
       const int i = (int)(g - rp->node_base);
       const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
-      const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
-      uint64_t* cp = W.cpref + rp->chunk_base;
-      uint64_t carry = 0;
-      for (int32_t a = st[i]; a < st[i + 1]; a += 32) {
-        int32_t idx = a + lane;
-        uint64_t v = idx < st[i + 1] ? __ldcg(&W.chunk_w[ls[idx]]) : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          uint64_t y = __shfl_up_sync(FULLMASK, v, o);
-          if (lane >= o) v += y;
-        }
-        if (idx < st[i + 1]) cp[idx] = carry + v;
-        carry += __shfl_sync(FULLMASK, v, 31);
-      }
+      SelInfo N;
+      N.seed = rp->seed;
+      N.T = T;
+      sel_strain_cum(W, rp, (int)g, N.cum);
+      N.a = rp->chunk_base + st[i];
+      N.n = st[i + 1] - st[i];
+      N.i = i;
+      N.t = rp->cur_t;
+      N.ns = rp->ns;
+      N.pad = 0;
+      info[g] = N;
     }
+  }
+  /* Prefix of the chunk weights over every simulation's CSR chunk lists
+   * (index x = chunk_base + list position; unlisted entries weigh 0), in two
+   * passes around a grid barrier: CTA totals, then offsets.  Node g's CDF is
+   * cp[x] - base[g], base[g] = cp[first x of the node - 1], exact in
+   * integers; the thread that holds a node's first entry writes its base. */
+  const int64_t X = W.total_chunks;
+  const int64_t xper = (X + gridDim.x - 1) / gridDim.x;
+  const int64_t x0 = min(X, (int64_t)blockIdx.x * xper), x1 = min(X, x0 + xper);
+  {
+    int64_t bsum = 0;
+    for (int64_t xb = x0; xb < x1; xb += blockDim.x) {
+      const int64_t x = xb + threadIdx.x;
+      int64_t tot;
+      (void)block_excl_scan(x < x1 ? (int64_t)csr_chunk_weight(W, x) : 0, &tot);
+      bsum += tot;
+    }
+    if (threadIdx.x == 0) W.sel_part[blockIdx.x] = (uint64_t)bsum;
   }
   if (!grid_sync(W)) return;
   {
-    /* target offsets of all nodes; every CTA computes the same values */
+    int64_t off = 0;
+    for (int j = threadIdx.x; j < (int)blockIdx.x; j += blockDim.x) off += (int64_t)__ldcg(&W.sel_part[j]);
+    int64_t tot;
+    (void)block_excl_scan(off, &tot);
+    int64_t carry = tot;
+    for (int64_t xb = x0; xb < x1; xb += blockDim.x) {
+      const int64_t x = xb + threadIdx.x;
+      int first_g = -1;
+      const int64_t w = x < x1 ? (int64_t)csr_chunk_weight(W, x, &first_g) : 0;
+      const int64_t ex = block_excl_scan(w, &tot);
+      if (x < x1) {
+        W.cpref[x] = (uint64_t)(carry + ex + w);
+        if (first_g >= 0) W.sel_base[first_g] = (uint64_t)(carry + ex);
+      }
+      carry += tot;
+    }
+  }
+  {
+    /* target offsets of all nodes; every CTA computes the same values and
+     * keeps them in shared memory when they fit */
     int64_t carry = 0;
     for (int base = 0; base < G; base += blockDim.x) {
-      int g = base + threadIdx.x;
-      int64_t k = g < G ? W.ksel[g] : 0;
+      const int g = base + threadIdx.x;
+      const int64_t k = g < G ? __ldcg(&W.ksel[g]) : 0;
       int64_t tot;
-      int64_t ex = block_excl_scan(k, &tot);
-      if (g < G) W.tgt_off[g] = carry + ex;
+      const int64_t ex = block_excl_scan(k, &tot);
+      if (g < G) {
+        W.tgt_off[g] = carry + ex;
+        if (offs_in_smem) s_off[g] = carry + ex;
+      }
       carry += tot;
     }
     if (threadIdx.x == 0) {
       W.tgt_off[G] = carry;
+      if (offs_in_smem) s_off[G] = carry;
       s_K = carry;
     }
     __syncthreads();
   }
+  if (!grid_sync(W)) return;
   const int64_t K = s_K;
   if (K > W.hits_cap) {
     if (gtid == 0) W.reps[0].error = LPG_ERR_INTERNAL;
     return;
   }
-  for (int64_t q = gtid; q < K; q += gsz) {
-    int lo = 0, hi = G;
-    while (lo < hi) { /* first g with tgt_off[g] > q */
-      int mid = (lo + hi) >> 1;
-      if (W.tgt_off[mid] > q) hi = mid; else lo = mid + 1;
+  const int64_t* offs = offs_in_smem ? s_off : W.tgt_off;
+  /* Targets go round-robin over the CTAs (target q on CTA q mod grid), so
+   * that a few thousand of them still use every SM, each located by a team
+   * of T lanes: the largest power of two <= 32 with T * K <= threads. */
+  {
+    int T = 1;
+    while (T < 32 && (int64_t)(2 * T) * K <= gsz) T *= 2;
+    const Team tm = make_team(T);
+    const int64_t nteams = gsz / T;
+    for (int64_t q = (int64_t)(threadIdx.x / T) * gridDim.x + blockIdx.x; q < K; q += nteams) {
+      const int g = sel_node_of(offs, G, q);
+      const SelInfo N = info[g];
+      const uint64_t base = __ldcg(&W.sel_base[g]);
+      const int64_t j = q - offs[g];
+      const uint64_t v = lpg_scale_target(lpg_u53(N.seed, LPG_P_SELECT, N.t, (uint64_t)N.i, 0, (uint64_t)j), N.T);
+      const int32_t* ls = W.node_chunks[W.reps[W.node_rep[g]].csr_cur] + N.a;
+      const uint32_t hit = locate_team(W, tm, ls, W.cpref + N.a, N.n, v, base);
+      if (tm.l == 0) {
+        if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
+        W.hits[q] = hit;
+      }
     }
-    const int g = lo - 1;
-    const DevRep* rp = &W.reps[W.node_rep[g]];
-    const int i = g - rp->node_base;
-    const int64_t j = q - W.tgt_off[g];
-    const uint64_t v = lpg_scale_target(lpg_u53(rp->seed, LPG_P_SELECT, rp->cur_t, (uint64_t)i, 0, (uint64_t)j), W.sw[g]);
-    const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
-    const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
-    const uint32_t hit = locate(W, ls, W.cpref + rp->chunk_base, st[i], st[i + 1], v);
-    if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
-    W.hits[q] = hit;
   }
+  const int64_t q0 = (int64_t)threadIdx.x * gridDim.x + blockIdx.x;
   if (!grid_sync(W)) return;
-  for (int64_t q = gtid; q < K; q += gsz) {
+  for (int64_t q = q0; q < K; q += gsz) {
     const uint32_t hit = W.hits[q];
-    if (hit != LPG_NONE) claim(W, hit);
+    if (hit == LPG_NONE) continue;
+    const int g = sel_node_of(offs, G, q);
+    claim(W, hit, g, info[g]);
   }
   if (!grid_sync(W)) return;
 
   /* ---- later rounds: one CTA per node that still needs agents ---- */
   __shared__ int64_t s_k;
   __shared__ uint64_t s_T;
+  __shared__ SelInfo s_N;
+  uint64_t* s_cp = reinterpret_cast<uint64_t*>(s_off); /* the offsets are no longer needed */
   for (int g = blockIdx.x; g < G; g += gridDim.x) {
     const DevRep* rp = &W.reps[W.node_rep[g]];
     if (!rp->active || !(rp->comps & LPG_COMP_TX)) continue;
     const int i = g - rp->node_base;
     const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
-    const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
-    uint64_t* cp = W.cpref + rp->chunk_base;
+    const int32_t a = st[i], n = st[i + 1] - st[i];
+    const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base + a;
+    uint64_t* cp = W.cpref + rp->chunk_base + a;
+    const bool local = n <= LPG_SEL_OFFS;
     /* this node's region of the target buffer: its own positions */
-    uint32_t* hits = W.hits + (int64_t)(rp->chunk_base + st[i]) * LPG_CHUNK;
+    uint32_t* hits = W.hits + (int64_t)(rp->chunk_base + a) * LPG_CHUNK;
     for (int round = 1; round < LPG_MAX_ROUNDS; ++round) {
       if (threadIdx.x == 0) {
         const int64_t k = __ldcg(&W.size[g]) - (int64_t)__ldcg((const unsigned long long*)&W.uniq[g]);
         s_T = __ldcg(&W.sw[g]);
         s_k = (k > 0 && s_T > 0) ? k : 0;
+        if (s_k > 0) {
+          s_N.seed = rp->seed;
+          s_N.t = rp->cur_t;
+          s_N.ns = rp->ns;
+          sel_strain_cum(W, rp, g, s_N.cum);
+        }
       }
       __syncthreads();
       const int64_t k = s_k;
       const uint64_t T = s_T;
       if (k == 0) break;
-      /* chunk prefix of the node (CTA scan) */
+      /* chunk prefix of the node (CTA scan; every weight requested at once),
+       * in shared memory when it fits */
+      uint64_t wv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int32_t idx = u * blockDim.x + threadIdx.x;
+        wv[u] = idx < n ? __ldcg(&W.chunk_w[ls[idx]]) : 0;
+      }
       uint64_t carry = 0;
-      for (int32_t a = st[i]; a < st[i + 1]; a += blockDim.x) {
-        const int32_t idx = a + threadIdx.x;
-        const int64_t v = idx < st[i + 1] ? (int64_t)__ldcg(&W.chunk_w[ls[idx]]) : 0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (u * (int)blockDim.x >= n) break;
+        const int32_t idx = u * blockDim.x + threadIdx.x;
+        const int64_t v = (int64_t)wv[u];
         int64_t tot;
         const int64_t ex = block_excl_scan(v, &tot);
-        if (idx < st[i + 1]) cp[idx] = carry + (uint64_t)ex + (uint64_t)v;
+        if (idx < n) {
+          if (local) s_cp[idx] = carry + (uint64_t)ex + (uint64_t)v;
+          else cp[idx] = carry + (uint64_t)ex + (uint64_t)v;
+        }
+        carry += (uint64_t)tot;
+      }
+      for (int32_t a0 = 8 * blockDim.x; a0 < n; a0 += blockDim.x) {
+        const int32_t idx = a0 + threadIdx.x;
+        const int64_t v = idx < n ? (int64_t)__ldcg(&W.chunk_w[ls[idx]]) : 0;
+        int64_t tot;
+        const int64_t ex = block_excl_scan(v, &tot);
+        if (idx < n) cp[idx] = carry + (uint64_t)ex + (uint64_t)v;
         carry += (uint64_t)tot;
       }
       __syncthreads();
-      for (int64_t j = threadIdx.x; j < k; j += blockDim.x) {
+      int TT = 1;
+      while (TT < 32 && (int64_t)(2 * TT) * k <= (int64_t)blockDim.x) TT *= 2;
+      const Team tm = make_team(TT);
+      for (int64_t j = threadIdx.x / TT; j < k; j += blockDim.x / TT) {
         const uint64_t v = lpg_scale_target(lpg_u53(rp->seed, LPG_P_SELECT, rp->cur_t, (uint64_t)i, (uint64_t)round, (uint64_t)j), T);
-        const uint32_t hit = locate(W, ls, cp, st[i], st[i + 1], v);
-        if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
-        hits[j] = hit;
+        const uint32_t hit = locate_team(W, tm, ls, local ? s_cp : cp, n, v, 0);
+        if (tm.l == 0) {
+          if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
+          hits[j] = hit;
+        }
       }
       __syncthreads();
       for (int64_t j = threadIdx.x; j < k; j += blockDim.x) {
         const uint32_t hit = hits[j];
-        if (hit != LPG_NONE) claim(W, hit);
+        if (hit != LPG_NONE) claim(W, hit, g, s_N);
       }
       __threadfence_block();
       __syncthreads();

@@ -839,6 +839,14 @@ double lpo_exp(double x) { return lpg_exp(x); }
 double lpo_expm1(double x) { return lpg_expm1(x); }
 double lpo_mlog(double x) { return lpg_log(x); }
 double lpo_lfact(int64_t k) { return lpg_lfact(k); }
+/* fixed-point weights: the double-precision definition and the integer form
+ * the CUDA engine uses, for many inputs at once (test export) */
+void lpo_fix_risk_many(const float* r, int64_t n, uint64_t* by_double, uint64_t* by_bits) {
+  for (int64_t i = 0; i < n; ++i) {
+    by_double[i] = fix_risk(r[i]);
+    by_bits[i] = lpg_fix_risk_bits(r[i]);
+  }
+}
 void lpo_poisson_many(uint64_t seed, double lam, int64_t n, int64_t* out) {
   for (int64_t i = 0; i < n; ++i) {
     lpg_stream st;

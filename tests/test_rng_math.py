@@ -76,3 +76,20 @@ def test_km_newborn_lifespans_follow_table():
     freq = np.bincount(years, minlength=5) / len(years)
     want = np.diff(np.concatenate([[0], cum])) / cum[-1]
     assert np.allclose(freq, want, atol=0.02)
+
+
+def test_fix_risk_integer_form_equals_double_definition():
+    from oracle.oracle import fix_risk_many
+
+    rng = np.random.default_rng(3)
+    bits = rng.integers(0, 2**32, 2_000_000, dtype=np.uint64).astype(np.uint32)
+    r = bits.view(np.float32)
+    special = np.array([0.0, -0.0, 1.0, 0.5, 1.5, 2.5, 2**-24, 1.5 * 2**-24, 2**-25, 3 * 2**-25, 2**-126,
+                        np.inf, -np.inf, np.nan, 2.0**38, 2.0**39, 3.4e38, 1e-45, 0.999999940395,
+                        1.00000011920929], dtype=np.float32)
+    # every float whose product with 2^24 lies near a half-integer
+    m = np.arange(1, 1 << 12, dtype=np.float64)
+    halves = ((m + 0.5) / 2.0**24).astype(np.float32)
+    r = np.concatenate([r, special, halves, np.nextafter(halves, np.float32(1)), np.nextafter(halves, np.float32(0))])
+    a, b = fix_risk_many(r)
+    np.testing.assert_array_equal(a, b)
