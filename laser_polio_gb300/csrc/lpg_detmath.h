@@ -17,6 +17,9 @@
  *          (high part with 33 significant bits so k*hi is exact), then the
  *          Taylor series of e^r to degree 14 (|r| <= ln2/2, truncation error
  *          below 1e-18 relative), then exact scaling by 2^k.
+ *   Every polynomial is evaluated by Estrin's scheme (short dependency
+ *   chains: double-precision latency, not throughput, bounds the
+ *   single-thread draws on the GPU).
  *   expm1  the same Taylor series without its constant term when
  *          |x| < ln2/2 (full relative precision for tiny rates), else exp-1.
  *   log    x = m 2^e with m in [sqrt(1/2), sqrt(2)), log m = 2 atanh(s),
@@ -79,46 +82,64 @@ LPG_HD double lpg_scale2(double p, int k) {
   return p * lpg_pow2i(k);
 }
 
-/* Horner evaluation of sum_{n=0}^{14} r^n / n! (coefficients are the
- * correctly rounded reciprocals of the exact double factorials). */
-LPG_HD double lpg_exp_series(double r) {
-  double p = 1.0 / 87178291200.0;            /* 1/14! */
-  p = p * r + 1.0 / 6227020800.0;            /* 1/13! */
-  p = p * r + 1.0 / 479001600.0;             /* 1/12! */
-  p = p * r + 1.0 / 39916800.0;              /* 1/11! */
-  p = p * r + 1.0 / 3628800.0;               /* 1/10! */
-  p = p * r + 1.0 / 362880.0;                /* 1/9!  */
-  p = p * r + 1.0 / 40320.0;                 /* 1/8!  */
-  p = p * r + 1.0 / 5040.0;                  /* 1/7!  */
-  p = p * r + 1.0 / 720.0;                   /* 1/6!  */
-  p = p * r + 1.0 / 120.0;                   /* 1/5!  */
-  p = p * r + 1.0 / 24.0;                    /* 1/4!  */
-  p = p * r + 1.0 / 6.0;                     /* 1/3!  */
-  p = p * r + 0.5;                           /* 1/2!  */
-  p = p * r + 1.0;                           /* 1/1!  */
-  p = p * r + 1.0;                           /* 1/0!  */
-  return p;
+/* Polynomials by Estrin's scheme (pairs, then powers r^2, r^4, r^8): the
+ * same polynomial as Horner's rule with a dependency depth of about 8
+ * operations instead of 2 per coefficient, which matters on a GPU whose
+ * double-precision operations have a long latency.  Coefficients are the
+ * correctly rounded reciprocals of the exact double factorials.  The series
+ * are arranged as r + r^2 P(r) so that the dominant term r is exact and the
+ * rounding of P is scaled down by r. */
+
+/* P(r) = sum_{n=0}^{14} r^n / (n+2)! */
+LPG_HD double lpg_em1_tail16(double r, double r2, double r4, double r8) {
+  const double q0 = 0.5 + (1.0 / 6.0) * r;
+  const double q1 = (1.0 / 24.0) + (1.0 / 120.0) * r;
+  const double q2 = (1.0 / 720.0) + (1.0 / 5040.0) * r;
+  const double q3 = (1.0 / 40320.0) + (1.0 / 362880.0) * r;
+  const double q4 = (1.0 / 3628800.0) + (1.0 / 39916800.0) * r;
+  const double q5 = (1.0 / 479001600.0) + (1.0 / 6227020800.0) * r;
+  const double q6 = (1.0 / 87178291200.0) + (1.0 / 1307674368000.0) * r;
+  const double q7 = 1.0 / 20922789888000.0;
+  const double s0 = q0 + q1 * r2;
+  const double s1 = q2 + q3 * r2;
+  const double s2 = q4 + q5 * r2;
+  const double s3 = q6 + q7 * r2;
+  const double t0 = s0 + s1 * r4;
+  const double t1 = s2 + s3 * r4;
+  return t0 + t1 * r8;
 }
 
-/* sum_{n=1}^{16} r^n / n! — the series of e^r - 1 without its constant. */
+/* P(r) = sum_{n=0}^{12} r^n / (n+2)! */
+LPG_HD double lpg_em1_tail14(double r, double r2, double r4, double r8) {
+  const double q0 = 0.5 + (1.0 / 6.0) * r;
+  const double q1 = (1.0 / 24.0) + (1.0 / 120.0) * r;
+  const double q2 = (1.0 / 720.0) + (1.0 / 5040.0) * r;
+  const double q3 = (1.0 / 40320.0) + (1.0 / 362880.0) * r;
+  const double q4 = (1.0 / 3628800.0) + (1.0 / 39916800.0) * r;
+  const double q5 = (1.0 / 479001600.0) + (1.0 / 6227020800.0) * r;
+  const double q6 = 1.0 / 87178291200.0;
+  const double s0 = q0 + q1 * r2;
+  const double s1 = q2 + q3 * r2;
+  const double s2 = q4 + q5 * r2;
+  const double t0 = s0 + s1 * r4;
+  const double t1 = s2 + q6 * r4;
+  return t0 + t1 * r8;
+}
+
+/* sum_{n=0}^{14} r^n / n! = 1 + (r + r^2 P(r)). */
+LPG_HD double lpg_exp_series(double r) {
+  const double r2 = r * r;
+  const double r4 = r2 * r2;
+  const double r8 = r4 * r4;
+  return 1.0 + (r + r2 * lpg_em1_tail14(r, r2, r4, r8));
+}
+
+/* sum_{n=1}^{16} r^n / n! = r + r^2 P(r) — e^r - 1 without its constant. */
 LPG_HD double lpg_expm1_series(double r) {
-  double p = 1.0 / 20922789888000.0;         /* 1/16! */
-  p = p * r + 1.0 / 1307674368000.0;         /* 1/15! */
-  p = p * r + 1.0 / 87178291200.0;
-  p = p * r + 1.0 / 6227020800.0;
-  p = p * r + 1.0 / 479001600.0;
-  p = p * r + 1.0 / 39916800.0;
-  p = p * r + 1.0 / 3628800.0;
-  p = p * r + 1.0 / 362880.0;
-  p = p * r + 1.0 / 40320.0;
-  p = p * r + 1.0 / 5040.0;
-  p = p * r + 1.0 / 720.0;
-  p = p * r + 1.0 / 120.0;
-  p = p * r + 1.0 / 24.0;
-  p = p * r + 1.0 / 6.0;
-  p = p * r + 0.5;
-  p = p * r + 1.0;
-  return p * r;
+  const double r2 = r * r;
+  const double r4 = r2 * r2;
+  const double r8 = r4 * r4;
+  return r + r2 * lpg_em1_tail16(r, r2, r4, r8);
 }
 
 LPG_HD double lpg_exp(double x) {
@@ -148,21 +169,25 @@ LPG_HD double lpg_log(double x) {
   double m = lpg_bitsd((b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL); /* [1,2) */
   if (m > LPG_SQRT2) { m = m * 0.5; e += 1; }
   double s = (m - 1.0) / (m + 1.0);
-  double s2 = s * s;
-  double q = 1.0 / 25.0;
-  q = q * s2 + 1.0 / 23.0;
-  q = q * s2 + 1.0 / 21.0;
-  q = q * s2 + 1.0 / 19.0;
-  q = q * s2 + 1.0 / 17.0;
-  q = q * s2 + 1.0 / 15.0;
-  q = q * s2 + 1.0 / 13.0;
-  q = q * s2 + 1.0 / 11.0;
-  q = q * s2 + 1.0 / 9.0;
-  q = q * s2 + 1.0 / 7.0;
-  q = q * s2 + 1.0 / 5.0;
-  q = q * s2 + 1.0 / 3.0;
-  q = q * s2 + 1.0;
-  double lm = 2.0 * s * q;
+  /* log m = 2s + 2s z Q(z), z = s^2, Q = sum_{n=0}^{11} z^n / (2n+3) by
+   * Estrin's scheme; the leading 2s is exact */
+  const double z = s * s;
+  const double z2 = z * z;
+  const double z4 = z2 * z2;
+  const double z8 = z4 * z4;
+  const double p0 = (1.0 / 3.0) + (1.0 / 5.0) * z;
+  const double p1 = (1.0 / 7.0) + (1.0 / 9.0) * z;
+  const double p2 = (1.0 / 11.0) + (1.0 / 13.0) * z;
+  const double p3 = (1.0 / 15.0) + (1.0 / 17.0) * z;
+  const double p4 = (1.0 / 19.0) + (1.0 / 21.0) * z;
+  const double p5 = (1.0 / 23.0) + (1.0 / 25.0) * z;
+  const double u0 = p0 + p1 * z2;
+  const double u1 = p2 + p3 * z2;
+  const double u2 = p4 + p5 * z2;
+  const double v0 = u0 + u1 * z4;
+  const double q = v0 + u2 * z8;
+  const double s2x = 2.0 * s;
+  double lm = s2x + (s2x * z) * q;
   double ed = (double)e;
   return ed * LPG_LN2_HI + (ed * LPG_LN2_LO + lm);
 }

@@ -494,7 +494,6 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.chunk_w, chunk_total);
   rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.cpref, chunk_total);
-  rc |= dalloc(h, &W.sel_part, 1024);
   rc |= dalloc(h, &W.node_chunks[0], chunk_total);
   rc |= dalloc(h, &W.node_chunks[1], chunk_total);
   rc |= dalloc(h, &W.node_chunk_start[0], csr_total);
@@ -517,7 +516,6 @@ extern "C" int lpg_start(lpg_handle* h) {
     rc |= dalloc(h, &si, (size_t)G * sizeof(SelInfo));
     W.sel_info = si;
   }
-  rc |= dalloc(h, &W.sel_base, G);
   /* selection targets (at most the susceptibles) and the E/I queue slabs
    * (at most one entry per position) share this buffer */
   int64_t hits = (int64_t)chunk_total * LPG_CHUNK;
@@ -816,7 +814,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
     case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
     case 6: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
-    case 7: k_node_tx<<<G, 256, 0, st>>>(W); break;
+    case 7: k_node_tx<<<G, LPG_NODE_TX_THREADS, 0, st>>>(W); break;
     case 8: {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(h->select_blocks);

@@ -166,8 +166,7 @@ typedef struct {
   int4* cmeta; /* per chunk: x node, y fill, z tick of the newborns written into it, w offset of the first */
   uint64_t* chunk_w;  /* susceptible weight total */
   uint64_t* sub_w;    /* [chunk][LPG_NSUB] */
-  uint64_t* cpref;    /* selection: prefix of chunk weights in CSR order */
-  uint64_t* sel_part; /* [1024] per-CTA totals of that prefix (round 0) */
+  uint64_t* cpref;    /* selection: node-local prefix of chunk weights, CSR order */
   int32_t* node_chunks[2];
   int32_t* node_chunk_start[2]; /* per sim: n_nodes + 1 entries at csr_base */
   /* per global node */
@@ -185,7 +184,6 @@ typedef struct {
   int64_t* ksel;
   int64_t* tgt_off; /* [G + 1] */
   void* sel_info;     /* [G] SelInfo: per-node selection record of the tick */
-  uint64_t* sel_base; /* [G] cpref before the node's first chunk-list entry */
   uint32_t* hits; /* selection targets */
   int64_t hits_cap;
   uint64_t* evq;     /* event queues of the sweeps: one slab per sweep CTA */

@@ -1253,23 +1253,85 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* Node-level force of infection and exposure counts; same arithmetic, in
- * the same order, as the oracle's lpo_node_tx.  One warp per node: lane l
- * accumulates the incoming infectivity of source nodes l, l+32, ... from the
- * transposed network row (contiguous), then lane 0 adds the 32 partial sums
- * in lane order. */
+/* Per-node record of one selection step, written once per tick so that a
+ * target needs one load to find everything about its node. */
+#define LPG_SEL_OFFS 2048 /* target offsets kept in shared memory when G < this */
+#define LPG_NODE_TX_THREADS 64
+
+struct SelInfo {
+  uint64_t seed;
+  uint64_t T;        /* remaining susceptible weight */
+  double cum[LPG_MAX_STRAINS]; /* cumulative relative FOI (model.py:1127-1135) */
+  int32_t a;         /* first entry of the node's chunk list in the concatenated lists */
+  int32_t n;         /* its chunks */
+  int32_t i;         /* node index in its simulation */
+  int32_t t;         /* tick */
+  int32_t ns;
+  int32_t pad;
+};
+
+/* Cumulative relative FOI that the strain draw compares against
+ * (model.py:1127-1135), formed with the same operations in the same order. */
+__device__ __forceinline__ void sel_strain_cum(const DevWorld& W, const DevRep* rp, int g, double* cum) {
+  double p[LPG_MAX_STRAINS], q[LPG_MAX_STRAINS];
+  double totalp = 0.0;
+  const int ns = rp->ns;
+#pragma unroll
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+    p[k] = k < ns ? W.prob[(int64_t)k * W.G + g] : 0.0;
+    if (k < ns) totalp = totalp + p[k];
+  }
+#pragma unroll
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k) q[k] = p[k] / totalp; /* independent divisions */
+  double c = 0.0;
+#pragma unroll
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+    if (k < ns) c = c + q[k];
+    cum[k] = c;
+  }
+}
+
+/* Node-local inclusive prefix of the chunk weights of a chunk list (n
+ * entries) into cp, by one warp (8 weights per lane requested at once). */
+__device__ __forceinline__ void warp_chunk_prefix(const DevWorld& W, const int32_t* ls, int32_t n, uint64_t* cp) {
+  const int lane = threadIdx.x & 31;
+  uint64_t carry = 0;
+  for (int32_t a0 = 0; a0 < n; a0 += 32 * 8) {
+    uint64_t wv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int32_t idx = a0 + u * 32 + lane;
+      wv[u] = idx < n ? __ldcg(&W.chunk_w[ls[idx]]) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      if (a0 + u * 32 >= n) break;
+      uint64_t x = wv[u];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(FULLMASK, x, o);
+        if (lane >= o) x += y;
+      }
+      const int32_t idx = a0 + u * 32 + lane;
+      if (idx < n) cp[idx] = carry + x;
+      carry += __shfl_sync(FULLMASK, x, 31);
+    }
+  }
+}
+
 /* Node-level force of infection and exposure counts (model.py:1327-1407);
  * the same arithmetic, in the same order, as the oracle's lpo_node_tx.
  * One CTA per node.  Incoming infectivity sum_i B_i N[i][n] is exact
  * integer arithmetic: B in units of 2^-32 times the network weight in units
  * of 2^-62 (transposed row, contiguous), 128-bit sums, one conversion; an
  * exact sum does not depend on how the threads split it. */
-__global__ void __launch_bounds__(256) k_node_tx(DevWorld W) {
+__global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
   const int g = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __shared__ uint64_t s_lo[8][LPG_MAX_STRAINS], s_hi[8][LPG_MAX_STRAINS];
+  __shared__ uint64_t s_lo[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS], s_hi[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS];
   if (g >= W.G) return;
   DevRep* rp = &W.reps[W.node_rep[g]];
+  if (threadIdx.x == 0) W.ksel[g] = 0;
   if (!rp->active) return;
   const int i = g - rp->node_base, n = rp->n_nodes, ns = rp->ns, t = rp->cur_t, G = W.G;
   const int nb = rp->node_base;
@@ -1287,14 +1349,41 @@ __global__ void __launch_bounds__(256) k_node_tx(DevWorld W) {
     W.uniq[g] = 0;
   }
   if (!(rp->comps & LPG_COMP_TX)) return;
+  /* inputs of lane 0's draw, requested now so that they arrive during the
+   * mixing */
+  double pre_seas = 0.0, pre_r0s = 0.0, pre_rowsum = 0.0;
+  uint64_t pre_bb = 0;
+  uint64_t pre_sw = 0;
+  int64_t pre_sc = 0;
+  /* lane k < ns of the first warp works on strain k after the mixing */
+  if (threadIdx.x < ns) {
+    pre_seas = rp->seas[t];
+    pre_r0s = rp->r0s[i];
+    pre_rowsum = rp->rowsum[i];
+    pre_bb = W.bb[(int64_t)threadIdx.x * G + g];
+  }
+  if (threadIdx.x == 0) {
+    pre_sw = W.sw[g];
+    pre_sc = W.tot[(int64_t)TT_S * G + g];
+  }
   const uint64_t* qrow = rp->netq_t + (int64_t)i * n; /* qrow[ii] = network[ii][i] in 2^-62 */
   unsigned __int128 part[LPG_MAX_STRAINS] = {0, 0, 0, 0};
-  for (int ii = threadIdx.x; ii < n; ii += blockDim.x) {
-    const uint64_t w = qrow[ii];
-    if (!w) continue;
+  /* batches of 4 source nodes per thread, every load of a batch issued
+   * before any multiply */
+  for (int ii0 = threadIdx.x; ii0 < n; ii0 += 4 * blockDim.x) {
+    uint64_t w[4], b[4][LPG_MAX_STRAINS];
 #pragma unroll
-    for (int k = 0; k < LPG_MAX_STRAINS; ++k)
-      if (k < ns) part[k] += (unsigned __int128)W.bb[(int64_t)k * G + nb + ii] * w;
+    for (int u = 0; u < 4; ++u) {
+      const int ii = ii0 + u * blockDim.x;
+      w[u] = ii < n ? qrow[ii] : 0;
+#pragma unroll
+      for (int k = 0; k < LPG_MAX_STRAINS; ++k) b[u][k] = (ii < n && k < ns) ? W.bb[(int64_t)k * G + nb + ii] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int k = 0; k < LPG_MAX_STRAINS; ++k)
+        if (k < ns) part[k] += (unsigned __int128)b[u][k] * w[u];
   }
 #pragma unroll
   for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
@@ -1313,36 +1402,62 @@ __global__ void __launch_bounds__(256) k_node_tx(DevWorld W) {
     }
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  double inc[LPG_MAX_STRAINS];
-  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+  if (wid == 1) {
+    /* the second warp: the node's chunk prefix for the selection that
+     * follows (node-local, exact in integers), while lane 0 of the first
+     * draws the exposure count */
+    const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+    const int32_t a = st[i], nch = st[i + 1] - st[i];
+    warp_chunk_prefix(W, W.node_chunks[rp->csr_cur] + rp->chunk_base + a, nch, W.cpref + rp->chunk_base + a);
+    return;
+  }
+  if (wid != 0) return;
+  /* Strain k on lane k (a double-precision warp instruction costs the same
+   * for one lane or 32): incoming infectivity, beta, rate, probability
+   * (model.py:1327-1363); then the sums over strains in strain order, as
+   * the oracle forms them. */
+  double pk = 0.0;
+  const double denom = (double)(pop_t > 1 ? pop_t : 1);
+  if (lane < ns) {
     uint64_t lo = 0, hi = 0;
-    for (int w8 = 0; w8 < (int)(blockDim.x >> 5); ++w8) {
-      const uint64_t nlo = lo + s_lo[w8][k];
-      hi = hi + s_hi[w8][k] + (nlo < lo ? 1 : 0);
+#pragma unroll
+    for (int w8 = 0; w8 < LPG_NODE_TX_THREADS / 32; ++w8) {
+      const uint64_t nlo = lo + s_lo[w8][lane];
+      hi = hi + s_hi[w8][lane] + (nlo < lo ? 1 : 0);
       lo = nlo;
     }
-    inc[k] = ((double)hi * 0x1.0p64 + (double)lo) * 0x1.0p-94;
-  }
-  double p[LPG_MAX_STRAINS];
-  double total_p = 0.0;
-  int local_zero = 1;
-  const double rowsum = rp->rowsum[i];
-  for (int k = 0; k < ns; ++k) {
-    const uint64_t bk = W.bb[(int64_t)k * G + g];
-    if (bk != 0) local_zero = 0;
-    const double bpre = (double)bk * 0x1.0p-32;
-    double beta = bpre + (inc[k] - bpre * rowsum);
-    beta = (beta * rp->seas[t]) * rp->r0s[i];
-    double denom = (double)(pop_t > 1 ? pop_t : 1);
-    double rate = beta / denom;
-    double pk = -lpg_expm1(-rate);
+    const double inck = ((double)hi * 0x1.0p64 + (double)lo) * 0x1.0p-94;
+    const double bpre = (double)pre_bb * 0x1.0p-32;
+    double beta = bpre + (inck - bpre * pre_rowsum);
+    beta = (beta * pre_seas) * pre_r0s;
+    const double rate = beta / denom;
+    pk = -lpg_expm1(-rate);
     if (!(pk > 0.0)) pk = 0.0;
-    p[k] = pk;
-    total_p = total_p + pk;
+    W.prob[(int64_t)lane * G + g] = pk;
   }
-  for (int k = 0; k < ns; ++k) W.prob[(int64_t)k * G + g] = p[k];
-  const double srisk = (double)W.sw[g] * 0x1.0p-24;
+  const int local_zero = __ballot_sync(FULLMASK, lane < ns && pre_bb != 0) == 0;
+  double p[LPG_MAX_STRAINS];
+#pragma unroll
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k) p[k] = __shfl_sync(FULLMASK, pk, k);
+  double total_p = 0.0;
+#pragma unroll
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k)
+    if (k < ns) total_p = total_p + p[k];
+  /* strain thresholds of the selection (sel_strain_cum's values), the
+   * divisions on their own lanes */
+  const double qk = pk / total_p;
+  double cum[LPG_MAX_STRAINS];
+  {
+    double c = 0.0;
+#pragma unroll
+    for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+      const double q = __shfl_sync(FULLMASK, qk, k);
+      if (k < ns) c = c + q;
+      cum[k] = c;
+    }
+  }
+  if (lane != 0) return;
+  const double srisk = (double)pre_sw * 0x1.0p-24;
   const double exposure = srisk * total_p;
   int64_t total = 0;
   lpg_stream sm;
@@ -1362,9 +1477,27 @@ __global__ void __launch_bounds__(256) k_node_tx(DevWorld W) {
   } else {
     total = lpg_poisson(&sm, exposure);
   }
-  const int64_t sc = W.tot[(int64_t)TT_S * G + g];
+  const int64_t sc = pre_sc;
   const int64_t size = total < sc ? total : sc;
   W.size[g] = size;
+  /* the selection record of the node (round 0 targets: all of size) */
+  const uint64_t Tw = pre_sw;
+  if (size > 0 && Tw > 0) {
+    const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+    SelInfo N;
+    N.seed = rp->seed;
+    N.T = Tw;
+#pragma unroll
+    for (int k = 0; k < LPG_MAX_STRAINS; ++k) N.cum[k] = cum[k];
+    N.a = rp->chunk_base + st[i];
+    N.n = st[i + 1] - st[i];
+    N.i = i;
+    N.t = t;
+    N.ns = ns;
+    N.pad = 0;
+    reinterpret_cast<SelInfo*>(W.sel_info)[g] = N;
+    W.ksel[g] = size;
+  }
   if (size > 0) rp->any_demand = 1;
 }
 
@@ -1397,27 +1530,6 @@ __device__ __forceinline__ bool grid_sync(DevWorld& W) {
   }
   __syncthreads();
   return *(volatile int32_t*)W.abort_flag == 0;
-}
-
-/* Weight of entry x of the concatenated CSR chunk lists (x = chunk_base of
- * a simulation + position in its list; 0 past the end of a list).  With
- * first_g: the global node whose list starts at x, else -1. */
-__device__ __forceinline__ uint64_t csr_chunk_weight(const DevWorld& W, int64_t x, int* first_g = nullptr) {
-  int lo = 0, hi = W.n_reps - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (W.reps[mid].chunk_base <= x) lo = mid; else hi = mid - 1;
-  }
-  const DevRep* rp = &W.reps[lo];
-  const int64_t j = x - rp->chunk_base;
-  const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
-  if (j < 0 || j >= st[rp->n_nodes]) return 0;
-  const int32_t cid = W.node_chunks[rp->csr_cur][rp->chunk_base + j];
-  if (first_g) {
-    const int g = W.cmeta[cid].x;
-    if (st[g - rp->node_base] == j) *first_g = g;
-  }
-  return __ldcg(&W.chunk_w[cid]);
 }
 
 /* Slot of target v inside chunk cid (v < the chunk's remaining weight):
@@ -1602,38 +1714,6 @@ __device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& t
   return __shfl_sync(tm.mask, hit, ol, T);
 }
 
-/* Per-node record of one selection step, written once per tick so that a
- * target needs one load to find everything about its node. */
-struct SelInfo {
-  uint64_t seed;
-  uint64_t T;        /* remaining susceptible weight */
-  double cum[LPG_MAX_STRAINS]; /* cumulative relative FOI (model.py:1127-1135) */
-  int32_t a;         /* first entry of the node's chunk list in the concatenated lists */
-  int32_t n;         /* its chunks */
-  int32_t i;         /* node index in its simulation */
-  int32_t t;         /* tick */
-  int32_t ns;
-  int32_t pad;
-};
-
-#define LPG_SEL_OFFS 2048 /* target offsets kept in shared memory when G < this */
-
-/* Cumulative relative FOI that the strain draw compares against
- * (model.py:1127-1135), formed with the same operations in the same order. */
-__device__ __forceinline__ void sel_strain_cum(const DevWorld& W, const DevRep* rp, int g, double* cum) {
-  double p[LPG_MAX_STRAINS];
-  double totalp = 0.0;
-  for (int k = 0; k < rp->ns; ++k) {
-    p[k] = W.prob[(int64_t)k * W.G + g];
-    totalp = totalp + p[k];
-  }
-  double c = 0.0;
-  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
-    if (k < rp->ns) c = c + p[k] / totalp;
-    cum[k] = c;
-  }
-}
-
 /* The first target to claim an agent (state 0 -> 1) exposes it: strain by
  * relative FOI (model.py:1127-1145) and every susceptible total. */
 __device__ __forceinline__ void claim(DevWorld& W, uint32_t hit, int g, const SelInfo& N) {
@@ -1685,11 +1765,12 @@ __device__ __forceinline__ int sel_node_of(const int64_t* off, int G, int64_t q)
 }
 
 /* Weighted selection without replacement (tx_infect_nb, model.py:1066-1147).
- * Round 0 runs over all nodes at once (four grid barriers): demand and the
- * per-node record, the prefix of chunk weights over every chunk list, target
- * offsets (kept in shared memory by every CTA), then every target is
- * located and then claimed, targets going round-robin over the CTAs.  The
- * few collisions left after round 0 are redrawn per node by one CTA in later
+ * k_node_tx has left, per node with demand, its round-0 target count
+ * (ksel), its selection record and its node-local chunk prefix.  Round 0
+ * runs over all nodes at once: every CTA forms the target offsets in
+ * shared memory, every target is located, then (grid barrier) claimed
+ * (grid barrier), targets going round-robin over the CTAs.  The few
+ * collisions left after round 0 are redrawn per node by one CTA in later
  * rounds, with CTA barriers only.  Round r of node n draws the (n, r, j)
  * uniforms of the oracle, so the CDF targets are the same whatever runs
  * them. */
@@ -1700,75 +1781,12 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
   if (!any) return;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
-  SelInfo* info = reinterpret_cast<SelInfo*>(W.sel_info);
+  const SelInfo* info = reinterpret_cast<const SelInfo*>(W.sel_info);
   __shared__ int64_t s_K;
   __shared__ int64_t s_off[LPG_SEL_OFFS];
   const bool offs_in_smem = G < LPG_SEL_OFFS;
 
   /* ---- round 0, all nodes ---- */
-  for (int64_t g = gtid; g < G; g += gsz) {
-    const DevRep* rp = &W.reps[W.node_rep[g]];
-    int64_t k = 0;
-    const uint64_t T = W.sw[g];
-    if (rp->active && (rp->comps & LPG_COMP_TX)) {
-      k = W.size[g] - W.uniq[g];
-      if (k < 0) k = 0;
-      if (T == 0) k = 0;
-    }
-    W.ksel[g] = k;
-    if (k > 0) {
-      const int i = (int)(g - rp->node_base);
-      const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
-      SelInfo N;
-      N.seed = rp->seed;
-      N.T = T;
-      sel_strain_cum(W, rp, (int)g, N.cum);
-      N.a = rp->chunk_base + st[i];
-      N.n = st[i + 1] - st[i];
-      N.i = i;
-      N.t = rp->cur_t;
-      N.ns = rp->ns;
-      N.pad = 0;
-      info[g] = N;
-    }
-  }
-  /* Prefix of the chunk weights over every simulation's CSR chunk lists
-   * (index x = chunk_base + list position; unlisted entries weigh 0), in two
-   * passes around a grid barrier: CTA totals, then offsets.  Node g's CDF is
-   * cp[x] - base[g], base[g] = cp[first x of the node - 1], exact in
-   * integers; the thread that holds a node's first entry writes its base. */
-  const int64_t X = W.total_chunks;
-  const int64_t xper = (X + gridDim.x - 1) / gridDim.x;
-  const int64_t x0 = min(X, (int64_t)blockIdx.x * xper), x1 = min(X, x0 + xper);
-  {
-    int64_t bsum = 0;
-    for (int64_t xb = x0; xb < x1; xb += blockDim.x) {
-      const int64_t x = xb + threadIdx.x;
-      int64_t tot;
-      (void)block_excl_scan(x < x1 ? (int64_t)csr_chunk_weight(W, x) : 0, &tot);
-      bsum += tot;
-    }
-    if (threadIdx.x == 0) W.sel_part[blockIdx.x] = (uint64_t)bsum;
-  }
-  if (!grid_sync(W)) return;
-  {
-    int64_t off = 0;
-    for (int j = threadIdx.x; j < (int)blockIdx.x; j += blockDim.x) off += (int64_t)__ldcg(&W.sel_part[j]);
-    int64_t tot;
-    (void)block_excl_scan(off, &tot);
-    int64_t carry = tot;
-    for (int64_t xb = x0; xb < x1; xb += blockDim.x) {
-      const int64_t x = xb + threadIdx.x;
-      int first_g = -1;
-      const int64_t w = x < x1 ? (int64_t)csr_chunk_weight(W, x, &first_g) : 0;
-      const int64_t ex = block_excl_scan(w, &tot);
-      if (x < x1) {
-        W.cpref[x] = (uint64_t)(carry + ex + w);
-        if (first_g >= 0) W.sel_base[first_g] = (uint64_t)(carry + ex);
-      }
-      carry += tot;
-    }
-  }
   {
     /* target offsets of all nodes; every CTA computes the same values and
      * keeps them in shared memory when they fit */
@@ -1779,19 +1797,18 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
       int64_t tot;
       const int64_t ex = block_excl_scan(k, &tot);
       if (g < G) {
-        W.tgt_off[g] = carry + ex;
         if (offs_in_smem) s_off[g] = carry + ex;
+        else W.tgt_off[g] = carry + ex;
       }
       carry += tot;
     }
     if (threadIdx.x == 0) {
-      W.tgt_off[G] = carry;
       if (offs_in_smem) s_off[G] = carry;
+      else W.tgt_off[G] = carry;
       s_K = carry;
     }
     __syncthreads();
   }
-  if (!grid_sync(W)) return;
   const int64_t K = s_K;
   if (K > W.hits_cap) {
     if (gtid == 0) W.reps[0].error = LPG_ERR_INTERNAL;
@@ -1809,11 +1826,10 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
     for (int64_t q = (int64_t)(threadIdx.x / T) * gridDim.x + blockIdx.x; q < K; q += nteams) {
       const int g = sel_node_of(offs, G, q);
       const SelInfo N = info[g];
-      const uint64_t base = __ldcg(&W.sel_base[g]);
       const int64_t j = q - offs[g];
       const uint64_t v = lpg_scale_target(lpg_u53(N.seed, LPG_P_SELECT, N.t, (uint64_t)N.i, 0, (uint64_t)j), N.T);
       const int32_t* ls = W.node_chunks[W.reps[W.node_rep[g]].csr_cur] + N.a;
-      const uint32_t hit = locate_team(W, tm, ls, W.cpref + N.a, N.n, v, base);
+      const uint32_t hit = locate_team(W, tm, ls, W.cpref + N.a, N.n, v, 0);
       if (tm.l == 0) {
         if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
         W.hits[q] = hit;
@@ -1921,6 +1937,7 @@ __global__ void k_end(DevWorld W) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= W.G) return;
   DevRep* rp = &W.reps[W.node_rep[g]];
+  if (threadIdx.x == 0) W.ksel[g] = 0;
   if (!rp->active) return;
   const int i = g - rp->node_base, n = rp->n_nodes, ns = rp->ns, t = rp->cur_t, G = W.G;
   const int32_t* ev = W.ev;

@@ -190,7 +190,27 @@ LPG_HD double lpg_std_gamma(lpg_stream* s, double a) {
   return d * boost;
 }
 
-/* Poisson(lam). */
+/* 1/x for 1 <= x <= 64, correctly rounded (constant expressions), so that
+ * the inversion below multiplies instead of dividing. */
+#define LPG_R8(b) 1.0 / (b + 1.0), 1.0 / (b + 2.0), 1.0 / (b + 3.0), 1.0 / (b + 4.0), \
+                  1.0 / (b + 5.0), 1.0 / (b + 6.0), 1.0 / (b + 7.0), 1.0 / (b + 8.0)
+#if defined(__CUDACC__)
+__constant__ double lpg_recip_tab_dev[64] = {LPG_R8(0.0), LPG_R8(8.0), LPG_R8(16.0), LPG_R8(24.0),
+                                             LPG_R8(32.0), LPG_R8(40.0), LPG_R8(48.0), LPG_R8(56.0)};
+#endif
+static const double lpg_recip_tab_host[64] = {LPG_R8(0.0), LPG_R8(8.0), LPG_R8(16.0), LPG_R8(24.0),
+                                              LPG_R8(32.0), LPG_R8(40.0), LPG_R8(48.0), LPG_R8(56.0)};
+#undef LPG_R8
+LPG_HD double lpg_recip_small(int64_t x) {
+#if defined(__CUDA_ARCH__)
+  return lpg_recip_tab_dev[x - 1];
+#else
+  return lpg_recip_tab_host[x - 1];
+#endif
+}
+
+/* Poisson(lam): inversion below 10 (p_x = p_{x-1} * lam * (1/x)), PTRS
+ * (Hormann's transformed rejection with squeeze) above. */
 LPG_HD int64_t lpg_poisson(lpg_stream* s, double lam) {
   if (!(lam > 0.0)) return 0;
   if (lam < 10.0) {
@@ -200,7 +220,7 @@ LPG_HD int64_t lpg_poisson(lpg_stream* s, double lam) {
     int64_t x = 0;
     while (u > f && x < 1000) {
       x += 1;
-      p = p * lam / (double)x;
+      p = x <= 64 ? (p * lam) * lpg_recip_small(x) : (p * lam) / (double)x;
       f = f + p;
     }
     return x;
