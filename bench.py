@@ -86,11 +86,14 @@ def tick_bytes(params, t):
 
 
 def sweep_a_bytes(params, t):
-    """Column bytes k_sweep<0> must read per agent slot on tick t: the state
-    byte always, date_of_death on VD ticks.  Timers, strain, flags, risk and
-    infectivity are read only for the agents whose state needs them (by the
-    queue kernels)."""
-    return 1.0 + (4.0 if t % params["vd_step"] == 0 else 0.0)
+    """Bytes k_sweep<0> must read per agent slot on tick t: the state byte
+    always; on VD ticks also the earliest date of death of each 128-slot
+    sub-block (4 B per 128 slots).  The dates of death of the sub-blocks
+    whose earliest date has come are extra, data-dependent reads (a few per
+    cent of the sub-blocks a week); they show in the measured traffic.
+    Timers, strain, flags, risk and infectivity are read only for the agents
+    whose state needs them (by the queue kernels)."""
+    return 1.0 + (4.0 / 128.0 if t % params["vd_step"] == 0 else 0.0)
 
 
 def sweep_b_bytes(params, t):
@@ -107,7 +110,7 @@ def sweep_b_bytes(params, t):
 # DRAM bytes per slot that ncu measured for k_sweep<0> (dram__bytes_read.sum +
 # dram__bytes_write.sum over the launch / slots scanned) on a 5.1e7-agent
 # population: plain ticks and VD ticks (profiles/k_sweep_dram_nigeria_5e7.md).
-NCU_SWEEP_A_BYTES_PER_SLOT = {"plain": 1.0006, "vd": 4.987}
+NCU_SWEEP_A_BYTES_PER_SLOT = {"plain": 1.0004, "vd": 1.06}
 
 
 class ClockSampler:

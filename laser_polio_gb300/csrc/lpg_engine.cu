@@ -70,7 +70,8 @@ struct lpg_handle {
   std::vector<cudaEvent_t> ev_pool;
   int64_t launches = 0;
   int sm_count = 0;
-  int sweep_blocks = 0;
+  int sweep_blocks = 0;  /* k_sweep<1> (staged through shared memory) */
+  int sweep0_blocks = 0; /* k_sweep<0> (direct loads, no staging) */
   int select_blocks = 0;
 };
 
@@ -198,7 +199,7 @@ __global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used
 }
 
 __global__ void k_cmp_counts(DevWorld W, const int32_t* tot, const uint64_t* sw, const uint64_t* bb,
-                             const uint64_t* cw, const uint64_t* subw, int* bad) {
+                             const uint64_t* cw, const uint64_t* subw, const int32_t* subd, int* bad) {
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid < W.G) {
     for (int k = 0; k < TT_N; ++k)
@@ -212,8 +213,10 @@ __global__ void k_cmp_counts(DevWorld W, const int32_t* tot, const uint64_t* sw,
     for (int64_t q = gid; q < rp->used_chunks; q += (int64_t)gridDim.x * blockDim.x) {
       int64_t cid = rp->chunk_base + q;
       if (cw[cid] != W.chunk_w[cid]) atomicOr(bad, 8);
-      for (int s = 0; s < LPG_NSUB; ++s)
+      for (int s = 0; s < LPG_NSUB; ++s) {
         if (subw[cid * LPG_NSUB + s] != W.sub_w[cid * LPG_NSUB + s]) atomicOr(bad, 16);
+        if (subd[cid * LPG_NSUB + s] != W.sub_dod[cid * LPG_NSUB + s]) atomicOr(bad, 32);
+      }
     }
   }
 }
@@ -493,6 +496,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.evq, (size_t)chunk_total * LPG_CHUNK);
   rc |= dalloc(h, &W.chunk_w, chunk_total);
   rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
+  rc |= dalloc(h, &W.sub_dod, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.cpref, chunk_total);
   rc |= dalloc(h, &W.node_chunks[0], chunk_total);
   rc |= dalloc(h, &W.node_chunks[1], chunk_total);
@@ -768,7 +772,9 @@ extern "C" int lpg_start(lpg_handle* h) {
   }
 
   /* 6. running totals and selection weights from a full count, then tick 0 */
-  k_count<<<std::max(1, h->sm_count * 4), LPG_SWEEP_THREADS, 0, st>>>(W, W.tot, W.sw, W.bb, W.chunk_w, W.sub_w);
+  CK(cudaMemsetAsync(W.sub_dod, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
+  k_count<<<std::max(1, h->sm_count * 4), LPG_SWEEP_THREADS, 0, st>>>(W, W.tot, W.sw, W.bb, W.chunk_w, W.sub_w,
+                                                                      W.sub_dod);
   CK(cudaGetLastError());
   for (int r = 0; r < R; ++r) {
     hr[r].started = 1;
@@ -788,6 +794,9 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaFuncSetAttribute(k_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM));
   h->sweep_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
+  occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_BLOCK, 0));
+  h->sweep0_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
   occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_select, 256, 0));
   h->select_blocks = std::min(1024, std::max(1, std::min(occ, 2)) * h->sm_count);
@@ -809,8 +818,8 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
   switch (k) {
     case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
     case 1: k_newborns<<<dim3(h->sm_count * 2, R), 256, 0, st>>>(W); break;
-    case 2: k_sweep<0><<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 3: k_dsq<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
+    case 2: k_sweep<0><<<h->sweep0_blocks, LPG_SWEEP_BLOCK, 0, st>>>(W); break;
+    case 3: k_dsq<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep0_blocks); break;
     case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
     case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
     case 6: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
@@ -1013,11 +1022,12 @@ extern "C" int lpg_check_invariants(lpg_handle* h) {
   CK(cudaSetDevice(h->device));
   DevWorld& W = h->W;
   const int G = W.G;
-  int32_t* tot;
+  int32_t *tot, *subd;
   uint64_t *sw, *bb, *cw, *subw;
   int* bad;
   if (dalloc(h, &tot, (size_t)TT_N * G) || dalloc(h, &sw, G) || dalloc(h, &bb, (size_t)LPG_MAX_STRAINS * G) ||
-      dalloc(h, &cw, W.total_chunks) || dalloc(h, &subw, (size_t)W.total_chunks * LPG_NSUB) || dalloc(h, &bad, 1))
+      dalloc(h, &cw, W.total_chunks) || dalloc(h, &subw, (size_t)W.total_chunks * LPG_NSUB) ||
+      dalloc(h, &subd, (size_t)W.total_chunks * LPG_NSUB) || dalloc(h, &bad, 1))
     return LPG_ERR_NOMEM;
   cudaStream_t st = h->stream;
   CK(cudaMemsetAsync(tot, 0, sizeof(int32_t) * TT_N * G, st));
@@ -1026,13 +1036,14 @@ extern "C" int lpg_check_invariants(lpg_handle* h) {
   CK(cudaMemsetAsync(cw, 0, sizeof(uint64_t) * W.total_chunks, st));
   CK(cudaMemsetAsync(subw, 0, sizeof(uint64_t) * W.total_chunks * LPG_NSUB, st));
   CK(cudaMemsetAsync(bad, 0, 4, st));
-  k_count<<<std::max(1, h->sm_count * 4), LPG_SWEEP_THREADS, 0, st>>>(W, tot, sw, bb, cw, subw);
-  k_cmp_counts<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, tot, sw, bb, cw, subw, bad);
+  CK(cudaMemsetAsync(subd, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
+  k_count<<<std::max(1, h->sm_count * 4), LPG_SWEEP_THREADS, 0, st>>>(W, tot, sw, bb, cw, subw, subd);
+  k_cmp_counts<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, tot, sw, bb, cw, subw, subd, bad);
   CK(cudaGetLastError());
   int hb = 0;
   CK(cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  void* ps[] = {tot, sw, bb, cw, subw, bad};
+  void* ps[] = {tot, sw, bb, cw, subw, subd, bad};
   for (void* p : ps) dfree_one(h, p);
   if (hb) return fail(h, LPG_ERR_INTERNAL, "running totals differ from a recount (mask 0x%x)", hb);
   return LPG_OK;

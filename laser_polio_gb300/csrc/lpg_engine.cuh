@@ -38,6 +38,7 @@
 #define LPG_SWEEP_THREADS 256
 #define LPG_SPT (LPG_CHUNK / LPG_SWEEP_THREADS) /* slots per thread = 8 */
 #define LPG_MAX_REPS 256
+#define LPG_NO_DOD 0x7f7f7f7f /* "no alive agent": bytes 0x7f, above every date of death */
 #define LPG_SWEEP_CONSUMERS 256
 #define LPG_SWEEP_BLOCK (LPG_SWEEP_CONSUMERS + 32)
 
@@ -166,6 +167,9 @@ typedef struct {
   int4* cmeta; /* per chunk: x node, y fill, z tick of the newborns written into it, w offset of the first */
   uint64_t* chunk_w;  /* susceptible weight total */
   uint64_t* sub_w;    /* [chunk][LPG_NSUB] */
+  int32_t* sub_dod;   /* [chunk][LPG_NSUB] earliest date of death of the sub-block's alive agents
+                         (LPG_NO_DOD when it has none); deaths on a VD tick need only the
+                         sub-blocks whose earliest date has come */
   uint64_t* cpref;    /* selection: node-local prefix of chunk weights, CSR order */
   int32_t* node_chunks[2];
   int32_t* node_chunk_start[2]; /* per sim: n_nodes + 1 entries at csr_base */

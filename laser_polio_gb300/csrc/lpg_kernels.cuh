@@ -282,7 +282,9 @@ __global__ void k_newborns(DevWorld W) {
     W.risk[pos] = risk;
     W.inf[pos] = rp->pl_inf[q];
     W.dob[pos] = t;
-    W.dod[pos] = t + km_newborn(rp, t, (uint64_t)ref);
+    const int32_t dod = t + km_newborn(rp, t, (uint64_t)ref);
+    W.dod[pos] = dod;
+    atomicMin(&W.sub_dod[(int64_t)cid * LPG_NSUB + off / LPG_SUB], dod);
     W.ref[pos] = (uint32_t)ref;
     W.ds[pos] = 0;
     uint64_t w = fix_risk(risk);
@@ -328,10 +330,19 @@ __global__ void k_newborns(DevWorld W) {
 #define LPG_MBAR_SPIN (1LL << 24)
 #define LPG_DIRECT_UNROLL 8
 
-/* 16-byte global load that bypasses L1 allocation (streamed once). */
-__device__ __forceinline__ uint4 ldg_stream16(const void* p) {
+/* 16-byte global loads that bypass L1 allocation (streamed once): through
+ * the non-coherent path for data the kernel does not write, coherent
+ * otherwise. */
+__device__ __forceinline__ uint4 ldg_stream16_nc(const void* p) {
   uint4 v;
   asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p));
+  return v;
+}
+__device__ __forceinline__ uint4 ldg_stream16(const void* p) {
+  uint4 v;
+  asm volatile("ld.global.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
                : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
                : "l"(p));
   return v;
@@ -375,7 +386,6 @@ enum { SF_WORK = 1, SF_DENSE = 2, SF_VD = 4, SF_DS = 8, SF_RI = 16, SF_SIA = 32 
 
 struct SweepPlan {
   int32_t total, nreps;
-  int32_t direct; /* PHASE 0 with state bytes only for every simulation: no staging */
   int32_t off[LPG_MAX_REPS + 1]; /* work-item offsets per simulation */
   int32_t cbase[LPG_MAX_REPS];   /* first chunk id per simulation */
   int32_t tick[LPG_MAX_REPS];
@@ -473,6 +483,22 @@ __device__ __forceinline__ uint32_t slab_reserve(uint32_t* s_cnt, uint32_t n) {
   return base + x - n;
 }
 
+/* Append one thread's queue entries of 16 slots (ei: agents in E or I,
+ * dead: deaths with their state before the sweep).  All 32 lanes call. */
+__device__ __forceinline__ void queue_a16(uint64_t* slab, uint32_t* s_cnt, int64_t pos0, uint32_t ei, uint32_t dead,
+                                          uint4 sv) {
+  if (__ballot_sync(FULLMASK, (ei | dead) != 0) == 0) return;
+  uint32_t at = slab_reserve(s_cnt, __popc(ei) + __popc(dead));
+  uint32_t m = ei | dead;
+  while (m) {
+    const int k = __ffs(m) - 1;
+    m &= m - 1;
+    const bool is_dead = (dead >> k) & 1u;
+    const uint32_t word = k < 4 ? sv.x : k < 8 ? sv.y : k < 12 ? sv.z : sv.w;
+    slab[at++] = q_entry(pos0 + k, is_dead ? QA_DEATH : QA_DS, is_dead ? (word >> (8 * (k & 3))) : 0u);
+  }
+}
+
 /* PHASE 0, one thread's 16 slots (pos0 .. pos0+15; sv the state bytes,
  * sdod the dates of death in shared memory or null): deaths are written
  * here (state -1) and queued with their old state for the bookkeeping;
@@ -529,16 +555,7 @@ __device__ __forceinline__ void sweep_a16(uint64_t* slab, uint32_t* s_cnt, DevWo
       }
     }
   }
-  if (__ballot_sync(FULLMASK, (ei | dead) != 0) == 0) return;
-  uint32_t at = slab_reserve(s_cnt, __popc(ei) + __popc(dead));
-  const uint32_t wv2[4] = {sv.x, sv.y, sv.z, sv.w};
-  uint32_t m = ei | dead;
-  while (m) {
-    const int k = __ffs(m) - 1;
-    m &= m - 1;
-    const bool is_dead = (dead >> k) & 1u;
-    slab[at++] = q_entry(pos0 + k, is_dead ? QA_DEATH : QA_DS, is_dead ? (wv2[k >> 2] >> (8 * (k & 3))) : 0u);
-  }
+  queue_a16(slab, s_cnt, pos0, ei, dead, sv);
 }
 
 /* PHASE 1, one thread's 16 slots: the RI countdown and the masks of agents
@@ -627,6 +644,130 @@ __device__ __forceinline__ void sweep_b16(uint64_t* slab, uint32_t* s_cnt, DevWo
   }
 }
 
+/* k_sweep<0>'s direct loop over one simulation's byte range [lo, lo +
+ * nbytes) of the state column on a tick without deaths: queue the agents in
+ * E or I (all 32 lanes of every warp call). */
+__device__ __forceinline__ void sweep_direct_ei(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, int64_t lo,
+                                                int64_t nbytes) {
+  const uint8_t* base = reinterpret_cast<const uint8_t*>(W.ds) + lo;
+  const int64_t step = (int64_t)LPG_SWEEP_BLOCK * 16 * LPG_DIRECT_UNROLL;
+  for (int64_t ob = 0; ob < nbytes; ob += step) {
+    uint4 v[LPG_DIRECT_UNROLL];
+    uint32_t e = 0;
+#pragma unroll
+    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
+      const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
+      v[u] = o < nbytes ? ldg_stream16_nc(base + o) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    }
+#pragma unroll
+    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u)
+      e |= __vcmpltu4(__vsub4(v[u].x, 0x01010101u), 0x02020202u) |
+           __vcmpltu4(__vsub4(v[u].y, 0x01010101u), 0x02020202u) |
+           __vcmpltu4(__vsub4(v[u].z, 0x01010101u), 0x02020202u) |
+           __vcmpltu4(__vsub4(v[u].w, 0x01010101u), 0x02020202u);
+    if (__ballot_sync(FULLMASK, e != 0) == 0) continue;
+#pragma unroll
+    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
+      const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
+      sweep_a16(slab, s_cnt, W, o < nbytes, true, 0, lo + o, (int)(o & (LPG_CHUNK - 1)), LPG_CHUNK, v[u], nullptr);
+    }
+  }
+}
+
+/* The same on a VD tick: also the deaths (model.py:1767-1781).  The dates
+ * of death of a 128-slot sub-block are read only when its earliest date has
+ * come; the 8 lanes holding the sub-block then rewrite that earliest date
+ * over the survivors. */
+__device__ __noinline__ void sweep_direct_vd(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, int64_t lo, int64_t nbytes,
+                                             int t, bool dsq) {
+  const int lane = threadIdx.x & 31;
+  const uint8_t* base = reinterpret_cast<const uint8_t*>(W.ds) + lo;
+  const int64_t step = (int64_t)LPG_SWEEP_BLOCK * 16 * LPG_DIRECT_UNROLL;
+  for (int64_t ob = 0; ob < nbytes; ob += step) {
+    uint4 v[LPG_DIRECT_UNROLL];
+    int32_t dmin[LPG_DIRECT_UNROLL];
+#pragma unroll
+    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
+      const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
+      const bool in = o < nbytes;
+      /* coherent loads: this kernel writes the state bytes of the dead */
+      v[u] = in ? ldg_stream16(base + o) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+      dmin[u] = in ? __ldcg(&W.sub_dod[(lo + o) >> 7]) : LPG_NO_DOD;
+    }
+    /* groups of this thread with an agent in E or I, or with a sub-block due */
+    uint32_t work = 0;
+#pragma unroll
+    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
+      uint32_t e = 0;
+      if (dsq)
+        e = __vcmpltu4(__vsub4(v[u].x, 0x01010101u), 0x02020202u) |
+            __vcmpltu4(__vsub4(v[u].y, 0x01010101u), 0x02020202u) |
+            __vcmpltu4(__vsub4(v[u].z, 0x01010101u), 0x02020202u) |
+            __vcmpltu4(__vsub4(v[u].w, 0x01010101u), 0x02020202u);
+      work |= (uint32_t)(e != 0 || dmin[u] <= t) << u;
+    }
+    if (__ballot_sync(FULLMASK, work != 0) == 0) continue;
+#pragma unroll
+    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
+      if (__ballot_sync(FULLMASK, (work >> u) & 1u) == 0) continue;
+      const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
+      const int64_t pos0 = lo + o;
+      uint32_t dead = 0;
+      if (__ballot_sync(FULLMASK, dmin[u] <= t)) {
+        int32_t nmin = LPG_NO_DOD;
+        if (dmin[u] <= t) {
+          /* this sub-block's earliest date of death has come */
+          const int4* d4 = reinterpret_cast<const int4*>(W.dod + pos0);
+          int4 dq[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) dq[q] = d4[q];
+          const int4 m = W.cmeta[pos0 >> 11];
+          const int off = (int)(pos0 & (LPG_CHUNK - 1));
+          const int nbo = (m.z == t) ? m.w : LPG_CHUNK; /* this tick's newborns are not checked */
+          const uint32_t wv[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int32_t dd[4] = {dq[q].x, dq[q].y, dq[q].z, dq[q].w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const int k = 4 * q + j;
+              const bool alive = ((wv[q] >> (8 * j + 7)) & 1u) == 0;
+              const bool dies = alive && dd[j] <= t && off + k < nbo;
+              dead |= (uint32_t)dies << k;
+              if (alive && !dies) nmin = min(nmin, dd[j]);
+            }
+          }
+          if (dead) {
+            uint4 out = v[u];
+            uint32_t* ow = reinterpret_cast<uint32_t*>(&out);
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+              if ((dead >> k) & 1u) ow[k >> 2] |= 0xffu << (8 * (k & 3));
+            *reinterpret_cast<uint4*>(W.ds + pos0) = out;
+          }
+        }
+        /* the sub-block's 8 lanes: earliest date among its survivors */
+        nmin = min(nmin, __shfl_xor_sync(FULLMASK, nmin, 4));
+        nmin = min(nmin, __shfl_xor_sync(FULLMASK, nmin, 2));
+        nmin = min(nmin, __shfl_xor_sync(FULLMASK, nmin, 1));
+        if (dmin[u] <= t && (lane & 7) == 0) W.sub_dod[pos0 >> 7] = nmin;
+      }
+      uint32_t ei = 0;
+      if (dsq && ((work >> u) & 1u)) {
+        const uint32_t wv[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint32_t eiw = __vcmpltu4(__vsub4(wv[q], 0x01010101u), 0x02020202u);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) ei |= ((eiw >> (8 * j + 7)) & 1u) << (4 * q + j);
+        }
+        ei &= ~dead;
+      }
+      queue_a16(slab, s_cnt, pos0, ei, dead, v[u]);
+    }
+  }
+}
+
 template <int PHASE>
 __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   extern __shared__ __align__(128) uint8_t sm_stage[];
@@ -662,10 +803,6 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
     P.off[R] = acc;
     P.total = acc;
     P.nreps = R;
-    int direct = PHASE == 0;
-    for (int r = 0; r < R; ++r)
-      if ((P.flags[r] & SF_WORK) && (P.flags[r] & (SF_DS | SF_VD)) != SF_DS) direct = 0;
-    P.direct = direct;
     s_qcnt = 0;
     s_issued = 0;
     s_abort = 0;
@@ -683,12 +820,14 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   uint64_t* slab = W.evq + (int64_t)w0 * LPG_CHUNK;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  if (PHASE == 0 && P.direct) {
-    /* Only state bytes to read: every warp streams them straight from global
-     * memory, LPG_DIRECT_UNROLL 16-byte loads in flight per thread, and
-     * queues the agents in E or I.  A simulation's work items map to
-     * consecutive chunks, so each simulation's share of [w0, w1) is one
-     * contiguous byte range. */
+  if (PHASE == 0) {
+    /* Every warp streams the state bytes straight from global memory,
+     * LPG_DIRECT_UNROLL 16-byte loads in flight per thread, and queues the
+     * agents in E or I.  On VD ticks the dates of death of a 128-slot
+     * sub-block are read only when its earliest date has come; the 8 lanes
+     * holding the sub-block then rewrite that earliest date over the
+     * survivors.  A simulation's work items map to consecutive chunks, so
+     * each simulation's share of [w0, w1) is one contiguous byte range. */
     int32_t w = w0;
     while (w < w1) {
       int r;
@@ -697,30 +836,11 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       const int64_t lo = (P.cbase[r] + (int64_t)(w - P.off[r])) * LPG_CHUNK;
       const int64_t nbytes = (int64_t)(we - w) * LPG_CHUNK;
       const int t = P.tick[r];
-      const uint8_t* base = reinterpret_cast<const uint8_t*>(W.ds) + lo;
-      const int64_t step = (int64_t)LPG_SWEEP_BLOCK * 16 * LPG_DIRECT_UNROLL;
-      for (int64_t ob = 0; ob < nbytes; ob += step) {
-        uint4 v[LPG_DIRECT_UNROLL];
-        uint32_t e = 0;
-#pragma unroll
-        for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
-          const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
-          v[u] = o < nbytes ? ldg_stream16(base + o) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-        }
-#pragma unroll
-        for (int u = 0; u < LPG_DIRECT_UNROLL; ++u)
-          e |= __vcmpltu4(__vsub4(v[u].x, 0x01010101u), 0x02020202u) |
-               __vcmpltu4(__vsub4(v[u].y, 0x01010101u), 0x02020202u) |
-               __vcmpltu4(__vsub4(v[u].z, 0x01010101u), 0x02020202u) |
-               __vcmpltu4(__vsub4(v[u].w, 0x01010101u), 0x02020202u);
-        if (__ballot_sync(FULLMASK, e != 0) == 0) continue;
-#pragma unroll
-        for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
-          const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
-          sweep_a16(slab, &s_qcnt, W, o < nbytes, true, t, lo + o, (int)(o & (LPG_CHUNK - 1)), LPG_CHUNK, v[u],
-                    nullptr);
-        }
-      }
+      const bool dsq = (P.flags[r] & SF_DS) != 0, vd = (P.flags[r] & SF_VD) != 0;
+      if (vd)
+        sweep_direct_vd(W, slab, &s_qcnt, lo, nbytes, t, dsq);
+      else if (dsq)
+        sweep_direct_ei(W, slab, &s_qcnt, lo, nbytes);
       w = we;
     }
   } else if (warp == LPG_SWEEP_CONSUMERS / 32) {
@@ -2012,8 +2132,8 @@ __global__ void k_end(DevWorld W) {
  * invariant check).  One CTA per chunk. */
 __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_count(DevWorld W, int32_t* tot_out, uint64_t* sw_out,
                                                              uint64_t* bb_out, uint64_t* chunk_w_out,
-                                                             uint64_t* sub_w_out) {
-  __shared__ int32_t s_tot[TT_N];
+                                                             uint64_t* sub_w_out, int32_t* sub_dod_out) {
+  __shared__ int32_t s_tot[TT_N], s_dmin[LPG_NSUB];
   __shared__ unsigned long long s_sw, s_bb[LPG_MAX_STRAINS], s_sub[LPG_NSUB];
   for (int r = 0; r < W.n_reps; ++r) {
     const DevRep* rp = &W.reps[r];
@@ -2022,7 +2142,10 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_count(DevWorld W, int32_t
       const int4 meta = W.cmeta[cid];
       const int g = meta.x;
       if (threadIdx.x < TT_N) s_tot[threadIdx.x] = 0;
-      if (threadIdx.x < LPG_NSUB) s_sub[threadIdx.x] = 0;
+      if (threadIdx.x < LPG_NSUB) {
+        s_sub[threadIdx.x] = 0;
+        s_dmin[threadIdx.x] = LPG_NO_DOD;
+      }
       if (threadIdx.x < LPG_MAX_STRAINS) s_bb[threadIdx.x] = 0;
       if (threadIdx.x == 0) s_sw = 0;
       __syncthreads();
@@ -2031,6 +2154,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_count(DevWorld W, int32_t
         const int64_t pos = cid * LPG_CHUNK + o;
         const int8_t s = W.ds[pos];
         if (s < 0) continue;
+        atomicMin(&s_dmin[o / LPG_SUB], W.dod[pos]);
         const int st = W.strain[pos];
         if (s == 0) {
           atomicAdd(&s_tot[TT_S], 1);
@@ -2055,7 +2179,10 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_count(DevWorld W, int32_t
       if (threadIdx.x < TT_N && s_tot[threadIdx.x]) atomicAdd(&tot_out[(int64_t)threadIdx.x * W.G + g], s_tot[threadIdx.x]);
       if (threadIdx.x < LPG_MAX_STRAINS && s_bb[threadIdx.x])
         atomicAdd((unsigned long long*)&bb_out[(int64_t)threadIdx.x * W.G + g], s_bb[threadIdx.x]);
-      if (threadIdx.x < LPG_NSUB) sub_w_out[cid * LPG_NSUB + threadIdx.x] = s_sub[threadIdx.x];
+      if (threadIdx.x < LPG_NSUB) {
+        sub_w_out[cid * LPG_NSUB + threadIdx.x] = s_sub[threadIdx.x];
+        sub_dod_out[cid * LPG_NSUB + threadIdx.x] = s_dmin[threadIdx.x];
+      }
       if (threadIdx.x == 0) {
         if (s_sw) atomicAdd((unsigned long long*)&sw_out[g], s_sw);
         chunk_w_out[cid] = s_sw;
