@@ -1056,7 +1056,8 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
         if (W.pp[pos] == 1) dPP -= 1;
         if (W.par[pos] == 1) dP -= 1;
       } else {
-        int8_t s = W.ds[pos];
+        const int8_t s0 = W.ds[pos];
+        int8_t s = s0;
         st = W.strain[pos];
         if (s == 1) {
           const int8_t ex = W.et[pos];
@@ -1098,11 +1099,13 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
             W.pt[pos] = dec_i8(p);
           }
         }
-        W.ds[pos] = s;
+        if (s != s0) W.ds[pos] = s;
       }
     }
-    const unsigned act = __ballot_sync(FULLMASK, on);
-    if (!on) continue;
+    /* nothing to add when every delta of the warp is zero */
+    const bool any = on && (dS | dE | dI | dR | dPP | dP | nPP | nP | nDead);
+    const unsigned act = __ballot_sync(FULLMASK, any);
+    if (!any) continue;
     const unsigned by_node = __match_any_sync(act, g);
     warp_add(&W.ev[(int64_t)EV_DEATHS * G + g], by_node, nDead);
     warp_add(&W.tot[(int64_t)TT_S * G + g], by_node, dS);
@@ -1970,8 +1973,28 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
   __shared__ int64_t s_k;
   __shared__ uint64_t s_T;
   __shared__ SelInfo s_N;
+  __shared__ int32_t s_need[256];
+  __shared__ int32_t s_nneed;
   uint64_t* s_cp = reinterpret_cast<uint64_t*>(s_off); /* the offsets are no longer needed */
-  for (int g = blockIdx.x; g < G; g += gridDim.x) {
+  /* this CTA's nodes (g = blockIdx.x + j * grid) checked at once: which
+   * still lack agents after round 0 */
+  if (threadIdx.x == 0) s_nneed = 0;
+  __syncthreads();
+  for (int j = threadIdx.x; blockIdx.x + (int64_t)j * gridDim.x < G; j += blockDim.x) {
+    const int g = blockIdx.x + j * gridDim.x;
+    if (__ldcg(&W.ksel[g]) <= 0) continue;
+    const int64_t k = __ldcg(&W.size[g]) - (int64_t)__ldcg((const unsigned long long*)&W.uniq[g]);
+    if (k > 0 && __ldcg(&W.sw[g]) > 0) {
+      const int at = atomicAdd(&s_nneed, 1);
+      if (at < 256) s_need[at] = g;
+    }
+  }
+  __syncthreads();
+  const int nneed = s_nneed;
+  for (int jn = 0; jn < (nneed < 256 ? nneed : 0) + (nneed >= 256 ? (G + gridDim.x - 1) / gridDim.x : 0); ++jn) {
+    /* the listed nodes, or (list overflow) every node of the CTA in order */
+    const int g = nneed < 256 ? s_need[jn] : blockIdx.x + jn * gridDim.x;
+    if (g >= G) break;
     const DevRep* rp = &W.reps[W.node_rep[g]];
     if (!rp->active || !(rp->comps & LPG_COMP_TX)) continue;
     const int i = g - rp->node_base;
