@@ -10,8 +10,9 @@ reference's loops do).
   value     W untimed ticks, then K ticks timed with CUDA events on the
             engine's stream, state resident in HBM (the agent table is far
             larger than L2, so no flush is needed between ticks).
-  e2e       a full run through the C ABI from pinned host columns: upload,
-            layout, K ticks, read back results and columns.
+  e2e       a full run through the C ABI from pinned host columns to pinned
+            host result arrays and columns: upload, layout, all ticks, read
+            back results and columns (phases_s gives the split).
   roofline  per-kernel CUDA-event times from a second run of the same ticks
             in profiling mode; the dominant kernel's algorithmic bytes per
             launch / its mean launch time against the measured HBM peak.
@@ -190,11 +191,29 @@ def make_bundle(args, rank, pinned):
     return synthetic.bundle("nigeria", n_agents=int(args.agents), n_nodes=args.nodes, seed=args.seed + rank, alloc=alloc)
 
 
-def result_arrays(params):
+def pinned_empty(shape, dtype):
+    """A numpy array over page-locked host memory (torch's pinned allocator)."""
+    import torch
+
+    n = int(np.prod(shape))
+    t = torch.empty(n, dtype=getattr(torch, np.dtype(dtype).name), pin_memory=True)
+    return t.numpy().reshape(shape)
+
+
+def result_arrays(params, pinned=False):
     from laser_polio_gb300 import _abi
 
     nt, n, ns = params["nt"], params["n_nodes"], params["n_strains"]
-    return {name: np.zeros((nt, n, ns) if wide else (nt, n), np.int32) for name, wide in _abi.RESULT_FIELDS}
+    out = {}
+    for name, wide in _abi.RESULT_FIELDS:
+        shape = (nt, n, ns) if wide else (nt, n)
+        if pinned:
+            a = pinned_empty(shape, np.int32)
+            a.fill(0)
+        else:
+            a = np.zeros(shape, np.int32)
+        out[name] = a
+    return out
 
 
 def run_cpu_baseline(params, cols, warmup, steps, seconds):
@@ -371,25 +390,36 @@ def main():
     # ---- end to end through the C ABI from pinned host columns --------------
     e2e = None
     if not args.no_e2e:
-        res = result_arrays(params)
-        out_cols = {k: np.empty_like(v) for k, v in cols.items()}
+        # output buffers page-locked like the input columns, allocated before the timed region
+        res = result_arrays(params, pinned=True)
+        out_cols = {k: pinned_empty(v.shape, v.dtype) for k, v in cols.items()}
         barrier()
         t0 = time.perf_counter()
+        marks = [t0]
         h = Handle([desc], device=dev)
         h.bind_columns(0, cols)
+        h.sync()
+        marks.append(time.perf_counter())
         h.start()
+        marks.append(time.perf_counter())
         h.step(W + K)
         h.sync()
+        marks.append(time.perf_counter())
         h.read_results(0, res)
+        marks.append(time.perf_counter())
         h.read_columns(0, out_cols)
         barrier()
+        marks.append(time.perf_counter())
         dt = time.perf_counter() - t0
+        phases = dict(zip(("create_bind", "start", "ticks", "read_results", "read_columns"),
+                          (b - a for a, b in zip(marks, marks[1:]))))
         h.close()
         cnt = counts_per_tick(params, res["births"])
         at = float(cnt[1 : W + K + 1].sum())
         res_bytes = sum(v.nbytes for v in res.values())
         e2e = {"value": at / dt, "unit": "agent-ticks/s", "h2d_bytes_per_step": int(col_bytes // (W + K)),
-               "d2h_bytes_per_step": int((res_bytes + col_bytes) // (W + K)), "seconds": dt, "ticks": W + K}
+               "d2h_bytes_per_step": int((res_bytes + col_bytes) // (W + K)), "seconds": dt, "ticks": W + K,
+               "phases_s": phases}
         del out_cols
 
     # ---- device-resident timed region ------------------------------------
