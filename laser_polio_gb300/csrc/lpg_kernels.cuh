@@ -109,21 +109,30 @@ __global__ void k_begin(DevWorld W) {
   __shared__ int s_active, s_vd, s_t;
   __shared__ unsigned long long s_sum;
   if (threadIdx.x == 0) {
-    int t = rp->t;
-    int active = rp->started && !rp->error && !rp->stopped && t >= 1 && t < rp->nt;
+    /* every field read before the first store (the stores could alias) */
+    const int t = rp->t;
+    const int started = rp->started, error = rp->error, stopped = rp->stopped, nt = rp->nt;
+    const uint32_t comps = rp->comps;
+    const int vd_step = rp->vd_step, ri_step = rp->ri_step, ri_enabled = rp->ri_enabled;
+    const int64_t count = rp->count;
+    const int active = started && !error && !stopped && t >= 1 && t < nt;
+    const int tt = active ? t : 0;
+    const int sia_cnt = rp->sia_cnt[tt], sia_first = rp->sia_first[tt];
+    const int seed_cnt = rp->seed_cnt[tt], seed_first = rp->seed_first[tt];
+    const int vd = active && (comps & LPG_COMP_VD) && (t % vd_step == 0);
     rp->cur_t = t;
     rp->active = active;
-    rp->vd_tick = active && (rp->comps & LPG_COMP_VD) && (t % rp->vd_step == 0);
-    rp->ri_tick = active && (rp->comps & LPG_COMP_RI) && rp->ri_enabled && (t % rp->ri_step == 0);
-    rp->sia_n = (active && (rp->comps & LPG_COMP_SIA)) ? rp->sia_cnt[t] : 0;
-    rp->sia_i0 = active ? rp->sia_first[t] : 0;
-    rp->seed_n = (active && (rp->comps & LPG_COMP_DS)) ? rp->seed_cnt[t] : 0;
-    rp->seed_i0 = active ? rp->seed_first[t] : 0;
+    rp->vd_tick = vd;
+    rp->ri_tick = active && (comps & LPG_COMP_RI) && ri_enabled && (t % ri_step == 0);
+    rp->sia_n = (active && (comps & LPG_COMP_SIA)) ? sia_cnt : 0;
+    rp->sia_i0 = active ? sia_first : 0;
+    rp->seed_n = (active && (comps & LPG_COMP_DS)) ? seed_cnt : 0;
+    rp->seed_i0 = active ? seed_first : 0;
     rp->nb_total = 0;
-    rp->count_before = rp->count;
+    rp->count_before = count;
     rp->any_demand = 0;
     s_active = active;
-    s_vd = rp->vd_tick;
+    s_vd = vd;
     s_t = t;
     s_sum = 0;
   }
@@ -1126,6 +1135,13 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
  * precomputed thresholds (same outcome as the double compares). */
 __global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
   __shared__ uint32_t s_pre[1025];
+  {
+    /* nothing queued unless some simulation has RI or SIA work today */
+    int any = 0;
+    for (int r = 0; r < W.n_reps && !any; ++r)
+      any = W.reps[r].active && (W.reps[r].ri_tick || W.reps[r].sia_n > 0);
+    if (!any) return;
+  }
   const uint32_t n = q_prefix(W, 1, s_pre, nslabs);
   const int64_t G = W.G;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -2080,74 +2096,104 @@ __global__ void k_end(DevWorld W) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= W.G) return;
   DevRep* rp = &W.reps[W.node_rep[g]];
-  if (threadIdx.x == 0) W.ksel[g] = 0;
-  if (!rp->active) return;
-  const int i = g - rp->node_base, n = rp->n_nodes, ns = rp->ns, t = rp->cur_t, G = W.G;
-  const int32_t* ev = W.ev;
-#define EVv(k) ev[(int64_t)(k) * G + g]
-#define TTv(k) W.tot[(int64_t)(k) * G + g]
-  if (rp->comps & LPG_COMP_TX) {
+  /* every field of the replicate record this thread needs, read before the
+   * first store (stores through int32_t* could otherwise alias them and
+   * force a reload after each one) */
+  const int active = rp->active;
+  if (!active) return;
+  const int i = g - rp->node_base, ns = rp->ns, t = rp->cur_t, G = W.G, n = rp->n_nodes;
+  const uint32_t comps = rp->comps;
+  const int vd_tick = rp->vd_tick, ri_tick = rp->ri_tick, ri_strain = rp->ri_strain;
+  const int64_t nb_total = rp->nb_total;
+  const int sia_n = rp->sia_n, sia_i0 = rp->sia_i0;
+  const DevSia* sia = rp->sia;
+  const int stop_at = rp->stop_at;
+  int32_t* const res = rp->res;
+  int64_t off[RS_N];
+#pragma unroll
+  for (int k = 0; k < RS_N; ++k) off[k] = rp->res_off[k];
+  int32_t ev[EV_N];
+#pragma unroll
+  for (int k = 0; k < EV_N; ++k) ev[k] = W.ev[(int64_t)k * G + g];
+  int32_t tt[TT_N];
+#pragma unroll
+  for (int k = 0; k < TT_N; ++k) tt[k] = W.tot[(int64_t)k * G + g];
+  const int64_t row1 = (int64_t)t * n, rowS = (int64_t)t * n * ns;
+#define ROW(k) (res + off[k] + row1)
+#define ROWS(k) (res + off[k] + rowS)
+  if (comps & LPG_COMP_TX) {
     int32_t e = 0, in = 0;
     for (int k = 0; k < ns; ++k) {
-      int32_t ek = TTv(TT_E0 + k), ik = TTv(TT_I0 + k);
-      RES(rp, RS_EBS, t)[i * ns + k] = ek;
-      RES(rp, RS_IBS, t)[i * ns + k] = ik;
+      const int32_t ek = tt[TT_E0 + k], ik = tt[TT_I0 + k];
+      ROWS(RS_EBS)[i * ns + k] = ek;
+      ROWS(RS_IBS)[i * ns + k] = ik;
       e += ek;
       in += ik;
     }
-    RES(rp, RS_S, t)[i] = TTv(TT_S);
-    RES(rp, RS_E, t)[i] = e;
-    RES(rp, RS_I, t)[i] = in;
-    RES(rp, RS_R, t)[i] += TTv(TT_R);
-    RES(rp, RS_POTP, t)[i] = TTv(TT_POTP);
-    RES(rp, RS_P, t)[i] = TTv(TT_P);
+    ROW(RS_S)[i] = tt[TT_S];
+    ROW(RS_E)[i] = e;
+    ROW(RS_I)[i] = in;
+    ROW(RS_R)[i] += tt[TT_R];
+    ROW(RS_POTP)[i] = tt[TT_POTP];
+    ROW(RS_P)[i] = tt[TT_P];
   }
   if (t >= 1) {
-    if (rp->comps & LPG_COMP_DS) {
-      RES(rp, RS_NEWPOTP, t)[i] = EVv(EV_NEWPOT);
-      RES(rp, RS_NEWP, t)[i] = EVv(EV_NEWPAR);
+    if (comps & LPG_COMP_DS) {
+      ROW(RS_NEWPOTP)[i] = ev[EV_NEWPOT];
+      ROW(RS_NEWP)[i] = ev[EV_NEWPAR];
     }
-    if (rp->vd_tick) {
-      RES(rp, RS_DEATHS, t)[i] = EVv(EV_DEATHS);
-      if (rp->nb_total > 0) RES(rp, RS_BIRTHS, t)[i] = EVv(EV_BIRTHS);
+    if (vd_tick) {
+      ROW(RS_DEATHS)[i] = ev[EV_DEATHS];
+      if (nb_total > 0) ROW(RS_BIRTHS)[i] = ev[EV_BIRTHS];
     }
     int32_t ne = 0;
     int32_t nebs[LPG_MAX_STRAINS] = {0, 0, 0, 0};
-    if (rp->ri_tick) {
-      int32_t prot = EVv(EV_RIPROT);
-      RES(rp, RS_RIVAC, t)[i] = EVv(EV_RIVAC);
-      RES(rp, RS_RIPROT, t)[i] = prot;
-      RES(rp, RS_RINEWEXPBS, t)[i * ns + rp->ri_strain] = prot;
-      RES(rp, RS_IPVVAC, t)[i] = EVv(EV_IPVVAC);
+    if (ri_tick) {
+      const int32_t prot = ev[EV_RIPROT];
+      ROW(RS_RIVAC)[i] = ev[EV_RIVAC];
+      ROW(RS_RIPROT)[i] = prot;
+      ROWS(RS_RINEWEXPBS)[i * ns + ri_strain] = prot;
+      ROW(RS_IPVVAC)[i] = ev[EV_IPVVAC];
       ne += prot;
-      nebs[rp->ri_strain] += prot;
+#pragma unroll
+      for (int k = 0; k < LPG_MAX_STRAINS; ++k) nebs[k] += k == ri_strain ? prot : 0;
     }
-    for (int k = 0; k < rp->sia_n; ++k) {
-      const DevSia& sv = rp->sia[rp->sia_i0 + k];
-      int32_t vac = EVv(EV_SIAVAC0 + k), prot = EVv(EV_SIAPROT0 + k);
-      RES(rp, RS_SIAVAC, t)[i] = vac;
-      RES(rp, RS_SIAPROT, t)[i] = prot;
-      RES(rp, RS_SIANEWEXPBS, t)[i * ns + sv.strain] += prot;
+    for (int k = 0; k < sia_n && k < LPG_MAX_SIA_PER_DAY; ++k) {
+      const int sst = sia[sia_i0 + k].strain;
+      int32_t vac = 0, prot = 0;
+#pragma unroll
+      for (int q = 0; q < LPG_MAX_SIA_PER_DAY; ++q)
+        if (q == k) {
+          vac = ev[EV_SIAVAC0 + q];
+          prot = ev[EV_SIAPROT0 + q];
+        }
+      ROW(RS_SIAVAC)[i] = vac;
+      ROW(RS_SIAPROT)[i] = prot;
+      ROWS(RS_SIANEWEXPBS)[i * ns + sst] += prot;
       ne += prot;
-      nebs[sv.strain] += prot;
+#pragma unroll
+      for (int q = 0; q < LPG_MAX_STRAINS; ++q) nebs[q] += q == sst ? prot : 0;
     }
-    if (rp->comps & LPG_COMP_TX) {
-      for (int k = 0; k < ns; ++k) {
-        int32_t v = EVv(EV_TXNEW0 + k);
-        ne += v;
-        nebs[k] += v;
-      }
+    if (comps & LPG_COMP_TX) {
+#pragma unroll
+      for (int k = 0; k < LPG_MAX_STRAINS; ++k)
+        if (k < ns) {
+          const int32_t v = ev[EV_TXNEW0 + k];
+          ne += v;
+          nebs[k] += v;
+        }
     }
-    RES(rp, RS_NEWEXP, t)[i] += ne;
-    for (int k = 0; k < ns; ++k) RES(rp, RS_NEWEXPBS, t)[i * ns + k] += nebs[k];
+    ROW(RS_NEWEXP)[i] += ne;
+#pragma unroll
+    for (int k = 0; k < LPG_MAX_STRAINS; ++k)
+      if (k < ns) ROWS(RS_NEWEXPBS)[i * ns + k] += nebs[k];
   }
-#undef EVv
-#undef TTv
+#undef ROW
+#undef ROWS
   if (i == 0) {
     rp->t = t + 1;
-    if (rp->stop_at == t) rp->stopped = 1;
+    if (stop_at == t) rp->stopped = 1;
   }
-  (void)n;
 }
 
 /* ------------------------------------------------------------------------ */
