@@ -242,4 +242,21 @@ LPG_HD uint64_t lpg_fix_risk_bits(float r) {
   return q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
 }
 
+/* The same weight with single-precision arithmetic: r * 2^24 is exact in
+ * float (a power-of-two scaling), and rounding an exact value to the nearest
+ * integer, ties to even, gives the same integer in float as in double (below
+ * 2^24 the result is representable; above 2^23 the value is already an
+ * integer).  One multiply and one rounding conversion, no branches on the
+ * bits. */
+LPG_HD uint64_t lpg_fix_risk_f32(float r) {
+  const float f = r * 16777216.0f;
+  if (!(f > 0.0f)) return 0;
+  if (f > 0x1.0p62f) return (uint64_t)1 << 62;
+#if defined(__CUDA_ARCH__)
+  return __float2ull_rn(f);
+#else
+  return (uint64_t)rintf(f);
+#endif
+}
+
 #endif /* LPG_DETMATH_H */

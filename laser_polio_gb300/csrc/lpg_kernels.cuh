@@ -39,7 +39,7 @@
 
 /* ------------------------------------------------------------------------ */
 /* fixed-point weights (identical definitions in the oracle)                */
-__device__ __forceinline__ uint64_t fix_risk(float r) { return lpg_fix_risk_bits(r); }
+__device__ __forceinline__ uint64_t fix_risk(float r) { return lpg_fix_risk_f32(r); }
 __device__ __forceinline__ uint64_t fix_beta(float inf, double scal) {
   double d = ((double)inf * scal) * 4294967296.0;
   if (!(d > 0.0)) return 0;

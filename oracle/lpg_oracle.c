@@ -841,10 +841,11 @@ double lpo_mlog(double x) { return lpg_log(x); }
 double lpo_lfact(int64_t k) { return lpg_lfact(k); }
 /* fixed-point weights: the double-precision definition and the integer form
  * the CUDA engine uses, for many inputs at once (test export) */
-void lpo_fix_risk_many(const float* r, int64_t n, uint64_t* by_double, uint64_t* by_bits) {
+void lpo_fix_risk_many(const float* r, int64_t n, uint64_t* by_double, uint64_t* by_bits, uint64_t* by_f32) {
   for (int64_t i = 0; i < n; ++i) {
     by_double[i] = fix_risk(r[i]);
     by_bits[i] = lpg_fix_risk_bits(r[i]);
+    by_f32[i] = lpg_fix_risk_f32(r[i]);
   }
 }
 void lpo_poisson_many(uint64_t seed, double lam, int64_t n, int64_t* out) {

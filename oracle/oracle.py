@@ -40,7 +40,7 @@ def lib():
             getattr(L, name).argtypes = [C.c_double]
         L.lpo_lfact.restype = C.c_double
         L.lpo_lfact.argtypes = [C.c_int64]
-        L.lpo_fix_risk_many.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        L.lpo_fix_risk_many.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
         L.lpo_poisson_many.argtypes = [C.c_uint64, C.c_double, C.c_int64, C.POINTER(C.c_int64)]
         L.lpo_gamma_many.argtypes = [C.c_uint64, C.c_double, C.c_int64, C.POINTER(C.c_double)]
         L.lpo_negbinom_many.argtypes = [C.c_uint64, C.c_double, C.c_double, C.c_int64, C.POINTER(C.c_int64)]
@@ -187,10 +187,11 @@ def count_seirp(node_id, disease_state, strain, potentially_paralyzed, paralyzed
 
 
 def fix_risk_many(r):
-    """(double-precision fixed-point weights, integer-bits weights) of the
-    float32 array r."""
+    """(double-precision, integer-bits and single-precision fixed-point
+    weights) of the float32 array r."""
     r = np.ascontiguousarray(r, dtype=np.float32)
     a = np.empty(len(r), np.uint64)
     b = np.empty(len(r), np.uint64)
-    lib().lpo_fix_risk_many(r.ctypes.data, len(r), a.ctypes.data, b.ctypes.data)
-    return a, b
+    c = np.empty(len(r), np.uint64)
+    lib().lpo_fix_risk_many(r.ctypes.data, len(r), a.ctypes.data, b.ctypes.data, c.ctypes.data)
+    return a, b, c

@@ -78,7 +78,7 @@ def test_km_newborn_lifespans_follow_table():
     assert np.allclose(freq, want, atol=0.02)
 
 
-def test_fix_risk_integer_form_equals_double_definition():
+def test_fix_risk_integer_and_single_forms_equal_double_definition():
     from oracle.oracle import fix_risk_many
 
     rng = np.random.default_rng(3)
@@ -91,5 +91,6 @@ def test_fix_risk_integer_form_equals_double_definition():
     m = np.arange(1, 1 << 12, dtype=np.float64)
     halves = ((m + 0.5) / 2.0**24).astype(np.float32)
     r = np.concatenate([r, special, halves, np.nextafter(halves, np.float32(1)), np.nextafter(halves, np.float32(0))])
-    a, b = fix_risk_many(r)
+    a, b, c = fix_risk_many(r)
     np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, c)
