@@ -253,6 +253,9 @@ LPG_HD uint64_t lpg_fix_risk_f32(float r) {
   if (!(f > 0.0f)) return 0;
   if (f > 0x1.0p62f) return (uint64_t)1 << 62;
 #if defined(__CUDA_ARCH__)
+  /* the 32-bit conversion (single-precision path) whenever the integer fits:
+   * every risk below 256; the 64-bit conversion is far slower on this GPU */
+  if (f < 4294967296.0f) return (uint64_t)__float2uint_rn(f);
   return __float2ull_rn(f);
 #else
   return (uint64_t)rintf(f);

@@ -1756,11 +1756,15 @@ __device__ __forceinline__ uint64_t team_incl_scan(const Team& tm, uint64_t x) {
 /* locate() by a team: the same answer, with a (T+1)-ary search of the chunk
  * prefix and, for T >= 4, the sub-block totals and the 128 slots split over
  * the lanes (each lane a contiguous run; a team scan finds the lane that
- * holds the target).  Every lane of the team returns the hit. */
+ * holds the target).  Every lane of the team returns the hit.  All 32 lanes
+ * of the warp call it together (teams without a target pass active = false)
+ * so that the warp reconverges between the stages: teams that diverged in
+ * the search would otherwise run the later stages one team at a time. */
 __device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& tm, const int32_t* ls,
-                                                const uint64_t* cp, int32_t n, uint64_t v, uint64_t base) {
+                                                const uint64_t* cp, int32_t n, uint64_t v, uint64_t base,
+                                                bool active = true) {
   const int T = tm.T;
-  int32_t lo = 0, hi = n - 1;
+  int32_t lo = 0, hi = active ? n - 1 : 0;
   while (lo < hi) {
     const int32_t m = hi - lo;
     const int32_t p = lo + (int32_t)(((int64_t)(tm.l + 1) * m) / (T + 1));
@@ -1774,52 +1778,63 @@ __device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& t
       hi = pc;
     }
   }
-  if (lo > 0) v -= cp[lo - 1] - base;
-  const int64_t cid = ls[lo];
+  __syncwarp();
+  uint32_t hit = LPG_NONE;
+  int64_t cid = 0;
+  if (active) {
+    if (lo > 0) v -= cp[lo - 1] - base;
+    cid = ls[lo];
+  }
   if (T < 4) {
-    const uint32_t h = tm.l == 0 ? locate_in_chunk(W, cid, v) : 0u;
-    return __shfl_sync(tm.mask, h, 0, T);
+    if (active && tm.l == 0) hit = locate_in_chunk(W, cid, v);
+    __syncwarp();
+    return active ? __shfl_sync(tm.mask, hit, 0, T) : LPG_NONE;
   }
   /* sub-block: lanes l < min(T, 16) hold 16 / min(T, 16) consecutive totals */
   const int TS = T < LPG_NSUB ? T : LPG_NSUB;
   const int per = LPG_NSUB / TS;
-  uint64_t sw[LPG_NSUB];
-  uint64_t sum = 0;
-#pragma unroll
-  for (int k = 0; k < LPG_NSUB; ++k) {
-    sw[k] = 0;
-    if (k < per && tm.l < TS) {
-      sw[k] = __ldcg(&W.sub_w[cid * LPG_NSUB + tm.l * per + k]);
-      sum += sw[k];
-    }
-  }
-  uint64_t incl = team_incl_scan(tm, sum);
-  uint64_t excl = incl - sum;
-  unsigned own = team_ballot(tm, sum > 0 && excl <= v && v < incl);
-  if (own == 0) return LPG_NONE;
-  int ol = __ffs(own) - 1;
   int sb = -1;
-  uint64_t vl = v - excl;
-  if (tm.l == ol) {
+  uint64_t vl = 0;
+  if (active) {
+    uint64_t sw[LPG_NSUB];
+    uint64_t sum = 0;
 #pragma unroll
     for (int k = 0; k < LPG_NSUB; ++k) {
-      if (sb < 0 && k < per) {
-        if (sw[k] > vl) sb = tm.l * per + k;
-        else vl -= sw[k];
+      sw[k] = 0;
+      if (k < per && tm.l < TS) {
+        sw[k] = __ldcg(&W.sub_w[cid * LPG_NSUB + tm.l * per + k]);
+        sum += sw[k];
       }
     }
+    const uint64_t incl = team_incl_scan(tm, sum);
+    const uint64_t excl = incl - sum;
+    const unsigned own = team_ballot(tm, sum > 0 && excl <= v && v < incl);
+    if (own != 0) {
+      const int ol = __ffs(own) - 1;
+      vl = v - excl;
+      if (tm.l == ol) {
+#pragma unroll
+        for (int k = 0; k < LPG_NSUB; ++k) {
+          if (sb < 0 && k < per) {
+            if (sw[k] > vl) sb = tm.l * per + k;
+            else vl -= sw[k];
+          }
+        }
+      }
+      sb = __shfl_sync(tm.mask, sb, ol, T);
+      vl = __shfl_sync(tm.mask, vl, ol, T);
+    }
   }
-  sb = __shfl_sync(tm.mask, sb, ol, T);
-  vl = __shfl_sync(tm.mask, vl, ol, T);
-  if (sb < 0) return LPG_NONE;
+  __syncwarp();
   /* slots: lane l holds L = 128 / T consecutive slots */
+  const bool go = active && sb >= 0;
   const int L = LPG_SUB / T;
-  const int64_t s0 = cid * LPG_CHUNK + (int64_t)sb * LPG_SUB + (int64_t)tm.l * L;
+  const int64_t s0 = go ? cid * LPG_CHUNK + (int64_t)sb * LPG_SUB + (int64_t)tm.l * L : 0;
   uint32_t dw[8];
   float4 rv[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    if (k < L / 4) {
+    if (go && k < L / 4) {
       dw[k] = __ldcg(reinterpret_cast<const uint32_t*>(W.ds + s0) + k);
       rv[k] = reinterpret_cast<const float4*>(W.risk + s0)[k];
     } else {
@@ -1833,24 +1848,28 @@ __device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& t
     if (k < L && ((dw[k >> 2] >> (8 * (k & 3))) & 0xffu) == 0)
       wsum += fix_risk(reinterpret_cast<const float*>(rv)[k]);
   }
-  incl = team_incl_scan(tm, wsum);
-  excl = incl - wsum;
-  own = team_ballot(tm, wsum > 0 && excl <= vl && vl < incl);
-  if (own == 0) return LPG_NONE;
-  ol = __ffs(own) - 1;
-  uint32_t hit = LPG_NONE;
-  if (tm.l == ol) {
-    uint64_t r = vl - excl;
+  if (go) {
+    const uint64_t incl = team_incl_scan(tm, wsum);
+    const uint64_t excl = incl - wsum;
+    const unsigned own = team_ballot(tm, wsum > 0 && excl <= vl && vl < incl);
+    if (own != 0) {
+      const int ol = __ffs(own) - 1;
+      if (tm.l == ol) {
+        uint64_t r = vl - excl;
 #pragma unroll
-    for (int k = 0; k < 32; ++k) {
-      if (hit == LPG_NONE && k < L && ((dw[k >> 2] >> (8 * (k & 3))) & 0xffu) == 0) {
-        const uint64_t w = fix_risk(reinterpret_cast<const float*>(rv)[k]);
-        if (w > r) hit = (uint32_t)(s0 + k);
-        else r -= w;
+        for (int k = 0; k < 32; ++k) {
+          if (hit == LPG_NONE && k < L && ((dw[k >> 2] >> (8 * (k & 3))) & 0xffu) == 0) {
+            const uint64_t w = fix_risk(reinterpret_cast<const float*>(rv)[k]);
+            if (w > r) hit = (uint32_t)(s0 + k);
+            else r -= w;
+          }
+        }
       }
+      hit = __shfl_sync(tm.mask, hit, ol, T);
     }
   }
-  return __shfl_sync(tm.mask, hit, ol, T);
+  __syncwarp();
+  return hit;
 }
 
 /* The first target to claim an agent (state 0 -> 1) exposes it: strain by
@@ -1962,14 +1981,25 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
     while (T < 32 && (int64_t)(2 * T) * K <= gsz) T *= 2;
     const Team tm = make_team(T);
     const int64_t nteams = gsz / T;
-    for (int64_t q = (int64_t)(threadIdx.x / T) * gridDim.x + blockIdx.x; q < K; q += nteams) {
-      const int g = sel_node_of(offs, G, q);
-      const SelInfo N = info[g];
-      const int64_t j = q - offs[g];
-      const uint64_t v = lpg_scale_target(lpg_u53(N.seed, LPG_P_SELECT, N.t, (uint64_t)N.i, 0, (uint64_t)j), N.T);
-      const int32_t* ls = W.node_chunks[W.reps[W.node_rep[g]].csr_cur] + N.a;
-      const uint32_t hit = locate_team(W, tm, ls, W.cpref + N.a, N.n, v, 0);
-      if (tm.l == 0) {
+    /* warp-uniform trip count: every lane stays until no team of its warp has a target */
+    for (int64_t q = (int64_t)(threadIdx.x / T) * gridDim.x + blockIdx.x; __any_sync(FULLMASK, q < K); q += nteams) {
+      const bool act = q < K;
+      int g = 0;
+      SelInfo N;
+      uint64_t v = 0;
+      const int32_t* ls = W.node_chunks[0];
+      if (act) {
+        g = sel_node_of(offs, G, q);
+        N = info[g];
+        const int64_t j = q - offs[g];
+        v = lpg_scale_target(lpg_u53(N.seed, LPG_P_SELECT, N.t, (uint64_t)N.i, 0, (uint64_t)j), N.T);
+        ls = W.node_chunks[W.reps[W.node_rep[g]].csr_cur] + N.a;
+      } else {
+        N.a = 0;
+        N.n = 1;
+      }
+      const uint32_t hit = locate_team(W, tm, ls, W.cpref + N.a, N.n, v, 0, act);
+      if (act && tm.l == 0) {
         if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
         W.hits[q] = hit;
       }
@@ -2071,10 +2101,11 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
       int TT = 1;
       while (TT < 32 && (int64_t)(2 * TT) * k <= (int64_t)blockDim.x) TT *= 2;
       const Team tm = make_team(TT);
-      for (int64_t j = threadIdx.x / TT; j < k; j += blockDim.x / TT) {
-        const uint64_t v = lpg_scale_target(lpg_u53(rp->seed, LPG_P_SELECT, rp->cur_t, (uint64_t)i, (uint64_t)round, (uint64_t)j), T);
-        const uint32_t hit = locate_team(W, tm, ls, local ? s_cp : cp, n, v, 0);
-        if (tm.l == 0) {
+      for (int64_t j = threadIdx.x / TT; __any_sync(FULLMASK, j < k); j += blockDim.x / TT) {
+        const bool act = j < k;
+        const uint64_t v = act ? lpg_scale_target(lpg_u53(rp->seed, LPG_P_SELECT, rp->cur_t, (uint64_t)i, (uint64_t)round, (uint64_t)j), T) : 0;
+        const uint32_t hit = locate_team(W, tm, ls, local ? s_cp : cp, n, v, 0, act);
+        if (act && tm.l == 0) {
           if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
           hits[j] = hit;
         }
