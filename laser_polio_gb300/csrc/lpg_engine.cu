@@ -171,7 +171,11 @@ __global__ void k_scatter(DevWorld W, ScatterArgs a) {
 }
 
 /* Positions of one simulation back to reference order. */
-__global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used, int32_t node_base) {
+/* Columns of one simulation back in reference slot order.  Timers of agents
+ * in E or I are brought up to the step of tick tc (the last that has run)
+ * when the simulation steps disease states (ds_on). */
+__global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used, int32_t node_base, int32_t tc,
+                         int ds_on) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (int64_t)used * LPG_CHUNK;
        q += (int64_t)gridDim.x * blockDim.x) {
     int64_t cid = chunk_base + q / LPG_CHUNK;
@@ -180,12 +184,16 @@ __global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used
     if (o >= meta.y) continue;
     int64_t pos = cid * LPG_CHUNK + o;
     uint32_t i = W.ref[pos];
-    s.ds[i] = W.ds[pos];
-    s.strain[i] = W.strain[pos];
-    s.et[i] = W.et[pos];
-    s.it[i] = W.it[pos];
-    s.pt[i] = W.pt[pos];
-    s.pp[i] = W.pp[pos];
+    const int8_t ds = W.ds[pos], st = W.strain[pos], pp = W.pp[pos];
+    int8_t et = W.et[pos], it = W.it[pos], pt = W.pt[pos];
+    if (ds_on && (ds == 1 || ds == 2)) /* the count-downs up to the step of tick tc */
+      ev_advance(ds, st, et, it, pt, tc - W.evt[pos] + 1 + ev_pure(ds, st, et, it, pt, pp));
+    s.ds[i] = ds;
+    s.strain[i] = st;
+    s.et[i] = et;
+    s.it[i] = it;
+    s.pt[i] = pt;
+    s.pp[i] = pp;
     s.par[i] = W.par[pos];
     s.ipv[i] = W.ipv[pos];
     s.cm[i] = W.cm[pos];
@@ -199,7 +207,8 @@ __global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used
 }
 
 __global__ void k_cmp_counts(DevWorld W, const int32_t* tot, const uint64_t* sw, const uint64_t* bb,
-                             const uint64_t* cw, const uint64_t* subw, const int32_t* subd, int* bad) {
+                             const uint64_t* cw, const uint64_t* subw, const int32_t* subd, const int32_t* sube,
+                             int* bad) {
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid < W.G) {
     for (int k = 0; k < TT_N; ++k)
@@ -216,6 +225,7 @@ __global__ void k_cmp_counts(DevWorld W, const int32_t* tot, const uint64_t* sw,
       for (int s = 0; s < LPG_NSUB; ++s) {
         if (subw[cid * LPG_NSUB + s] != W.sub_w[cid * LPG_NSUB + s]) atomicOr(bad, 16);
         if (subd[cid * LPG_NSUB + s] != W.sub_dod[cid * LPG_NSUB + s]) atomicOr(bad, 32);
+        if (W.sub_evt[cid * LPG_NSUB + s] > sube[cid * LPG_NSUB + s]) atomicOr(bad, 64);
       }
     }
   }
@@ -489,6 +499,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.inf, P);
   rc |= dalloc(h, &W.dob, P);
   rc |= dalloc(h, &W.dod, P);
+  rc |= dalloc(h, &W.evt, P);
   rc |= dalloc(h, &W.ref, P);
   rc |= dalloc(h, &W.cmeta, chunk_total);
   rc |= dalloc(h, &W.qcnt, 2048);
@@ -497,6 +508,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.chunk_w, chunk_total);
   rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.sub_dod, (size_t)chunk_total * LPG_NSUB);
+  rc |= dalloc(h, &W.sub_evt, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.cpref, chunk_total);
   rc |= dalloc(h, &W.node_chunks[0], chunk_total);
   rc |= dalloc(h, &W.node_chunks[1], chunk_total);
@@ -775,6 +787,9 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaMemsetAsync(W.sub_dod, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
   k_count<<<std::max(1, h->sm_count * 4), LPG_SWEEP_THREADS, 0, st>>>(W, W.tot, W.sw, W.bb, W.chunk_w, W.sub_w,
                                                                       W.sub_dod);
+  /* first events of the agents in E or I at tick 0 */
+  CK(cudaMemsetAsync(W.sub_evt, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
+  k_init_events<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, W.evt, W.sub_evt, 0);
   CK(cudaGetLastError());
   for (int r = 0; r < R; ++r) {
     hr[r].started = 1;
@@ -990,7 +1005,8 @@ extern "C" int lpg_read_columns(lpg_handle* h, int32_t sim, const lpg_columns* c
   Staging s;
   int rc = alloc_staging(h, s, std::max<int64_t>(r.count, 1));
   if (rc) return rc;
-  k_gather<<<2048, 256, 0, h->stream>>>(h->W, s, r.chunk_base, r.used_chunks, r.node_base);
+  k_gather<<<2048, 256, 0, h->stream>>>(h->W, s, r.chunk_base, r.used_chunks, r.node_base, r.t - 1,
+                                        (r.comps & LPG_COMP_DS) ? 1 : 0);
   CK(cudaGetLastError());
   const size_t n = (size_t)r.count;
 #define OUT(dst, src, esz) \
@@ -1022,12 +1038,13 @@ extern "C" int lpg_check_invariants(lpg_handle* h) {
   CK(cudaSetDevice(h->device));
   DevWorld& W = h->W;
   const int G = W.G;
-  int32_t *tot, *subd;
+  int32_t *tot, *subd, *sube;
   uint64_t *sw, *bb, *cw, *subw;
   int* bad;
   if (dalloc(h, &tot, (size_t)TT_N * G) || dalloc(h, &sw, G) || dalloc(h, &bb, (size_t)LPG_MAX_STRAINS * G) ||
       dalloc(h, &cw, W.total_chunks) || dalloc(h, &subw, (size_t)W.total_chunks * LPG_NSUB) ||
-      dalloc(h, &subd, (size_t)W.total_chunks * LPG_NSUB) || dalloc(h, &bad, 1))
+      dalloc(h, &subd, (size_t)W.total_chunks * LPG_NSUB) || dalloc(h, &sube, (size_t)W.total_chunks * LPG_NSUB) ||
+      dalloc(h, &bad, 1))
     return LPG_ERR_NOMEM;
   cudaStream_t st = h->stream;
   CK(cudaMemsetAsync(tot, 0, sizeof(int32_t) * TT_N * G, st));
@@ -1038,12 +1055,14 @@ extern "C" int lpg_check_invariants(lpg_handle* h) {
   CK(cudaMemsetAsync(bad, 0, 4, st));
   CK(cudaMemsetAsync(subd, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
   k_count<<<std::max(1, h->sm_count * 4), LPG_SWEEP_THREADS, 0, st>>>(W, tot, sw, bb, cw, subw, subd);
-  k_cmp_counts<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, tot, sw, bb, cw, subw, subd, bad);
+  CK(cudaMemsetAsync(sube, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
+  k_count_events<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, sube);
+  k_cmp_counts<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, tot, sw, bb, cw, subw, subd, sube, bad);
   CK(cudaGetLastError());
   int hb = 0;
   CK(cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  void* ps[] = {tot, sw, bb, cw, subw, subd, bad};
+  void* ps[] = {tot, sw, bb, cw, subw, subd, sube, bad};
   for (void* p : ps) dfree_one(h, p);
   if (hb) return fail(h, LPG_ERR_INTERNAL, "running totals differ from a recount (mask 0x%x)", hb);
   return LPG_OK;

@@ -162,11 +162,14 @@ typedef struct {
   int16_t* ri;
   float *risk, *inf;
   int32_t *dob, *dod;
+  int32_t* evt; /* agents in E or I: tick of the next disease-state step that is an event */
   uint32_t* ref;
   /* per chunk */
   int4* cmeta; /* per chunk: x node, y fill, z tick of the newborns written into it, w offset of the first */
   uint64_t* chunk_w;  /* susceptible weight total */
   uint64_t* sub_w;    /* [chunk][LPG_NSUB] */
+  int32_t* sub_evt;   /* [chunk][LPG_NSUB] earliest evt of the sub-block's agents in E or I, a lower
+                         bound (LPG_NO_DOD when none): only sub-blocks with an event due are read */
   int32_t* sub_dod;   /* [chunk][LPG_NSUB] earliest date of death of the sub-block's alive agents
                          (LPG_NO_DOD when it has none); deaths on a VD tick need only the
                          sub-blocks whose earliest date has come */

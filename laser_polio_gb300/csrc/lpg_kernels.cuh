@@ -47,6 +47,37 @@ __device__ __forceinline__ uint64_t fix_beta(float inf, double scal) {
   return (uint64_t)rint(d);
 }
 __device__ __forceinline__ int8_t dec_i8(int8_t v) { return (int8_t)(uint8_t)((uint8_t)v - 1u); }
+__device__ __forceinline__ int8_t sub_i8(int8_t v, int k) { return (int8_t)(uint8_t)((uint8_t)v - (uint8_t)k); }
+
+/* Disease-state timers on events (disease_state_step_kernel, model.py:393-454).
+ * The reference counts every timer of an agent in E or I down by one each
+ * tick.  Here an agent keeps its timers as of the last tick tm at which they
+ * were brought up to date, plus evt = tm + 1 + K: K = ev_pure(...) is the
+ * number of steps that only count down before the next step that is an
+ * event (E: exposure timer <= 0, the move to I; I: infection timer <= 0, the
+ * move to R, or for strain 0 with potentially_paralyzed still -1 the
+ * paralysis check at paralysis timer <= 0).  Only event steps touch the
+ * agent; the skipped count-downs are applied (ev_advance, int8 wrap like the
+ * reference's stores) when the agent is next touched: at its event, death,
+ * a seed, or when the columns are read back.  With tc the last tick whose
+ * step has run, the skipped steps are tc - tm = tc - evt + 1 + K. */
+__device__ __forceinline__ int ev_pure(int8_t ds, int8_t strain, int8_t et, int8_t it, int8_t pt, int8_t pp) {
+  if (ds == 1) return et > 0 ? et : 0;
+  int k = it > 0 ? it : 0;
+  if (strain == 0 && pp == -1) {
+    const int kp = pt > 0 ? pt : 0;
+    k = kp < k ? kp : k;
+  }
+  return k;
+}
+__device__ __forceinline__ void ev_advance(int8_t ds, int8_t strain, int8_t& et, int8_t& it, int8_t& pt, int k) {
+  if (ds == 1) {
+    et = sub_i8(et, k);
+  } else {
+    it = sub_i8(it, k);
+    if (strain == 0) pt = sub_i8(pt, k);
+  }
+}
 __device__ __forceinline__ unsigned long long neg64(uint64_t w) { return (unsigned long long)(0ULL - w); }
 
 __device__ __forceinline__ int32_t* RES(const DevRep* rp, int k, int t) {
@@ -339,16 +370,7 @@ __global__ void k_newborns(DevWorld W) {
 #define LPG_MBAR_SPIN (1LL << 24)
 #define LPG_DIRECT_UNROLL 8
 
-/* 16-byte global loads that bypass L1 allocation (streamed once): through
- * the non-coherent path for data the kernel does not write, coherent
- * otherwise. */
-__device__ __forceinline__ uint4 ldg_stream16_nc(const void* p) {
-  uint4 v;
-  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
-               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-               : "l"(p));
-  return v;
-}
+/* 16-byte global load that bypasses L1 allocation (streamed once). */
 __device__ __forceinline__ uint4 ldg_stream16(const void* p) {
   uint4 v;
   asm volatile("ld.global.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
@@ -653,79 +675,81 @@ __device__ __forceinline__ void sweep_b16(uint64_t* slab, uint32_t* s_cnt, DevWo
   }
 }
 
-/* k_sweep<0>'s direct loop over one simulation's byte range [lo, lo +
- * nbytes) of the state column on a tick without deaths: queue the agents in
- * E or I (all 32 lanes of every warp call). */
-__device__ __forceinline__ void sweep_direct_ei(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, int64_t lo,
-                                                int64_t nbytes) {
-  const uint8_t* base = reinterpret_cast<const uint8_t*>(W.ds) + lo;
-  const int64_t step = (int64_t)LPG_SWEEP_BLOCK * 16 * LPG_DIRECT_UNROLL;
-  for (int64_t ob = 0; ob < nbytes; ob += step) {
-    uint4 v[LPG_DIRECT_UNROLL];
-    uint32_t e = 0;
+/* Of one thread's 16 slots (state bytes v, event ticks from evt at pos0):
+ * the agents in E or I whose event is at t or before (bit mask), and the
+ * earliest later event among the others (LPG_NO_DOD if none).  `dead`
+ * slots are left out of both. */
+__device__ __forceinline__ uint32_t ev_due16(const DevWorld& W, int64_t pos0, uint4 v, uint32_t dead, int t,
+                                            int32_t& nmin) {
+  const int4* e4 = reinterpret_cast<const int4*>(W.evt + pos0);
+  int4 eq[4];
 #pragma unroll
-    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
-      const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
-      v[u] = o < nbytes ? ldg_stream16_nc(base + o) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-    }
+  for (int q = 0; q < 4; ++q) eq[q] = __ldcg(e4 + q);
+  const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+  uint32_t due = 0;
 #pragma unroll
-    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u)
-      e |= __vcmpltu4(__vsub4(v[u].x, 0x01010101u), 0x02020202u) |
-           __vcmpltu4(__vsub4(v[u].y, 0x01010101u), 0x02020202u) |
-           __vcmpltu4(__vsub4(v[u].z, 0x01010101u), 0x02020202u) |
-           __vcmpltu4(__vsub4(v[u].w, 0x01010101u), 0x02020202u);
-    if (__ballot_sync(FULLMASK, e != 0) == 0) continue;
+  for (int q = 0; q < 4; ++q) {
+    const int32_t ee[4] = {eq[q].x, eq[q].y, eq[q].z, eq[q].w};
 #pragma unroll
-    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
-      const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
-      sweep_a16(slab, s_cnt, W, o < nbytes, true, 0, lo + o, (int)(o & (LPG_CHUNK - 1)), LPG_CHUNK, v[u], nullptr);
+    for (int j = 0; j < 4; ++j) {
+      const int k = 4 * q + j;
+      const uint32_t b = (wv[q] >> (8 * j)) & 0xffu;
+      if ((b == 1 || b == 2) && !((dead >> k) & 1u)) {
+        if (ee[j] <= t) due |= 1u << k;
+        else nmin = min(nmin, ee[j]);
+      }
     }
   }
+  return due;
 }
 
-/* The same on a VD tick: also the deaths (model.py:1767-1781).  The dates
- * of death of a 128-slot sub-block are read only when its earliest date has
- * come; the 8 lanes holding the sub-block then rewrite that earliest date
- * over the survivors. */
-__device__ __noinline__ void sweep_direct_vd(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, int64_t lo, int64_t nbytes,
-                                             int t, bool dsq) {
+/* Earliest value over the 8 lanes of a 128-slot sub-block (all 32 lanes call). */
+__device__ __forceinline__ int32_t sub8_min(int32_t x) {
+  x = min(x, __shfl_xor_sync(FULLMASK, x, 4));
+  x = min(x, __shfl_xor_sync(FULLMASK, x, 2));
+  return min(x, __shfl_xor_sync(FULLMASK, x, 1));
+}
+
+/* k_sweep<0> over one simulation's byte range [lo, lo + nbytes) of the
+ * state column.  Groups of 16 slots, LPG_DIRECT_UNROLL per thread per pass;
+ * the 8 lanes of a group's 128-slot sub-block see the same index entries.
+ * A group is read only when its sub-block has an event due (sub_evt <= t;
+ * dsq: the simulation steps disease states) or, on VD ticks (vd), a date of
+ * death that has come (sub_dod <= t).  Then: deaths (model.py:1767-1781;
+ * this tick's newborns are not checked), the queue of the agents whose
+ * event is now, and the sub-blocks' new earliest event and date of death
+ * over the rest.  All 32 lanes of every warp run it. */
+__device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, int64_t lo, int64_t nbytes,
+                                          int t, bool dsq, bool vd) {
   const int lane = threadIdx.x & 31;
   const uint8_t* base = reinterpret_cast<const uint8_t*>(W.ds) + lo;
   const int64_t step = (int64_t)LPG_SWEEP_BLOCK * 16 * LPG_DIRECT_UNROLL;
   for (int64_t ob = 0; ob < nbytes; ob += step) {
-    uint4 v[LPG_DIRECT_UNROLL];
-    int32_t dmin[LPG_DIRECT_UNROLL];
+    int32_t emin[LPG_DIRECT_UNROLL], dmin[LPG_DIRECT_UNROLL];
 #pragma unroll
     for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
       const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
       const bool in = o < nbytes;
-      /* coherent loads: this kernel writes the state bytes of the dead */
-      v[u] = in ? ldg_stream16(base + o) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-      dmin[u] = in ? __ldcg(&W.sub_dod[(lo + o) >> 7]) : LPG_NO_DOD;
+      emin[u] = (dsq && in) ? __ldcg(&W.sub_evt[(lo + o) >> 7]) : LPG_NO_DOD;
+      dmin[u] = (vd && in) ? __ldcg(&W.sub_dod[(lo + o) >> 7]) : LPG_NO_DOD;
     }
-    /* groups of this thread with an agent in E or I, or with a sub-block due */
     uint32_t work = 0;
 #pragma unroll
-    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
-      uint32_t e = 0;
-      if (dsq)
-        e = __vcmpltu4(__vsub4(v[u].x, 0x01010101u), 0x02020202u) |
-            __vcmpltu4(__vsub4(v[u].y, 0x01010101u), 0x02020202u) |
-            __vcmpltu4(__vsub4(v[u].z, 0x01010101u), 0x02020202u) |
-            __vcmpltu4(__vsub4(v[u].w, 0x01010101u), 0x02020202u);
-      work |= (uint32_t)(e != 0 || dmin[u] <= t) << u;
-    }
+    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) work |= (uint32_t)(emin[u] <= t || dmin[u] <= t) << u;
     if (__ballot_sync(FULLMASK, work != 0) == 0) continue;
 #pragma unroll
     for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
       if (__ballot_sync(FULLMASK, (work >> u) & 1u) == 0) continue;
       const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
       const int64_t pos0 = lo + o;
+      const bool edue = emin[u] <= t, ddue = dmin[u] <= t;
+      /* coherent loads: this kernel writes the state bytes of the dead */
+      const uint4 v = ((work >> u) & 1u) ? ldg_stream16(base + o)
+                                          : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
       uint32_t dead = 0;
-      if (__ballot_sync(FULLMASK, dmin[u] <= t)) {
+      if (__ballot_sync(FULLMASK, ddue)) {
         int32_t nmin = LPG_NO_DOD;
-        if (dmin[u] <= t) {
-          /* this sub-block's earliest date of death has come */
+        if (ddue) {
           const int4* d4 = reinterpret_cast<const int4*>(W.dod + pos0);
           int4 dq[4];
 #pragma unroll
@@ -733,7 +757,7 @@ __device__ __noinline__ void sweep_direct_vd(DevWorld& W, uint64_t* slab, uint32
           const int4 m = W.cmeta[pos0 >> 11];
           const int off = (int)(pos0 & (LPG_CHUNK - 1));
           const int nbo = (m.z == t) ? m.w : LPG_CHUNK; /* this tick's newborns are not checked */
-          const uint32_t wv[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+          const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             const int32_t dd[4] = {dq[q].x, dq[q].y, dq[q].z, dq[q].w};
@@ -747,7 +771,7 @@ __device__ __noinline__ void sweep_direct_vd(DevWorld& W, uint64_t* slab, uint32
             }
           }
           if (dead) {
-            uint4 out = v[u];
+            uint4 out = v;
             uint32_t* ow = reinterpret_cast<uint32_t*>(&out);
 #pragma unroll
             for (int k = 0; k < 16; ++k)
@@ -755,24 +779,18 @@ __device__ __noinline__ void sweep_direct_vd(DevWorld& W, uint64_t* slab, uint32
             *reinterpret_cast<uint4*>(W.ds + pos0) = out;
           }
         }
-        /* the sub-block's 8 lanes: earliest date among its survivors */
-        nmin = min(nmin, __shfl_xor_sync(FULLMASK, nmin, 4));
-        nmin = min(nmin, __shfl_xor_sync(FULLMASK, nmin, 2));
-        nmin = min(nmin, __shfl_xor_sync(FULLMASK, nmin, 1));
-        if (dmin[u] <= t && (lane & 7) == 0) W.sub_dod[pos0 >> 7] = nmin;
+        nmin = sub8_min(nmin);
+        if (ddue && (lane & 7) == 0) W.sub_dod[pos0 >> 7] = nmin;
       }
       uint32_t ei = 0;
-      if (dsq && ((work >> u) & 1u)) {
-        const uint32_t wv[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint32_t eiw = __vcmpltu4(__vsub4(wv[q], 0x01010101u), 0x02020202u);
-#pragma unroll
-          for (int j = 0; j < 4; ++j) ei |= ((eiw >> (8 * j + 7)) & 1u) << (4 * q + j);
-        }
-        ei &= ~dead;
+      if (__ballot_sync(FULLMASK, edue)) {
+        int32_t nmin = LPG_NO_DOD;
+        if (edue) ei = ev_due16(W, pos0, v, dead, t, nmin);
+        nmin = sub8_min(nmin);
+        /* the agents due now get their next event from k_dsq (atomicMin) */
+        if (edue && (lane & 7) == 0) W.sub_evt[pos0 >> 7] = nmin;
       }
-      queue_a16(slab, s_cnt, pos0, ei, dead, v[u]);
+      queue_a16(slab, s_cnt, pos0, ei, dead, v);
     }
   }
 }
@@ -830,13 +848,10 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (PHASE == 0) {
-    /* Every warp streams the state bytes straight from global memory,
-     * LPG_DIRECT_UNROLL 16-byte loads in flight per thread, and queues the
-     * agents in E or I.  On VD ticks the dates of death of a 128-slot
-     * sub-block are read only when its earliest date has come; the 8 lanes
-     * holding the sub-block then rewrite that earliest date over the
-     * survivors.  A simulation's work items map to consecutive chunks, so
-     * each simulation's share of [w0, w1) is one contiguous byte range. */
+    /* No staging: every warp reads the sub-block indexes of its range and
+     * only the slots of sub-blocks with an event or a death due
+     * (sweep_direct).  A simulation's work items map to consecutive chunks,
+     * so each simulation's share of [w0, w1) is one contiguous range. */
     int32_t w = w0;
     while (w < w1) {
       int r;
@@ -846,10 +861,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       const int64_t nbytes = (int64_t)(we - w) * LPG_CHUNK;
       const int t = P.tick[r];
       const bool dsq = (P.flags[r] & SF_DS) != 0, vd = (P.flags[r] & SF_VD) != 0;
-      if (vd)
-        sweep_direct_vd(W, slab, &s_qcnt, lo, nbytes, t, dsq);
-      else if (dsq)
-        sweep_direct_ei(W, slab, &s_qcnt, lo, nbytes);
+      if (vd || dsq) sweep_direct(W, slab, &s_qcnt, lo, nbytes, t, dsq, vd);
       w = we;
     }
   } else if (warp == LPG_SWEEP_CONSUMERS / 32) {
@@ -1059,41 +1071,56 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
             const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
             if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
           }
+          /* timers frozen at death: brought up to the step of t - 1 (they
+           * count down only where disease states are stepped) */
+          int8_t et = W.et[pos], it = W.it[pos], pt = W.pt[pos];
+          const int k = (rp->comps & LPG_COMP_DS) ? t - W.evt[pos] + ev_pure(s, (int8_t)st, et, it, pt, W.pp[pos]) : 0;
+          if (k > 0) {
+            ev_advance(s, (int8_t)st, et, it, pt, k);
+            if (s == 1) W.et[pos] = et;
+            else {
+              W.it[pos] = it;
+              if (st == 0) W.pt[pos] = pt;
+            }
+          }
         } else if (s == 3) {
           dR = -1;
         }
         if (W.pp[pos] == 1) dPP -= 1;
         if (W.par[pos] == 1) dP -= 1;
       } else {
+        /* an event step of an agent in E or I (its evt is t) */
         const int8_t s0 = W.ds[pos];
         int8_t s = s0;
         st = W.strain[pos];
+        int8_t et = W.et[pos], it = W.it[pos], pt = W.pt[pos], pp = W.pp[pos];
+        /* the count-downs skipped since the timers were last brought up to date */
+        ev_advance(s0, (int8_t)st, et, it, pt, t - W.evt[pos] + ev_pure(s0, (int8_t)st, et, it, pt, pp));
         if (s == 1) {
-          const int8_t ex = W.et[pos];
-          if (ex <= 0) {
+          if (et <= 0) {
             s = 2;
             dE -= 1;
             dI += 1;
             const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
             if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], (unsigned long long)bw);
           }
-          W.et[pos] = dec_i8(ex);
+          et = dec_i8(et);
+          W.et[pos] = et;
         }
         if (s == 2) {
-          const int8_t i = W.it[pos];
-          if (i <= 0) {
+          if (it <= 0) {
             s = 3;
             dI -= 1;
             dR += 1;
             const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
             if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
           }
-          W.it[pos] = dec_i8(i);
+          it = dec_i8(it);
+          W.it[pos] = it;
           if (st == 0) {
-            const int8_t p = W.pt[pos];
-            if (p <= 0 && W.pp[pos] == -1) {
+            if (pt <= 0 && pp == -1) {
               if (W.ipv[pos] == 0) {
-                W.pp[pos] = 1;
+                pp = 1;
                 dPP += 1;
                 nPP += 1;
                 if (lpg_u53(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < rp->thr_par) {
@@ -1102,13 +1129,20 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
                   nP += 1;
                 }
               } else {
-                W.pp[pos] = 0;
+                pp = 0;
               }
+              W.pp[pos] = pp;
             }
-            W.pt[pos] = dec_i8(p);
+            pt = dec_i8(pt);
+            W.pt[pos] = pt;
           }
         }
         if (s != s0) W.ds[pos] = s;
+        if (s == 1 || s == 2) {
+          const int32_t e1 = t + 1 + ev_pure(s, (int8_t)st, et, it, pt, pp);
+          W.evt[pos] = e1;
+          atomicMin(&W.sub_evt[pos >> 7], e1);
+        }
       }
     }
     /* nothing to add when every delta of the warp is zero */
@@ -1201,6 +1235,10 @@ __global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
       }
       if (exposed) {
         dS = -1;
+        const int8_t et = W.et[pos];
+        const int32_t e1 = t + 1 + (et > 0 ? et : 0);
+        W.evt[pos] = e1;
+        atomicMin(&W.sub_evt[pos >> 7], e1);
         const uint64_t w = fix_risk(W.risk[pos]);
         if (w) {
           atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
@@ -1362,6 +1400,17 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
       int8_t s = W.ds[pos];
       int sti = W.strain[pos];
       const int64_t cid = pos / LPG_CHUNK;
+      if (s == 1 || s == 2) {
+        /* timers up to this tick's step, which has run */
+        int8_t et = W.et[pos], it = W.it[pos], pt = W.pt[pos];
+        const int k = t - W.evt[pos] + 1 + ev_pure(s, (int8_t)sti, et, it, pt, W.pp[pos]);
+        if (k > 0) {
+          ev_advance(s, (int8_t)sti, et, it, pt, k);
+          W.et[pos] = et;
+          W.it[pos] = it;
+          W.pt[pos] = pt;
+        }
+      }
       if (s != 2) {
         uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[sti]);
         if (s == 0) {
@@ -1385,6 +1434,11 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
         lpg_stream sm;
         lpg_stream_init(&sm, rp->seed, LPG_P_SEEDTIMER, t, W.ref[pos], (uint64_t)ev.pad);
         W.it[pos] = lpg_trunc_i8(lpg_dist_sample(&sm, rp->dur_kind, rp->dur_p1, rp->dur_p2));
+      }
+      {
+        const int32_t e1 = t + 1 + ev_pure(2, (int8_t)sti, W.et[pos], W.it[pos], W.pt[pos], W.pp[pos]);
+        W.evt[pos] = e1;
+        atomicMin(&W.sub_evt[pos >> 7], e1);
       }
     }
     __syncthreads();
@@ -1900,6 +1954,13 @@ __device__ __forceinline__ void claim(DevWorld& W, uint32_t hit, int g, const Se
       break;
     }
   W.strain[pos] = (int8_t)s;
+  {
+    /* first step in E is at t + 1 (model.py:393-454) */
+    const int8_t et = W.et[pos];
+    const int32_t e1 = N.t + 1 + (et > 0 ? et : 0);
+    W.evt[pos] = e1;
+    atomicMin(&W.sub_evt[pos >> 7], e1);
+  }
   const uint64_t w = fix_risk(W.risk[pos]);
   atomicAdd(&W.tot[(int64_t)TT_S * G + g], -1);
   atomicAdd(&W.tot[(int64_t)(TT_E0 + s) * G + g], 1);
@@ -2224,6 +2285,41 @@ __global__ void k_end(DevWorld W) {
   if (i == 0) {
     rp->t = t + 1;
     if (stop_at == t) rp->stopped = 1;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Next events of the agents in E or I whose timers are as of tick tm (the
+ * start: tm = 0), and their sub-blocks' earliest events (sub_evt cleared to
+ * LPG_NO_DOD before). */
+__global__ void k_init_events(DevWorld W, int32_t* evt, int32_t* sub_evt, int tm) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < W.n_reps; ++r) {
+    const DevRep* rp = &W.reps[r];
+    const int64_t n = (int64_t)rp->used_chunks * LPG_CHUNK;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+      const int64_t pos = (int64_t)rp->chunk_base * LPG_CHUNK + q;
+      const int8_t ds = W.ds[pos];
+      if (ds != 1 && ds != 2) continue;
+      const int32_t e = tm + 1 + ev_pure(ds, W.strain[pos], W.et[pos], W.it[pos], W.pt[pos], W.pp[pos]);
+      evt[pos] = e;
+      atomicMin(&sub_evt[pos >> 7], e);
+    }
+  }
+}
+
+/* Recount of the sub-blocks' earliest events from the evt column (the
+ * invariant check: the kept index must not exceed it). */
+__global__ void k_count_events(DevWorld W, int32_t* sub_evt_out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < W.n_reps; ++r) {
+    const DevRep* rp = &W.reps[r];
+    const int64_t n = (int64_t)rp->used_chunks * LPG_CHUNK;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+      const int64_t pos = (int64_t)rp->chunk_base * LPG_CHUNK + q;
+      const int8_t ds = W.ds[pos];
+      if (ds == 1 || ds == 2) atomicMin(&sub_evt_out[pos >> 7], W.evt[pos]);
+    }
   }
 }
 
