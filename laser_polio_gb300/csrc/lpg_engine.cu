@@ -834,7 +834,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
     case 1: k_newborns<<<dim3(h->sm_count * 2, R), 256, 0, st>>>(W); break;
     case 2: k_sweep<0><<<h->sweep0_blocks, LPG_SWEEP_BLOCK, 0, st>>>(W); break;
-    case 3: k_dsq<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep0_blocks); break;
+    case 3: k_dsq<<<h->sm_count * 4, 256, 0, st>>>(W, h->sweep0_blocks); break;
     case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
     case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
     case 6: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;

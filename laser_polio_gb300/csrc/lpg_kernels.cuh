@@ -710,42 +710,53 @@ __device__ __forceinline__ int32_t sub8_min(int32_t x) {
   return min(x, __shfl_xor_sync(FULLMASK, x, 1));
 }
 
-/* k_sweep<0> over one simulation's byte range [lo, lo + nbytes) of the
- * state column.  Groups of 16 slots, LPG_DIRECT_UNROLL per thread per pass;
- * the 8 lanes of a group's 128-slot sub-block see the same index entries.
- * A group is read only when its sub-block has an event due (sub_evt <= t;
- * dsq: the simulation steps disease states) or, on VD ticks (vd), a date of
- * death that has come (sub_dod <= t).  Then: deaths (model.py:1767-1781;
- * this tick's newborns are not checked), the queue of the agents whose
- * event is now, and the sub-blocks' new earliest event and date of death
- * over the rest.  All 32 lanes of every warp run it. */
-__device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, int64_t lo, int64_t nbytes,
-                                          int t, bool dsq, bool vd) {
+/* k_sweep<0> over one simulation's range of sub-blocks [sb0, sb0 + nsb)
+ * (128 slots each), in windows of LPG_DUE_MAX sub-blocks:
+ *  1. the CTA reads the window of the index of earliest events (sub_evt;
+ *     dsq: the simulation steps disease states) and, on VD ticks (vd), of
+ *     earliest dates of death (sub_dod), 4 entries per 16-byte load, and
+ *     lists the sub-blocks with something due at t in shared memory;
+ *  2. 8 lanes per listed sub-block (16 slots each) read its state bytes,
+ *     the dates of death when a death is due and the event ticks when an
+ *     event is due: deaths (model.py:1767-1781; this tick's newborns are not
+ *     checked), the queue of the agents whose event is now, and the
+ *     sub-block's new earliest event and date of death over the rest.
+ * All threads of the CTA run it. */
+#define LPG_DUE_MAX 8192
+__device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, int64_t sb0, int64_t nsb,
+                                          int t, bool dsq, bool vd, uint32_t* s_due, int* s_ndue) {
   const int lane = threadIdx.x & 31;
-  const uint8_t* base = reinterpret_cast<const uint8_t*>(W.ds) + lo;
-  const int64_t step = (int64_t)LPG_SWEEP_BLOCK * 16 * LPG_DIRECT_UNROLL;
-  for (int64_t ob = 0; ob < nbytes; ob += step) {
-    int32_t emin[LPG_DIRECT_UNROLL], dmin[LPG_DIRECT_UNROLL];
+  for (int64_t wb = 0; wb < nsb; wb += LPG_DUE_MAX) {
+    const int nw = (int)min((int64_t)LPG_DUE_MAX, nsb - wb);
+    if (threadIdx.x == 0) *s_ndue = 0;
+    __syncthreads();
+    /* 1. due sub-blocks of the window (sb0 and the window are multiples of 16) */
+    for (int q = threadIdx.x * 4; q < nw; q += blockDim.x * 4) {
+      const int64_t sb = sb0 + wb + q;
+      int4 e4 = make_int4(LPG_NO_DOD, LPG_NO_DOD, LPG_NO_DOD, LPG_NO_DOD), d4 = e4;
+      if (dsq) e4 = __ldcg(reinterpret_cast<const int4*>(W.sub_evt + sb));
+      if (vd) d4 = __ldcg(reinterpret_cast<const int4*>(W.sub_dod + sb));
+      const int32_t ee[4] = {e4.x, e4.y, e4.z, e4.w}, dd[4] = {d4.x, d4.y, d4.z, d4.w};
 #pragma unroll
-    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
-      const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
-      const bool in = o < nbytes;
-      emin[u] = (dsq && in) ? __ldcg(&W.sub_evt[(lo + o) >> 7]) : LPG_NO_DOD;
-      dmin[u] = (vd && in) ? __ldcg(&W.sub_dod[(lo + o) >> 7]) : LPG_NO_DOD;
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t f = (ee[j] <= t ? 1u : 0u) | (dd[j] <= t ? 2u : 0u);
+        if (f && q + j < nw) {
+          const int at = atomicAdd(s_ndue, 1);
+          s_due[at] = ((uint32_t)(q + j) << 2) | f;
+        }
+      }
     }
-    uint32_t work = 0;
-#pragma unroll
-    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) work |= (uint32_t)(emin[u] <= t || dmin[u] <= t) << u;
-    if (__ballot_sync(FULLMASK, work != 0) == 0) continue;
-#pragma unroll
-    for (int u = 0; u < LPG_DIRECT_UNROLL; ++u) {
-      if (__ballot_sync(FULLMASK, (work >> u) & 1u) == 0) continue;
-      const int64_t o = ob + ((int64_t)u * LPG_SWEEP_BLOCK + threadIdx.x) * 16;
-      const int64_t pos0 = lo + o;
-      const bool edue = emin[u] <= t, ddue = dmin[u] <= t;
-      /* coherent loads: this kernel writes the state bytes of the dead */
-      const uint4 v = ((work >> u) & 1u) ? ldg_stream16(base + o)
-                                          : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    __syncthreads();
+    const int ndue = *s_ndue;
+    /* 2. 8 lanes per due sub-block; warp-uniform passes */
+    const int per_pass = (blockDim.x / 32) * 4;
+    for (int base = 0; base < ndue; base += per_pass) {
+      const int item = base + (threadIdx.x >> 5) * 4 + (lane >> 3);
+      const bool on = item < ndue;
+      const uint32_t rec = on ? s_due[item] : 0u;
+      const bool edue = (rec & 1u) != 0, ddue = (rec & 2u) != 0;
+      const int64_t pos0 = (sb0 + wb + (rec >> 2)) * LPG_SUB + (int64_t)(lane & 7) * 16;
+      const uint4 v = on ? ldg_stream16(W.ds + pos0) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
       uint32_t dead = 0;
       if (__ballot_sync(FULLMASK, ddue)) {
         int32_t nmin = LPG_NO_DOD;
@@ -792,6 +803,7 @@ __device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t*
       }
       queue_a16(slab, s_cnt, pos0, ei, dead, v);
     }
+    __syncthreads();
   }
 }
 
@@ -803,6 +815,8 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   __shared__ __align__(8) uint64_t empty[LPG_NST];
   __shared__ uint32_t s_qcnt;
   __shared__ int32_t s_issued;
+  __shared__ uint32_t s_due[PHASE == 0 ? LPG_DUE_MAX : 1];
+  __shared__ int s_ndue;
   __shared__ volatile int s_abort;
   const int R = W.n_reps < LPG_MAX_REPS ? W.n_reps : LPG_MAX_REPS;
   if (threadIdx.x == 0) {
@@ -861,7 +875,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       const int64_t nbytes = (int64_t)(we - w) * LPG_CHUNK;
       const int t = P.tick[r];
       const bool dsq = (P.flags[r] & SF_DS) != 0, vd = (P.flags[r] & SF_VD) != 0;
-      if (vd || dsq) sweep_direct(W, slab, &s_qcnt, lo, nbytes, t, dsq, vd);
+      if (vd || dsq) sweep_direct(W, slab, &s_qcnt, lo / LPG_SUB, nbytes / LPG_SUB, t, dsq, vd, s_due, &s_ndue);
       w = we;
     }
   } else if (warp == LPG_SWEEP_CONSUMERS / 32) {
