@@ -86,17 +86,6 @@ def tick_bytes(params, t):
     return b
 
 
-def sweep_a_bytes(params, t):
-    """Bytes k_sweep<0> must read per agent slot on tick t: the state byte
-    always; on VD ticks also the earliest date of death of each 128-slot
-    sub-block (4 B per 128 slots).  The dates of death of the sub-blocks
-    whose earliest date has come are extra, data-dependent reads (a few per
-    cent of the sub-blocks a week); they show in the measured traffic.
-    Timers, strain, flags, risk and infectivity are read only for the agents
-    whose state needs them (by the queue kernels)."""
-    return 1.0 + (4.0 / 128.0 if t % params["vd_step"] == 0 else 0.0)
-
-
 def sweep_b_bytes(params, t):
     """Column bytes k_sweep<1> moves per agent slot on tick t (0 when it has
     nothing to do): state, chronically_missed, ri_timer read and write on RI
@@ -108,10 +97,53 @@ def sweep_b_bytes(params, t):
     return 1.0 + 1.0 + (4.0 if ri else 0.0) + (4.0 if sia else 0.0)
 
 
-# DRAM bytes per slot that ncu measured for k_sweep<0> (dram__bytes_read.sum +
-# dram__bytes_write.sum over the launch / slots scanned) on a 5.1e7-agent
-# population: plain ticks and VD ticks (profiles/k_sweep_dram_nigeria_5e7.md).
-NCU_SWEEP_A_BYTES_PER_SLOT = {"plain": 1.0004, "vd": 1.06}
+# DRAM bytes ncu measured per unit of counted work, by kernel: (counter,
+# bytes per unit, bytes per launch besides), and where they were measured.
+NCU_TRAFFIC_PER_UNIT = {}
+NCU_TRAFFIC_SOURCE = {}
+
+
+# Algorithmic bytes per unit of counted work (the device work counters of
+# lpg_read_counters), by kernel:
+#   k_sweep<0>: 4 B per sub-block index entry read; per visited 128-slot
+#     sub-block its 128 state bytes; 512 B of event ticks and a 4 B index
+#     write when an event is due; 512 B of dates of death and a 4 B index
+#     write when a death is due; 8 B per queue entry written.
+#   k_dsq: per queue entry the 8 B entry, then state, strain, three timers
+#     and the event tick read (9 B) and state, timers and event tick written
+#     (8 B).
+#   k_evb: per queue entry the 8 B entry, then state, RI timer, flags and
+#     date of birth read (10 B) and state and timer written (5 B).
+#   k_select: per target located, the chunk prefix entry (8 B), the
+#     sub-block totals (16 x 8 B), the sub-block's 128 state bytes and 128
+#     risks (512 B), the target's hit written and read back (8 B); per agent
+#     exposed, state, strain, timers, event tick and its index (14 B).
+#   k_node_tx: the network rows (nodes^2 x 8 B per simulation) and, per
+#     chunk of the population, its list entry, weight and prefix (20 B).
+SWEEP_INDEX_B, SWEEP_DUE_B, SWEEP_EVT_B, SWEEP_DOD_B, QUEUE_ENTRY_B = 4.0, 128.0, 516.0, 516.0, 8.0
+DSQ_ENTRY_B = 8.0 + 9.0 + 8.0
+EVB_ENTRY_B = 8.0 + 10.0 + 5.0
+SEL_TARGET_B = 8.0 + 128.0 + 128.0 + 512.0 + 8.0
+SEL_CLAIM_B = 14.0
+NODE_TX_CHUNK_B = 20.0
+
+
+def kernel_alg_bytes(params, ticks, cnt, work, new_exposed):
+    """Algorithmic bytes of each modelled kernel over the ticks (total, all
+    launches), from the work counters of the same ticks."""
+    n = params["n_nodes"]
+    chunks = float(params["capacity"]) / 2048.0
+    out = {
+        "k_sweep_a": (SWEEP_INDEX_B * work["sweep_index"] + SWEEP_DUE_B * work["sweep_due"]
+                      + SWEEP_EVT_B * work["sweep_evt_due"] + SWEEP_DOD_B * work["sweep_dod_due"]
+                      + QUEUE_ENTRY_B * work["queue_ds"]),
+        "k_dsq": DSQ_ENTRY_B * work["queue_ds"],
+        "k_sweep_b": float(sum(sweep_b_bytes(params, t) * cnt[t] for t in ticks)) + QUEUE_ENTRY_B * work["queue_rs"],
+        "k_evb": EVB_ENTRY_B * work["queue_rs"],
+        "k_select": SEL_TARGET_B * work["sel_targets"] + SEL_CLAIM_B * float(new_exposed),
+        "k_node_tx": len(ticks) * (n * n * 8.0 + NODE_TX_CHUNK_B * chunks),
+    }
+    return out
 
 
 class ClockSampler:
@@ -428,6 +460,7 @@ def main():
     h.start()
     h.step(W)
     h.sync()
+    c0 = h.counters()
     stream = torch.cuda.ExternalStream(h.cuda_stream())
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -441,6 +474,8 @@ def main():
         barrier()
     ms = e0.elapsed_time(e1)
     launches = h.kernel_launches() - l0
+    c1 = h.counters()
+    work = {k: c1[k] - c0[k] for k in c1}
     res = result_arrays(params)
     h.read_results(0, res)
     st = h.state(0)
@@ -478,34 +513,46 @@ def main():
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         peak = float(peaks.get("hbm_gbs", 6800.0))
         which = "measured" if "hbm_gbs" in peaks else "fallback"
+        share = {k: v[0] / sum(x[0] for x in prof.values()) for k, v in prof.items()}
+        # agents exposed by transmission: new exposures less the RI and SIA protections counted with them
+        new_exposed = int(res["new_exposed"][ticks].sum() - res["ri_protected"][ticks].sum()
+                          - res["sia_protected"][ticks].sum())
+        alg = kernel_alg_bytes(params, ticks, cnt, work, new_exposed)
+        per_kernel = {}
+        for k, (tot_ms, nl) in prof.items():
+            row = {"ms_per_launch": tot_ms / max(1, nl), "launches": nl, "share": share[k]}
+            if k in alg:
+                row["alg_bytes_per_launch"] = alg[k] / max(1, nl)
+                row["achieved_gbs"] = alg[k] / (tot_ms / 1e3) / 1e9 if tot_ms > 0 else None
+                row["frac"] = row["achieved_gbs"] / peak if row["achieved_gbs"] is not None else None
+            per_kernel[k] = row
         top = max(prof, key=lambda k: prof[k][0])
-        sweep_ms, sweep_n = prof["k_sweep_a"]
-        alg = sum(tick_bytes(params, t) * cnt[t] for t in ticks) / K
-        kern = sum(sweep_a_bytes(params, t) * cnt[t] for t in ticks) / K
-        traffic = sum(NCU_SWEEP_A_BYTES_PER_SLOT["vd" if t % params["vd_step"] == 0 else "plain"] * cnt[t]
-                      for t in ticks) / K
-        b_ticks = [t for t in ticks if sweep_b_bytes(params, t) > 0]
-        kern_b = sum(sweep_b_bytes(params, t) * cnt[t] for t in b_ticks) / max(1, len(b_ticks))
-        per_launch_ms = sweep_ms / max(1, sweep_n)
+        t_ms, t_n = prof[top]
+        per_launch_ms = t_ms / max(1, t_n)
+        t_alg = alg.get(top)
+        achieved = t_alg / (t_ms / 1e3) / 1e9 if t_alg is not None else None
+        traffic = None
+        if top in NCU_TRAFFIC_PER_UNIT:
+            unit, per_unit, fixed = NCU_TRAFFIC_PER_UNIT[top]
+            traffic = (per_unit * work[unit] + fixed * t_n) / max(1, t_n)
+        col = sum(tick_bytes(params, t) * cnt[t] for t in ticks) / K
         roof = {
-            "kernel": "k_sweep_a",
+            "kernel": top,
             "bound": "hbm",
-            "achieved": kern / (per_launch_ms / 1e3) / 1e9,
+            "achieved": achieved,
             "peak": peak,
             "unit": "GB/s",
-            "frac": kern / (per_launch_ms / 1e3) / 1e9 / peak,
+            "frac": achieved / peak if achieved is not None else None,
             "traffic": traffic,
-            "traffic_source": "ncu DRAM bytes per slot of k_sweep<0> on plain and VD ticks (5.1e7 agents), "
-                              "times the slots of each timed launch",
+            "traffic_source": NCU_TRAFFIC_SOURCE.get(top),
             "peak_source": which,
-            "alg_bytes_per_launch": kern,
-            "reference_column_bytes_per_launch": alg,
-            "reference_column_equiv_gbs": alg / (per_launch_ms / 1e3) / 1e9,
+            "alg_bytes_per_launch": t_alg / max(1, t_n) if t_alg is not None else None,
             "mean_launch_ms": per_launch_ms,
-            "k_sweep_b": {"alg_bytes_per_active_launch": kern_b, "active_launches": len(b_ticks)},
-            "top_kernel": top,
-            "kernel_ms_per_tick": {k: v[0] / max(1, v[1]) for k, v in prof.items()},
-            "kernel_share": {k: v[0] / sum(x[0] for x in prof.values()) for k, v in prof.items()},
+            "share_of_tick": share[top],
+            "work": work,
+            "reference_column_bytes_per_tick": col,
+            "reference_column_equiv_gbs": col / (ms / K / 1e3) / 1e9,
+            "kernels": per_kernel,
         }
 
     cpu = None
@@ -538,6 +585,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "gpu_launches": launches,
+            "work_counters": work,
             "final_tick": st.t,
             "new_exposed_total": int(res["new_exposed"].sum()),
         }

@@ -243,9 +243,29 @@ int lpg_check_invariants(lpg_handle* h);
 /* Use CUDA graphs for lpg_step (default on).  Off = plain launches. */
 int lpg_set_graphs(lpg_handle* h, int32_t enable);
 
-/* Per-kernel CUDA-event timing of lpg_step (forces plain launches). */
+/* Per-kernel CUDA-event timing of lpg_step (forces plain launches).
+ * Turning it on also sets the work counters below to zero. */
 int lpg_set_profiling(lpg_handle* h, int32_t enable);
 int lpg_read_profile(lpg_handle* h, lpg_profile* out);
+
+/* Work counters the tick kernels accumulate on the device (all simulations
+ * of the handle), from lpg_create or the last lpg_set_profiling(h, 1): the
+ * data-dependent amounts of work behind each kernel's algorithmic bytes.
+ * No counterpart in the reference. */
+enum {
+  LPG_CTR_SWEEP_INDEX = 0,   /* sub-block index entries k_sweep<0> read */
+  LPG_CTR_SWEEP_DUE = 1,     /* sub-blocks it visited (an event or a death due) */
+  LPG_CTR_SWEEP_EVT_DUE = 2, /* of those, with an event due */
+  LPG_CTR_SWEEP_DOD_DUE = 3, /* of those, with a death due */
+  LPG_CTR_QUEUE_DS = 4,      /* queue entries of k_sweep<0> (deaths, disease steps) */
+  LPG_CTR_QUEUE_RS = 5,      /* queue entries of k_sweep<1> (RI, SIA) */
+  LPG_CTR_SEL_TARGETS = 6,   /* targets k_select located, all rounds */
+  LPG_CTR_SEL_NODE_ROUNDS = 7, /* node rounds after round 0 */
+  LPG_NUM_COUNTERS = 8
+};
+/* Copies min(n, LPG_NUM_COUNTERS) counters to out (host memory) after the
+ * handle's stream has finished; returns LPG_OK or an error code. */
+int lpg_read_counters(lpg_handle* h, uint64_t* out, int32_t n);
 
 /* The CUDA stream the handle launches on, as an opaque pointer. */
 void* lpg_cuda_stream(lpg_handle* h);

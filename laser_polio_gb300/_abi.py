@@ -170,6 +170,11 @@ class lpg_sim_state(C.Structure):
     _fields_ = [("t", C.c_int32), ("stopped", C.c_int32), ("count", C.c_int64), ("error", C.c_int32)]
 
 
+# lpg.h's LPG_CTR_* indices, in order
+COUNTER_NAMES = ("sweep_index", "sweep_due", "sweep_evt_due", "sweep_dod_due", "queue_ds", "queue_rs",
+                 "sel_targets", "sel_node_rounds")
+
+
 class lpg_profile(C.Structure):
     _fields_ = [
         ("n_kernels", C.c_int32),

@@ -31,6 +31,7 @@ SIGNATURES = {
     "lpg_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
     "lpg_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
     "lpg_read_profile": (C.c_int, [C.c_void_p, C.POINTER(_abi.lpg_profile)]),
+    "lpg_read_counters": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int32]),
     "lpg_cuda_stream": (C.c_void_p, [C.c_void_p]),
     "lpg_kernel_launches": (C.c_int64, [C.c_void_p]),
     "lpg_last_error": (C.c_char_p, [C.c_void_p]),
@@ -130,6 +131,12 @@ class Handle:
         p = _abi.lpg_profile()
         self._check(self.lib.lpg_read_profile(self.h, C.byref(p)))
         return {p.names[k].decode(): (p.total_ms[k], p.launches[k]) for k in range(p.n_kernels)}
+
+    def counters(self) -> dict:
+        """The device work counters (lpg_read_counters), by name."""
+        buf = (C.c_uint64 * len(_abi.COUNTER_NAMES))()
+        self._check(self.lib.lpg_read_counters(self.h, buf, len(buf)))
+        return dict(zip(_abi.COUNTER_NAMES, (int(x) for x in buf)))
 
     def cuda_stream(self) -> int:
         return self.lib.lpg_cuda_stream(self.h) or 0

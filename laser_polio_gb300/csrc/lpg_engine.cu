@@ -540,6 +540,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.bar_count, 1);
   rc |= dalloc(h, &W.bar_gen, 1);
   rc |= dalloc(h, &W.abort_flag, 1);
+  rc |= dalloc(h, &W.ctr, LPG_NUM_COUNTERS);
   rc |= dalloc(h, &W.reps, R);
   if (rc) return LPG_ERR_NOMEM;
   CK(cudaMemsetAsync(W.ds, 0xff, P, st));
@@ -555,6 +556,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaMemsetAsync(W.bar_count, 0, 4, st));
   CK(cudaMemsetAsync(W.bar_gen, 0, 4, st));
   CK(cudaMemsetAsync(W.abort_flag, 0, 4, st));
+  CK(cudaMemsetAsync(W.ctr, 0, sizeof(unsigned long long) * LPG_NUM_COUNTERS, st));
 
   /* 4. per-simulation static data, results, pools, chunk tables */
   std::vector<int4> h_meta(chunk_total, make_int4(-1, 0, -1, 0));
@@ -1082,7 +1084,18 @@ extern "C" int lpg_set_profiling(lpg_handle* h, int32_t enable) {
       h->prof_ms[k] = 0;
       h->prof_n[k] = 0;
     }
+    if (h->W.ctr) CK(cudaMemsetAsync(h->W.ctr, 0, sizeof(unsigned long long) * LPG_NUM_COUNTERS, h->stream));
   }
+  return LPG_OK;
+}
+
+extern "C" int lpg_read_counters(lpg_handle* h, uint64_t* out, int32_t n) {
+  if (!h || !out || n < 0) return LPG_ERR_ARG;
+  if (!h->W.ctr) return LPG_ERR_STATE;
+  unsigned long long c[LPG_NUM_COUNTERS];
+  CK(cudaMemcpyAsync(c, h->W.ctr, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < n && k < LPG_NUM_COUNTERS; ++k) out[k] = (uint64_t)c[k];
   return LPG_OK;
 }
 

@@ -200,6 +200,7 @@ typedef struct {
   uint32_t* bar_count;
   uint32_t* bar_gen;
   int32_t* abort_flag;
+  unsigned long long* ctr; /* [LPG_NUM_COUNTERS] work counters */
 } DevWorld;
 
 #endif

@@ -726,9 +726,13 @@ __device__ __forceinline__ int32_t sub8_min(int32_t x) {
 __device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, int64_t sb0, int64_t nsb,
                                           int t, bool dsq, bool vd, uint32_t* s_due, int* s_ndue) {
   const int lane = threadIdx.x & 31;
+  uint32_t n_due = 0, n_edue = 0, n_ddue = 0; /* work counters, lanes (lane & 7) == 0 */
   for (int64_t wb = 0; wb < nsb; wb += LPG_DUE_MAX) {
     const int nw = (int)min((int64_t)LPG_DUE_MAX, nsb - wb);
-    if (threadIdx.x == 0) *s_ndue = 0;
+    if (threadIdx.x == 0) {
+      *s_ndue = 0;
+      atomicAdd(&W.ctr[LPG_CTR_SWEEP_INDEX], (unsigned long long)nw * ((dsq ? 1 : 0) + (vd ? 1 : 0)));
+    }
     __syncthreads();
     /* 1. due sub-blocks of the window (sb0 and the window are multiples of 16) */
     for (int q = threadIdx.x * 4; q < nw; q += blockDim.x * 4) {
@@ -755,6 +759,11 @@ __device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t*
       const bool on = item < ndue;
       const uint32_t rec = on ? s_due[item] : 0u;
       const bool edue = (rec & 1u) != 0, ddue = (rec & 2u) != 0;
+      if (on && (lane & 7) == 0) {
+        n_due += 1;
+        n_edue += edue ? 1 : 0;
+        n_ddue += ddue ? 1 : 0;
+      }
       const int64_t pos0 = (sb0 + wb + (rec >> 2)) * LPG_SUB + (int64_t)(lane & 7) * 16;
       const uint4 v = on ? ldg_stream16(W.ds + pos0) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
       uint32_t dead = 0;
@@ -804,6 +813,14 @@ __device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t*
       queue_a16(slab, s_cnt, pos0, ei, dead, v);
     }
     __syncthreads();
+  }
+  n_due = __reduce_add_sync(FULLMASK, n_due);
+  n_edue = __reduce_add_sync(FULLMASK, n_edue);
+  n_ddue = __reduce_add_sync(FULLMASK, n_ddue);
+  if (lane == 0 && n_due) {
+    atomicAdd(&W.ctr[LPG_CTR_SWEEP_DUE], (unsigned long long)n_due);
+    atomicAdd(&W.ctr[LPG_CTR_SWEEP_EVT_DUE], (unsigned long long)n_edue);
+    atomicAdd(&W.ctr[LPG_CTR_SWEEP_DOD_DUE], (unsigned long long)n_ddue);
   }
 }
 
@@ -1051,6 +1068,7 @@ __device__ __forceinline__ uint32_t q_prefix(const DevWorld& W, int phase, uint3
 __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
   __shared__ uint32_t s_pre[1025];
   const uint32_t n = q_prefix(W, 0, s_pre, nslabs);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&W.ctr[LPG_CTR_QUEUE_DS], (unsigned long long)n);
   const int64_t G = W.G;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t q = base + threadIdx.x;
@@ -1191,6 +1209,7 @@ __global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
     if (!any) return;
   }
   const uint32_t n = q_prefix(W, 1, s_pre, nslabs);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&W.ctr[LPG_CTR_QUEUE_RS], (unsigned long long)n);
   const int64_t G = W.G;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t q = base + threadIdx.x;
@@ -2047,6 +2066,7 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
     if (gtid == 0) W.reps[0].error = LPG_ERR_INTERNAL;
     return;
   }
+  if (gtid == 0 && K) atomicAdd(&W.ctr[LPG_CTR_SEL_TARGETS], (unsigned long long)K);
   const int64_t* offs = offs_in_smem ? s_off : W.tgt_off;
   /* Targets go round-robin over the CTAs (target q on CTA q mod grid), so
    * that a few thousand of them still use every SM, each located by a team
@@ -2132,6 +2152,8 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
         s_T = __ldcg(&W.sw[g]);
         s_k = (k > 0 && s_T > 0) ? k : 0;
         if (s_k > 0) {
+          atomicAdd(&W.ctr[LPG_CTR_SEL_TARGETS], (unsigned long long)s_k);
+          atomicAdd(&W.ctr[LPG_CTR_SEL_NODE_ROUNDS], 1ULL);
           s_N.seed = rp->seed;
           s_N.t = rp->cur_t;
           s_N.ns = rp->ns;

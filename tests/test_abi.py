@@ -70,3 +70,10 @@ def test_create_without_gpu_reports_cuda_error():
     rc = lib.lpg_create(C.byref(d), 1, 0, C.byref(h))
     assert rc != 0
     lib.lpg_destroy(h)
+
+
+def test_counter_names_follow_header_enum():
+    text = HEADER.read_text()
+    found = dict((m.group(1).lower(), int(m.group(2))) for m in re.finditer(r"LPG_CTR_([A-Z_]+)\s*=\s*(\d+)", text))
+    assert [found[n] for n in _abi.COUNTER_NAMES] == list(range(len(_abi.COUNTER_NAMES)))
+    assert int(re.search(r"LPG_NUM_COUNTERS\s*=\s*(\d+)", text).group(1)) == len(_abi.COUNTER_NAMES)

@@ -217,3 +217,32 @@ def test_parity_batched_replicates():
         assert_same(res_o, res_g, f"replicate {i} result")
         assert_same(cols_o, cols_g, f"replicate {i} column", count=so.count)
     h.close()
+
+
+def test_work_counters_are_consistent():
+    """The device work counters (lpg_read_counters) start at zero, are reset
+    by turning profiling on, and agree with the results they stand behind."""
+    from laser_polio_gb300._lib import Handle
+
+    sim = _busy_sim(seed=11, dur=150)
+    spec, cols, res = snapshot(sim)
+    h = Handle([spec.desc])
+    h.bind_columns(0, cols)
+    h.start()
+    assert all(v == 0 for v in h.counters().values())
+    h.step(40)
+    h.sync()
+    h.set_profiling(True)
+    assert all(v == 0 for v in h.counters().values())
+    h.step(sim.nt - 41)
+    h.sync()
+    c = h.counters()
+    h.read_results(0, res)
+    h.close()
+    assert 0 < c["sweep_due"] <= c["sweep_index"]
+    assert c["sweep_evt_due"] <= c["sweep_due"] and c["sweep_dod_due"] <= c["sweep_due"]
+    assert c["sweep_evt_due"] + c["sweep_dod_due"] >= c["sweep_due"]
+    assert c["queue_ds"] >= int(res["deaths"][41:].sum())
+    assert c["queue_rs"] > 0
+    if res["new_exposed"][41:].sum() > 0:
+        assert c["sel_targets"] > 0
