@@ -87,14 +87,15 @@ def tick_bytes(params, t):
 
 
 def sweep_b_bytes(params, t):
-    """Column bytes k_sweep<1> moves per agent slot on tick t (0 when it has
-    nothing to do): state, chronically_missed, ri_timer read and write on RI
-    ticks; state, chronically_missed, date_of_birth on SIA days."""
+    """Column bytes k_sweep<1> stages per agent slot on tick t: on SIA days
+    state, chronically_missed and date_of_birth, plus ri_timer and the
+    reference index when RI falls on the same day; 0 on other ticks (RI
+    alone goes through the due index, counted by the work counters)."""
     ri = bool(params["ri_enabled"]) and t % params["ri_step"] == 0
     sia = any(e[0] == t for e in params["sia"])
-    if not (ri or sia):
+    if not sia:
         return 0.0
-    return 1.0 + 1.0 + (4.0 if ri else 0.0) + (4.0 if sia else 0.0)
+    return 1.0 + 1.0 + 4.0 + (6.0 if ri else 0.0)
 
 
 # DRAM bytes ncu measured per unit of counted work, by kernel: (counter,
@@ -118,6 +119,9 @@ NCU_TRAFFIC_SOURCE = {}
 #     sub-block totals (16 x 8 B), the sub-block's 128 state bytes and 128
 #     risks (512 B), the target's hit written and read back (8 B); per agent
 #     exposed, state, strain, timers, event tick and its index (14 B).
+#   k_sweep<1> on RI ticks: 4 B per RI due index entry read; per visited
+#     sub-block its state, chronically-missed flags, RI timers, reference
+#     indexes and dates of birth (128 x 12 B) and the index write (4 B).
 #   k_node_tx: the network rows (nodes^2 x 8 B per simulation) and, per
 #     chunk of the population, its list entry, weight and prefix (20 B).
 SWEEP_INDEX_B, SWEEP_DUE_B, SWEEP_EVT_B, SWEEP_DOD_B, QUEUE_ENTRY_B = 4.0, 128.0, 516.0, 516.0, 8.0
@@ -126,6 +130,7 @@ EVB_ENTRY_B = 8.0 + 10.0 + 5.0
 SEL_TARGET_B = 8.0 + 128.0 + 128.0 + 512.0 + 8.0
 SEL_CLAIM_B = 14.0
 NODE_TX_CHUNK_B = 20.0
+RI_INDEX_B, RI_DUE_B = 4.0, 128.0 * 12.0 + 4.0
 
 
 def kernel_alg_bytes(params, ticks, cnt, work, new_exposed):
@@ -138,7 +143,8 @@ def kernel_alg_bytes(params, ticks, cnt, work, new_exposed):
                       + SWEEP_EVT_B * work["sweep_evt_due"] + SWEEP_DOD_B * work["sweep_dod_due"]
                       + QUEUE_ENTRY_B * work["queue_ds"]),
         "k_dsq": DSQ_ENTRY_B * work["queue_ds"],
-        "k_sweep_b": float(sum(sweep_b_bytes(params, t) * cnt[t] for t in ticks)) + QUEUE_ENTRY_B * work["queue_rs"],
+        "k_sweep_b": (float(sum(sweep_b_bytes(params, t) * cnt[t] for t in ticks)) + RI_INDEX_B * work["ri_index"]
+                      + RI_DUE_B * work["ri_due"] + QUEUE_ENTRY_B * work["queue_rs"]),
         "k_evb": EVB_ENTRY_B * work["queue_rs"],
         "k_select": SEL_TARGET_B * work["sel_targets"] + SEL_CLAIM_B * float(new_exposed),
         "k_node_tx": len(ticks) * (n * n * 8.0 + NODE_TX_CHUNK_B * chunks),

@@ -261,7 +261,9 @@ enum {
   LPG_CTR_QUEUE_RS = 5,      /* queue entries of k_sweep<1> (RI, SIA) */
   LPG_CTR_SEL_TARGETS = 6,   /* targets k_select located, all rounds */
   LPG_CTR_SEL_NODE_ROUNDS = 7, /* node rounds after round 0 */
-  LPG_NUM_COUNTERS = 8
+  LPG_CTR_RI_INDEX = 8,      /* RI due index entries k_sweep<1> read */
+  LPG_CTR_RI_DUE = 9,        /* sub-blocks it visited with an RI due tick come */
+  LPG_NUM_COUNTERS = 10
 };
 /* Copies min(n, LPG_NUM_COUNTERS) counters to out (host memory) after the
  * handle's stream has finished; returns LPG_OK or an error code. */

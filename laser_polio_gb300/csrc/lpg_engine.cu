@@ -170,12 +170,15 @@ __global__ void k_scatter(DevWorld W, ScatterArgs a) {
   }
 }
 
-/* Positions of one simulation back to reference order. */
-/* Columns of one simulation back in reference slot order.  Timers of agents
- * in E or I are brought up to the step of tick tc (the last that has run)
- * when the simulation steps disease states (ds_on). */
+/* Columns of one simulation (rep) back in reference slot order.  Timers of
+ * agents in E or I are brought up to the step of tick tc (the last that has
+ * run) when the simulation steps disease states (ds_on); RI timers of the
+ * alive, not chronically-missed agents to the RI ticks up to tc when RI
+ * runs. */
 __global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used, int32_t node_base, int32_t tc,
-                         int ds_on) {
+                         int ds_on, int rep) {
+  const DevRep* rp = &W.reps[rep];
+  const bool ri_on = ri_runs(rp);
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (int64_t)used * LPG_CHUNK;
        q += (int64_t)gridDim.x * blockDim.x) {
     int64_t cid = chunk_base + q / LPG_CHUNK;
@@ -185,6 +188,7 @@ __global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used
     int64_t pos = cid * LPG_CHUNK + o;
     uint32_t i = W.ref[pos];
     const int8_t ds = W.ds[pos], st = W.strain[pos], pp = W.pp[pos];
+    const uint8_t cm = W.cm[pos];
     int8_t et = W.et[pos], it = W.it[pos], pt = W.pt[pos];
     if (ds_on && (ds == 1 || ds == 2)) /* the count-downs up to the step of tick tc */
       ev_advance(ds, st, et, it, pt, tc - W.evt[pos] + 1 + ev_pure(ds, st, et, it, pt, pp));
@@ -196,9 +200,11 @@ __global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used
     s.pp[i] = pp;
     s.par[i] = W.par[pos];
     s.ipv[i] = W.ipv[pos];
-    s.cm[i] = W.cm[pos];
+    s.cm[i] = cm;
     s.node[i] = (int16_t)(meta.x - node_base);
-    s.ri[i] = W.ri[pos];
+    int16_t ri = W.ri[pos];
+    if (ri_on && ds >= 0 && cm != 1) ri = ri_now(rp, ri, i, W.dob[pos], tc);
+    s.ri[i] = ri;
     s.risk[i] = W.risk[pos];
     s.inf[i] = W.inf[pos];
     s.dob[i] = W.dob[pos];
@@ -208,7 +214,7 @@ __global__ void k_gather(DevWorld W, Staging s, int32_t chunk_base, int32_t used
 
 __global__ void k_cmp_counts(DevWorld W, const int32_t* tot, const uint64_t* sw, const uint64_t* bb,
                              const uint64_t* cw, const uint64_t* subw, const int32_t* subd, const int32_t* sube,
-                             int* bad) {
+                             const int32_t* subr, int* bad) {
   int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid < W.G) {
     for (int k = 0; k < TT_N; ++k)
@@ -226,6 +232,7 @@ __global__ void k_cmp_counts(DevWorld W, const int32_t* tot, const uint64_t* sw,
         if (subw[cid * LPG_NSUB + s] != W.sub_w[cid * LPG_NSUB + s]) atomicOr(bad, 16);
         if (subd[cid * LPG_NSUB + s] != W.sub_dod[cid * LPG_NSUB + s]) atomicOr(bad, 32);
         if (W.sub_evt[cid * LPG_NSUB + s] > sube[cid * LPG_NSUB + s]) atomicOr(bad, 64);
+        if (W.sub_rdt[cid * LPG_NSUB + s] > subr[cid * LPG_NSUB + s]) atomicOr(bad, 128);
       }
     }
   }
@@ -500,6 +507,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.dob, P);
   rc |= dalloc(h, &W.dod, P);
   rc |= dalloc(h, &W.evt, P);
+  rc |= dalloc(h, &W.rdt, P);
   rc |= dalloc(h, &W.ref, P);
   rc |= dalloc(h, &W.cmeta, chunk_total);
   rc |= dalloc(h, &W.qcnt, 2048);
@@ -509,6 +517,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.sub_dod, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.sub_evt, (size_t)chunk_total * LPG_NSUB);
+  rc |= dalloc(h, &W.sub_rdt, (size_t)chunk_total * LPG_NSUB);
   rc |= dalloc(h, &W.cpref, chunk_total);
   rc |= dalloc(h, &W.node_chunks[0], chunk_total);
   rc |= dalloc(h, &W.node_chunks[1], chunk_total);
@@ -792,6 +801,9 @@ extern "C" int lpg_start(lpg_handle* h) {
   /* first events of the agents in E or I at tick 0 */
   CK(cudaMemsetAsync(W.sub_evt, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
   k_init_events<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, W.evt, W.sub_evt, 0);
+  /* RI due ticks of the initial population */
+  CK(cudaMemsetAsync(W.sub_rdt, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
+  k_ri_index<<<std::max(1, h->sm_count * 8), 256, 0, st>>>(W, W.sub_rdt, 1, nullptr);
   CK(cudaGetLastError());
   for (int r = 0; r < R; ++r) {
     hr[r].started = 1;
@@ -834,7 +846,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
   }
   switch (k) {
     case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
-    case 1: k_newborns<<<dim3(h->sm_count * 2, R), 256, 0, st>>>(W); break;
+    case 1: k_newborns<<<dim3(h->sm_count * 8, R), 256, 0, st>>>(W); break;
     case 2: k_sweep<0><<<h->sweep0_blocks, LPG_SWEEP_BLOCK, 0, st>>>(W); break;
     case 3: k_dsq<<<h->sm_count * 4, 256, 0, st>>>(W, h->sweep0_blocks); break;
     case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
@@ -1008,7 +1020,7 @@ extern "C" int lpg_read_columns(lpg_handle* h, int32_t sim, const lpg_columns* c
   int rc = alloc_staging(h, s, std::max<int64_t>(r.count, 1));
   if (rc) return rc;
   k_gather<<<2048, 256, 0, h->stream>>>(h->W, s, r.chunk_base, r.used_chunks, r.node_base, r.t - 1,
-                                        (r.comps & LPG_COMP_DS) ? 1 : 0);
+                                        (r.comps & LPG_COMP_DS) ? 1 : 0, sim);
   CK(cudaGetLastError());
   const size_t n = (size_t)r.count;
 #define OUT(dst, src, esz) \
@@ -1040,13 +1052,13 @@ extern "C" int lpg_check_invariants(lpg_handle* h) {
   CK(cudaSetDevice(h->device));
   DevWorld& W = h->W;
   const int G = W.G;
-  int32_t *tot, *subd, *sube;
+  int32_t *tot, *subd, *sube, *subr;
   uint64_t *sw, *bb, *cw, *subw;
   int* bad;
   if (dalloc(h, &tot, (size_t)TT_N * G) || dalloc(h, &sw, G) || dalloc(h, &bb, (size_t)LPG_MAX_STRAINS * G) ||
       dalloc(h, &cw, W.total_chunks) || dalloc(h, &subw, (size_t)W.total_chunks * LPG_NSUB) ||
       dalloc(h, &subd, (size_t)W.total_chunks * LPG_NSUB) || dalloc(h, &sube, (size_t)W.total_chunks * LPG_NSUB) ||
-      dalloc(h, &bad, 1))
+      dalloc(h, &subr, (size_t)W.total_chunks * LPG_NSUB) || dalloc(h, &bad, 1))
     return LPG_ERR_NOMEM;
   cudaStream_t st = h->stream;
   CK(cudaMemsetAsync(tot, 0, sizeof(int32_t) * TT_N * G, st));
@@ -1059,12 +1071,14 @@ extern "C" int lpg_check_invariants(lpg_handle* h) {
   k_count<<<std::max(1, h->sm_count * 4), LPG_SWEEP_THREADS, 0, st>>>(W, tot, sw, bb, cw, subw, subd);
   CK(cudaMemsetAsync(sube, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
   k_count_events<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, sube);
-  k_cmp_counts<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, tot, sw, bb, cw, subw, subd, sube, bad);
+  CK(cudaMemsetAsync(subr, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
+  k_ri_index<<<std::max(1, h->sm_count * 8), 256, 0, st>>>(W, subr, 0, bad);
+  k_cmp_counts<<<std::max(1, h->sm_count * 4), 256, 0, st>>>(W, tot, sw, bb, cw, subw, subd, sube, subr, bad);
   CK(cudaGetLastError());
   int hb = 0;
   CK(cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  void* ps[] = {tot, sw, bb, cw, subw, subd, sube, bad};
+  void* ps[] = {tot, sw, bb, cw, subw, subd, sube, subr, bad};
   for (void* p : ps) dfree_one(h, p);
   if (hb) return fail(h, LPG_ERR_INTERNAL, "running totals differ from a recount (mask 0x%x)", hb);
   return LPG_OK;

@@ -31,6 +31,7 @@
 
 #include "lpg.h"
 #include "lpg_rng.h"
+#include "lpg_ri.h"
 
 #define LPG_CHUNK 2048
 #define LPG_SUB 128
@@ -147,7 +148,10 @@ typedef struct {
   int32_t cur_t, active, vd_tick, ri_tick;
   int32_t sia_n, sia_i0, seed_n, seed_i0;
   int64_t nb_total, count_before;
-  int32_t any_demand, pad2;
+  int32_t any_demand;
+  int32_t csr_flip;    /* the node -> chunk lists were rebuilt this tick (k_newborns fills them) */
+  int32_t used_before; /* used_chunks before this tick's new chunks */
+  int32_t pad2;
 } DevRep;
 
 /* Global device state shared by the kernels of one handle. */
@@ -159,10 +163,12 @@ typedef struct {
   /* per position */
   int8_t *ds, *strain, *et, *it, *pt, *pp, *par, *ipv;
   uint8_t* cm;
-  int16_t* ri;
+  int16_t* ri; /* where RI runs: alive, not chronically-missed agents keep the timer before their
+                  first RI tick (lpg_ri.h); the dead keep the value they died with */
   float *risk, *inf;
   int32_t *dob, *dod;
   int32_t* evt; /* agents in E or I: tick of the next disease-state step that is an event */
+  int32_t* rdt; /* RI due tick (lpg_ri.h), LPG_NO_DOD for the chronically missed or where RI does not run */
   uint32_t* ref;
   /* per chunk */
   int4* cmeta; /* per chunk: x node, y fill, z tick of the newborns written into it, w offset of the first */
@@ -173,6 +179,9 @@ typedef struct {
   int32_t* sub_dod;   /* [chunk][LPG_NSUB] earliest date of death of the sub-block's alive agents
                          (LPG_NO_DOD when it has none); deaths on a VD tick need only the
                          sub-blocks whose earliest date has come */
+  int32_t* sub_rdt;   /* [chunk][LPG_NSUB] earliest RI due tick of the sub-block's alive, not
+                         chronically-missed agents, a lower bound (LPG_NO_DOD when none): RI
+                         ticks read only the sub-blocks with an agent due */
   uint64_t* cpref;    /* selection: node-local prefix of chunk weights, CSR order */
   int32_t* node_chunks[2];
   int32_t* node_chunk_start[2]; /* per sim: n_nodes + 1 entries at csr_base */

@@ -80,6 +80,21 @@ __device__ __forceinline__ void ev_advance(int8_t ds, int8_t strain, int8_t& et,
 }
 __device__ __forceinline__ unsigned long long neg64(uint64_t w) { return (unsigned long long)(0ULL - w); }
 
+/* RI runs for the simulation: RI_ABM among the components and vx_prob_ri
+ * set (model.py:1920-1923).  Only then do the timers count down. */
+__device__ __forceinline__ bool ri_runs(const DevRep* rp) { return (rp->comps & LPG_COMP_RI) && rp->ri_enabled; }
+/* RI due tick of an agent from its base timer u, reference index and date
+ * of birth (lpg_ri.h). */
+__device__ __forceinline__ int32_t ri_due_of(const DevRep* rp, int16_t u, uint32_t ref, int32_t dob) {
+  const int32_t s = rp->ri_step;
+  return lpg_ri_due_tick(u, lpg_ri_first((int64_t)ref >= rp->count0, dob, s), s);
+}
+/* The reference's ri_timer of an agent once the RI ticks up to t_last have run. */
+__device__ __forceinline__ int16_t ri_now(const DevRep* rp, int16_t u, uint32_t ref, int32_t dob, int32_t t_last) {
+  const int32_t s = rp->ri_step;
+  return lpg_ri_value(u, lpg_ri_applied(lpg_ri_first((int64_t)ref >= rp->count0, dob, s), t_last, s), s);
+}
+
 __device__ __forceinline__ int32_t* RES(const DevRep* rp, int k, int t) {
   int wide = (k == RS_EBS || k == RS_IBS || k == RS_NEWEXPBS || k == RS_RINEWEXPBS || k == RS_SIANEWEXPBS);
   return rp->res + rp->res_off[k] + (int64_t)t * rp->n_nodes * (wide ? rp->ns : 1);
@@ -87,8 +102,7 @@ __device__ __forceinline__ int32_t* RES(const DevRep* rp, int k, int t) {
 
 /* Newborn lifespan: restates laser_core's KaplanMeierEstimator for age 0
  * (model.py:1725).  Same arithmetic as the oracle's lpo_km_newborn. */
-__device__ int32_t km_newborn(const DevRep* rp, int32_t t, uint64_t slot) {
-  const int64_t* cum = rp->km;
+__device__ int32_t km_newborn(const DevRep* rp, int32_t t, uint64_t slot, const int64_t* cum) {
   int32_t top = rp->km_max_year < rp->km_len - 1 ? rp->km_max_year : rp->km_len - 1;
   int64_t total = cum[top];
   int32_t y = top;
@@ -162,6 +176,7 @@ __global__ void k_begin(DevWorld W) {
     rp->nb_total = 0;
     rp->count_before = count;
     rp->any_demand = 0;
+    rp->csr_flip = 0;
     s_active = active;
     s_vd = vd;
     s_t = t;
@@ -234,43 +249,33 @@ __global__ void k_begin(DevWorld W) {
   __syncthreads();
   if (!s_ok || carry_b == 0) return;
 
-  int cur = rp->csr_cur;
+  const int cur = rp->csr_cur;
+  const int32_t* so = W.node_chunk_start[cur] + rp->csr_base;
+  const int32_t* lo_ = W.node_chunks[cur] + rp->chunk_base;
+  const int32_t used0 = rp->used_chunks;
   if (carry_c > 0) {
-    /* rebuild the node -> chunk lists into the other buffer */
-    int nw = 1 - cur;
-    const int32_t* so = W.node_chunk_start[cur] + rp->csr_base;
-    int32_t* sn = W.node_chunk_start[nw] + rp->csr_base;
-    const int32_t* lo_ = W.node_chunks[cur] + rp->chunk_base;
-    int32_t* ln = W.node_chunks[nw] + rp->chunk_base;
+    /* the new node -> chunk starts, in the other buffer; k_newborns copies
+     * the lists (many CTAs) before any later kernel reads them */
+    int32_t* sn = W.node_chunk_start[1 - cur] + rp->csr_base;
     for (int i = threadIdx.x; i < n; i += blockDim.x) sn[i] = so[i] + (int32_t)W.ksel[nb + i];
     if (threadIdx.x == 0) sn[n] = so[n] + (int32_t)carry_c;
-    __syncthreads();
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (int i = wid; i < n; i += nwarp) {
-      int32_t a0 = so[i], a1 = so[i + 1], d0 = sn[i];
-      for (int k = lane; k < a1 - a0; k += 32) ln[d0 + k] = lo_[a0 + k];
-      int32_t added = (sn[i + 1] - sn[i]) - (a1 - a0);
-      for (int k = lane; k < added; k += 32) {
-        int32_t cid = rp->chunk_base + rp->used_chunks + (int32_t)W.ksel[nb + i] + k;
-        ln[d0 + (a1 - a0) + k] = cid;
-        W.cmeta[cid] = make_int4(nb + i, 0, -1, 0);
-        W.chunk_w[cid] = 0;
-        for (int s = 0; s < LPG_NSUB; ++s) W.sub_w[(int64_t)cid * LPG_NSUB + s] = 0;
-      }
-    }
-    __syncthreads();
-    cur = nw;
   }
-  /* chunk fills and newborn markers */
-  const int32_t* st = W.node_chunk_start[cur] + rp->csr_base;
-  const int32_t* ls = W.node_chunks[cur] + rp->chunk_base;
+  /* chunk fills and newborn markers.  Chunk k of node i is entry k of its
+   * current list, or its (k - listed)-th new chunk: new chunks are numbered
+   * from used0 in node order (W.ksel holds the count before each node). */
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     int g = nb + i;
     int64_t b = W.ev[(int64_t)EV_BIRTHS * G + g];
     if (b == 0) continue;
     int64_t li0 = W.nb_li0[g], newc = li0 + b;
+    const int32_t nold = so[i + 1] - so[i];
     for (int64_t k = li0 / LPG_CHUNK; k <= (newc - 1) / LPG_CHUNK; ++k) {
-      int32_t cid = ls[st[i] + k];
+      const bool added = k >= nold;
+      const int32_t cid = added ? rp->chunk_base + used0 + (int32_t)W.ksel[g] + (int32_t)(k - nold) : lo_[so[i] + k];
+      if (added) {
+        W.chunk_w[cid] = 0;
+        for (int s = 0; s < LPG_NSUB; ++s) W.sub_w[(int64_t)cid * LPG_NSUB + s] = 0;
+      }
       int64_t f = newc - k * LPG_CHUNK;
       W.cmeta[cid] = make_int4(nb + i, (int32_t)(f < LPG_CHUNK ? f : LPG_CHUNK), t,
                                (k == li0 / LPG_CHUNK) ? (int32_t)(li0 % LPG_CHUNK) : 0);
@@ -279,7 +284,9 @@ __global__ void k_begin(DevWorld W) {
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    rp->csr_cur = cur;
+    rp->csr_cur = carry_c > 0 ? 1 - cur : cur;
+    rp->csr_flip = carry_c > 0;
+    rp->used_before = used0;
     rp->used_chunks += (int32_t)carry_c;
     rp->count += carry_b;
     rp->nb_total = carry_b;
@@ -287,80 +294,188 @@ __global__ void k_begin(DevWorld W) {
 }
 
 /* ------------------------------------------------------------------------ */
-__global__ void k_newborns(DevWorld W) {
+/* Warp reductions over runs of consecutive lanes that hold the same key
+ * (equal keys only ever form one contiguous run).  run_merge_bits: bit k set
+ * when the lane 2^k above holds the same key; the run_* reductions then
+ * leave the run's total on its first lane (run_head).  All 32 lanes call. */
+__device__ __forceinline__ uint32_t run_merge_bits(uint64_t key) {
+  const int lane = threadIdx.x & 31;
+  uint32_t m = 0;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const uint64_t o = __shfl_down_sync(FULLMASK, key, 1 << k);
+    if (lane + (1 << k) < 32 && o == key) m |= 1u << k;
+  }
+  return m;
+}
+__device__ __forceinline__ bool run_head(uint64_t key) {
+  const uint64_t p = __shfl_up_sync(FULLMASK, key, 1);
+  return (threadIdx.x & 31) == 0 || p != key;
+}
+__device__ __forceinline__ uint64_t run_sum_u64(uint64_t v, uint32_t m) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const uint64_t y = __shfl_down_sync(FULLMASK, v, 1 << k);
+    if ((m >> k) & 1u) v += y;
+  }
+  return v;
+}
+__device__ __forceinline__ int32_t run_sum_i32(int32_t v, uint32_t m) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int32_t y = __shfl_down_sync(FULLMASK, v, 1 << k);
+    if ((m >> k) & 1u) v += y;
+  }
+  return v;
+}
+__device__ __forceinline__ int32_t run_min_i32(int32_t v, uint32_t m) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int32_t y = __shfl_down_sync(FULLMASK, v, 1 << k);
+    if ((m >> k) & 1u) v = min(v, y);
+  }
+  return v;
+}
+
+/* Newborns of a VD tick (model.py:1719-1733), one thread each, after k_begin
+ * placed them: rows from the unborn pool, the Kaplan-Meier date of death,
+ * and the running totals and indexes, summed over each warp's runs of
+ * newborns that share a node, chunk or sub-block before one atomic per run.
+ * On ticks that added chunks it first copies the node -> chunk lists into
+ * the buffer k_begin switched to (one warp per node).  Chunk k of a node is
+ * entry k of its previous list or its (k - listed)-th new chunk, numbered
+ * from used_before in node order (W.ksel: new chunks before each node). */
+#define LPG_NB_SMEM 4096
+#define LPG_KM_SMEM 256
+__global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
   const DevRep* rp = &W.reps[blockIdx.y];
   if (!rp->active || !rp->vd_tick || rp->nb_total == 0) return;
+  __shared__ int64_t s_end[LPG_NB_SMEM];
+  __shared__ int64_t s_km[LPG_KM_SMEM];
   const int n = rp->n_nodes, nb = rp->node_base, t = rp->cur_t, G = W.G;
+  const int lane = threadIdx.x & 31;
   const int64_t total = rp->nb_total;
-  const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
-  const int32_t* ls = W.node_chunks[rp->csr_cur] + rp->chunk_base;
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-      int mid = (lo + hi) >> 1;
-      if (W.nb_end[nb + mid] > j) hi = mid; else lo = mid + 1;
+  const int cur = rp->csr_cur, prev = rp->csr_flip ? 1 - cur : cur;
+  const int32_t* so = W.node_chunk_start[prev] + rp->csr_base;
+  const int32_t* lo_ = W.node_chunks[prev] + rp->chunk_base;
+  const int32_t add0 = rp->chunk_base + rp->used_before;
+  if (rp->csr_flip) {
+    const int32_t* sn = W.node_chunk_start[cur] + rp->csr_base;
+    int32_t* ln = W.node_chunks[cur] + rp->chunk_base;
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = gw; i < n; i += nw) {
+      const int32_t a0 = so[i], nold = so[i + 1] - a0, d0 = sn[i], nnew = sn[i + 1] - d0;
+      const int32_t c0 = add0 + (int32_t)W.ksel[nb + i];
+      for (int32_t k = lane; k < nnew; k += 32) ln[d0 + k] = k < nold ? lo_[a0 + k] : c0 + (k - nold);
     }
-    int g = nb + lo;
-    int64_t bstart = W.nb_end[g] - W.ev[(int64_t)EV_BIRTHS * G + g];
-    int64_t li = W.nb_li0[g] + (j - bstart);
-    int32_t cid = ls[st[lo] + li / LPG_CHUNK];
-    int64_t off = li % LPG_CHUNK;
-    int64_t pos = (int64_t)cid * LPG_CHUNK + off;
-    int64_t ref = rp->count_before + j;
-    int64_t q = ref - rp->count0;
-    W.et[pos] = rp->pl_et[q];
-    W.it[pos] = rp->pl_it[q];
-    W.pt[pos] = rp->pl_pt[q];
-    W.strain[pos] = rp->pl_strain[q];
-    int8_t pp = rp->pl_pp[q], par = rp->pl_par[q];
-    W.pp[pos] = pp;
-    W.par[pos] = par;
-    W.ipv[pos] = rp->pl_ipv[q];
-    W.cm[pos] = rp->pl_cm[q];
-    W.ri[pos] = rp->pl_ri[q];
-    float risk = rp->pl_risk[q];
-    W.risk[pos] = risk;
-    W.inf[pos] = rp->pl_inf[q];
-    W.dob[pos] = t;
-    const int32_t dod = t + km_newborn(rp, t, (uint64_t)ref);
-    W.dod[pos] = dod;
-    atomicMin(&W.sub_dod[(int64_t)cid * LPG_NSUB + off / LPG_SUB], dod);
-    W.ref[pos] = (uint32_t)ref;
-    W.ds[pos] = 0;
-    uint64_t w = fix_risk(risk);
-    atomicAdd(&W.tot[(int64_t)TT_S * G + g], 1);
-    if (w) {
-      atomicAdd((unsigned long long*)&W.sw[g], (unsigned long long)w);
-      atomicAdd((unsigned long long*)&W.chunk_w[cid], (unsigned long long)w);
-      atomicAdd((unsigned long long*)&W.sub_w[(int64_t)cid * LPG_NSUB + off / LPG_SUB], (unsigned long long)w);
+  }
+  const bool end_sm = n <= LPG_NB_SMEM, km_sm = rp->km_len <= LPG_KM_SMEM;
+  if (end_sm)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s_end[i] = W.nb_end[nb + i];
+  if (km_sm)
+    for (int i = threadIdx.x; i < rp->km_len; i += blockDim.x) s_km[i] = rp->km[i];
+  __syncthreads();
+  const int64_t* nbe = end_sm ? s_end : W.nb_end + nb;
+  const int64_t* km = km_sm ? s_km : rp->km;
+  const bool ri_on = ri_runs(rp);
+  for (int64_t j0 = (int64_t)blockIdx.x * blockDim.x;; j0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = j0 + threadIdx.x;
+    if (__all_sync(FULLMASK, j >= total)) break;
+    const bool on = j < total;
+    uint64_t kg = ~0ULL - (uint64_t)lane, kc = kg, ks = kg; /* idle lanes: keys of their own */
+    uint64_t w = 0;
+    int32_t dod = LPG_NO_DOD, rdt = LPG_NO_DOD, one = 0;
+    int g = 0;
+    int32_t cid = 0;
+    if (on) {
+      int lo = 0, hi = n - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (nbe[mid] > j) hi = mid; else lo = mid + 1;
+      }
+      g = nb + lo;
+      const int64_t bstart = nbe[lo] - W.ev[(int64_t)EV_BIRTHS * G + g];
+      const int64_t li = W.nb_li0[g] + (j - bstart);
+      const int64_t k = li / LPG_CHUNK;
+      const int32_t nold = so[lo + 1] - so[lo];
+      cid = k < nold ? lo_[so[lo] + k] : add0 + (int32_t)W.ksel[g] + (int32_t)(k - nold);
+      const int64_t off = li % LPG_CHUNK;
+      const int64_t pos = (int64_t)cid * LPG_CHUNK + off;
+      const int64_t ref = rp->count_before + j;
+      const int64_t q = ref - rp->count0;
+      W.et[pos] = rp->pl_et[q];
+      W.it[pos] = rp->pl_it[q];
+      W.pt[pos] = rp->pl_pt[q];
+      W.strain[pos] = rp->pl_strain[q];
+      const int8_t pp = rp->pl_pp[q], par = rp->pl_par[q];
+      const uint8_t cm = rp->pl_cm[q];
+      const int16_t ri = rp->pl_ri[q];
+      W.pp[pos] = pp;
+      W.par[pos] = par;
+      W.ipv[pos] = rp->pl_ipv[q];
+      W.cm[pos] = cm;
+      W.ri[pos] = ri;
+      const float risk = rp->pl_risk[q];
+      W.risk[pos] = risk;
+      W.inf[pos] = rp->pl_inf[q];
+      W.dob[pos] = t;
+      dod = t + km_newborn(rp, t, (uint64_t)ref, km);
+      W.dod[pos] = dod;
+      W.ref[pos] = (uint32_t)ref;
+      W.ds[pos] = 0;
+      if (ri_on && cm != 1) rdt = ri_due_of(rp, ri, (uint32_t)ref, t);
+      W.rdt[pos] = rdt;
+      w = fix_risk(risk);
+      one = 1;
+      if (pp == 1) atomicAdd(&W.tot[(int64_t)TT_POTP * G + g], 1);
+      if (par == 1) atomicAdd(&W.tot[(int64_t)TT_P * G + g], 1);
+      kg = (uint64_t)g;
+      kc = (uint64_t)cid;
+      ks = (uint64_t)cid * LPG_NSUB + (uint64_t)(off / LPG_SUB);
     }
-    if (pp == 1) atomicAdd(&W.tot[(int64_t)TT_POTP * G + g], 1);
-    if (par == 1) atomicAdd(&W.tot[(int64_t)TT_P * G + g], 1);
+    const uint32_t mg = run_merge_bits(kg), mc = run_merge_bits(kc), ms = run_merge_bits(ks);
+    const bool hg = run_head(kg), hc = run_head(kc), hs = run_head(ks);
+    const uint64_t wg = run_sum_u64(w, mg), wc = run_sum_u64(w, mc), wsb = run_sum_u64(w, ms);
+    const int32_t ng = run_sum_i32(one, mg);
+    const int32_t dmin = run_min_i32(dod, ms), rmin = run_min_i32(rdt, ms);
+    if (on && hg) {
+      atomicAdd(&W.tot[(int64_t)TT_S * G + g], ng);
+      if (wg) atomicAdd((unsigned long long*)&W.sw[g], (unsigned long long)wg);
+    }
+    if (on && hc && wc) atomicAdd((unsigned long long*)&W.chunk_w[cid], (unsigned long long)wc);
+    if (on && hs) {
+      atomicMin(&W.sub_dod[ks], dmin);
+      if (rmin != LPG_NO_DOD) atomicMin(&W.sub_rdt[ks], rmin);
+      if (wsb) atomicAdd((unsigned long long*)&W.sub_w[ks], (unsigned long long)wsb);
+    }
   }
 }
 
-/* Fused sweep over every agent slot, in two launches per tick.
+/* The sweeps, two launches per tick.
  *   PHASE 0: deaths (get_deaths, model.py:1767-1781) on VD ticks, and the
- *            queue of agents in E or I for disease progression (k_dsq).
+ *            queue of agents in E or I whose disease-state event is due
+ *            (k_dsq); through the sub-block indexes (sweep_direct).
  *   PHASE 1: routine immunisation (fast_ri, model.py:1784-1855) and SIA
  *            campaigns (fast_sia, :1994-2060), on the ticks that have them,
  *            after progression and the seed schedule as in default_run_order.
+ *            RI alone goes through the RI due index (ri_direct); SIA days
+ *            stage every slot.
  *
- * Warp-specialised pipeline.  Each CTA owns a contiguous range of chunks.
- * One producer warp stages chunk metadata and the columns every agent needs
- * into shared memory with 1-D bulk copies (cp.async.bulk; completion on a
- * "full" mbarrier), through a ring of LPG_NST stages; eight consumer warps
- * process a stage and release it on an "empty" mbarrier.  A stage holds k
- * consecutive chunks, k = as many as fit in LPG_COL_BYTES given the tick's
- * columns: state bytes always; date_of_death on VD ticks; ri_timer and
- * chronically_missed on RI ticks; chronically_missed and date_of_birth on
- * SIA days.  Each consumer thread tests 16 slots at a time with SIMD byte
- * compares and appends the agents that need work to its CTA's queue slab;
- * on ticks that stage only state bytes, a warp whose 512 slots hold no
- * agent in E or I moves on after one vote.  Each consumer warp releases a
- * stage with one arrival.  There is no CTA-wide barrier in the steady state.
- * Every mbarrier wait is bounded; on a timeout the kernel raises an error,
- * stops issuing, waits (bounded) for the copies it issued and returns. */
+ * The staged path is a warp-specialised pipeline.  Each CTA owns a
+ * contiguous range of chunks.  One producer warp stages chunk metadata and
+ * the columns every agent needs into shared memory with 1-D bulk copies
+ * (cp.async.bulk; completion on a "full" mbarrier), through a ring of
+ * LPG_NST stages; eight consumer warps process a stage and release it on an
+ * "empty" mbarrier.  A stage holds k consecutive chunks, k = as many as fit
+ * in LPG_COL_BYTES given the day's columns: state bytes,
+ * chronically_missed and date_of_birth, and the RI due ticks when RI falls
+ * on the same day.  Each consumer thread tests 16 slots at a time with SIMD
+ * byte compares and appends the agents that need work to its CTA's queue
+ * slab.  Each consumer warp releases a stage with one arrival.  There is no
+ * CTA-wide barrier in the steady state.  Every mbarrier wait is bounded; on
+ * a timeout the kernel raises an error, stops issuing, waits (bounded) for
+ * the copies it issued and returns. */
 #define LPG_NST 4
 #define LPG_META_BYTES 256
 #define LPG_COL_BYTES (24 * 1024)
@@ -425,7 +540,7 @@ struct SweepPlan {
 
 /* Staged bytes per chunk for a simulation's flags. */
 __device__ __forceinline__ int chunk_bytes(uint8_t f) {
-  return LPG_CHUNK + ((f & SF_VD) ? 4 * LPG_CHUNK : 0) + ((f & SF_RI) ? 2 * LPG_CHUNK : 0) +
+  return LPG_CHUNK + ((f & SF_VD) ? 4 * LPG_CHUNK : 0) + ((f & SF_RI) ? 4 * LPG_CHUNK : 0) +
          ((f & (SF_RI | SF_SIA)) ? LPG_CHUNK : 0) + ((f & SF_SIA) ? 4 * LPG_CHUNK : 0);
 }
 /* Chunks per stage (k consecutive chunks: each column is one contiguous copy). */
@@ -434,7 +549,7 @@ __device__ __forceinline__ int stage_chunks(uint8_t f) {
   return k < LPG_PLAIN_GROUP ? k : LPG_PLAIN_GROUP;
 }
 struct StageLayout {
-  int ds, dod, ri, cm, dob;
+  int ds, dod, rdt, cm, dob;
 };
 __device__ __forceinline__ StageLayout stage_layout(uint8_t f, int k) {
   StageLayout L;
@@ -443,8 +558,8 @@ __device__ __forceinline__ StageLayout stage_layout(uint8_t f, int k) {
   off += k * LPG_CHUNK;
   L.dod = off;
   if (f & SF_VD) off += k * 4 * LPG_CHUNK;
-  L.ri = off;
-  if (f & SF_RI) off += k * 2 * LPG_CHUNK;
+  L.rdt = off;
+  if (f & SF_RI) off += k * 4 * LPG_CHUNK;
   L.cm = off;
   if (f & (SF_RI | SF_SIA)) off += k * LPG_CHUNK;
   L.dob = off;
@@ -596,7 +711,7 @@ __device__ __forceinline__ void sweep_a16(uint64_t* slab, uint32_t* s_cnt, DevWo
  * is a range test on the old value. */
 __device__ __forceinline__ void sweep_b16(uint64_t* slab, uint32_t* s_cnt, DevWorld& W, bool on, const DevRep* rp,
                                           uint8_t fl, int t, int ni, int64_t pos0, int off, uint4 sv,
-                                          const uint8_t* scm, const int16_t* sri, const int32_t* sdob) {
+                                          const uint8_t* scm, const int32_t* srdt, const int32_t* sdob) {
   uint32_t fri = 0;
   uint32_t fsia[LPG_MAX_SIA_PER_DAY] = {0, 0, 0, 0, 0, 0, 0, 0};
   int nsia_used = 0;
@@ -615,27 +730,15 @@ __device__ __forceinline__ void sweep_b16(uint64_t* slab, uint32_t* s_cnt, DevWo
       any_reach |= reachw[q];
     }
     if (any_reach && (fl & SF_RI)) {
-      const int step = rp->ri_step;
-      const uint32_t step2 = ((uint32_t)step & 0xffffu) * 0x00010001u;
-      uint4 r4[2];
-      r4[0] = *reinterpret_cast<const uint4*>(sri + off);
-      r4[1] = *reinterpret_cast<const uint4*>(sri + off + 8);
-      uint32_t* rw = reinterpret_cast<uint32_t*>(r4);
-      const uint32_t lo2 = t == step ? 0x00000000u : 0x00010001u; /* eligible: lo <= old <= step */
-      const uint32_t hi2 = step2;
+      /* RI on an SIA day (staged): the agents whose RI due tick is today */
+      const int4* r4 = reinterpret_cast<const int4*>(srdt + off);
 #pragma unroll
-      for (int h = 0; h < 8; ++h) {
-        /* 16-bit lanes of slots 2h, 2h+1: byte masks of the reach word */
-        const uint32_t rb = reachw[h >> 1] >> (16 * (h & 1));
-        const uint32_t m2 = ((rb & 0xffu) ? 0x0000ffffu : 0u) | ((rb & 0xff00u) ? 0xffff0000u : 0u);
-        const uint32_t old = rw[h];
-        const uint32_t nw = __vsub2(old, step2);
-        const uint32_t el = __vcmpges2(old, lo2) & __vcmples2(old, hi2) & m2;
-        rw[h] = (nw & m2) | (old & ~m2);
-        fri |= ((el & 1u) << (2 * h)) | (((el >> 16) & 1u) << (2 * h + 1));
+      for (int q = 0; q < 4; ++q) {
+        const int4 d = r4[q];
+        const int32_t dd[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) fri |= (uint32_t)(((reachw[q] >> (8 * j)) & 1u) && dd[j] == t) << (4 * q + j);
       }
-      *reinterpret_cast<uint4*>(W.ri + pos0) = r4[0];
-      *reinterpret_cast<uint4*>(W.ri + pos0 + 8) = r4[1];
     }
     if (any_reach && (fl & SF_SIA)) {
       const int4* d4 = reinterpret_cast<const int4*>(sdob + off);
@@ -698,6 +801,30 @@ __device__ __forceinline__ uint32_t ev_due16(const DevWorld& W, int64_t pos0, ui
         if (ee[j] <= t) due |= 1u << k;
         else nmin = min(nmin, ee[j]);
       }
+    }
+  }
+  return due;
+}
+
+/* Of one thread's 16 slots at pos0 (state bytes v): the alive agents whose
+ * RI due tick (rdt: LPG_NO_DOD for the chronically missed and where RI does
+ * not run) is t (bit mask), and the earliest due tick after t among the
+ * others (nmin, LPG_NO_DOD if none). */
+__device__ __forceinline__ uint32_t ri_due16(const DevWorld& W, int64_t pos0, uint4 v, int t, int32_t& nmin) {
+  const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+  if ((__vcmpltu4(wv[0], 0x80808080u) | __vcmpltu4(wv[1], 0x80808080u) | __vcmpltu4(wv[2], 0x80808080u) |
+       __vcmpltu4(wv[3], 0x80808080u)) == 0)
+    return 0;
+  uint32_t due = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int4 d = __ldcg(reinterpret_cast<const int4*>(W.rdt + pos0) + q);
+    const int32_t dd[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if ((wv[q] >> (8 * j + 7)) & 1u) continue; /* dead */
+      if (dd[j] == t) due |= 1u << (4 * q + j);
+      else if (dd[j] > t) nmin = min(nmin, dd[j]);
     }
   }
   return due;
@@ -824,6 +951,80 @@ __device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t*
   }
 }
 
+/* k_sweep<1> on an RI tick without SIA, over one simulation's sub-blocks
+ * [sb0, sb0 + nsb), in windows of LPG_DUE_MAX sub-blocks: the CTA lists the
+ * sub-blocks whose earliest RI due tick (sub_rdt) has come, then 8 lanes
+ * per listed sub-block queue the agents due now (fast_ri, model.py:1825-1854:
+ * alive, not chronically missed, the subtraction landing in the window) and
+ * write the sub-block's next due tick.  No timer is written: the column
+ * keeps each agent's base (lpg_ri.h).  All threads of the CTA run it. */
+__device__ __noinline__ void ri_direct(DevWorld& W, const DevRep* rp, uint64_t* slab, uint32_t* s_cnt, int64_t sb0,
+                                       int64_t nsb, int t, uint32_t* s_due, int* s_ndue) {
+  const int lane = threadIdx.x & 31;
+  uint32_t n_due = 0;
+  for (int64_t wb = 0; wb < nsb; wb += LPG_DUE_MAX) {
+    const int nw = (int)min((int64_t)LPG_DUE_MAX, nsb - wb);
+    if (threadIdx.x == 0) {
+      *s_ndue = 0;
+      atomicAdd(&W.ctr[LPG_CTR_RI_INDEX], (unsigned long long)nw);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x * 4; q < nw; q += blockDim.x * 4) {
+      const int4 e4 = __ldcg(reinterpret_cast<const int4*>(W.sub_rdt + sb0 + wb + q));
+      const int32_t ee[4] = {e4.x, e4.y, e4.z, e4.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (ee[j] <= t && q + j < nw) {
+          const int at = atomicAdd(s_ndue, 1);
+          s_due[at] = (uint32_t)(q + j);
+        }
+      }
+    }
+    __syncthreads();
+    const int ndue = *s_ndue;
+    const int per_pass = (blockDim.x / 32) * 4;
+    for (int base = 0; base < ndue; base += per_pass) {
+      const int item = base + (threadIdx.x >> 5) * 4 + (lane >> 3);
+      const bool on = item < ndue;
+      const int64_t sb = sb0 + wb + (on ? s_due[item] : 0u);
+      const int64_t pos0 = sb * LPG_SUB + (int64_t)(lane & 7) * 16;
+      int32_t nmin = LPG_NO_DOD;
+      uint32_t due = 0;
+      if (on) {
+        n_due += (lane & 7) == 0 ? 1u : 0u;
+        due = ri_due16(W, pos0, ldg_stream16(W.ds + pos0), t, nmin);
+      }
+      nmin = sub8_min(nmin);
+      if (on && (lane & 7) == 0) W.sub_rdt[sb] = nmin;
+      if (__ballot_sync(FULLMASK, due != 0)) {
+        uint32_t at = slab_reserve(s_cnt, __popc(due));
+        while (due) {
+          const int k = __ffs(due) - 1;
+          due &= due - 1;
+          slab[at++] = q_entry(pos0 + k, QB_RI, 0);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  n_due = __reduce_add_sync(FULLMASK, n_due);
+  if (lane == 0 && n_due) atomicAdd(&W.ctr[LPG_CTR_RI_DUE], (unsigned long long)n_due);
+}
+
+/* The first work item at or after w whose simulation is staged (dense), or w1. */
+__device__ __forceinline__ int32_t dense_from(const SweepPlan& P, int32_t w, int32_t w1) {
+  while (w < w1) {
+    int lo = 0, hi = P.nreps - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (P.off[mid] <= w) lo = mid; else hi = mid - 1;
+    }
+    if (P.flags[lo] & SF_DENSE) return w;
+    w = min(w1, P.off[lo + 1]);
+  }
+  return w1;
+}
+
 template <int PHASE>
 __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   extern __shared__ __align__(128) uint8_t sm_stage[];
@@ -850,7 +1051,8 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
         } else {
           if (rp->ri_tick) f |= SF_RI;
           if (rp->sia_n > 0) f |= SF_SIA;
-          if (f) f |= SF_WORK | SF_DENSE;
+          if (f) f |= SF_WORK;
+          if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due index */
         }
       }
       P.flags[r] = f;
@@ -878,6 +1080,25 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   uint64_t* slab = W.evq + (int64_t)w0 * LPG_CHUNK;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
+  if (PHASE == 1) {
+    /* Simulations with RI today and no SIA: the due sub-blocks only
+     * (ri_direct), all threads, with the list in the stage buffers before
+     * any bulk copy reaches them. */
+    int32_t w = w0;
+    while (w < w1) {
+      int r;
+      (void)stage_end(P, w, w1, &r);
+      const int32_t we = min(w1, P.off[r + 1]);
+      if ((P.flags[r] & (SF_WORK | SF_DENSE)) == SF_WORK) {
+        const int64_t sb0 = (P.cbase[r] + (int64_t)(w - P.off[r])) * LPG_NSUB;
+        ri_direct(W, &W.reps[r], slab, &s_qcnt, sb0, (int64_t)(we - w) * LPG_NSUB, P.tick[r],
+                  reinterpret_cast<uint32_t*>(sm_stage), &s_ndue);
+      }
+      w = we;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+  }
   if (PHASE == 0) {
     /* No staging: every warp reads the sub-block indexes of its range and
      * only the slots of sub-blocks with an event or a death due
@@ -898,7 +1119,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   } else if (warp == LPG_SWEEP_CONSUMERS / 32) {
     /* ---- producer warp: one lane issues the stages ---- */
     if (lane == 0 && w0 < w1) {
-      int32_t wp = w0;
+      int32_t wp = dense_from(P, w0, w1);
       int32_t i = 0;
       for (; wp < w1; ++i) {
         const int b = i % LPG_NST;
@@ -921,16 +1142,16 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
         bulk_g2s(dst, W.cmeta + cid, (uint32_t)nc * 16u, &full[b]);
         bulk_g2s(cols + L.ds, W.ds + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
         if (f & SF_VD) bulk_g2s(cols + L.dod, W.dod + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
-        if (f & SF_RI) bulk_g2s(cols + L.ri, W.ri + cid * LPG_CHUNK, (uint32_t)nc * 2 * LPG_CHUNK, &full[b]);
+        if (f & SF_RI) bulk_g2s(cols + L.rdt, W.rdt + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
         if (f & (SF_RI | SF_SIA)) bulk_g2s(cols + L.cm, W.cm + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
         if (f & SF_SIA) bulk_g2s(cols + L.dob, W.dob + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
-        wp = we;
+        wp = dense_from(P, we, w1);
       }
       s_issued = i;
     }
   } else if (w0 < w1) {
     /* ---- consumer warps: 16-slot groups of the stage, 256 groups per pass ---- */
-    int32_t wc = w0;
+    int32_t wc = dense_from(P, w0, w1);
     for (int32_t i = 0; wc < w1; ++i) {
       const int b = i % LPG_NST;
       const uint32_t parity = (uint32_t)(i / LPG_NST) & 1u;
@@ -979,7 +1200,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[b]);
-        wc = we;
+        wc = dense_from(P, we, w1);
         continue;
       }
       for (int gb = 0; gb < ngroups; gb += LPG_SWEEP_CONSUMERS) {
@@ -1003,13 +1224,13 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
         } else {
           const int ni = meta[kk].x - rp->node_base;
           sweep_b16(slab, &s_qcnt, W, on, rp, fl, t, ni, pos0, off, sv, cols + L.cm + kk * LPG_CHUNK,
-                    reinterpret_cast<const int16_t*>(cols + L.ri + kk * 2 * LPG_CHUNK),
+                    reinterpret_cast<const int32_t*>(cols + L.rdt + kk * 4 * LPG_CHUNK),
                     reinterpret_cast<const int32_t*>(cols + L.dob + kk * 4 * LPG_CHUNK));
         }
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[b]);
-      wc = we;
+      wc = dense_from(P, we, w1);
     }
   }
   __syncthreads();
@@ -1036,6 +1257,20 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
 __device__ __forceinline__ void warp_add(int32_t* p, unsigned peers, int32_t v) {
   const int32_t tot = __reduce_add_sync(peers, v);
   if ((threadIdx.x & 31) == __ffs(peers) - 1 && tot) atomicAdd(p, tot);
+}
+/* Sum of 64-bit values over the lanes of peers, exact modulo 2^64 (four
+ * 16-bit parts, each summed in 32 bits without overflow). */
+__device__ __forceinline__ uint64_t warp_sum_u64(unsigned peers, uint64_t w) {
+  uint64_t tot = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    tot += (uint64_t)__reduce_add_sync(peers, (uint32_t)((w >> (16 * k)) & 0xffffu)) << (16 * k);
+  return tot;
+}
+/* The lowest lane of peers subtracts the peers' total weight from *p. */
+__device__ __forceinline__ void warp_sub_w(unsigned long long* p, unsigned peers, uint64_t w) {
+  const uint64_t tot = warp_sum_u64(peers, w);
+  if ((threadIdx.x & 31) == __ffs(peers) - 1 && tot) atomicAdd(p, neg64(tot));
 }
 
 /* Entry q of the queue of sweep PHASE (prefix of the slab sizes in s_pre). */
@@ -1118,6 +1353,8 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
         } else if (s == 3) {
           dR = -1;
         }
+        /* the RI timer stops at death: its value after the RI ticks before t */
+        if (ri_runs(rp) && W.cm[pos] != 1) W.ri[pos] = ri_now(rp, W.ri[pos], W.ref[pos], W.dob[pos], t - 1);
         if (W.pp[pos] == 1) dPP -= 1;
         if (W.par[pos] == 1) dP -= 1;
       } else {
@@ -1220,6 +1457,11 @@ __global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
     int32_t sv[LPG_MAX_SIA_PER_DAY] = {0, 0, 0, 0, 0, 0, 0, 0};
     int32_t sp[LPG_MAX_SIA_PER_DAY] = {0, 0, 0, 0, 0, 0, 0, 0};
     int nsia = 0;
+    /* an exposure's next event tick and weight, summed per sub-block, chunk
+     * and node over the warp before the atomics */
+    int32_t ex_e1 = LPG_NO_DOD;
+    uint64_t ex_w = 0;
+    int64_t ex_pos = 0;
     if (on) {
       const uint64_t e = q_get(W, 1, s_pre, nslabs, q);
       const int64_t pos = (int64_t)(uint32_t)e;
@@ -1269,21 +1511,26 @@ __global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
       if (exposed) {
         dS = -1;
         const int8_t et = W.et[pos];
-        const int32_t e1 = t + 1 + (et > 0 ? et : 0);
-        W.evt[pos] = e1;
-        atomicMin(&W.sub_evt[pos >> 7], e1);
-        const uint64_t w = fix_risk(W.risk[pos]);
-        if (w) {
-          atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
-          atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
-          atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
-        }
+        ex_e1 = t + 1 + (et > 0 ? et : 0);
+        W.evt[pos] = ex_e1;
+        ex_w = fix_risk(W.risk[pos]);
       }
       if (s != s_in) W.ds[pos] = s;
+      ex_pos = pos;
     }
     const unsigned act = __ballot_sync(FULLMASK, on);
     if (!on) continue;
     const unsigned by_node = __match_any_sync(act, g);
+    if (__any_sync(act, ex_e1 != LPG_NO_DOD)) {
+      const uint32_t sb = (uint32_t)(ex_pos >> 7), ch = (uint32_t)(ex_pos / LPG_CHUNK);
+      const unsigned by_sub = __match_any_sync(act, sb);
+      const unsigned by_chunk = __match_any_sync(act, ch);
+      const int32_t emin = __reduce_min_sync(by_sub, ex_e1);
+      if ((int)(threadIdx.x & 31) == __ffs(by_sub) - 1 && emin != LPG_NO_DOD) atomicMin(&W.sub_evt[sb], emin);
+      warp_sub_w((unsigned long long*)&W.sub_w[sb], by_sub, ex_w);
+      warp_sub_w((unsigned long long*)&W.chunk_w[ch], by_chunk, ex_w);
+      warp_sub_w((unsigned long long*)&W.sw[g], by_node, ex_w);
+    }
     warp_add(&W.ev[(int64_t)EV_RIVAC * G + g], by_node, rivac);
     warp_add(&W.ev[(int64_t)EV_RIPROT * G + g], by_node, riprot);
     warp_add(&W.ev[(int64_t)EV_IPVVAC * G + g], by_node, ipvvac);
@@ -2340,6 +2587,44 @@ __global__ void k_init_events(DevWorld W, int32_t* evt, int32_t* sub_evt, int tm
       const int32_t e = tm + 1 + ev_pure(ds, W.strain[pos], W.et[pos], W.it[pos], W.pt[pos], W.pp[pos]);
       evt[pos] = e;
       atomicMin(&sub_evt[pos >> 7], e);
+    }
+  }
+}
+
+/* RI due ticks from their definition (base timer, reference index, date
+ * of birth; lpg_ri.h) for every agent, and per sub-block the earliest due
+ * tick after tick tl of its alive agents, written to out (LPG_NO_DOD for
+ * none, or where RI does not run).  At the start (tl = 0) it also writes the
+ * rdt column; the invariant check recounts with tl = the last tick run and
+ * flags (bad) any rdt entry that differs from its definition.  One thread
+ * per slot, a warp per 32 slots (4 warps per sub-block). */
+__global__ void k_ri_index(DevWorld W, int32_t* out, int at_start, int* bad) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < W.n_reps; ++r) {
+    const DevRep* rp = &W.reps[r];
+    const bool on_r = ri_runs(rp);
+    const int tl = at_start ? 0 : rp->t - 1;
+    const int64_t p0 = (int64_t)rp->chunk_base * LPG_CHUNK, np = (int64_t)rp->used_chunks * LPG_CHUNK;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q - lane < np; q += stride) {
+      const bool on = q < np;
+      const int64_t pos = p0 + q;
+      int32_t d = LPG_NO_DOD, m = LPG_NO_DOD;
+      if (on && on_r) {
+        const int8_t ds = W.ds[pos];
+        if (W.cm[pos] != 1) d = ri_due_of(rp, W.ri[pos], W.ref[pos], W.dob[pos]);
+        if (ds >= 0) {
+          if (at_start) W.rdt[pos] = d;
+          else if (W.rdt[pos] != d) atomicOr(bad, 256);
+          if (d > tl) m = d;
+        } else if (at_start) {
+          W.rdt[pos] = d;
+        }
+      } else if (on && at_start) {
+        W.rdt[pos] = LPG_NO_DOD;
+      }
+      m = __reduce_min_sync(FULLMASK, m);
+      if (lane == 0 && q < np) atomicMin(&out[pos >> 7], m);
     }
   }
 }

@@ -244,5 +244,47 @@ def test_work_counters_are_consistent():
     assert c["sweep_evt_due"] + c["sweep_dod_due"] >= c["sweep_due"]
     assert c["queue_ds"] >= int(res["deaths"][41:].sum())
     assert c["queue_rs"] > 0
+    assert 0 < c["ri_due"] <= c["ri_index"]
     if res["new_exposed"][41:].sum() > 0:
         assert c["sel_targets"] > 0
+
+
+def test_parity_ri_timers_extremes_and_mid_run_reads():
+    """RI timers over the whole int16 range (wrap-around, zero, the first RI
+    tick's wider window), deaths and births, with the columns read back in
+    the middle of the run and at its end."""
+    from laser_polio_gb300._lib import Handle
+    from oracle.oracle import OracleSim
+
+    sim = _busy_sim(seed=17, dur=130, cbr=600)
+    n = sim.people.count
+    rng = np.random.default_rng(3)
+    edge = np.array([-32768, -32767, -32760, -15, -14, -13, -1, 0, 1, 13, 14, 15, 28, 29, 32760, 32766, 32767])
+    ri = rng.integers(-32768, 32768, n)
+    ri[: n // 3] = rng.choice(edge, n // 3)
+    ri[n // 3 : n // 2] = rng.integers(-30, 200, n // 2 - n // 3)
+    sim.people.ri_timer[:n] = ri.astype(np.int16)
+    spec, cols_o, res_o = snapshot(sim)
+    _, cols_g, res_g = snapshot(sim)
+    o = OracleSim(spec.desc, keepalive=spec)
+    o.bind_columns(cols_o)
+    o.start()
+    h = Handle([spec.desc])
+    h.bind_columns(0, cols_g)
+    h.start()
+    for n_ticks in (29, 41, sim.nt - 71):
+        o.step(n_ticks)
+        h.step(n_ticks)
+        h.sync()
+        o.read_columns(cols_o)
+        h.read_columns(0, cols_g)
+        so, sg = o.state(), h.state(0)
+        assert (sg.t, sg.count) == (so.t, so.count)
+        assert_same(cols_o, cols_g, "column", count=so.count)
+    h.check_invariants()
+    o.read_results(res_o)
+    h.read_results(0, res_g)
+    o.close()
+    h.close()
+    assert_same(res_o, res_g, "result")
+    assert res_o["ri_vaccinated"].sum() > 0
