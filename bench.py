@@ -87,7 +87,7 @@ def tick_bytes(params, t):
 
 
 def sweep_b_bytes(params, t):
-    """Column bytes k_sweep<1> stages per agent slot on tick t: on SIA days
+    """Column bytes k_sweep_rs stages per agent slot on tick t: on SIA days
     state, chronically_missed and date_of_birth, plus ri_timer and the
     reference index when RI falls on the same day; 0 on other ticks (RI
     alone goes through the due index, counted by the work counters)."""
@@ -106,10 +106,12 @@ NCU_TRAFFIC_SOURCE = {}
 
 # Algorithmic bytes per unit of counted work (the device work counters of
 # lpg_read_counters), by kernel:
-#   k_sweep<0>: 4 B per sub-block index entry read; per visited 128-slot
-#     sub-block its 128 state bytes; 512 B of event ticks and a 4 B index
-#     write when an event is due; 512 B of dates of death and a 4 B index
-#     write when a death is due; 8 B per queue entry written.
+#   k_due: 4 B per sub-block index entry read; 8 B per due sub-block
+#     listed.
+#   k_sweep_due (k_sweep_a): per listed 128-slot sub-block its 8 B list
+#     entry and 128 state bytes; 512 B of event ticks and a 4 B index write
+#     when an event is due; 512 B of dates of death and a 4 B index write
+#     when a death is due; 8 B per queue entry written.
 #   k_dsq: per queue entry the 8 B entry, then state, strain, three timers
 #     and the event tick read (9 B) and state, timers and event tick written
 #     (8 B).
@@ -119,12 +121,13 @@ NCU_TRAFFIC_SOURCE = {}
 #     sub-block totals (16 x 8 B), the sub-block's 128 state bytes and 128
 #     risks (512 B), the target's hit written and read back (8 B); per agent
 #     exposed, state, strain, timers, event tick and its index (14 B).
-#   k_sweep<1> on RI ticks: 4 B per RI due index entry read; per visited
+#   k_sweep_rs (k_sweep_b) on RI ticks: 4 B per RI due index entry read; per visited
 #     sub-block its state, chronically-missed flags, RI timers, reference
 #     indexes and dates of birth (128 x 12 B) and the index write (4 B).
 #   k_node_tx: the network rows (nodes^2 x 8 B per simulation) and, per
 #     chunk of the population, its list entry, weight and prefix (20 B).
 SWEEP_INDEX_B, SWEEP_DUE_B, SWEEP_EVT_B, SWEEP_DOD_B, QUEUE_ENTRY_B = 4.0, 128.0, 516.0, 516.0, 8.0
+DUE_ITEM_B = 8.0
 DSQ_ENTRY_B = 8.0 + 9.0 + 8.0
 EVB_ENTRY_B = 8.0 + 10.0 + 5.0
 SEL_TARGET_B = 8.0 + 128.0 + 128.0 + 512.0 + 8.0
@@ -139,7 +142,8 @@ def kernel_alg_bytes(params, ticks, cnt, work, new_exposed):
     n = params["n_nodes"]
     chunks = float(params["capacity"]) / 2048.0
     out = {
-        "k_sweep_a": (SWEEP_INDEX_B * work["sweep_index"] + SWEEP_DUE_B * work["sweep_due"]
+        "k_due": SWEEP_INDEX_B * work["sweep_index"] + DUE_ITEM_B * work["sweep_due"],
+        "k_sweep_a": (DUE_ITEM_B * work["sweep_due"] + SWEEP_DUE_B * work["sweep_due"]
                       + SWEEP_EVT_B * work["sweep_evt_due"] + SWEEP_DOD_B * work["sweep_dod_due"]
                       + QUEUE_ENTRY_B * work["queue_ds"]),
         "k_dsq": DSQ_ENTRY_B * work["queue_ds"],

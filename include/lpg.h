@@ -253,15 +253,15 @@ int lpg_read_profile(lpg_handle* h, lpg_profile* out);
  * data-dependent amounts of work behind each kernel's algorithmic bytes.
  * No counterpart in the reference. */
 enum {
-  LPG_CTR_SWEEP_INDEX = 0,   /* sub-block index entries k_sweep<0> read */
-  LPG_CTR_SWEEP_DUE = 1,     /* sub-blocks it visited (an event or a death due) */
+  LPG_CTR_SWEEP_INDEX = 0,   /* sub-block index entries k_due read */
+  LPG_CTR_SWEEP_DUE = 1,     /* sub-blocks k_sweep_due visited (an event or a death due) */
   LPG_CTR_SWEEP_EVT_DUE = 2, /* of those, with an event due */
   LPG_CTR_SWEEP_DOD_DUE = 3, /* of those, with a death due */
-  LPG_CTR_QUEUE_DS = 4,      /* queue entries of k_sweep<0> (deaths, disease steps) */
-  LPG_CTR_QUEUE_RS = 5,      /* queue entries of k_sweep<1> (RI, SIA) */
+  LPG_CTR_QUEUE_DS = 4,      /* queue entries of k_sweep_due (deaths, disease steps) */
+  LPG_CTR_QUEUE_RS = 5,      /* queue entries of k_sweep_rs (RI, SIA) */
   LPG_CTR_SEL_TARGETS = 6,   /* targets k_select located, all rounds */
   LPG_CTR_SEL_NODE_ROUNDS = 7, /* node rounds after round 0 */
-  LPG_CTR_RI_INDEX = 8,      /* RI due index entries k_sweep<1> read */
+  LPG_CTR_RI_INDEX = 8,      /* RI due index entries k_sweep_rs read */
   LPG_CTR_RI_DUE = 9,        /* sub-blocks it visited with an RI due tick come */
   LPG_NUM_COUNTERS = 10
 };

@@ -21,8 +21,9 @@
 
 namespace {
 
-const char* kKernelNames[] = {"k_begin", "k_newborns", "k_sweep_a", "k_dsq", "k_seed", "k_sweep_b", "k_evb", "k_node_tx", "k_select", "k_end"};
-constexpr int kNumTickKernels = 10;
+const char* kKernelNames[] = {"k_begin", "k_newborns", "k_due", "k_sweep_a", "k_dsq", "k_seed",
+                              "k_sweep_b", "k_evb", "k_node_tx", "k_select", "k_end"};
+constexpr int kNumTickKernels = 11;
 constexpr int kTicksPerGraph = 8;
 
 /* Reference-ordered columns of one simulation on the device. */
@@ -70,8 +71,9 @@ struct lpg_handle {
   std::vector<cudaEvent_t> ev_pool;
   int64_t launches = 0;
   int sm_count = 0;
-  int sweep_blocks = 0;  /* k_sweep<1> (staged through shared memory) */
-  int sweep0_blocks = 0; /* k_sweep<0> (direct loads, no staging) */
+  int sweep_blocks = 0;  /* k_sweep_rs (staged through shared memory) */
+  int sweep0_blocks = 0; /* k_sweep_due (direct loads, no staging) */
+  int due_blocks = 0;    /* k_due */
   int select_blocks = 0;
 };
 
@@ -512,6 +514,8 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.cmeta, chunk_total);
   rc |= dalloc(h, &W.qcnt, 2048);
   rc |= dalloc(h, &W.qfirst, 2048);
+  rc |= dalloc(h, &W.due, (size_t)chunk_total * LPG_NSUB);
+  rc |= dalloc(h, &W.due_n, 1);
   rc |= dalloc(h, &W.evq, (size_t)chunk_total * LPG_CHUNK);
   rc |= dalloc(h, &W.chunk_w, chunk_total);
   rc |= dalloc(h, &W.sub_w, (size_t)chunk_total * LPG_NSUB);
@@ -556,6 +560,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaMemsetAsync(W.ref, 0xff, P * 4, st));
   CK(cudaMemsetAsync(W.qcnt, 0, 4 * 2048, st));
   CK(cudaMemsetAsync(W.qfirst, 0, 4 * 2048, st));
+  CK(cudaMemsetAsync(W.due_n, 0, 4, st));
   CK(cudaMemsetAsync(W.ev, 0, sizeof(int32_t) * EV_N * G, st));
   CK(cudaMemsetAsync(W.tot, 0, sizeof(int32_t) * TT_N * G, st));
   CK(cudaMemsetAsync(W.sw, 0, sizeof(uint64_t) * G, st));
@@ -819,13 +824,15 @@ extern "C" int lpg_start(lpg_handle* h) {
 
   /* launch geometry */
   int occ = 0;
-  CK(cudaFuncSetAttribute(k_sweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
-  CK(cudaFuncSetAttribute(k_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM));
+  CK(cudaFuncSetAttribute(k_sweep_rs, cudaFuncAttributeMaxDynamicSharedMemorySize, LPG_SWEEP_SMEM));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep_rs, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM));
   h->sweep_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
   occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep<0>, LPG_SWEEP_BLOCK, 0));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep_due, LPG_SWEEP_BLOCK, 0));
   h->sweep0_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
+  occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_due, 256, 0));
+  h->due_blocks = std::max(1, occ) * h->sm_count;
   occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_select, 256, 0));
   h->select_blocks = std::min(1024, std::max(1, std::min(occ, 2)) * h->sm_count);
@@ -847,13 +854,14 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
   switch (k) {
     case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
     case 1: k_newborns<<<dim3(h->sm_count * 8, R), 256, 0, st>>>(W); break;
-    case 2: k_sweep<0><<<h->sweep0_blocks, LPG_SWEEP_BLOCK, 0, st>>>(W); break;
-    case 3: k_dsq<<<h->sm_count * 4, 256, 0, st>>>(W, h->sweep0_blocks); break;
-    case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
-    case 5: k_sweep<1><<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 6: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
-    case 7: k_node_tx<<<G, LPG_NODE_TX_THREADS, 0, st>>>(W); break;
-    case 8: {
+    case 2: k_due<<<h->due_blocks, 256, 0, st>>>(W); break;
+    case 3: k_sweep_due<<<h->sweep0_blocks, LPG_SWEEP_BLOCK, 0, st>>>(W); break;
+    case 4: k_dsq<<<h->sm_count * 4, 256, 0, st>>>(W, h->sweep0_blocks); break;
+    case 5: k_seed<<<R, 1024, 0, st>>>(W); break;
+    case 6: k_sweep_rs<<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
+    case 7: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
+    case 8: k_node_tx<<<G, LPG_NODE_TX_THREADS, 0, st>>>(W); break;
+    case 9: {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(h->select_blocks);
       cfg.blockDim = dim3(256);
@@ -867,7 +875,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
       CK(cudaLaunchKernelEx(&cfg, k_select, W));
       break;
     }
-    case 9: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
+    case 10: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
   }
   CK(cudaGetLastError());
   if (timed) CK(cudaEventRecord(e1, st));

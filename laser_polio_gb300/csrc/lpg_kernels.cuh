@@ -8,14 +8,17 @@
  *                counters, births per node (model.py:1711-1716) and their
  *                chunk placement
  *   k_newborns   newborn rows (model.py:1719-1730)
- *   k_sweep<0>   streaming sweep over every chunk: deaths (get_deaths,
+ *   k_due        the sub-blocks with a disease-state event or a death due,
+ *                from the per-sub-block indexes
+ *   k_sweep_due  those sub-blocks, evenly over the CTAs: deaths (get_deaths,
  *                model.py:1767-1781) and the queue of agents in E or I
+ *                whose event is now
  *   k_dsq        death bookkeeping and disease progression and paralysis of
  *                the queued agents (model.py:393-454)
  *   k_seed       the seed schedule (model.py:759-786)
- *   k_sweep<1>   streaming sweep on RI/SIA ticks: the RI countdown and the
- *                queue of agents that RI (fast_ri, :1784-1855) or today's
- *                SIA campaigns (fast_sia, :1994-2060) reach
+ *   k_sweep_rs   on RI/SIA ticks: the queue of agents that RI (fast_ri,
+ *                :1784-1855; due sub-blocks only) or today's SIA campaigns
+ *                (fast_sia, :1994-2060; every slot, staged) reach
  *   k_evb        their draws and exposures
  *   k_node_tx    per node: population (model.py:1751-1755), mixing,
  *                seasonality, probabilities and exposure counts
@@ -452,11 +455,11 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
   }
 }
 
-/* The sweeps, two launches per tick.
- *   PHASE 0: deaths (get_deaths, model.py:1767-1781) on VD ticks, and the
- *            queue of agents in E or I whose disease-state event is due
- *            (k_dsq); through the sub-block indexes (sweep_direct).
- *   PHASE 1: routine immunisation (fast_ri, model.py:1784-1855) and SIA
+/* The sweeps.
+ *   k_due, k_sweep_due: deaths (get_deaths, model.py:1767-1781) on VD ticks
+ *            and the queue of agents in E or I whose disease-state event is
+ *            due (k_dsq), through the sub-block indexes.
+ *   k_sweep_rs: routine immunisation (fast_ri, model.py:1784-1855) and SIA
  *            campaigns (fast_sia, :1994-2060), on the ticks that have them,
  *            after progression and the seed schedule as in default_run_order.
  *            RI alone goes through the RI due index (ri_direct); SIA days
@@ -528,7 +531,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 }
 
 /* per-simulation flags of the launch, cached in shared memory */
-enum { SF_WORK = 1, SF_DENSE = 2, SF_VD = 4, SF_DS = 8, SF_RI = 16, SF_SIA = 32 };
+enum { SF_WORK = 1, SF_DENSE = 2, SF_RI = 16, SF_SIA = 32 };
 
 struct SweepPlan {
   int32_t total, nreps;
@@ -540,7 +543,7 @@ struct SweepPlan {
 
 /* Staged bytes per chunk for a simulation's flags. */
 __device__ __forceinline__ int chunk_bytes(uint8_t f) {
-  return LPG_CHUNK + ((f & SF_VD) ? 4 * LPG_CHUNK : 0) + ((f & SF_RI) ? 4 * LPG_CHUNK : 0) +
+  return LPG_CHUNK + ((f & SF_RI) ? 4 * LPG_CHUNK : 0) +
          ((f & (SF_RI | SF_SIA)) ? LPG_CHUNK : 0) + ((f & SF_SIA) ? 4 * LPG_CHUNK : 0);
 }
 /* Chunks per stage (k consecutive chunks: each column is one contiguous copy). */
@@ -549,15 +552,13 @@ __device__ __forceinline__ int stage_chunks(uint8_t f) {
   return k < LPG_PLAIN_GROUP ? k : LPG_PLAIN_GROUP;
 }
 struct StageLayout {
-  int ds, dod, rdt, cm, dob;
+  int ds, rdt, cm, dob;
 };
 __device__ __forceinline__ StageLayout stage_layout(uint8_t f, int k) {
   StageLayout L;
   int off = 0;
   L.ds = off;
   off += k * LPG_CHUNK;
-  L.dod = off;
-  if (f & SF_VD) off += k * 4 * LPG_CHUNK;
   L.rdt = off;
   if (f & SF_RI) off += k * 4 * LPG_CHUNK;
   L.cm = off;
@@ -645,70 +646,9 @@ __device__ __forceinline__ void queue_a16(uint64_t* slab, uint32_t* s_cnt, int64
   }
 }
 
-/* PHASE 0, one thread's 16 slots (pos0 .. pos0+15; sv the state bytes,
- * sdod the dates of death in shared memory or null): deaths are written
- * here (state -1) and queued with their old state for the bookkeeping;
- * agents in E or I that survive are queued for progression. */
-__device__ __forceinline__ void sweep_a16(uint64_t* slab, uint32_t* s_cnt, DevWorld& W, bool on, bool ds, int t,
-                                          int64_t pos0, int off, int nbo, uint4 sv, const int32_t* sdod) {
-  uint32_t ei = 0, dead = 0;
-  if (on) {
-    const uint32_t wv[4] = {sv.x, sv.y, sv.z, sv.w};
-    uint32_t eiw[4];
-    uint32_t any_ei = 0;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      eiw[q] = __vcmpltu4(__vsub4(wv[q], 0x01010101u), 0x02020202u);
-      any_ei |= eiw[q];
-    }
-    if (ds && any_ei) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) ei |= ((eiw[q] >> (8 * j + 7)) & 1u) << (4 * q + j);
-    }
-    if (sdod) {
-      const int4* d4 = reinterpret_cast<const int4*>(sdod + off);
-      int32_t mn = 0x7fffffff;
-      int4 dq[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        dq[q] = d4[q];
-        mn = min(mn, min(min(dq[q].x, dq[q].y), min(dq[q].z, dq[q].w)));
-      }
-      if (mn <= t) { /* rare: somebody's date of death has come */
-        uint32_t alive = 0, due = 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int32_t dd[4] = {dq[q].x, dq[q].y, dq[q].z, dq[q].w};
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int k = 4 * q + j;
-            alive |= (((wv[q] >> (8 * j + 7)) & 1u) ^ 1u) << k;
-            due |= (uint32_t)(dd[j] <= t && (off + k) < nbo) << k;
-          }
-        }
-        dead = alive & due;
-        if (dead) {
-          uint4 out = sv;
-          uint32_t* ow = reinterpret_cast<uint32_t*>(&out);
-#pragma unroll
-          for (int k = 0; k < 16; ++k)
-            if ((dead >> k) & 1u) ow[k >> 2] |= 0xffu << (8 * (k & 3));
-          *reinterpret_cast<uint4*>(W.ds + pos0) = out;
-          ei &= ~dead;
-        }
-      }
-    }
-  }
-  queue_a16(slab, s_cnt, pos0, ei, dead, sv);
-}
-
-/* PHASE 1, one thread's 16 slots: the RI countdown and the masks of agents
- * that RI or today's SIA campaigns reach (queued with their event flags).
- * The countdown is packed 16-bit arithmetic: the stored value wraps like
- * the reference's int16 store, and eligibility  -step <(=) old - step <= 0
- * is a range test on the old value. */
+/* k_sweep_rs on an SIA day, one thread's 16 staged slots: the masks of the
+ * agents that RI (due today) or today's SIA campaigns reach, queued with
+ * their event flags. */
 __device__ __forceinline__ void sweep_b16(uint64_t* slab, uint32_t* s_cnt, DevWorld& W, bool on, const DevRep* rp,
                                           uint8_t fl, int t, int ni, int64_t pos0, int off, uint4 sv,
                                           const uint8_t* scm, const int32_t* srdt, const int32_t* sdob) {
@@ -837,109 +777,145 @@ __device__ __forceinline__ int32_t sub8_min(int32_t x) {
   return min(x, __shfl_xor_sync(FULLMASK, x, 1));
 }
 
-/* k_sweep<0> over one simulation's range of sub-blocks [sb0, sb0 + nsb)
- * (128 slots each), in windows of LPG_DUE_MAX sub-blocks:
- *  1. the CTA reads the window of the index of earliest events (sub_evt;
- *     dsq: the simulation steps disease states) and, on VD ticks (vd), of
- *     earliest dates of death (sub_dod), 4 entries per 16-byte load, and
- *     lists the sub-blocks with something due at t in shared memory;
- *  2. 8 lanes per listed sub-block (16 slots each) read its state bytes,
- *     the dates of death when a death is due and the event ticks when an
- *     event is due: deaths (model.py:1767-1781; this tick's newborns are not
- *     checked), the queue of the agents whose event is now, and the
- *     sub-block's new earliest event and date of death over the rest.
- * All threads of the CTA run it. */
+/* Sub-blocks with something due at this tick, the work list of
+ * k_sweep_due: the index of earliest events (sub_evt) where the simulation
+ * steps disease states, and on VD ticks the index of earliest dates of
+ * death (sub_dod), read 4 entries per 16-byte load, four loads in flight per
+ * thread over each simulation's sub-blocks.  A due sub-block is appended to
+ * W.due as (sub-block | simulation << 32 | what << 48; what: 1 event, 2
+ * death), one global atomic per warp. */
 #define LPG_DUE_MAX 8192
-__device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t* s_cnt, int64_t sb0, int64_t nsb,
-                                          int t, bool dsq, bool vd, uint32_t* s_due, int* s_ndue) {
+__global__ void __launch_bounds__(256) k_due(DevWorld W) {
   const int lane = threadIdx.x & 31;
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
+  const int4 none = make_int4(LPG_NO_DOD, LPG_NO_DOD, LPG_NO_DOD, LPG_NO_DOD);
+  for (int r = 0; r < W.n_reps; ++r) {
+    const DevRep* rp = &W.reps[r];
+    if (!rp->active) continue;
+    const bool dsq = (rp->comps & LPG_COMP_DS) != 0, vd = rp->vd_tick != 0;
+    if (!dsq && !vd) continue;
+    const int t = rp->cur_t;
+    const int64_t sb0 = (int64_t)rp->chunk_base * LPG_NSUB;
+    const int64_t nq = (int64_t)rp->used_chunks * (LPG_NSUB / 4);
+    if (gtid == 0) atomicAdd(&W.ctr[LPG_CTR_SWEEP_INDEX], (unsigned long long)(nq * 4 * ((dsq ? 1 : 0) + (vd ? 1 : 0))));
+    for (int64_t q0 = gtid; q0 - lane < nq; q0 += 4 * gsz) {
+      int4 e[4], d[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t q = q0 + u * gsz;
+        e[u] = (dsq && q < nq) ? __ldcg(reinterpret_cast<const int4*>(W.sub_evt + sb0) + q) : none;
+        d[u] = (vd && q < nq) ? __ldcg(reinterpret_cast<const int4*>(W.sub_dod + sb0) + q) : none;
+      }
+      uint32_t fl = 0; /* 2 bits per entry, 16 entries */
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int32_t ee[4] = {e[u].x, e[u].y, e[u].z, e[u].w}, dd[4] = {d[u].x, d[u].y, d[u].z, d[u].w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          fl |= ((ee[j] <= t ? 1u : 0u) | (dd[j] <= t ? 2u : 0u)) << (2 * (4 * u + j));
+      }
+      const uint32_t nf = __popc((fl | (fl >> 1)) & 0x55555555u);
+      uint32_t x = nf;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULLMASK, x, o);
+        if (lane >= o) x += y;
+      }
+      const uint32_t tot = __shfl_sync(FULLMASK, x, 31);
+      if (tot == 0) continue;
+      uint32_t base = 0;
+      if (lane == 31) base = atomicAdd(W.due_n, tot);
+      uint32_t at = __shfl_sync(FULLMASK, base, 31) + x - nf;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const uint32_t f = (fl >> (2 * (4 * u + j))) & 3u;
+          if (f) W.due[at++] = (uint64_t)(sb0 + 4 * (q0 + u * gsz) + j) | ((uint64_t)r << 32) | ((uint64_t)f << 48);
+        }
+    }
+  }
+}
+
+/* The due sub-blocks of W.due, split evenly over the CTAs (an outbreak makes
+ * most sub-blocks of a few nodes due while most others have none), 8 lanes
+ * per sub-block (16 slots each): state bytes, the dates of death when a
+ * death is due and the event ticks when an event is due.  Deaths
+ * (model.py:1767-1781; this tick's newborns are not checked), the queue of
+ * the agents whose event is now, and the sub-block's new earliest event
+ * and date of death over the rest, with no atomics.  A CTA's queue slab
+ * starts at its first item times 128 entries of evq. */
+__global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_due(DevWorld W) {
+  __shared__ uint32_t s_qcnt;
+  const int lane = threadIdx.x & 31;
+  const int64_t D = (int64_t)*(volatile uint32_t*)W.due_n;
+  const int64_t i0 = D * blockIdx.x / gridDim.x, i1 = D * (blockIdx.x + 1) / gridDim.x;
+  uint64_t* slab = W.evq + i0 * LPG_SUB;
+  if (threadIdx.x == 0) s_qcnt = 0;
+  __syncthreads();
   uint32_t n_due = 0, n_edue = 0, n_ddue = 0; /* work counters, lanes (lane & 7) == 0 */
-  for (int64_t wb = 0; wb < nsb; wb += LPG_DUE_MAX) {
-    const int nw = (int)min((int64_t)LPG_DUE_MAX, nsb - wb);
-    if (threadIdx.x == 0) {
-      *s_ndue = 0;
-      atomicAdd(&W.ctr[LPG_CTR_SWEEP_INDEX], (unsigned long long)nw * ((dsq ? 1 : 0) + (vd ? 1 : 0)));
+  const int per_pass = (blockDim.x / 32) * 4;
+  for (int64_t base = i0; base < i1; base += per_pass) {
+    const int64_t item = base + (threadIdx.x >> 5) * 4 + (lane >> 3);
+    const bool on = item < i1;
+    const uint64_t rec = on ? __ldcg(W.due + item) : 0ULL;
+    const int64_t sb = (int64_t)(uint32_t)rec;
+    const uint32_t f = (uint32_t)(rec >> 48);
+    const bool edue = (f & 1u) != 0, ddue = (f & 2u) != 0;
+    const int t = on ? W.reps[(rec >> 32) & 0xffffu].cur_t : 0;
+    if (on && (lane & 7) == 0) {
+      n_due += 1;
+      n_edue += edue ? 1 : 0;
+      n_ddue += ddue ? 1 : 0;
     }
-    __syncthreads();
-    /* 1. due sub-blocks of the window (sb0 and the window are multiples of 16) */
-    for (int q = threadIdx.x * 4; q < nw; q += blockDim.x * 4) {
-      const int64_t sb = sb0 + wb + q;
-      int4 e4 = make_int4(LPG_NO_DOD, LPG_NO_DOD, LPG_NO_DOD, LPG_NO_DOD), d4 = e4;
-      if (dsq) e4 = __ldcg(reinterpret_cast<const int4*>(W.sub_evt + sb));
-      if (vd) d4 = __ldcg(reinterpret_cast<const int4*>(W.sub_dod + sb));
-      const int32_t ee[4] = {e4.x, e4.y, e4.z, e4.w}, dd[4] = {d4.x, d4.y, d4.z, d4.w};
+    const int64_t pos0 = sb * LPG_SUB + (int64_t)(lane & 7) * 16;
+    const uint4 v = on ? ldg_stream16(W.ds + pos0) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    uint32_t dead = 0;
+    if (__ballot_sync(FULLMASK, ddue)) {
+      int32_t nmin = LPG_NO_DOD;
+      if (ddue) {
+        const int4* d4 = reinterpret_cast<const int4*>(W.dod + pos0);
+        int4 dq[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const uint32_t f = (ee[j] <= t ? 1u : 0u) | (dd[j] <= t ? 2u : 0u);
-        if (f && q + j < nw) {
-          const int at = atomicAdd(s_ndue, 1);
-          s_due[at] = ((uint32_t)(q + j) << 2) | f;
-        }
-      }
-    }
-    __syncthreads();
-    const int ndue = *s_ndue;
-    /* 2. 8 lanes per due sub-block; warp-uniform passes */
-    const int per_pass = (blockDim.x / 32) * 4;
-    for (int base = 0; base < ndue; base += per_pass) {
-      const int item = base + (threadIdx.x >> 5) * 4 + (lane >> 3);
-      const bool on = item < ndue;
-      const uint32_t rec = on ? s_due[item] : 0u;
-      const bool edue = (rec & 1u) != 0, ddue = (rec & 2u) != 0;
-      if (on && (lane & 7) == 0) {
-        n_due += 1;
-        n_edue += edue ? 1 : 0;
-        n_ddue += ddue ? 1 : 0;
-      }
-      const int64_t pos0 = (sb0 + wb + (rec >> 2)) * LPG_SUB + (int64_t)(lane & 7) * 16;
-      const uint4 v = on ? ldg_stream16(W.ds + pos0) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-      uint32_t dead = 0;
-      if (__ballot_sync(FULLMASK, ddue)) {
-        int32_t nmin = LPG_NO_DOD;
-        if (ddue) {
-          const int4* d4 = reinterpret_cast<const int4*>(W.dod + pos0);
-          int4 dq[4];
+        for (int q = 0; q < 4; ++q) dq[q] = d4[q];
+        const int4 m = W.cmeta[pos0 >> 11];
+        const int off = (int)(pos0 & (LPG_CHUNK - 1));
+        const int nbo = (m.z == t) ? m.w : LPG_CHUNK; /* this tick's newborns are not checked */
+        const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-          for (int q = 0; q < 4; ++q) dq[q] = d4[q];
-          const int4 m = W.cmeta[pos0 >> 11];
-          const int off = (int)(pos0 & (LPG_CHUNK - 1));
-          const int nbo = (m.z == t) ? m.w : LPG_CHUNK; /* this tick's newborns are not checked */
-          const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+        for (int q = 0; q < 4; ++q) {
+          const int32_t dd[4] = {dq[q].x, dq[q].y, dq[q].z, dq[q].w};
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int32_t dd[4] = {dq[q].x, dq[q].y, dq[q].z, dq[q].w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              const int k = 4 * q + j;
-              const bool alive = ((wv[q] >> (8 * j + 7)) & 1u) == 0;
-              const bool dies = alive && dd[j] <= t && off + k < nbo;
-              dead |= (uint32_t)dies << k;
-              if (alive && !dies) nmin = min(nmin, dd[j]);
-            }
-          }
-          if (dead) {
-            uint4 out = v;
-            uint32_t* ow = reinterpret_cast<uint32_t*>(&out);
-#pragma unroll
-            for (int k = 0; k < 16; ++k)
-              if ((dead >> k) & 1u) ow[k >> 2] |= 0xffu << (8 * (k & 3));
-            *reinterpret_cast<uint4*>(W.ds + pos0) = out;
+          for (int j = 0; j < 4; ++j) {
+            const int k = 4 * q + j;
+            const bool alive = ((wv[q] >> (8 * j + 7)) & 1u) == 0;
+            const bool dies = alive && dd[j] <= t && off + k < nbo;
+            dead |= (uint32_t)dies << k;
+            if (alive && !dies) nmin = min(nmin, dd[j]);
           }
         }
-        nmin = sub8_min(nmin);
-        if (ddue && (lane & 7) == 0) W.sub_dod[pos0 >> 7] = nmin;
+        if (dead) {
+          uint4 out = v;
+          uint32_t* ow = reinterpret_cast<uint32_t*>(&out);
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            if ((dead >> k) & 1u) ow[k >> 2] |= 0xffu << (8 * (k & 3));
+          *reinterpret_cast<uint4*>(W.ds + pos0) = out;
+        }
       }
-      uint32_t ei = 0;
-      if (__ballot_sync(FULLMASK, edue)) {
-        int32_t nmin = LPG_NO_DOD;
-        if (edue) ei = ev_due16(W, pos0, v, dead, t, nmin);
-        nmin = sub8_min(nmin);
-        /* the agents due now get their next event from k_dsq (atomicMin) */
-        if (edue && (lane & 7) == 0) W.sub_evt[pos0 >> 7] = nmin;
-      }
-      queue_a16(slab, s_cnt, pos0, ei, dead, v);
+      nmin = sub8_min(nmin);
+      if (ddue && (lane & 7) == 0) W.sub_dod[sb] = nmin;
     }
-    __syncthreads();
+    uint32_t ei = 0;
+    if (__ballot_sync(FULLMASK, edue)) {
+      int32_t nmin = LPG_NO_DOD;
+      if (edue) ei = ev_due16(W, pos0, v, dead, t, nmin);
+      nmin = sub8_min(nmin);
+      /* the agents due now get their next event from k_dsq (atomicMin) */
+      if (edue && (lane & 7) == 0) W.sub_evt[sb] = nmin;
+    }
+    queue_a16(slab, &s_qcnt, pos0, ei, dead, v);
   }
   n_due = __reduce_add_sync(FULLMASK, n_due);
   n_edue = __reduce_add_sync(FULLMASK, n_edue);
@@ -949,9 +925,14 @@ __device__ __noinline__ void sweep_direct(DevWorld& W, uint64_t* slab, uint32_t*
     atomicAdd(&W.ctr[LPG_CTR_SWEEP_EVT_DUE], (unsigned long long)n_edue);
     atomicAdd(&W.ctr[LPG_CTR_SWEEP_DOD_DUE], (unsigned long long)n_ddue);
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    W.qcnt[blockIdx.x] = s_qcnt;
+    W.qfirst[blockIdx.x] = (uint32_t)(i0 * LPG_SUB);
+  }
 }
 
-/* k_sweep<1> on an RI tick without SIA, over one simulation's sub-blocks
+/* k_sweep_rs on an RI tick without SIA, over one simulation's sub-blocks
  * [sb0, sb0 + nsb), in windows of LPG_DUE_MAX sub-blocks: the CTA lists the
  * sub-blocks whose earliest RI due tick (sub_rdt) has come, then 8 lanes
  * per listed sub-block queue the agents due now (fast_ri, model.py:1825-1854:
@@ -1025,15 +1006,13 @@ __device__ __forceinline__ int32_t dense_from(const SweepPlan& P, int32_t w, int
   return w1;
 }
 
-template <int PHASE>
-__global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
+__global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
   extern __shared__ __align__(128) uint8_t sm_stage[];
   __shared__ SweepPlan P;
   __shared__ __align__(8) uint64_t full[LPG_NST];
   __shared__ __align__(8) uint64_t empty[LPG_NST];
   __shared__ uint32_t s_qcnt;
   __shared__ int32_t s_issued;
-  __shared__ uint32_t s_due[PHASE == 0 ? LPG_DUE_MAX : 1];
   __shared__ int s_ndue;
   __shared__ volatile int s_abort;
   const int R = W.n_reps < LPG_MAX_REPS ? W.n_reps : LPG_MAX_REPS;
@@ -1044,16 +1023,10 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       const DevRep* rp = &W.reps[r];
       uint8_t f = 0;
       if (rp->active) {
-        if (PHASE == 0) {
-          if (rp->vd_tick) f |= SF_VD | SF_DENSE;
-          if (rp->comps & LPG_COMP_DS) f |= SF_DS;
-          if (f) f |= SF_WORK;
-        } else {
-          if (rp->ri_tick) f |= SF_RI;
-          if (rp->sia_n > 0) f |= SF_SIA;
-          if (f) f |= SF_WORK;
-          if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due index */
-        }
+        if (rp->ri_tick) f |= SF_RI;
+        if (rp->sia_n > 0) f |= SF_SIA;
+        if (f) f |= SF_WORK;
+        if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due index */
       }
       P.flags[r] = f;
       P.cbase[r] = rp->chunk_base;
@@ -1080,7 +1053,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
   uint64_t* slab = W.evq + (int64_t)w0 * LPG_CHUNK;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  if (PHASE == 1) {
+  {
     /* Simulations with RI today and no SIA: the due sub-blocks only
      * (ri_direct), all threads, with the list in the stage buffers before
      * any bulk copy reaches them. */
@@ -1099,24 +1072,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
   }
-  if (PHASE == 0) {
-    /* No staging: every warp reads the sub-block indexes of its range and
-     * only the slots of sub-blocks with an event or a death due
-     * (sweep_direct).  A simulation's work items map to consecutive chunks,
-     * so each simulation's share of [w0, w1) is one contiguous range. */
-    int32_t w = w0;
-    while (w < w1) {
-      int r;
-      (void)stage_end(P, w, w1, &r);
-      const int32_t we = min(w1, P.off[r + 1]);
-      const int64_t lo = (P.cbase[r] + (int64_t)(w - P.off[r])) * LPG_CHUNK;
-      const int64_t nbytes = (int64_t)(we - w) * LPG_CHUNK;
-      const int t = P.tick[r];
-      const bool dsq = (P.flags[r] & SF_DS) != 0, vd = (P.flags[r] & SF_VD) != 0;
-      if (vd || dsq) sweep_direct(W, slab, &s_qcnt, lo / LPG_SUB, nbytes / LPG_SUB, t, dsq, vd, s_due, &s_ndue);
-      w = we;
-    }
-  } else if (warp == LPG_SWEEP_CONSUMERS / 32) {
+  if (warp == LPG_SWEEP_CONSUMERS / 32) {
     /* ---- producer warp: one lane issues the stages ---- */
     if (lane == 0 && w0 < w1) {
       int32_t wp = dense_from(P, w0, w1);
@@ -1141,7 +1097,6 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
         mbar_expect_tx(&full[b], bytes);
         bulk_g2s(dst, W.cmeta + cid, (uint32_t)nc * 16u, &full[b]);
         bulk_g2s(cols + L.ds, W.ds + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
-        if (f & SF_VD) bulk_g2s(cols + L.dod, W.dod + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
         if (f & SF_RI) bulk_g2s(cols + L.rdt, W.rdt + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
         if (f & (SF_RI | SF_SIA)) bulk_g2s(cols + L.cm, W.cm + cid * LPG_CHUNK, (uint32_t)nc * LPG_CHUNK, &full[b]);
         if (f & SF_SIA) bulk_g2s(cols + L.dob, W.dob + cid * LPG_CHUNK, (uint32_t)nc * 4 * LPG_CHUNK, &full[b]);
@@ -1172,37 +1127,6 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
       const int nc = we - wc;
       const StageLayout L = stage_layout(fl, nc);
       const int ngroups = nc * (LPG_CHUNK / 16);
-      if (PHASE == 0 && (fl & (SF_DS | SF_VD)) == SF_DS) {
-        /* state bytes only: queue the agents in E or I.  Two 16-slot groups
-         * per thread per pass; a warp with none in either skips the rest. */
-        const uint8_t* dsb = cols + L.ds;
-        const int nbytes = nc * LPG_CHUNK;
-        const int64_t pos_base = (P.cbase[r] + (int64_t)(wc - P.off[r])) * LPG_CHUNK;
-        for (int ob = 0; ob < nbytes; ob += 2 * LPG_SWEEP_CONSUMERS * 16) {
-          const int oa = ob + threadIdx.x * 16, oc = oa + LPG_SWEEP_CONSUMERS * 16;
-          const uint4 none = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-          const uint4 va = oa < nbytes ? *reinterpret_cast<const uint4*>(dsb + oa) : none;
-          const uint4 vc = oc < nbytes ? *reinterpret_cast<const uint4*>(dsb + oc) : none;
-          const uint32_t ea = __vcmpltu4(__vsub4(va.x, 0x01010101u), 0x02020202u) |
-                              __vcmpltu4(__vsub4(va.y, 0x01010101u), 0x02020202u) |
-                              __vcmpltu4(__vsub4(va.z, 0x01010101u), 0x02020202u) |
-                              __vcmpltu4(__vsub4(va.w, 0x01010101u), 0x02020202u);
-          const uint32_t ec = __vcmpltu4(__vsub4(vc.x, 0x01010101u), 0x02020202u) |
-                              __vcmpltu4(__vsub4(vc.y, 0x01010101u), 0x02020202u) |
-                              __vcmpltu4(__vsub4(vc.z, 0x01010101u), 0x02020202u) |
-                              __vcmpltu4(__vsub4(vc.w, 0x01010101u), 0x02020202u);
-          const unsigned vote = __ballot_sync(FULLMASK, ea != 0) | __ballot_sync(FULLMASK, ec != 0);
-          if (vote == 0) continue;
-          sweep_a16(slab, &s_qcnt, W, oa < nbytes, true, t, pos_base + oa, oa & (LPG_CHUNK - 1), LPG_CHUNK, va,
-                    nullptr);
-          sweep_a16(slab, &s_qcnt, W, oc < nbytes, true, t, pos_base + oc, oc & (LPG_CHUNK - 1), LPG_CHUNK, vc,
-                    nullptr);
-        }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[b]);
-        wc = dense_from(P, we, w1);
-        continue;
-      }
       for (int gb = 0; gb < ngroups; gb += LPG_SWEEP_CONSUMERS) {
         const int gi = gb + threadIdx.x;
         const bool on = gi < ngroups;
@@ -1214,19 +1138,10 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
          * out of every test below without a fill check */
         const uint4 sv = on ? *reinterpret_cast<const uint4*>(cols + L.ds + kk * LPG_CHUNK + off)
                             : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-        if (PHASE == 0) {
-          if (fl & (SF_DS | SF_VD)) {
-            const int4 m = meta[kk];
-            const int nbo = (m.z == t) ? m.w : LPG_CHUNK;
-            sweep_a16(slab, &s_qcnt, W, on, (fl & SF_DS) != 0, t, pos0, off, nbo, sv,
-                      (fl & SF_VD) ? reinterpret_cast<const int32_t*>(cols + L.dod + kk * 4 * LPG_CHUNK) : nullptr);
-          }
-        } else {
-          const int ni = meta[kk].x - rp->node_base;
-          sweep_b16(slab, &s_qcnt, W, on, rp, fl, t, ni, pos0, off, sv, cols + L.cm + kk * LPG_CHUNK,
-                    reinterpret_cast<const int32_t*>(cols + L.rdt + kk * 4 * LPG_CHUNK),
-                    reinterpret_cast<const int32_t*>(cols + L.dob + kk * 4 * LPG_CHUNK));
-        }
+        const int ni = meta[kk].x - rp->node_base;
+        sweep_b16(slab, &s_qcnt, W, on, rp, fl, t, ni, pos0, off, sv, cols + L.cm + kk * LPG_CHUNK,
+                  reinterpret_cast<const int32_t*>(cols + L.rdt + kk * 4 * LPG_CHUNK),
+                  reinterpret_cast<const int32_t*>(cols + L.dob + kk * 4 * LPG_CHUNK));
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[b]);
@@ -1245,8 +1160,8 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep(DevWorld W) {
     }
   }
   if (threadIdx.x == 0) {
-    W.qcnt[PHASE * 1024 + blockIdx.x] = s_qcnt;
-    W.qfirst[PHASE * 1024 + blockIdx.x] = w0;
+    W.qcnt[1024 + blockIdx.x] = s_qcnt;
+    W.qfirst[1024 + blockIdx.x] = (uint32_t)w0 * LPG_CHUNK;
   }
 }
 
@@ -1280,7 +1195,7 @@ __device__ __forceinline__ uint64_t q_get(const DevWorld& W, int phase, const ui
     int mid = (lo + hi + 1) >> 1;
     if (s_pre[mid] <= q) lo = mid; else hi = mid - 1;
   }
-  return W.evq[(int64_t)W.qfirst[phase * 1024 + lo] * LPG_CHUNK + (q - s_pre[lo])];
+  return W.evq[(int64_t)W.qfirst[phase * 1024 + lo] + (q - s_pre[lo])];
 }
 
 __device__ __forceinline__ uint32_t q_prefix(const DevWorld& W, int phase, uint32_t* s_pre, int nslabs) {
@@ -1298,12 +1213,15 @@ __device__ __forceinline__ uint32_t q_prefix(const DevWorld& W, int phase, uint3
   return s_pre[nslabs];
 }
 
-/* Queue of k_sweep<0>: deaths (bookkeeping of get_deaths, model.py:1767-1781)
+/* Queue of k_sweep_due: deaths (bookkeeping of get_deaths, model.py:1767-1781)
  * and disease progression (disease_state_step_kernel, model.py:393-454). */
 __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
   __shared__ uint32_t s_pre[1025];
   const uint32_t n = q_prefix(W, 0, s_pre, nslabs);
-  if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&W.ctr[LPG_CTR_QUEUE_DS], (unsigned long long)n);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (n) atomicAdd(&W.ctr[LPG_CTR_QUEUE_DS], (unsigned long long)n);
+    *W.due_n = 0; /* k_sweep_due has read it; k_due of the next tick appends */
+  }
   const int64_t G = W.G;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const uint32_t q = base + threadIdx.x;
@@ -1432,7 +1350,7 @@ __global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
   }
 }
 
-/* Queue of k_sweep<1>: the draws of RI (fast_ri, model.py:1845-1854) and of
+/* Queue of k_sweep_rs: the draws of RI (fast_ri, model.py:1845-1854) and of
  * the SIA campaigns of the day (fast_sia, :2047-2059), in that order per
  * agent.  Probability tests are integer compares of the 53-bit draw with
  * precomputed thresholds (same outcome as the double compares). */
