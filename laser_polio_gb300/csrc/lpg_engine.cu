@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -20,6 +21,19 @@
 #include "lpg_kernels.cuh"
 
 namespace {
+
+/* Kernels a tick needs only on some ticks; the host knows the schedule, so
+ * a tick without them does not launch them. */
+enum { NEED_NB = 1, NEED_SEED = 2, NEED_RS = 4 };
+static bool kernel_needed(int k, uint8_t need) {
+  switch (k) {
+    case 1: return (need & NEED_NB) != 0;
+    case 5: return (need & NEED_SEED) != 0;
+    case 6:
+    case 7: return (need & NEED_RS) != 0;
+    default: return true;
+  }
+}
 
 const char* kKernelNames[] = {"k_begin", "k_newborns", "k_due", "k_sweep_a", "k_dsq", "k_seed",
                               "k_sweep_b", "k_evb", "k_node_tx", "k_select", "k_end"};
@@ -63,8 +77,10 @@ struct lpg_handle {
   bool started = false;
   std::string err;
   bool use_graphs = true;
-  cudaGraphExec_t graph = nullptr;
+  std::map<uint32_t, std::pair<cudaGraphExec_t, int>> graphs; /* by the needs of 8 ticks: graph, launches */
   bool graph_failed = false;
+  std::vector<uint8_t> tick_need; /* per tick: the optional kernels some simulation needs (NEED_*) */
+  int32_t next_tick = 0;          /* the tick the next launch runs */
   bool profiling = false;
   double prof_ms[16] = {0};
   int64_t prof_n[16] = {0};
@@ -412,7 +428,7 @@ extern "C" int lpg_bind_columns(lpg_handle* h, int32_t sim, const lpg_columns* c
   return LPG_OK;
 }
 
-static int launch_tick(lpg_handle* h, bool capture);
+static int launch_tick(lpg_handle* h, uint8_t need, int* n_launched);
 
 extern "C" int lpg_start(lpg_handle* h) {
   if (!h) return LPG_ERR_ARG;
@@ -687,6 +703,17 @@ extern "C" int lpg_start(lpg_handle* h) {
     for (int tt = 0; tt < d.nt; ++tt)
       for (auto& e : s.seeds)
         if (e.tick > tt) future[tt] = 1;
+    /* the ticks that need the optional kernels (the conditions k_begin sets
+     * vd_tick, ri_tick, sia_n and seed_n by) */
+    if ((int)h->tick_need.size() < d.nt) h->tick_need.resize(d.nt, 0);
+    for (int tt = 1; tt < d.nt; ++tt) {
+      uint8_t m = 0;
+      if ((d.components & LPG_COMP_VD) && tt % rp.vd_step == 0) m |= NEED_NB;
+      if ((d.components & LPG_COMP_DS) && dcnt_[tt] > 0) m |= NEED_SEED;
+      if ((d.components & LPG_COMP_RI) && rp.ri_enabled && tt % rp.ri_step == 0) m |= NEED_RS;
+      if ((d.components & LPG_COMP_SIA) && scnt[tt] > 0) m |= NEED_RS;
+      h->tick_need[tt] |= m;
+    }
     int32_t* i32;
     uint8_t* u8;
     if (dupload(h, &i32, sfirst)) return LPG_ERR_NOMEM;
@@ -836,6 +863,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_select, 256, 0));
   h->select_blocks = std::min(1024, std::max(1, std::min(occ, 2)) * h->sm_count);
+  h->next_tick = 1; /* tick 0 ran above (k_end); the components run from tick 1 */
   h->started = true;
   return LPG_OK;
 }
@@ -882,20 +910,34 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
   return 0;
 }
 
-static int launch_tick(lpg_handle* h, bool capture) {
-  (void)capture;
+static uint8_t need_of(const lpg_handle* h, int64_t t) {
+  return (t >= 0 && t < (int64_t)h->tick_need.size()) ? h->tick_need[(size_t)t] : 0;
+}
+
+static int launch_tick(lpg_handle* h, uint8_t need, int* n_launched) {
   for (int k = 0; k < kNumTickKernels; ++k) {
+    if (!kernel_needed(k, need)) continue;
     int rc = launch_one(h, k, false);
     if (rc) return rc;
+    ++*n_launched;
   }
   return 0;
 }
 
-static int build_graph(lpg_handle* h) {
+/* The graph of kTicksPerGraph ticks whose needs pack into key (3 bits a
+ * tick), captured on first use; null if capture is not available. */
+static int get_graph(lpg_handle* h, uint32_t key, cudaGraphExec_t* out, int* n_launched) {
+  auto it = h->graphs.find(key);
+  if (it != h->graphs.end()) {
+    *out = it->second.first;
+    *n_launched = it->second.second;
+    return 0;
+  }
+  *out = nullptr;
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  int rc = 0;
-  for (int t = 0; t < kTicksPerGraph && !rc; ++t) rc = launch_tick(h, true);
+  int rc = 0, n = 0;
+  for (int t = 0; t < kTicksPerGraph && !rc; ++t) rc = launch_tick(h, (uint8_t)((key >> (3 * t)) & 7u), &n);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   if (rc || e != cudaSuccess || !g) {
     if (g) cudaGraphDestroy(g);
@@ -903,13 +945,17 @@ static int build_graph(lpg_handle* h) {
     h->graph_failed = true;
     return 0;
   }
-  e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphExec_t ge = nullptr;
+  e = cudaGraphInstantiate(&ge, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    h->graph = nullptr;
     h->graph_failed = true;
+    return 0;
   }
+  h->graphs[key] = {ge, n};
+  *out = ge;
+  *n_launched = n;
   return 0;
 }
 
@@ -924,39 +970,45 @@ extern "C" int lpg_step(lpg_handle* h, int32_t n_ticks) {
       for (auto& e : h->ev_pool) CK(cudaEventCreate(&e));
     }
     for (int t = 0; t < n_ticks; ++t) {
+      const uint8_t need = need_of(h, h->next_tick);
       for (int k = 0; k < kNumTickKernels; ++k) {
+        if (!kernel_needed(k, need)) continue;
         int rc = launch_one(h, k, true);
         if (rc) return rc;
       }
       CK(cudaStreamSynchronize(h->stream));
       for (int k = 0; k < kNumTickKernels; ++k) {
+        if (!kernel_needed(k, need)) continue;
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, h->ev_pool[2 * k], h->ev_pool[2 * k + 1]));
         h->prof_ms[k] += ms;
         h->prof_n[k] += 1;
+        h->launches += 1;
       }
-      h->launches += kNumTickKernels;
+      h->next_tick += 1;
     }
     return LPG_OK;
   }
   int left = n_ticks;
-  if (h->use_graphs && !h->graph_failed && n_ticks >= kTicksPerGraph) {
-    if (!h->graph) {
-      int rc = build_graph(h);
-      if (rc) return rc;
-    }
-    if (h->graph) {
-      while (left >= kTicksPerGraph) {
-        CK(cudaGraphLaunch(h->graph, h->stream));
-        h->launches += (int64_t)kTicksPerGraph * kNumTickKernels;
-        left -= kTicksPerGraph;
-      }
-    }
+  while (h->use_graphs && !h->graph_failed && left >= kTicksPerGraph) {
+    uint32_t key = 0;
+    for (int t = 0; t < kTicksPerGraph; ++t) key |= (uint32_t)need_of(h, (int64_t)h->next_tick + t) << (3 * t);
+    cudaGraphExec_t ge = nullptr;
+    int n = 0;
+    int rc = get_graph(h, key, &ge, &n);
+    if (rc) return rc;
+    if (!ge) break;
+    CK(cudaGraphLaunch(ge, h->stream));
+    h->launches += n;
+    h->next_tick += kTicksPerGraph;
+    left -= kTicksPerGraph;
   }
   for (; left > 0; --left) {
-    int rc = launch_tick(h, false);
+    int n = 0;
+    int rc = launch_tick(h, need_of(h, h->next_tick), &n);
     if (rc) return rc;
-    h->launches += kNumTickKernels;
+    h->launches += n;
+    h->next_tick += 1;
   }
   return LPG_OK;
 }
@@ -1136,7 +1188,7 @@ extern "C" void lpg_destroy(lpg_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second.first);
   for (auto e : h->ev_pool) cudaEventDestroy(e);
   for (void* p : h->allocs) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);

@@ -2208,14 +2208,24 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
     /* target offsets of all nodes; every CTA computes the same values and
      * keeps them in shared memory when they fit */
     int64_t carry = 0;
-    for (int base = 0; base < G; base += blockDim.x) {
-      const int g = base + threadIdx.x;
-      const int64_t k = g < G ? __ldcg(&W.ksel[g]) : 0;
+    for (int base = 0; base < G; base += 4 * blockDim.x) {
+      /* 4 consecutive nodes a thread: one block scan per 4 * blockDim nodes */
+      const int g0 = base + 4 * threadIdx.x;
+      int64_t k[4], sum = 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        k[u] = g0 + u < G ? __ldcg(&W.ksel[g0 + u]) : 0;
+        sum += k[u];
+      }
       int64_t tot;
-      const int64_t ex = block_excl_scan(k, &tot);
-      if (g < G) {
-        if (offs_in_smem) s_off[g] = carry + ex;
-        else W.tgt_off[g] = carry + ex;
+      int64_t run = carry + block_excl_scan(sum, &tot);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (g0 + u < G) {
+          if (offs_in_smem) s_off[g0 + u] = run;
+          else W.tgt_off[g0 + u] = run;
+        }
+        run += k[u];
       }
       carry += tot;
     }
