@@ -111,10 +111,9 @@ NCU_TRAFFIC_SOURCE = {}
 #   k_sweep_due (k_sweep_a): per listed 128-slot sub-block its 8 B list
 #     entry and 128 state bytes; 512 B of event ticks and a 4 B index write
 #     when an event is due; 512 B of dates of death and a 4 B index write
-#     when a death is due; 8 B per queue entry written.
-#   k_dsq: per queue entry the 8 B entry, then state, strain, three timers
-#     and the event tick read (9 B) and state, timers and event tick written
-#     (8 B).
+#     when a death is due; per queue entry the 8 B entry written and read
+#     back, then state, strain, three timers and the event tick read (9 B)
+#     and state, timers and event tick written (8 B).
 #   k_evb: per queue entry the 8 B entry, then state, RI timer, flags and
 #     date of birth read (10 B) and state and timer written (5 B).
 #   k_select: per target located, the chunk prefix entry (8 B), the
@@ -145,8 +144,7 @@ def kernel_alg_bytes(params, ticks, cnt, work, new_exposed):
         "k_due": SWEEP_INDEX_B * work["sweep_index"] + DUE_ITEM_B * work["sweep_due"],
         "k_sweep_a": (DUE_ITEM_B * work["sweep_due"] + SWEEP_DUE_B * work["sweep_due"]
                       + SWEEP_EVT_B * work["sweep_evt_due"] + SWEEP_DOD_B * work["sweep_dod_due"]
-                      + QUEUE_ENTRY_B * work["queue_ds"]),
-        "k_dsq": DSQ_ENTRY_B * work["queue_ds"],
+                      + (QUEUE_ENTRY_B + DSQ_ENTRY_B) * work["queue_ds"]),
         "k_sweep_b": (float(sum(sweep_b_bytes(params, t) * cnt[t] for t in ticks)) + RI_INDEX_B * work["ri_index"]
                       + RI_DUE_B * work["ri_due"] + QUEUE_ENTRY_B * work["queue_rs"]),
         "k_evb": EVB_ENTRY_B * work["queue_rs"],

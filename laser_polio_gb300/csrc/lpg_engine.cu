@@ -28,16 +28,16 @@ enum { NEED_NB = 1, NEED_SEED = 2, NEED_RS = 4 };
 static bool kernel_needed(int k, uint8_t need) {
   switch (k) {
     case 1: return (need & NEED_NB) != 0;
-    case 5: return (need & NEED_SEED) != 0;
-    case 6:
-    case 7: return (need & NEED_RS) != 0;
+    case 4: return (need & NEED_SEED) != 0;
+    case 5:
+    case 6: return (need & NEED_RS) != 0;
     default: return true;
   }
 }
 
-const char* kKernelNames[] = {"k_begin", "k_newborns", "k_due", "k_sweep_a", "k_dsq", "k_seed",
+const char* kKernelNames[] = {"k_begin", "k_newborns", "k_due", "k_sweep_a", "k_seed",
                               "k_sweep_b", "k_evb", "k_node_tx", "k_select", "k_end"};
-constexpr int kNumTickKernels = 11;
+constexpr int kNumTickKernels = 10;
 constexpr int kTicksPerGraph = 8;
 
 /* Reference-ordered columns of one simulation on the device. */
@@ -884,12 +884,11 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 1: k_newborns<<<dim3(h->sm_count * 8, R), 256, 0, st>>>(W); break;
     case 2: k_due<<<h->due_blocks, 256, 0, st>>>(W); break;
     case 3: k_sweep_due<<<h->sweep0_blocks, LPG_SWEEP_BLOCK, 0, st>>>(W); break;
-    case 4: k_dsq<<<h->sm_count * 4, 256, 0, st>>>(W, h->sweep0_blocks); break;
-    case 5: k_seed<<<R, 1024, 0, st>>>(W); break;
-    case 6: k_sweep_rs<<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 7: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
-    case 8: k_node_tx<<<G, LPG_NODE_TX_THREADS, 0, st>>>(W); break;
-    case 9: {
+    case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
+    case 5: k_sweep_rs<<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
+    case 6: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
+    case 7: k_node_tx<<<G, LPG_NODE_TX_THREADS, 0, st>>>(W); break;
+    case 8: {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(h->select_blocks);
       cfg.blockDim = dim3(256);
@@ -903,7 +902,7 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
       CK(cudaLaunchKernelEx(&cfg, k_select, W));
       break;
     }
-    case 10: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
+    case 9: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
   }
   CK(cudaGetLastError());
   if (timed) CK(cudaEventRecord(e1, st));

@@ -206,7 +206,7 @@ typedef struct {
   uint32_t* qcnt;    /* [2][1024] entries per slab (k_sweep_due, k_sweep_rs) */
   uint32_t* qfirst;  /* [2][1024] first entry of the slab of each sweep CTA in evq */
   uint64_t* due;     /* sub-blocks with something due this tick: sub-block | sim << 32 | what << 48 */
-  uint32_t* due_n;   /* entries of due (k_due appends, k_dsq clears) */
+  uint32_t* due_n;   /* entries of due (k_due appends, k_end clears) */
   /* grid barrier of the cooperative selection kernel */
   uint32_t* bar_count;
   uint32_t* bar_gen;

@@ -11,10 +11,9 @@
  *   k_due        the sub-blocks with a disease-state event or a death due,
  *                from the per-sub-block indexes
  *   k_sweep_due  those sub-blocks, evenly over the CTAs: deaths (get_deaths,
- *                model.py:1767-1781) and the queue of agents in E or I
- *                whose event is now
- *   k_dsq        death bookkeeping and disease progression and paralysis of
- *                the queued agents (model.py:393-454)
+ *                model.py:1767-1781), then each CTA's queue of deaths and
+ *                of agents in E or I whose event is now: death bookkeeping,
+ *                disease progression and paralysis (model.py:393-454)
  *   k_seed       the seed schedule (model.py:759-786)
  *   k_sweep_rs   on RI/SIA ticks: the queue of agents that RI (fast_ri,
  *                :1784-1855; due sub-blocks only) or today's SIA campaigns
@@ -457,8 +456,8 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
 
 /* The sweeps.
  *   k_due, k_sweep_due: deaths (get_deaths, model.py:1767-1781) on VD ticks
- *            and the queue of agents in E or I whose disease-state event is
- *            due (k_dsq), through the sub-block indexes.
+ *            and the agents in E or I whose disease-state event is due,
+ *            through the sub-block indexes.
  *   k_sweep_rs: routine immunisation (fast_ri, model.py:1784-1855) and SIA
  *            campaigns (fast_sia, :1994-2060), on the ticks that have them,
  *            after progression and the seed schedule as in default_run_order.
@@ -838,99 +837,6 @@ __global__ void __launch_bounds__(256) k_due(DevWorld W) {
   }
 }
 
-/* The due sub-blocks of W.due, split evenly over the CTAs (an outbreak makes
- * most sub-blocks of a few nodes due while most others have none), 8 lanes
- * per sub-block (16 slots each): state bytes, the dates of death when a
- * death is due and the event ticks when an event is due.  Deaths
- * (model.py:1767-1781; this tick's newborns are not checked), the queue of
- * the agents whose event is now, and the sub-block's new earliest event
- * and date of death over the rest, with no atomics.  A CTA's queue slab
- * starts at its first item times 128 entries of evq. */
-__global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_due(DevWorld W) {
-  __shared__ uint32_t s_qcnt;
-  const int lane = threadIdx.x & 31;
-  const int64_t D = (int64_t)*(volatile uint32_t*)W.due_n;
-  const int64_t i0 = D * blockIdx.x / gridDim.x, i1 = D * (blockIdx.x + 1) / gridDim.x;
-  uint64_t* slab = W.evq + i0 * LPG_SUB;
-  if (threadIdx.x == 0) s_qcnt = 0;
-  __syncthreads();
-  uint32_t n_due = 0, n_edue = 0, n_ddue = 0; /* work counters, lanes (lane & 7) == 0 */
-  const int per_pass = (blockDim.x / 32) * 4;
-  for (int64_t base = i0; base < i1; base += per_pass) {
-    const int64_t item = base + (threadIdx.x >> 5) * 4 + (lane >> 3);
-    const bool on = item < i1;
-    const uint64_t rec = on ? __ldcg(W.due + item) : 0ULL;
-    const int64_t sb = (int64_t)(uint32_t)rec;
-    const uint32_t f = (uint32_t)(rec >> 48);
-    const bool edue = (f & 1u) != 0, ddue = (f & 2u) != 0;
-    const int t = on ? W.reps[(rec >> 32) & 0xffffu].cur_t : 0;
-    if (on && (lane & 7) == 0) {
-      n_due += 1;
-      n_edue += edue ? 1 : 0;
-      n_ddue += ddue ? 1 : 0;
-    }
-    const int64_t pos0 = sb * LPG_SUB + (int64_t)(lane & 7) * 16;
-    const uint4 v = on ? ldg_stream16(W.ds + pos0) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-    uint32_t dead = 0;
-    if (__ballot_sync(FULLMASK, ddue)) {
-      int32_t nmin = LPG_NO_DOD;
-      if (ddue) {
-        const int4* d4 = reinterpret_cast<const int4*>(W.dod + pos0);
-        int4 dq[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) dq[q] = d4[q];
-        const int4 m = W.cmeta[pos0 >> 11];
-        const int off = (int)(pos0 & (LPG_CHUNK - 1));
-        const int nbo = (m.z == t) ? m.w : LPG_CHUNK; /* this tick's newborns are not checked */
-        const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int32_t dd[4] = {dq[q].x, dq[q].y, dq[q].z, dq[q].w};
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int k = 4 * q + j;
-            const bool alive = ((wv[q] >> (8 * j + 7)) & 1u) == 0;
-            const bool dies = alive && dd[j] <= t && off + k < nbo;
-            dead |= (uint32_t)dies << k;
-            if (alive && !dies) nmin = min(nmin, dd[j]);
-          }
-        }
-        if (dead) {
-          uint4 out = v;
-          uint32_t* ow = reinterpret_cast<uint32_t*>(&out);
-#pragma unroll
-          for (int k = 0; k < 16; ++k)
-            if ((dead >> k) & 1u) ow[k >> 2] |= 0xffu << (8 * (k & 3));
-          *reinterpret_cast<uint4*>(W.ds + pos0) = out;
-        }
-      }
-      nmin = sub8_min(nmin);
-      if (ddue && (lane & 7) == 0) W.sub_dod[sb] = nmin;
-    }
-    uint32_t ei = 0;
-    if (__ballot_sync(FULLMASK, edue)) {
-      int32_t nmin = LPG_NO_DOD;
-      if (edue) ei = ev_due16(W, pos0, v, dead, t, nmin);
-      nmin = sub8_min(nmin);
-      /* the agents due now get their next event from k_dsq (atomicMin) */
-      if (edue && (lane & 7) == 0) W.sub_evt[sb] = nmin;
-    }
-    queue_a16(slab, &s_qcnt, pos0, ei, dead, v);
-  }
-  n_due = __reduce_add_sync(FULLMASK, n_due);
-  n_edue = __reduce_add_sync(FULLMASK, n_edue);
-  n_ddue = __reduce_add_sync(FULLMASK, n_ddue);
-  if (lane == 0 && n_due) {
-    atomicAdd(&W.ctr[LPG_CTR_SWEEP_DUE], (unsigned long long)n_due);
-    atomicAdd(&W.ctr[LPG_CTR_SWEEP_EVT_DUE], (unsigned long long)n_edue);
-    atomicAdd(&W.ctr[LPG_CTR_SWEEP_DOD_DUE], (unsigned long long)n_ddue);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    W.qcnt[blockIdx.x] = s_qcnt;
-    W.qfirst[blockIdx.x] = (uint32_t)(i0 * LPG_SUB);
-  }
-}
 
 /* k_sweep_rs on an RI tick without SIA, over one simulation's sub-blocks
  * [sb0, sb0 + nsb), in windows of LPG_DUE_MAX sub-blocks: the CTA lists the
@@ -1188,7 +1094,7 @@ __device__ __forceinline__ void warp_sub_w(unsigned long long* p, unsigned peers
   if ((threadIdx.x & 31) == __ffs(peers) - 1 && tot) atomicAdd(p, neg64(tot));
 }
 
-/* Entry q of the queue of sweep PHASE (prefix of the slab sizes in s_pre). */
+/* Entry q of the queue of k_sweep_rs (prefix of the slab sizes in s_pre). */
 __device__ __forceinline__ uint64_t q_get(const DevWorld& W, int phase, const uint32_t* s_pre, int nslabs, uint32_t q) {
   int lo = 0, hi = nslabs - 1;
   while (lo < hi) {
@@ -1213,140 +1119,232 @@ __device__ __forceinline__ uint32_t q_prefix(const DevWorld& W, int phase, uint3
   return s_pre[nslabs];
 }
 
-/* Queue of k_sweep_due: deaths (bookkeeping of get_deaths, model.py:1767-1781)
- * and disease progression (disease_state_step_kernel, model.py:393-454). */
-__global__ void __launch_bounds__(256) k_dsq(DevWorld W, int nslabs) {
-  __shared__ uint32_t s_pre[1025];
-  const uint32_t n = q_prefix(W, 0, s_pre, nslabs);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    if (n) atomicAdd(&W.ctr[LPG_CTR_QUEUE_DS], (unsigned long long)n);
-    *W.due_n = 0; /* k_sweep_due has read it; k_due of the next tick appends */
-  }
+/* One entry e of k_sweep_due's queue (on: the lane has one; all 32 lanes of
+ * the warp call): death bookkeeping (get_deaths, model.py:1767-1781) or the
+ * disease-state step of an agent whose event is now
+ * (disease_state_step_kernel, model.py:393-454), node totals summed per
+ * warp before the atomics. */
+__device__ __forceinline__ void ds_queue_step(DevWorld& W, uint64_t e, bool on) {
   const int64_t G = W.G;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-    const uint32_t q = base + threadIdx.x;
-    const bool on = q < n;
-    int g = -1, st = 0;
-    int32_t dS = 0, dE = 0, dI = 0, dR = 0, dPP = 0, dP = 0, nPP = 0, nP = 0, nDead = 0;
-    if (on) {
-      const uint64_t e = q_get(W, 0, s_pre, nslabs, q);
-      const int64_t pos = (int64_t)(uint32_t)e;
-      const uint32_t kind = (uint32_t)(e >> 32) & 0xffffu;
-      const int64_t cid = pos / LPG_CHUNK;
-      g = W.cmeta[cid].x;
-      const DevRep* rp = &W.reps[W.node_rep[g]];
-      const int t = rp->cur_t;
-      if (kind == QA_DEATH) {
-        const int8_t s = (int8_t)(uint8_t)(e >> 48);
-        nDead = 1;
-        if (s == 0) {
-          dS = -1;
-          const uint64_t w = fix_risk(W.risk[pos]);
-          if (w) {
-            atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
-            atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
-            atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
-          }
-        } else if (s == 1 || s == 2) {
-          st = W.strain[pos];
-          if (s == 1) {
-            dE = -1;
-          } else {
-            dI = -1;
-            const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-            if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
-          }
-          /* timers frozen at death: brought up to the step of t - 1 (they
-           * count down only where disease states are stepped) */
-          int8_t et = W.et[pos], it = W.it[pos], pt = W.pt[pos];
-          const int k = (rp->comps & LPG_COMP_DS) ? t - W.evt[pos] + ev_pure(s, (int8_t)st, et, it, pt, W.pp[pos]) : 0;
-          if (k > 0) {
-            ev_advance(s, (int8_t)st, et, it, pt, k);
-            if (s == 1) W.et[pos] = et;
-            else {
-              W.it[pos] = it;
-              if (st == 0) W.pt[pos] = pt;
-            }
-          }
-        } else if (s == 3) {
-          dR = -1;
+  int g = -1, st = 0;
+  int32_t dS = 0, dE = 0, dI = 0, dR = 0, dPP = 0, dP = 0, nPP = 0, nP = 0, nDead = 0;
+  if (on) {
+    const int64_t pos = (int64_t)(uint32_t)e;
+    const uint32_t kind = (uint32_t)(e >> 32) & 0xffffu;
+    const int64_t cid = pos / LPG_CHUNK;
+    g = W.cmeta[cid].x;
+    const DevRep* rp = &W.reps[W.node_rep[g]];
+    const int t = rp->cur_t;
+    if (kind == QA_DEATH) {
+      const int8_t s = (int8_t)(uint8_t)(e >> 48);
+      nDead = 1;
+      if (s == 0) {
+        dS = -1;
+        const uint64_t w = fix_risk(W.risk[pos]);
+        if (w) {
+          atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
+          atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
+          atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
         }
-        /* the RI timer stops at death: its value after the RI ticks before t */
-        if (ri_runs(rp) && W.cm[pos] != 1) W.ri[pos] = ri_now(rp, W.ri[pos], W.ref[pos], W.dob[pos], t - 1);
-        if (W.pp[pos] == 1) dPP -= 1;
-        if (W.par[pos] == 1) dP -= 1;
-      } else {
-        /* an event step of an agent in E or I (its evt is t) */
-        const int8_t s0 = W.ds[pos];
-        int8_t s = s0;
+      } else if (s == 1 || s == 2) {
         st = W.strain[pos];
-        int8_t et = W.et[pos], it = W.it[pos], pt = W.pt[pos], pp = W.pp[pos];
-        /* the count-downs skipped since the timers were last brought up to date */
-        ev_advance(s0, (int8_t)st, et, it, pt, t - W.evt[pos] + ev_pure(s0, (int8_t)st, et, it, pt, pp));
         if (s == 1) {
-          if (et <= 0) {
-            s = 2;
-            dE -= 1;
-            dI += 1;
-            const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-            if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], (unsigned long long)bw);
-          }
-          et = dec_i8(et);
-          W.et[pos] = et;
+          dE = -1;
+        } else {
+          dI = -1;
+          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
         }
-        if (s == 2) {
-          if (it <= 0) {
-            s = 3;
-            dI -= 1;
-            dR += 1;
-            const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-            if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
+        /* timers frozen at death: brought up to the step of t - 1 (they
+         * count down only where disease states are stepped) */
+        int8_t et = W.et[pos], it = W.it[pos], pt = W.pt[pos];
+        const int k = (rp->comps & LPG_COMP_DS) ? t - W.evt[pos] + ev_pure(s, (int8_t)st, et, it, pt, W.pp[pos]) : 0;
+        if (k > 0) {
+          ev_advance(s, (int8_t)st, et, it, pt, k);
+          if (s == 1) W.et[pos] = et;
+          else {
+            W.it[pos] = it;
+            if (st == 0) W.pt[pos] = pt;
           }
-          it = dec_i8(it);
-          W.it[pos] = it;
-          if (st == 0) {
-            if (pt <= 0 && pp == -1) {
-              if (W.ipv[pos] == 0) {
-                pp = 1;
-                dPP += 1;
-                nPP += 1;
-                if (lpg_u53(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < rp->thr_par) {
-                  W.par[pos] = 1;
-                  dP += 1;
-                  nP += 1;
-                }
-              } else {
-                pp = 0;
+        }
+      } else if (s == 3) {
+        dR = -1;
+      }
+      /* the RI timer stops at death: its value after the RI ticks before t */
+      if (ri_runs(rp) && W.cm[pos] != 1) W.ri[pos] = ri_now(rp, W.ri[pos], W.ref[pos], W.dob[pos], t - 1);
+      if (W.pp[pos] == 1) dPP -= 1;
+      if (W.par[pos] == 1) dP -= 1;
+    } else {
+      /* an event step of an agent in E or I (its evt is t) */
+      const int8_t s0 = W.ds[pos];
+      int8_t s = s0;
+      st = W.strain[pos];
+      int8_t et = W.et[pos], it = W.it[pos], pt = W.pt[pos], pp = W.pp[pos];
+      /* the count-downs skipped since the timers were last brought up to date */
+      ev_advance(s0, (int8_t)st, et, it, pt, t - W.evt[pos] + ev_pure(s0, (int8_t)st, et, it, pt, pp));
+      if (s == 1) {
+        if (et <= 0) {
+          s = 2;
+          dE -= 1;
+          dI += 1;
+          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], (unsigned long long)bw);
+        }
+        et = dec_i8(et);
+        W.et[pos] = et;
+      }
+      if (s == 2) {
+        if (it <= 0) {
+          s = 3;
+          dI -= 1;
+          dR += 1;
+          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
+        }
+        it = dec_i8(it);
+        W.it[pos] = it;
+        if (st == 0) {
+          if (pt <= 0 && pp == -1) {
+            if (W.ipv[pos] == 0) {
+              pp = 1;
+              dPP += 1;
+              nPP += 1;
+              if (lpg_u53(rp->seed, LPG_P_PARALYSIS, t, W.ref[pos], 0, 0) < rp->thr_par) {
+                W.par[pos] = 1;
+                dP += 1;
+                nP += 1;
               }
-              W.pp[pos] = pp;
+            } else {
+              pp = 0;
             }
-            pt = dec_i8(pt);
-            W.pt[pos] = pt;
+            W.pp[pos] = pp;
           }
-        }
-        if (s != s0) W.ds[pos] = s;
-        if (s == 1 || s == 2) {
-          const int32_t e1 = t + 1 + ev_pure(s, (int8_t)st, et, it, pt, pp);
-          W.evt[pos] = e1;
-          atomicMin(&W.sub_evt[pos >> 7], e1);
+          pt = dec_i8(pt);
+          W.pt[pos] = pt;
         }
       }
+      if (s != s0) W.ds[pos] = s;
+      if (s == 1 || s == 2) {
+        const int32_t e1 = t + 1 + ev_pure(s, (int8_t)st, et, it, pt, pp);
+        W.evt[pos] = e1;
+        atomicMin(&W.sub_evt[pos >> 7], e1);
+      }
     }
-    /* nothing to add when every delta of the warp is zero */
-    const bool any = on && (dS | dE | dI | dR | dPP | dP | nPP | nP | nDead);
-    const unsigned act = __ballot_sync(FULLMASK, any);
-    if (!any) continue;
-    const unsigned by_node = __match_any_sync(act, g);
-    warp_add(&W.ev[(int64_t)EV_DEATHS * G + g], by_node, nDead);
-    warp_add(&W.tot[(int64_t)TT_S * G + g], by_node, dS);
-    warp_add(&W.tot[(int64_t)TT_R * G + g], by_node, dR);
-    warp_add(&W.tot[(int64_t)TT_POTP * G + g], by_node, dPP);
-    warp_add(&W.tot[(int64_t)TT_P * G + g], by_node, dP);
-    warp_add(&W.ev[(int64_t)EV_NEWPOT * G + g], by_node, nPP);
-    warp_add(&W.ev[(int64_t)EV_NEWPAR * G + g], by_node, nP);
-    const unsigned by_ns = __match_any_sync(act, g * LPG_MAX_STRAINS + st);
-    warp_add(&W.tot[(int64_t)(TT_E0 + st) * G + g], by_ns, dE);
-    warp_add(&W.tot[(int64_t)(TT_I0 + st) * G + g], by_ns, dI);
+  }
+  /* nothing to add when every delta of the warp is zero */
+  const bool any = on && (dS | dE | dI | dR | dPP | dP | nPP | nP | nDead);
+  const unsigned act = __ballot_sync(FULLMASK, any);
+  if (!any) return;
+  const unsigned by_node = __match_any_sync(act, g);
+  warp_add(&W.ev[(int64_t)EV_DEATHS * G + g], by_node, nDead);
+  warp_add(&W.tot[(int64_t)TT_S * G + g], by_node, dS);
+  warp_add(&W.tot[(int64_t)TT_R * G + g], by_node, dR);
+  warp_add(&W.tot[(int64_t)TT_POTP * G + g], by_node, dPP);
+  warp_add(&W.tot[(int64_t)TT_P * G + g], by_node, dP);
+  warp_add(&W.ev[(int64_t)EV_NEWPOT * G + g], by_node, nPP);
+  warp_add(&W.ev[(int64_t)EV_NEWPAR * G + g], by_node, nP);
+  const unsigned by_ns = __match_any_sync(act, g * LPG_MAX_STRAINS + st);
+  warp_add(&W.tot[(int64_t)(TT_E0 + st) * G + g], by_ns, dE);
+  warp_add(&W.tot[(int64_t)(TT_I0 + st) * G + g], by_ns, dI);
+}
+
+
+/* The due sub-blocks of W.due, split evenly over the CTAs (an outbreak makes
+ * most sub-blocks of a few nodes due while most others have none), 8 lanes
+ * per sub-block (16 slots each): state bytes, the dates of death when a
+ * death is due and the event ticks when an event is due.  Deaths
+ * (model.py:1767-1781; this tick's newborns are not checked), the queue of
+ * the agents whose event is now, and the sub-block's new earliest event
+ * and date of death over the rest, with no atomics; then the steps of the
+ * queued agents (ds_queue_step).  A CTA's queue slab starts at its first
+ * item times 128 entries of evq. */
+__global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_due(DevWorld W) {
+  __shared__ uint32_t s_qcnt;
+  const int lane = threadIdx.x & 31;
+  const int64_t D = (int64_t)*(volatile uint32_t*)W.due_n;
+  const int64_t i0 = D * blockIdx.x / gridDim.x, i1 = D * (blockIdx.x + 1) / gridDim.x;
+  uint64_t* slab = W.evq + i0 * LPG_SUB;
+  if (threadIdx.x == 0) s_qcnt = 0;
+  __syncthreads();
+  uint32_t n_due = 0, n_edue = 0, n_ddue = 0; /* work counters, lanes (lane & 7) == 0 */
+  const int per_pass = (blockDim.x / 32) * 4;
+  for (int64_t base = i0; base < i1; base += per_pass) {
+    const int64_t item = base + (threadIdx.x >> 5) * 4 + (lane >> 3);
+    const bool on = item < i1;
+    const uint64_t rec = on ? __ldcg(W.due + item) : 0ULL;
+    const int64_t sb = (int64_t)(uint32_t)rec;
+    const uint32_t f = (uint32_t)(rec >> 48);
+    const bool edue = (f & 1u) != 0, ddue = (f & 2u) != 0;
+    const int t = on ? W.reps[(rec >> 32) & 0xffffu].cur_t : 0;
+    if (on && (lane & 7) == 0) {
+      n_due += 1;
+      n_edue += edue ? 1 : 0;
+      n_ddue += ddue ? 1 : 0;
+    }
+    const int64_t pos0 = sb * LPG_SUB + (int64_t)(lane & 7) * 16;
+    const uint4 v = on ? ldg_stream16(W.ds + pos0) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    uint32_t dead = 0;
+    if (__ballot_sync(FULLMASK, ddue)) {
+      int32_t nmin = LPG_NO_DOD;
+      if (ddue) {
+        const int4* d4 = reinterpret_cast<const int4*>(W.dod + pos0);
+        int4 dq[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dq[q] = d4[q];
+        const int4 m = W.cmeta[pos0 >> 11];
+        const int off = (int)(pos0 & (LPG_CHUNK - 1));
+        const int nbo = (m.z == t) ? m.w : LPG_CHUNK; /* this tick's newborns are not checked */
+        const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int32_t dd[4] = {dq[q].x, dq[q].y, dq[q].z, dq[q].w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int k = 4 * q + j;
+            const bool alive = ((wv[q] >> (8 * j + 7)) & 1u) == 0;
+            const bool dies = alive && dd[j] <= t && off + k < nbo;
+            dead |= (uint32_t)dies << k;
+            if (alive && !dies) nmin = min(nmin, dd[j]);
+          }
+        }
+        if (dead) {
+          uint4 out = v;
+          uint32_t* ow = reinterpret_cast<uint32_t*>(&out);
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            if ((dead >> k) & 1u) ow[k >> 2] |= 0xffu << (8 * (k & 3));
+          *reinterpret_cast<uint4*>(W.ds + pos0) = out;
+        }
+      }
+      nmin = sub8_min(nmin);
+      if (ddue && (lane & 7) == 0) W.sub_dod[sb] = nmin;
+    }
+    uint32_t ei = 0;
+    if (__ballot_sync(FULLMASK, edue)) {
+      int32_t nmin = LPG_NO_DOD;
+      if (edue) ei = ev_due16(W, pos0, v, dead, t, nmin);
+      nmin = sub8_min(nmin);
+      /* the agents due now get their next event in ds_queue_step (atomicMin) */
+      if (edue && (lane & 7) == 0) W.sub_evt[sb] = nmin;
+    }
+    queue_a16(slab, &s_qcnt, pos0, ei, dead, v);
+  }
+  n_due = __reduce_add_sync(FULLMASK, n_due);
+  n_edue = __reduce_add_sync(FULLMASK, n_edue);
+  n_ddue = __reduce_add_sync(FULLMASK, n_ddue);
+  if (lane == 0 && n_due) {
+    atomicAdd(&W.ctr[LPG_CTR_SWEEP_DUE], (unsigned long long)n_due);
+    atomicAdd(&W.ctr[LPG_CTR_SWEEP_EVT_DUE], (unsigned long long)n_edue);
+    atomicAdd(&W.ctr[LPG_CTR_SWEEP_DOD_DUE], (unsigned long long)n_ddue);
+  }
+  /* the CTA's own queue: its sub-blocks are its alone, so the steps need
+   * no other CTA's sweep (the index entries it wrote above come first) */
+  __syncthreads();
+  const uint32_t n = s_qcnt;
+  if (threadIdx.x == 0 && n) atomicAdd(&W.ctr[LPG_CTR_QUEUE_DS], (unsigned long long)n);
+  for (uint32_t b = 0; b < n; b += blockDim.x) {
+    const uint32_t q = b + threadIdx.x;
+    ds_queue_step(W, q < n ? slab[q] : 0ULL, q < n);
   }
 }
 
@@ -2396,6 +2394,7 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
 /* ------------------------------------------------------------------------ */
 /* Results rows of the tick and the tick advance. */
 __global__ void k_end(DevWorld W) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *W.due_n = 0; /* the due list of the tick is spent */
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= W.G) return;
   DevRep* rp = &W.reps[W.node_rep[g]];
