@@ -135,6 +135,19 @@ NODE_TX_CHUNK_B = 20.0
 RI_INDEX_B, RI_DUE_B = 4.0, 128.0 * 12.0 + 4.0
 
 
+def merge_selection(prof):
+    """The selection's three kernels (k_sel_locate, k_sel_claim,
+    k_sel_rounds) as one entry, k_select, per tick."""
+    out = {}
+    for k, (ms, n) in prof.items():
+        if k.startswith("k_sel_"):
+            m0, n0 = out.get("k_select", (0.0, 0))
+            out["k_select"] = (m0 + ms, max(n0, n))
+        else:
+            out[k] = (ms, n)
+    return out
+
+
 def kernel_alg_bytes(params, ticks, cnt, work, new_exposed):
     """Algorithmic bytes of each modelled kernel over the ticks (total, all
     launches), from the work counters of the same ticks."""
@@ -516,7 +529,7 @@ def main():
         h.set_profiling(True)
         h.step(K)
         h.sync()
-        prof = h.profile()
+        prof = merge_selection(h.profile())
         h.close()
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         peak = float(peaks.get("hbm_gbs", 6800.0))

@@ -36,8 +36,9 @@ static bool kernel_needed(int k, uint8_t need) {
 }
 
 const char* kKernelNames[] = {"k_begin", "k_newborns", "k_due", "k_sweep_a", "k_seed",
-                              "k_sweep_b", "k_evb", "k_node_tx", "k_select", "k_end"};
-constexpr int kNumTickKernels = 10;
+                              "k_sweep_b", "k_evb", "k_node_tx", "k_sel_locate", "k_sel_claim",
+                              "k_sel_rounds", "k_end"};
+constexpr int kNumTickKernels = 12;
 constexpr int kTicksPerGraph = 8;
 
 /* Reference-ordered columns of one simulation on the device. */
@@ -90,7 +91,8 @@ struct lpg_handle {
   int sweep_blocks = 0;  /* k_sweep_rs (staged through shared memory) */
   int sweep0_blocks = 0; /* k_sweep_due (direct loads, no staging) */
   int due_blocks = 0;    /* k_due */
-  int select_blocks = 0;
+  int select_blocks = 0; /* k_sel_locate, k_sel_rounds */
+  int claim_blocks = 0;
 };
 
 static int fail(lpg_handle* h, int code, const char* fmt, ...) {
@@ -566,9 +568,6 @@ extern "C" int lpg_start(lpg_handle* h) {
   int64_t hits = (int64_t)chunk_total * LPG_CHUNK;
   W.hits_cap = hits;
   rc |= dalloc(h, &W.hits, hits);
-  rc |= dalloc(h, &W.bar_count, 1);
-  rc |= dalloc(h, &W.bar_gen, 1);
-  rc |= dalloc(h, &W.abort_flag, 1);
   rc |= dalloc(h, &W.ctr, LPG_NUM_COUNTERS);
   rc |= dalloc(h, &W.reps, R);
   if (rc) return LPG_ERR_NOMEM;
@@ -583,9 +582,6 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaMemsetAsync(W.bb, 0, sizeof(uint64_t) * LPG_MAX_STRAINS * G, st));
   CK(cudaMemsetAsync(W.size, 0, sizeof(int64_t) * G, st));
   CK(cudaMemsetAsync(W.uniq, 0, sizeof(int64_t) * G, st));
-  CK(cudaMemsetAsync(W.bar_count, 0, 4, st));
-  CK(cudaMemsetAsync(W.bar_gen, 0, 4, st));
-  CK(cudaMemsetAsync(W.abort_flag, 0, 4, st));
   CK(cudaMemsetAsync(W.ctr, 0, sizeof(unsigned long long) * LPG_NUM_COUNTERS, st));
 
   /* 4. per-simulation static data, results, pools, chunk tables */
@@ -861,8 +857,11 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_due, 256, 0));
   h->due_blocks = std::max(1, occ) * h->sm_count;
   occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_select, 256, 0));
-  h->select_blocks = std::min(1024, std::max(1, std::min(occ, 2)) * h->sm_count);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sel_locate, 256, 0));
+  h->select_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
+  occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sel_claim, 256, 0));
+  h->claim_blocks = std::min(2048, std::max(1, occ) * h->sm_count);
   h->next_tick = 1; /* tick 0 ran above (k_end); the components run from tick 1 */
   h->started = true;
   return LPG_OK;
@@ -888,21 +887,10 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 5: k_sweep_rs<<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
     case 6: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
     case 7: k_node_tx<<<G, LPG_NODE_TX_THREADS, 0, st>>>(W); break;
-    case 8: {
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(h->select_blocks);
-      cfg.blockDim = dim3(256);
-      cfg.dynamicSmemBytes = 0;
-      cfg.stream = st;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeCooperative;
-      attr[0].val.cooperative = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      CK(cudaLaunchKernelEx(&cfg, k_select, W));
-      break;
-    }
-    case 9: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
+    case 8: k_sel_locate<<<h->select_blocks, 256, 0, st>>>(W); break;
+    case 9: k_sel_claim<<<h->claim_blocks, 256, 0, st>>>(W); break;
+    case 10: k_sel_rounds<<<h->select_blocks, 256, 0, st>>>(W); break;
+    case 11: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
   }
   CK(cudaGetLastError());
   if (timed) CK(cudaEventRecord(e1, st));
@@ -1017,9 +1005,6 @@ extern "C" int lpg_sync(lpg_handle* h) {
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   if (!h->started) return LPG_OK;
-  int32_t ab = 0;
-  CK(cudaMemcpy(&ab, h->W.abort_flag, 4, cudaMemcpyDeviceToHost));
-  if (ab) return fail(h, LPG_ERR_TIMEOUT, "a bounded grid barrier of the selection kernel timed out");
   std::vector<DevRep> reps(h->W.n_reps);
   CK(cudaMemcpy(reps.data(), h->W.reps, sizeof(DevRep) * reps.size(), cudaMemcpyDeviceToHost));
   for (size_t r = 0; r < reps.size(); ++r) {

@@ -207,10 +207,6 @@ typedef struct {
   uint32_t* qfirst;  /* [2][1024] first entry of the slab of each sweep CTA in evq */
   uint64_t* due;     /* sub-blocks with something due this tick: sub-block | sim << 32 | what << 48 */
   uint32_t* due_n;   /* entries of due (k_due appends, k_end clears) */
-  /* grid barrier of the cooperative selection kernel */
-  uint32_t* bar_count;
-  uint32_t* bar_gen;
-  int32_t* abort_flag;
   unsigned long long* ctr; /* [LPG_NUM_COUNTERS] work counters */
 } DevWorld;
 

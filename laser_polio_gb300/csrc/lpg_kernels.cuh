@@ -22,8 +22,8 @@
  *   k_node_tx    per node: population (model.py:1751-1755), mixing,
  *                seasonality, probabilities and exposure counts
  *                (model.py:1327-1407)
- *   k_select     cooperative: weighted selection rounds and strain
- *                assignment (tx_infect_nb, model.py:1010-1149)
+ *   k_sel_locate, k_sel_claim, k_sel_rounds   weighted selection rounds
+ *                and strain assignment (tx_infect_nb, model.py:1010-1149)
  *   k_end        results rows of the tick (model.py:1461-1487 and the
  *                result writes of every component)
  */
@@ -37,7 +37,6 @@
 #define FULLMASK 0xffffffffu
 #define LPG_NONE 0xffffffffu
 #define LPG_MAX_ROUNDS 1000000
-#define LPG_SPIN_LIMIT (1LL << 25)
 
 /* ------------------------------------------------------------------------ */
 /* fixed-point weights (identical definitions in the oracle)                */
@@ -1891,35 +1890,6 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* Software grid barrier for the cooperative selection kernel (all CTAs are
- * co-resident by cooperative launch).  Every wait is bounded: on timeout the
- * kernel raises abort_flag and all CTAs leave. */
-__device__ __forceinline__ bool grid_sync(DevWorld& W) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile uint32_t* genp = W.bar_gen;
-    uint32_t gen = *genp;
-    __threadfence();
-    uint32_t arrived = atomicAdd(W.bar_count, 1u) + 1u;
-    if (arrived == gridDim.x) {
-      atomicExch(W.bar_count, 0u);
-      __threadfence();
-      atomicAdd(W.bar_gen, 1u);
-    } else {
-      long long it = 0;
-      while (*genp == gen) {
-        __nanosleep(64);
-        if (++it > LPG_SPIN_LIMIT) {
-          atomicExch(W.abort_flag, 1);
-          break;
-        }
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return *(volatile int32_t*)W.abort_flag == 0;
-}
 
 /* Slot of target v inside chunk cid (v < the chunk's remaining weight):
  * sub-block by its 16 totals, slot by the 128 state bytes and risks.
@@ -2179,17 +2149,17 @@ __device__ __forceinline__ int sel_node_of(const int64_t* off, int G, int64_t q)
   return lo - 1;
 }
 
-/* Weighted selection without replacement (tx_infect_nb, model.py:1066-1147).
- * k_node_tx has left, per node with demand, its round-0 target count
- * (ksel), its selection record and its node-local chunk prefix.  Round 0
- * runs over all nodes at once: every CTA forms the target offsets in
- * shared memory, every target is located, then (grid barrier) claimed
- * (grid barrier), targets going round-robin over the CTAs.  The few
- * collisions left after round 0 are redrawn per node by one CTA in later
- * rounds, with CTA barriers only.  Round r of node n draws the (n, r, j)
- * uniforms of the oracle, so the CDF targets are the same whatever runs
- * them. */
-__global__ void __launch_bounds__(256) k_select(DevWorld W) {
+/* Weighted selection without replacement (tx_infect_nb, model.py:1066-1147),
+ * in three kernels.  k_node_tx has left, per node with demand, its round-0
+ * target count (ksel), its selection record and its node-local chunk
+ * prefix.  Round 0 runs over all nodes at once: k_sel_locate forms the
+ * target offsets in every CTA's shared memory and locates every target;
+ * k_sel_claim claims them, targets going round-robin over the CTAs.  The
+ * few collisions left after round 0 are redrawn per node by one CTA in
+ * later rounds (k_sel_rounds), with CTA barriers only.  Round r of node n
+ * draws the (n, r, j) uniforms of the oracle, so the CDF targets are the
+ * same whatever runs them. */
+__global__ void __launch_bounds__(256) k_sel_locate(DevWorld W) {
   const int R = W.n_reps, G = W.G;
   int any = 0;
   for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
@@ -2221,7 +2191,7 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
       for (int u = 0; u < 4; ++u) {
         if (g0 + u < G) {
           if (offs_in_smem) s_off[g0 + u] = run;
-          else W.tgt_off[g0 + u] = run;
+          if (!offs_in_smem || blockIdx.x == 0) W.tgt_off[g0 + u] = run; /* for the claims */
         }
         run += k[u];
       }
@@ -2229,7 +2199,7 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
     }
     if (threadIdx.x == 0) {
       if (offs_in_smem) s_off[G] = carry;
-      else W.tgt_off[G] = carry;
+      if (!offs_in_smem || blockIdx.x == 0) W.tgt_off[G] = carry;
       s_K = carry;
     }
     __syncthreads();
@@ -2273,23 +2243,50 @@ __global__ void __launch_bounds__(256) k_select(DevWorld W) {
       }
     }
   }
-  const int64_t q0 = (int64_t)threadIdx.x * gridDim.x + blockIdx.x;
-  if (!grid_sync(W)) return;
-  for (int64_t q = q0; q < K; q += gsz) {
+}
+
+/* Round 0 claims (after every target of round 0 has been located): the
+ * first target to reach an agent exposes it. */
+__global__ void __launch_bounds__(256) k_sel_claim(DevWorld W) {
+  const int R = W.n_reps, G = W.G;
+  int any = 0;
+  for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
+  if (!any) return;
+  const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
+  const SelInfo* info = reinterpret_cast<const SelInfo*>(W.sel_info);
+  __shared__ int64_t s_off[LPG_SEL_OFFS];
+  const bool offs_in_smem = G < LPG_SEL_OFFS;
+  if (offs_in_smem) {
+    for (int g = threadIdx.x; g <= G; g += blockDim.x) s_off[g] = __ldcg(&W.tgt_off[g]);
+    __syncthreads();
+  }
+  const int64_t* offs = offs_in_smem ? s_off : W.tgt_off;
+  const int64_t K = __ldcg(&W.tgt_off[G]);
+  if (K > W.hits_cap) return;
+  for (int64_t q = (int64_t)threadIdx.x * gridDim.x + blockIdx.x; q < K; q += gsz) {
     const uint32_t hit = W.hits[q];
     if (hit == LPG_NONE) continue;
     const int g = sel_node_of(offs, G, q);
     claim(W, hit, g, info[g]);
   }
-  if (!grid_sync(W)) return;
+}
 
-  /* ---- later rounds: one CTA per node that still needs agents ---- */
+/* Later rounds (after the round 0 claims): one CTA per node that still
+ * lacks agents, rounds of its remaining target count over its current
+ * weights until the node is served or has no susceptible weight left. */
+__global__ void __launch_bounds__(256) k_sel_rounds(DevWorld W) {
+  const int R = W.n_reps, G = W.G;
+  int any = 0;
+  for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
+  if (!any) return;
+  __shared__ int64_t s_off[LPG_SEL_OFFS];
+
   __shared__ int64_t s_k;
   __shared__ uint64_t s_T;
   __shared__ SelInfo s_N;
   __shared__ int32_t s_need[256];
   __shared__ int32_t s_nneed;
-  uint64_t* s_cp = reinterpret_cast<uint64_t*>(s_off); /* the offsets are no longer needed */
+  uint64_t* s_cp = reinterpret_cast<uint64_t*>(s_off);
   /* this CTA's nodes (g = blockIdx.x + j * grid) checked at once: which
    * still lack agents after round 0 */
   if (threadIdx.x == 0) s_nneed = 0;
