@@ -11,21 +11,26 @@
  * that depends on an exp() or a log() (Poisson counts, gamma variates,
  * probabilities of exposure).
  *
- * Methods (all textbook mathematics, coefficients derived from first
- * principles, not taken from any vendor library):
- *   exp    Cody–Waite reduction x = k ln2 + r with a two-part ln2
- *          (high part with 33 significant bits so k*hi is exact), then the
- *          Taylor series of e^r to degree 14 (|r| <= ln2/2, truncation error
- *          below 1e-18 relative), then exact scaling by 2^k.
- *   Every polynomial is evaluated by Estrin's scheme (short dependency
- *   chains: double-precision latency, not throughput, bounds the
- *   single-thread draws on the GPU).
- *   expm1  the same Taylor series without its constant term when
- *          |x| < ln2/2 (full relative precision for tiny rates), else exp-1.
- *   log    x = m 2^e with m in [sqrt(1/2), sqrt(2)), log m = 2 atanh(s),
- *          s = (m-1)/(m+1), |s| <= 0.1716, atanh series to s^25.
+ * Methods (all textbook mathematics, table values computed here from
+ * 60-digit decimal arithmetic by gen_detmath_tables.py, not taken from any
+ * vendor library): table-driven reductions (Tang's method) that leave a
+ * short polynomial, because double-precision latency, not throughput,
+ * bounds the single-thread draws on the GPU (a dependent add or multiply
+ * takes about 65 cycles on the GB300, a division about 430).
+ *   exp    x = (64 q + j) ln2/64 + r with a two-part ln2/64 (the high part
+ *          with 33 significant bits so k*hi is exact), |r| <= ln2/128;
+ *          e^x = 2^q * 2^(j/64) * (1 + (e^r - 1)), 2^(j/64) a double-double
+ *          from the table, e^r - 1 to degree 6, exact scaling by 2^q.
+ *   expm1  the degree-6 series for |x| <= ln2/128; to |x| = 1 the same
+ *          reduction with the exact (2^q 2^(j/64) - 1) first, so small
+ *          results keep their relative precision; beyond, exp - 1.
+ *   log    x = 2^e m, F = 1 + j/128 the table point nearest m (halved with
+ *          m for m >= 1.5), ln x = e ln2 + ln F + ln(1 + r), r = (m - F)/F
+ *          (m - F exact, |r| <= 1/192), ln F a double-double from the
+ *          table, ln(1 + r) to degree 8.
  *   lfact  log(k!) exactly from the double k! for k < 20, else Stirling's
  *          series for log Gamma(k+1) to the x^-7 term.
+ * Every polynomial is evaluated by Estrin's scheme.
  * Accuracy is a few ulp; the tests compare against numpy.
  */
 #ifndef LPG_DETMATH_H
@@ -82,114 +87,276 @@ LPG_HD double lpg_scale2(double p, int k) {
   return p * lpg_pow2i(k);
 }
 
-/* Polynomials by Estrin's scheme (pairs, then powers r^2, r^4, r^8): the
- * same polynomial as Horner's rule with a dependency depth of about 8
- * operations instead of 2 per coefficient, which matters on a GPU whose
- * double-precision operations have a long latency.  Coefficients are the
- * correctly rounded reciprocals of the exact double factorials.  The series
- * are arranged as r + r^2 P(r) so that the dominant term r is exact and the
- * rounding of P is scaled down by r. */
+/* Tables (gen_detmath_tables.py, correctly rounded from 60-digit decimal
+ * arithmetic): ln F_j as double-doubles and 1/F_j for the 129 log points,
+ * F_j = 1 + j/128 (j < 64) or (1 + j/128)/2 (j >= 64); 2^(j/64) as
+ * double-doubles for exp. */
+#define LPG_INIT_LOG_HI \
+  { \
+  0x0.0p+0, 0x1.fe02a6b106789p-8, 0x1.fc0a8b0fc03e4p-7, 0x1.7b91b07d5b11bp-6, \
+  0x1.f829b0e783300p-6, 0x1.39e87b9febd60p-5, 0x1.77458f632dcfcp-5, 0x1.b42dd711971bfp-5, \
+  0x1.f0a30c01162a6p-5, 0x1.16536eea37ae1p-4, 0x1.341d7961bd1d1p-4, 0x1.51b073f06183fp-4, \
+  0x1.6f0d28ae56b4cp-4, 0x1.8c345d6319b21p-4, 0x1.a926d3a4ad563p-4, 0x1.c5e548f5bc743p-4, \
+  0x1.e27076e2af2e6p-4, 0x1.fec9131dbeabbp-4, 0x1.0d77e7cd08e59p-3, 0x1.1b72ad52f67a0p-3, \
+  0x1.29552f81ff523p-3, 0x1.371fc201e8f74p-3, 0x1.44d2b6ccb7d1ep-3, 0x1.526e5e3a1b438p-3, \
+  0x1.5ff3070a793d4p-3, 0x1.6d60fe719d21dp-3, 0x1.7ab890210d909p-3, 0x1.87fa06520c911p-3, \
+  0x1.9525a9cf456b4p-3, 0x1.a23bc1fe2b563p-3, 0x1.af3c94e80bff3p-3, 0x1.bc286742d8cd6p-3, \
+  0x1.c8ff7c79a9a22p-3, 0x1.d5c216b4fbb91p-3, 0x1.e27076e2af2e6p-3, 0x1.ef0adcbdc5936p-3, \
+  0x1.fb9186d5e3e2bp-3, 0x1.0402594b4d041p-2, 0x1.0a324e27390e3p-2, 0x1.1058bf9ae4ad5p-2, \
+  0x1.1675cababa60ep-2, 0x1.1c898c16999fbp-2, 0x1.22941fbcf7966p-2, 0x1.2895a13de86a3p-2, \
+  0x1.2e8e2bae11d31p-2, 0x1.347dd9a987d55p-2, 0x1.3a64c556945eap-2, 0x1.404308686a7e4p-2, \
+  0x1.4618bc21c5ec2p-2, 0x1.4be5f957778a1p-2, 0x1.51aad872df82dp-2, 0x1.5767717455a6cp-2, \
+  0x1.5d1bdbf5809cap-2, 0x1.62c82f2b9c795p-2, 0x1.686c81e9b14afp-2, 0x1.6e08eaa2ba1e4p-2, \
+  0x1.739d7f6bbd007p-2, 0x1.792a55fdd47a2p-2, 0x1.7eaf83b82afc3p-2, 0x1.842d1da1e8b17p-2, \
+  0x1.89a3386c1425bp-2, 0x1.8f11e873662c7p-2, 0x1.947941c2116fbp-2, 0x1.99d958117e08bp-2, \
+  -0x1.269621134db92p-2, -0x1.214456d0eb8d4p-2, -0x1.1bf99635a6b95p-2, -0x1.16b5ccbacfb73p-2, \
+  -0x1.1178e8227e47cp-2, -0x1.0c42d676162e3p-2, -0x1.07138604d5862p-2, -0x1.01eae5626c691p-2, \
+  -0x1.f991c6cb3b379p-3, -0x1.ef5ade4dcffe6p-3, -0x1.e530effe71012p-3, -0x1.db13db0d48940p-3, \
+  -0x1.d1037f2655e7bp-3, -0x1.c6ffbc6f00f71p-3, -0x1.bd087383bd8adp-3, -0x1.b31d8575bce3dp-3, \
+  -0x1.a93ed3c8ad9e3p-3, -0x1.9f6c407089664p-3, -0x1.95a5adcf7017fp-3, -0x1.8beafeb38fe8cp-3, \
+  -0x1.823c16551a3c2p-3, -0x1.7898d85444c73p-3, -0x1.6f0128b756abcp-3, -0x1.6574ebe8c133ap-3, \
+  -0x1.5bf406b543db2p-3, -0x1.527e5e4a1b58dp-3, -0x1.4913d8333b561p-3, -0x1.3fb45a59928ccp-3, \
+  -0x1.365fcb0159016p-3, -0x1.2d1610c86813ap-3, -0x1.23d712a49c202p-3, -0x1.1aa2b7e23f72ap-3, \
+  -0x1.1178e8227e47cp-3, -0x1.08598b59e3a07p-3, -0x1.fe89139dbd566p-4, -0x1.ec739830a1120p-4, \
+  -0x1.da727638446a2p-4, -0x1.c885801bc4b23p-4, -0x1.b6ac88dad5b1cp-4, -0x1.a4e7640b1bc38p-4, \
+  -0x1.9335e5d594989p-4, -0x1.8197e2f40e3f0p-4, -0x1.700d30aeac0e1p-4, -0x1.5e95a4d9791cbp-4, \
+  -0x1.4d3115d207eacp-4, -0x1.3bdf5a7d1ee64p-4, -0x1.2aa04a44717a5p-4, -0x1.1973bd1465567p-4, \
+  -0x1.08598b59e3a07p-4, -0x1.eea31c006b87cp-5, -0x1.ccb73cdddb2ccp-5, -0x1.aaef2d0fb10fcp-5, \
+  -0x1.894aa149fb343p-5, -0x1.67c94f2d4bb58p-5, -0x1.466aed42de3eap-5, -0x1.252f32f8d183fp-5, \
+  -0x1.0415d89e74444p-5, -0x1.c63d2ec14aaf2p-6, -0x1.8492528c8cabfp-6, -0x1.432a925980cc1p-6, \
+  -0x1.0205658935847p-6, -0x1.82448a388a2aap-7, -0x1.010157588de71p-7, -0x1.0080559588b35p-8, \
+  0x0.0p+0 \
+  }
 
-/* P(r) = sum_{n=0}^{14} r^n / (n+2)! */
-LPG_HD double lpg_em1_tail16(double r, double r2, double r4, double r8) {
+#define LPG_INIT_LOG_LO \
+  { \
+  0x0.0p+0, -0x1.e44b7e3711ebfp-67, -0x1.83092c59642a1p-62, -0x1.5b602ace3a510p-60, \
+  0x1.33e3f04f1ef23p-60, -0x1.5bfa937f551bbp-59, 0x1.18d3ca87b9296p-59, -0x1.eb9759c130499p-60, \
+  0x1.85f325c5bbacdp-59, -0x1.79da3e8c22cdap-60, -0x1.b599f227becbbp-58, 0x1.a49e39a1a8be4p-58, \
+  -0x1.906d99184b992p-58, -0x1.4a697ab3424a9p-61, 0x1.942f48aa70ea9p-58, 0x1.5d617ef8161b1p-60, \
+  -0x1.61578001e0162p-60, -0x1.5746b9981b36cp-58, 0x1.9a5dc5e9030acp-57, 0x1.483023472cd74p-58, \
+  0x1.301771c407dbfp-57, 0x1.de6cb62af18a0p-58, 0x1.9f4f6543e1f88p-57, -0x1.746ff8a470d3ap-57, \
+  -0x1.bc60efafc6f6ep-58, -0x1.caae268ecd179p-57, 0x1.be36b2d6a0608p-59, -0x1.bf7fdbfa08d9ap-57, \
+  0x1.d904c1d4e2e26p-57, 0x1.93711b07a998cp-59, -0x1.398cff3641985p-58, 0x1.4fce744870f55p-58, \
+  -0x1.4f689f8434012p-57, 0x1.6e443597e4d40p-57, -0x1.61578001e0162p-59, 0x1.48637950dc20dp-57, \
+  -0x1.caaae64f21acbp-57, -0x1.28ec217a5022dp-57, 0x1.7dcfde8061c03p-56, 0x1.89fa0ab4cb31dp-58, \
+  0x1.ce63eab883717p-61, -0x1.0e5c62aff1c44p-60, -0x1.76f5eb09628afp-56, 0x1.7ad24c13f040ep-56, \
+  -0x1.8f4cdb95ebdf9p-56, -0x1.4dd4c580919f8p-57, -0x1.c68651945f97cp-57, -0x1.0bcfb6082ce6dp-56, \
+  0x1.f42decdeccf1dp-56, -0x1.259b35b04813dp-57, 0x1.3927ac19f55e3p-59, 0x1.526adb283660cp-56, \
+  0x1.4236383dc7fe1p-56, 0x1.7b7af915300e5p-57, -0x1.ddea0f7f58e3dp-57, -0x1.cfb1b39ca3a0fp-56, \
+  -0x1.8c76ceb014b04p-56, 0x1.f057691fe9ed7p-56, 0x1.92ce979ed2950p-56, 0x1.24ec519784676p-56, \
+  -0x1.29639dfbbf0fbp-56, 0x1.f85da755a61a3p-56, -0x1.16cc8bae0bbe4p-56, -0x1.a2b6889dc3e72p-57, \
+  -0x1.e0efadd9db02bp-56, -0x1.f7ae91aeba60ap-57, 0x1.12aeb84249223p-57, -0x1.66fbd28b40935p-56, \
+  0x1.0e63a5f01c691p-57, -0x1.162c79d5d11eep-58, -0x1.cdb16ed4e9138p-56, 0x1.18290bd2932e2p-59, \
+  -0x1.f665066f980a2p-57, 0x1.08ab2ddc708a0p-58, -0x1.2276041f43042p-59, -0x1.aa11d49f96cb9p-58, \
+  -0x1.60629242471a2p-57, 0x1.8e58b2c57a4a5p-57, -0x1.dd355f6a516d7p-60, 0x1.6353ab386a94dp-57, \
+  -0x1.bcafa9de97203p-57, -0x1.35a19605e67efp-59, -0x1.142c507fb7a3dp-58, -0x1.55aa8b6997a40p-58, \
+  0x1.1232ce70be781p-57, -0x1.ef8f6ebcfb201p-58, 0x1.8de59c21e166cp-57, 0x1.d34f0f4621bedp-60, \
+  0x1.1f5b44c0df7e7p-61, 0x1.71a9682395bfdp-61, 0x1.0d5604930f135p-58, 0x1.d87e6a354d056p-57, \
+  -0x1.7d411a5b944adp-58, 0x1.499a3f25af95fp-58, 0x1.6e38161051d69p-57, 0x1.c6ef1d9b2ef7ep-59, \
+  0x1.0e63a5f01c691p-58, 0x1.dd7009902bf32p-57, 0x1.ac9f4215f9393p-58, 0x1.a2bf991780d3fp-59, \
+  -0x1.401fa71733019p-58, -0x1.a38cb559a6706p-58, 0x1.0057eed1ca59fp-59, 0x1.5b5ca203e4259p-58, \
+  0x1.478a85704ccb7p-58, -0x1.b9f2dffbeed43p-60, 0x1.72566212cdd05p-61, -0x1.f38745c5c450ap-58, \
+  -0x1.769f42c7842ccp-58, -0x1.7a976d3b5b45fp-59, 0x1.d15d38d2fa3f7p-58, 0x1.7558367a6acf6p-59, \
+  0x1.dd7009902bf32p-58, 0x1.3e4fc93b7b66cp-59, 0x1.e48fb0500efd4p-59, -0x1.a353bb42e0addp-61, \
+  -0x1.a8be97660a23dp-60, -0x1.0413e6505e603p-59, 0x1.cdd6f7f4a137ep-59, 0x1.947f792615916p-59, \
+  -0x1.c05cf1d753622p-59, 0x1.ce030a686bd86p-60, 0x1.d192d0619fa67p-60, 0x1.8cdaf39004192p-60, \
+  -0x1.27c8e8416e71fp-60, -0x1.04b16137f09a0p-62, -0x1.46662d417ced0p-62, -0x1.f96638cf63677p-62, \
+  0x0.0p+0 \
+  }
+
+#define LPG_INIT_INV \
+  { \
+  0x1.0000000000000p+0, 0x1.fc07f01fc07f0p-1, 0x1.f81f81f81f820p-1, 0x1.f44659e4a4271p-1, \
+  0x1.f07c1f07c1f08p-1, 0x1.ecc07b301ecc0p-1, 0x1.e9131abf0b767p-1, 0x1.e573ac901e574p-1, \
+  0x1.e1e1e1e1e1e1ep-1, 0x1.de5d6e3f8868ap-1, 0x1.dae6076b981dbp-1, 0x1.d77b654b82c34p-1, \
+  0x1.d41d41d41d41dp-1, 0x1.d0cb58f6ec074p-1, 0x1.cd85689039b0bp-1, 0x1.ca4b3055ee191p-1, \
+  0x1.c71c71c71c71cp-1, 0x1.c3f8f01c3f8f0p-1, 0x1.c0e070381c0e0p-1, 0x1.bdd2b899406f7p-1, \
+  0x1.bacf914c1bad0p-1, 0x1.b7d6c3dda338bp-1, 0x1.b4e81b4e81b4fp-1, 0x1.b2036406c80d9p-1, \
+  0x1.af286bca1af28p-1, 0x1.ac5701ac5701bp-1, 0x1.a98ef606a63bep-1, 0x1.a6d01a6d01a6dp-1, \
+  0x1.a41a41a41a41ap-1, 0x1.a16d3f97a4b02p-1, 0x1.9ec8e951033d9p-1, 0x1.9c2d14ee4a102p-1, \
+  0x1.999999999999ap-1, 0x1.970e4f80cb872p-1, 0x1.948b0fcd6e9e0p-1, 0x1.920fb49d0e229p-1, \
+  0x1.8f9c18f9c18fap-1, 0x1.8d3018d3018d3p-1, 0x1.8acb90f6bf3aap-1, 0x1.886e5f0abb04ap-1, \
+  0x1.8618618618618p-1, 0x1.83c977ab2beddp-1, 0x1.8181818181818p-1, 0x1.7f405fd017f40p-1, \
+  0x1.7d05f417d05f4p-1, 0x1.7ad2208e0ecc3p-1, 0x1.78a4c8178a4c8p-1, 0x1.767dce434a9b1p-1, \
+  0x1.745d1745d1746p-1, 0x1.724287f46debcp-1, 0x1.702e05c0b8170p-1, 0x1.6e1f76b4337c7p-1, \
+  0x1.6c16c16c16c17p-1, 0x1.6a13cd1537290p-1, 0x1.6816816816817p-1, 0x1.661ec6a5122f9p-1, \
+  0x1.642c8590b2164p-1, 0x1.623fa77016240p-1, 0x1.6058160581606p-1, 0x1.5e75bb8d015e7p-1, \
+  0x1.5c9882b931057p-1, 0x1.5ac056b015ac0p-1, 0x1.58ed2308158edp-1, 0x1.571ed3c506b3ap-1, \
+  0x1.5555555555555p+0, 0x1.5390948f40febp+0, 0x1.51d07eae2f815p+0, 0x1.5015015015015p+0, \
+  0x1.4e5e0a72f0539p+0, 0x1.4cab88725af6ep+0, 0x1.4afd6a052bf5bp+0, 0x1.49539e3b2d067p+0, \
+  0x1.47ae147ae147bp+0, 0x1.460cbc7f5cf9ap+0, 0x1.446f86562d9fbp+0, 0x1.42d6625d51f87p+0, \
+  0x1.4141414141414p+0, 0x1.3fb013fb013fbp+0, 0x1.3e22cbce4a902p+0, 0x1.3c995a47babe7p+0, \
+  0x1.3b13b13b13b14p+0, 0x1.3991c2c187f63p+0, 0x1.3813813813814p+0, 0x1.3698df3de0748p+0, \
+  0x1.3521cfb2b78c1p+0, 0x1.33ae45b57bcb2p+0, 0x1.323e34a2b10bfp+0, 0x1.30d190130d190p+0, \
+  0x1.2f684bda12f68p+0, 0x1.2e025c04b8097p+0, 0x1.2c9fb4d812ca0p+0, 0x1.2b404ad012b40p+0, \
+  0x1.29e4129e4129ep+0, 0x1.288b01288b013p+0, 0x1.27350b8812735p+0, 0x1.25e22708092f1p+0, \
+  0x1.2492492492492p+0, 0x1.23456789abcdfp+0, 0x1.21fb78121fb78p+0, 0x1.20b470c67c0d9p+0, \
+  0x1.1f7047dc11f70p+0, 0x1.1e2ef3b3fb874p+0, 0x1.1cf06ada2811dp+0, 0x1.1bb4a4046ed29p+0, \
+  0x1.1a7b9611a7b96p+0, 0x1.19453808ca29cp+0, 0x1.1811811811812p+0, 0x1.16e0689427379p+0, \
+  0x1.15b1e5f75270dp+0, 0x1.1485f0e0acd3bp+0, 0x1.135c81135c811p+0, 0x1.12358e75d3033p+0, \
+  0x1.1111111111111p+0, 0x1.0fef010fef011p+0, 0x1.0ecf56be69c90p+0, 0x1.0db20a88f4696p+0, \
+  0x1.0c9714fbcda3bp+0, 0x1.0b7e6ec259dc8p+0, 0x1.0a6810a6810a7p+0, 0x1.0953f39010954p+0, \
+  0x1.0842108421084p+0, 0x1.073260a47f7c6p+0, 0x1.0624dd2f1a9fcp+0, 0x1.05197f7d73404p+0, \
+  0x1.0410410410410p+0, 0x1.03091b51f5e1ap+0, 0x1.0204081020408p+0, 0x1.0101010101010p+0, \
+  0x1.0000000000000p+0 \
+  }
+
+#define LPG_INIT_EXP_HI \
+  { \
+  0x1.0000000000000p+0, 0x1.02c9a3e778061p+0, 0x1.059b0d3158574p+0, 0x1.0874518759bc8p+0, \
+  0x1.0b5586cf9890fp+0, 0x1.0e3ec32d3d1a2p+0, 0x1.11301d0125b51p+0, 0x1.1429aaea92de0p+0, \
+  0x1.172b83c7d517bp+0, 0x1.1a35beb6fcb75p+0, 0x1.1d4873168b9aap+0, 0x1.2063b88628cd6p+0, \
+  0x1.2387a6e756238p+0, 0x1.26b4565e27cddp+0, 0x1.29e9df51fdee1p+0, 0x1.2d285a6e4030bp+0, \
+  0x1.306fe0a31b715p+0, 0x1.33c08b26416ffp+0, 0x1.371a7373aa9cbp+0, 0x1.3a7db34e59ff7p+0, \
+  0x1.3dea64c123422p+0, 0x1.4160a21f72e2ap+0, 0x1.44e086061892dp+0, 0x1.486a2b5c13cd0p+0, \
+  0x1.4bfdad5362a27p+0, 0x1.4f9b2769d2ca7p+0, 0x1.5342b569d4f82p+0, 0x1.56f4736b527dap+0, \
+  0x1.5ab07dd485429p+0, 0x1.5e76f15ad2148p+0, 0x1.6247eb03a5585p+0, 0x1.6623882552225p+0, \
+  0x1.6a09e667f3bcdp+0, 0x1.6dfb23c651a2fp+0, 0x1.71f75e8ec5f74p+0, 0x1.75feb564267c9p+0, \
+  0x1.7a11473eb0187p+0, 0x1.7e2f336cf4e62p+0, 0x1.82589994cce13p+0, 0x1.868d99b4492edp+0, \
+  0x1.8ace5422aa0dbp+0, 0x1.8f1ae99157736p+0, 0x1.93737b0cdc5e5p+0, 0x1.97d829fde4e50p+0, \
+  0x1.9c49182a3f090p+0, 0x1.a0c667b5de565p+0, 0x1.a5503b23e255dp+0, 0x1.a9e6b5579fdbfp+0, \
+  0x1.ae89f995ad3adp+0, 0x1.b33a2b84f15fbp+0, 0x1.b7f76f2fb5e47p+0, 0x1.bcc1e904bc1d2p+0, \
+  0x1.c199bdd85529cp+0, 0x1.c67f12e57d14bp+0, 0x1.cb720dcef9069p+0, 0x1.d072d4a07897cp+0, \
+  0x1.d5818dcfba487p+0, 0x1.da9e603db3285p+0, 0x1.dfc97337b9b5fp+0, 0x1.e502ee78b3ff6p+0, \
+  0x1.ea4afa2a490dap+0, 0x1.efa1bee615a27p+0, 0x1.f50765b6e4540p+0, 0x1.fa7c1819e90d8p+0 \
+  }
+
+#define LPG_INIT_EXP_LO \
+  { \
+  0x0.0p+0, -0x1.19083535b085dp-56, 0x1.d73e2a475b465p-55, 0x1.186be4bb284ffp-57, \
+  0x1.8a62e4adc610bp-54, 0x1.03a1727c57b53p-59, -0x1.6c51039449b3ap-54, -0x1.32fbf9af1369ep-54, \
+  -0x1.19041b9d78a76p-55, 0x1.e5b4c7b4968e4p-55, 0x1.e016e00a2643cp-54, 0x1.dc775814a8495p-55, \
+  0x1.9b07eb6c70573p-54, 0x1.2bd339940e9d9p-55, 0x1.612e8afad1255p-55, 0x1.0024754db41d5p-54, \
+  0x1.6f46ad23182e4p-55, 0x1.32721843659a6p-54, -0x1.63aeabf42eae2p-54, -0x1.5e436d661f5e3p-56, \
+  0x1.ada0911f09ebcp-55, -0x1.ef3691c309278p-58, 0x1.89b7a04ef80d0p-59, 0x1.3c1a3b69062f0p-56, \
+  0x1.d4397afec42e2p-56, -0x1.4b309d25957e3p-54, -0x1.07abe1db13cadp-55, 0x1.9bb2c011d93adp-54, \
+  0x1.6324c054647adp-54, 0x1.ba6f93080e65ep-54, -0x1.383c17e40b497p-54, -0x1.bb60987591c34p-54, \
+  -0x1.bdd3413b26456p-54, -0x1.bbe3a683c88abp-57, -0x1.16e4786887a99p-55, -0x1.0245957316dd3p-54, \
+  -0x1.41577ee04992fp-55, 0x1.05d02ba15797ep-56, -0x1.d4c1dd41532d8p-54, -0x1.fc6f89bd4f6bap-54, \
+  0x1.6e9f156864b27p-54, 0x1.5cc13a2e3976cp-55, -0x1.75fc781b57ebcp-57, -0x1.d185b7c1b85d1p-54, \
+  0x1.c7c46b071f2bep-56, -0x1.359495d1cd533p-54, -0x1.d2f6edb8d41e1p-54, 0x1.0fac90ef7fd31p-54, \
+  0x1.7a1cd345dcc81p-54, -0x1.2805e3084d708p-57, -0x1.5584f7e54ac3bp-56, 0x1.23dd07a2d9e84p-55, \
+  0x1.11065895048ddp-55, 0x1.2884dff483cadp-54, 0x1.503cbd1e949dbp-56, -0x1.cbc3743797a9cp-54, \
+  0x1.2ed02d75b3707p-55, 0x1.c2300696db532p-54, -0x1.1a5cd4f184b5cp-54, 0x1.39e8980a9cc8fp-55, \
+  -0x1.e9c23179c2893p-54, 0x1.dc7f486a4b6b0p-54, 0x1.9d3e12dd8a18bp-54, 0x1.74853f3a5931ep-55 \
+  }
+
+#if defined(__CUDACC__)
+__constant__ double lpg_tab_log_hi_dev[129] = LPG_INIT_LOG_HI;
+__constant__ double lpg_tab_log_lo_dev[129] = LPG_INIT_LOG_LO;
+__constant__ double lpg_tab_inv_dev[129] = LPG_INIT_INV;
+__constant__ double lpg_tab_exp_hi_dev[64] = LPG_INIT_EXP_HI;
+__constant__ double lpg_tab_exp_lo_dev[64] = LPG_INIT_EXP_LO;
+#endif
+static const double lpg_tab_log_hi_host[129] = LPG_INIT_LOG_HI;
+static const double lpg_tab_log_lo_host[129] = LPG_INIT_LOG_LO;
+static const double lpg_tab_inv_host[129] = LPG_INIT_INV;
+static const double lpg_tab_exp_hi_host[64] = LPG_INIT_EXP_HI;
+static const double lpg_tab_exp_lo_host[64] = LPG_INIT_EXP_LO;
+#if defined(__CUDA_ARCH__)
+#define LPG_TAB(name) lpg_tab_##name##_dev
+#else
+#define LPG_TAB(name) lpg_tab_##name##_host
+#endif
+
+/* Polynomials by Estrin's scheme (pairs, then powers r^2, r^4): the same
+ * polynomial as Horner's rule with a shorter dependency chain, which
+ * matters on a GPU whose double-precision operations have a long latency.
+ * The series are arranged as r + r^2 P(r) so that the dominant term r is
+ * exact and the rounding of P is scaled down by r. */
+
+/* e^r - 1 = r + r^2 (1/2 + r/6 + r^2/24 + r^3/120 + r^4/720) for
+ * |r| <= ln2/128 (the omitted r^7/5040 is below 2^-60 of the result). */
+LPG_HD double lpg_em1_small(double r) {
+  const double r2 = r * r;
   const double q0 = 0.5 + (1.0 / 6.0) * r;
   const double q1 = (1.0 / 24.0) + (1.0 / 120.0) * r;
-  const double q2 = (1.0 / 720.0) + (1.0 / 5040.0) * r;
-  const double q3 = (1.0 / 40320.0) + (1.0 / 362880.0) * r;
-  const double q4 = (1.0 / 3628800.0) + (1.0 / 39916800.0) * r;
-  const double q5 = (1.0 / 479001600.0) + (1.0 / 6227020800.0) * r;
-  const double q6 = (1.0 / 87178291200.0) + (1.0 / 1307674368000.0) * r;
-  const double q7 = 1.0 / 20922789888000.0;
   const double s0 = q0 + q1 * r2;
-  const double s1 = q2 + q3 * r2;
-  const double s2 = q4 + q5 * r2;
-  const double s3 = q6 + q7 * r2;
-  const double t0 = s0 + s1 * r4;
-  const double t1 = s2 + s3 * r4;
-  return t0 + t1 * r8;
+  const double p = s0 + (1.0 / 720.0) * (r2 * r2);
+  return r + r2 * p;
 }
 
-/* P(r) = sum_{n=0}^{12} r^n / (n+2)! */
-LPG_HD double lpg_em1_tail14(double r, double r2, double r4, double r8) {
-  const double q0 = 0.5 + (1.0 / 6.0) * r;
-  const double q1 = (1.0 / 24.0) + (1.0 / 120.0) * r;
-  const double q2 = (1.0 / 720.0) + (1.0 / 5040.0) * r;
-  const double q3 = (1.0 / 40320.0) + (1.0 / 362880.0) * r;
-  const double q4 = (1.0 / 3628800.0) + (1.0 / 39916800.0) * r;
-  const double q5 = (1.0 / 479001600.0) + (1.0 / 6227020800.0) * r;
-  const double q6 = 1.0 / 87178291200.0;
-  const double s0 = q0 + q1 * r2;
-  const double s1 = q2 + q3 * r2;
-  const double s2 = q4 + q5 * r2;
-  const double t0 = s0 + s1 * r4;
-  const double t1 = s2 + q6 * r4;
-  return t0 + t1 * r8;
+/* kd = round(x * 64 / ln2) split as kd = 64 q + j (0 <= j < 64), and the
+ * reduced argument r = x - kd ln2/64 with a two-part ln2/64 (kd * hi exact
+ * for |kd| < 2^20); |r| <= ln2/128 up to rounding. */
+LPG_HD double lpg_exp_reduce(double x, int* q, int* j) {
+  const double kd = floor(x * (64.0 * LPG_INV_LN2) + 0.5);
+  const double r = (x - kd * (LPG_LN2_HI * 0x1.0p-6)) - kd * (LPG_LN2_LO * 0x1.0p-6);
+  const int k = (int)kd;
+  *j = k & 63;
+  *q = (k - *j) / 64;
+  return r;
 }
 
-/* sum_{n=0}^{14} r^n / n! = 1 + (r + r^2 P(r)). */
-LPG_HD double lpg_exp_series(double r) {
-  const double r2 = r * r;
-  const double r4 = r2 * r2;
-  const double r8 = r4 * r4;
-  return 1.0 + (r + r2 * lpg_em1_tail14(r, r2, r4, r8));
-}
-
-/* sum_{n=1}^{16} r^n / n! = r + r^2 P(r) — e^r - 1 without its constant. */
-LPG_HD double lpg_expm1_series(double r) {
-  const double r2 = r * r;
-  const double r4 = r2 * r2;
-  const double r8 = r4 * r4;
-  return r + r2 * lpg_em1_tail16(r, r2, r4, r8);
-}
-
+/* e^x = 2^q 2^(j/64) e^r: table value times (1 + (e^r - 1)). */
 LPG_HD double lpg_exp(double x) {
   if (x != x) return x;
   if (x > 709.782712893384) return lpg_bitsd(0x7ff0000000000000ULL);
   if (x < -745.2) return 0.0;
-  double kd = floor(x * LPG_INV_LN2 + 0.5);
-  double r = (x - kd * LPG_LN2_HI) - kd * LPG_LN2_LO;
-  return lpg_scale2(lpg_exp_series(r), (int)kd);
+  int q, j;
+  const double r = lpg_exp_reduce(x, &q, &j);
+  const double p = lpg_em1_small(r);
+  const double th = LPG_TAB(exp_hi)[j], tl = LPG_TAB(exp_lo)[j];
+  return lpg_scale2(th + (tl + th * p), q);
 }
 
+/* e^x - 1: the short series for |x| <= ln2/128; up to |x| = 1 the reduced
+ * form (2^q T - 1) + 2^q (T_lo + T p), whose first term is exact
+ * (Sterbenz), so small results keep their relative precision; beyond, e^x - 1. */
 LPG_HD double lpg_expm1(double x) {
   if (x != x) return x;
-  if (x > -0.3465 && x < 0.3465) return lpg_expm1_series(x);
+  if (x > -0x1.62e42fefa39efp-8 && x < 0x1.62e42fefa39efp-8) return lpg_em1_small(x);
   if (x < -40.0) return -1.0;
-  return lpg_exp(x) - 1.0;
+  if (x > 1.0 || x < -1.0) return lpg_exp(x) - 1.0;
+  int q, j;
+  const double r = lpg_exp_reduce(x, &q, &j);
+  const double p = lpg_em1_small(r);
+  const double s = lpg_pow2i(q);
+  const double th = LPG_TAB(exp_hi)[j] * s, tl = LPG_TAB(exp_lo)[j] * s;
+  return (th - 1.0) + (tl + th * p);
 }
 
+/* ln(1 + r) - r = r^2 (-1/2 + r/3 - r^2/4 + r^3/5 - r^4/6 + r^5/7 - r^6/8)
+ * for |r| <= 1/192 (the omitted r^9/9 is below 2^-60 of r). */
+LPG_HD double lpg_l1p_tail(double r) {
+  const double r2 = r * r;
+  const double r4 = r2 * r2;
+  const double q0 = -0.5 + (1.0 / 3.0) * r;
+  const double q1 = -0.25 + 0.2 * r;
+  const double q2 = (-1.0 / 6.0) + (1.0 / 7.0) * r;
+  const double s0 = q0 + q1 * r2;
+  const double s1 = q2 + (-0.125) * r2;
+  return r2 * (s0 + s1 * r4);
+}
+
+/* ln x = e ln2 + ln F_j + ln(1 + r), x = 2^e m, F_j = 1 + j/128 the table
+ * point nearest m (for the upper half m and F_j halved and e raised, so
+ * that a result near 0 never comes from cancelling e ln2 against ln F_j,
+ * and x just below 1 meets F = 1 exactly), r = (m - F_j)/F_j with m - F_j
+ * exact and |r| <= 1/192. */
 LPG_HD double lpg_log(double x) {
   if (x != x) return x;
   if (x <= 0.0) return x == 0.0 ? -lpg_bitsd(0x7ff0000000000000ULL) : lpg_bitsd(0x7ff8000000000000ULL);
   if (x == lpg_bitsd(0x7ff0000000000000ULL)) return x;
   int eadj = 0;
   if (x < 0x1.0p-1022) { x = x * 0x1.0p54; eadj = -54; }
-  uint64_t b = lpg_dbits(x);
+  const uint64_t b = lpg_dbits(x);
   int e = (int)((b >> 52) & 0x7ff) - 1023 + eadj;
-  double m = lpg_bitsd((b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL); /* [1,2) */
-  if (m > LPG_SQRT2) { m = m * 0.5; e += 1; }
-  double s = (m - 1.0) / (m + 1.0);
-  /* log m = 2s + 2s z Q(z), z = s^2, Q = sum_{n=0}^{11} z^n / (2n+3) by
-   * Estrin's scheme; the leading 2s is exact */
-  const double z = s * s;
-  const double z2 = z * z;
-  const double z4 = z2 * z2;
-  const double z8 = z4 * z4;
-  const double p0 = (1.0 / 3.0) + (1.0 / 5.0) * z;
-  const double p1 = (1.0 / 7.0) + (1.0 / 9.0) * z;
-  const double p2 = (1.0 / 11.0) + (1.0 / 13.0) * z;
-  const double p3 = (1.0 / 15.0) + (1.0 / 17.0) * z;
-  const double p4 = (1.0 / 19.0) + (1.0 / 21.0) * z;
-  const double p5 = (1.0 / 23.0) + (1.0 / 25.0) * z;
-  const double u0 = p0 + p1 * z2;
-  const double u1 = p2 + p3 * z2;
-  const double u2 = p4 + p5 * z2;
-  const double v0 = u0 + u1 * z4;
-  const double q = v0 + u2 * z8;
-  const double s2x = 2.0 * s;
-  double lm = s2x + (s2x * z) * q;
-  double ed = (double)e;
-  return ed * LPG_LN2_HI + (ed * LPG_LN2_LO + lm);
+  const uint64_t mant = b & 0x000fffffffffffffULL;
+  const int j = (int)((mant + (1ULL << 44)) >> 45); /* 0 .. 128 */
+  double m = lpg_bitsd(mant | 0x3ff0000000000000ULL); /* [1,2) */
+  double f = 1.0 + (double)j * 0.0078125;
+  if (j >= 64) {
+    m = m * 0.5;
+    f = f * 0.5;
+    e += 1;
+  }
+  const double r = (m - f) * LPG_TAB(inv)[j];
+  const double ed = (double)e;
+  const double hi = ed * LPG_LN2_HI + LPG_TAB(log_hi)[j];
+  const double lo = (ed * LPG_LN2_LO + LPG_TAB(log_lo)[j]) + (r + lpg_l1p_tail(r));
+  return hi + lo;
 }
 
 /* log(k!) for integer k >= 0. */

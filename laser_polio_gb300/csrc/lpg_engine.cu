@@ -606,6 +606,7 @@ extern "C" int lpg_start(lpg_handle* h) {
     rp.km_len = d.km_len;
     rp.km_max_year = d.km_max_year;
     rp.nb_r = d.nb_r;
+    if (d.nb_r >= 1) lpg_gamma_consts((double)d.nb_r, &rp.nb_d, &rp.nb_c);
     rp.count0 = d.count;
     rp.capacity = d.capacity;
     rp.seed = d.seed;

@@ -95,6 +95,7 @@ typedef struct {
   int32_t n_nodes, ns, nt, comps;
   int32_t stop_if, vd_step, ri_step, ri_enabled;
   int32_t ri_strain, km_len, km_max_year, nb_r;
+  double nb_d, nb_c; /* Marsaglia–Tsang's constants of nb_r (lpg_gamma_consts) when nb_r >= 1 */
   int32_t node_base;  /* first global node id */
   int32_t chunk_base; /* first chunk id */
   int32_t chunk_cap;  /* chunks reserved */

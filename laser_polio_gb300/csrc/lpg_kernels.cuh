@@ -1756,19 +1756,19 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
   }
   const uint64_t* qrow = rp->netq_t + (int64_t)i * n; /* qrow[ii] = network[ii][i] in 2^-62 */
   unsigned __int128 part[LPG_MAX_STRAINS] = {0, 0, 0, 0};
-  /* batches of 4 source nodes per thread, every load of a batch issued
-   * before any multiply */
-  for (int ii0 = threadIdx.x; ii0 < n; ii0 += 4 * blockDim.x) {
-    uint64_t w[4], b[4][LPG_MAX_STRAINS];
+  /* batches of 8 source nodes per thread, every load of a batch issued
+   * before any multiply (two batches for up to 1024 nodes) */
+  for (int ii0 = threadIdx.x; ii0 < n; ii0 += 8 * blockDim.x) {
+    uint64_t w[8], b[8][LPG_MAX_STRAINS];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 8; ++u) {
       const int ii = ii0 + u * blockDim.x;
       w[u] = ii < n ? qrow[ii] : 0;
 #pragma unroll
       for (int k = 0; k < LPG_MAX_STRAINS; ++k) b[u][k] = (ii < n && k < ns) ? W.bb[(int64_t)k * G + nb + ii] : 0;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 8; ++u)
 #pragma unroll
       for (int k = 0; k < LPG_MAX_STRAINS; ++k)
         if (k < ns) part[k] += (unsigned __int128)b[u][k] * w[u];
@@ -1800,6 +1800,11 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
     return;
   }
   if (wid != 0) return;
+  /* the first two blocks of lane 0's exposure-count stream, formed while
+   * the double-precision work below waits on its latencies */
+  lpg_stream sm;
+  lpg_stream_init(&sm, rp->seed, LPG_P_TXCOUNT, t, (uint64_t)i, 0);
+  lpg_stream_ahead(&sm);
   /* Strain k on lane k (a double-precision warp instruction costs the same
    * for one lane or 32): incoming infectivity, beta, rate, probability
    * (model.py:1327-1363); then the sums over strains in strain order, as
@@ -1848,8 +1853,6 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
   const double srisk = (double)pre_sw * 0x1.0p-24;
   const double exposure = srisk * total_p;
   int64_t total = 0;
-  lpg_stream sm;
-  lpg_stream_init(&sm, rp->seed, LPG_P_TXCOUNT, t, (uint64_t)i, 0);
   if (!(exposure > 0.0)) {
     total = 0;
   } else if (local_zero) {
@@ -1860,7 +1863,7 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
       double r = (double)rp->nb_r;
       double pp = r / (r + mean);
       double u = lpg_next(&sm);
-      total = (u < rp->zi) ? 0 : lpg_negbinom(&sm, r, pp);
+      total = (u < rp->zi) ? 0 : rp->nb_r >= 1 ? lpg_negbinom_dc(&sm, rp->nb_d, rp->nb_c, pp) : lpg_negbinom(&sm, r, pp);
     }
   } else {
     total = lpg_poisson(&sm, exposure);

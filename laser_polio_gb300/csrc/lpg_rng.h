@@ -125,6 +125,8 @@ typedef struct {
   uint64_t k;
   uint64_t blk[4];
   uint64_t blk_id;
+  uint64_t nxt[4]; /* a block generated ahead (lpg_stream_ahead) */
+  uint64_t nxt_id;
 } lpg_stream;
 
 LPG_HD void lpg_stream_init(lpg_stream* s, uint64_t seed, uint32_t purpose, int32_t tick, uint64_t a, uint64_t b) {
@@ -135,16 +137,35 @@ LPG_HD void lpg_stream_init(lpg_stream* s, uint64_t seed, uint32_t purpose, int3
   s->b = b;
   s->k = 0;
   s->blk_id = ~(uint64_t)0;
+  s->nxt_id = ~(uint64_t)0;
+}
+
+LPG_HD void lpg_stream_block(const lpg_stream* s, uint64_t id, uint64_t* out) {
+  out[0] = s->a;
+  out[1] = s->b;
+  out[2] = ((uint64_t)s->purpose << 32) | (uint64_t)(uint32_t)s->tick;
+  out[3] = id;
+  lpg_philox4x64_10(out, s->seed, LPG_KEY_TAG);
+}
+
+/* Blocks 0 and 1 of the stream formed now, before any draw needs them (the
+ * draws are the same; on the GPU the integer work then overlaps the
+ * double-precision chain that precedes the first draw). */
+LPG_HD void lpg_stream_ahead(lpg_stream* s) {
+  lpg_stream_block(s, 0, s->blk);
+  s->blk_id = 0;
+  lpg_stream_block(s, 1, s->nxt);
+  s->nxt_id = 1;
 }
 
 LPG_HD double lpg_next(lpg_stream* s) {
   uint64_t id = s->k >> 2;
   if (id != s->blk_id) {
-    s->blk[0] = s->a;
-    s->blk[1] = s->b;
-    s->blk[2] = ((uint64_t)s->purpose << 32) | (uint64_t)(uint32_t)s->tick;
-    s->blk[3] = id;
-    lpg_philox4x64_10(s->blk, s->seed, LPG_KEY_TAG);
+    if (id == s->nxt_id) {
+      for (int j = 0; j < 4; ++j) s->blk[j] = s->nxt[j];
+    } else {
+      lpg_stream_block(s, id, s->blk);
+    }
     s->blk_id = id;
   }
   uint64_t w = s->blk[s->k & 3];
@@ -166,17 +187,14 @@ LPG_HD double lpg_std_normal(lpg_stream* s) {
   return 0.0;
 }
 
-/* Gamma(shape a, scale 1). */
-LPG_HD double lpg_std_gamma(lpg_stream* s, double a) {
-  if (!(a > 0.0)) return 0.0;
-  double boost = 1.0;
-  if (a < 1.0) {
-    double u = lpg_next(s);
-    boost = lpg_exp(lpg_log(u) / a);
-    a = a + 1.0;
-  }
-  double d = a - 1.0 / 3.0;
-  double c = 1.0 / sqrt(9.0 * d);
+/* Marsaglia–Tsang's constants for shape a >= 1: d = a - 1/3, c = 1/sqrt(9d). */
+LPG_HD void lpg_gamma_consts(double a, double* d, double* c) {
+  *d = a - 1.0 / 3.0;
+  *c = 1.0 / sqrt(9.0 * *d);
+}
+
+/* Marsaglia–Tsang's rejection loop with its constants, times boost. */
+LPG_HD double lpg_gamma_mt(lpg_stream* s, double d, double c, double boost) {
   for (int it = 0; it < LPG_MAX_REJECT; ++it) {
     double x = lpg_std_normal(s);
     double v = 1.0 + c * x;
@@ -188,6 +206,20 @@ LPG_HD double lpg_std_gamma(lpg_stream* s, double a) {
     if (lpg_log(u) < 0.5 * x2 + d * (1.0 - v + lpg_log(v))) return d * v * boost;
   }
   return d * boost;
+}
+
+/* Gamma(shape a, scale 1). */
+LPG_HD double lpg_std_gamma(lpg_stream* s, double a) {
+  if (!(a > 0.0)) return 0.0;
+  double boost = 1.0;
+  if (a < 1.0) {
+    double u = lpg_next(s);
+    boost = lpg_exp(lpg_log(u) / a);
+    a = a + 1.0;
+  }
+  double d, c;
+  lpg_gamma_consts(a, &d, &c);
+  return lpg_gamma_mt(s, d, c, boost);
 }
 
 /* 1/x for 1 <= x <= 64, correctly rounded (constant expressions), so that
@@ -226,7 +258,8 @@ LPG_HD int64_t lpg_poisson(lpg_stream* s, double lam) {
     return x;
   }
   double slam = sqrt(lam);
-  double loglam = lpg_log(lam);
+  double loglam = 0.0, logia = 0.0; /* formed on the first squeeze failure */
+  int have_logs = 0;
   double b = 0.931 + 2.53 * slam;
   double a = -0.059 + 0.02483 * b;
   double invalpha = 1.1239 + 1.1328 / (b - 3.4);
@@ -238,7 +271,12 @@ LPG_HD int64_t lpg_poisson(lpg_stream* s, double lam) {
     double kd = floor((2.0 * a / us + b) * u + lam + 0.43);
     if (us >= 0.07 && v <= vr) return (int64_t)kd;
     if (kd < 0.0 || (us < 0.013 && v > us)) continue;
-    double lhs = lpg_log(v) + lpg_log(invalpha) - lpg_log(a / (us * us) + b);
+    if (!have_logs) {
+      loglam = lpg_log(lam);
+      logia = lpg_log(invalpha);
+      have_logs = 1;
+    }
+    double lhs = lpg_log(v) + logia - lpg_log(a / (us * us) + b);
     double rhs = -lam + kd * loglam - lpg_lfact((int64_t)kd);
     if (lhs <= rhs) return (int64_t)kd;
   }
@@ -249,6 +287,13 @@ LPG_HD int64_t lpg_poisson(lpg_stream* s, double lam) {
  * probability p), as the gamma–Poisson mixture. */
 LPG_HD int64_t lpg_negbinom(lpg_stream* s, double r, double p) {
   double y = lpg_std_gamma(s, r) * ((1.0 - p) / p);
+  return lpg_poisson(s, y);
+}
+
+/* The same for r >= 1 with Marsaglia–Tsang's constants of r formed once
+ * (lpg_gamma_consts): equal draws, two fewer dependent operations. */
+LPG_HD int64_t lpg_negbinom_dc(lpg_stream* s, double d, double c, double p) {
+  double y = lpg_gamma_mt(s, d, c, 1.0) * ((1.0 - p) / p);
   return lpg_poisson(s, y);
 }
 
