@@ -345,13 +345,12 @@ LPG_HD double lpg_log(double x) {
   int e = (int)((b >> 52) & 0x7ff) - 1023 + eadj;
   const uint64_t mant = b & 0x000fffffffffffffULL;
   const int j = (int)((mant + (1ULL << 44)) >> 45); /* 0 .. 128 */
-  double m = lpg_bitsd(mant | 0x3ff0000000000000ULL); /* [1,2) */
-  double f = 1.0 + (double)j * 0.0078125;
-  if (j >= 64) {
-    m = m * 0.5;
-    f = f * 0.5;
-    e += 1;
-  }
+  /* m in [1, 2) and F = 1 + j/128 from their bits, both halved (exponent
+   * field 0x3fe) for j >= 64; F = 2/2 = 1 for j = 128 */
+  const uint64_t ex = j >= 64 ? 0x3fe0000000000000ULL : 0x3ff0000000000000ULL;
+  e += j >= 64 ? 1 : 0;
+  const double m = lpg_bitsd(mant | ex);
+  const double f = lpg_bitsd(ex + ((uint64_t)j << 45));
   const double r = (m - f) * LPG_TAB(inv)[j];
   const double ed = (double)e;
   const double hi = ed * LPG_LN2_HI + LPG_TAB(log_hi)[j];
