@@ -22,11 +22,13 @@
 
 namespace {
 
-/* Kernels a tick needs only on some ticks; the host knows the schedule, so
- * a tick without them does not launch them. */
+/* Kernels a tick needs only on some ticks (births: k_begin, k_newborns;
+ * seeds; RI/SIA); the host knows the schedule, so a tick without them does
+ * not launch them. */
 enum { NEED_NB = 1, NEED_SEED = 2, NEED_RS = 4 };
 static bool kernel_needed(int k, uint8_t need) {
   switch (k) {
+    case 0:
     case 1: return (need & NEED_NB) != 0;
     case 4: return (need & NEED_SEED) != 0;
     case 5:
@@ -569,6 +571,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   W.hits_cap = hits;
   rc |= dalloc(h, &W.hits, hits);
   rc |= dalloc(h, &W.ctr, LPG_NUM_COUNTERS);
+  rc |= dalloc(h, &W.end_done, 1);
   rc |= dalloc(h, &W.reps, R);
   if (rc) return LPG_ERR_NOMEM;
   CK(cudaMemsetAsync(W.ds, 0xff, P, st));
@@ -583,6 +586,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaMemsetAsync(W.size, 0, sizeof(int64_t) * G, st));
   CK(cudaMemsetAsync(W.uniq, 0, sizeof(int64_t) * G, st));
   CK(cudaMemsetAsync(W.ctr, 0, sizeof(unsigned long long) * LPG_NUM_COUNTERS, st));
+  CK(cudaMemsetAsync(W.end_done, 0, 4, st));
 
   /* 4. per-simulation static data, results, pools, chunk tables */
   std::vector<int4> h_meta(chunk_total, make_int4(-1, 0, -1, 0));

@@ -152,7 +152,7 @@ typedef struct {
   int32_t any_demand;
   int32_t csr_flip;    /* the node -> chunk lists were rebuilt this tick (k_newborns fills them) */
   int32_t used_before; /* used_chunks before this tick's new chunks */
-  int32_t pad2;
+  int32_t ei_sum;      /* k_end: nodes with E > 0 plus nodes with I > 0 (the next tick's stop rule) */
 } DevRep;
 
 /* Global device state shared by the kernels of one handle. */
@@ -209,6 +209,7 @@ typedef struct {
   uint64_t* due;     /* sub-blocks with something due this tick: sub-block | sim << 32 | what << 48 */
   uint32_t* due_n;   /* entries of due (k_due appends, k_end clears) */
   unsigned long long* ctr; /* [LPG_NUM_COUNTERS] work counters */
+  uint32_t* end_done;      /* CTAs of k_end done with the tick (the last prepares the next) */
 } DevWorld;
 
 #endif

@@ -150,58 +150,42 @@ __device__ int64_t block_excl_scan(int64_t v, int64_t* total) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* The flags of the replicate's next tick (rp->t): which components run and
+ * the tick's schedule entries (model.py:246-282 with each component's own
+ * step condition), and the per-tick bookkeeping reset.  k_end's last CTA
+ * calls it for every replicate, so a tick starts prepared. */
+__device__ void rep_prepare(DevRep* rp) {
+  /* every field read before the first store (the stores could alias) */
+  const int t = rp->t;
+  const int started = rp->started, error = rp->error, stopped = rp->stopped, nt = rp->nt;
+  const uint32_t comps = rp->comps;
+  const int vd_step = rp->vd_step, ri_step = rp->ri_step, ri_enabled = rp->ri_enabled;
+  const int64_t count = rp->count;
+  const int active = started && !error && !stopped && t >= 1 && t < nt;
+  const int tt = active ? t : 0;
+  const int sia_cnt = rp->sia_cnt[tt], sia_first = rp->sia_first[tt];
+  const int seed_cnt = rp->seed_cnt[tt], seed_first = rp->seed_first[tt];
+  rp->cur_t = t;
+  rp->active = active;
+  rp->vd_tick = active && (comps & LPG_COMP_VD) && (t % vd_step == 0);
+  rp->ri_tick = active && (comps & LPG_COMP_RI) && ri_enabled && (t % ri_step == 0);
+  rp->sia_n = (active && (comps & LPG_COMP_SIA)) ? sia_cnt : 0;
+  rp->sia_i0 = active ? sia_first : 0;
+  rp->seed_n = (active && (comps & LPG_COMP_DS)) ? seed_cnt : 0;
+  rp->seed_i0 = active ? seed_first : 0;
+  rp->nb_total = 0;
+  rp->count_before = count;
+  rp->any_demand = 0;
+  rp->csr_flip = 0;
+}
+
+/* VD ticks: births per node and their chunk placement (the tick's flags,
+ * the stop rule and the cleared event counters come from the previous
+ * tick's k_end). */
 __global__ void k_begin(DevWorld W) {
   DevRep* rp = &W.reps[blockIdx.x];
-  __shared__ int s_active, s_vd, s_t;
-  __shared__ unsigned long long s_sum;
-  if (threadIdx.x == 0) {
-    /* every field read before the first store (the stores could alias) */
-    const int t = rp->t;
-    const int started = rp->started, error = rp->error, stopped = rp->stopped, nt = rp->nt;
-    const uint32_t comps = rp->comps;
-    const int vd_step = rp->vd_step, ri_step = rp->ri_step, ri_enabled = rp->ri_enabled;
-    const int64_t count = rp->count;
-    const int active = started && !error && !stopped && t >= 1 && t < nt;
-    const int tt = active ? t : 0;
-    const int sia_cnt = rp->sia_cnt[tt], sia_first = rp->sia_first[tt];
-    const int seed_cnt = rp->seed_cnt[tt], seed_first = rp->seed_first[tt];
-    const int vd = active && (comps & LPG_COMP_VD) && (t % vd_step == 0);
-    rp->cur_t = t;
-    rp->active = active;
-    rp->vd_tick = vd;
-    rp->ri_tick = active && (comps & LPG_COMP_RI) && ri_enabled && (t % ri_step == 0);
-    rp->sia_n = (active && (comps & LPG_COMP_SIA)) ? sia_cnt : 0;
-    rp->sia_i0 = active ? sia_first : 0;
-    rp->seed_n = (active && (comps & LPG_COMP_DS)) ? seed_cnt : 0;
-    rp->seed_i0 = active ? seed_first : 0;
-    rp->nb_total = 0;
-    rp->count_before = count;
-    rp->any_demand = 0;
-    rp->csr_flip = 0;
-    s_active = active;
-    s_vd = vd;
-    s_t = t;
-    s_sum = 0;
-  }
-  __syncthreads();
-  if (!s_active) return;
-  const int n = rp->n_nodes, nb = rp->node_base, t = s_t, G = W.G;
-  for (int k = 0; k < EV_N; ++k)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) W.ev[(int64_t)k * G + nb + i] = 0;
-
-  /* stop rule: evaluated on the E/I results of t-1 (model.py:788-795) */
-  if ((rp->comps & LPG_COMP_DS) && rp->stop_if) {
-    unsigned long long local = 0;
-    if (rp->comps & LPG_COMP_TX) {
-      const int32_t* E = RES(rp, RS_E, t - 1);
-      const int32_t* I = RES(rp, RS_I, t - 1);
-      for (int i = threadIdx.x; i < n; i += blockDim.x) local += (unsigned long long)(E[i] > 0) + (I[i] > 0);
-    }
-    if (local) atomicAdd(&s_sum, local);
-    __syncthreads();
-    if (threadIdx.x == 0 && s_sum == 0 && !rp->future_seed[t]) rp->stop_at = t;
-  }
-  if (!s_vd) return;
+  if (!rp->active || !rp->vd_tick) return;
+  const int n = rp->n_nodes, nb = rp->node_base, t = rp->cur_t, G = W.G;
 
   /* births per node: integer part + Bernoulli on the fraction (model.py:1711-1716) */
   const int32_t* pop1 = RES(rp, RS_POP, t - 1);
@@ -2393,10 +2377,43 @@ __global__ void __launch_bounds__(256) k_sel_rounds(DevWorld W) {
 
 /* ------------------------------------------------------------------------ */
 /* Results rows of the tick and the tick advance. */
+/* The tick's node rows (one thread per node), then the next tick's setup by
+ * the last CTA: the stop rule (model.py:788-795: no node with E or I at this
+ * tick and no seed after the next), the flags of every replicate
+ * (rep_prepare), the due list emptied. */
+__device__ void k_end_node(DevWorld& W, int g, int* ei_out);
 __global__ void k_end(DevWorld W) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) *W.due_n = 0; /* the due list of the tick is spent */
+  __shared__ int s_last;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= W.G) return;
+  int ei = 0;
+  if (g < W.G) k_end_node(W, g, &ei);
+  /* stop rule input: nodes with E > 0 plus nodes with I > 0, per replicate */
+  if (g < W.G && ei) atomicAdd(&W.reps[W.node_rep[g]].ei_sum, ei);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(W.end_done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int r = threadIdx.x; r < W.n_reps; r += blockDim.x) {
+    DevRep* rp = &W.reps[r];
+    const int ran = rp->active, sum = rp->ei_sum;
+    rp->ei_sum = 0;
+    const int tn = rp->t;
+    if (ran && (rp->comps & LPG_COMP_DS) && rp->stop_if && !rp->stopped && !rp->error && tn < rp->nt && sum == 0 &&
+        !rp->future_seed[tn])
+      rp->stop_at = tn;
+    rep_prepare(rp);
+  }
+  if (threadIdx.x == 0) {
+    *W.due_n = 0; /* the due list of the tick is spent */
+    *W.end_done = 0;
+  }
+}
+
+__device__ void k_end_node(DevWorld& W, int g, int* ei_out) {
   DevRep* rp = &W.reps[W.node_rep[g]];
   /* every field of the replicate record this thread needs, read before the
    * first store (stores through int32_t* could otherwise alias them and
@@ -2435,6 +2452,7 @@ __global__ void k_end(DevWorld W) {
     ROW(RS_S)[i] = tt[TT_S];
     ROW(RS_E)[i] = e;
     ROW(RS_I)[i] = in;
+    *ei_out = (e > 0 ? 1 : 0) + (in > 0 ? 1 : 0);
     ROW(RS_R)[i] += tt[TT_R];
     ROW(RS_POTP)[i] = tt[TT_POTP];
     ROW(RS_P)[i] = tt[TT_P];
@@ -2492,6 +2510,9 @@ __global__ void k_end(DevWorld W) {
   }
 #undef ROW
 #undef ROWS
+  /* the tick's event counters are spent: cleared for the next */
+#pragma unroll
+  for (int k = 0; k < EV_N; ++k) W.ev[(int64_t)k * G + g] = 0;
   if (i == 0) {
     rp->t = t + 1;
     if (stop_at == t) rp->stopped = 1;
