@@ -39,8 +39,8 @@ static bool kernel_needed(int k, uint8_t need) {
 
 const char* kKernelNames[] = {"k_begin", "k_newborns", "k_due", "k_sweep_a", "k_seed",
                               "k_sweep_b", "k_evb", "k_node_tx", "k_sel_locate", "k_sel_claim",
-                              "k_sel_rounds", "k_end"};
-constexpr int kNumTickKernels = 12;
+                              "k_sel_rounds"};
+constexpr int kNumTickKernels = 11; /* k_sel_rounds ends the tick (results rows, next tick's setup) */
 constexpr int kTicksPerGraph = 8;
 
 /* Reference-ordered columns of one simulation on the device. */
@@ -895,7 +895,6 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 8: k_sel_locate<<<h->select_blocks, 256, 0, st>>>(W); break;
     case 9: k_sel_claim<<<h->claim_blocks, 256, 0, st>>>(W); break;
     case 10: k_sel_rounds<<<h->select_blocks, 256, 0, st>>>(W); break;
-    case 11: k_end<<<(G + 255) / 256, 256, 0, st>>>(W); break;
   }
   CK(cudaGetLastError());
   if (timed) CK(cudaEventRecord(e1, st));

@@ -1,13 +1,12 @@
 /*
  * lpg_kernels.cuh — device kernels of the per-tick agent step.
  *
- * One tick is this fixed launch sequence (every kernel reads the tick and
- * its flags from device memory, so the sequence is captured once in a CUDA
- * graph and replayed):
- *   k_begin      per simulation: stop rule (model.py:788-795), per-tick
- *                counters, births per node (model.py:1711-1716) and their
- *                chunk placement
- *   k_newborns   newborn rows (model.py:1719-1730)
+ * One tick is this launch sequence (every kernel reads the tick and its
+ * flags from device memory, so blocks of ticks are captured in CUDA graphs
+ * and replayed; the kernels only some ticks need are launched only then):
+ *   k_begin      birth ticks, per simulation: births per node
+ *                (model.py:1711-1716) and their chunk placement
+ *   k_newborns   birth ticks: newborn rows (model.py:1719-1730)
  *   k_due        the sub-blocks with a disease-state event or a death due,
  *                from the per-sub-block indexes
  *   k_sweep_due  those sub-blocks, evenly over the CTAs: deaths (get_deaths,
@@ -23,9 +22,10 @@
  *                seasonality, probabilities and exposure counts
  *                (model.py:1327-1407)
  *   k_sel_locate, k_sel_claim, k_sel_rounds   weighted selection rounds
- *                and strain assignment (tx_infect_nb, model.py:1010-1149)
- *   k_end        results rows of the tick (model.py:1461-1487 and the
- *                result writes of every component)
+ *                and strain assignment (tx_infect_nb, model.py:1010-1149);
+ *                k_sel_rounds then ends the tick (end_tick): results rows
+ *                (model.py:1461-1487 and the result writes of every
+ *                component), the next tick's flags and stop rule
  */
 #ifndef LPG_KERNELS_CUH
 #define LPG_KERNELS_CUH
@@ -2260,12 +2260,24 @@ __global__ void __launch_bounds__(256) k_sel_claim(DevWorld W) {
 
 /* Later rounds (after the round 0 claims): one CTA per node that still
  * lacks agents, rounds of its remaining target count over its current
- * weights until the node is served or has no susceptible weight left. */
+ * weights until the node is served or has no susceptible weight left; then
+ * the end of the tick (end_tick) for the CTA's nodes.  All threads of the
+ * CTA run sel_rounds. */
+__device__ __noinline__ void sel_rounds(DevWorld& W);
+__device__ void end_tick(DevWorld& W, int64_t g0, int64_t gstride);
 __global__ void __launch_bounds__(256) k_sel_rounds(DevWorld W) {
-  const int R = W.n_reps, G = W.G;
+  const int R = W.n_reps;
   int any = 0;
   for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
-  if (!any) return;
+  if (any) sel_rounds(W);
+  /* every node of this CTA is served: the tick's rows of its nodes, and the
+   * next tick's setup by the last CTA (end_tick) */
+  __syncthreads();
+  end_tick(W, blockIdx.x + (int64_t)threadIdx.x * gridDim.x, (int64_t)blockDim.x * gridDim.x);
+}
+
+__device__ __noinline__ void sel_rounds(DevWorld& W) {
+  const int G = W.G;
   __shared__ int64_t s_off[LPG_SEL_OFFS];
 
   __shared__ int64_t s_k;
@@ -2377,18 +2389,21 @@ __global__ void __launch_bounds__(256) k_sel_rounds(DevWorld W) {
 
 /* ------------------------------------------------------------------------ */
 /* Results rows of the tick and the tick advance. */
-/* The tick's node rows (one thread per node), then the next tick's setup by
- * the last CTA: the stop rule (model.py:788-795: no node with E or I at this
- * tick and no seed after the next), the flags of every replicate
- * (rep_prepare), the due list emptied. */
+/* The tick's node rows (k_end_node), then the next tick's setup by the last
+ * CTA: the stop rule (model.py:788-795: no node with E or I at this tick and
+ * no seed after the next), the flags of every replicate (rep_prepare), the
+ * due list emptied. */
 __device__ void k_end_node(DevWorld& W, int g, int* ei_out);
-__global__ void k_end(DevWorld W) {
+/* The end of a tick for nodes g0, g0 + gstride, ... of this thread; all
+ * threads of every CTA of the launch call it. */
+__device__ void end_tick(DevWorld& W, int64_t g0, int64_t gstride) {
   __shared__ int s_last;
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  int ei = 0;
-  if (g < W.G) k_end_node(W, g, &ei);
-  /* stop rule input: nodes with E > 0 plus nodes with I > 0, per replicate */
-  if (g < W.G && ei) atomicAdd(&W.reps[W.node_rep[g]].ei_sum, ei);
+  for (int64_t g = g0; g < W.G; g += gstride) {
+    int ei = 0;
+    k_end_node(W, (int)g, &ei);
+    /* stop rule input: nodes with E > 0 plus nodes with I > 0, per replicate */
+    if (ei) atomicAdd(&W.reps[W.node_rep[g]].ei_sum, ei);
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -2411,6 +2426,11 @@ __global__ void k_end(DevWorld W) {
     *W.due_n = 0; /* the due list of the tick is spent */
     *W.end_done = 0;
   }
+}
+
+/* The end of tick 0 (lpg_start); later ticks end in k_sel_rounds. */
+__global__ void k_end(DevWorld W) {
+  end_tick(W, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 __device__ void k_end_node(DevWorld& W, int g, int* ei_out) {
