@@ -700,16 +700,11 @@ __device__ __forceinline__ void sweep_b16(uint64_t* slab, uint32_t* s_cnt, DevWo
   }
 }
 
-/* Of one thread's 16 slots (state bytes v, event ticks from evt at pos0):
+/* Of one thread's 16 slots (state bytes v, event ticks eq):
  * the agents in E or I whose event is at t or before (bit mask), and the
  * earliest later event among the others (LPG_NO_DOD if none).  `dead`
  * slots are left out of both. */
-__device__ __forceinline__ uint32_t ev_due16(const DevWorld& W, int64_t pos0, uint4 v, uint32_t dead, int t,
-                                            int32_t& nmin) {
-  const int4* e4 = reinterpret_cast<const int4*>(W.evt + pos0);
-  int4 eq[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) eq[q] = __ldcg(e4 + q);
+__device__ __forceinline__ uint32_t ev_due16(const int4* eq, uint4 v, uint32_t dead, int t, int32_t& nmin) {
   const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
   uint32_t due = 0;
 #pragma unroll
@@ -1266,6 +1261,10 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_due(DevWorld W) {
     }
     const int64_t pos0 = sb * LPG_SUB + (int64_t)(lane & 7) * 16;
     const uint4 v = on ? ldg_stream16(W.ds + pos0) : make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    /* the event ticks requested with the state bytes, before the deaths */
+    int4 eq[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) eq[q] = edue ? __ldcg(reinterpret_cast<const int4*>(W.evt + pos0) + q) : make_int4(0, 0, 0, 0);
     uint32_t dead = 0;
     if (__ballot_sync(FULLMASK, ddue)) {
       int32_t nmin = LPG_NO_DOD;
@@ -1305,7 +1304,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_due(DevWorld W) {
     uint32_t ei = 0;
     if (__ballot_sync(FULLMASK, edue)) {
       int32_t nmin = LPG_NO_DOD;
-      if (edue) ei = ev_due16(W, pos0, v, dead, t, nmin);
+      if (edue) ei = ev_due16(eq, v, dead, t, nmin);
       nmin = sub8_min(nmin);
       /* the agents due now get their next event in ds_queue_step (atomicMin) */
       if (edue && (lane & 7) == 0) W.sub_evt[sb] = nmin;
@@ -2333,34 +2332,28 @@ __device__ __noinline__ void sel_rounds(DevWorld& W) {
       const int64_t k = s_k;
       const uint64_t T = s_T;
       if (k == 0) break;
-      /* chunk prefix of the node (CTA scan; every weight requested at once),
-       * in shared memory when it fits */
-      uint64_t wv[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int32_t idx = u * blockDim.x + threadIdx.x;
-        wv[u] = idx < n ? __ldcg(&W.chunk_w[ls[idx]]) : 0;
-      }
+      /* chunk prefix of the node (8 consecutive chunks a thread, every weight
+       * requested at once, one CTA scan per 8 * blockDim chunks), in shared
+       * memory when it fits */
       uint64_t carry = 0;
+      for (int32_t a0 = 0; a0 < n; a0 += 8 * blockDim.x) {
+        const int32_t i0 = a0 + 8 * threadIdx.x;
+        uint64_t wv[8], sum = 0;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        if (u * (int)blockDim.x >= n) break;
-        const int32_t idx = u * blockDim.x + threadIdx.x;
-        const int64_t v = (int64_t)wv[u];
-        int64_t tot;
-        const int64_t ex = block_excl_scan(v, &tot);
-        if (idx < n) {
-          if (local) s_cp[idx] = carry + (uint64_t)ex + (uint64_t)v;
-          else cp[idx] = carry + (uint64_t)ex + (uint64_t)v;
+        for (int u = 0; u < 8; ++u) {
+          wv[u] = i0 + u < n ? __ldcg(&W.chunk_w[ls[i0 + u]]) : 0;
+          sum += wv[u];
         }
-        carry += (uint64_t)tot;
-      }
-      for (int32_t a0 = 8 * blockDim.x; a0 < n; a0 += blockDim.x) {
-        const int32_t idx = a0 + threadIdx.x;
-        const int64_t v = idx < n ? (int64_t)__ldcg(&W.chunk_w[ls[idx]]) : 0;
         int64_t tot;
-        const int64_t ex = block_excl_scan(v, &tot);
-        if (idx < n) cp[idx] = carry + (uint64_t)ex + (uint64_t)v;
+        uint64_t run = carry + (uint64_t)block_excl_scan((int64_t)sum, &tot);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          run += wv[u];
+          if (i0 + u < n) {
+            if (local) s_cp[i0 + u] = run;
+            else cp[i0 + u] = run;
+          }
+        }
         carry += (uint64_t)tot;
       }
       __syncthreads();
