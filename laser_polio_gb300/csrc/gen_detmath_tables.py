@@ -4,6 +4,7 @@ arithmetic (Python's decimal module), printed as C hex-float initialisers.
   log: for j = 0..128, F_j = 1 + j/128 (j < 64) or (1 + j/128) / 2 (j >= 64);
        LOG_HI[j] + LOG_LO[j] = ln F_j (a double-double), INV[j] = 1 / F_j.
   exp: for j = 0..63, EXP_HI[j] + EXP_LO[j] = 2^(j/64).
+  lfact: for k = 0..255, LFACT[k] = ln k! (Poisson inversion from the mode).
 
 python gen_detmath_tables.py > /dev/stdout   (paste into lpg_detmath.h)
 """
@@ -40,7 +41,13 @@ def main():
         h, l = dd((ln2 * Decimal(j) / Decimal(64)).exp())
         exp_hi.append(h)
         exp_lo.append(l)
-    for name, vals in (("LOG_HI", log_hi), ("LOG_LO", log_lo), ("INV", inv), ("EXP_HI", exp_hi), ("EXP_LO", exp_lo)):
+    lfact, acc = [], Decimal(0)
+    for k in range(256):
+        if k >= 2:
+            acc += Decimal(k).ln()
+        lfact.append(float(acc))
+    for name, vals in (("LOG_HI", log_hi), ("LOG_LO", log_lo), ("INV", inv), ("EXP_HI", exp_hi), ("EXP_LO", exp_lo),
+                       ("LFACT", lfact)):
         print(table(f"LPG_TAB_{name}[{len(vals)}]", vals))
 
 

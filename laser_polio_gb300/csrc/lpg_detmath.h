@@ -90,7 +90,7 @@ LPG_HD double lpg_scale2(double p, int k) {
 /* Tables (gen_detmath_tables.py, correctly rounded from 60-digit decimal
  * arithmetic): ln F_j as double-doubles and 1/F_j for the 129 log points,
  * F_j = 1 + j/128 (j < 64) or (1 + j/128)/2 (j >= 64); 2^(j/64) as
- * double-doubles for exp. */
+ * double-doubles for exp; ln k! for k < 256. */
 #define LPG_INIT_LOG_HI \
   { \
   0x0.0p+0, 0x1.fe02a6b106789p-8, 0x1.fc0a8b0fc03e4p-7, 0x1.7b91b07d5b11bp-6, \
@@ -242,13 +242,83 @@ LPG_HD double lpg_scale2(double p, int k) {
   -0x1.e9c23179c2893p-54, 0x1.dc7f486a4b6b0p-54, 0x1.9d3e12dd8a18bp-54, 0x1.74853f3a5931ep-55 \
   }
 
+#define LPG_INIT_LFACT \
+  { \
+  0x0.0p+0, 0x0.0p+0, 0x1.62e42fefa39efp-1, 0x1.cab0bfa2a2002p+0, \
+  0x1.96ca77c922cf9p+1, 0x1.326643c4479c9p+2, 0x1.a51273acf01cap+2, 0x1.10ce1f32dcc30p+3, \
+  0x1.5358e82fcb70dp+3, 0x1.99a8921a7f7cfp+3, 0x1.e357590954d15p+3, 0x1.180973f3a8d74p+4, \
+  0x1.3fcba16d50143p+4, 0x1.68d5a9c3b32cep+4, 0x1.930f3df162a42p+4, 0x1.be636a63fd346p+4, \
+  0x1.eabff061f1a84p+4, 0x1.0c0a63f2f353ap+5, 0x1.2329df2d5ee52p+5, 0x1.3ab8153363985p+5, \
+  0x1.52af57aed77bep+5, 0x1.6b0a8643472a9p+5, 0x1.83c4faba84f06p+5, 0x1.9cda78b856a45p+5, \
+  0x1.b6472034e8d14p+5, 0x1.d007622cd65e7p+5, 0x1.ea17f717c6794p+5, 0x1.023aeb67e4fefp+6, \
+  0x1.0f8f18d330240p+6, 0x1.1d07353917231p+6, 0x1.2aa208b59d0e5p+6, 0x1.385e6fd9e5a40p+6, \
+  0x1.463b59b942084p+6, 0x1.5437c633ace4ap+6, 0x1.6252c474896bap+6, 0x1.708b719e11658p+6, \
+  0x1.7ee0f79b26758p+6, 0x1.8d528c1243d96p+6, 0x1.9bdf6f75257a3p+6, 0x1.aa86ec2969812p+6, \
+  0x1.b94855c702ba2p+6, 0x1.c8230869ca105p+6, 0x1.d7166813e12eep+6, 0x1.e621e01eeba4fp+6, \
+  0x1.f544e2ba69cf1p+6, 0x1.023f743addd9fp+7, 0x1.09e7b7ea41ea9p+7, 0x1.119afe762626bp+7, \
+  0x1.19590c853a559p+7, 0x1.2121a930c6ec3p+7, 0x1.28f49ddeb1f31p+7, 0x1.30d1b61e86335p+7, \
+  0x1.38b8bf8931ddbp+7, 0x1.40a989a33a6cdp+7, 0x1.48a3e5c12af19p+7, 0x1.50a7a6ee08711p+7, \
+  0x1.58b4a1d39da73p+7, 0x1.60caaca474746p+7, 0x1.68e99f0757979p+7, 0x1.711152043b2c4p+7, \
+  0x1.79419ff26dc59p+7, 0x1.817a6467f6fb9p+7, 0x1.89bb7c2a0aea1p+7, 0x1.9204c51e7c761p+7, \
+  0x1.9a561e3e1a4bdp+7, 0x1.a2af6787e4609p+7, 0x1.ab1081f509726p+7, 0x1.b3794f6d9d7afp+7, \
+  0x1.bbe9b2bdfb621p+7, 0x1.c4618f8cc56f7p+7, 0x1.cce0ca5179100p+7, 0x1.d567484b8b7b6p+7, \
+  0x1.ddf4ef7a05a70p+7, 0x1.e689a69396befp+7, 0x1.ef2554ff15148p+7, 0x1.f7c7e2cc66183p+7, \
+  0x1.00389c56e3462p+8, 0x1.04909ff8b652bp+8, 0x1.08ebf13dbf263p+8, 0x1.0d4a85602b129p+8, \
+  0x1.11ac51df8932ap+8, 0x1.16114c7e34736p+8, 0x1.1a796b3ede1acp+8, 0x1.1ee4a46236d3ep+8, \
+  0x1.2352ee64b46d5p+8, 0x1.27c43ffc72962p+8, 0x1.2c3890172d057p+8, 0x1.30afd5d851956p+8, \
+  0x1.352a089728f1bp+8, 0x1.39a71fdd14947p+8, 0x1.3e271363e0df7p+8, 0x1.42a9db142a36ap+8, \
+  0x1.472f6f03d410cp+8, 0x1.4bb7c77491066p+8, 0x1.5042dcd27af64p+8, 0x1.54d0a7b2ba658p+8, \
+  0x1.596120d23c4ecp+8, 0x1.5df4411475a1cp+8, 0x1.628a018233bedp+8, 0x1.67225b4879462p+8, \
+  0x1.6bbd47b7669b6p+8, 0x1.705ac0412d89fp+8, 0x1.74fabe790f7bep+8, 0x1.799d3c1265c0ep+8, \
+  0x1.7e4232dfb367dp+8, 0x1.82e99cd1c0368p+8, 0x1.879373f6bc4fep+8, 0x1.8c3fb2796c21cp+8, \
+  0x1.90ee52a05c35fp+8, 0x1.959f4ecd1c8b3p+8, 0x1.9a52a17b831ccp+8, 0x1.9f084540f545ep+8, \
+  0x1.a3c034cbb7b2cp+8, 0x1.a87a6ae24493ap+8, 0x1.ad36e262a7cc0p+8, 0x1.b1f59641e0db5p+8, \
+  0x1.b6b6818b4a3ebp+8, 0x1.bb799f600610ap+8, 0x1.c03eeaf66facdp+8, 0x1.c5065f9992226p+8, \
+  0x1.c9cff8a8a340dp+8, 0x1.ce9bb196830eap+8, 0x1.d36985e93f7b8p+8, 0x1.d83971399c213p+8, \
+  0x1.dd0b6f329dea4p+8, 0x1.e1df7b911a74cp+8, 0x1.e6b592234b0c9p+8, 0x1.eb8daec863182p+8, \
+  0x1.f067cd7029d4dp+8, 0x1.f543ea1a97428p+8, 0x1.fa2200d7741ebp+8, 0x1.ff020dc5fcd0cp+8, \
+  0x1.01f2068a4395cp+9, 0x1.0463fd801573cp+9, 0x1.06d6e9ea365edp+9, 0x1.094ac9f576038p+9, \
+  0x1.0bbf9bd589663p+9, 0x1.0e355dc4e4164p+9, 0x1.10ac0e0492828p+9, 0x1.1323aadc1563ep+9, \
+  0x1.159c32993e34fp+9, 0x1.1815a3900cac1p+9, 0x1.1a8ffc1a8d2fep+9, 0x1.1d0b3a98b83c1p+9, \
+  0x1.1f875d7052afep+9, 0x1.2204630ccefc3p+9, 0x1.248249df2f2b1p+9, 0x1.2701105de7b8dp+9, \
+  0x1.2980b504c3372p+9, 0x1.2c013654c6b40p+9, 0x1.2e8292d416dddp+9, 0x1.3104c90dddddep+9, \
+  0x1.3387d79231e3dp+9, 0x1.360bbcf5fc5bfp+9, 0x1.389077d2e1cb2p+9, 0x1.3b1606c72a4a4p+9, \
+  0x1.3d9c6875aa9cfp+9, 0x1.40239b85adddfp+9, 0x1.42ab9ea2dfbd1p+9, 0x1.4534707d3748fp+9, \
+  0x1.47be0fc8e241ep+9, 0x1.4a487b3e30effp+9, 0x1.4cd3b19982794p+9, 0x1.4f5fb19b31b3fp+9, \
+  0x1.51ec7a0782708p+9, 0x1.547a09a68f387p+9, 0x1.57085f44377dfp+9, 0x1.599779b00e38ep+9, \
+  0x1.5c2757bd48ee8p+9, 0x1.5eb7f842af200p+9, 0x1.61495a1a8a1d5p+9, 0x1.63db7c229538bp+9, \
+  0x1.666e5d3bee594p+9, 0x1.6901fc4b06e89p+9, 0x1.6b96583795197p+9, 0x1.6e2b6fec85852p+9, \
+  0x1.70c14257ed1c3p+9, 0x1.7357ce6afb697p+9, 0x1.75ef1319ed23cp+9, 0x1.78870f5bff0cdp+9, \
+  0x1.7b1fc22b611b3p+9, 0x1.7db92a8529ed1p+9, 0x1.805347694a819p+9, 0x1.82ee17da82373p+9, \
+  0x1.85899ade530d2p+9, 0x1.8825cf7cf6261p+9, 0x1.8ac2b4c15089cp+9, 0x1.8d6049b8e8253p+9, \
+  0x1.8ffe8d73d9061p+9, 0x1.929d7f04cad12p+9, 0x1.953d1d80e671bp+9, 0x1.97dd67ffcbffcp+9, \
+  0x1.9a7e5d9b88dd4p+9, 0x1.9d1ffd708e071p+9, 0x1.9fc2469da6998p+9, 0x1.a2653843ee86cp+9, \
+  0x1.a508d186c97e3p+9, 0x1.a7ad118bda02bp+9, 0x1.aa51f77af8af4p+9, 0x1.acf7827e2ba8fp+9, \
+  0x1.af9db1c19e3c7p+9, 0x1.b244847398a6bp+9, 0x1.b4ebf9c47806ep+9, 0x1.b79410e6a6799p+9, \
+  0x1.ba3cc90e935b7p+9, 0x1.bce62172abb2ap+9, 0x1.bf90194b52be1p+9, 0x1.c23aafd2daa98p+9, \
+  0x1.c4e5e4457d65ep+9, 0x1.c791b5e155a48p+9, 0x1.ca3e23e657f4cp+9, 0x1.cceb2d964c030p+9, \
+  0x1.cf98d234c5f8ap+9, 0x1.d24711071ffb9p+9, 0x1.d4f5e95473cd6p+9, 0x1.d7a55a6594889p+9, \
+  0x1.da556385087b9p+9, 0x1.dd0603ff03211p+9, 0x1.dfb73b215f34ap+9, 0x1.e269083b98e2bp+9, \
+  0x1.e51b6a9ec8146p+9, 0x1.e7ce619d9ad52p+9, 0x1.ea81ec8c4fd29p+9, 0x1.ed360ac0b0f5ep+9, \
+  0x1.efeabb920e153p+9, 0x1.f29ffe5937be4p+9, 0x1.f555d2707a179p+9, 0x1.f80c373397d9cp+9, \
+  0x1.fac32bffc55eep+9, 0x1.fd7ab033a3c7fp+9, 0x1.001961979e1c4p+10, 0x1.0175b229fd937p+10, \
+  0x1.02d2498255e0cp+10, 0x1.042f2752b9b42p+10, 0x1.058c4b4de69d1p+10, 0x1.06e9b52742dadp+10, \
+  0x1.08476492db365p+10, 0x1.09a5594560e57p+10, 0x1.0b0392f427775p+10, 0x1.0c62115522c95p+10, \
+  0x1.0dc0d41ee5056p+10, 0x1.0f1fdb089ca83p+10, 0x1.107f25ca12901p+10, 0x1.11deb41ba8145p+10, \
+  0x1.133e85b655240p+10, 0x1.149e9a53a66d0p+10, 0x1.15fef1adbb8aep+10, 0x1.175f8b7f453cep+10, \
+  0x1.18c0678383a39p+10, 0x1.1a2185764485fp+10, 0x1.1b82e513e19d0p+10, 0x1.1ce486193ee72p+10, \
+  0x1.1e466843c9018p+10, 0x1.1fa88b517388ep+10, 0x1.210aef00b7803p+10, 0x1.226d931091be7p+10 \
+  }
+
 #if defined(__CUDACC__)
+__constant__ double lpg_tab_lfact_dev[256] = LPG_INIT_LFACT;
 __constant__ double lpg_tab_log_hi_dev[129] = LPG_INIT_LOG_HI;
 __constant__ double lpg_tab_log_lo_dev[129] = LPG_INIT_LOG_LO;
 __constant__ double lpg_tab_inv_dev[129] = LPG_INIT_INV;
 __constant__ double lpg_tab_exp_hi_dev[64] = LPG_INIT_EXP_HI;
 __constant__ double lpg_tab_exp_lo_dev[64] = LPG_INIT_EXP_LO;
 #endif
+static const double lpg_tab_lfact_host[256] = LPG_INIT_LFACT;
 static const double lpg_tab_log_hi_host[129] = LPG_INIT_LOG_HI;
 static const double lpg_tab_log_lo_host[129] = LPG_INIT_LOG_LO;
 static const double lpg_tab_inv_host[129] = LPG_INIT_INV;

@@ -1696,10 +1696,18 @@ __device__ __forceinline__ void warp_chunk_prefix(const DevWorld& W, const int32
  * integer arithmetic: B in units of 2^-32 times the network weight in units
  * of 2^-62 (transposed row, contiguous), 128-bit sums, one conversion; an
  * exact sum does not depend on how the threads split it. */
+/* Lane k < ns of the second warp: this node's incoming-infectivity total of
+ * strain k (the first warp's pre_bb). */
+__device__ __forceinline__ uint64_t pre_bb_w1(const DevWorld& W, int g, int lane, int ns) {
+  return lane < ns ? W.bb[(int64_t)lane * W.G + g] : 0;
+}
+
 __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
   const int g = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __shared__ uint64_t s_lo[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS], s_hi[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS];
+  __shared__ double s_gam;   /* the negative binomial's gamma variate, formed ahead by the second warp */
+  __shared__ uint64_t s_gamk; /* the exposure stream's position after it */
   if (g >= W.G) return;
   DevRep* rp = &W.reps[W.node_rep[g]];
   if (threadIdx.x == 0) W.ksel[g] = 0;
@@ -1774,8 +1782,24 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
   }
   __syncthreads();
   if (wid == 1) {
-    /* the second warp: the node's chunk prefix for the selection that
-     * follows (node-local, exact in integers), while lane 0 of the first
+    /* the second warp: when the node has no local infectivity (the
+     * zero-inflated negative binomial, model.py:1383-1395), its gamma
+     * variate first: it uses the exposure stream from its second draw and
+     * not the tick's force of infection, so it is formed while the first
+     * warp works out the probabilities (a warp's double-precision operations
+     * do not overlap, another warp's do) */
+    const bool lz = __ballot_sync(FULLMASK, lane < ns && pre_bb_w1(W, g, lane, ns) != 0) == 0;
+    if (lane == 0 && lz && rp->zi < 1.0 && rp->nb_r >= 1) {
+      lpg_stream sg;
+      lpg_stream_init(&sg, rp->seed, LPG_P_TXCOUNT, t, (uint64_t)i, 0);
+      sg.k = 1; /* draw 0 is the zero-inflation test */
+      s_gam = lpg_gamma_mt(&sg, rp->nb_d, rp->nb_c, 1.0);
+      s_gamk = sg.k;
+    }
+    __syncwarp();
+    asm volatile("bar.sync 1, 64;" ::: "memory");
+    /* then the node's chunk prefix for the selection that follows
+     * (node-local, exact in integers), while lane 0 of the first warp
      * draws the exposure count */
     const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
     const int32_t a = st[i], nch = st[i + 1] - st[i];
@@ -1832,6 +1856,8 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
       cum[k] = c;
     }
   }
+  __syncwarp();
+  asm volatile("bar.sync 1, 64;" ::: "memory"); /* the second warp's gamma variate is in s_gam */
   if (lane != 0) return;
   const double srisk = (double)pre_sw * 0x1.0p-24;
   const double exposure = srisk * total_p;
@@ -1846,7 +1872,15 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
       double r = (double)rp->nb_r;
       double pp = r / (r + mean);
       double u = lpg_next(&sm);
-      total = (u < rp->zi) ? 0 : rp->nb_r >= 1 ? lpg_negbinom_dc(&sm, rp->nb_d, rp->nb_c, pp) : lpg_negbinom(&sm, r, pp);
+      if (u < rp->zi) {
+        total = 0;
+      } else if (rp->nb_r >= 1) {
+        /* lpg_negbinom_dc with its gamma variate from the second warp */
+        sm.k = s_gamk;
+        total = lpg_poisson(&sm, s_gam * ((1.0 - pp) / pp));
+      } else {
+        total = lpg_negbinom(&sm, r, pp);
+      }
     }
   } else {
     total = lpg_poisson(&sm, exposure);

@@ -48,6 +48,23 @@ def test_poisson_sampler_moments():
     assert stats.chisquare(obs, exp * obs.sum() / exp.sum()).pvalue > 1e-4
 
 
+def test_poisson_inversion_from_mode_and_ptrs_distribution():
+    # the three samplers: inversion from 0 (< 10), from the mode (10 - 200), PTRS (>= 200)
+    for seed, lam in [(21, 9.5), (22, 10.0), (23, 30.0), (24, 150.7), (25, 199.9), (26, 200.0), (27, 640.0)]:
+        x = O.poisson_many(seed, lam, 200000)
+        lo, hi = int(lam - 4 * math.sqrt(lam)), int(lam + 4 * math.sqrt(lam)) + 1
+        lo = max(lo, 0)
+        edges = np.arange(lo, hi + 1)
+        obs = np.array([np.count_nonzero(x < lo)] + [np.count_nonzero(x == k) for k in edges[:-1]]
+                       + [np.count_nonzero(x >= hi)])
+        cdf = stats.poisson.cdf
+        exp = np.array([cdf(lo - 1, lam)] + list(stats.poisson.pmf(edges[:-1], lam)) + [1 - cdf(hi - 1, lam)])
+        exp = exp * len(x)
+        keep = exp > 5
+        assert stats.chisquare(obs[keep], exp[keep] * obs[keep].sum() / exp[keep].sum()).pvalue > 1e-4, lam
+        assert abs(x.mean() - lam) < 5 * math.sqrt(lam / len(x))
+
+
 def test_gamma_and_negbinom_moments():
     for a in [0.5, 1.0, 4.0, 1000.0]:
         g = O.gamma_many(3, a, 40000)
