@@ -2116,9 +2116,15 @@ __device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& t
  * relative FOI (model.py:1127-1145) and every susceptible total. */
 __device__ __forceinline__ void claim(DevWorld& W, uint32_t hit, int g, const SelInfo& N) {
   const int64_t pos = hit;
+  /* the agent's fixed columns requested first, and its strain draw formed
+   * while the claim's atomic is in flight (a lost claim discards them) */
+  const uint32_t ref = W.ref[pos];
+  const int8_t et = W.et[pos];
+  const float risk = W.risk[pos];
   uint32_t* wp = reinterpret_cast<uint32_t*>(W.ds + (pos & ~3LL));
   const int sh = (int)(pos & 3) * 8;
   uint32_t old = *(volatile uint32_t*)wp;
+  const double r = lpg_u01(N.seed, LPG_P_STRAIN, N.t, ref, 0, 0);
   bool won = false;
   while (((old >> sh) & 0xffu) == 0) {
     const uint32_t nw = (old & ~(0xffu << sh)) | (1u << sh);
@@ -2132,7 +2138,6 @@ __device__ __forceinline__ void claim(DevWorld& W, uint32_t hit, int g, const Se
   if (!won) return;
   const int G = W.G;
   const int64_t cid = pos / LPG_CHUNK;
-  const double r = lpg_u01(N.seed, LPG_P_STRAIN, N.t, W.ref[pos], 0, 0);
   int s = 0;
   for (int k = 0; k < N.ns; ++k)
     if (r < N.cum[k]) {
@@ -2142,12 +2147,11 @@ __device__ __forceinline__ void claim(DevWorld& W, uint32_t hit, int g, const Se
   W.strain[pos] = (int8_t)s;
   {
     /* first step in E is at t + 1 (model.py:393-454) */
-    const int8_t et = W.et[pos];
     const int32_t e1 = N.t + 1 + (et > 0 ? et : 0);
     W.evt[pos] = e1;
     atomicMin(&W.sub_evt[pos >> 7], e1);
   }
-  const uint64_t w = fix_risk(W.risk[pos]);
+  const uint64_t w = fix_risk(risk);
   atomicAdd(&W.tot[(int64_t)TT_S * G + g], -1);
   atomicAdd(&W.tot[(int64_t)(TT_E0 + s) * G + g], 1);
   atomicAdd(&W.ev[(int64_t)(EV_TXNEW0 + s) * G + g], 1);
