@@ -613,9 +613,11 @@ __device__ __forceinline__ uint32_t slab_reserve(uint32_t* s_cnt, uint32_t n) {
 }
 
 /* Append one thread's queue entries of 16 slots (ei: agents in E or I,
- * dead: deaths with their state before the sweep).  All 32 lanes call. */
+ * dead: deaths with their state before the sweep) of simulation sim: the
+ * entry's kind field holds QA_* in bits 0-1 and sim in bits 2-15.  All 32
+ * lanes call. */
 __device__ __forceinline__ void queue_a16(uint64_t* slab, uint32_t* s_cnt, int64_t pos0, uint32_t ei, uint32_t dead,
-                                          uint4 sv) {
+                                          uint4 sv, uint32_t sim) {
   if (__ballot_sync(FULLMASK, (ei | dead) != 0) == 0) return;
   uint32_t at = slab_reserve(s_cnt, __popc(ei) + __popc(dead));
   uint32_t m = ei | dead;
@@ -624,7 +626,7 @@ __device__ __forceinline__ void queue_a16(uint64_t* slab, uint32_t* s_cnt, int64
     m &= m - 1;
     const bool is_dead = (dead >> k) & 1u;
     const uint32_t word = k < 4 ? sv.x : k < 8 ? sv.y : k < 12 ? sv.z : sv.w;
-    slab[at++] = q_entry(pos0 + k, is_dead ? QA_DEATH : QA_DS, is_dead ? (word >> (8 * (k & 3))) : 0u);
+    slab[at++] = q_entry(pos0 + k, (is_dead ? QA_DEATH : QA_DS) | (sim << 2), is_dead ? (word >> (8 * (k & 3))) : 0u);
   }
 }
 
@@ -1108,10 +1110,10 @@ __device__ __forceinline__ void ds_queue_step(DevWorld& W, uint64_t e, bool on) 
   int32_t dS = 0, dE = 0, dI = 0, dR = 0, dPP = 0, dP = 0, nPP = 0, nP = 0, nDead = 0;
   if (on) {
     const int64_t pos = (int64_t)(uint32_t)e;
-    const uint32_t kind = (uint32_t)(e >> 32) & 0xffffu;
+    const uint32_t kind = (uint32_t)(e >> 32) & 3u;
     const int64_t cid = pos / LPG_CHUNK;
     g = W.cmeta[cid].x;
-    const DevRep* rp = &W.reps[W.node_rep[g]];
+    const DevRep* rp = &W.reps[(e >> 34) & 0x3fffu]; /* the simulation, carried by the entry */
     const int t = rp->cur_t;
     if (kind == QA_DEATH) {
       const int8_t s = (int8_t)(uint8_t)(e >> 48);
@@ -1309,7 +1311,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_due(DevWorld W) {
       /* the agents due now get their next event in ds_queue_step (atomicMin) */
       if (edue && (lane & 7) == 0) W.sub_evt[sb] = nmin;
     }
-    queue_a16(slab, &s_qcnt, pos0, ei, dead, v);
+    queue_a16(slab, &s_qcnt, pos0, ei, dead, v, (uint32_t)(rec >> 32) & 0x3fffu);
   }
   n_due = __reduce_add_sync(FULLMASK, n_due);
   n_edue = __reduce_add_sync(FULLMASK, n_edue);
@@ -2360,10 +2362,12 @@ __device__ __noinline__ void sel_rounds(DevWorld& W) {
         if (s_k > 0) {
           atomicAdd(&W.ctr[LPG_CTR_SEL_TARGETS], (unsigned long long)s_k);
           atomicAdd(&W.ctr[LPG_CTR_SEL_NODE_ROUNDS], 1ULL);
-          s_N.seed = rp->seed;
-          s_N.t = rp->cur_t;
-          s_N.ns = rp->ns;
-          sel_strain_cum(W, rp, g, s_N.cum);
+          if (round == 1) { /* the node's strain thresholds are the same every round */
+            s_N.seed = rp->seed;
+            s_N.t = rp->cur_t;
+            s_N.ns = rp->ns;
+            sel_strain_cum(W, rp, g, s_N.cum);
+          }
         }
       }
       __syncthreads();
