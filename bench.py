@@ -100,7 +100,7 @@ def sweep_b_bytes(params, t):
 
 # DRAM bytes ncu measured per unit of counted work, by kernel: (counter,
 # bytes per unit, bytes per launch besides), and where they were measured.
-NCU_TRAFFIC_PER_UNIT = {"k_select": ("sel_targets", 1077.0, 0.0)}
+NCU_TRAFFIC_PER_UNIT = {"k_select": ("sel_targets", 1071.0, 0.0)}
 NCU_TRAFFIC_SOURCE = {
     "k_select": "ncu DRAM read+write of k_sel_locate + k_sel_claim + k_sel_rounds per target located, "
                 "tick 151 of the 5e7-agent case (profiles/tick_kernels_nigeria_5e7_t151.md), "
