@@ -37,7 +37,6 @@
 #define LPG_SUB 128
 #define LPG_NSUB (LPG_CHUNK / LPG_SUB)
 #define LPG_SWEEP_THREADS 256
-#define LPG_SPT (LPG_CHUNK / LPG_SWEEP_THREADS) /* slots per thread = 8 */
 #define LPG_MAX_REPS 256
 #define LPG_NO_DOD 0x7f7f7f7f /* "no alive agent": bytes 0x7f, above every date of death */
 #define LPG_SWEEP_CONSUMERS 256

@@ -468,7 +468,6 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
 #define LPG_PLAIN_GROUP (LPG_COL_BYTES / LPG_CHUNK)
 #define LPG_SWEEP_SMEM (LPG_NST * LPG_STAGE_BYTES)
 #define LPG_MBAR_SPIN (1LL << 24)
-#define LPG_DIRECT_UNROLL 8
 
 /* 16-byte global load that bypasses L1 allocation (streamed once). */
 __device__ __forceinline__ uint4 ldg_stream16(const void* p) {
@@ -561,32 +560,9 @@ __device__ __forceinline__ int32_t stage_end(const SweepPlan& P, int32_t w, int3
   return min(lim, w + stage_chunks(P.flags[lo]));
 }
 
-/* Byte mask (bit j for byte j) of the bytes of x equal to 1 or 2. */
-__device__ __forceinline__ uint32_t ei_bits(uint64_t x) {
-  uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
-  uint32_t a = __vcmpltu4(__vsub4(lo, 0x01010101u), 0x02020202u);
-  uint32_t b = __vcmpltu4(__vsub4(hi, 0x01010101u), 0x02020202u);
-  uint32_t m = 0;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    m |= ((a >> (8 * j + 7)) & 1u) << j;
-    m |= ((b >> (8 * j + 7)) & 1u) << (j + 4);
-  }
-  return m;
-}
-/* Byte mask of the non-negative (alive) bytes of x. */
-__device__ __forceinline__ uint32_t alive_bits(uint64_t x) {
-  uint32_t m = 0;
-#pragma unroll
-  for (int j = 0; j < 8; ++j) m |= ((uint32_t)((x >> (8 * j + 7)) & 1u) ^ 1u) << j;
-  return m;
-}
-__device__ __forceinline__ uint64_t set_byte(uint64_t x, int j, int8_t v) {
-  return (x & ~(0xffULL << (8 * j))) | ((uint64_t)(uint8_t)v << (8 * j));
-}
-
-/* Queue entries of the sweeps (u64): bits 0-31 position, bits 32-47 kind or
- * event flags, bits 48-55 the state byte before the sweep (deaths). */
+/* Queue entries of the sweeps (u64): bits 0-31 position, bits 32-47 kind
+ * and simulation (k_sweep_due) or event flags (k_sweep_rs), bits 48-55 the
+ * state byte before the sweep (deaths). */
 #define QA_DS 1u
 #define QA_DEATH 2u
 #define QB_RI 1u /* bit 0: RI-eligible; bit 1 + k: candidate of SIA event k */
