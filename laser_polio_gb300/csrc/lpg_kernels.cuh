@@ -2091,8 +2091,9 @@ __device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& t
 }
 
 /* The first target to claim an agent (state 0 -> 1) exposes it: strain by
- * relative FOI (model.py:1127-1145) and every susceptible total. */
-__device__ __forceinline__ void claim(DevWorld& W, uint32_t hit, int g, const SelInfo& N) {
+ * relative FOI (model.py:1127-1145) and every susceptible total.  Returns
+ * whether this target claimed it (and the weight it removed in *w_out). */
+__device__ __forceinline__ bool claim(DevWorld& W, uint32_t hit, int g, const SelInfo& N, uint64_t* w_out = nullptr) {
   const int64_t pos = hit;
   /* the agent's fixed columns requested first, and its strain draw formed
    * while the claim's atomic is in flight (a lost claim discards them) */
@@ -2113,7 +2114,7 @@ __device__ __forceinline__ void claim(DevWorld& W, uint32_t hit, int g, const Se
     }
     old = prev;
   }
-  if (!won) return;
+  if (!won) return false;
   const int G = W.G;
   const int64_t cid = pos / LPG_CHUNK;
   int s = 0;
@@ -2139,6 +2140,8 @@ __device__ __forceinline__ void claim(DevWorld& W, uint32_t hit, int g, const Se
     atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
     atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
   }
+  if (w_out) *w_out = w;
+  return true;
 }
 
 /* Node of target q: the last g with off[g] <= q. */
@@ -2297,6 +2300,8 @@ __device__ __noinline__ void sel_rounds(DevWorld& W) {
 
   __shared__ int64_t s_k;
   __shared__ uint64_t s_T;
+  __shared__ unsigned int s_won;
+  __shared__ unsigned long long s_wsum;
   __shared__ SelInfo s_N;
   __shared__ int32_t s_need[256];
   __shared__ int32_t s_nneed;
@@ -2332,9 +2337,22 @@ __device__ __noinline__ void sel_rounds(DevWorld& W) {
     uint32_t* hits = W.hits + (int64_t)(rp->chunk_base + a) * LPG_CHUNK;
     for (int round = 1; round < LPG_MAX_ROUNDS; ++round) {
       if (threadIdx.x == 0) {
-        const int64_t k = __ldcg(&W.size[g]) - (int64_t)__ldcg((const unsigned long long*)&W.uniq[g]);
-        s_T = __ldcg(&W.sw[g]);
-        s_k = (k > 0 && s_T > 0) ? k : 0;
+        /* round 1 from the node's totals after round 0; later rounds from the
+         * previous round's claims, all made by this CTA (the totals equal
+         * these values: size - uniq, and sw less the claimed weights) */
+        int64_t k;
+        uint64_t T;
+        if (round == 1) {
+          k = __ldcg(&W.size[g]) - (int64_t)__ldcg((const unsigned long long*)&W.uniq[g]);
+          T = __ldcg(&W.sw[g]);
+        } else {
+          k = s_k - (int64_t)s_won;
+          T = s_T - s_wsum;
+        }
+        s_T = T;
+        s_k = (k > 0 && T > 0) ? k : 0;
+        s_won = 0;
+        s_wsum = 0;
         if (s_k > 0) {
           atomicAdd(&W.ctr[LPG_CTR_SEL_TARGETS], (unsigned long long)s_k);
           atomicAdd(&W.ctr[LPG_CTR_SEL_NODE_ROUNDS], 1ULL);
@@ -2390,7 +2408,11 @@ __device__ __noinline__ void sel_rounds(DevWorld& W) {
       __syncthreads();
       for (int64_t j = threadIdx.x; j < k; j += blockDim.x) {
         const uint32_t hit = hits[j];
-        if (hit != LPG_NONE) claim(W, hit, g, s_N);
+        uint64_t w = 0;
+        if (hit != LPG_NONE && claim(W, hit, g, s_N, &w)) {
+          atomicAdd(&s_won, 1u);
+          if (w) atomicAdd(&s_wsum, (unsigned long long)w);
+        }
       }
       __threadfence_block();
       __syncthreads();
