@@ -71,6 +71,21 @@ def dist_env():
     return ws, rank, local
 
 
+def reduce_over_ranks(ms, agent_ticks, ws, device):
+    """Whole-job figures of N independent replicas (one per rank): the
+    slowest rank's time and the agent-ticks of all ranks."""
+    if ws <= 1:
+        return ms, agent_ticks
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    a = torch.tensor([agent_ticks], device=device, dtype=torch.float64)
+    dist.all_reduce(a)
+    return float(t.item()), float(a.item())
+
+
 def tick_bytes(params, t):
     """Bytes per agent slot on tick t of every column the reference's loops
     read that tick, each counted once (state, node, strain, three timers,
@@ -508,17 +523,7 @@ def main():
     cnt = counts_per_tick(params, res["births"])
     ticks = np.arange(W + 1, W + K + 1)
     agent_ticks = float(cnt[ticks].sum())
-    ms_max = ms
-    at_total = agent_ticks
-    if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-        a = torch.tensor([agent_ticks], device="cuda", dtype=torch.float64)
-        dist.all_reduce(a)
-        at_total = float(a.item())
+    ms_max, at_total = reduce_over_ranks(ms, agent_ticks, ws, "cuda")
     value = at_total / (ms_max / 1e3)
 
     # ---- per-kernel times (profiling mode, same ticks) --------------------
