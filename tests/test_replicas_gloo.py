@@ -22,7 +22,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank(rank, ws, port, out):
+def _rank(rank, ws, port, outdir):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws))
     sys.path.insert(0, str(ROOT))
     import torch.distributed as dist
@@ -32,17 +32,16 @@ def _rank(rank, ws, port, out):
     dist.init_process_group("gloo", rank=rank, world_size=ws)
     ms = [12.5, 20.0][rank]
     agent_ticks = [3.0e9, 5.0e9][rank]
-    out[rank] = bench.reduce_over_ranks(ms, agent_ticks, ws, "cpu")
+    got = bench.reduce_over_ranks(ms, agent_ticks, ws, "cpu")
+    Path(outdir, f"rank{rank}").write_text(repr(got))
     assert bench.dist_env() == (ws, rank, 0)
     dist.destroy_process_group()
 
 
-def test_two_replicas_reduce_to_slowest_time_and_total_work():
+def test_two_replicas_reduce_to_slowest_time_and_total_work(tmp_path):
     ws, port = 2, _free_port()
-    with mp.Manager() as m:
-        out = m.dict()
-        mp.spawn(_rank, args=(ws, port, out), nprocs=ws, join=True)
-        got = dict(out)
+    mp.spawn(_rank, args=(ws, port, str(tmp_path)), nprocs=ws, join=True)  # spawn: no fork
+    got = [eval((tmp_path / f"rank{r}").read_text()) for r in range(ws)]
     assert got[0] == got[1] == (20.0, 8.0e9)
 
 
