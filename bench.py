@@ -27,6 +27,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import subprocess
 import sys
 import threading
@@ -61,6 +62,8 @@ def parse():
     ap.add_argument("--out", default=None)
     ap.add_argument("--batch", type=int, default=0,
                     help="instead: R calibration replicates (730 ticks) batched in one handle vs run one by one")
+    ap.add_argument("--incidence", type=int, default=0, metavar="T",
+                    help="instead: loss and gradient of the expected incidence over T ticks (the adjoint)")
     return ap.parse_args()
 
 
@@ -424,6 +427,113 @@ def batch_arm(args):
         Path(args.out).write_text(json.dumps(line, indent=1))
 
 
+def incidence_eval(ops, inp, target):
+    """One loss and gradient evaluation: L = sum (log1p(lam) - log1p(target))^2
+    over ticks and nodes; lam through the C ABI, dL/dlam on the host, then
+    the vector-Jacobian product through the C ABI."""
+    lam, _ = ops.expected_incidence(inp)
+    resid = np.log1p(lam) - np.log1p(target)
+    g = 2.0 * resid / (1.0 + lam)
+    _, grads = ops.expected_incidence(inp, g)
+    return float((resid * resid).sum()), grads
+
+
+def incidence_arm(args):
+    """Loss and gradient of the expected incidence (lpg_expected_incidence)
+    over T ticks of replayed Nigeria-scale aggregates (774 nodes, 3 strains),
+    against targets from perturbed parameters.  e2e: wall time per
+    evaluation through the C ABI from host arrays (uploads, two calls,
+    downloads).  value: the same evaluations counted against the device time
+    of their kernels alone (torch.profiler's CUPTI records)."""
+    import torch
+
+    from laser_polio_gb300 import ops, synthetic
+
+    T = args.incidence
+    inp = synthetic.incidence_inputs(T=T, n_nodes=args.nodes, seed=args.seed)
+    G, S = inp["r0s"].shape[0], inp["beta"].shape[2]
+    rng = np.random.default_rng(args.seed + 1)
+    pert = dict(inp, R=1.1, amp=0.35, peak=170.0, k=0.6, r0s=inp["r0s"] * rng.lognormal(0.0, 0.05, G))
+    target, _ = ops.expected_incidence(pert)
+    W, K = max(3, args.warmup), max(1, min(args.steps, 50))
+    for _ in range(W):
+        incidence_eval(ops, inp, target)
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(K):
+            loss, grads = incidence_eval(ops, inp, target)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) / K
+    kernels, dev_ms = None, None
+    try:
+        from torch.profiler import ProfilerActivity, profile
+
+        with profile(activities=[ProfilerActivity.CUDA]) as prof:
+            for _ in range(K):
+                incidence_eval(ops, inp, target)
+            torch.cuda.synchronize()
+        kernels = {}
+        for ev in prof.key_averages():
+            us = getattr(ev, "device_time_total", None)
+            if us is None:
+                us = getattr(ev, "cuda_time_total", 0.0)
+            m = re.search(r"k_inc_\w+(<\d>)?", ev.key)
+            if us and m:
+                kernels[m.group(0)] = {"launches": ev.count, "ms_per_eval": us / 1e3 / K}
+        dev_ms = sum(v["ms_per_eval"] for v in kernels.values()) or None
+    except Exception as exc:  # the profiler is optional evidence; the e2e number stands without it
+        kernels = {"unavailable": f"{type(exc).__name__}: {exc}"}
+    gemm_flop = 2.0 * T * S * G * G  # one (T S) x G x G product
+    roof = None
+    if isinstance(kernels, dict) and kernels:
+        gk = {k: v for k, v in kernels.items() if k.startswith("k_inc_gemm")}
+        if gk:
+            launches = sum(v["launches"] for v in gk.values()) / K
+            ms = sum(v["ms_per_eval"] for v in gk.values()) / launches
+            ach = gemm_flop / (ms / 1e3) / 1e12
+            roof = {"bound": "fp64", "achieved": ach, "peak": 1.25, "unit": "TFLOP/s", "frac": ach / 1.25,
+                    "peak_kind": "nominal GB300 FP64 (no measured FP64 peak)", "traffic": None,
+                    "flop_per_launch": gemm_flop}
+    h2d = sum(inp[k].nbytes for k in ("srisk", "beta", "pop", "doy", "year", "r0s", "pops", "dist"))
+    cpu = None
+    if not args.no_cpu:
+        from oracle import incidence as oracle_incidence
+
+        t0 = time.perf_counter()
+        lam, _ = oracle_incidence.incidence(inp)
+        resid = np.log1p(lam) - np.log1p(target)
+        oracle_incidence.incidence(inp, 2.0 * resid / (1.0 + lam))
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": 1.0 / cpu_s, "unit": "evaluations/s", "cores": 1, "kind": "port",
+               "sample": f"one loss and gradient evaluation, T={T}, numpy FP64 restatement"}
+    line = {
+        "metric": "expected-incidence loss and gradient evaluations/s",
+        "value": (1e3 / dev_ms) if dev_ms else None,
+        "unit": "evaluations/s",
+        "n_gpus": 1,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": dev_ms,
+        "higher_is_better": True,
+        "dtype": "f64",
+        "data": "synthetic (seeded numpy, replayed-aggregate shapes)",
+        "config": {"workload": f"adjoint of expected incidence, {G} nodes, {T} ticks, {S} strains",
+                   "loss": "sum (log1p(lam) - log1p(target))^2", "l2": "inputs uploaded per call"},
+        "e2e": {"value": 1.0 / wall, "unit": "evaluations/s", "ms_per_eval": wall * 1e3,
+                "h2d_bytes_per_step": 2 * h2d + 8 * T * G, "d2h_bytes_per_step": 8 * (2 * T * G + G + G * G)},
+        "kernels": kernels,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "loss": loss,
+        "grad": {k: grads[k] for k in ("R", "amp", "peak", "k", "a", "b", "c")},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if args.out:
+        Path(args.out).write_text(json.dumps(line, indent=1))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -431,6 +541,9 @@ def main():
         return
     if args.batch:
         batch_arm(args)
+        return
+    if args.incidence:
+        incidence_arm(args)
         return
     import torch
 

@@ -321,6 +321,50 @@ int lpg_count_seirp_static(const int16_t* node_id, const int8_t* disease_state, 
                            int32_t* E_by_strain, int32_t* I_by_strain, int32_t* POTP, int32_t* P,
                            int64_t* n_invalid, void* stream);
 
+/* Expected incidence of a replayed tick range and its vector-Jacobian
+ * product, for gradient-based calibration.  No counterpart in the reference
+ * (its calibration samples parameters with Optuna, laser_polio/calibration,
+ * and differentiates nothing).  With the agent state held fixed, the
+ * node-level part of the transmission step (model.py:1315-1363) maps
+ * per-tick aggregates to the expected new exposures
+ *   N        = rownorm(gravity(pops, dist, k, a, b, c) / (sum pops)^c, max_frac)
+ *                                                   (model.py:1250-1258)
+ *   u[t,n,s] = beta[t,n,s] (1 - sum_j N[n,j]) + sum_i N[i,n] beta[t,i,s]
+ *   seas[t]  = 1 + amp cos(2 pi (doy[t] - peak) / year[t])  (utils.py:589-625)
+ *   lam[t,n] = srisk[t,n] sum_s (1 - exp(-u seas[t] r0s[n] R / max(pop[t,n], 1)))
+ * gravity[i][j] = k pops_i^a pops_j^b / dist_ij^c off the diagonal, 0 on it;
+ * a row whose sum exceeds max_frac is scaled down to max_frac.  R scales
+ * every agent's infectivity (R0 over the R0 the aggregates were taken at).
+ * All arrays are host, row-major FP64. */
+typedef struct {
+  int32_t T, G, S;    /* ticks, nodes, strains (S <= LPG_MAX_STRAINS) */
+  const double* srisk; /* [T][G] susceptibles' summed acquisition risk */
+  const double* beta;  /* [T][G][S] summed infectivity before mixing */
+  const double* pop;   /* [T][G] node population */
+  const double* doy;   /* [T] day of year of each tick */
+  const double* year;  /* [T] days in that year */
+  const double* r0s;   /* [G] per-node R0 scalars */
+  const double* pops;  /* [G] gravity populations */
+  const double* dist;  /* [G][G] distances (the diagonal is ignored) */
+  double R, amp, peak; /* infectivity scale, seasonal amplitude, peak day */
+  double k, a, b, c;   /* gravity parameters */
+  double max_frac;     /* row-sum cap of the network */
+} lpg_incidence_in;
+
+typedef struct {
+  double R, amp, peak, k, a, b, c; /* dL/d of each scalar */
+  double* r0s;                     /* [G] dL/dr0s, or NULL */
+  double* network;                 /* [G][G] dL/dN (zero diagonal), or NULL */
+} lpg_incidence_grad;
+
+/* lam_out [T][G] (host) receives lam.  With g_lam non-NULL ([T][G], host:
+ * dL/dlam), *grad receives the gradients of L = sum g_lam * lam.  Device
+ * scratch is allocated and freed per call; synchronous on `stream`.
+ * Reductions use atomics: results match a sequential FP64 evaluation to
+ * rounding, not bit for bit.  Errors: lpg_op_last_error(). */
+int lpg_expected_incidence(const lpg_incidence_in* in, double* lam_out, const double* g_lam,
+                           lpg_incidence_grad* grad, void* stream);
+
 const char* lpg_op_last_error(void);
 
 #ifdef __cplusplus

@@ -184,6 +184,27 @@ class lpg_profile(C.Structure):
     ]
 
 
+class lpg_incidence_in(C.Structure):
+    _fields_ = [
+        ("T", C.c_int32),
+        ("G", C.c_int32),
+        ("S", C.c_int32),
+        *[(name, C.POINTER(C.c_double)) for name in ("srisk", "beta", "pop", "doy", "year", "r0s", "pops", "dist")],
+        *[(name, C.c_double) for name in ("R", "amp", "peak", "k", "a", "b", "c", "max_frac")],
+    ]
+
+
+INCIDENCE_SCALAR_GRADS = ("R", "amp", "peak", "k", "a", "b", "c")
+
+
+class lpg_incidence_grad(C.Structure):
+    _fields_ = [
+        *[(name, C.c_double) for name in INCIDENCE_SCALAR_GRADS],
+        ("r0s", C.POINTER(C.c_double)),
+        ("network", C.POINTER(C.c_double)),
+    ]
+
+
 def ptr(arr, ctype):
     """Pointer to the first element of a contiguous numpy array (or NULL)."""
     if arr is None:

@@ -38,6 +38,8 @@ SIGNATURES = {
     "lpg_destroy": (None, [C.c_void_p]),
     "lpg_count_seirp": (C.c_int, [C.c_void_p] * 5 + [C.c_int32, C.c_int32, C.c_int64] + [C.c_void_p] * 10),
     "lpg_count_seirp_static": (C.c_int, [C.c_void_p] * 5 + [C.c_int32, C.c_int32, C.c_int64] + [C.c_void_p] * 10),
+    "lpg_expected_incidence": (C.c_int, [C.POINTER(_abi.lpg_incidence_in), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double), C.POINTER(_abi.lpg_incidence_grad), C.c_void_p]),
     "lpg_op_last_error": (C.c_char_p, []),
 }
 

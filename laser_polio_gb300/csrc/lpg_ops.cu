@@ -61,6 +61,15 @@ static int op_fail(int code, const char* fmt, ...) {
   return code;
 }
 
+/* The same error text for the ops of other translation units (lpg_adjoint.cu). */
+int lpg_ops_fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
 extern "C" const char* lpg_op_last_error(void) { return g_err; }
 
 /* ------------------------------------------------------------------------ */

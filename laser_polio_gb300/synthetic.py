@@ -335,6 +335,38 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
     return params, cols
 
 
+def incidence_inputs(T=365, n_nodes=774, n_strains=3, n_agents=2.2e8, seed=42):
+    """Node-level aggregates of a replayed Nigeria-scale run, for the
+    expected-incidence map and its adjoint (laser_polio_gb300.ops.
+    expected_incidence): node populations lognormal(ln 2.8e5, 0.7) summing
+    to n_agents on a 1000 km square, growing at CBR 37 minus a flat 10 per
+    1000; susceptibles 5-30% of a node carrying unit mean risk; infectivity
+    by strain (1, 0.25, 0.125 of the VDPV2 level) of about 0.6 per infected
+    agent-day from a few hundred infected agents, zero in 30% of node-ticks;
+    ticks from 2019-01-01 with their day of year and year length; the
+    gravity network k=0.5, a=b=1, c=2, max export fraction 0.2; R0 over the
+    recorded R0 = 1, seasonal amplitude 0.4 peaking on day 180, r0_scalars
+    lognormal(0, 0.3).  Returns the dict expected_incidence takes."""
+    import datetime as dt
+
+    rng = np.random.default_rng(seed)
+    pops = _node_pops(rng, n_nodes, np.log(2.8e5), 0.7, n_agents).astype(np.float64)
+    dist = _gravity_distances(rng, n_nodes, 1000.0)
+    growth = (37.0 - 10.0) / 365000.0
+    pop = pops[None, :] * (1.0 + growth) ** np.arange(T)[:, None]
+    sus = rng.uniform(0.05, 0.3, n_nodes)
+    srisk = pop * sus[None, :] * rng.lognormal(-0.005, 0.1, (T, n_nodes))
+    scal = np.array([1.0, 0.25, 0.125, 0.0625])[:n_strains]
+    infected = rng.gamma(2.0, 150.0, (T, n_nodes, n_strains)) * (rng.uniform(size=(T, n_nodes, n_strains)) > 0.3)
+    beta = 0.6 * infected * scal[None, None, :]
+    dates = [dt.date(2019, 1, 1) + dt.timedelta(days=i) for i in range(T)]
+    doy = np.array([d.timetuple().tm_yday for d in dates], np.float64)
+    year = np.array([366.0 if (d.year % 4 == 0 and (d.year % 100 != 0 or d.year % 400 == 0)) else 365.0
+                     for d in dates])
+    return dict(srisk=srisk, beta=beta, pop=pop, doy=doy, year=year, r0s=rng.lognormal(0.0, 0.3, n_nodes), R=1.0,
+                amp=0.4, peak=180.0, pops=pops, dist=dist, k=0.5, a=1.0, b=1.0, c=2.0, max_frac=0.2)
+
+
 def replicate_specs(n=64, seed=42, dur=730):
     """Per-replicate settings of a calibration batch: node counts from
     {14, 44, 120, 300}, agents log-uniform in [1e6, 2e7] (about 4e8 in total

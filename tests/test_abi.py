@@ -40,6 +40,8 @@ def test_struct_layout_matches_header(tmp_path):
         "lpg_dist": _abi.lpg_dist,
         "lpg_sim_state": _abi.lpg_sim_state,
         "lpg_profile": _abi.lpg_profile,
+        "lpg_incidence_in": _abi.lpg_incidence_in,
+        "lpg_incidence_grad": _abi.lpg_incidence_grad,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "lpg.h"', "int main(void){"]
     for name, cls in structs.items():

@@ -1,0 +1,145 @@
+"""Expected incidence and its vector-Jacobian product (lpg_expected_incidence).
+
+CPU: the numpy restatement (oracle/incidence.py) is pinned to the package's
+network and seasonality builders (the ones the engine runs on) and its
+reverse pass to fourth-order central finite differences of its own forward
+pass, with and without capped network rows.  GPU: the CUDA path against the
+oracle on the same inputs; FP64 with atomically reduced sums, so agreement
+is to a relative 1e-9, not bit for bit."""
+
+import datetime
+
+import numpy as np
+import pytest
+
+from laser_polio_gb300 import ops
+from laser_polio_gb300.core import gravity, row_normalizer
+from laser_polio_gb300.utils import seasonality_table
+from oracle import incidence as I
+
+SCALARS = ("R", "amp", "peak", "k", "a", "b", "c")
+FD_RTOL = 1e-6
+
+
+def _loss(inp, g, **mod):
+    x = dict(inp)
+    x.update(mod)
+    return float((g * I.incidence(x)[0]).sum())
+
+
+def _fd(f, x0, h):
+    return (-f(x0 + 2 * h) + 8 * f(x0 + h) - 8 * f(x0 - h) + f(x0 - 2 * h)) / (12 * h)
+
+
+def _case(max_frac):
+    inp = I.random_inputs(10, 8, 2, seed=3)
+    inp["max_frac"] = max_frac
+    g = np.random.default_rng(2).normal(size=(10, 8))
+    return inp, g
+
+
+@pytest.mark.parametrize("max_frac", [0.2, 3.5e-6], ids=["uncapped", "capped"])
+def test_oracle_vjp_matches_finite_differences(max_frac):
+    inp, g = _case(max_frac)
+    _, _, rs, capped = I.network(inp["pops"], inp["dist"], inp["k"], inp["a"], inp["b"], inp["c"], max_frac)
+    if max_frac < 1e-3:
+        assert 0 < capped.sum() < len(capped)
+        # keep every row sum away from the cap under the steps below
+        assert np.min(np.abs(rs / max_frac - 1.0)) > 0.05
+    else:
+        assert not capped.any()
+    _, gr = I.incidence(inp, g)
+    for name in SCALARS:
+        h = 1e-3 * max(1.0, abs(inp[name]))
+        fd = _fd(lambda v: _loss(inp, g, **{name: v}), inp[name], h)
+        # L is ~1e4 and moves by ~1e-4 per unit of k, a, b, c: cancellation
+        # limits those differences to ~1e-4 here; the chain check below is tight
+        tol = FD_RTOL if name in ("R", "amp", "peak") else 5e-4
+        assert abs(gr[name] - fd) <= tol * abs(fd), (name, gr[name], fd)
+    # k, a, b, c through the network alone: d/dtheta sum(dL/dN * N(theta))
+    W = gr["network"]
+    par = {n: inp[n] for n in ("k", "a", "b", "c")}
+    for name in par:
+        def f(v, name=name):
+            q = dict(par, **{name: v})
+            return float((W * I.network(inp["pops"], inp["dist"], q["k"], q["a"], q["b"], q["c"], max_frac)[0]).sum())
+        fd = _fd(f, par[name], 1e-3 * max(1.0, abs(par[name])))
+        assert abs(gr[name] - fd) <= FD_RTOL * abs(fd), ("chain", name, gr[name], fd)
+    for j in (0, 5):
+        def f(v, j=j):
+            r = inp["r0s"].copy()
+            r[j] = v
+            return _loss(inp, g, r0s=r)
+        fd = _fd(f, inp["r0s"][j], 1e-3)
+        assert abs(gr["r0s"][j] - fd) <= FD_RTOL * abs(fd), ("r0s", j)
+    # dL/dN: perturb the normalised network directly
+    N = I.network(inp["pops"], inp["dist"], inp["k"], inp["a"], inp["b"], inp["c"], max_frac)[0]
+    args = [inp[n] for n in ("srisk", "beta", "pop", "doy", "year", "r0s", "R", "amp", "peak")]
+    for a, b in ((2, 5), (7, 0)):
+        def f(v, a=a, b=b):
+            M = N.copy()
+            M[a, b] = v
+            return float((g * I.forward(*args, M)[0]).sum())
+        fd = _fd(f, N[a, b], 1e-4)
+        assert abs(gr["network"][a, b] - fd) <= FD_RTOL * abs(fd) + 1e-12, ("network", a, b)
+    assert np.all(np.diag(gr["network"]) == 0.0)
+
+
+def test_oracle_network_is_the_engines_network():
+    inp = I.random_inputs(2, 40, 1, seed=7)
+    for max_frac in (0.2, 1e-5):
+        N = I.network(inp["pops"], inp["dist"], 0.5, 1.0, 1.0, 2.0, max_frac)[0]
+        want = row_normalizer(gravity(inp["pops"], inp["dist"], 0.5, 1.0, 1.0, 2.0)
+                              / np.power(inp["pops"].sum(), 2.0), max_frac)
+        np.testing.assert_allclose(N, want, rtol=1e-14, atol=0)
+
+
+def test_oracle_seasonality_is_the_engines_seasonality():
+    dates = [datetime.date(2019, 1, 1) + datetime.timedelta(days=d) for d in range(800)]  # 2020 is a leap year
+    doy = np.array([d.timetuple().tm_yday for d in dates], np.float64)
+    year = np.array([366.0 if d.year == 2020 else 365.0 for d in dates])
+    inp = I.random_inputs(len(dates), 3, 1, seed=1)
+    inp.update(doy=doy, year=year, amp=0.3, peak=200.0)
+    N = I.network(inp["pops"], inp["dist"], inp["k"], inp["a"], inp["b"], inp["c"], inp["max_frac"])[0]
+    _, mid = I.forward(*[inp[n] for n in ("srisk", "beta", "pop", "doy", "year", "r0s", "R", "amp", "peak")], N)
+    np.testing.assert_allclose(mid["seas"], seasonality_table(dates, 0.3, 200.0), rtol=1e-14, atol=0)
+
+
+def test_wrapper_rejects_bad_shapes_before_any_device_call():
+    inp = I.random_inputs(4, 5, 2, seed=0)
+    bad = dict(inp, pop=inp["pop"][:, :3])
+    with pytest.raises(ValueError, match="pop"):
+        ops.expected_incidence(bad)
+    with pytest.raises(ValueError, match="g has shape"):
+        ops.expected_incidence(inp, np.zeros((4, 4)))
+
+
+def _close(got, want, rtol, what):
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    scale = np.max(np.abs(want)) if want.size else 0.0
+    err = np.max(np.abs(got - want)) if want.size else 0.0
+    assert err <= rtol * max(scale, 1e-300), (what, err, scale)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize(
+    "T,G,S,max_frac,seed",
+    [(1, 1, 1, 0.2, 0), (10, 8, 2, 3.5e-6, 3), (37, 33, 3, 0.2, 5), (365, 100, 1, 1e-5, 11), (30, 774, 4, 0.2, 2)],
+)
+def test_gpu_incidence_and_vjp_match_oracle(T, G, S, max_frac, seed):
+    """Relative 1e-9 of each output's largest magnitude (FP64; the GPU sums
+    in another order and with atomics)."""
+    inp = I.random_inputs(T, G, S, seed=seed)
+    inp["max_frac"] = max_frac
+    g = np.random.default_rng(seed + 100).normal(size=(T, G))
+    want_lam, want = I.incidence(inp, g)
+    lam0, none = ops.expected_incidence(inp)
+    assert none is None
+    lam, got = ops.expected_incidence(inp, g)
+    _close(lam0, want_lam, 1e-12, "lam")
+    _close(lam, want_lam, 1e-12, "lam with g")
+    for name in SCALARS:
+        _close(got[name], want[name], 1e-9, name)
+    _close(got["r0s"], want["r0s"], 1e-9, "r0s")
+    _close(got["network"], want["network"], 1e-9, "network")
+    assert np.all(np.diag(got["network"]) == 0.0)

@@ -3,6 +3,7 @@ exchange step): its whole-job figures are the slowest rank's time and the
 sum of every rank's agent-ticks.  Checked here with two gloo ranks on the
 CPU."""
 
+import ast
 import os
 import socket
 import sys
@@ -41,7 +42,7 @@ def _rank(rank, ws, port, outdir):
 def test_two_replicas_reduce_to_slowest_time_and_total_work(tmp_path):
     ws, port = 2, _free_port()
     mp.spawn(_rank, args=(ws, port, str(tmp_path)), nprocs=ws, join=True)  # spawn: no fork
-    got = [eval((tmp_path / f"rank{r}").read_text()) for r in range(ws)]
+    got = [ast.literal_eval((tmp_path / f"rank{r}").read_text()) for r in range(ws)]
     assert got[0] == got[1] == (20.0, 8.0e9)
 
 
