@@ -427,24 +427,17 @@ def batch_arm(args):
         Path(args.out).write_text(json.dumps(line, indent=1))
 
 
-def incidence_eval(ops, inp, target):
-    """One loss and gradient evaluation: L = sum (log1p(lam) - log1p(target))^2
-    over ticks and nodes; lam through the C ABI, dL/dlam on the host, then
-    the vector-Jacobian product through the C ABI."""
-    lam, _ = ops.expected_incidence(inp)
-    resid = np.log1p(lam) - np.log1p(target)
-    g = 2.0 * resid / (1.0 + lam)
-    _, grads = ops.expected_incidence(inp, g)
-    return float((resid * resid).sum()), grads
-
-
 def incidence_arm(args):
-    """Loss and gradient of the expected incidence (lpg_expected_incidence)
-    over T ticks of replayed Nigeria-scale aggregates (774 nodes, 3 strains),
-    against targets from perturbed parameters.  e2e: wall time per
-    evaluation through the C ABI from host arrays (uploads, two calls,
-    downloads).  value: the same evaluations counted against the device time
-    of their kernels alone (torch.profiler's CUPTI records)."""
+    """Loss and gradient of the expected incidence over T ticks of replayed
+    Nigeria-scale aggregates (774 nodes, 3 strains), against a target curve
+    from perturbed parameters: L = sum (log1p(lam) - log1p(target))^2 and its
+    gradient with respect to R, amp, peak, r0s and k, a, b, c.  One step = one
+    evaluation on a resident plan (lpg_incidence_plan_eval: parameters up,
+    loss and gradients down).  value: K evaluations between CUDA events on
+    the plan's stream.  e2e: wall time from host arrays, the plan's one-time
+    upload of the aggregates and target included, over the same K
+    evaluations.  roofline: the mixing product's FLOPs over its mean launch
+    time (profiling pass) against the nominal FP64 rate."""
     import torch
 
     from laser_polio_gb300 import ops, synthetic
@@ -455,47 +448,42 @@ def incidence_arm(args):
     rng = np.random.default_rng(args.seed + 1)
     pert = dict(inp, R=1.1, amp=0.35, peak=170.0, k=0.6, r0s=inp["r0s"] * rng.lognormal(0.0, 0.05, G))
     target, _ = ops.expected_incidence(pert)
-    W, K = max(3, args.warmup), max(1, min(args.steps, 50))
-    for _ in range(W):
-        incidence_eval(ops, inp, target)
+    W, K = max(3, args.warmup), max(1, min(args.steps, 200))
     torch.cuda.synchronize()
     with ClockSampler(0) as clocks:
         t0 = time.perf_counter()
-        for _ in range(K):
-            loss, grads = incidence_eval(ops, inp, target)
+        plan = ops.IncidencePlan(inp, target)
+        t_setup = time.perf_counter() - t0
+        for _ in range(W):
+            plan.evaluate(inp, network_grad=False)
+        stream = torch.cuda.ExternalStream(plan.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        wall = (time.perf_counter() - t0) / K
-    kernels, dev_ms = None, None
-    try:
-        from torch.profiler import ProfilerActivity, profile
-
-        with profile(activities=[ProfilerActivity.CUDA]) as prof:
-            for _ in range(K):
-                incidence_eval(ops, inp, target)
-            torch.cuda.synchronize()
-        kernels = {}
-        for ev in prof.key_averages():
-            us = getattr(ev, "device_time_total", None)
-            if us is None:
-                us = getattr(ev, "cuda_time_total", 0.0)
-            m = re.search(r"k_inc_\w+(<\d>)?", ev.key)
-            if us and m:
-                kernels[m.group(0)] = {"launches": ev.count, "ms_per_eval": us / 1e3 / K}
-        dev_ms = sum(v["ms_per_eval"] for v in kernels.values()) or None
-    except Exception as exc:  # the profiler is optional evidence; the e2e number stands without it
-        kernels = {"unavailable": f"{type(exc).__name__}: {exc}"}
+        t1 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(K):
+            res = plan.evaluate(inp, network_grad=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_eval = time.perf_counter() - t1
+        dev_ms = e0.elapsed_time(e1) / K
+    plan.set_profiling(True)
+    for _ in range(K):
+        plan.evaluate(inp, network_grad=False)
+    prof = plan.profile()
+    plan.close()
+    tot = sum(ms for ms, _ in prof.values())
+    kernels = {name: {"launches": n, "ms_per_eval": ms / K, "share": ms / tot if tot else None}
+               for name, (ms, n) in prof.items()}
     gemm_flop = 2.0 * T * S * G * G  # one (T S) x G x G product
-    roof = None
-    if isinstance(kernels, dict) and kernels:
-        gk = {k: v for k, v in kernels.items() if k.startswith("k_inc_gemm")}
-        if gk:
-            launches = sum(v["launches"] for v in gk.values()) / K
-            ms = sum(v["ms_per_eval"] for v in gk.values()) / launches
-            ach = gemm_flop / (ms / 1e3) / 1e12
-            roof = {"bound": "fp64", "achieved": ach, "peak": 1.25, "unit": "TFLOP/s", "frac": ach / 1.25,
-                    "peak_kind": "nominal GB300 FP64 (no measured FP64 peak)", "traffic": None,
-                    "flop_per_launch": gemm_flop}
-    h2d = sum(inp[k].nbytes for k in ("srisk", "beta", "pop", "doy", "year", "r0s", "pops", "dist"))
+    top = max(prof, key=lambda n: prof[n][0])
+    ms_mix = prof["k_inc_gemm_mix"][0] / max(1, prof["k_inc_gemm_mix"][1])
+    ach = gemm_flop / (ms_mix / 1e3) / 1e12
+    roof = {"kernel": "k_inc_gemm_mix", "top_kernel": top, "bound": "fp64", "achieved": ach, "peak": 1.25,
+            "unit": "TFLOP/s", "frac": ach / 1.25, "peak_kind": "nominal GB300 FP64 (no measured FP64 peak)",
+            "traffic": None, "flop_per_launch": gemm_flop}
+    h2d_setup = sum(inp[k].nbytes for k in ("srisk", "beta", "pop", "doy", "year", "pops", "dist")) + target.nbytes
     cpu = None
     if not args.no_cpu:
         from oracle import incidence as oracle_incidence
@@ -509,7 +497,7 @@ def incidence_arm(args):
                "sample": f"one loss and gradient evaluation, T={T}, numpy FP64 restatement"}
     line = {
         "metric": "expected-incidence loss and gradient evaluations/s",
-        "value": (1e3 / dev_ms) if dev_ms else None,
+        "value": 1e3 / dev_ms,
         "unit": "evaluations/s",
         "n_gpus": 1,
         "steps": K,
@@ -519,14 +507,17 @@ def incidence_arm(args):
         "dtype": "f64",
         "data": "synthetic (seeded numpy, replayed-aggregate shapes)",
         "config": {"workload": f"adjoint of expected incidence, {G} nodes, {T} ticks, {S} strains",
-                   "loss": "sum (log1p(lam) - log1p(target))^2", "l2": "inputs uploaded per call"},
-        "e2e": {"value": 1.0 / wall, "unit": "evaluations/s", "ms_per_eval": wall * 1e3,
-                "h2d_bytes_per_step": 2 * h2d + 8 * T * G, "d2h_bytes_per_step": 8 * (2 * T * G + G + G * G)},
+                   "loss": "sum (log1p(lam) - log1p(target))^2",
+                   "l2": "working set (~40 MB) L2-resident by design; no flush"},
+        "e2e": {"value": K / (t_setup + t_eval), "unit": "evaluations/s", "setup_ms": t_setup * 1e3,
+                "ms_per_eval": t_eval / K * 1e3, "h2d_bytes_per_step": h2d_setup / K + 8 * G,
+                "d2h_bytes_per_step": 8 * (8 + G)},
+        "gpu_launches": 7 * K,  # per evaluation: network, mix, forward, backward + seasonal, flows, network_grad
         "kernels": kernels,
         "roofline": roof,
         "cpu_baseline": cpu,
-        "loss": loss,
-        "grad": {k: grads[k] for k in ("R", "amp", "peak", "k", "a", "b", "c")},
+        "loss": res["loss"],
+        "grad": {k: res["grad"][k] for k in ("R", "amp", "peak", "k", "a", "b", "c")},
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)

@@ -357,9 +357,40 @@ typedef struct {
   double* network;                 /* [G][G] dL/dN (zero diagonal), or NULL */
 } lpg_incidence_grad;
 
-/* lam_out [T][G] (host) receives lam.  With g_lam non-NULL ([T][G], host:
- * dL/dlam), *grad receives the gradients of L = sum g_lam * lam.  Device
- * scratch is allocated and freed per call; synchronous on `stream`.
+/* The parameters a calibration varies, per evaluation. */
+typedef struct {
+  double R, amp, peak, k, a, b, c, max_frac;
+  const double* r0s; /* [G] host */
+} lpg_incidence_params;
+
+/* A plan keeps the aggregates (and an optional target curve) resident on
+ * the current device and evaluates the map at any parameters without
+ * re-uploading them.  Not thread-safe; calls on one plan are serialized. */
+typedef struct lpg_incidence_plan lpg_incidence_plan;
+
+/* Copies in's arrays (r0s and the scalars are not used) and, if non-NULL,
+ * target [T][G] (host) to the device.  stream: a cudaStream_t the plan
+ * works on, or NULL for a stream of its own. */
+int lpg_incidence_plan_create(const lpg_incidence_in* in, const double* target, void* stream,
+                              lpg_incidence_plan** out);
+
+/* One evaluation at *prm, synchronous:
+ *   lam_out  [T][G] host, or NULL: lam;
+ *   loss_out (needs a target), or NULL: L = sum (log1p(lam) - log1p(target))^2;
+ *   grad     or NULL: the gradients of L = sum g_lam * lam when g_lam
+ *            ([T][G] host) is given, else of the target loss. */
+int lpg_incidence_plan_eval(lpg_incidence_plan* p, const lpg_incidence_params* prm, const double* g_lam,
+                            double* lam_out, double* loss_out, lpg_incidence_grad* grad);
+void* lpg_incidence_plan_stream(lpg_incidence_plan* p);
+/* Per-kernel device time (CUDA events on the plan's stream) of the
+ * evaluations made while profiling is on; enabling resets the sums. */
+int lpg_incidence_plan_set_profiling(lpg_incidence_plan* p, int32_t enable);
+int lpg_incidence_plan_read_profile(lpg_incidence_plan* p, lpg_profile* out);
+void lpg_incidence_plan_destroy(lpg_incidence_plan* p);
+
+/* One-shot: a plan on `stream`, one evaluation at in's parameters, freed.
+ * lam_out [T][G] (host) receives lam.  With g_lam non-NULL ([T][G], host:
+ * dL/dlam), *grad receives the gradients of L = sum g_lam * lam.
  * Reductions use atomics: results match a sequential FP64 evaluation to
  * rounding, not bit for bit.  Errors: lpg_op_last_error(). */
 int lpg_expected_incidence(const lpg_incidence_in* in, double* lam_out, const double* g_lam,

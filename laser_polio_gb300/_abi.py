@@ -205,6 +205,13 @@ class lpg_incidence_grad(C.Structure):
     ]
 
 
+class lpg_incidence_params(C.Structure):
+    _fields_ = [
+        *[(name, C.c_double) for name in ("R", "amp", "peak", "k", "a", "b", "c", "max_frac")],
+        ("r0s", C.POINTER(C.c_double)),
+    ]
+
+
 def ptr(arr, ctype):
     """Pointer to the first element of a contiguous numpy array (or NULL)."""
     if arr is None:

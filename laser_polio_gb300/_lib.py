@@ -40,6 +40,15 @@ SIGNATURES = {
     "lpg_count_seirp_static": (C.c_int, [C.c_void_p] * 5 + [C.c_int32, C.c_int32, C.c_int64] + [C.c_void_p] * 10),
     "lpg_expected_incidence": (C.c_int, [C.POINTER(_abi.lpg_incidence_in), C.POINTER(C.c_double),
                                          C.POINTER(C.c_double), C.POINTER(_abi.lpg_incidence_grad), C.c_void_p]),
+    "lpg_incidence_plan_create": (C.c_int, [C.POINTER(_abi.lpg_incidence_in), C.POINTER(C.c_double), C.c_void_p,
+                                            C.POINTER(C.c_void_p)]),
+    "lpg_incidence_plan_eval": (C.c_int, [C.c_void_p, C.POINTER(_abi.lpg_incidence_params), C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                          C.POINTER(_abi.lpg_incidence_grad)]),
+    "lpg_incidence_plan_stream": (C.c_void_p, [C.c_void_p]),
+    "lpg_incidence_plan_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
+    "lpg_incidence_plan_read_profile": (C.c_int, [C.c_void_p, C.POINTER(_abi.lpg_profile)]),
+    "lpg_incidence_plan_destroy": (None, [C.c_void_p]),
     "lpg_op_last_error": (C.c_char_p, []),
 }
 

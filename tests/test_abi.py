@@ -42,6 +42,7 @@ def test_struct_layout_matches_header(tmp_path):
         "lpg_profile": _abi.lpg_profile,
         "lpg_incidence_in": _abi.lpg_incidence_in,
         "lpg_incidence_grad": _abi.lpg_incidence_grad,
+        "lpg_incidence_params": _abi.lpg_incidence_params,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "lpg.h"', "int main(void){"]
     for name, cls in structs.items():

@@ -143,3 +143,59 @@ def test_gpu_incidence_and_vjp_match_oracle(T, G, S, max_frac, seed):
     _close(got["r0s"], want["r0s"], 1e-9, "r0s")
     _close(got["network"], want["network"], 1e-9, "network")
     assert np.all(np.diag(got["network"]) == 0.0)
+
+
+def test_plan_without_gpu_reports_cuda_error():
+    import torch
+
+    from laser_polio_gb300 import _lib
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(_lib.LpgError):
+        ops.IncidencePlan(I.random_inputs(3, 4, 1, seed=0))
+
+
+def _oracle_loss_grad(inp, target):
+    lam, _ = I.incidence(inp)
+    r = np.log1p(lam) - np.log1p(target)
+    _, grads = I.incidence(inp, 2.0 * r / (1.0 + lam))
+    return lam, float((r * r).sum()), grads
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("T,G,S,max_frac", [(20, 16, 3, 0.2), (60, 120, 2, 1e-5)])
+def test_gpu_plan_target_loss_and_gradient_match_oracle(T, G, S, max_frac):
+    """A plan with a target curve: the loss and its gradient at several
+    parameter sets against the oracle (relative 1e-9; loss 1e-11), the
+    aggregates uploaded once."""
+    inp = I.random_inputs(T, G, S, seed=9)
+    inp["max_frac"] = max_frac
+    rng = np.random.default_rng(4)
+    target = I.incidence(dict(inp, R=1.3, amp=0.3, r0s=inp["r0s"] * rng.lognormal(0, 0.1, G)))[0]
+    plan = ops.IncidencePlan(inp, target)
+    plan.set_profiling(True)
+    try:
+        for R, amp, peak, k in ((1.1, 0.4, 180.0, 0.5), (0.9, 0.25, 30.0, 0.8), (1.1, 0.4, 180.0, 0.5)):
+            x = dict(inp, R=R, amp=amp, peak=peak, k=k)
+            want_lam, want_loss, want = _oracle_loss_grad(x, target)
+            got = plan.evaluate(x, lam=True)
+            _close(got["lam"], want_lam, 1e-12, "lam")
+            assert abs(got["loss"] - want_loss) <= 1e-11 * want_loss, (got["loss"], want_loss)
+            for name in SCALARS:
+                _close(got["grad"][name], want[name], 1e-9, name)
+            _close(got["grad"]["r0s"], want["r0s"], 1e-9, "r0s")
+            _close(got["grad"]["network"], want["network"], 1e-9, "network")
+        # an explicit g overrides the target loss's dL/dlam
+        g = rng.normal(size=(T, G))
+        got = plan.evaluate(inp, g, network_grad=False)
+        _, want = I.incidence(inp, g)
+        assert "network" not in got["grad"]
+        for name in SCALARS:
+            _close(got["grad"][name], want[name], 1e-9, name)
+        prof = plan.profile()
+        assert list(prof) == ["k_inc_network", "k_inc_gemm_mix", "k_inc_forward", "k_inc_backward",
+                              "k_inc_gemm_flows", "k_inc_network_grad"]
+        assert all(ms > 0 and n >= 4 for ms, n in prof.values())
+    finally:
+        plan.close()
