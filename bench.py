@@ -436,8 +436,8 @@ def incidence_arm(args):
     loss and gradients down).  value: K evaluations between CUDA events on
     the plan's stream.  e2e: wall time from host arrays, the plan's one-time
     upload of the aggregates and target included, over the same K
-    evaluations.  roofline: the mixing product's FLOPs over its mean launch
-    time (profiling pass) against the nominal FP64 rate."""
+    evaluations.  roofline: the slower product's FP32 instructions over its
+    mean launch time (profiling pass) against the nominal FP32 issue rate."""
     import torch
 
     from laser_polio_gb300 import ops, synthetic
@@ -476,13 +476,19 @@ def incidence_arm(args):
     tot = sum(ms for ms, _ in prof.values())
     kernels = {name: {"launches": n, "ms_per_eval": ms / K, "share": ms / tot if tot else None}
                for name, (ms, n) in prof.items()}
-    gemm_flop = 2.0 * T * S * G * G  # one (T S) x G x G product
+    # the products run in double-float on the FP32 pipe: 12 FP32 instructions per term
+    # (Dekker product by FMA, two cross terms, Knuth TwoSum), T S G G terms per launch
+    terms = float(T * S * G * G)
     top = max(prof, key=lambda n: prof[n][0])
-    ms_mix = prof["k_inc_gemm_mix"][0] / max(1, prof["k_inc_gemm_mix"][1])
-    ach = gemm_flop / (ms_mix / 1e3) / 1e12
-    roof = {"kernel": "k_inc_gemm_mix", "top_kernel": top, "bound": "fp64", "achieved": ach, "peak": 1.25,
-            "unit": "TFLOP/s", "frac": ach / 1.25, "peak_kind": "nominal GB300 FP64 (no measured FP64 peak)",
-            "traffic": None, "flop_per_launch": gemm_flop}
+    gemm = max(("k_inc_gemm_mix", "k_inc_gemm_flows"), key=lambda n: prof[n][0])
+    ms_g = prof[gemm][0] / max(1, prof[gemm][1])
+    fp32_peak = 152 * 128 * 2.07e9 / 1e12  # lane-instructions/s at the maximum SM clock (nominal)
+    ach = 12.0 * terms / (ms_g / 1e3) / 1e12
+    roof = {"kernel": gemm, "top_kernel": top, "bound": "fp32", "achieved": ach, "peak": fp32_peak,
+            "unit": "T FP32 lane-instructions/s", "frac": ach / fp32_peak,
+            "peak_kind": "nominal GB300 FP32 issue rate, 152 SMs x 128 lanes x 2.07 GHz (not measured)",
+            "fp64_equivalent_tflops": 2.0 * terms / (ms_g / 1e3) / 1e12, "traffic": None,
+            "instructions_per_launch": 12.0 * terms}
     h2d_setup = sum(inp[k].nbytes for k in ("srisk", "beta", "pop", "doy", "year", "pops", "dist")) + target.nbytes
     cpu = None
     if not args.no_cpu:

@@ -25,13 +25,22 @@
  * Layout in HBM: a plan keeps the aggregates resident — srisk, pop [T][G];
  * beta as [T][S][G] (strain-major per tick, so that the (t, s) rows of the
  * mixing product and every elementwise pass read G consecutive doubles);
- * u, exp(-r) and dL/du the same way; the network and its gradients [G][G].
+ * u, exp(-r) and dL/du the same way; log(dist) and the network and its
+ * gradients [G][G]; log(pops) [G].
  *
- * Everything is double precision.  The two contractions, u = beta N per
- * (t, s) row and dL/dN = beta^T dL/du, are (T S) x G x G products done by
- * one shared-memory tiled kernel; the rest is elementwise work and per-row
- * or per-tick reductions.  The sums use atomics, so results agree with a
- * sequential evaluation to rounding, not bit for bit.
+ * Arithmetic: double precision throughout, except inside the two
+ * contractions, u = beta N per (t, s) row and dL/dN = beta^T dL/du, both
+ * (T S) x G x G.  GB300 issues about two FP64 FMAs per clock per SM and 128
+ * FP32 FMAs, so the products run in double-float: their operands are held
+ * as FP32 pairs hi + lo (beta split once per plan, N and dL/du by the
+ * kernels that produce them), each term hi*hi is formed exactly (Dekker's
+ * product via FMA) with the cross terms, and the running sum is an FP32
+ * pair kept by Knuth's TwoSum — about 2^-44 relative per dot product,
+ * twelve FP32 operations per term and no FP64 work inside the products.
+ * The FP32 pair cannot hold magnitudes below 2^-126, so products of
+ * operands under about 1e-19 each lose relative (not absolute) accuracy.
+ * The sums use atomics, so results agree with a sequential FP64 evaluation
+ * to rounding, not bit for bit.
  */
 #include <cuda_runtime.h>
 
@@ -46,8 +55,12 @@ int lpg_ops_fail(int code, const char* fmt, ...);
 namespace {
 
 constexpr double kTwoPi = 6.283185307179586476925286766559;
-#define INC_TILE 32
 #define INC_THREADS 256
+#define DF_BM 32      /* product tile rows */
+#define DF_BN 64      /* product tile columns */
+#define DF_BK 32      /* product tile depth */
+#define DF_THREADS 128 /* 4 x 4 outputs per thread */
+#define DF_MAX_SPLIT 8 /* depth slices of the flows product */
 
 enum { PH_NETWORK, PH_MIX, PH_FORWARD, PH_BACKWARD, PH_FLOWS, PH_NETWORK_GRAD, PH_COUNT };
 const char* const kPhaseNames[PH_COUNT] = {"k_inc_network", "k_inc_gemm_mix", "k_inc_forward",
@@ -69,20 +82,58 @@ __device__ __forceinline__ double block_sum(double v, double* s_part) {
   return r;
 }
 
-/* One row i per CTA: the scaled gravity flows G[i,j] = k p_i^a p_j^b /
- * d_ij^c / P^c (zero diagonal), their sum rs[i], and the normalised row
- * N[i,j] (scaled down to max_frac when rs[i] exceeds it) with its sum. */
+/* An FP64 value as an FP32 pair hi + lo. */
+__device__ __forceinline__ float2 df_split(double x) {
+  const float hi = __double2float_rn(x);
+  return make_float2(hi, __double2float_rn(x - (double)hi));
+}
+
+__global__ void __launch_bounds__(INC_THREADS) k_inc_split(size_t n, const double* x, float2* y) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < n) y[idx] = df_split(x[idx]);
+}
+
+/* log(pops) [G] and log(dist) [G][G] (the diagonal is never read), once
+ * per plan.  Zero gives -inf. */
 __global__ void __launch_bounds__(INC_THREADS)
-    k_inc_network(int G, const double* pops, const double* dist, double k, double a, double b, double c, double Pc,
-                  double max_frac, double* Gm, double* N, double* rs, double* rsN, int* capped) {
+    k_inc_logs(int G, const double* pops, const double* dist, double* logp, double* logd) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < (size_t)G * G) logd[idx] = log(dist[idx]);
+  if (idx < (size_t)G) logp[idx] = log(pops[idx]);
+}
+
+/* Blocks [0, G): one network row i each — the scaled gravity flows
+ * G[i,j] = k p_i^a p_j^b / d_ij^c / P^c (zero diagonal; non-finite
+ * values are 0), formed as k p_i^a exp(b log p_j - c log d_ij) / P^c with
+ * the 0^0 = 1 convention kept, their sum rs[i], and the normalised row
+ * N[i,j] (scaled down to max_frac when rs[i] exceeds it; stored as FP32
+ * pairs for the mixing product) with its FP64 sum.
+ * Blocks [G, G + ceil(T/256)): the seasonal factor of each tick and its
+ * derivatives with respect to amp and peak. */
+__global__ void __launch_bounds__(INC_THREADS)
+    k_inc_network(int G, int T, const double* pops, const double* logp, const double* logd, double k, double a,
+                  double b, double c, double Pc, double max_frac, double* Gm, float2* N, double* rs, double* rsN,
+                  int* capped, const double* doy, const double* year, IncScalars sc, double* seas) {
   __shared__ double s_part[INC_THREADS];
+  if ((int)blockIdx.x >= G) {
+    const int t = (blockIdx.x - G) * INC_THREADS + threadIdx.x;
+    if (t < T) {
+      const double ang = kTwoPi * (doy[t] - sc.peak) / year[t];
+      const double ca = cos(ang);
+      seas[t] = 1.0 + sc.amp * ca;
+      seas[T + t] = ca;                                      /* d seas / d amp */
+      seas[2 * T + t] = sc.amp * sin(ang) * kTwoPi / year[t]; /* d seas / d peak */
+    }
+    return;
+  }
   const int i = blockIdx.x;
-  const double pa = pow(pops[i], a);
+  const double kpa = k * pow(pops[i], a) / Pc;
   double sum = 0.0;
   for (int j = threadIdx.x; j < G; j += blockDim.x) {
     double v = 0.0;
     if (j != i) {
-      v = k * pa * pow(pops[j], b) / pow(dist[(size_t)i * G + j], c) / Pc;
+      const double x = (b == 0.0 ? 0.0 : b * logp[j]) - (c == 0.0 ? 0.0 : c * logd[(size_t)i * G + j]);
+      v = kpa * exp(x);
       if (!isfinite(v)) v = 0.0;
     }
     Gm[(size_t)i * G + j] = v;
@@ -94,7 +145,7 @@ __global__ void __launch_bounds__(INC_THREADS)
   for (int j = threadIdx.x; j < G; j += blockDim.x) {
     const double v = Gm[(size_t)i * G + j]; /* written by this thread above */
     const double nv = cap ? v * (max_frac / r) : v;
-    N[(size_t)i * G + j] = nv;
+    N[(size_t)i * G + j] = df_split(nv);
     sumN += nv;
   }
   const double rn = block_sum(sumN, s_part);
@@ -105,72 +156,112 @@ __global__ void __launch_bounds__(INC_THREADS)
   }
 }
 
-/* C[M][N] = sum_k A(m, k) B[k][n], row-major, over 32 x 32 tiles staged in
- * shared memory; 256 threads, each with a 2 x 2 block of outputs (rows
- * ty, ty + 16; columns tx, tx + 16).  A(m, k) = A[m][k] (M x K) or, with
- * TRANS_A, A[k][m] (K x M).  The FP64 pipe bounds it (GB300 issues about
- * two FP64 FMAs per clock per SM; two shared loads per FMA are far inside
- * the shared-memory bandwidth). */
+/* (sh, sl) += a * b for FP32 pairs a, b: the exact product of the high
+ * parts (Dekker, by FMA) plus the cross terms, added by Knuth's TwoSum.
+ * The _rn intrinsics are never contracted or reassociated. */
+__device__ __forceinline__ void df_fma(float& sh, float& sl, float2 a, float2 b) {
+  const float ph = __fmul_rn(a.x, b.x);
+  float pl = __fmaf_rn(a.x, b.x, -ph);
+  pl = __fmaf_rn(a.x, b.y, pl);
+  pl = __fmaf_rn(a.y, b.x, pl);
+  const float s = __fadd_rn(sh, ph);
+  const float bp = __fsub_rn(s, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bp)), __fsub_rn(ph, bp));
+  sl = __fadd_rn(sl, __fadd_rn(err, pl));
+  sh = s;
+}
+
+/* C_z[M][N] = sum over k in slice z of A(m, k) B[k][n], row-major, in
+ * double-float, A and B given as FP32 pairs.  A(m, k) = A[m][k] (M x K) or, with TRANS_A, A[k][m]
+ * (K x M).  blockIdx.z picks the depth slice [z kchunk, (z+1) kchunk) and
+ * the output C + z M N.  32 x 64 tiles, 128 threads with 4 x 4 outputs
+ * each (rows ty + 8i, columns tx + 16j). */
 template <bool TRANS_A>
-__global__ void __launch_bounds__(INC_THREADS)
-    k_inc_gemm(int M, int N, int K, const double* __restrict__ A, const double* __restrict__ B, double* C) {
-  __shared__ double sA[INC_TILE][INC_TILE + 1]; /* [k][m] */
-  __shared__ double sB[INC_TILE][INC_TILE + 1]; /* [k][n] */
+__global__ void __launch_bounds__(DF_THREADS)
+    k_inc_gemm(int M, int N, int K, int kchunk, const float2* __restrict__ A, const float2* __restrict__ B,
+               double* C) {
+  __shared__ float2 sA[DF_BK][DF_BM + 1]; /* [k][m] */
+  __shared__ float2 sB[DF_BK][DF_BN];     /* [k][n] */
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int m0 = blockIdx.y * INC_TILE, n0 = blockIdx.x * INC_TILE;
-  double c00 = 0.0, c01 = 0.0, c10 = 0.0, c11 = 0.0;
-  for (int k0 = 0; k0 < K; k0 += INC_TILE) {
+  const int m0 = blockIdx.y * DF_BM, n0 = blockIdx.x * DF_BN;
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+  float sh[4][4], sl[4][4];
 #pragma unroll
-    for (int r = 0; r < (INC_TILE * INC_TILE) / INC_THREADS; ++r) {
-      const int e = tid + r * INC_THREADS;
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) sh[i][j] = sl[i][j] = 0.f;
+  for (int k0 = kb; k0 < ke; k0 += DF_BK) {
+#pragma unroll
+    for (int r = 0; r < (DF_BK * DF_BM) / DF_THREADS; ++r) {
+      const int e = tid + r * DF_THREADS;
       const int hi = e >> 5, lo = e & 31;
-      double va = 0.0;
+      float2 v = make_float2(0.f, 0.f);
       if (TRANS_A) { /* hi = k, lo = m: consecutive threads read consecutive m */
-        if (k0 + hi < K && m0 + lo < M) va = A[(size_t)(k0 + hi) * M + m0 + lo];
-        sA[hi][lo] = va;
+        if (k0 + hi < ke && m0 + lo < M) v = A[(size_t)(k0 + hi) * M + m0 + lo];
+        sA[hi][lo] = v;
       } else { /* hi = m, lo = k: consecutive threads read consecutive k */
-        if (m0 + hi < M && k0 + lo < K) va = A[(size_t)(m0 + hi) * K + k0 + lo];
-        sA[lo][hi] = va;
+        if (m0 + hi < M && k0 + lo < ke) v = A[(size_t)(m0 + hi) * K + k0 + lo];
+        sA[lo][hi] = v;
       }
-      double vb = 0.0;
-      if (k0 + hi < K && n0 + lo < N) vb = B[(size_t)(k0 + hi) * N + n0 + lo];
-      sB[hi][lo] = vb;
+    }
+#pragma unroll
+    for (int r = 0; r < (DF_BK * DF_BN) / DF_THREADS; ++r) {
+      const int e = tid + r * DF_THREADS;
+      const int hi = e >> 6, lo = e & 63;
+      float2 v = make_float2(0.f, 0.f);
+      if (k0 + hi < ke && n0 + lo < N) v = B[(size_t)(k0 + hi) * N + n0 + lo];
+      sB[hi][lo] = v;
     }
     __syncthreads();
-#pragma unroll 8
-    for (int q = 0; q < INC_TILE; ++q) {
-      const double a0 = sA[q][ty], a1 = sA[q][ty + 16];
-      const double b0 = sB[q][tx], b1 = sB[q][tx + 16];
-      c00 = fma(a0, b0, c00); /* fused even under --fmad=false */
-      c01 = fma(a0, b1, c01);
-      c10 = fma(a1, b0, c10);
-      c11 = fma(a1, b1, c11);
+#pragma unroll 4
+    for (int q = 0; q < DF_BK; ++q) {
+      float2 av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = sA[q][ty + 8 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = sB[q][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) df_fma(sh[i][j], sl[i][j], av[i], bv[j]);
     }
+    /* renormalise each pair (Fast2Sum: |sh| >= |sl|) so that sl stays small */
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float t = __fadd_rn(sh[i][j], sl[i][j]);
+        sl[i][j] = __fsub_rn(sl[i][j], __fsub_rn(t, sh[i][j]));
+        sh[i][j] = t;
+      }
     __syncthreads();
   }
-  const int r0 = m0 + ty, r1 = m0 + ty + 16, q0 = n0 + tx, q1 = n0 + tx + 16;
-  if (r0 < M && q0 < N) C[(size_t)r0 * N + q0] = c00;
-  if (r0 < M && q1 < N) C[(size_t)r0 * N + q1] = c01;
-  if (r1 < M && q0 < N) C[(size_t)r1 * N + q0] = c10;
-  if (r1 < M && q1 < N) C[(size_t)r1 * N + q1] = c11;
+  double* Cz = C + (size_t)blockIdx.z * M * N;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int row = m0 + ty + 8 * i;
+    if (row >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int col = n0 + tx + 16 * j;
+      if (col < N) Cz[(size_t)row * N + col] = (double)sh[i][j] + (double)sl[i][j];
+    }
+  }
 }
 
-__device__ __forceinline__ double seasonal(const double* doy, const double* year, int t, const IncScalars& sc) {
-  return 1.0 + sc.amp * cos(kTwoPi * (doy[t] - sc.peak) / year[t]);
-}
-
-/* Per (t, n): the mixing's diagonal term, the rates, exp(-r) kept for the
- * reverse pass, lam, and with a target the loss term and dL/dlam. */
+/* Per (t, n), one tick per blockIdx.y: the mixing's diagonal term, the
+ * rates, exp(-r) kept for the reverse pass, lam, and with a target the
+ * loss term and dL/dlam. */
 __global__ void __launch_bounds__(INC_THREADS)
-    k_inc_forward(int T, int G, int S, const double* srisk, const double* beta, const double* pop, const double* doy,
-                  const double* year, const double* r0s, const double* rsN, IncScalars sc, double* u, double* e,
+    k_inc_forward(int T, int G, int S, const double* srisk, const double* beta, const double* pop,
+                  const double* seas, const double* r0s, const double* rsN, IncScalars sc, double* u, double* e,
                   double* lam, const double* target, double* g, double* loss) {
   __shared__ double s_part[INC_THREADS];
-  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y, n = blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t idx = (size_t)t * G + n;
   double part = 0.0;
-  if (idx < (size_t)T * G) {
-    const int t = (int)(idx / G), n = (int)(idx % G);
-    const double q = seasonal(doy, year, t, sc) * r0s[n] * sc.R / fmax(pop[idx], 1.0);
+  if (n < G) {
+    const double q = seas[t] * r0s[n] * sc.R / fmax(pop[idx], 1.0);
     double l = 0.0;
     for (int s = 0; s < S; ++s) {
       const size_t k = ((size_t)t * S + s) * G + n;
@@ -194,45 +285,49 @@ __global__ void __launch_bounds__(INC_THREADS)
   }
 }
 
-/* Per (t, n) of the reverse pass: dL/du (kept for the dL/dN product) and
- * the contributions to dL/dseas[t], dL/dr0s[n] and dL/dR. */
+/* Per (t, n) of the reverse pass, one tick per blockIdx.y: dL/du (as FP32
+ * pairs for the dL/dN product) and the contributions to dL/dseas[t],
+ * dL/dr0s[n] and dL/dR (block sums for the per-tick and scalar ones). */
 __global__ void __launch_bounds__(INC_THREADS)
-    k_inc_backward(int T, int G, int S, const double* g, const double* srisk, const double* pop, const double* doy,
-                   const double* year, const double* r0s, IncScalars sc, const double* u, const double* e,
-                   double* gu, double* g_seas, double* g_r0s, double* g_R) {
+    k_inc_backward(int T, int G, int S, const double* g, const double* srisk, const double* pop, const double* seas,
+                   const double* r0s, IncScalars sc, const double* u, const double* e, float2* gu, double* g_seas,
+                   double* g_r0s, double* g_R) {
   __shared__ double s_part[INC_THREADS];
-  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double cR = 0.0;
-  if (idx < (size_t)T * G) {
-    const int t = (int)(idx / G), n = (int)(idx % G);
-    const double seas = seasonal(doy, year, t, sc);
+  const int t = blockIdx.y, n = blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t idx = (size_t)t * G + n;
+  double cR = 0.0, cS = 0.0;
+  if (n < G) {
+    const double st = seas[t];
     const double popc = fmax(pop[idx], 1.0);
-    const double q = seas * r0s[n] * sc.R / popc;
+    const double q = st * r0s[n] * sc.R / popc;
     const double gs = g[idx] * srisk[idx];
     double gq = 0.0;
     for (int s = 0; s < S; ++s) {
       const size_t k = ((size_t)t * S + s) * G + n;
       const double gr = gs * e[k];
-      gu[k] = gr * q;
+      gu[k] = df_split(gr * q);
       gq += gr * u[k];
     }
-    atomicAdd(&g_seas[t], gq * r0s[n] * sc.R / popc);
-    atomicAdd(&g_r0s[n], gq * seas * sc.R / popc);
-    cR = gq * seas * r0s[n] / popc;
+    cS = gq * r0s[n] * sc.R / popc;
+    atomicAdd(&g_r0s[n], gq * st * sc.R / popc);
+    cR = gq * st * r0s[n] / popc;
   }
-  const double tot = block_sum(cR, s_part);
-  if (threadIdx.x == 0) atomicAdd(g_R, tot);
+  const double tS = block_sum(cS, s_part);
+  const double tR = block_sum(cR, s_part);
+  if (threadIdx.x == 0) {
+    atomicAdd(&g_seas[t], tS);
+    atomicAdd(g_R, tR);
+  }
 }
 
 /* dL/damp and dL/dpeak from dL/dseas[t] (one CTA). */
 __global__ void __launch_bounds__(INC_THREADS)
-    k_inc_seasonal(int T, const double* doy, const double* year, const double* g_seas, IncScalars sc, double* out) {
+    k_inc_seasonal(int T, const double* seas, const double* g_seas, double* out) {
   __shared__ double s_part[INC_THREADS];
   double ga = 0.0, gp = 0.0;
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
-    const double ang = kTwoPi * (doy[t] - sc.peak) / year[t];
-    ga += g_seas[t] * cos(ang);
-    gp += g_seas[t] * sc.amp * sin(ang) * kTwoPi / year[t];
+    ga += g_seas[t] * seas[T + t];
+    gp += g_seas[t] * seas[2 * T + t];
   }
   ga = block_sum(ga, s_part);
   gp = block_sum(gp, s_part);
@@ -242,37 +337,42 @@ __global__ void __launch_bounds__(INC_THREADS)
   }
 }
 
-/* One row a per CTA: dL/dN[a][b] = C[a][b] - C[a][a] (zero on the
- * diagonal), then dL/dG through the row normalisation and the row's
- * contributions to dL/dk, dL/da, dL/db, dL/dc. */
+/* One row a per CTA: C[a][b] = the sum of the flows product's nsplit
+ * depth slices, dL/dN[a][b] = C[a][b] - C[a][a] (zero on the diagonal),
+ * then dL/dG through the row normalisation and the row's contributions to
+ * dL/dk, dL/da, dL/db, dL/dc. */
 __global__ void __launch_bounds__(INC_THREADS)
-    k_inc_network_grad(int G, const double* C, const double* Gm, const double* rs, const int* capped,
-                       const double* pops, const double* dist, double k, double logP, double max_frac, double* gN,
+    k_inc_network_grad(int G, int nsplit, const double* C, const double* Gm, const double* rs, const int* capped,
+                       const double* logp, const double* logd, double k, double logP, double max_frac, double* gN,
                        double* g_theta) {
   __shared__ double s_part[INC_THREADS];
   const int a = blockIdx.x;
-  const double diag = C[(size_t)a * G + a];
+  const size_t GG = (size_t)G * G, row = (size_t)a * G;
+  double diag = 0.0;
+  for (int z = 0; z < nsplit; ++z) diag += C[z * GG + row + a];
   double cpl = 0.0; /* the row's sum of dL/dN * G (the normalisation's coupling term) */
   for (int b = threadIdx.x; b < G; b += blockDim.x) {
-    const double v = b == a ? 0.0 : C[(size_t)a * G + b] - diag;
-    gN[(size_t)a * G + b] = v;
-    cpl += v * Gm[(size_t)a * G + b];
+    double cab = 0.0;
+    for (int z = 0; z < nsplit; ++z) cab += C[z * GG + row + b];
+    const double v = b == a ? 0.0 : cab - diag;
+    gN[row + b] = v;
+    cpl += v * Gm[row + b];
   }
   const double coupling = block_sum(cpl, s_part);
   const bool cap = capped[a] != 0;
   const double ra = rs[a];
-  const double lpa = log(pops[a]);
+  const double lpa = logp[a];
   double wk = 0.0, wa = 0.0, wb = 0.0, wc = 0.0;
   for (int b = threadIdx.x; b < G; b += blockDim.x) {
     if (b == a) continue;
-    const double gn = gN[(size_t)a * G + b]; /* written by this thread above */
+    const double gn = gN[row + b]; /* written by this thread above */
     const double gg = cap ? (max_frac / ra) * (gn - coupling / ra) : gn;
-    const double w = gg * Gm[(size_t)a * G + b];
+    const double w = gg * Gm[row + b];
     if (w == 0.0) continue; /* a zero flow: its logs may be infinite */
     wk += w;
     wa += w * lpa;
-    wb += w * log(pops[b]);
-    wc += w * (-log(dist[(size_t)a * G + b]) - logP);
+    wb += w * logp[b];
+    wc += w * (-logd[row + b] - logP);
   }
   wk = block_sum(wk, s_part);
   wa = block_sum(wa, s_part);
@@ -290,16 +390,18 @@ __global__ void __launch_bounds__(INC_THREADS)
 
 struct lpg_incidence_plan {
   int T = 0, G = 0, S = 0;
+  int nsm = 0;
   cudaStream_t st = nullptr;
   bool own_stream = false;
   double P = 0.0, logP = 0.0;
   /* resident inputs */
   double *srisk = nullptr, *beta = nullptr, *pop = nullptr, *doy = nullptr, *year = nullptr, *pops = nullptr,
-         *dist = nullptr, *target = nullptr;
+         *logp = nullptr, *logd = nullptr, *target = nullptr;
   /* per evaluation */
-  double *r0s = nullptr, *Gm = nullptr, *N = nullptr, *rs = nullptr, *rsN = nullptr, *u = nullptr, *e = nullptr,
-         *lam = nullptr, *g = nullptr, *gu = nullptr, *gseas = nullptr, *gr0s = nullptr, *scal = nullptr,
+  double *r0s = nullptr, *seas = nullptr, *Gm = nullptr, *rs = nullptr, *rsN = nullptr, *u = nullptr,
+         *e = nullptr, *lam = nullptr, *g = nullptr, *gseas = nullptr, *gr0s = nullptr, *scal = nullptr,
          *C = nullptr, *gN = nullptr;
+  float2 *beta_hl = nullptr, *N = nullptr, *gu = nullptr; /* the products' operands as FP32 pairs */
   int* cap = nullptr;
   double* h_scal = nullptr; /* pinned: [0] loss, [1] R, [2] amp, [3] peak, [4..7] k, a, b, c */
   /* profiling */
@@ -315,10 +417,10 @@ int plan_cuda(cudaError_t e, const char* what) {
   return e == cudaSuccess ? LPG_OK : lpg_ops_fail(LPG_ERR_CUDA, "incidence plan: %s: %s", what, cudaGetErrorString(e));
 }
 
-#define PCK(call)                                \
-  do {                                           \
-    const int rc_ = plan_cuda((call), #call);    \
-    if (rc_ != LPG_OK) return rc_;               \
+#define PCK(call)                             \
+  do {                                        \
+    const int rc_ = plan_cuda((call), #call); \
+    if (rc_ != LPG_OK) return rc_;            \
   } while (0)
 
 template <typename T>
@@ -331,9 +433,9 @@ int dalloc(T** p, size_t n) {
 }
 
 void plan_free(lpg_incidence_plan* p) {
-  void* ps[] = {p->srisk, p->beta, p->pop,   p->doy,   p->year, p->pops, p->dist, p->target, p->r0s, p->Gm,
-                p->N,     p->rs,   p->rsN,   p->u,     p->e,    p->lam,  p->g,    p->gu,     p->gseas, p->gr0s,
-                p->scal,  p->C,    p->gN,    p->cap};
+  void* ps[] = {p->srisk, p->beta, p->pop, p->doy, p->year,  p->pops, p->logp, p->logd, p->target,
+                p->r0s,   p->seas, p->Gm,  p->N,   p->rs,    p->rsN,  p->u,    p->e,    p->lam,
+                p->g,     p->gu,   p->gseas, p->gr0s, p->scal, p->C,   p->gN,   p->cap,  p->beta_hl};
   for (void* q : ps)
     if (q) cudaFree(q);
   if (p->h_scal) cudaFreeHost(p->h_scal);
@@ -348,12 +450,14 @@ int plan_alloc(lpg_incidence_plan* p) {
   int rc;
   if ((rc = dalloc(&p->srisk, TG)) || (rc = dalloc(&p->beta, TSG)) || (rc = dalloc(&p->pop, TG)) ||
       (rc = dalloc(&p->doy, T)) || (rc = dalloc(&p->year, T)) || (rc = dalloc(&p->pops, G)) ||
-      (rc = dalloc(&p->dist, GG)) || (rc = dalloc(&p->r0s, G)) || (rc = dalloc(&p->Gm, GG)) ||
-      (rc = dalloc(&p->N, GG)) || (rc = dalloc(&p->rs, G)) || (rc = dalloc(&p->rsN, G)) ||
-      (rc = dalloc(&p->cap, G)) || (rc = dalloc(&p->u, TSG)) || (rc = dalloc(&p->e, TSG)) ||
-      (rc = dalloc(&p->lam, TG)) || (rc = dalloc(&p->g, TG)) || (rc = dalloc(&p->gu, TSG)) ||
-      (rc = dalloc(&p->gseas, T)) || (rc = dalloc(&p->gr0s, G)) || (rc = dalloc(&p->scal, 8)) ||
-      (rc = dalloc(&p->C, GG)) || (rc = dalloc(&p->gN, GG)))
+      (rc = dalloc(&p->logp, G)) || (rc = dalloc(&p->logd, GG)) || (rc = dalloc(&p->r0s, G)) ||
+      (rc = dalloc(&p->seas, 3 * T)) || (rc = dalloc(&p->Gm, GG)) || (rc = dalloc(&p->N, GG)) ||
+      (rc = dalloc(&p->beta_hl, TSG)) ||
+      (rc = dalloc(&p->rs, G)) || (rc = dalloc(&p->rsN, G)) || (rc = dalloc(&p->cap, G)) ||
+      (rc = dalloc(&p->u, TSG)) || (rc = dalloc(&p->e, TSG)) || (rc = dalloc(&p->lam, TG)) ||
+      (rc = dalloc(&p->g, TG)) || (rc = dalloc(&p->gu, TSG)) || (rc = dalloc(&p->gseas, T)) ||
+      (rc = dalloc(&p->gr0s, G)) || (rc = dalloc(&p->scal, 8)) || (rc = dalloc(&p->C, DF_MAX_SPLIT * GG)) ||
+      (rc = dalloc(&p->gN, GG)))
     return rc;
   PCK(cudaMallocHost((void**)&p->h_scal, 8 * sizeof(double)));
   for (auto& ev : p->ev) PCK(cudaEventCreate(&ev));
@@ -368,39 +472,42 @@ inline void mark(lpg_incidence_plan* p, int ph, int n_launch) {
 
 int plan_forward(lpg_incidence_plan* p, const lpg_incidence_params* prm, IncScalars sc, bool with_loss) {
   const int T = p->T, G = p->G, S = p->S;
-  const size_t TG = (size_t)T * G;
   const double Pc = pow(p->P, prm->c);
   mark(p, PH_NETWORK, 1);
-  k_inc_network<<<G, INC_THREADS, 0, p->st>>>(G, p->pops, p->dist, prm->k, prm->a, prm->b, prm->c, Pc,
-                                              prm->max_frac, p->Gm, p->N, p->rs, p->rsN, p->cap);
+  k_inc_network<<<G + (T + INC_THREADS - 1) / INC_THREADS, INC_THREADS, 0, p->st>>>(
+      G, T, p->pops, p->logp, p->logd, prm->k, prm->a, prm->b, prm->c, Pc, prm->max_frac, p->Gm, p->N, p->rs,
+      p->rsN, p->cap, p->doy, p->year, sc, p->seas);
   mark(p, PH_MIX, 1);
   {
-    const dim3 grd((G + INC_TILE - 1) / INC_TILE, (T * S + INC_TILE - 1) / INC_TILE);
-    k_inc_gemm<false><<<grd, INC_THREADS, 0, p->st>>>(T * S, G, G, p->beta, p->N, p->u);
+    const dim3 grd((G + DF_BN - 1) / DF_BN, (T * S + DF_BM - 1) / DF_BM, 1);
+    k_inc_gemm<false><<<grd, DF_THREADS, 0, p->st>>>(T * S, G, G, G, p->beta_hl, p->N, p->u);
   }
   mark(p, PH_FORWARD, 1);
-  k_inc_forward<<<(unsigned)((TG + INC_THREADS - 1) / INC_THREADS), INC_THREADS, 0, p->st>>>(
-      T, G, S, p->srisk, p->beta, p->pop, p->doy, p->year, p->r0s, p->rsN, sc, p->u, p->e, p->lam,
+  k_inc_forward<<<dim3((G + INC_THREADS - 1) / INC_THREADS, T), INC_THREADS, 0, p->st>>>(
+      T, G, S, p->srisk, p->beta, p->pop, p->seas, p->r0s, p->rsN, sc, p->u, p->e, p->lam,
       with_loss ? p->target : nullptr, p->g, p->scal);
   return plan_cuda(cudaGetLastError(), "forward launch");
 }
 
 int plan_backward(lpg_incidence_plan* p, const lpg_incidence_params* prm, IncScalars sc) {
   const int T = p->T, G = p->G, S = p->S;
-  const size_t TG = (size_t)T * G;
   mark(p, PH_BACKWARD, 2);
-  k_inc_backward<<<(unsigned)((TG + INC_THREADS - 1) / INC_THREADS), INC_THREADS, 0, p->st>>>(
-      T, G, S, p->g, p->srisk, p->pop, p->doy, p->year, p->r0s, sc, p->u, p->e, p->gu, p->gseas, p->gr0s,
-      p->scal + 1);
-  k_inc_seasonal<<<1, INC_THREADS, 0, p->st>>>(T, p->doy, p->year, p->gseas, sc, p->scal + 2);
+  k_inc_backward<<<dim3((G + INC_THREADS - 1) / INC_THREADS, T), INC_THREADS, 0, p->st>>>(
+      T, G, S, p->g, p->srisk, p->pop, p->seas, p->r0s, sc, p->u, p->e, p->gu, p->gseas, p->gr0s, p->scal + 1);
+  k_inc_seasonal<<<1, INC_THREADS, 0, p->st>>>(T, p->seas, p->gseas, p->scal + 2);
   mark(p, PH_FLOWS, 1);
-  {
-    const dim3 grd((G + INC_TILE - 1) / INC_TILE, (G + INC_TILE - 1) / INC_TILE);
-    k_inc_gemm<true><<<grd, INC_THREADS, 0, p->st>>>(G, G, T * S, p->beta, p->gu, p->C);
-  }
+  /* depth slices so that the G x G output fills the SMs about four deep */
+  const int K = T * S, gx = (G + DF_BN - 1) / DF_BN, gy = (G + DF_BM - 1) / DF_BM;
+  const int ktiles = (K + DF_BK - 1) / DF_BK;
+  int split = (4 * p->nsm + gx * gy - 1) / (gx * gy);
+  split = split < 1 ? 1 : split > DF_MAX_SPLIT ? DF_MAX_SPLIT : split;
+  if (split > ktiles) split = ktiles;
+  const int kchunk = ((ktiles + split - 1) / split) * DF_BK;
+  const int nsplit = (K + kchunk - 1) / kchunk;
+  k_inc_gemm<true><<<dim3(gx, gy, nsplit), DF_THREADS, 0, p->st>>>(G, G, K, kchunk, p->beta_hl, p->gu, p->C);
   mark(p, PH_NETWORK_GRAD, 1);
-  k_inc_network_grad<<<G, INC_THREADS, 0, p->st>>>(G, p->C, p->Gm, p->rs, p->cap, p->pops, p->dist, prm->k,
-                                                   p->logP, prm->max_frac, p->gN, p->scal + 4);
+  k_inc_network_grad<<<G, INC_THREADS, 0, p->st>>>(G, nsplit, p->C, p->Gm, p->rs, p->cap, p->logp, p->logd,
+                                                   prm->k, p->logP, prm->max_frac, p->gN, p->scal + 4);
   return plan_cuda(cudaGetLastError(), "backward launch");
 }
 
@@ -413,8 +520,9 @@ extern "C" int lpg_incidence_plan_create(const lpg_incidence_in* in, const doubl
   const int T = in->T, G = in->G, S = in->S;
   if (T <= 0 || G <= 0 || S <= 0 || S > LPG_MAX_STRAINS)
     return lpg_ops_fail(LPG_ERR_ARG, "incidence plan: bad sizes T=%d G=%d S=%d", T, G, S);
-  if ((int64_t)T * S > 65535LL * INC_TILE)
-    return lpg_ops_fail(LPG_ERR_ARG, "incidence plan: T*S = %lld above %d", (long long)T * S, 65535 * INC_TILE);
+  if ((int64_t)T * S > 65535LL * DF_BM || T > 65535)
+    return lpg_ops_fail(LPG_ERR_ARG, "incidence plan: T=%d or T*S = %lld too large (T <= 65535, T*S <= %d)", T,
+                        (long long)T * S, 65535 * DF_BM);
   if (!in->srisk || !in->beta || !in->pop || !in->doy || !in->year || !in->pops || !in->dist)
     return lpg_ops_fail(LPG_ERR_ARG, "incidence plan: null input array");
   double P = 0.0;
@@ -423,6 +531,9 @@ extern "C" int lpg_incidence_plan_create(const lpg_incidence_in* in, const doubl
     P += in->pops[i];
   }
   if (!(P > 0.0) || !std::isfinite(P)) return lpg_ops_fail(LPG_ERR_ARG, "incidence plan: total population %g", P);
+  for (size_t i = 0; i < (size_t)G * G; ++i)
+    if ((int)(i / G) != (int)(i % G) && !(in->dist[i] >= 0.0))
+      return lpg_ops_fail(LPG_ERR_ARG, "incidence plan: dist[%zu][%zu] is negative", i / G, i % G);
   lpg_incidence_plan* p = new lpg_incidence_plan;
   p->T = T;
   p->G = G;
@@ -430,13 +541,20 @@ extern "C" int lpg_incidence_plan_create(const lpg_incidence_in* in, const doubl
   p->P = P;
   p->logP = log(P);
   int rc = LPG_OK;
-  if (stream) {
-    p->st = (cudaStream_t)stream;
-  } else {
-    rc = plan_cuda(cudaStreamCreateWithFlags(&p->st, cudaStreamNonBlocking), "stream");
-    p->own_stream = rc == LPG_OK;
+  int dev = 0;
+  rc = plan_cuda(cudaGetDevice(&dev), "device");
+  if (rc == LPG_OK) rc = plan_cuda(cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  if (rc == LPG_OK) {
+    if (stream) {
+      p->st = (cudaStream_t)stream;
+    } else {
+      rc = plan_cuda(cudaStreamCreateWithFlags(&p->st, cudaStreamNonBlocking), "stream");
+      p->own_stream = rc == LPG_OK;
+    }
   }
   if (rc == LPG_OK) rc = plan_alloc(p);
+  double* d_dist = nullptr;
+  if (rc == LPG_OK) rc = dalloc(&d_dist, (size_t)G * G);
   if (rc == LPG_OK) {
     const size_t TG = (size_t)T * G, GG = (size_t)G * G;
     std::vector<double> bt(TG * S); /* [T][G][S] -> [T][S][G] */
@@ -447,11 +565,19 @@ extern "C" int lpg_incidence_plan_create(const lpg_incidence_in* in, const doubl
       double* dst;
       const double* src;
       size_t n;
-    } up[] = {{p->srisk, in->srisk, TG}, {p->beta, bt.data(), TG * S}, {p->pop, in->pop, TG}, {p->doy, in->doy, (size_t)T},
-              {p->year, in->year, (size_t)T}, {p->pops, in->pops, (size_t)G}, {p->dist, in->dist, GG}};
+    } up[] = {{p->srisk, in->srisk, TG},       {p->beta, bt.data(), TG * S},        {p->pop, in->pop, TG},
+              {p->doy, in->doy, (size_t)T},    {p->year, in->year, (size_t)T},      {p->pops, in->pops, (size_t)G},
+              {d_dist, in->dist, GG}};
     for (auto& c : up) {
       rc = plan_cuda(cudaMemcpyAsync(c.dst, c.src, sizeof(double) * c.n, cudaMemcpyHostToDevice, p->st), "upload");
       if (rc != LPG_OK) break;
+    }
+    if (rc == LPG_OK) {
+      k_inc_logs<<<(unsigned)((GG + INC_THREADS - 1) / INC_THREADS), INC_THREADS, 0, p->st>>>(G, p->pops, d_dist,
+                                                                                             p->logp, p->logd);
+      k_inc_split<<<(unsigned)((TG * S + INC_THREADS - 1) / INC_THREADS), INC_THREADS, 0, p->st>>>(TG * S, p->beta,
+                                                                                                 p->beta_hl);
+      rc = plan_cuda(cudaGetLastError(), "log launch");
     }
     if (rc == LPG_OK && target) {
       rc = dalloc(&p->target, TG);
@@ -461,6 +587,7 @@ extern "C" int lpg_incidence_plan_create(const lpg_incidence_in* in, const doubl
     }
     if (rc == LPG_OK) rc = plan_cuda(cudaStreamSynchronize(p->st), "upload sync");
   }
+  if (d_dist) cudaFree(d_dist);
   if (rc != LPG_OK) {
     plan_free(p);
     return rc;
@@ -478,10 +605,10 @@ extern "C" int lpg_incidence_plan_eval(lpg_incidence_plan* p, const lpg_incidenc
   const int T = p->T, G = p->G;
   const size_t TG = (size_t)T * G, GG = (size_t)G * G;
   const IncScalars sc{prm->R, prm->amp, prm->peak};
-  const bool with_loss = p->target != nullptr && !g_lam;
+  const bool with_loss = p->target != nullptr && (!g_lam || loss_out);
   PCK(cudaMemcpyAsync(p->r0s, prm->r0s, sizeof(double) * G, cudaMemcpyHostToDevice, p->st));
   PCK(cudaMemsetAsync(p->scal, 0, sizeof(double) * 8, p->st));
-  int rc = plan_forward(p, prm, sc, with_loss || (p->target && loss_out));
+  int rc = plan_forward(p, prm, sc, with_loss);
   if (rc != LPG_OK) return rc;
   if (grad) {
     if (g_lam) PCK(cudaMemcpyAsync(p->g, g_lam, sizeof(double) * TG, cudaMemcpyHostToDevice, p->st));
