@@ -231,6 +231,18 @@ int lpg_get_state(lpg_handle* h, int32_t sim, lpg_sim_state* out);
 /* Copy results of `sim` into caller arrays (sim.results.*). */
 int lpg_read_results(lpg_handle* h, int32_t sim, const lpg_results_view* out);
 
+/* Record, on every tick the transmission step runs, each node's inputs of
+ * the expected-incidence map (lpg_incidence_plan_create) and the engine's own
+ * expected new exposures; call before lpg_start.  No counterpart in the
+ * reference.  The values are those of model.py:1315-1363 on that tick:
+ * srisk = exposure_by_node (the susceptibles' summed acquisition risk),
+ * beta = beta_by_node_strain before mixing, pop = results.pop[t], and
+ * lam = expected_exposures_per_node. */
+int lpg_record_aggregates(lpg_handle* h, int32_t sim, int32_t enable);
+/* srisk, pop, lam [nt][n_nodes] and beta [nt][n_nodes][n_strains] (host;
+ * any may be NULL).  Rows of ticks on which transmission did not run are 0. */
+int lpg_read_aggregates(lpg_handle* h, int32_t sim, double* srisk, double* beta, double* pop, double* lam);
+
 /* Copy the current agent columns of `sim` back in reference slot order
  * (slots [0, count) are written; slots past count are left untouched). */
 int lpg_read_columns(lpg_handle* h, int32_t sim, const lpg_columns* out);

@@ -27,6 +27,8 @@ SIGNATURES = {
     "lpg_get_state": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(_abi.lpg_sim_state)]),
     "lpg_read_results": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(_abi.lpg_results_view)]),
     "lpg_read_columns": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(_abi.lpg_columns)]),
+    "lpg_record_aggregates": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "lpg_read_aggregates": (C.c_int, [C.c_void_p, C.c_int32] + [C.POINTER(C.c_double)] * 4),
     "lpg_check_invariants": (C.c_int, [C.c_void_p]),
     "lpg_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
     "lpg_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
@@ -128,6 +130,23 @@ class Handle:
 
     def read_columns(self, sim: int, cols: dict):
         self._check(self.lib.lpg_read_columns(self.h, sim, C.byref(_abi.make_columns(cols))))
+
+    def record_aggregates(self, sim: int, on: bool = True):
+        """Record the expected-incidence map's inputs on every transmission
+        tick (lpg_record_aggregates); before start()."""
+        self._check(self.lib.lpg_record_aggregates(self.h, sim, int(bool(on))))
+
+    def read_aggregates(self, sim: int, nt: int, n_nodes: int, n_strains: int) -> dict:
+        """srisk, pop, lam [nt, n_nodes] and beta [nt, n_nodes, n_strains] as
+        recorded (lpg_read_aggregates); zero rows where transmission did not run."""
+        import numpy as np
+
+        out = {"srisk": np.zeros((nt, n_nodes)), "beta": np.zeros((nt, n_nodes, n_strains)),
+               "pop": np.zeros((nt, n_nodes)), "lam": np.zeros((nt, n_nodes))}
+        dp = C.POINTER(C.c_double)
+        self._check(self.lib.lpg_read_aggregates(self.h, sim, *[_abi.ptr(out[k], dp)
+                                                               for k in ("srisk", "beta", "pop", "lam")]))
+        return out
 
     def check_invariants(self):
         self._check(self.lib.lpg_check_invariants(self.h))

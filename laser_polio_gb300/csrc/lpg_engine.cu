@@ -66,6 +66,7 @@ struct SimHost {
   std::vector<int32_t> pop0, Rpre;
   Staging stg;
   int64_t res_elems = 0;
+  bool record = false; /* lpg_record_aggregates */
 };
 
 }  // namespace
@@ -745,6 +746,11 @@ extern "C" int lpg_start(lpg_handle* h) {
     CK(cudaMemcpyAsync(rp.res + rp.res_off[RS_POP], s.pop0.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
     if (!s.Rpre.empty())
       CK(cudaMemcpyAsync(rp.res + rp.res_off[RS_R], s.Rpre.data(), sizeof(int32_t) * s.Rpre.size(), cudaMemcpyHostToDevice, st));
+    if (s.record) {
+      const size_t nrec = (size_t)d.nt * n * (3 + d.n_strains);
+      if (dalloc(h, &rp.rec, nrec)) return LPG_ERR_NOMEM;
+      CK(cudaMemsetAsync(rp.rec, 0, sizeof(double) * nrec, st));
+    }
     /* unborn pool: reference slots [count, capacity) */
     const int64_t np = std::max<int64_t>(d.capacity - d.count, 1);
     rc = 0;
@@ -1053,6 +1059,38 @@ extern "C" int lpg_read_results(lpg_handle* h, int32_t sim, const lpg_results_vi
     if (!outs[k]) continue;
     size_t n = (size_t)d.nt * d.n_nodes * (res_wide[k] ? d.n_strains : 1);
     CK(cudaMemcpy(outs[k], r.res + r.res_off[k], n * sizeof(int32_t), cudaMemcpyDefault));
+  }
+  return LPG_OK;
+}
+
+extern "C" int lpg_record_aggregates(lpg_handle* h, int32_t sim, int32_t enable) {
+  if (!h || sim < 0 || sim >= (int)h->sims.size()) return LPG_ERR_ARG;
+  if (h->started) return fail(h, LPG_ERR_STATE, "lpg_record_aggregates after lpg_start");
+  h->sims[sim].record = enable != 0;
+  return LPG_OK;
+}
+
+extern "C" int lpg_read_aggregates(lpg_handle* h, int32_t sim, double* srisk, double* beta, double* pop,
+                                   double* lam) {
+  if (!h || sim < 0 || sim >= (int)h->sims.size()) return LPG_ERR_ARG;
+  if (!h->started) return fail(h, LPG_ERR_STATE, "no aggregates before lpg_start");
+  if (!h->sims[sim].record) return fail(h, LPG_ERR_STATE, "simulation %d does not record aggregates", sim);
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  DevRep r;
+  CK(cudaMemcpy(&r, h->W.reps + sim, sizeof(DevRep), cudaMemcpyDeviceToHost));
+  const lpg_sim_desc& d = h->sims[sim].d;
+  const int w = 3 + d.n_strains;
+  const size_t rows = (size_t)d.nt * d.n_nodes;
+  std::vector<double> buf(rows * w);
+  CK(cudaMemcpy(buf.data(), r.rec, sizeof(double) * buf.size(), cudaMemcpyDeviceToHost));
+  for (size_t q = 0; q < rows; ++q) {
+    const double* b = buf.data() + q * w;
+    if (srisk) srisk[q] = b[0];
+    if (pop) pop[q] = b[1];
+    if (lam) lam[q] = b[2];
+    if (beta)
+      for (int s = 0; s < d.n_strains; ++s) beta[q * d.n_strains + s] = b[3 + s];
   }
   return LPG_OK;
 }

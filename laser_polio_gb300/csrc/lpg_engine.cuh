@@ -130,6 +130,12 @@ typedef struct {
   const uint8_t* future_seed; /* [nt] 1 if a seed event is scheduled after tick t */
   int32_t* res;               /* results base */
   int64_t res_off[RS_N];
+  /* aggregates the expected-incidence map replays, recorded by k_node_tx
+   * when lpg_record_aggregates asked for them, else NULL: per tick and
+   * node, [0] the susceptibles' summed risk, [1] the population, [2] the
+   * expected new exposures, [3 + s] the pre-mixing infectivity of strain s
+   * ([nt][n_nodes][3 + ns]) */
+  double* rec;
   /* unborn pool columns, indexed by reference slot - count0 */
   int8_t *pl_et, *pl_it, *pl_pt, *pl_strain, *pl_pp, *pl_par, *pl_ipv;
   uint8_t* pl_cm;

@@ -1723,6 +1723,14 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
     pre_sw = W.sw[g];
     pre_sc = W.tot[(int64_t)TT_S * G + g];
   }
+  if (rp->rec) { /* the aggregates the expected-incidence map replays */
+    double* rr = rp->rec + ((int64_t)t * n + i) * (3 + ns);
+    if (threadIdx.x == 0) {
+      rr[0] = (double)pre_sw * 0x1.0p-24;
+      rr[1] = (double)pop_t;
+    }
+    if (threadIdx.x < ns) rr[3 + threadIdx.x] = (double)pre_bb * 0x1.0p-32;
+  }
   const uint64_t* qrow = rp->netq_t + (int64_t)i * n; /* qrow[ii] = network[ii][i] in 2^-62 */
   unsigned __int128 part[LPG_MAX_STRAINS] = {0, 0, 0, 0};
   /* batches of 8 source nodes per thread, every load of a batch issued
@@ -1839,6 +1847,7 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
   if (lane != 0) return;
   const double srisk = (double)pre_sw * 0x1.0p-24;
   const double exposure = srisk * total_p;
+  if (rp->rec) rp->rec[((int64_t)t * n + i) * (3 + ns) + 2] = exposure;
   int64_t total = 0;
   if (!(exposure > 0.0)) {
     total = 0;

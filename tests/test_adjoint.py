@@ -199,3 +199,48 @@ def test_gpu_plan_target_loss_and_gradient_match_oracle(T, G, S, max_frac):
         assert all(ms > 0 and n >= 4 for ms, n in prof.values())
     finally:
         plan.close()
+
+
+@pytest.mark.gpu
+def test_gpu_engine_records_the_aggregates_its_exposures_come_from():
+    """A forward run of the engine records, per transmission tick, the
+    aggregates the adjoint replays (lpg_record_aggregates); the expected-
+    incidence map on them reproduces the engine's own expected exposures
+    (relative 1e-9 of the largest: the engine mixes in exact integers and
+    uses expm1, the map in double-float and 1 - exp, as model.py does)."""
+    from laser_polio_gb300 import synthetic
+    from laser_polio_gb300._lib import Handle
+    from laser_polio_gb300.engine import make_desc
+
+    params, cols = synthetic.bundle(kind="nigeria", n_agents=300_000, n_nodes=30, dur=150, seed=7)
+    G, ns, nt = params["n_nodes"], params["n_strains"], params["nt"]
+    rng = np.random.default_rng(1)
+    xy = rng.uniform(0, 300, (G, 2))
+    dist = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
+    np.fill_diagonal(dist, 0.0)
+    pops = params["pop0"].astype(np.float64)
+    net = dict(k=1.2e4, a=1.0, b=1.0, c=2.0, max_frac=0.05)  # 16 of 30 rows capped
+    params["network"] = row_normalizer(gravity(pops, dist, net["k"], net["a"], net["b"], net["c"])
+                                       / np.power(pops.sum(), net["c"]), net["max_frac"])
+    assert 0 < (params["network"].sum(1) >= net["max_frac"] * (1 - 1e-12)).sum() < G  # capped and uncapped rows
+    desc, _keep = make_desc(params)
+    h = Handle([desc])
+    try:
+        h.record_aggregates(0)
+        h.bind_columns(0, cols)
+        h.start()
+        h.step(nt - 1)
+        h.sync()
+        agg = h.read_aggregates(0, nt, G, ns)
+    finally:
+        h.close()
+    dates = [datetime.date(2019, 1, 1) + datetime.timedelta(days=d) for d in range(nt)]
+    np.testing.assert_array_equal(seasonality_table(dates, 0.4, 180), params["seasonality"])
+    doy = np.array([d.timetuple().tm_yday for d in dates], np.float64)
+    year = np.array([366.0 if d.year % 4 == 0 else 365.0 for d in dates])
+    ticks = slice(1, nt)  # no component runs on tick 0
+    assert np.all(agg["pop"][ticks] > 0) and agg["lam"][ticks].sum() > 0
+    inp = dict(srisk=agg["srisk"][ticks], beta=agg["beta"][ticks], pop=agg["pop"][ticks], doy=doy[ticks],
+               year=year[ticks], r0s=params["r0_scalars"], R=1.0, amp=0.4, peak=180.0, pops=pops, dist=dist, **net)
+    lam, _ = ops.expected_incidence(inp)
+    _close(lam, agg["lam"][ticks], 1e-9, "engine exposures")
