@@ -244,3 +244,20 @@ def test_gpu_engine_records_the_aggregates_its_exposures_come_from():
                year=year[ticks], r0s=params["r0_scalars"], R=1.0, amp=0.4, peak=180.0, pops=pops, dist=dist, **net)
     lam, _ = ops.expected_incidence(inp)
     _close(lam, agg["lam"][ticks], 1e-9, "engine exposures")
+
+
+def test_plan_rejects_bad_arguments_before_any_device_call():
+    """lpg_incidence_plan_create checks sizes and inputs on the host first
+    (LPG_ERR_ARG -> ValueError), with or without a GPU."""
+    inp = I.random_inputs(4, 5, 2, seed=0)
+    with pytest.raises(ValueError, match="pops"):
+        ops.IncidencePlan(dict(inp, pops=-inp["pops"]))
+    dist = inp["dist"].copy()
+    dist[1, 3] = -1.0
+    with pytest.raises(ValueError, match="dist"):
+        ops.IncidencePlan(dict(inp, dist=dist))
+    with pytest.raises(ValueError, match="total population"):
+        ops.IncidencePlan(dict(inp, pops=np.zeros_like(inp["pops"])))
+    beta5 = np.zeros((4, 5, 5))
+    with pytest.raises(ValueError, match="bad sizes"):
+        ops.IncidencePlan(dict(inp, beta=beta5))
