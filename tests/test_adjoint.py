@@ -4,7 +4,8 @@ CPU: the numpy restatement (oracle/incidence.py) is pinned to the package's
 network and seasonality builders (the ones the engine runs on) and its
 reverse pass to fourth-order central finite differences of its own forward
 pass, with and without capped network rows.  GPU: the CUDA path against the
-oracle on the same inputs; FP64 with atomically reduced sums, so agreement
+oracle on the same inputs; FP64 elementwise work, double-float products
+(about 2^-45 of the summed terms) and atomically reduced sums, so agreement
 is to a relative 1e-9, not bit for bit."""
 
 import datetime
@@ -127,8 +128,8 @@ def _close(got, want, rtol, what):
     [(1, 1, 1, 0.2, 0), (10, 8, 2, 3.5e-6, 3), (37, 33, 3, 0.2, 5), (365, 100, 1, 1e-5, 11), (30, 774, 4, 0.2, 2)],
 )
 def test_gpu_incidence_and_vjp_match_oracle(T, G, S, max_frac, seed):
-    """Relative 1e-9 of each output's largest magnitude (FP64; the GPU sums
-    in another order and with atomics)."""
+    """Relative 1e-9 of each output's largest magnitude (the GPU sums in
+    another order, with atomics and double-float products)."""
     inp = I.random_inputs(T, G, S, seed=seed)
     inp["max_frac"] = max_frac
     g = np.random.default_rng(seed + 100).normal(size=(T, G))
