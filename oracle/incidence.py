@@ -11,7 +11,10 @@ per tick t, node n, strain s
     r       = u seas[t] r0s[n] R / max(pop[t,n], 1)                       model.py:1339-1347
     lam[t,n] = srisk[t,n] sum_s (1 - exp(-r))                             model.py:1348-1363
 
-(R scales every agent's infectivity: R0 / R0_ref).  The reverse pass gives,
+(R scales every agent's infectivity: R0 / R0_ref).  Pinned against the C oracle
+of the agent step (lpg_oracle.c, lpo_record_aggregates): on the aggregates
+that oracle mixes, forward() reproduces its expected exposures per tick and
+node (tests/test_adjoint.py).  The reverse pass gives,
 for an upstream gradient g[t,n] = dL/dlam[t,n], the gradients of L with
 respect to R, amp, peak, r0s[n], the network N[a,b] and the gravity
 parameters k, a, b, c.  gravity[i,j] = k p_i^a p_j^b / d_ij^c with a zero

@@ -60,6 +60,9 @@ typedef struct {
   int32_t err;
   int32_t started;
   int32_t* res[NRES];
+  /* per transmission tick and node: srisk, pop, the expected new exposures,
+   * beta before mixing by strain ([nt][n_nodes][3 + ns]), or NULL */
+  double* rec;
   char msg[256];
 } lpo_sim;
 
@@ -166,6 +169,7 @@ void lpo_destroy(lpo_sim* s) {
                 s->it, s->pt, s->pp, s->par, s->ipv, s->cm, s->node, s->ri, s->risk, s->inf, s->dob, s->dod};
   for (size_t i = 0; i < sizeof ps / sizeof ps[0]; ++i) free(ps[i]);
   for (int k = 0; k < NRES; ++k) free(s->res[k]);
+  free(s->rec);
   free(s);
 }
 
@@ -603,7 +607,7 @@ static inline uint64_t lpo_netq(double w) {
  * (model.py:1327-1407), restated in the order the engine evaluates it. */
 void lpo_node_tx(int n, int ns, const uint64_t* B, const uint64_t* SW, const int32_t* Scount, const double* net,
                  const double* r0s, double seas, const int32_t* pop, int use_pop, double zi, int32_t nb_r,
-                 uint64_t seed, int32_t t, double* prob_out, int64_t* size_out) {
+                 uint64_t seed, int32_t t, double* prob_out, int64_t* size_out, double* rec_t) {
   for (int nd = 0; nd < n; ++nd) {
     double p[LPG_MAX_STRAINS];
     double total_p = 0.0;
@@ -631,6 +635,13 @@ void lpo_node_tx(int n, int ns, const uint64_t* B, const uint64_t* SW, const int
     for (int k = 0; k < ns; ++k) prob_out[(size_t)nd * ns + k] = p[k];
     double srisk = (double)SW[nd] * 0x1.0p-24;
     double exposure = srisk * total_p;
+    if (rec_t) { /* the inputs of the expected-incidence map, and its value */
+      double* rr = rec_t + (size_t)nd * (3 + ns);
+      rr[0] = srisk;
+      rr[1] = (double)pop[nd];
+      rr[2] = exposure;
+      for (int k = 0; k < ns; ++k) rr[3 + k] = (double)B[(size_t)nd * ns + k] * 0x1.0p-32;
+    }
     int64_t total = 0;
     lpg_stream st;
     lpg_stream_init(&st, seed, LPG_P_TXCOUNT, t, (uint64_t)nd, 0);
@@ -700,7 +711,8 @@ static void lpo_tx(lpo_sim* s, int32_t t) {
   int64_t* size = calloc((size_t)n, sizeof(int64_t));
   int use_pop = 1;
   lpo_node_tx(n, ns, B, SW, Sc, s->network, s->r0_scalars, s->seasonality[t], RES(R_POP, t), use_pop,
-              s->d.zero_inflation, s->d.nb_r, s->d.seed, t, prob, size);
+              s->d.zero_inflation, s->d.nb_r, s->d.seed, t, prob, size,
+              s->rec ? s->rec + (size_t)t * n * (3 + ns) : NULL);
 
   /* serial gather of susceptible slots per node, index order (:1055-1061) */
   int64_t* off = calloc((size_t)n + 1, sizeof(int64_t));
@@ -832,6 +844,31 @@ int lpo_step(lpo_sim* s, int32_t n_ticks) {
 }
 
 int lpo_num_threads(void) { return nthreads(); }
+
+/* Record the expected-incidence map's inputs on every transmission tick
+ * (the engine's lpg_record_aggregates); before lpo_start. */
+int lpo_record_aggregates(lpo_sim* s, int enable) {
+  if (s->started) return LPG_ERR_STATE;
+  free(s->rec);
+  s->rec = enable ? calloc((size_t)s->d.nt * NN * (3 + NS), sizeof(double)) : NULL;
+  return 0;
+}
+
+/* lpg_read_aggregates' layout: srisk, pop, lam [nt][n] and beta [nt][n][ns]. */
+int lpo_read_aggregates(lpo_sim* s, double* srisk, double* beta, double* pop, double* lam) {
+  if (!s->rec) return LPG_ERR_STATE;
+  const int w = 3 + NS;
+  const size_t rows = (size_t)s->d.nt * NN;
+  for (size_t q = 0; q < rows; ++q) {
+    const double* b = s->rec + q * w;
+    if (srisk) srisk[q] = b[0];
+    if (pop) pop[q] = b[1];
+    if (lam) lam[q] = b[2];
+    if (beta)
+      for (int k = 0; k < NS; ++k) beta[q * NS + k] = b[3 + k];
+  }
+  return 0;
+}
 
 /* Building blocks exposed for the unit tests of the draw hook. */
 void lpo_philox(uint64_t ctr[4], uint64_t k0, uint64_t k1) { lpg_philox4x64_10(ctr, k0, k1); }

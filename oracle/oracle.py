@@ -48,6 +48,8 @@ def lib():
         L.lpo_km_newborn.restype = C.c_int32
         L.lpo_km_newborn.argtypes = [C.POINTER(C.c_int64), C.c_int32, C.c_int32, C.c_uint64, C.c_int32, C.c_uint64]
         L.lpo_num_threads.restype = C.c_int
+        L.lpo_record_aggregates.argtypes = [C.c_void_p, C.c_int]
+        L.lpo_read_aggregates.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 4
         _lib = L
     return _lib
 
@@ -81,6 +83,22 @@ class OracleSim:
 
     def read_columns(self, cols: dict):
         lib().lpo_read_columns(self.h, C.byref(_abi.make_columns(cols)))
+
+    def record_aggregates(self, on: bool = True):
+        """Record the expected-incidence map's inputs per transmission tick
+        (as the engine's lpg_record_aggregates); before start()."""
+        if lib().lpo_record_aggregates(self.h, int(bool(on))) != 0:
+            raise RuntimeError("oracle: record_aggregates after start")
+
+    def read_aggregates(self) -> dict:
+        """srisk, pop, lam [nt, n_nodes] and beta [nt, n_nodes, n_strains]."""
+        nt, n, ns = self.desc.nt, self.desc.n_nodes, self.desc.n_strains
+        out = {"srisk": np.zeros((nt, n)), "beta": np.zeros((nt, n, ns)), "pop": np.zeros((nt, n)),
+               "lam": np.zeros((nt, n))}
+        dp = C.POINTER(C.c_double)
+        if lib().lpo_read_aggregates(self.h, *[_abi.ptr(out[k], dp) for k in ("srisk", "beta", "pop", "lam")]) != 0:
+            raise RuntimeError("oracle: aggregates were not recorded")
+        return out
 
     def close(self):
         if self.h:

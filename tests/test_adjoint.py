@@ -262,3 +262,76 @@ def test_plan_rejects_bad_arguments_before_any_device_call():
     beta5 = np.zeros((4, 5, 5))
     with pytest.raises(ValueError, match="bad sizes"):
         ops.IncidencePlan(dict(inp, beta=beta5))
+
+
+def _recording_bundle(n_agents, n_nodes, dur, seed, capped_rows):
+    """A synthetic run with its own gravity network (distances kept), k set
+    so that about ``capped_rows`` rows reach max_frac."""
+    from laser_polio_gb300 import synthetic
+
+    params, cols = synthetic.bundle(kind="nigeria", n_agents=n_agents, n_nodes=n_nodes, dur=dur, seed=seed)
+    G = params["n_nodes"]
+    rng = np.random.default_rng(seed + 1)
+    xy = rng.uniform(0, 300, (G, 2))
+    dist = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
+    np.fill_diagonal(dist, 0.0)
+    pops = params["pop0"].astype(np.float64)
+    raw = (gravity(pops, dist, 1.0, 1.0, 1.0, 2.0) / pops.sum() ** 2).sum(1)
+    k = float("%.2g" % (0.05 / np.sort(raw)[::-1][capped_rows - 1] * 0.99))
+    net = dict(k=k, a=1.0, b=1.0, c=2.0, max_frac=0.05)
+    params["network"] = row_normalizer(gravity(pops, dist, k, 1.0, 1.0, 2.0) / pops.sum() ** 2, 0.05)
+    return params, cols, pops, dist, net
+
+
+def _replay_inputs(params, agg, pops, dist, net):
+    nt = params["nt"]
+    dates = [datetime.date(2019, 1, 1) + datetime.timedelta(days=d) for d in range(nt)]
+    np.testing.assert_array_equal(seasonality_table(dates, 0.4, 180), params["seasonality"])
+    doy = np.array([d.timetuple().tm_yday for d in dates], np.float64)
+    year = np.array([366.0 if d.year % 4 == 0 else 365.0 for d in dates])
+    ticks = slice(1, nt)  # no component runs on tick 0
+    return dict(srisk=agg["srisk"][ticks], beta=agg["beta"][ticks], pop=agg["pop"][ticks], doy=doy[ticks],
+                year=year[ticks], r0s=params["r0_scalars"], R=1.0, amp=0.4, peak=180.0, pops=pops, dist=dist, **net)
+
+
+def test_oracle_map_reproduces_the_oracles_transmission_exposures():
+    """The CPU oracle of the agent step (pinned to the reference's tests)
+    records, per transmission tick, the aggregates it mixes and its expected
+    exposures (model.py:1315-1363); the numpy expected-incidence map on those
+    aggregates reproduces them (relative 1e-12 of the largest; measured 5e-15:
+    the oracle mixes in exact integers and uses expm1, the map 1 - exp as
+    model.py does), and recording leaves the run's results unchanged."""
+    from laser_polio_gb300.engine import make_desc
+    from oracle.oracle import OracleSim
+
+    params, cols, pops, dist, net = _recording_bundle(60_000, 12, 90, seed=5, capped_rows=5)
+    N = row_normalizer(gravity(pops, dist, net["k"], 1.0, 1.0, 2.0) / pops.sum() ** 2, 0.05)
+    assert 0 < (N.sum(1) >= 0.05 * (1 - 1e-12)).sum() < len(pops)
+    desc, keep = make_desc(params)
+    runs = []
+    for record in (True, False):
+        o = OracleSim(desc, keepalive=keep)
+        if record:
+            o.record_aggregates()
+        o.bind_columns({k: v.copy() for k, v in cols.items()})
+        o.start()
+        o.step(params["nt"] - 1)
+        res = _results_like(params)
+        o.read_results(res)
+        agg = o.read_aggregates() if record else None
+        o.close()
+        runs.append((res, agg))
+    for name in runs[0][0]:
+        np.testing.assert_array_equal(runs[0][0][name], runs[1][0][name], err_msg=name)
+    agg = runs[0][1]
+    assert agg["lam"][1:].sum() > 0 and np.all(agg["pop"][1:] > 0)
+    np.testing.assert_array_equal(agg["pop"][1:], runs[0][0]["pop"][1:])  # nothing is recorded on tick 0
+    lam, _ = I.incidence(_replay_inputs(params, agg, pops, dist, net))
+    _close(lam, agg["lam"][1:], 1e-12, "oracle exposures")
+
+
+def _results_like(params):
+    from laser_polio_gb300 import _abi
+
+    nt, n, ns = params["nt"], params["n_nodes"], params["n_strains"]
+    return {name: np.zeros((nt, n, ns) if wide else (nt, n), np.int32) for name, wide in _abi.RESULT_FIELDS}
