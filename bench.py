@@ -64,6 +64,8 @@ def parse():
                     help="instead: R calibration replicates (730 ticks) batched in one handle vs run one by one")
     ap.add_argument("--incidence", type=int, default=0, metavar="T",
                     help="instead: loss and gradient of the expected incidence over T ticks (the adjoint)")
+    ap.add_argument("--export", action="store_true",
+                    help="instead: save_sim_results' CSV of a Nigeria-scale results table (host only)")
     return ap.parse_args()
 
 
@@ -531,8 +533,82 @@ def incidence_arm(args):
         Path(args.out).write_text(json.dumps(line, indent=1))
 
 
+def export_arm(args):
+    """save_sim_results' CSV (utils.py:689-786) of a 2556-tick x 774-node
+    results table (1.98e6 rows, seeded synthetic counts): the native writer
+    (lpg_write_results_csv, host threads) against a restatement of the same
+    file with Python's csv module (the reference writes it with pandas, which
+    is absent here).  Host only; rows/s over K writes after W warm-up writes."""
+    import csv
+    import datetime
+    import tempfile
+    import types
+
+    from laser_polio_gb300.core import PropertySet
+    from laser_polio_gb300.utils import RESULT_TABLE_COLUMNS, save_sim_results
+
+    nt, nodes = 2556, args.nodes
+    rng = np.random.default_rng(args.seed)
+    sim = types.SimpleNamespace(
+        nt=nt, nodes=np.arange(nodes),
+        results=types.SimpleNamespace(**{a: rng.integers(0, 200_000, (nt, nodes)).astype(np.int32)
+                                         for _, a in RESULT_TABLE_COLUMNS}),
+        datevec=[datetime.date(2019, 1, 1) + datetime.timedelta(days=d) for d in range(nt)],
+        pars=PropertySet({"node_lookup": {n: {"dot_name": f"AFRO:NIGERIA:STATE_{n % 37}:LGA_{n}"}
+                                          for n in range(nodes)}}))
+    rows = nt * nodes
+    W, K = max(1, min(args.warmup, 3)), max(1, min(args.steps, 5))
+    with tempfile.TemporaryDirectory() as d:
+        path = Path(d) / "results.csv"
+        for _ in range(W):
+            save_sim_results(sim, path)
+        t0 = time.perf_counter()
+        for _ in range(K):
+            save_sim_results(sim, path)
+        native_s = (time.perf_counter() - t0) / K
+        size = path.stat().st_size
+        native_bytes = path.read_bytes()
+        ref = Path(d) / "ref.csv"
+        t0 = time.perf_counter()
+        names = [c for c, _ in RESULT_TABLE_COLUMNS]
+        arrs = [getattr(sim.results, a) for _, a in RESULT_TABLE_COLUMNS]
+        with open(ref, "w", newline="") as f:
+            w = csv.writer(f, lineterminator="\n")
+            w.writerow(["timestep", "date", "node", "dot_name", *names])
+            lookup = sim.pars.node_lookup
+            for t in range(nt):
+                ds = str(sim.datevec[t])
+                for n in range(nodes):
+                    w.writerow([t, ds, n, lookup[n]["dot_name"], *[int(a[t, n]) for a in arrs]])
+        py_s = time.perf_counter() - t0
+        same = ref.read_bytes() == native_bytes
+    line = {
+        "metric": "results table rows/s written as CSV",
+        "value": rows / native_s,
+        "unit": "rows/s",
+        "n_gpus": 0,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": native_s * 1e3,
+        "higher_is_better": True,
+        "dtype": "int32",
+        "data": "synthetic (seeded counts)",
+        "config": {"workload": f"save_sim_results CSV, {nt} timesteps x {nodes} nodes = {rows} rows",
+                   "bytes": size, "threads": os.cpu_count()},
+        "cpu_baseline": {"value": rows / py_s, "unit": "rows/s", "cores": 1, "kind": "port",
+                         "sample": "the same file with Python's csv module, one write"},
+        "identical_bytes": same,
+    }
+    print(json.dumps(line), flush=True)
+    if args.out:
+        Path(args.out).write_text(json.dumps(line, indent=1))
+
+
 def main():
     args = parse()
+    if args.export:
+        export_arm(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
         return

@@ -408,6 +408,19 @@ void lpg_incidence_plan_destroy(lpg_incidence_plan* p);
 int lpg_expected_incidence(const lpg_incidence_in* in, double* lam_out, const double* g_lam,
                            lpg_incidence_grad* grad, void* stream);
 
+/* save_sim_results' table (utils.py:689-786) as CSV, written by host threads:
+ * one row per (timestep, node), timestep-major, with the columns timestep,
+ * date, node, dot_name and then field_names[0..n_fields); the format of
+ * pandas' DataFrame.to_csv(index=False) ('\n' rows, QUOTE_MINIMAL strings).
+ * dates [nt] and dot_names [n_nodes] are NUL-terminated strings; fields[k]
+ * is an int32 array [nt][n_nodes].  Host memory only; needs no GPU.  The
+ * DataFrame the reference also returns and its summary groupings
+ * (utils.py:1040-1160) are not built here. */
+#define LPG_EXPORT_MAX_FIELDS 64
+int lpg_write_results_csv(const char* path, int32_t nt, int32_t n_nodes, const char* const* dates,
+                          const char* const* dot_names, int32_t n_fields, const char* const* field_names,
+                          const int32_t* const* fields);
+
 const char* lpg_op_last_error(void);
 
 #ifdef __cplusplus

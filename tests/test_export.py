@@ -1,0 +1,113 @@
+"""save_sim_results (utils.py:689-786) with the native CSV writer
+(lpg_write_results_csv), on the CPU.
+
+The reference's own tests (tests/test_report_saving.py) ask for the columns
+below, nt x nodes rows, a round trip through the file, and one dot_name per
+node.  The format of pandas' to_csv(index=False) is restated here with the
+csv module (',' separator, '\\n' rows, QUOTE_MINIMAL), and the native file
+must equal it byte for byte."""
+
+import csv
+import datetime
+import io
+import types
+
+import numpy as np
+import pytest
+
+from laser_polio_gb300.core import PropertySet
+from laser_polio_gb300.utils import RESULT_TABLE_COLUMNS
+from laser_polio_gb300.utils import save_sim_results
+
+COLUMNS = ["timestep", "date", "node", "dot_name"] + [c for c, _ in RESULT_TABLE_COLUMNS]
+
+
+def _fake_sim(nt, nodes, seed=0, names=None):
+    rng = np.random.default_rng(seed)
+    start = datetime.date(2019, 1, 1)
+    results = types.SimpleNamespace(**{attr: rng.integers(-5, 2_000_000, (nt, nodes)).astype(np.int32)
+                                       for _, attr in RESULT_TABLE_COLUMNS})
+    if names is None:
+        names = [f"AFRO:NIGERIA:STATE_{n % 7}:LGA_{n}" for n in range(nodes)]
+    lookup = {n: {"dot_name": names[n]} for n in range(nodes) if names[n] is not None}
+    return types.SimpleNamespace(nt=nt, nodes=np.arange(nodes), results=results,
+                                 datevec=[start + datetime.timedelta(days=d) for d in range(nt)],
+                                 pars=PropertySet({"node_lookup": lookup}))
+
+
+def _pandas_like_csv(sim):
+    nodes = len(sim.nodes)
+    lookup = sim.pars.node_lookup
+    buf = io.StringIO()
+    w = csv.writer(buf, lineterminator="\n", quoting=csv.QUOTE_MINIMAL)
+    w.writerow(COLUMNS)
+    for t in range(sim.nt):
+        for n in range(nodes):
+            row = [t, str(sim.datevec[t]), n, lookup.get(n, {}).get("dot_name", "UNKNOWN")]
+            row += [int(getattr(sim.results, attr)[t, n]) for _, attr in RESULT_TABLE_COLUMNS]
+            w.writerow(row)
+    return buf.getvalue().encode()
+
+
+def test_csv_is_the_pandas_format_byte_for_byte(tmp_path):
+    names = ["AFRO:NIGERIA:ZAMFARA:ANKA", 'AFRO:X:"QUOTED":Y', "AFRO:X:A,B:C", None, "AFRO:Z:LINE\nBREAK:W"]
+    sim = _fake_sim(7, 5, seed=1, names=names)
+    out = tmp_path / "results.csv"
+    table = save_sim_results(sim, out)
+    assert out.read_bytes() == _pandas_like_csv(sim)
+    assert len(table["timestep"]) == sim.nt * 5
+
+
+def test_many_blocks_and_threads_keep_row_order(tmp_path):
+    sim = _fake_sim(400, 300, seed=2)  # 120k rows: several 64k-row blocks formatted by threads
+    out = tmp_path / "big.csv"
+    save_sim_results(sim, out)
+    assert out.read_bytes() == _pandas_like_csv(sim)
+
+
+def test_round_trip_rows_columns_and_names(tmp_path):
+    """The checks of the reference's test_save_sim_results, on the native file."""
+    sim = _fake_sim(11, 14, seed=3)
+    out = tmp_path / "rt.csv"
+    save_sim_results(sim, out)
+    with open(out, newline="") as f:
+        rows = list(csv.reader(f))
+    assert rows[0] == COLUMNS
+    body = rows[1:]
+    assert len(body) == sim.nt * len(sim.nodes)
+    assert max(int(r[0]) for r in body) < sim.nt
+    assert len({r[3] for r in body}) == len(sim.nodes)
+    for k, (_, attr) in enumerate(RESULT_TABLE_COLUMNS):
+        got = np.array([int(r[4 + k]) for r in body]).reshape(sim.nt, -1)
+        np.testing.assert_array_equal(got, getattr(sim.results, attr))
+    assert [r[1] for r in body[:: len(sim.nodes)]] == [str(d) for d in sim.datevec]
+
+
+def test_real_sim_object_and_empty_table(tmp_path):
+    from laser_polio_gb300 import synthetic
+
+    sim = synthetic.zamfara_like(n_agents=5_000, dur=6, seed=4)
+    out = tmp_path / "z.csv"
+    save_sim_results(sim, out)
+    lines = out.read_text().splitlines()
+    assert lines[0] == ",".join(COLUMNS)
+    assert len(lines) == 1 + sim.nt * len(sim.nodes)
+    empty = _fake_sim(0, 3)
+    save_sim_results(empty, tmp_path / "empty.csv")
+    assert (tmp_path / "empty.csv").read_text() == ",".join(COLUMNS) + "\n"
+
+
+def test_errors(tmp_path):
+    sim = _fake_sim(3, 2)
+    with pytest.raises(NotImplementedError):
+        save_sim_results(sim, tmp_path / "x.csv", summary_config={"grouping_level": "adm0"})
+    with pytest.raises(OSError, match="cannot open"):
+        save_sim_results(sim, tmp_path / "no_such_dir" / "x.csv")
+    sim.results.S = sim.results.S[:, :1]
+    with pytest.raises(ValueError, match="results.S"):
+        save_sim_results(sim, tmp_path / "x.csv")
+    try:
+        import pandas  # noqa: F401
+    except ImportError:
+        with pytest.raises(ImportError, match="pandas"):
+            save_sim_results(_fake_sim(3, 2), tmp_path / "x.h5")
