@@ -335,3 +335,43 @@ def _results_like(params):
 
     nt, n, ns = params["nt"], params["n_nodes"], params["n_strains"]
     return {name: np.zeros((nt, n, ns) if wide else (nt, n), np.int32) for name, wide in _abi.RESULT_FIELDS}
+
+
+class _OraclePlan:
+    """IncidencePlan's evaluate() restated by the numpy oracle (CPU)."""
+
+    def __init__(self, inp, target):
+        self.inp, self.target, self.calls = inp, target, 0
+
+    def evaluate(self, params, g=None, *, network_grad=True):
+        self.calls += 1
+        x = dict(self.inp, **{k: params[k] for k in ("R", "amp", "peak", "k", "a", "b", "c", "max_frac")},
+                 r0s=params["r0s"])
+        _, loss, grads = _oracle_loss_grad(x, self.target)
+        return {"loss": loss, "grad": grads}
+
+
+def test_fit_incidence_recovers_the_parameters_of_the_target():
+    """Gradient-based calibration (calibrate.fit_incidence, L-BFGS-B on the
+    adjoint's loss and gradient) recovers R, amp and peak of a target curve,
+    and then the per-node r0 scalars as well."""
+    from laser_polio_gb300.calibrate import fit_incidence
+
+    inp = I.random_inputs(60, 10, 2, seed=21)
+    truth = dict(R=1.25, amp=0.3, peak=150.0, k=0.5)
+    target = I.incidence(dict(inp, **truth))[0]
+    plan = _OraclePlan(inp, target)
+    start = dict(inp, R=1.0, amp=0.45, peak=175.0)
+    fit, res = fit_incidence(plan, start, free=("R", "amp", "peak"), bounds={"amp": (0.0, 1.0)})
+    assert res.success, res.message
+    for name in ("R", "amp", "peak"):
+        assert abs(fit[name] - truth[name]) <= 1e-5 * max(1.0, abs(truth[name])), (name, fit[name])
+    # the per-node r0 scalars too, with R held at its fitted value (R and r0s are not separable)
+    r0_true = inp["r0s"].copy()
+    target2 = I.incidence(dict(inp, **truth))[0]
+    plan2 = _OraclePlan(inp, target2)
+    fit2, res2 = fit_incidence(plan2, dict(fit, r0s=r0_true * 1.1), free=(), fit_r0s=True)
+    assert res2.success, res2.message
+    np.testing.assert_allclose(fit2["r0s"], r0_true, rtol=1e-5)
+    with pytest.raises(ValueError, match="unknown"):
+        fit_incidence(plan, start, free=("R0",))
