@@ -213,6 +213,36 @@ def build_sim_spec(sim) -> SimSpec:
     return SimSpec(d, keep, columns, results)
 
 
+def run_replicates(sims) -> None:
+    """Run several SEIR_ABM (drop-in GPU components) as one batch: one
+    handle, one launch sequence per tick for all of them.  The reference's
+    calibration runs its replicates one after another (calib/objective.py:
+    47-70, run_sim per replicate).  The sims may differ in nodes, agents,
+    durations and components; each stops at its own last tick or stop rule.
+    Afterwards every sim holds what its own run() would have left: results,
+    people columns and count, t and should_stop."""
+    sims = list(sims)
+    if not sims:
+        return
+    specs = [build_sim_spec(s) for s in sims]
+    handle = _lib.Handle([sp.desc for sp in specs])
+    try:
+        for i, sp in enumerate(specs):
+            handle.bind_columns(i, sp.columns)
+        handle.start()
+        handle.step(max(int(s.nt) for s in sims) - 1)
+        handle.sync()
+        for i, (sim, sp) in enumerate(zip(sims, specs)):
+            handle.read_results(i, sp.results)
+            handle.read_columns(i, sp.columns)
+            st = handle.state(i)
+            sim.people._set_count(st.count)
+            sim.t = st.t
+            sim.should_stop = bool(st.stopped)
+    finally:
+        handle.close()
+
+
 class GpuTick:
     """Runs the components' per-tick work of one SEIR_ABM on the GPU."""
 
