@@ -19,9 +19,10 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_build" / "liblpg.so"
 SOURCES = [CSRC / "lpg_engine.cu", CSRC / "lpg_ops.cu", CSRC / "lpg_adjoint.cu", CSRC / "lpg_export.cpp"]
 DEPS = SOURCES + [CSRC / "lpg_kernels.cuh", CSRC / "lpg_engine.cuh", CSRC / "lpg_rng.h", CSRC / "lpg_detmath.h",
-                  ROOT / "include" / "lpg.h"]
+                  CSRC / "lpg_ri.h", ROOT / "include" / "lpg.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-math-errno"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler",
+         "-fPIC,-ffp-contract=off,-fno-math-errno,-pthread"]
 
 
 def nvcc() -> str:
@@ -49,7 +50,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         raise subprocess.CalledProcessError(1, failed[0])
     tmp = OUT.with_suffix(f".{tag}.tmp")
     try:
-        subprocess.run([nvcc(), ARCH, "-shared", *[str(o) for o in objs], "-o", str(tmp)], check=True)
+        subprocess.run([nvcc(), ARCH, "-shared", "-Xcompiler", "-pthread", *[str(o) for o in objs], "-o", str(tmp)],
+                       check=True)
     finally:
         for obj in objs:
             obj.unlink(missing_ok=True)
