@@ -496,13 +496,16 @@ def incidence_arm(args):
     if not args.no_cpu:
         from oracle import incidence as oracle_incidence
 
-        t0 = time.perf_counter()
-        lam, _ = oracle_incidence.incidence(inp)
-        resid = np.log1p(lam) - np.log1p(target)
-        oracle_incidence.incidence(inp, 2.0 * resid / (1.0 + lam))
-        cpu_s = time.perf_counter() - t0
-        cpu = {"value": 1.0 / cpu_s, "unit": "evaluations/s", "cores": 1, "kind": "port",
-               "sample": f"one loss and gradient evaluation, T={T}, numpy FP64 restatement"}
+        n_cpu, t0 = 0, time.perf_counter()
+        while n_cpu < 50 and (n_cpu == 0 or time.perf_counter() - t0 < 10.0):
+            lam, _ = oracle_incidence.incidence(inp)
+            resid = np.log1p(lam) - np.log1p(target)
+            oracle_incidence.incidence(inp, 2.0 * resid / (1.0 + lam))
+            n_cpu += 1
+        cpu_s = (time.perf_counter() - t0) / n_cpu
+        cpu = {"value": 1.0 / cpu_s, "unit": "evaluations/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{n_cpu} loss and gradient evaluations, T={T}, numpy FP64 restatement "
+                         "(products through BLAS on the host's threads)"}
     line = {
         "metric": "expected-incidence loss and gradient evaluations/s",
         "value": 1e3 / dev_ms,

@@ -49,7 +49,8 @@ def network(pops, dist, k, a, b, c, max_frac):
 def forward(srisk, beta, pop, doy, year, r0s, R, amp, peak, N):
     """lam [T, G] and the intermediates of the reverse pass."""
     rsN = N.sum(axis=1)
-    u = beta * (1.0 - rsN)[None, :, None] + np.einsum("in,tis->tns", N, beta)
+    # sum_i N[i,n] beta[t,i,s] as one BLAS product (np.tensordot), not einsum's loops
+    u = beta * (1.0 - rsN)[None, :, None] + np.tensordot(N, beta, axes=([0], [1])).transpose(1, 0, 2)
     ang = 2.0 * np.pi * (doy - peak) / year
     seas = 1.0 + amp * np.cos(ang)
     q = seas[:, None] * r0s[None, :] * R / np.maximum(pop, 1.0)
@@ -72,7 +73,7 @@ def backward(g, srisk, beta, pop, doy, year, r0s, R, amp, peak, N, mid, pops, di
     g_amp = (g_seas * np.cos(ang)).sum()
     g_peak = (g_seas * amp * np.sin(ang) * 2.0 * np.pi / year).sum()
     # u[n] = beta[n] (1 - sum_k N[n,k]) + sum_i N[i,n] beta[i]
-    gN = np.einsum("tas,tbs->ab", beta, gu) - np.einsum("tas,tas->a", beta, gu)[:, None]
+    gN = np.tensordot(beta, gu, axes=([0, 2], [0, 2])) - np.einsum("tas,tas->a", beta, gu)[:, None]
     np.fill_diagonal(gN, 0.0)
     # through rownorm: capped rows N = m G / rs
     gG = gN.copy()
