@@ -487,3 +487,74 @@ def test_linear_transmission(backend):
         assert after.size > 0 and np.all(I[peaks[k] + after[0]:, k] == 0), k
     assert peaks[2] > peaks[1] and peaks[3] > peaks[2]
     assert np.where(I[peaks[3]:, 3] == 0)[0].size > 0
+
+
+def _tx_sim(seed, r0=14, r0_scalars=None, init_immun=0.8, init_prev=0.01):
+    """tests/test_transmission.py:21-58 (setup_sim): two nodes of 10000, one tick."""
+    pars = PropertySet(
+        {
+            "seed": seed,
+            "start_date": lp.date("2020-01-01"),
+            "dur": 1,
+            "init_pop": np.array([10000, 10000]),
+            "cbr": np.array([30, 25]),
+            "r0_scalars": np.array([0.5, 2.0], dtype=np.float32) if r0_scalars is None else r0_scalars,
+            "init_immun": init_immun,
+            "init_prev": init_prev,
+            "p_paralysis": 1 / 2000,
+            "r0": r0,
+            "risk_mult_var": 4.0,
+            "corr_risk_inf": 0.8,
+            "seasonal_amplitude": 0.0,
+            "seasonal_peak_doy": 180,
+            "distances": np.array([[0, 1], [1, 0]]),
+            "gravity_k": 0.5,
+            "gravity_a": 1,
+            "gravity_b": 1,
+            "gravity_c": 2.0,
+            "max_migr_frac": 0.01,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.DiseaseState_ABM, lp.Transmission_ABM, lp.VitalDynamics_ABM]
+    return sim
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_trans_default(backend):
+    """tests/test_transmission.py:61-95: over 10 one-tick replicates the
+    mean number of exposures is within 2 binomial standard errors of
+    sum_n S_n (1 - exp(-(R0 / D) r0s_n I_n / N_n)).  The reference draws
+    unseeded replicates; seeds 1-10 here."""
+    exposures = []
+    for seed in range(1, 11):
+        sim = run(_tx_sim(seed), backend)
+        exposures.append(int(sim.results.E[1:].sum()))
+    exposures = np.array(exposures)
+    assert np.all(exposures > 0)
+    D = np.mean(sim.pars["dur_inf"](1000))
+    S, E, I, R = (sim.results.S[0], sim.results.E[0], sim.results.I[0], sim.results.R[0])
+    N = S + E + I + R
+    p_inf = 1 - np.exp(-(sim.pars["r0"] / D) * np.asarray(sim.pars["r0_scalars"]) * I / N)
+    exp_E = np.sum(S * p_inf)
+    stderr = np.sqrt(S * p_inf * (1 - p_inf)).sum()
+    assert abs(exposures.mean() - exp_E) < 2 * stderr, (exposures.mean(), exp_E, stderr)
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_double_trans(backend):
+    """tests/test_transmission.py:116-145: doubling r0, the r0 scalars or
+    the initial prevalence about doubles the exposures of one tick (mean
+    over the reference's ten seeds, within 20%)."""
+    seeds = [12345, 23456, 34567, 45678, 56789, 67890, 78901, 89012, 90123, 11234]
+    r0s = np.array([1.0, 1.0])
+
+    def mean_exposures(**kw):
+        args = dict(init_immun=0.0, r0=5, r0_scalars=r0s, init_prev=0.01)
+        args.update(kw)
+        return np.mean([run(_tx_sim(s, **args), backend).results.E[1:].sum() for s in seeds])
+
+    base = mean_exposures()
+    for label, kw in (("r0", {"r0": 10}), ("r0_scalars", {"r0_scalars": r0s * 2}), ("init_prev", {"init_prev": 0.02})):
+        ratio = mean_exposures(**kw) / base
+        assert np.isclose(ratio, 2.0, rtol=0.2), (label, ratio)
