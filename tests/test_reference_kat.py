@@ -558,3 +558,55 @@ def test_double_trans(backend):
     for label, kw in (("r0", {"r0": 10}), ("r0_scalars", {"r0_scalars": r0s * 2}), ("init_prev", {"init_prev": 0.02})):
         ratio = mean_exposures(**kw) / base
         assert np.isclose(ratio, 2.0, rtol=0.2), (label, ratio)
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_zero_inflation(backend):
+    """tests/test_transmission.py:247-352: 20 nodes, infection only in node
+    0, strong mixing; 90% zero inflation of the seeding draw leaves fewer
+    nodes with cases (on day 1 and over 10 days) than none, and 99% fewer
+    still.  The reference's seeds 1000-1019."""
+    n = 20
+
+    def sim_for(zi, seed):
+        init_prev = np.zeros(n, dtype=np.float32)
+        init_prev[0] = 0.3
+        pars = PropertySet(
+            {
+                "seed": int(seed),
+                "start_date": lp.date("2020-01-01"),
+                "dur": 10,
+                "init_pop": np.array([5000] * n),
+                "cbr": np.array([36.5] * n, dtype=np.float32),
+                "r0_scalars": np.ones(n, dtype=np.float32),
+                "init_immun": np.array([0.8] * n, dtype=np.float32),
+                "init_prev": init_prev,
+                "distances": np.ones((n, n)),
+                "gravity_k": 5,
+                "gravity_a": 5,
+                "gravity_b": 5,
+                "gravity_c": 1.0,
+                "max_migr_frac": 1.0,
+                "node_seeding_zero_inflation": zi,
+                "node_seeding_dispersion": 10,
+            }
+        )
+        sim = lp.SEIR_ABM(pars)
+        sim.components = [lp.DiseaseState_ABM, lp.Transmission_ABM, lp.VitalDynamics_ABM]
+        return run(sim, backend)
+
+    def counts(zi, seeds):
+        total, day1 = [], []
+        for s in seeds:
+            E = sim_for(zi, s).results.E
+            total.append(int(np.sum(E[1:].sum(axis=0) > 0)))
+            day1.append(int(np.sum(E[1] > 0)))
+        return np.array(total), np.array(day1)
+
+    seeds = np.arange(1000, 1020)
+    tot0, d0 = counts(0.0, seeds)
+    tot9, d9 = counts(0.9, seeds)
+    assert np.all(tot0 >= 1) and np.all(tot9 >= 1)
+    assert d9.mean() < d0.mean() and tot9.mean() < tot0.mean()
+    totx, dx = counts(0.99, seeds[:5])
+    assert dx.mean() < d9.mean() and totx.mean() < tot9.mean()
