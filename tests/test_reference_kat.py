@@ -610,3 +610,46 @@ def test_zero_inflation(backend):
     assert d9.mean() < d0.mean() and tot9.mean() < tot0.mean()
     totx, dx = counts(0.99, seeds[:5])
     assert dx.mean() < d9.mean() and totx.mean() < tot9.mean()
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+@pytest.mark.parametrize("heterogeneity", [False, True], ids=["sans_heterogeneity", "with_heterogeneity"])
+def test_r0_one_infection(backend, heterogeneity):
+    """tests/test_transmission.py:354-460 (and its with-heterogeneity twin):
+    one infectious agent in a fully susceptible population, R0 = 14,
+    infectious for 25 days and exposed for 60, no seasonality or births:
+    after 30 days it has recovered and about 14 agents (within 7) are
+    exposed, averaged over 10 replicates.  The reference runs Zamfara's
+    data through run_sim; one synthetic node of 50000 agents here, seeds
+    1-10."""
+    E_final, I_init, I_final = [], [], []
+    for seed in range(1, 11):
+        pars = PropertySet(
+            {
+                "seed": seed,
+                "start_date": lp.date("2018-01-01"),
+                "dur": 30,
+                "init_pop": np.array([50000]),
+                "distances": np.zeros((1, 1)),
+                "cbr": np.array([0.0]),
+                "r0_scalars": np.ones(1),
+                "init_immun": 0.0,
+                "init_prev": 1,
+                "r0": 14,
+                "individual_heterogeneity": heterogeneity,
+                "seasonal_amplitude": 0.0,
+                "dur_inf": lp.constant(value=25),
+                "dur_exp": lp.constant(value=60),
+                "stop_if_no_cases": False,
+            }
+        )
+        sim = lp.SEIR_ABM(pars)
+        sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.Transmission_ABM]
+        run(sim, backend)
+        E = sim.results.E_by_strain[:, :, 0].sum(axis=1)
+        I = sim.results.I_by_strain[:, :, 0].sum(axis=1)
+        E_final.append(int(E[-1]))
+        I_init.append(int(I[0]))
+        I_final.append(int(I[-1]))
+    assert np.all(np.array(I_init) == 1) and np.all(np.array(I_final) == 0), (I_init, I_final)
+    assert np.isclose(np.mean(E_final), 14, atol=7), E_final
