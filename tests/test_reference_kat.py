@@ -680,3 +680,47 @@ def test_prng_seeding(backend):
     assert a.results.ri_vaccinated.sum() > 0 and a.results.sia_vaccinated.sum() > 0
     for other in (_seeded_run(13, backend=backend), _seeded_run(42, model_seed=13, backend=backend)):
         assert not all(np.array_equal(getattr(a.results, f), getattr(other.results, f)) for f in _SEEDED_FIELDS)
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_ri_manually_seeded(backend):
+    """tests/test_interventions.py:49-57: 1000 agents whose RI timers fall
+    due within the run are all vaccinated, OPV and IPV."""
+    n_vx, dur = 1000, 28
+    sim = _interventions_sim(dur=dur, vx_prob_ri=1.0, vx_prob_ipv=1.0)
+    sim.people.ri_timer[:n_vx] = np.random.default_rng(7).integers(0, dur, n_vx)
+    run(sim, backend)
+    assert sim.results.ri_vaccinated.sum() >= n_vx
+    assert sim.results.ipv_vaccinated.sum() >= n_vx
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_ri_on_births(backend):
+    """tests/test_interventions.py:60-66: with many births over a year, RI
+    gives OPV and IPV doses."""
+    sim = _interventions_sim(dur=365, cbr=np.array([300, 250]), vx_prob_ri=1.0, init_pop=np.array([10000, 10000]))
+    run(sim, backend)
+    assert np.sum(sim.results.ri_vaccinated) > 0
+    assert np.sum(sim.results.ipv_vaccinated) > 0
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_ri_vx_prob(backend):
+    """tests/test_interventions.py:93-135: 100 agents all due within 28 days,
+    no births: over 10 replicates the mean OPV and IPV dose counts are within
+    2 binomial standard deviations of 100 p (p = 0.65, 0.85), and every OPV
+    dose exposes its agent (efficacy 1, within one)."""
+    total, dur, p_ri, p_ipv = 100, 28, 0.65, 0.85
+    vx, ipv, exposed = [], [], []
+    for rep in range(10):
+        sim = _interventions_sim(init_pop=np.array([50, 50]), dur=dur, vx_prob_ri=p_ri, vx_prob_ipv=p_ipv,
+                                 cbr=np.array([0, 0]), seed=rep)
+        sim.people.ri_timer[:total] = np.random.default_rng(100 + rep).integers(0, dur, total)
+        run(sim, backend)
+        vx.append(int(np.sum(sim.results.ri_vaccinated)))
+        ipv.append(int(np.sum(sim.results.ipv_vaccinated)))
+        exposed.append(int(np.sum(sim.results.new_exposed)))
+    vx, ipv, exposed = np.array(vx), np.array(ipv), np.array(exposed)
+    assert abs(vx.mean() - total * p_ri) < 2 * np.sqrt(total * p_ri * (1 - p_ri)), vx
+    assert abs(ipv.mean() - total * p_ipv) < 2 * np.sqrt(total * p_ipv * (1 - p_ipv)), ipv
+    assert np.all(np.abs(vx - exposed) <= 1), (vx, exposed)
