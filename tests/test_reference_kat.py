@@ -724,3 +724,73 @@ def test_ri_vx_prob(backend):
     assert abs(vx.mean() - total * p_ri) < 2 * np.sqrt(total * p_ri * (1 - p_ri)), vx
     assert abs(ipv.mean() - total * p_ipv) < 2 * np.sqrt(total * p_ipv * (1 - p_ipv)), ipv
     assert np.all(np.abs(vx - exposed) <= 1), (vx, exposed)
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_paralysis_probability(backend):
+    """tests/test_diseasestate_abm.py:355-380: everyone exposed, DiseaseState
+    alone for 100 days: some are paralysed, at most twice p_paralysis of
+    the population."""
+    pars = PropertySet(
+        {
+            "start_date": lp.date("2020-01-01"),
+            "dur": 100,
+            "init_pop": np.array([50000, 50000]),
+            "cbr": np.array([30, 25]),
+            "r0_scalars": np.array([0.5, 2.0]),
+            "init_immun": 0.0,
+            "init_prev": 1.0,
+            "dur_exp": lp.constant(value=1),
+            "dur_inf": lp.constant(value=1),
+            "p_paralysis": 1 / 2000,
+            "stop_if_no_cases": False,
+            "seed": 9,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.DiseaseState_ABM]
+    sim.people.disease_state[: sim.pars.init_pop.sum()] = 1
+    run(sim, backend)
+    expected = int(pars.p_paralysis * pars.init_pop.sum())
+    assert 0 < np.sum(sim.people.paralyzed == 1) <= expected * 2
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_seed_schedule_by_name_and_node(backend):
+    """tests/test_diseasestate_abm.py:397-456: with r0 = 0, infections
+    appear only where the seed schedule puts them — node 1 on day 1 and
+    node 5 on day 2 by date and dot_name, node 13 on day 3 by timestep and
+    node id; nothing outside node 0 on day 0.  The reference runs Zamfara's
+    14 LGAs through run_sim; 14 synthetic nodes with their own lookup here."""
+    n = 14
+    names = [f"AFRO:NIGERIA:ZAMFARA:LGA{k}" for k in range(n)]
+    init_prev = np.zeros(n)
+    init_prev[0] = 0.01
+    pars = PropertySet(
+        {
+            "start_date": lp.date("2019-01-01"),
+            "dur": 30,
+            "init_pop": np.full(n, 3000),
+            "distances": np.ones((n, n)) * 50,
+            "r0_scalars": np.ones(n),
+            "cbr": np.full(n, 30.0),
+            "init_prev": init_prev,
+            "r0": 0,
+            "node_lookup": {k: {"dot_name": names[k]} for k in range(n)},
+            "seed_schedule": [
+                {"date": "2019-01-02", "dot_name": names[1], "prevalence": 0.1},
+                {"date": "2019-01-03", "dot_name": names[5], "prevalence": 0.1},
+                {"timestep": 3, "node_id": 13, "prevalence": 0.05},
+            ],
+            "stop_if_no_cases": False,
+            "seed": 11,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.Transmission_ABM]
+    run(sim, backend)
+    I = sim.results.I
+    assert np.sum(I[0, 1:]) == 0
+    assert I[1, 1] > 0 and I[2, 5] > 0 and I[3, 13] > 0
+    others = [k for k in range(n) if k not in (0, 1, 5, 13)]
+    assert np.sum(I[:, others]) == 0
