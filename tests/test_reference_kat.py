@@ -794,3 +794,58 @@ def test_seed_schedule_by_name_and_node(backend):
     assert I[1, 1] > 0 and I[2, 5] > 0 and I[3, 13] > 0
     others = [k for k in range(n) if k not in (0, 1, 5, 13)]
     assert np.sum(I[:, others]) == 0
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_sia_different_vaccine_types(backend):
+    """tests/test_strain_transmission.py:204-244: an SIA with nOPV2 or with
+    mOPV2 gives vaccine-strain exposures and never VDPV2."""
+    for vt in ("nOPV2", "mOPV2"):
+        sia = [{"date": "2019-01-05", "nodes": [0], "age_range": (0, 5 * 365), "vaccinetype": vt}]
+        sim = run(_strain_sim(dur=30, init_prev=np.array([0.0, 0.0]), vx_prob_sia=np.array([1.0, 0.0]),
+                              sia_schedule=sia), backend)
+        v = sim.pars.strain_ids["VDPV2"]
+        eb, ib = sim.results.E_by_strain, sim.results.I_by_strain
+        assert eb[:, :, 1:].sum() > 0 or ib[:, :, 1:].sum() > 0, vt
+        assert eb[:, :, v].sum() == 0 and ib[:, :, v].sum() == 0, vt
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_strain_r0_scalars_nopv2_vs_sabin2(backend):
+    """tests/test_strain_transmission.py:388-488: the same SIA with mOPV2
+    (Sabin2) and with nOPV2, seed 123: both strains are exposed on the SIA
+    day, Sabin2 more (higher efficacy); afterwards nOPV2 spreads less
+    (lower strain_r0_scalars); no other strain appears."""
+    sims = {}
+    for vt in ("mOPV2", "nOPV2"):
+        sia = [{"date": "2019-01-10", "nodes": [0, 1], "age_range": (0, 5 * 365), "vaccinetype": vt}]
+        sims[vt] = run(_strain_sim(dur=90, init_prev=np.array([0.0, 0.0]), vx_prob_sia=np.array([0.2, 0.2]),
+                                   sia_schedule=sia, r0=5, seed=123), backend)
+    ids = sims["mOPV2"].pars.strain_ids
+    s2, n2, v2 = ids["Sabin2"], ids["nOPV2"], ids["VDPV2"]
+    rs, rn = sims["mOPV2"].results, sims["nOPV2"].results
+    assert rs.E_by_strain[:, :, s2].sum() > 0 and rs.I_by_strain[:, :, s2].sum() > 0
+    assert rn.E_by_strain[:, :, n2].sum() > 0 and rn.I_by_strain[:, :, n2].sum() > 0
+    day = 9
+    assert rs.E_by_strain[day, :, s2].sum() > rn.E_by_strain[day, :, n2].sum() > 0
+    post = slice(16, 90)
+    assert rn.new_exposed_by_strain[post, :, n2].sum() < rs.new_exposed_by_strain[post, :, s2].sum()
+    assert rs.E_by_strain[:, :, v2].sum() == 0 and rs.E_by_strain[:, :, n2].sum() == 0
+    assert rn.E_by_strain[:, :, v2].sum() == 0 and rn.E_by_strain[:, :, s2].sum() == 0
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_new_exposed_by_strain_results(backend):
+    """tests/test_strain_transmission.py:491-535: new_exposed is the sum over
+    strains of new_exposed_by_strain, and at least the SIA's share
+    (sia_new_exposed_by_strain).  The reference runs two years of Sokoto;
+    a synthetic 8-node population with RI off and SIAs every 180 days here."""
+    from laser_polio_gb300 import synthetic
+
+    sim = synthetic.nigeria_like(n_agents=80_000, n_nodes=8, dur=400, seed=42)
+    sim.pars.vx_prob_ri = np.zeros(8)
+    run(sim, backend)
+    r = sim.results
+    assert r.new_exposed.sum() > 0 and r.sia_new_exposed_by_strain.sum() > 0
+    assert np.all(r.new_exposed == r.new_exposed_by_strain.sum(axis=2))
+    assert np.all(r.new_exposed >= r.sia_new_exposed_by_strain.sum(axis=2))
