@@ -849,3 +849,68 @@ def test_new_exposed_by_strain_results(backend):
     assert r.new_exposed.sum() > 0 and r.sia_new_exposed_by_strain.sum() > 0
     assert np.all(r.new_exposed == r.new_exposed_by_strain.sum(axis=2))
     assert np.all(r.new_exposed >= r.sia_new_exposed_by_strain.sum(axis=2))
+
+
+def _paralysis_sim(ipv):
+    """tests/test_diseasestate_abm.py:544-610: a million agents, all
+    infected, one day exposed and one infectious, DiseaseState and
+    Transmission only, 60 days."""
+    pars = PropertySet(
+        {
+            "start_date": lp.date("2020-01-01"),
+            "dur": 60,
+            "init_pop": np.array([500000, 500000]),
+            "cbr": np.array([0]),
+            "r0_scalars": np.array([1.0]),
+            "init_immun": 0.0,
+            "init_prev": 1.0,
+            "dur_exp": lp.constant(value=1),
+            "dur_inf": lp.constant(value=1),
+            "p_paralysis": 0.0005,
+            "stop_if_no_cases": False,
+            "seed": 13,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.DiseaseState_ABM, lp.Transmission_ABM]
+    if ipv:
+        sim.people.ipv_protected[:] = 1
+    return sim
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_paralysis_fraction(backend):
+    """Without IPV everyone becomes potentially paralysed and 1/2000 are
+    paralysed (the running totals equal the sums of the new counts); with
+    IPV protection nobody is either."""
+    n = 1_000_000
+    r = run(_paralysis_sim(ipv=False), backend).results
+    pot, par = int(np.sum(r.potentially_paralyzed[-1])), int(np.sum(r.paralyzed[-1]))
+    assert np.sum(r.new_potentially_paralyzed) == pot and np.sum(r.new_paralyzed) == par
+    assert np.isclose(pot / n, 1.0, atol=0.05) and np.isclose(par / n, 0.0005, atol=0.001), (pot, par)
+    r = run(_paralysis_sim(ipv=True), backend).results
+    assert np.sum(r.potentially_paralyzed[-1]) == 0 and np.sum(r.paralyzed[-1]) == 0
+    assert np.sum(r.new_potentially_paralyzed) == 0 and np.sum(r.new_paralyzed) == 0
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_potential_paralysis(backend):
+    """tests/test_diseasestate_abm.py:612-680: with several strains in
+    circulation, potential paralysis never exceeds new exposures, paralysis
+    is about 1/2000 of it (within 17), and only the paralytic strain (VDPV2)
+    marks agents potentially paralysed.  The reference runs two years of
+    Zamfara; a synthetic 10-node population with SIAs (vaccine strains)
+    and RI off here."""
+    from laser_polio_gb300 import synthetic
+
+    sim = synthetic.nigeria_like(n_agents=300_000, n_nodes=10, dur=540, seed=1)
+    sim.pars.vx_prob_ri = np.zeros(10)
+    run(sim, backend)
+    r, p = sim.results, sim.people
+    n = p.count
+    assert len(np.unique(p.strain[:n][p.disease_state[:n] > 0])) > 1
+    assert np.sum(r.new_potentially_paralyzed) <= np.sum(r.new_exposed)
+    assert np.isclose(np.sum(r.new_potentially_paralyzed) / 2000, np.sum(r.new_paralyzed), atol=17)
+    paralytic = p.strain[:n] == 0
+    assert np.isin(p.potentially_paralyzed[:n][paralytic], [-1, 0, 1]).all()
+    assert np.isin(p.potentially_paralyzed[:n][~paralytic], [-1]).all()
