@@ -914,3 +914,57 @@ def test_potential_paralysis(backend):
     paralytic = p.strain[:n] == 0
     assert np.isin(p.potentially_paralyzed[:n][paralytic], [-1, 0, 1]).all()
     assert np.isin(p.potentially_paralyzed[:n][~paralytic], [-1]).all()
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_progression_with_transmission(backend):
+    """tests/test_diseasestate_abm.py:126-256: 150 agents, r0 = 999, two
+    days exposed and one infectious: the initial counts, then S, E, I, R
+    day by day exactly as the tick order implies (exposures at the end of
+    day 1, recoveries on day 2, the new cohort infectious on day 4 and
+    recovered on day 5), and the final columns agree with day 6's row."""
+    pars = PropertySet(
+        {
+            "start_date": lp.date("2020-01-01"),
+            "dur": 6,
+            "init_pop": np.array([100, 50]),
+            "cbr": np.array([30, 25]),
+            "r0_scalars": np.array([0.5, 2.0]),
+            "init_immun": 0.8,
+            "init_prev": 0.1,
+            "dur_exp": lp.constant(value=2),
+            "dur_inf": lp.constant(value=1),
+            "p_paralysis": 1 / 2000,
+            "r0": 999,
+            "risk_mult_var": 4.0,
+            "corr_risk_inf": 0.8,
+            "seasonal_amplitude": 0.125,
+            "seasonal_peak_doy": 180,
+            "distances": np.array([[0, 1], [1, 0]]),
+            "gravity_k": 0.5,
+            "gravity_a": 1,
+            "gravity_b": 1,
+            "gravity_c": 2.0,
+            "max_migr_frac": 0.01,
+            "stop_if_no_cases": False,
+            "seed": 21,
+        }
+    )
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.DiseaseState_ABM, lp.Transmission_ABM, lp.VitalDynamics_ABM]
+    ds = sim.people.disease_state[: sim.people.count]
+    s0, e0, i0, r0 = (int(np.sum(ds == k)) for k in range(4))
+    tot = sim.pars.init_pop.sum()
+    assert np.isclose(s0, tot * 0.2 * 0.9, atol=10) and e0 == 0
+    assert np.isclose(i0, tot * 0.1, atol=5) and np.isclose(r0, tot * 0.8 * 0.9, atol=5)
+    run(sim, backend)
+    S, E, I, R = (getattr(sim.results, k).sum(axis=1) for k in "SEIR")
+    assert (S[0], E[0], I[0], R[0]) == (s0, e0, i0, r0)
+    assert S[1] < S[0] and E[1] > 0 and I[1] == I[0] and R[1] == R[0]
+    assert S[2] == S[1] and E[2] == E[1] and I[2] == 0 and R[2] == I[1] + R[1]
+    assert S[3] == S[2] and E[3] == E[2] and I[3] == 0 and R[3] == R[2]
+    assert S[4] == S[3] - E[4] and I[4] == E[3] and R[4] == R[3]
+    assert S[5] == S[4] and E[5] == E[4] and I[5] == 0 and R[5] == R[4] + I[4]
+    assert S[6] == S[5] and E[6] == E[5] and I[6] == 0 and R[6] == R[5]
+    ds = sim.people.disease_state[: sim.people.count]
+    assert tuple(int(np.sum(ds == k)) for k in range(4)) == (S[6], E[6], I[6], R[6])
