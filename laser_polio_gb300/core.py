@@ -125,6 +125,11 @@ class LaserFrame:
     def _set_count(self, n: int):
         self._count = int(n)
 
+    def __len__(self) -> int:
+        """The active count, as laser_core's LaserFrame (len(sim.people) in
+        tests/test_seir_abm_init.py:25)."""
+        return self._count
+
     def add_scalar_property(self, name, dtype=np.uint32, default=0):
         setattr(self, name, np.full(self._capacity, default, dtype=dtype))
 
