@@ -75,3 +75,25 @@ def test_time_to_paralysis():
     assert np.isclose(dist.mean(), 12.5, atol=3) and np.isclose(dist.std(), 3.5, atol=3)
     assert np.isclose(p_timer.mean() + e_timer.mean(), 12.5, atol=3)
     assert np.isclose(p_timer.std(), 3.5, atol=3)
+
+
+def test_component_columns_and_result_arrays():
+    """tests/test_vital_dynamics.py:27-34, tests/test_interventions.py:41-46,
+    tests/test_strain_transmission.py:58-83: the columns and result arrays
+    the components add, the strain result shapes and the strain ids."""
+    from oracle_backend import run_with_oracle
+
+    pars = PropertySet({"start_date": lp.date("2019-01-01"), "dur": 10, "init_pop": np.array([10000, 10000]),
+                        "cbr": np.array([30, 25]), "init_prev": np.array([0.001, 0.0]), "stop_if_no_cases": False,
+                        "seed": 5})
+    sim = lp.SEIR_ABM(pars)
+    sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.RI_ABM, lp.SIA_ABM, lp.Transmission_ABM]
+    for name in ("date_of_birth", "date_of_death", "ri_timer"):
+        assert hasattr(sim.people, name), name
+    for name in ("births", "deaths", "ri_vaccinated"):
+        assert hasattr(sim.results, name), name
+    run_with_oracle(sim)
+    nt, nn, ns = sim.results.I_by_strain.shape
+    assert (nt, nn, ns) == (sim.pars.dur + 1, len(sim.pars.init_pop), len(sim.pars.strain_ids))
+    assert sim.results.E_by_strain.shape == sim.results.I_by_strain.shape
+    assert sim.pars.strain_ids["VDPV2"] == 0 and sim.pars.strain_ids["Sabin2"] == 1 and sim.pars.strain_ids["nOPV2"] == 2
