@@ -968,3 +968,58 @@ def test_progression_with_transmission(backend):
     assert S[6] == S[5] and E[6] == E[5] and I[6] == 0 and R[6] == R[5]
     ds = sim.people.disease_state[: sim.people.count]
     assert tuple(int(np.sum(ds == k)) for k in range(4)) == (S[6], E[6], I[6], R[6])
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_radiation_spread(backend):
+    """tests/test_migration.py:12-70: with a radiation network, infection
+    seeded in one node stays there at k = 1e-5, reaches more nodes at k =
+    1e-2, and at least 2 nodes more again at k = 1e-1 (means over the
+    reference's seeds 1000-1004).  The reference runs Zamfara's 14 LGAs at a
+    tenth of their population, with the immunity its data give; 14 synthetic
+    nodes of the same total (lognormal sizes, coordinates in a 200 km square)
+    with 80% immune here (fully susceptible, R0 = 14 grows an outbreak that
+    seeds a neighbour even at k = 1e-5).  Spread with these seeds: 1, 6-9
+    and 13-14 nodes."""
+    n = 14
+    rng = np.random.default_rng(77)
+    raw = rng.lognormal(np.log(3.2e4), 0.5, n)
+    pops = np.maximum(1, np.round(raw / raw.sum() * 450_000)).astype(np.int64)
+    xy = rng.uniform(0, 200, (n, 2))
+    dist = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
+    init_prev = np.zeros(n)
+    init_prev[0] = 0.01
+
+    def spread(k_log10, seed):
+        pars = PropertySet(
+            {
+                "seed": seed,
+                "start_date": lp.date("2018-01-01"),
+                "dur": 30,
+                "init_pop": pops,
+                "cbr": np.full(n, 35.0),
+                "r0_scalars": np.ones(n),
+                "distances": dist,
+                "init_prev": init_prev,
+                "init_immun": 0.8,
+                "r0": 14,
+                "migration_method": "radiation",
+                "radiation_k_log10": k_log10,
+                "max_migr_frac": 1.0,
+                "vx_prob_ri": None,
+                "vx_prob_sia": None,
+                "stop_if_no_cases": False,
+            }
+        )
+        sim = lp.SEIR_ABM(pars)
+        sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.Transmission_ABM]
+        run(sim, backend)
+        return int(np.count_nonzero(np.sum(sim.results.I, axis=0) > 0))
+
+    seeds = range(1000, 1005)
+    zero = np.mean([spread(-5, s) for s in seeds])
+    low = np.mean([spread(-2, s) for s in seeds])
+    high = np.mean([spread(-1, s) for s in seeds])
+    assert zero == 1.0, zero
+    assert low > zero, (low, zero)
+    assert high >= low + 2, (high, low)
