@@ -7,7 +7,12 @@ C ABI in include/lpg.h.  The parameter contract (pars), the Distribution
 objects and the sim.results arrays are the reference's.
 """
 
+from pathlib import Path
+
 __version__ = "0.1.0"
+
+# the project root, as laser_polio.root (tests patch it to find data files)
+root = Path(__file__).resolve().parents[1]
 
 from .core import LaserFrame
 from .core import PropertySet
@@ -33,6 +38,15 @@ from .utils import date
 from .utils import daterange
 from .utils import get_doy
 from .utils import get_seasonality
+from .utils import save_sim_results
+
+
+def count_SEIRP(*args, **kwargs):
+    """laser_polio.count_SEIRP (model.py:869-899) on the GPU: see
+    laser_polio_gb300.ops.count_SEIRP (imported on first use, with torch)."""
+    from .ops import count_SEIRP as _count
+
+    return _count(*args, **kwargs)
 
 __all__ = [
     "RI_ABM",
@@ -45,6 +59,7 @@ __all__ = [
     "Transmission_ABM",
     "VitalDynamics_ABM",
     "constant",
+    "count_SEIRP",
     "create_cumulative_deaths",
     "date",
     "daterange",
@@ -58,5 +73,7 @@ __all__ = [
     "lognormal_int",
     "normal",
     "poisson",
+    "root",
+    "save_sim_results",
     "uniform",
 ]
