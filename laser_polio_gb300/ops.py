@@ -243,3 +243,45 @@ class IncidencePlan:
 
     def __del__(self):
         self.close()
+
+
+_AUTOGRAD_SCALARS = ("R", "amp", "peak", "k", "a", "b", "c")
+
+
+class ExpectedIncidence(torch.autograd.Function):
+    """lam [T, G] of an IncidencePlan as a differentiable function of the
+    scalars R, amp, peak, k, a, b, c (0-dim float64 tensors) and r0s [G].
+    forward() evaluates the map; backward() runs the plan's reverse pass
+    with the incoming dL/dlam (one lpg_incidence_plan_eval each), so any
+    torch loss over lam and any torch optimiser can drive a calibration.
+    Use through expected_incidence_torch."""
+
+    @staticmethod
+    def forward(ctx, plan, max_frac, R, amp, peak, k, a, b, c, r0s):
+        values = (R, amp, peak, k, a, b, c)
+        params = {name: float(v) for name, v in zip(_AUTOGRAD_SCALARS, values)}
+        params["max_frac"] = float(max_frac)
+        params["r0s"] = r0s.detach().to("cpu", torch.float64).contiguous().numpy()
+        out = plan.evaluate(params, lam=True, loss=False, grad=False)
+        ctx.plan, ctx.params, ctx.device = plan, params, r0s.device
+        return torch.as_tensor(out["lam"], dtype=torch.float64, device=r0s.device)
+
+    @staticmethod
+    def backward(ctx, g_lam):
+        g = g_lam.detach().to("cpu", torch.float64).contiguous().numpy()
+        gr = ctx.plan.evaluate(ctx.params, g, loss=False, network_grad=False)["grad"]
+        scalars = [torch.tensor(gr[name], dtype=torch.float64, device=ctx.device) for name in _AUTOGRAD_SCALARS]
+        return (None, None, *scalars, torch.as_tensor(gr["r0s"], dtype=torch.float64, device=ctx.device))
+
+
+def expected_incidence_torch(plan, params: dict) -> torch.Tensor:
+    """lam = ExpectedIncidence.apply over ``params``: R, amp, peak, k, a, b,
+    c as 0-dim tensors (or floats, then constant), r0s as a [G] tensor (or
+    array), and max_frac a float.  Gradients flow to every tensor that
+    requires them."""
+
+    def t(x):
+        return x if isinstance(x, torch.Tensor) else torch.tensor(x, dtype=torch.float64)
+
+    args = [t(params[name]) for name in _AUTOGRAD_SCALARS]
+    return ExpectedIncidence.apply(plan, float(params["max_frac"]), *args, t(params["r0s"]))

@@ -343,12 +343,18 @@ class _OraclePlan:
     def __init__(self, inp, target):
         self.inp, self.target, self.calls = inp, target, 0
 
-    def evaluate(self, params, g=None, *, network_grad=True):
+    def evaluate(self, params, g=None, *, lam=False, loss=None, grad=True, network_grad=True):
         self.calls += 1
         x = dict(self.inp, **{k: params[k] for k in ("R", "amp", "peak", "k", "a", "b", "c", "max_frac")},
                  r0s=params["r0s"])
-        _, loss, grads = _oracle_loss_grad(x, self.target)
-        return {"loss": loss, "grad": grads}
+        lam_v, _ = I.incidence(x)
+        out = {"lam": lam_v} if lam else {}
+        r = np.log1p(lam_v) - np.log1p(self.target)
+        if self.target is not None if loss is None else loss:
+            out["loss"] = float((r * r).sum())
+        if grad:
+            out["grad"] = I.incidence(x, 2.0 * r / (1.0 + lam_v) if g is None else g)[1]
+        return out
 
 
 def test_fit_incidence_recovers_the_parameters_of_the_target():
@@ -375,3 +381,63 @@ def test_fit_incidence_recovers_the_parameters_of_the_target():
     np.testing.assert_allclose(fit2["r0s"], r0_true, rtol=1e-5)
     with pytest.raises(ValueError, match="unknown"):
         fit_incidence(plan, start, free=("R0",))
+
+
+def test_torch_autograd_function_gives_the_adjoints_gradient():
+    """ops.ExpectedIncidence (a torch.autograd.Function over a plan): the
+    calibration loss written in torch and backpropagated gives the oracle's
+    gradient (relative 1e-12), and torch.autograd.gradcheck passes.  Every
+    node-tick gets some local infectivity: where only mixing reaches a node,
+    the rate is ~1e-10 and 1 - exp(-r) (the reference's form) cancels to
+    ~1e-6 relative, which gradcheck's numerical Jacobian would inherit."""
+    import torch
+
+    inp = I.random_inputs(6, 5, 2, seed=13)
+    inp["beta"] = inp["beta"] + 1.0
+    target = I.incidence(dict(inp, R=1.2, amp=0.3))[0]
+    plan = _OraclePlan(inp, target)
+    params = {n: torch.tensor(float(inp[n]), dtype=torch.float64, requires_grad=True) for n in SCALARS}
+    params["r0s"] = torch.tensor(inp["r0s"], dtype=torch.float64, requires_grad=True)
+    params["max_frac"] = inp["max_frac"]
+    lam = ops.expected_incidence_torch(plan, params)
+    loss = ((torch.log1p(lam) - torch.log1p(torch.as_tensor(target))) ** 2).sum()
+    loss.backward()
+    _, want_loss, want = _oracle_loss_grad(inp, target)
+    assert abs(loss.item() - want_loss) <= 1e-12 * want_loss
+    for n in SCALARS:
+        _close(params[n].grad.item(), want[n], 1e-12, n)
+    _close(params["r0s"].grad.numpy(), want["r0s"], 1e-12, "r0s")
+
+    def f(R, amp, r0s):
+        return ops.expected_incidence_torch(plan, dict(params, R=R, amp=amp, r0s=r0s))
+
+    args = (torch.tensor(1.1, dtype=torch.float64, requires_grad=True),
+            torch.tensor(0.35, dtype=torch.float64, requires_grad=True),
+            torch.tensor(inp["r0s"], dtype=torch.float64, requires_grad=True))
+    # eps 1e-4: at 1e-6 the central differences carry ~1e-5 of rounding noise
+    assert torch.autograd.gradcheck(f, args, eps=1e-4, atol=1e-6, rtol=1e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_torch_autograd_function_on_a_plan():
+    """ExpectedIncidence over a device plan: a torch loss backpropagated
+    through it gives the oracle's gradient (relative 1e-9)."""
+    import torch
+
+    inp = I.random_inputs(30, 40, 3, seed=17)
+    target = I.incidence(dict(inp, R=1.2, amp=0.3))[0]
+    plan = ops.IncidencePlan(inp)
+    try:
+        params = {n: torch.tensor(float(inp[n]), dtype=torch.float64, requires_grad=True) for n in SCALARS}
+        params["r0s"] = torch.tensor(inp["r0s"], dtype=torch.float64, requires_grad=True)
+        params["max_frac"] = inp["max_frac"]
+        lam = ops.expected_incidence_torch(plan, params)
+        loss = ((torch.log1p(lam) - torch.log1p(torch.as_tensor(target))) ** 2).sum()
+        loss.backward()
+    finally:
+        plan.close()
+    _, want_loss, want = _oracle_loss_grad(inp, target)
+    assert abs(loss.item() - want_loss) <= 1e-11 * want_loss
+    for n in SCALARS:
+        _close(params[n].grad.item(), want[n], 1e-9, n)
+    _close(params["r0s"].grad.numpy(), want["r0s"], 1e-9, "r0s")
