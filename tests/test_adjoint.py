@@ -349,7 +349,7 @@ class _OraclePlan:
                  r0s=params["r0s"])
         lam_v, _ = I.incidence(x)
         out = {"lam": lam_v} if lam else {}
-        r = np.log1p(lam_v) - np.log1p(self.target)
+        r = None if self.target is None else np.log1p(lam_v) - np.log1p(self.target)
         if self.target is not None if loss is None else loss:
             out["loss"] = float((r * r).sum())
         if grad:
