@@ -441,3 +441,22 @@ def test_gpu_torch_autograd_function_on_a_plan():
     for n in SCALARS:
         _close(params[n].grad.item(), want[n], 1e-9, n)
     _close(params["r0s"].grad.numpy(), want["r0s"], 1e-9, "r0s")
+
+
+def test_oracle_recording_must_be_asked_before_start():
+    """lpo_record_aggregates after the start is refused, and reading
+    aggregates that were not recorded raises (as the engine's calls)."""
+    from laser_polio_gb300 import synthetic
+    from laser_polio_gb300.engine import make_desc
+    from oracle.oracle import OracleSim
+
+    params, cols = synthetic.bundle(kind="zamfara", n_agents=5_000, dur=5, seed=1)
+    desc, keep = make_desc(params)
+    o = OracleSim(desc, keepalive=keep)
+    o.bind_columns(cols)
+    o.start()
+    with pytest.raises(RuntimeError, match="after start"):
+        o.record_aggregates()
+    with pytest.raises(RuntimeError, match="not recorded"):
+        o.read_aggregates()
+    o.close()

@@ -111,3 +111,27 @@ def test_errors(tmp_path):
     except ImportError:
         with pytest.raises(ImportError, match="pandas"):
             save_sim_results(_fake_sim(3, 2), tmp_path / "x.h5")
+
+
+def test_c_entry_point_rejects_bad_arguments(tmp_path):
+    """lpg_write_results_csv's own checks (LPG_ERR_ARG = -1 with a message)."""
+    import ctypes as C
+
+    from laser_polio_gb300 import _lib
+
+    lib = _lib.load()
+    names = (C.c_char_p * 1)(b"S")
+    dates = (C.c_char_p * 1)(b"2019-01-01")
+    dots = (C.c_char_p * 1)(b"A:B:C:D")
+    field = np.zeros(1, np.int32)
+    fields = (C.c_void_p * 1)(field.ctypes.data)
+    path = str(tmp_path / "x.csv").encode()
+    assert lib.lpg_write_results_csv(None, 1, 1, dates, dots, 1, names, fields) == -1
+    assert b"null path" in lib.lpg_op_last_error()
+    assert lib.lpg_write_results_csv(path, -1, 1, dates, dots, 1, names, fields) == -1
+    assert lib.lpg_write_results_csv(path, 1, 1, dates, dots, 65, names, fields) == -1
+    assert b"bad sizes" in lib.lpg_op_last_error()
+    assert lib.lpg_write_results_csv(path, 1, 1, None, dots, 1, names, fields) == -1
+    assert b"NULL" in lib.lpg_op_last_error()
+    assert lib.lpg_write_results_csv(path, 1, 1, dates, dots, 1, names, fields) == 0
+    assert (tmp_path / "x.csv").read_text() == "timestep,date,node,dot_name,S\n0,2019-01-01,0,A:B:C:D,0\n"
