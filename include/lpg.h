@@ -410,16 +410,19 @@ int lpg_expected_incidence(const lpg_incidence_in* in, double* lam_out, const do
 
 /* save_sim_results' table (utils.py:689-786) as CSV, written by host threads:
  * one row per (timestep, node), timestep-major, with the columns timestep,
- * date, node, dot_name and then field_names[0..n_fields); the format of
- * pandas' DataFrame.to_csv(index=False) ('\n' rows, QUOTE_MINIMAL strings).
- * dates [nt] and dot_names [n_nodes] are NUL-terminated strings; fields[k]
- * is an int32 array [nt][n_nodes].  Host memory only; needs no GPU.  The
- * DataFrame the reference also returns and its summary groupings
- * (utils.py:1040-1160) are not built here. */
+ * date, node, dot_name, then field_names[0..n_fields), then the summary
+ * groupings' string columns (utils.py:1040-1160): n_tick_cols by tick
+ * (tick_cols[c * nt + t], e.g. time_period) and then n_node_cols by node
+ * (node_cols[c * n_nodes + n], e.g. adm0, adm1, adm01, region).  The format
+ * of pandas' DataFrame.to_csv(index=False) ('\n' rows, QUOTE_MINIMAL
+ * strings).  dates [nt] and dot_names [n_nodes] are NUL-terminated strings;
+ * fields[k] is an int32 array [nt][n_nodes].  Host memory only; needs no GPU. */
 #define LPG_EXPORT_MAX_FIELDS 64
 int lpg_write_results_csv(const char* path, int32_t nt, int32_t n_nodes, const char* const* dates,
                           const char* const* dot_names, int32_t n_fields, const char* const* field_names,
-                          const int32_t* const* fields);
+                          const int32_t* const* fields, int32_t n_tick_cols, const char* const* tick_col_names,
+                          const char* const* tick_cols, int32_t n_node_cols, const char* const* node_col_names,
+                          const char* const* node_cols);
 
 const char* lpg_op_last_error(void);
 

@@ -53,7 +53,9 @@ SIGNATURES = {
     "lpg_incidence_plan_destroy": (None, [C.c_void_p]),
     "lpg_write_results_csv": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.POINTER(C.c_char_p),
                                         C.POINTER(C.c_char_p), C.c_int32, C.POINTER(C.c_char_p),
-                                        C.POINTER(C.c_void_p)]),
+                                        C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_char_p),
+                                        C.POINTER(C.c_char_p), C.c_int32, C.POINTER(C.c_char_p),
+                                        C.POINTER(C.c_char_p)]),
     "lpg_op_last_error": (C.c_char_p, []),
 }
 

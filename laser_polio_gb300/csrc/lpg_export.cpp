@@ -8,6 +8,9 @@
  * of the column names, ',' between fields and '\n' after every row.
  * Integers are written in decimal.  Strings are quoted only when they hold
  * ',', '"', '\n' or '\r', with inner quotes doubled (csv.QUOTE_MINIMAL).
+ * After the integer result fields come the summary groupings' string
+ * columns (utils.py:1040-1160): per-tick ones (time_period) and then per-node
+ * ones (adm0, adm1, adm01, region), in the order pandas appends them.
  * At the Nigeria scale the table has 2555 x 774 = 2.0e6 rows.  Here, blocks
  * of timesteps are formatted in parallel by host threads and written to the
  * file in order.
@@ -51,9 +54,16 @@ void put_int(std::string& out, int64_t v) {
   while (n) out += buf[--n];
 }
 
+/* String columns by tick ([col][t]) and by node ([col][n]), quoted once. */
+struct StrCols {
+  int32_t n_tick = 0, n_node = 0;
+  std::vector<std::string> tick, node;
+};
+
 /* Rows of timesteps [t0, t1) into out. */
 void format_rows(std::string& out, int32_t t0, int32_t t1, int32_t n_nodes, const std::vector<std::string>& dates,
-                 const std::vector<std::string>& names, int32_t n_fields, const int32_t* const* fields) {
+                 const std::vector<std::string>& names, int32_t n_fields, const int32_t* const* fields,
+                 const StrCols& sc, int32_t nt) {
   for (int32_t t = t0; t < t1; ++t) {
     for (int32_t n = 0; n < n_nodes; ++n) {
       const size_t q = (size_t)t * n_nodes + n;
@@ -68,13 +78,23 @@ void format_rows(std::string& out, int32_t t0, int32_t t1, int32_t n_nodes, cons
         out += ',';
         put_int(out, fields[k][q]);
       }
+      for (int32_t c = 0; c < sc.n_tick; ++c) {
+        out += ',';
+        out += sc.tick[(size_t)c * nt + t];
+      }
+      for (int32_t c = 0; c < sc.n_node; ++c) {
+        out += ',';
+        out += sc.node[(size_t)c * n_nodes + n];
+      }
       out += '\n';
     }
   }
 }
 
 int write_csv(const char* path, int32_t nt, int32_t n_nodes, const char* const* dates, const char* const* dot_names,
-              int32_t n_fields, const char* const* field_names, const int32_t* const* fields) {
+              int32_t n_fields, const char* const* field_names, const int32_t* const* fields, int32_t n_tick_cols,
+              const char* const* tick_col_names, const char* const* tick_cols, int32_t n_node_cols,
+              const char* const* node_col_names, const char* const* node_cols) {
   if (!path) return lpg_ops_fail(LPG_ERR_ARG, "write_results_csv: null path");
   if (nt < 0 || n_nodes < 0 || n_fields < 0 || n_fields > LPG_EXPORT_MAX_FIELDS)
     return lpg_ops_fail(LPG_ERR_ARG, "write_results_csv: bad sizes nt=%d n_nodes=%d n_fields=%d", nt, n_nodes,
@@ -84,6 +104,28 @@ int write_csv(const char* path, int32_t nt, int32_t n_nodes, const char* const* 
   for (int32_t k = 0; k < n_fields; ++k)
     if (!field_names[k] || (!fields[k] && nt > 0 && n_nodes > 0))
       return lpg_ops_fail(LPG_ERR_ARG, "write_results_csv: field %d is NULL", k);
+  if (n_tick_cols < 0 || n_node_cols < 0 || n_tick_cols + n_node_cols > LPG_EXPORT_MAX_FIELDS ||
+      (n_tick_cols > 0 && (!tick_col_names || (nt > 0 && !tick_cols))) ||
+      (n_node_cols > 0 && (!node_col_names || (n_nodes > 0 && !node_cols))))
+    return lpg_ops_fail(LPG_ERR_ARG, "write_results_csv: bad string columns (%d by tick, %d by node)", n_tick_cols,
+                        n_node_cols);
+  for (int32_t c = 0; c < n_tick_cols; ++c)
+    if (!tick_col_names[c]) return lpg_ops_fail(LPG_ERR_ARG, "write_results_csv: a column name is NULL");
+  for (int32_t c = 0; c < n_node_cols; ++c)
+    if (!node_col_names[c]) return lpg_ops_fail(LPG_ERR_ARG, "write_results_csv: a column name is NULL");
+  StrCols sc;
+  sc.n_tick = n_tick_cols;
+  sc.n_node = n_node_cols;
+  sc.tick.resize((size_t)n_tick_cols * nt);
+  sc.node.resize((size_t)n_node_cols * n_nodes);
+  for (size_t q = 0; q < sc.tick.size(); ++q) {
+    if (!tick_cols[q]) return lpg_ops_fail(LPG_ERR_ARG, "write_results_csv: a tick column value is NULL");
+    sc.tick[q] = csv_field(tick_cols[q]);
+  }
+  for (size_t q = 0; q < sc.node.size(); ++q) {
+    if (!node_cols[q]) return lpg_ops_fail(LPG_ERR_ARG, "write_results_csv: a node column value is NULL");
+    sc.node[q] = csv_field(node_cols[q]);
+  }
   std::vector<std::string> ds(nt), nm(n_nodes);
   for (int32_t t = 0; t < nt; ++t) {
     if (!dates[t]) return lpg_ops_fail(LPG_ERR_ARG, "write_results_csv: date %d is NULL", t);
@@ -99,6 +141,14 @@ int write_csv(const char* path, int32_t nt, int32_t n_nodes, const char* const* 
   for (int32_t k = 0; k < n_fields; ++k) {
     head += ',';
     head += csv_field(field_names[k]);
+  }
+  for (int32_t c = 0; c < n_tick_cols; ++c) {
+    head += ',';
+    head += csv_field(tick_col_names[c]);
+  }
+  for (int32_t c = 0; c < n_node_cols; ++c) {
+    head += ',';
+    head += csv_field(node_col_names[c]);
   }
   head += '\n';
   bool ok = fwrite(head.data(), 1, head.size(), f) == head.size();
@@ -117,7 +167,7 @@ int write_csv(const char* path, int32_t nt, int32_t n_nodes, const char* const* 
       bufs[w].clear();
       auto job = [&, w, a, b]() {
         try {
-          format_rows(bufs[w], a, b, n_nodes, ds, nm, n_fields, fields);
+          format_rows(bufs[w], a, b, n_nodes, ds, nm, n_fields, fields, sc, nt);
         } catch (...) {
           failed[w] = 1;
         }
@@ -142,9 +192,13 @@ int write_csv(const char* path, int32_t nt, int32_t n_nodes, const char* const* 
 
 extern "C" int lpg_write_results_csv(const char* path, int32_t nt, int32_t n_nodes, const char* const* dates,
                                      const char* const* dot_names, int32_t n_fields, const char* const* field_names,
-                                     const int32_t* const* fields) {
+                                     const int32_t* const* fields, int32_t n_tick_cols,
+                                     const char* const* tick_col_names, const char* const* tick_cols,
+                                     int32_t n_node_cols, const char* const* node_col_names,
+                                     const char* const* node_cols) {
   try {
-    return write_csv(path, nt, n_nodes, dates, dot_names, n_fields, field_names, fields);
+    return write_csv(path, nt, n_nodes, dates, dot_names, n_fields, field_names, fields, n_tick_cols, tick_col_names,
+                     tick_cols, n_node_cols, node_col_names, node_cols);
   } catch (...) { /* allocation or thread creation failed: nothing escapes the C ABI */
     return lpg_ops_fail(LPG_ERR_NOMEM, "write_results_csv: out of host resources");
   }
