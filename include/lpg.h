@@ -424,6 +424,15 @@ int lpg_write_results_csv(const char* path, int32_t nt, int32_t n_nodes, const c
                           const char* const* tick_cols, int32_t n_node_cols, const char* const* node_col_names,
                           const char* const* node_cols);
 
+/* The radiation migration network (the reference builds it with laser_core's
+ * radiation at model.py:1252-1254; migration_method's default): out[i][j] =
+ * k p_i p_j / ((p_i + s_ij)(p_i + p_j + s_ij)), s_ij the population strictly
+ * closer to i than j without i and j, zero diagonal (pops on it when
+ * include_home).  Host arrays, row-major [n][n]; rows on host threads; no
+ * GPU.  Equal bit for bit to laser_polio_gb300.core's Python definition. */
+int lpg_radiation_network(const double* pops, const double* dist, int32_t n, double k, int32_t include_home,
+                          double* out);
+
 const char* lpg_op_last_error(void);
 
 #ifdef __cplusplus

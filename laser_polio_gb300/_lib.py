@@ -56,6 +56,8 @@ SIGNATURES = {
                                         C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_char_p),
                                         C.POINTER(C.c_char_p), C.c_int32, C.POINTER(C.c_char_p),
                                         C.POINTER(C.c_char_p)]),
+    "lpg_radiation_network": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32, C.c_double,
+                                        C.c_int32, C.POINTER(C.c_double)]),
     "lpg_op_last_error": (C.c_char_p, []),
 }
 

@@ -17,7 +17,8 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build" / "liblpg.so"
-SOURCES = [CSRC / "lpg_engine.cu", CSRC / "lpg_ops.cu", CSRC / "lpg_adjoint.cu", CSRC / "lpg_export.cpp"]
+SOURCES = [CSRC / "lpg_engine.cu", CSRC / "lpg_ops.cu", CSRC / "lpg_adjoint.cu", CSRC / "lpg_export.cpp",
+           CSRC / "lpg_network.cpp"]
 DEPS = SOURCES + [CSRC / "lpg_kernels.cuh", CSRC / "lpg_engine.cuh", CSRC / "lpg_rng.h", CSRC / "lpg_detmath.h",
                   CSRC / "lpg_ri.h", ROOT / "include" / "lpg.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"

@@ -184,7 +184,31 @@ def gravity(pops, distances, k, a, b, c):
 def radiation(pops, distances, k, include_home=False):
     """Radiation-model flows (Simini et al., Nature 484, 2012):
     k * p_i * p_j / ((p_i + s_ij) (p_i + p_j + s_ij)), s_ij = population
-    strictly closer to i than j, excluding i and j."""
+    strictly closer to i than j, excluding i and j.  Computed by the native
+    lpg_radiation_network (host threads), equal bit for bit to the
+    definition in _radiation_py."""
+    import ctypes as C
+
+    from . import _lib
+
+    p = np.ascontiguousarray(np.asarray(pops, dtype=np.float64))
+    d = np.ascontiguousarray(np.asarray(distances, dtype=np.float64))
+    n = len(p)
+    if d.shape != (n, n):
+        raise ValueError(f"radiation: distances have shape {d.shape}, expected {(n, n)}")
+    out = np.empty((n, n), dtype=np.float64)
+    lib = _lib.load()
+    dp = C.POINTER(C.c_double)
+    rc = lib.lpg_radiation_network(p.ctypes.data_as(dp), d.ctypes.data_as(dp), n, float(k), int(bool(include_home)),
+                                   out.ctypes.data_as(dp))
+    if rc != 0:
+        raise ValueError(lib.lpg_op_last_error().decode())
+    return out
+
+
+def _radiation_py(pops, distances, k, include_home=False):
+    """radiation() as a Python loop: the definition the native builder
+    follows operation for operation."""
     pops = np.asarray(pops, dtype=np.float64)
     d = np.asarray(distances, dtype=np.float64)
     n = len(pops)
