@@ -28,3 +28,30 @@ def test_radiation_rejects_bad_shapes():
         radiation(np.ones(3), np.zeros((2, 2)), 1.0)
     with pytest.raises(ValueError, match="NaN"):
         radiation(np.ones(2), np.array([[0.0, np.nan], [1.0, 0.0]]), 1.0)
+
+
+def test_gravity_and_row_normalizer_on_the_references_example():
+    """scripts/sandbox/debug_row_normalizer.py:7-32: three nodes (populations
+    99510, 595855, 263884 scaled by 1e-3; distances 4, 66, 827), k = 100,
+    a = b = 1, c = 2: gravity is k p_i p_j / d_ij^2 off the diagonal (the
+    script's own comment), and rows summing above 0.3 are scaled to 0.3, as
+    the script's manual restatement does.  Expected values computed here
+    element by element."""
+    from laser_polio_gb300.core import gravity, row_normalizer
+
+    pops = np.array([99510, 595855, 263884]) / 1e3
+    dist = np.array([[0, 4, 66], [4, 0, 827], [66, 827, 0]])
+    want = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(3):
+            if i != j:
+                want[i, j] = 100 * pops[i] * pops[j] / float(dist[i, j]) ** 2
+    got = gravity(pops, dist, 100, 1, 1, 2.0)
+    np.testing.assert_allclose(got, want, rtol=1e-15)
+    norm = row_normalizer(got, 0.3)
+    for i in range(3):
+        s = want[i].sum()
+        np.testing.assert_allclose(norm[i], want[i] * (0.3 / s) if s > 0.3 else want[i], rtol=1e-15)
+    # the script's integer network, promoted to float as its fix does
+    net = row_normalizer(np.array([[0, 6, 2], [10, 0, 13], [15, 10, 0]], dtype=float), 0.3)
+    np.testing.assert_allclose(net.sum(axis=1), [0.3, 0.3, 0.3], rtol=1e-15)
