@@ -16,8 +16,12 @@ reference's loops do).
   roofline  per-kernel CUDA-event times from a second run of the same ticks
             in profiling mode; the dominant kernel's algorithmic bytes per
             launch / its mean launch time against the measured HBM peak.
-  cpu_baseline  the C/OpenMP oracle on the machine's cores over the first ticks
-            of the same population.
+  cpu_baseline  the C/OpenMP oracle on the machine's cores over the same W + K
+            ticks of the same population (ticks W+1 .. W+K timed).
+  parity    the oracle's results and agent columns after those ticks
+            compared, every array and every slot, with the end-to-end run's.
+  full_run  the whole 2555-tick run replayed on the device, and the mean
+            time of each kind of tick (plain, births, RI, SIA days).
 
 python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
@@ -49,8 +53,8 @@ B_SIA = 5.0  # date_of_birth, chronically_missed on SIA days
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2548)
-    ap.add_argument("--warmup", type=int, default=7)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--agents", type=float, default=2.2e8)
     ap.add_argument("--nodes", type=int, default=774)
@@ -59,6 +63,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--no-full-run", action="store_true")
+    ap.add_argument("--parity-ticks", type=int, default=60,
+                    help="the oracle's parity leg runs min(W + K, this) ticks of the same population")
     ap.add_argument("--out", default=None)
     ap.add_argument("--batch", type=int, default=0,
                     help="instead: R calibration replicates (730 ticks) batched in one handle vs run one by one")
@@ -123,8 +130,7 @@ def sweep_b_bytes(params, t):
 NCU_TRAFFIC_PER_UNIT = {"k_select": ("sel_targets", 1071.0, 0.0)}
 NCU_TRAFFIC_SOURCE = {
     "k_select": "ncu DRAM read+write of k_sel_locate + k_sel_claim + k_sel_rounds per target located, "
-                "tick 151 of the 5e7-agent case (profiles/tick_kernels_nigeria_5e7_t151.md), "
-                "times the targets of the timed ticks",
+                "on tick 151 of the 5e7-agent Nigeria-like case, times the targets of the timed ticks",
 }
 
 
@@ -293,8 +299,19 @@ def result_arrays(params, pinned=False):
     return out
 
 
-def run_cpu_baseline(params, cols, warmup, steps, seconds):
-    """The oracle over the first ticks of the same population."""
+def workload_config(params, W, K, ws=1):
+    """The `config` of both arms' lines: the same workload and the same ticks."""
+    return {"workload": f"nigeria_like {params['n_nodes']} nodes x {params['count']:.3g} agents, capacity +30%, "
+                        f"ticks {W + 1}-{W + K} of a {params['nt'] - 1}-tick run",
+            "agents": params["count"], "capacity": params["capacity"], "nodes": params["n_nodes"],
+            "l2": "state columns larger than L2 (no flush needed)", "replicas": ws}
+
+
+def oracle_leg(params, cols, warmup, steps, seconds=None):
+    """The oracle (C/OpenMP restatement of the reference's loops) over ticks
+    1 .. warmup+steps of the same population: `warmup` untimed ticks, then up
+    to `steps` timed ticks (fewer only when `seconds` runs out).  Returns the
+    timing and the open OracleSim for the parity comparison."""
     from laser_polio_gb300.engine import make_desc
     from oracle.oracle import OracleSim
     from oracle.oracle import num_threads
@@ -310,11 +327,35 @@ def run_cpu_baseline(params, cols, warmup, steps, seconds):
         o.step(1)
         done += 1
         agent_ticks += o.state().count
-        if time.perf_counter() - t0 > seconds:
+        if seconds is not None and time.perf_counter() - t0 > seconds:
             break
     dt = time.perf_counter() - t0
-    o.close()
-    return {"value": agent_ticks / dt, "ticks": done, "seconds": dt, "cores": num_threads(), "warmup": warmup}
+    return {"value": agent_ticks / dt, "ticks": done, "seconds": dt, "cores": num_threads(), "warmup": warmup,
+            "oracle": o, "keep": keep}
+
+
+def compare_with_oracle(o, res_gpu, read_gpu_column, params, count):
+    """Every result array and every agent column of the GPU run against the
+    oracle's after the same ticks; columns one at a time through a reusable
+    buffer (the oracle keeps its own copy of the table)."""
+    from laser_polio_gb300 import _abi
+
+    mismatch = []
+    res_o = result_arrays(params)
+    o.read_results(res_o)
+    for name, a in res_o.items():
+        if not np.array_equal(a, res_gpu[name]):
+            mismatch.append(f"result {name}: {int((a != res_gpu[name]).sum())} entries")
+    n_cols = 0
+    for name, _, dtype in _abi.COLUMN_FIELDS:
+        buf = np.empty(count, dtype=dtype)
+        o.read_columns({name: buf})
+        gpu = read_gpu_column(name, dtype)
+        n_cols += 1
+        if not np.array_equal(buf, gpu[:count]):
+            mismatch.append(f"column {name}: {int((buf != gpu[:count]).sum())} slots")
+    return {"bit_exact": not mismatch, "results_compared": len(res_o), "columns_compared": n_cols,
+            "slots_compared": int(count), "mismatches": mismatch[:8]}
 
 
 def reference_arm(args):
@@ -322,9 +363,12 @@ def reference_arm(args):
     if rank != 0:
         return
     params, cols = make_bundle(args, 0, pinned=False)
-    warm = args.warmup
-    cpu = run_cpu_baseline(params, cols, warm, args.steps, args.cpu_seconds)
-    sample = (f"first {cpu['ticks']} ticks after {warm} untimed of the {params['count']:.3g}-agent, "
+    W, K = args.warmup, args.steps
+    if W + K > params["nt"] - 1:
+        K = max(1, params["nt"] - 1 - W)
+    cpu = oracle_leg(params, cols, W, K, args.cpu_seconds)
+    cpu["oracle"].close()
+    sample = (f"ticks {W + 1}-{W + cpu['ticks']} after {W} untimed of the {params['count']:.3g}-agent, "
               f"{params['n_nodes']}-node population ({cpu['seconds']:.1f} s)")
     line = {
         "impl": "reference",
@@ -333,20 +377,85 @@ def reference_arm(args):
         "unit": "agent-ticks/s",
         "n_gpus": ws,
         "steps": cpu["ticks"],
-        "warmup": warm,
+        "warmup": W,
+        "ms_per_step": cpu["seconds"] / max(1, cpu["ticks"]) * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "int8/int32 state, f64 node FOI",
         "data": "synthetic (seeded numpy, Nigeria-scale shapes)",
-        "config": {"workload": f"nigeria_like {params['n_nodes']} nodes x {params['count']:.3g} agents, "
-                               "capacity +30%, 2555-tick run",
-                   "agents": params["count"], "nodes": params["n_nodes"]},
+        "config": workload_config(params, W, K, ws),
         "cpu_baseline": {"value": cpu["value"], "unit": "agent-ticks/s", "cores": cpu["cores"], "kind": "port",
                          "sample": sample},
         "e2e": {"value": cpu["value"], "unit": "agent-ticks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def tick_kind(params, t):
+    """plain / vd / vd+ri / sia ... : the components that act on tick t
+    besides the every-tick ones."""
+    parts = []
+    if t % params["vd_step"] == 0:
+        parts.append("vd")
+    if params["ri_enabled"] and t % params["ri_step"] == 0:
+        parts.append("ri")
+    if any(e[0] == t for e in params["sia"]):
+        parts.append("sia")
+    return "+".join(parts) or "plain"
+
+
+def full_run(desc, cols, params, dev):
+    """The whole run on the device: once replayed as the engine runs it
+    (graphs of 8 ticks), timed between CUDA events on its stream; once tick by
+    tick with an event pair per tick, for the mean time of each kind of tick.
+    Returns (line entry, the handle's end-of-run results)."""
+    import torch
+
+    from laser_polio_gb300._lib import Handle
+
+    n = params["nt"] - 1
+    h = Handle([desc], device=dev)
+    h.bind_columns(0, cols)
+    h.start()
+    h.sync()
+    stream = torch.cuda.ExternalStream(h.cuda_stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    h.step(n)
+    e1.record(stream)
+    h.sync()
+    ms_all = e0.elapsed_time(e1)
+    res = result_arrays(params)
+    h.read_results(0, res)
+    h.close()
+    cnt = counts_per_tick(params, res["births"])
+    at = float(cnt[1 : n + 1].sum())
+
+    h = Handle([desc], device=dev)
+    h.bind_columns(0, cols)
+    h.start()
+    h.sync()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(n + 1)]
+    evs[0].record(stream := torch.cuda.ExternalStream(h.cuda_stream()))
+    for t in range(1, n + 1):
+        h.step(1)
+        evs[t].record(stream)
+    h.sync()
+    per_tick = np.array([evs[t - 1].elapsed_time(evs[t]) for t in range(1, n + 1)])
+    h.close()
+    kinds = {}
+    for t in range(1, n + 1):
+        k = tick_kind(params, t)
+        us, c = kinds.get(k, (0.0, 0))
+        kinds[k] = (us + per_tick[t - 1] * 1e3, c + 1)
+    by_kind = {k: {"ticks": c, "us_per_tick": us / c, "share": us / (per_tick.sum() * 1e3)}
+               for k, (us, c) in sorted(kinds.items(), key=lambda kv: -kv[1][1])}
+    return {"ticks": n, "value": at / (ms_all / 1e3), "unit": "agent-ticks/s", "ms_total": ms_all,
+            "ms_per_tick": ms_all / n, "new_exposed_total": int(res["new_exposed"].sum()),
+            "by_tick_kind": by_kind,
+            "by_tick_kind_note": "one tick per launch sequence with an event pair per tick (no graphs), so the "
+                                 "per-kind sum exceeds the replayed total"}
 
 
 def batch_arm(args):
@@ -647,9 +756,14 @@ def main():
     if W + K > nt - 1:
         K = max(1, nt - 1 - W)
     col_bytes = sum(v.nbytes for v in cols.values())
+    P = min(W + K, args.parity_ticks)  # ticks of the oracle's parity leg
+
+    clocks = ClockSampler(dev)
+    clocks.__enter__()  # the whole device phase: end to end, timed region, full run, profiling
 
     # ---- end to end through the C ABI from pinned host columns --------------
     e2e = None
+    e2e_res = e2e_cols = None
     if not args.no_e2e:
         # output buffers page-locked like the input columns, allocated before the timed region
         res = result_arrays(params, pinned=True)
@@ -674,6 +788,7 @@ def main():
         dt = time.perf_counter() - t0
         phases = dict(zip(("create_bind", "start", "ticks", "read_results", "read_columns"),
                           (b - a for a, b in zip(marks, marks[1:]))))
+        e2e_count = h.state(0).count
         h.close()
         cnt = counts_per_tick(params, res["births"])
         at = float(cnt[1 : W + K + 1].sum())
@@ -681,7 +796,10 @@ def main():
         e2e = {"value": at / dt, "unit": "agent-ticks/s", "h2d_bytes_per_step": int(col_bytes // (W + K)),
                "d2h_bytes_per_step": int((res_bytes + col_bytes) // (W + K)), "seconds": dt, "ticks": W + K,
                "phases_s": phases}
-        del out_cols
+        if P == W + K:
+            e2e_res, e2e_cols = res, out_cols
+        else:
+            del out_cols
 
     # ---- device-resident timed region ------------------------------------
     h = Handle([desc], device=dev)
@@ -695,12 +813,13 @@ def main():
     e1 = torch.cuda.Event(enable_timing=True)
     l0 = h.kernel_launches()
     barrier()
-    with ClockSampler(dev) as clocks:
-        e0.record(stream)
-        h.step(K)
-        e1.record(stream)
-        h.sync()
-        barrier()
+    timed_from = len(clocks.lines)
+    e0.record(stream)
+    h.step(K)
+    e1.record(stream)
+    h.sync()
+    barrier()
+    timed_to = len(clocks.lines)
     ms = e0.elapsed_time(e1)
     launches = h.kernel_launches() - l0
     c1 = h.counters()
@@ -714,6 +833,11 @@ def main():
     agent_ticks = float(cnt[ticks].sum())
     ms_max, at_total = reduce_over_ranks(ms, agent_ticks, ws, "cuda")
     value = at_total / (ms_max / 1e3)
+
+    # ---- the whole run, and the time of each kind of tick ------------------
+    full = None
+    if not args.no_full_run:
+        full = full_run(desc, cols, params, dev)
 
     # ---- per-kernel times (profiling mode, same ticks) --------------------
     roof = None
@@ -774,15 +898,45 @@ def main():
             "kernels": per_kernel,
         }
 
+    # the parity leg's own device run when the e2e run covered other ticks
+    if rank == 0 and not args.no_cpu and e2e_res is None:
+        h = Handle([desc], device=dev)
+        h.bind_columns(0, cols)
+        h.start()
+        h.step(P)
+        h.sync()
+        e2e_res = result_arrays(params)
+        h.read_results(0, e2e_res)
+        e2e_count = h.state(0).count
+        e2e_cols = {k: np.empty(v.shape, v.dtype) for k, v in cols.items()}
+        h.read_columns(0, e2e_cols)
+        h.close()
+    clocks.__exit__(None, None, None)
+
+    # ---- CPU baseline and parity: the oracle over the same ticks -----------
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
         del h
-        cpu_res = run_cpu_baseline(params, cols, 3, 1000, args.cpu_seconds)
+        cpu_res = oracle_leg(params, cols, min(W, P - 1), P - min(W, P - 1))
+        o = cpu_res.pop("oracle")
+        if o.state().t - 1 != P or e2e_count != o.state().count:
+            parity = {"bit_exact": False, "mismatches": [f"state: oracle at tick {o.state().t} with "
+                                                         f"{o.state().count} agents, GPU {e2e_count}"]}
+        else:
+            parity = compare_with_oracle(o, e2e_res, lambda name, dtype: e2e_cols[name], params, e2e_count)
+        parity = {"ticks": P, "agents": params["count"], **parity}
+        o.close()
+        w0 = min(W, P - 1)
         cpu = {"value": cpu_res["value"], "unit": "agent-ticks/s", "cores": cpu_res["cores"], "kind": "port",
-               "sample": f"oracle, {cpu_res['ticks']} ticks after 3 untimed of the same population "
+               "sample": f"oracle, ticks {w0 + 1}-{P} after {w0} untimed of the same population "
                          f"({cpu_res['seconds']:.1f} s)"}
 
     if rank == 0:
+        summ = clocks.summary()
+        summ["samples_in_timed_region"] = timed_to - timed_from
+        summ["window"] = "nvidia-smi every 100 ms over the whole device phase (end to end, timed region, " \
+                         "full run, profiling)"
         line = {
             "metric": "agent-ticks/s (774 nodes, 2.2e8 agents, full agent step)",
             "value": value,
@@ -796,14 +950,13 @@ def main():
             "vs_baseline": None,
             "dtype": "int8/int32 state, f64 node FOI",
             "data": "synthetic (seeded numpy, Nigeria-scale shapes)",
-            "config": {"workload": f"nigeria_like {params['n_nodes']} nodes x {params['count']:.3g} agents, "
-                                   f"capacity +30%, ticks {W + 1}-{W + K} of a 2555-tick run",
-                       "agents": params["count"], "capacity": params["capacity"], "nodes": params["n_nodes"],
-                       "l2": "state columns larger than L2 (no flush needed)", "replicas": ws},
+            "config": workload_config(params, W, K, ws),
             "e2e": e2e,
             "roofline": roof,
             "cpu_baseline": cpu,
-            "clocks": clocks.summary(),
+            "parity": parity,
+            "full_run": full,
+            "clocks": summ,
             "gpu_launches": launches,
             "work_counters": work,
             "final_tick": st.t,

@@ -498,4 +498,42 @@ LPG_HD uint64_t lpg_fix_risk_f32(float r) {
 #endif
 }
 
+/* ------------------------------------------------------------------------ */
+/* Exact mixing of fixed-point infectivity over the network.
+ *
+ * A network weight w is held in two fixed-point parts, w = hi 2^-62 +
+ * lo 2^-120: hi = floor(w 2^62) and lo the rest in units of 2^-120.  Both
+ * steps are exact for every double w >= 2^-62 (scaling by a power of two is
+ * exact, a double minus its floor is exact, and that fraction has at most 52
+ * bits, so lo is an integer below 2^58); smaller weights are rounded to
+ * 2^-120.  w >= 4 saturates hi (no row-normalised network reaches it).
+ * A node's incoming infectivity sum_i B_i w_i (B in units of 2^-40) is then
+ * A 2^-102 + R 2^-160 with A = sum_i B_i hi_i and R = sum_i B_i lo_i, each
+ * summed exactly in three 64-bit words, so the result does not depend on
+ * how the sum is split.  lpg_mix_value turns the two sums into one double
+ * with a fixed sequence of roundings, identical on every target. */
+LPG_HD void lpg_net_split(double w, uint64_t* hi, uint64_t* lo) {
+  if (!(w > 0.0)) {
+    *hi = 0;
+    *lo = 0;
+    return;
+  }
+  if (w >= 4.0) {
+    *hi = 0xFFFFFFFFFFFFFFFFULL;
+    *lo = 0;
+    return;
+  }
+  const double s = w * 0x1.0p62;
+  const double f = floor(s);
+  *hi = (uint64_t)f;
+  *lo = (uint64_t)rint((s - f) * 0x1.0p58);
+}
+
+/* (a2 2^128 + a1 2^64 + a0) 2^-102 + (r2 2^128 + r1 2^64 + r0) 2^-160 */
+LPG_HD double lpg_mix_value(uint64_t a0, uint64_t a1, uint64_t a2, uint64_t r0, uint64_t r1, uint64_t r2) {
+  const double A = ((double)a2 * 0x1.0p64 + (double)a1) * 0x1.0p64 + (double)a0;
+  const double R = ((double)r2 * 0x1.0p64 + (double)r1) * 0x1.0p64 + (double)r0;
+  return A * 0x1.0p-102 + R * 0x1.0p-160;
+}
+
 #endif /* LPG_DETMATH_H */

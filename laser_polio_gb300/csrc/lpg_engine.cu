@@ -315,14 +315,13 @@ extern "C" int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t devi
     s.net = vec(d.network, n * n, 0.0);
     s.r0s = vec(d.r0_scalars, n, 1.0);
     s.seas = vec(d.seasonality, (size_t)d.nt, 1.0);
-    s.netq_t.assign(n * n, 0);
+    s.netq_t.assign(2 * n * n, 0);
     for (size_t i = 0; i < n; ++i)
       for (size_t j = 0; j < n; ++j) {
-        const double w = s.net[i * n + j];
-        uint64_t q = 0;
-        if (w >= 4.0) q = 0xFFFFFFFFFFFFFFFFULL;
-        else if (w > 0.0) q = (uint64_t)std::nearbyint(w * 0x1.0p62);
-        s.netq_t[j * n + i] = q;
+        uint64_t hi, lo;
+        lpg_net_split(s.net[i * n + j], &hi, &lo);
+        s.netq_t[2 * (j * n + i)] = hi;
+        s.netq_t[2 * (j * n + i) + 1] = lo;
       }
     s.rowsum.assign(n, 0.0);
     for (size_t i = 0; i < n; ++i) {

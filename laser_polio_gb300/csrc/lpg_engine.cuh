@@ -22,7 +22,7 @@
  * model.py:869-929; tx_step_prep, :932-1007) are kept as running integer
  * totals, updated by every transition that changes them (exact, so they
  * equal a recount bit for bit).  Susceptible acquisition risk is summed in
- * units of 2^-24, infectivity x strain scalar in units of 2^-32.
+ * units of 2^-24, infectivity x strain scalar in units of 2^-40.
  */
 #ifndef LPG_ENGINE_CUH
 #define LPG_ENGINE_CUH
@@ -115,7 +115,7 @@ typedef struct {
   const double* p_ipv;
   const double* strain_scal;
   const double* net;   /* network[i][j], row-major */
-  const uint64_t* netq_t; /* transposed, quantised: netq_t[j][i] = network[i][j] in units of 2^-62 */
+  const uint64_t* netq_t; /* transposed, in two fixed-point parts: netq_t[j][i][0..1] = network[i][j] (lpg_net_split) */
   const double* rowsum;
   const double* r0s;
   const double* seas;

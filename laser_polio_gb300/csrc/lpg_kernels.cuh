@@ -42,10 +42,24 @@
 /* fixed-point weights (identical definitions in the oracle)                */
 __device__ __forceinline__ uint64_t fix_risk(float r) { return lpg_fix_risk_f32(r); }
 __device__ __forceinline__ uint64_t fix_beta(float inf, double scal) {
-  double d = ((double)inf * scal) * 4294967296.0;
+  double d = ((double)inf * scal) * 0x1.0p40;
   if (!(d > 0.0)) return 0;
   if (d > 0x1.0p62) d = 0x1.0p62;
   return (uint64_t)rint(d);
+}
+/* Three-word (192-bit) unsigned accumulators with the carry chain in PTX:
+ * acc3_mul adds the 128-bit product x*y, acc3_add another accumulator. */
+__device__ __forceinline__ void acc3_mul(uint64_t& a0, uint64_t& a1, uint64_t& a2, uint64_t x, uint64_t y) {
+  const uint64_t lo = x * y, hi = __umul64hi(x, y);
+  asm("add.cc.u64 %0, %0, %3;\n\taddc.cc.u64 %1, %1, %4;\n\taddc.u64 %2, %2, 0;"
+      : "+l"(a0), "+l"(a1), "+l"(a2)
+      : "l"(lo), "l"(hi));
+}
+__device__ __forceinline__ void acc3_add(uint64_t& a0, uint64_t& a1, uint64_t& a2, uint64_t b0, uint64_t b1,
+                                         uint64_t b2) {
+  asm("add.cc.u64 %0, %0, %3;\n\taddc.cc.u64 %1, %1, %4;\n\taddc.u64 %2, %2, %5;"
+      : "+l"(a0), "+l"(a1), "+l"(a2)
+      : "l"(b0), "l"(b1), "l"(b2));
 }
 __device__ __forceinline__ int8_t dec_i8(int8_t v) { return (int8_t)(uint8_t)((uint8_t)v - 1u); }
 __device__ __forceinline__ int8_t sub_i8(int8_t v, int k) { return (int8_t)(uint8_t)((uint8_t)v - (uint8_t)k); }
@@ -1671,9 +1685,10 @@ __device__ __forceinline__ void warp_chunk_prefix(const DevWorld& W, const int32
 /* Node-level force of infection and exposure counts (model.py:1327-1407);
  * the same arithmetic, in the same order, as the oracle's lpo_node_tx.
  * One CTA per node.  Incoming infectivity sum_i B_i N[i][n] is exact
- * integer arithmetic: B in units of 2^-32 times the network weight in units
- * of 2^-62 (transposed row, contiguous), 128-bit sums, one conversion; an
- * exact sum does not depend on how the threads split it. */
+ * integer arithmetic: B in units of 2^-40 times the network weight in its
+ * two fixed-point parts (lpg_net_split; transposed row, contiguous), the two
+ * products summed in three-word accumulators, one conversion
+ * (lpg_mix_value); an exact sum does not depend on how the threads split it. */
 /* Lane k < ns of the second warp: this node's incoming-infectivity total of
  * strain k (the first warp's pre_bb). */
 __device__ __forceinline__ uint64_t pre_bb_w1(const DevWorld& W, int g, int lane, int ns) {
@@ -1683,7 +1698,7 @@ __device__ __forceinline__ uint64_t pre_bb_w1(const DevWorld& W, int g, int lane
 __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
   const int g = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __shared__ uint64_t s_lo[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS], s_hi[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS];
+  __shared__ uint64_t s_mix[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS][6]; /* per warp: A, R words */
   __shared__ double s_gam;   /* the negative binomial's gamma variate, formed ahead by the second warp */
   __shared__ uint64_t s_gamk; /* the exposure stream's position after it */
   if (g >= W.G) return;
@@ -1729,18 +1744,22 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
       rr[0] = (double)pre_sw * 0x1.0p-24;
       rr[1] = (double)pop_t;
     }
-    if (threadIdx.x < ns) rr[3 + threadIdx.x] = (double)pre_bb * 0x1.0p-32;
+    if (threadIdx.x < ns) rr[3 + threadIdx.x] = (double)pre_bb * 0x1.0p-40;
   }
-  const uint64_t* qrow = rp->netq_t + (int64_t)i * n; /* qrow[ii] = network[ii][i] in 2^-62 */
-  unsigned __int128 part[LPG_MAX_STRAINS] = {0, 0, 0, 0};
+  /* qrow[ii] = network[ii][i] as (hi 2^-62, lo 2^-120), lpg_net_split */
+  const ulonglong2* qrow = reinterpret_cast<const ulonglong2*>(rp->netq_t) + (int64_t)i * n;
+  /* per strain: A = sum B hi and R = sum B lo, three words each, exact */
+  uint64_t a0[LPG_MAX_STRAINS] = {0, 0, 0, 0}, a1[LPG_MAX_STRAINS] = {0, 0, 0, 0}, a2[LPG_MAX_STRAINS] = {0, 0, 0, 0};
+  uint64_t r0[LPG_MAX_STRAINS] = {0, 0, 0, 0}, r1[LPG_MAX_STRAINS] = {0, 0, 0, 0}, r2[LPG_MAX_STRAINS] = {0, 0, 0, 0};
   /* batches of 8 source nodes per thread, every load of a batch issued
    * before any multiply (two batches for up to 1024 nodes) */
   for (int ii0 = threadIdx.x; ii0 < n; ii0 += 8 * blockDim.x) {
-    uint64_t w[8], b[8][LPG_MAX_STRAINS];
+    ulonglong2 w[8];
+    uint64_t b[8][LPG_MAX_STRAINS];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int ii = ii0 + u * blockDim.x;
-      w[u] = ii < n ? qrow[ii] : 0;
+      w[u] = ii < n ? qrow[ii] : make_ulonglong2(0, 0);
 #pragma unroll
       for (int k = 0; k < LPG_MAX_STRAINS; ++k) b[u][k] = (ii < n && k < ns) ? W.bb[(int64_t)k * G + nb + ii] : 0;
     }
@@ -1748,22 +1767,29 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
     for (int u = 0; u < 8; ++u)
 #pragma unroll
       for (int k = 0; k < LPG_MAX_STRAINS; ++k)
-        if (k < ns) part[k] += (unsigned __int128)b[u][k] * w[u];
+        if (k < ns) {
+          acc3_mul(a0[k], a1[k], a2[k], b[u][k], w[u].x);
+          acc3_mul(r0[k], r1[k], r2[k], b[u][k], w[u].y);
+        }
   }
 #pragma unroll
   for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
-    uint64_t lo = (uint64_t)part[k], hi = (uint64_t)(part[k] >> 64);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t olo = __shfl_down_sync(FULLMASK, lo, off);
-      const uint64_t ohi = __shfl_down_sync(FULLMASK, hi, off);
-      const uint64_t nlo = lo + olo;
-      hi = hi + ohi + (nlo < lo ? 1 : 0);
-      lo = nlo;
+      const uint64_t x0 = __shfl_down_sync(FULLMASK, a0[k], off), x1 = __shfl_down_sync(FULLMASK, a1[k], off),
+                     x2 = __shfl_down_sync(FULLMASK, a2[k], off);
+      acc3_add(a0[k], a1[k], a2[k], x0, x1, x2);
+      const uint64_t y0 = __shfl_down_sync(FULLMASK, r0[k], off), y1 = __shfl_down_sync(FULLMASK, r1[k], off),
+                     y2 = __shfl_down_sync(FULLMASK, r2[k], off);
+      acc3_add(r0[k], r1[k], r2[k], y0, y1, y2);
     }
     if (lane == 0) {
-      s_lo[wid][k] = lo;
-      s_hi[wid][k] = hi;
+      s_mix[wid][k][0] = a0[k];
+      s_mix[wid][k][1] = a1[k];
+      s_mix[wid][k][2] = a2[k];
+      s_mix[wid][k][3] = r0[k];
+      s_mix[wid][k][4] = r1[k];
+      s_mix[wid][k][5] = r2[k];
     }
   }
   __syncthreads();
@@ -1805,15 +1831,14 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
   double pk = 0.0;
   const double denom = (double)(pop_t > 1 ? pop_t : 1);
   if (lane < ns) {
-    uint64_t lo = 0, hi = 0;
+    uint64_t x0 = 0, x1 = 0, x2 = 0, y0 = 0, y1 = 0, y2 = 0;
 #pragma unroll
     for (int w8 = 0; w8 < LPG_NODE_TX_THREADS / 32; ++w8) {
-      const uint64_t nlo = lo + s_lo[w8][lane];
-      hi = hi + s_hi[w8][lane] + (nlo < lo ? 1 : 0);
-      lo = nlo;
+      acc3_add(x0, x1, x2, s_mix[w8][lane][0], s_mix[w8][lane][1], s_mix[w8][lane][2]);
+      acc3_add(y0, y1, y2, s_mix[w8][lane][3], s_mix[w8][lane][4], s_mix[w8][lane][5]);
     }
-    const double inck = ((double)hi * 0x1.0p64 + (double)lo) * 0x1.0p-94;
-    const double bpre = (double)pre_bb * 0x1.0p-32;
+    const double inck = lpg_mix_value(x0, x1, x2, y0, y1, y2);
+    const double bpre = (double)pre_bb * 0x1.0p-40;
     double beta = bpre + (inck - bpre * pre_rowsum);
     beta = (beta * pre_seas) * pre_r0s;
     const double rate = beta / denom;

@@ -15,7 +15,7 @@
  *   2. Per-node sums that the reference accumulates in float32 thread-local
  *      buffers (model.py:952-954) are exact fixed-point integers here:
  *      acquisition risk in units of 2^-24, infectivity x strain scalar in
- *      units of 2^-32.  The weighted selection CDF (model.py:1108) is the
+ *      units of 2^-40.  The weighted selection CDF (model.py:1108) is the
  *      integer prefix of the same risk units.  Integer sums do not depend
  *      on summation order.
  * Citations are laser_polio/model.py unless stated.
@@ -63,6 +63,10 @@ typedef struct {
   /* per transmission tick and node: srisk, pop, the expected new exposures,
    * beta before mixing by strain ([nt][n_nodes][3 + ns]), or NULL */
   double* rec;
+  /* the same tick's susceptible risk and infectivity sums straight from the
+   * float32 columns in FP64, without the fixed-point units the step uses
+   * ([nt][n_nodes][1 + ns]; set with rec) */
+  double* rec64;
   char msg[256];
 } lpo_sim;
 
@@ -96,7 +100,7 @@ static inline uint64_t fix_risk(float r) {
   return (uint64_t)nearbyint(d);
 }
 static inline uint64_t fix_beta(float inf, double scal) {
-  double d = ((double)inf * scal) * 4294967296.0; /* 2^32 */
+  double d = ((double)inf * scal) * 0x1.0p40;
   if (!(d > 0.0)) return 0;
   if (d > 0x1.0p62) d = 0x1.0p62;
   return (uint64_t)nearbyint(d);
@@ -170,6 +174,7 @@ void lpo_destroy(lpo_sim* s) {
   for (size_t i = 0; i < sizeof ps / sizeof ps[0]; ++i) free(ps[i]);
   for (int k = 0; k < NRES; ++k) free(s->res[k]);
   free(s->rec);
+  free(s->rec64);
   free(s);
 }
 
@@ -596,11 +601,14 @@ static void lpo_sia(lpo_sim* s, int32_t t) {
 }
 
 /* ---------------------------------------------------------------------- */
-/* Network weight in units of 2^-62 (saturating at 4). */
-static inline uint64_t lpo_netq(double w) {
-  if (!(w > 0.0)) return 0;
-  if (w >= 4.0) return 0xFFFFFFFFFFFFFFFFULL;
-  return (uint64_t)nearbyint(w * 0x1.0p62);
+/* Three-word accumulator: a += x*y (128-bit product). */
+static inline void lpo_acc3_mul(uint64_t a[3], uint64_t x, uint64_t y) {
+  unsigned __int128 p = (unsigned __int128)x * y;
+  unsigned __int128 lo = ((unsigned __int128)a[1] << 64) | a[0];
+  unsigned __int128 sum = lo + p;
+  if (sum < lo) a[2] += 1;
+  a[0] = (uint64_t)sum;
+  a[1] = (uint64_t)(sum >> 64);
 }
 
 /* Node-level force of infection and exposure counts
@@ -614,15 +622,21 @@ void lpo_node_tx(int n, int ns, const uint64_t* B, const uint64_t* SW, const int
     int local_zero = 1;
     for (int k = 0; k < ns; ++k) {
       if (B[(size_t)nd * ns + k] != 0) local_zero = 0;
-      /* incoming infectivity sum_i beta_i N[i][nd], exact: B (units 2^-32)
-       * times the network weight quantised to units of 2^-62, summed in 128
-       * bits, converted once */
-      unsigned __int128 acc = 0;
-      for (int i = 0; i < n; ++i) acc += (unsigned __int128)B[(size_t)i * ns + k] * (unsigned __int128)lpo_netq(net[(size_t)i * n + nd]);
-      double inc = ((double)(uint64_t)(acc >> 64) * 0x1.0p64 + (double)(uint64_t)acc) * 0x1.0p-94;
+      /* incoming infectivity sum_i beta_i N[i][nd], exact: B (units 2^-40)
+       * times the network weight in its two fixed-point parts
+       * (lpg_net_split), each product summed in three words, converted once
+       * (lpg_mix_value) */
+      uint64_t A[3] = {0, 0, 0}, Rr[3] = {0, 0, 0};
+      for (int i = 0; i < n; ++i) {
+        uint64_t whi, wlo;
+        lpg_net_split(net[(size_t)i * n + nd], &whi, &wlo);
+        lpo_acc3_mul(A, B[(size_t)i * ns + k], whi);
+        lpo_acc3_mul(Rr, B[(size_t)i * ns + k], wlo);
+      }
+      double inc = lpg_mix_value(A[0], A[1], A[2], Rr[0], Rr[1], Rr[2]);
       double rowsum = 0.0;
       for (int j = 0; j < n; ++j) rowsum = rowsum + net[(size_t)nd * n + j];
-      double bpre = (double)B[(size_t)nd * ns + k] * 0x1.0p-32;
+      double bpre = (double)B[(size_t)nd * ns + k] * 0x1.0p-40;
       double beta = bpre + (inc - bpre * rowsum);
       beta = (beta * seas) * r0s[nd];
       double denom = use_pop ? (double)(pop[nd] > 1 ? pop[nd] : 1) : 1.0;
@@ -640,7 +654,7 @@ void lpo_node_tx(int n, int ns, const uint64_t* B, const uint64_t* SW, const int
       rr[0] = srisk;
       rr[1] = (double)pop[nd];
       rr[2] = exposure;
-      for (int k = 0; k < ns; ++k) rr[3 + k] = (double)B[(size_t)nd * ns + k] * 0x1.0p-32;
+      for (int k = 0; k < ns; ++k) rr[3 + k] = (double)B[(size_t)nd * ns + k] * 0x1.0p-40;
     }
     int64_t total = 0;
     lpg_stream st;
@@ -713,6 +727,15 @@ static void lpo_tx(lpo_sim* s, int32_t t) {
   lpo_node_tx(n, ns, B, SW, Sc, s->network, s->r0_scalars, s->seasonality[t], RES(R_POP, t), use_pop,
               s->d.zero_inflation, s->d.nb_r, s->d.seed, t, prob, size,
               s->rec ? s->rec + (size_t)t * n * (3 + ns) : NULL);
+  if (s->rec64) { /* FP64 sums of the unquantised columns (a check of the fixed-point units) */
+    double* r64 = s->rec64 + (size_t)t * n * (1 + ns);
+    for (int64_t i = 0; i < count; ++i) {
+      int8_t st = s->ds[i];
+      double* rr = r64 + (size_t)s->node[i] * (1 + ns);
+      if (st == 0) rr[0] += (double)s->risk[i];
+      else if (st == 2) rr[1 + s->strain[i]] += (double)s->inf[i] * s->strain_r0_scalars[s->strain[i]];
+    }
+  }
 
   /* serial gather of susceptible slots per node, index order (:1055-1061) */
   int64_t* off = calloc((size_t)n + 1, sizeof(int64_t));
@@ -850,7 +873,9 @@ int lpo_num_threads(void) { return nthreads(); }
 int lpo_record_aggregates(lpo_sim* s, int enable) {
   if (s->started) return LPG_ERR_STATE;
   free(s->rec);
+  free(s->rec64);
   s->rec = enable ? calloc((size_t)s->d.nt * NN * (3 + NS), sizeof(double)) : NULL;
+  s->rec64 = enable ? calloc((size_t)s->d.nt * NN * (1 + NS), sizeof(double)) : NULL;
   return 0;
 }
 
@@ -866,6 +891,21 @@ int lpo_read_aggregates(lpo_sim* s, double* srisk, double* beta, double* pop, do
     if (lam) lam[q] = b[2];
     if (beta)
       for (int k = 0; k < NS; ++k) beta[q * NS + k] = b[3 + k];
+  }
+  return 0;
+}
+
+/* The FP64 sums recorded beside the aggregates: srisk [nt][n] and beta
+ * [nt][n][ns] from the float32 columns without fixed-point units. */
+int lpo_read_aggregates_fp64(lpo_sim* s, double* srisk, double* beta) {
+  if (!s->rec64) return LPG_ERR_STATE;
+  const int w = 1 + NS;
+  const size_t rows = (size_t)s->d.nt * NN;
+  for (size_t q = 0; q < rows; ++q) {
+    const double* b = s->rec64 + q * w;
+    if (srisk) srisk[q] = b[0];
+    if (beta)
+      for (int k = 0; k < NS; ++k) beta[q * NS + k] = b[1 + k];
   }
   return 0;
 }

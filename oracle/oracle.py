@@ -50,6 +50,7 @@ def lib():
         L.lpo_num_threads.restype = C.c_int
         L.lpo_record_aggregates.argtypes = [C.c_void_p, C.c_int]
         L.lpo_read_aggregates.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 4
+        L.lpo_read_aggregates_fp64.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 2
         _lib = L
     return _lib
 
@@ -97,6 +98,17 @@ class OracleSim:
                "lam": np.zeros((nt, n))}
         dp = C.POINTER(C.c_double)
         if lib().lpo_read_aggregates(self.h, *[_abi.ptr(out[k], dp) for k in ("srisk", "beta", "pop", "lam")]) != 0:
+            raise RuntimeError("oracle: aggregates were not recorded")
+        return out
+
+    def read_aggregates_fp64(self) -> dict:
+        """srisk [nt, n_nodes] and beta [nt, n_nodes, n_strains] of the same
+        ticks summed in FP64 straight from the float32 risk and infectivity
+        columns, without the fixed-point units the step itself uses."""
+        nt, n, ns = self.desc.nt, self.desc.n_nodes, self.desc.n_strains
+        out = {"srisk": np.zeros((nt, n)), "beta": np.zeros((nt, n, ns))}
+        dp = C.POINTER(C.c_double)
+        if lib().lpo_read_aggregates_fp64(self.h, _abi.ptr(out["srisk"], dp), _abi.ptr(out["beta"], dp)) != 0:
             raise RuntimeError("oracle: aggregates were not recorded")
         return out
 
