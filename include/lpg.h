@@ -202,6 +202,15 @@ typedef struct lpg_handle lpg_handle;
 /* Library version and the name of the device code it carries. */
 int lpg_version(void);
 
+/* Every check lpg_create makes on one simulation's description (sizes,
+ * required arrays, event ranges, and that the parameter arrays are finite
+ * and in range, where the reference raises ValueError: model.py:169-170,
+ * 602, 687, 702, 770, 1256), on the host, without a GPU.  LPG_OK or the
+ * status lpg_create would return; the text from lpg_op_last_error().  A
+ * caller batching replicates checks each one first and leaves the failing
+ * ones out (calib/objective.py:47-70 runs each replicate in its own try). */
+int lpg_check_desc(const lpg_sim_desc* sim);
+
 /* Create a handle for n_sims simulations on CUDA device `device`.
  * Replaces SEIR_ABM.__init__ + the components setter as far as the device
  * state is concerned (model.py:101-175, 209-244). */
@@ -223,7 +232,13 @@ int lpg_start(lpg_handle* h);
  * early-stop tick.  Asynchronous: returns once the work is queued. */
 int lpg_step(lpg_handle* h, int32_t n_ticks);
 
-/* Wait for queued work; reports a sticky device-side error if one was set. */
+/* Wait for queued work; reports a sticky device-side error if one was set.
+ * Device-side errors belong to one simulation (lpg_sim_state.error): a
+ * simulation whose births exceed its capacity (LPG_ERR_CAPACITY), or whose
+ * staged sweep gave up a bounded wait (LPG_ERR_TIMEOUT), stops at that tick
+ * while the handle's other simulations run on.  lpg_sync returns the first
+ * such error; read every simulation's own with lpg_get_state.  LPG_ERR_CUDA
+ * is a failure of the whole handle. */
 int lpg_sync(lpg_handle* h);
 
 int lpg_get_state(lpg_handle* h, int32_t sim, lpg_sim_state* out);
@@ -280,6 +295,16 @@ enum {
 /* Copies min(n, LPG_NUM_COUNTERS) counters to out (host memory) after the
  * handle's stream has finished; returns LPG_OK or an error code. */
 int lpg_read_counters(lpg_handle* h, uint64_t* out, int32_t n);
+
+/* Test hook, no counterpart in the reference: the staged RI/SIA sweep's
+ * producer issues at most `stages` stages per CTA (negative: all) and its
+ * consumers give up a wait after `wait_spin` iterations (0: the normal
+ * limit).  A withheld stage makes the consumers' bounded wait run out, as
+ * a copy that never landed would: the CTA records LPG_ERR_TIMEOUT against
+ * the simulations whose staged chunks it was sweeping, waits (on the normal
+ * limit) for the copies it did issue, and returns.  Nothing faults and the
+ * context stays usable.  Cached CUDA graphs are dropped. */
+int lpg_test_stall_sweep(lpg_handle* h, int32_t stages, int64_t wait_spin);
 
 /* The CUDA stream the handle launches on, as an opaque pointer. */
 void* lpg_cuda_stream(lpg_handle* h);
@@ -426,10 +451,12 @@ int lpg_write_results_csv(const char* path, int32_t nt, int32_t n_nodes, const c
 
 /* The radiation migration network (the reference builds it with laser_core's
  * radiation at model.py:1252-1254; migration_method's default): out[i][j] =
- * k p_i p_j / ((p_i + s_ij)(p_i + p_j + s_ij)), s_ij the population strictly
- * closer to i than j without i and j, zero diagonal (pops on it when
- * include_home).  Host arrays, row-major [n][n]; rows on host threads; no
- * GPU.  Equal bit for bit to laser_polio_gb300.core's Python definition. */
+ * k p_i p_j / ((p_i + s_ij)(p_i + p_j + s_ij)), s_ij the population of the
+ * nodes other than i and j strictly closer to i than j (nodes tied with j
+ * are outside), zero diagonal.  include_home must be 0 (the reference only
+ * builds include_home=False): LPG_ERR_ARG otherwise.  Host arrays, row-major
+ * [n][n]; rows on host threads; no GPU.  Equal bit for bit to
+ * laser_polio_gb300.core's Python definition. */
 int lpg_radiation_network(const double* pops, const double* dist, int32_t n, double k, int32_t include_home,
                           double* out);
 

@@ -59,6 +59,8 @@ SIGNATURES = {
     "lpg_radiation_network": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32, C.c_double,
                                         C.c_int32, C.POINTER(C.c_double)]),
     "lpg_op_last_error": (C.c_char_p, []),
+    "lpg_check_desc": (C.c_int, [C.POINTER(_abi.lpg_sim_desc)]),
+    "lpg_test_stall_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
 }
 
 
@@ -94,6 +96,24 @@ class LpgError(RuntimeError):
         super().__init__(f"{_abi.STATUS_NAMES.get(code, code)}: {msg}")
 
 
+def error_for(code: int, msg: str) -> Exception:
+    """The exception a failed call raises: ValueError where the reference
+    raises one (capacity exhausted, LaserFrame.add; bad parameters), else
+    LpgError carrying the status."""
+    if code in (-1, -2, -3):
+        return ValueError(f"{_abi.STATUS_NAMES.get(code, code)}: {msg}" if code != -2 else msg)
+    return LpgError(code, msg)
+
+
+def check_desc(desc) -> None:
+    """Raise what lpg_create would for this one simulation description
+    (lpg_check_desc: host only, needs no GPU)."""
+    lib = load()
+    rc = lib.lpg_check_desc(C.byref(desc))
+    if rc != 0:
+        raise error_for(rc, lib.lpg_op_last_error().decode())
+
+
 class Handle:
     """One lpg_handle: simulations that advance together on one GPU."""
 
@@ -125,12 +145,34 @@ class Handle:
     def sync(self):
         self._check(self.lib.lpg_sync(self.h))
 
-    def state(self, sim: int = 0) -> _abi.lpg_sim_state:
+    def sync_statuses(self) -> list:
+        """Wait for queued work and return each simulation's own status (0 or
+        a negative lpg_status): a simulation that failed on the device (births
+        beyond its capacity, a timed-out wait, an internal check) stops there
+        while the others run on.  A failure of the whole handle (a CUDA
+        error) raises."""
+        rc = self.lib.lpg_sync(self.h)
+        if rc == -5:  # LPG_ERR_CUDA
+            self._check(rc)
+        out = []
+        for i in range(len(self._descs)):
+            st = _abi.lpg_sim_state()
+            self._check(self.lib.lpg_get_state(self.h, i, C.byref(st)))
+            out.append(int(st.error))
+        return out
+
+    def state(self, sim: int = 0, check: bool = True) -> _abi.lpg_sim_state:
         st = _abi.lpg_sim_state()
         self._check(self.lib.lpg_get_state(self.h, sim, C.byref(st)))
-        if st.error:
+        if st.error and check:
             self.sync()
         return st
+
+    def test_stall_sweep(self, stages: int, wait_spin: int = 0):
+        """Test hook (lpg_test_stall_sweep): the staged RI/SIA sweep issues
+        only `stages` stages and its consumers give up after `wait_spin`
+        iterations, so that a test can make the bounded wait run out."""
+        self._check(self.lib.lpg_test_stall_sweep(self.h, int(stages), int(wait_spin)))
 
     def read_results(self, sim: int, res: dict):
         self._check(self.lib.lpg_read_results(self.h, sim, C.byref(_abi.make_results_view(res))))

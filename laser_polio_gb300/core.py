@@ -184,9 +184,11 @@ def gravity(pops, distances, k, a, b, c):
 def radiation(pops, distances, k, include_home=False):
     """Radiation-model flows (Simini et al., Nature 484, 2012):
     k * p_i * p_j / ((p_i + s_ij) (p_i + p_j + s_ij)), s_ij = population
-    strictly closer to i than j, excluding i and j.  Computed by the native
-    lpg_radiation_network (host threads), equal bit for bit to the
-    definition in _radiation_py."""
+    strictly closer to i than j, excluding i and j (nodes tied with j are
+    outside).  Computed by the native lpg_radiation_network (host threads),
+    equal bit for bit to the definition in _radiation_py.  include_home=True
+    is rejected: the reference only builds include_home=False
+    (model.py:1252-1254)."""
     import ctypes as C
 
     from . import _lib
@@ -208,7 +210,11 @@ def radiation(pops, distances, k, include_home=False):
 
 def _radiation_py(pops, distances, k, include_home=False):
     """radiation() as a Python loop: the definition the native builder
-    follows operation for operation."""
+    follows operation for operation.  s_ij counts the nodes other than i and
+    j strictly closer to i than j (ties with j are outside the circle)."""
+    if include_home:
+        raise ValueError("include_home=True is not supported (the reference builds its network with "
+                         "include_home=False)")
     pops = np.asarray(pops, dtype=np.float64)
     d = np.asarray(distances, dtype=np.float64)
     n = len(pops)
@@ -218,15 +224,15 @@ def _radiation_py(pops, distances, k, include_home=False):
         order = np.argsort(di, kind="stable")
         sorted_p = pops[order]
         cum = np.cumsum(sorted_p)
+        before = np.concatenate([[0.0], cum[:-1]])  # populations of the ranks before each rank
+        for rank in range(1, n):  # a tie starts no new sum: the nodes at j's distance are not inside
+            if di[order[rank]] == di[order[rank - 1]]:
+                before[rank] = before[rank - 1]
         for rank, j in enumerate(order):
             if j == i:
                 continue
-            inside = cum[rank] - sorted_p[rank]  # population strictly before j in distance order
-            s = inside - (pops[i] if di[i] <= di[j] else 0.0)
-            s = max(s, 0.0)
+            s = before[rank] - (pops[i] if di[i] < di[j] else 0.0)
             out[i, j] = k * pops[i] * pops[j] / ((pops[i] + s) * (pops[i] + pops[j] + s))
-    if include_home:
-        out[np.diag_indices(n)] = pops
     return out
 
 

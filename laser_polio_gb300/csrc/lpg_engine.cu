@@ -81,6 +81,8 @@ struct lpg_handle {
   bool started = false;
   std::string err;
   bool use_graphs = true;
+  int32_t test_stall_after = -1; /* lpg_test_stall_sweep */
+  int64_t test_wait_spin = 0;
   std::map<uint32_t, std::pair<cudaGraphExec_t, int>> graphs; /* by the needs of 8 ticks: graph, launches */
   bool graph_failed = false;
   std::vector<uint8_t> tick_need; /* per tick: the optional kernels some simulation needs (NEED_*) */
@@ -280,6 +282,85 @@ static uint64_t u53_threshold(double p) {
 
 static const int res_wide[RS_N] = {0, 0, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 1, 0, 0, 0, 1};
 
+/* Every check lpg_create makes on one simulation's description: sizes,
+ * required arrays, event ranges, and that every parameter array holds finite
+ * values in its range (the reference raises ValueError on such inputs, e.g.
+ * model.py:169-170, 602, 687, 702, 770, 1256; a NaN here would silently turn
+ * into zero probabilities on the device). */
+static int validate_desc(const lpg_sim_desc& d, int r, std::string* msg) {
+  char buf[256];
+  auto bad = [&](int code, const char* fmt, auto... args) {
+    snprintf(buf, sizeof buf, fmt, args...);
+    *msg = buf;
+    return code;
+  };
+  if (d.n_nodes < 1 || d.n_nodes > 32767) return bad(LPG_ERR_ARG, "sim %d: n_nodes %d out of range", r, d.n_nodes);
+  if (d.n_strains < 1 || d.n_strains > LPG_MAX_STRAINS)
+    return bad(LPG_ERR_ARG, "sim %d: n_strains %d out of range [1, %d]", r, d.n_strains, LPG_MAX_STRAINS);
+  if (d.nt < 1) return bad(LPG_ERR_ARG, "sim %d: nt must be >= 1", r);
+  if (d.count < 0 || d.capacity < d.count || d.capacity >= (int64_t)0xFFFFFFF0LL)
+    return bad(LPG_ERR_ARG, "sim %d: count %lld / capacity %lld invalid", r, (long long)d.count, (long long)d.capacity);
+  if (d.vd_step < 1 || d.ri_step < 1) return bad(LPG_ERR_ARG, "sim %d: step sizes must be >= 1", r);
+  if (!d.pop0) return bad(LPG_ERR_ARG, "sim %d: pop0 is required", r);
+  if ((d.components & LPG_COMP_TX) && (!d.network || !d.seasonality || !d.strain_r0_scalars || !d.r0_scalars))
+    return bad(LPG_ERR_ARG, "sim %d: transmission needs network, seasonality and scalars", r);
+  if (d.km_len < 1 || !d.km_cumdeaths) return bad(LPG_ERR_ARG, "sim %d: km table required", r);
+  const size_t n = (size_t)d.n_nodes;
+  auto check = [&](const double* a, size_t k, double lo, double hi, const char* name) -> int {
+    if (!a) return 0;
+    for (size_t i = 0; i < k; ++i)
+      if (!std::isfinite(a[i]) || a[i] < lo || a[i] > hi)
+        return bad(LPG_ERR_ARG, "sim %d: %s[%zu] = %g is not finite or outside [%g, %g]", r, name, i, a[i], lo, hi);
+    return 0;
+  };
+  const double inf = HUGE_VAL;
+  int rc = 0;
+  if ((rc = check(d.birth_rate, n, 0.0, inf, "birth_rate"))) return rc;
+  if ((rc = check(d.vx_prob_ri, n, 0.0, 1.0, "vx_prob_ri"))) return rc;
+  if ((rc = check(d.vx_prob_ipv, n, 0.0, 1.0, "vx_prob_ipv"))) return rc;
+  if ((rc = check(d.strain_r0_scalars, (size_t)d.n_strains, 0.0, inf, "strain_r0_scalars"))) return rc;
+  if ((rc = check(d.network, n * n, 0.0, inf, "network"))) return rc;
+  if ((rc = check(d.r0_scalars, n, 0.0, inf, "r0_scalars"))) return rc;
+  if ((rc = check(d.seasonality, (size_t)d.nt, -inf, inf, "seasonality"))) return rc;
+  if (d.vx_prob_sia)
+    for (size_t i = 0; i < n; ++i)
+      if (!std::isfinite(d.vx_prob_sia[i]) || d.vx_prob_sia[i] < 0.0f || d.vx_prob_sia[i] > 1.0f)
+        return bad(LPG_ERR_ARG, "sim %d: vx_prob_sia[%zu] = %g is not finite or outside [0, 1]", r, i,
+                   (double)d.vx_prob_sia[i]);
+  if (!std::isfinite(d.p_paralysis) || d.p_paralysis < 0.0f || d.p_paralysis > 1.0f)
+    return bad(LPG_ERR_ARG, "sim %d: p_paralysis %g outside [0, 1]", r, (double)d.p_paralysis);
+  if (!std::isfinite(d.zero_inflation) || d.zero_inflation < 0.0)
+    return bad(LPG_ERR_ARG, "sim %d: zero inflation %g is not finite and >= 0", r, d.zero_inflation);
+  for (int i = 0; i < (int)n; ++i)
+    if (d.pop0[i] < 0) return bad(LPG_ERR_ARG, "sim %d: pop0[%d] = %d is negative", r, i, d.pop0[i]);
+  for (int k = 0; k < d.n_seeds; ++k) {
+    const lpg_seed_event& e = d.seeds[k];
+    if (e.node < 0 || e.node >= d.n_nodes) return bad(LPG_ERR_NODE, "sim %d: seed event node %d out of range", r, e.node);
+    if (!std::isfinite(e.value) || e.value < 0.0) return bad(LPG_ERR_ARG, "sim %d: seed event value %g", r, e.value);
+  }
+  std::vector<int32_t> per_tick(d.nt, 0);
+  for (int k = 0; k < d.n_sia; ++k) {
+    const lpg_sia_event& e = d.sia[k];
+    if (e.tick < 0 || e.tick >= d.nt) continue;
+    if (e.strain < 0 || e.strain >= d.n_strains) return bad(LPG_ERR_ARG, "sim %d: SIA strain out of range", r);
+    if (!std::isfinite(e.efficacy)) return bad(LPG_ERR_ARG, "sim %d: SIA efficacy %g is not finite", r, e.efficacy);
+    if (++per_tick[e.tick] > LPG_MAX_SIA_PER_DAY)
+      return bad(LPG_ERR_ARG, "sim %d: more than %d SIA events on tick %d", r, LPG_MAX_SIA_PER_DAY, e.tick);
+  }
+  if (d.ri_strain < 0 || d.ri_strain >= d.n_strains) return bad(LPG_ERR_ARG, "sim %d: RI strain out of range", r);
+  return LPG_OK;
+}
+
+int lpg_ops_fail(int code, const char* fmt, ...);
+
+extern "C" int lpg_check_desc(const lpg_sim_desc* d) {
+  if (!d) return lpg_ops_fail(LPG_ERR_ARG, "null description");
+  std::string msg;
+  const int rc = validate_desc(*d, 0, &msg);
+  if (rc) return lpg_ops_fail(rc, "%s", msg.c_str());
+  return LPG_OK;
+}
+
 extern "C" int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t device, lpg_handle** out) {
   if (!out) return LPG_ERR_ARG;
   *out = nullptr;
@@ -289,17 +370,11 @@ extern "C" int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t devi
   h->device = device;
   for (int r = 0; r < n_sims; ++r) {
     const lpg_sim_desc& d = sims[r];
-    if (d.n_nodes < 1 || d.n_nodes > 32767) return fail(h, LPG_ERR_ARG, "sim %d: n_nodes %d out of range", r, d.n_nodes);
-    if (d.n_strains < 1 || d.n_strains > LPG_MAX_STRAINS)
-      return fail(h, LPG_ERR_ARG, "sim %d: n_strains %d out of range [1, %d]", r, d.n_strains, LPG_MAX_STRAINS);
-    if (d.nt < 1) return fail(h, LPG_ERR_ARG, "sim %d: nt must be >= 1", r);
-    if (d.count < 0 || d.capacity < d.count || d.capacity >= (int64_t)0xFFFFFFF0LL)
-      return fail(h, LPG_ERR_ARG, "sim %d: count %lld / capacity %lld invalid", r, (long long)d.count, (long long)d.capacity);
-    if (d.vd_step < 1 || d.ri_step < 1) return fail(h, LPG_ERR_ARG, "sim %d: step sizes must be >= 1", r);
-    if (!d.pop0) return fail(h, LPG_ERR_ARG, "sim %d: pop0 is required", r);
-    if ((d.components & LPG_COMP_TX) && (!d.network || !d.seasonality || !d.strain_r0_scalars || !d.r0_scalars))
-      return fail(h, LPG_ERR_ARG, "sim %d: transmission needs network, seasonality and scalars", r);
-    if (d.km_len < 1 || !d.km_cumdeaths) return fail(h, LPG_ERR_ARG, "sim %d: km table required", r);
+    {
+      std::string msg;
+      const int rc = validate_desc(d, r, &msg);
+      if (rc) return fail(h, rc, "%s", msg.c_str());
+    }
     SimHost s;
     s.d = d;
     const size_t n = (size_t)d.n_nodes;
@@ -334,20 +409,14 @@ extern "C" int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t devi
     s.km.assign(d.km_cumdeaths, d.km_cumdeaths + d.km_len);
     for (int k = 0; k < d.n_seeds; ++k) {
       lpg_seed_event e = d.seeds[k];
-      if (e.node < 0 || e.node >= d.n_nodes) return fail(h, LPG_ERR_NODE, "sim %d: seed event node %d out of range", r, e.node);
       s.seeds.push_back(e);
     }
-    std::vector<int32_t> per_tick(d.nt, 0);
     for (int k = 0; k < d.n_sia; ++k) {
       lpg_sia_event e = d.sia[k];
       if (e.tick < 0 || e.tick >= d.nt) continue;
-      if (e.strain < 0 || e.strain >= d.n_strains) return fail(h, LPG_ERR_ARG, "sim %d: SIA strain out of range", r);
-      if (++per_tick[e.tick] > LPG_MAX_SIA_PER_DAY)
-        return fail(h, LPG_ERR_ARG, "sim %d: more than %d SIA events on tick %d", r, LPG_MAX_SIA_PER_DAY, e.tick);
       s.sia.push_back(e);
       s.sia_masks.emplace_back(e.node_mask, e.node_mask + n);
     }
-    if (d.ri_strain < 0 || d.ri_strain >= d.n_strains) return fail(h, LPG_ERR_ARG, "sim %d: RI strain out of range", r);
     s.pop0.assign(d.pop0, d.pop0 + n);
     if (d.R_preseed) s.Rpre.assign(d.R_preseed, d.R_preseed + (size_t)d.nt * n);
     h->sims.push_back(std::move(s));
@@ -512,6 +581,8 @@ extern "C" int lpg_start(lpg_handle* h) {
   W.n_reps = R;
   W.G = G;
   W.total_chunks = chunk_total;
+  W.stall_after = h->test_stall_after;
+  W.wait_spin = h->test_wait_spin > 0 ? h->test_wait_spin : LPG_MBAR_SPIN;
   const int64_t P = (int64_t)chunk_total * LPG_CHUNK;
   int rc = 0;
   rc |= dalloc(h, &W.ds, P);
@@ -1166,6 +1237,19 @@ extern "C" int lpg_check_invariants(lpg_handle* h) {
   void* ps[] = {tot, sw, bb, cw, subw, subd, sube, subr, bad};
   for (void* p : ps) dfree_one(h, p);
   if (hb) return fail(h, LPG_ERR_INTERNAL, "running totals differ from a recount (mask 0x%x)", hb);
+  return LPG_OK;
+}
+
+extern "C" int lpg_test_stall_sweep(lpg_handle* h, int32_t stages, int64_t wait_spin) {
+  if (!h) return LPG_ERR_ARG;
+  if (wait_spin < 0 || wait_spin > LPG_MBAR_SPIN) return fail(h, LPG_ERR_ARG, "wait_spin %lld out of range", (long long)wait_spin);
+  h->test_stall_after = stages < 0 ? -1 : stages;
+  h->test_wait_spin = wait_spin;
+  h->W.stall_after = h->test_stall_after;
+  h->W.wait_spin = wait_spin > 0 ? wait_spin : LPG_MBAR_SPIN;
+  /* graphs hold the kernels' arguments as captured: capture again */
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second.first);
+  h->graphs.clear();
   return LPG_OK;
 }
 

@@ -164,7 +164,9 @@ typedef struct {
 typedef struct {
   int32_t n_reps, G; /* replicates, global nodes */
   int32_t total_chunks;
-  int32_t pad;
+  int32_t stall_after; /* test hook (lpg_test_stall_sweep): the staged sweep's producer issues only this many
+                          stages (-1: all) */
+  int64_t wait_spin;   /* iterations of the staged sweep's consumer waits before they give up */
   DevRep* reps;
   /* per position */
   int8_t *ds, *strain, *et, *it, *pt, *pp, *par, *ipv;

@@ -517,8 +517,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 /* bounded wait; false on timeout */
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long it = 0; it < LPG_MBAR_SPIN; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = LPG_MBAR_SPIN) {
+  for (long long it = 0; it < limit; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if (it > 64) __nanosleep(32);
   }
@@ -960,6 +960,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
           break;
         }
         if (s_abort) break;
+        if (W.stall_after >= 0 && i >= W.stall_after) break; /* test hook: withhold the rest */
         int r;
         const int32_t we = stage_end(P, wp, w1, &r);
         const uint8_t f = P.flags[r];
@@ -988,7 +989,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
       const uint32_t parity = (uint32_t)(i / LPG_NST) & 1u;
       int r;
       const int32_t we = stage_end(P, wc, w1, &r);
-      bool ok = !s_abort && mbar_wait(&full[b], parity);
+      bool ok = !s_abort && mbar_wait(&full[b], parity, W.wait_spin);
       ok = __all_sync(FULLMASK, ok);
       if (!ok) {
         s_abort = 1;
@@ -1026,8 +1027,12 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
   }
   __syncthreads();
   if (s_abort && threadIdx.x == LPG_SWEEP_CONSUMERS) {
-    /* leave no bulk copy in flight into this CTA's shared memory */
-    W.reps[0].error = LPG_ERR_TIMEOUT;
+    /* the error goes to every simulation whose staged chunks this CTA was
+     * sweeping (RI-only simulations take the due index, not the stages);
+     * then leave no bulk copy in flight into this CTA's shared memory (the
+     * drain waits on the normal limit) */
+    for (int r = 0; r < P.nreps; ++r)
+      if ((P.flags[r] & SF_DENSE) && P.off[r] < w1 && P.off[r + 1] > w0) W.reps[r].error = LPG_ERR_TIMEOUT;
     const int32_t n = s_issued;
     for (int b = 0; b < LPG_NST; ++b) {
       int32_t last = -1;

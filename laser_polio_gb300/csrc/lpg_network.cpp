@@ -5,15 +5,18 @@
  * The reference builds its network once per run (model.py:1244-1256) with
  * laser_core's radiation model (Simini et al., Nature 484, 2012):
  *   out[i][j] = k p_i p_j / ((p_i + s_ij) (p_i + p_j + s_ij)),
- * where s_ij is the population strictly closer to i than j, not counting i
- * and j.  radiation is migration_method's default (pars.py:55).  This follows
- * the package's restatement (core.radiation) operation for operation, so the
- * two agree bit for bit:
+ * where s_ij is the population of the nodes k other than i and j with
+ * d_ik < d_ij strictly: nodes at the same distance as j are not inside the
+ * circle, so the value of s_ij does not depend on how ties are ordered.
+ * radiation is migration_method's default (pars.py:55); the reference only
+ * ever asks for include_home=False (model.py:1252-1254), and laser_core's
+ * diagonal for include_home=True is not known here, so it is rejected.  This
+ * follows the package's restatement (core.radiation) operation for
+ * operation, so the two agree bit for bit:
  *   - each row orders the nodes by distance from i, ties by index (numpy's
- *     stable argsort);
- *   - the populations are summed in that order;
- *   - s = (cumulative population up to and including j) - p_j, minus p_i
- *     when d_ii <= d_ij, clamped below at 0 as Python's max(s, 0.0);
+ *     stable argsort), and sums the populations in that order;
+ *   - s = the cumulative population before the first node at j's distance,
+ *     minus p_i when d_ii < d_ij;
  *   - the product and quotient are evaluated left to right, with no FMA
  *     contraction (-ffp-contract=off).
  */
@@ -41,10 +44,12 @@ void radiation_rows(int32_t i0, int32_t i1, int32_t n, const double* pops, const
     const double* di = dist + (size_t)i * n;
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [di](int32_t a, int32_t b) { return di[a] < di[b]; });
+    /* cum[r] = populations of ranks before r; before[r] = that sum at the
+     * first rank of r's distance */
     double c = 0.0;
     for (int32_t r = 0; r < n; ++r) {
+      cum[r] = (r > 0 && di[order[r]] == di[order[r - 1]]) ? cum[r - 1] : c;
       c = c + pops[order[r]];
-      cum[r] = c;
     }
     double* oi = out + (size_t)i * n;
     for (int32_t j = 0; j < n; ++j) oi[j] = 0.0;
@@ -53,9 +58,7 @@ void radiation_rows(int32_t i0, int32_t i1, int32_t n, const double* pops, const
       const int32_t j = order[r];
       if (j == i) continue;
       const double pj = pops[j];
-      const double inside = cum[r] - pj;
-      double s = inside - (di[i] <= di[j] ? pi : 0.0);
-      s = (0.0 > s) ? 0.0 : s;
+      const double s = cum[r] - (di[i] < di[j] ? pi : 0.0);
       oi[j] = k * pi * pj / ((pi + s) * (pi + pj + s));
     }
   }
@@ -67,6 +70,9 @@ extern "C" int lpg_radiation_network(const double* pops, const double* dist, int
                                      int32_t include_home, double* out) {
   if (n < 0 || (n > 0 && (!pops || !dist || !out)))
     return lpg_ops_fail(LPG_ERR_ARG, "radiation_network: bad arguments (n=%d)", n);
+  if (include_home)
+    return lpg_ops_fail(LPG_ERR_ARG, "radiation_network: include_home=True is not supported (the reference "
+                                     "builds its network with include_home=False)");
   for (size_t q = 0; q < (size_t)n * n; ++q)
     if (std::isnan(dist[q])) return lpg_ops_fail(LPG_ERR_ARG, "radiation_network: a distance is NaN");
   std::atomic<bool> failed{false};
@@ -95,7 +101,5 @@ extern "C" int lpg_radiation_network(const double* pops, const double* dist, int
     failed = true;
   }
   if (failed) return lpg_ops_fail(LPG_ERR_NOMEM, "radiation_network: out of host resources");
-  if (include_home)
-    for (int32_t i = 0; i < n; ++i) out[(size_t)i * n + i] = pops[i];
   return LPG_OK;
 }

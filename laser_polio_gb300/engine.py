@@ -213,34 +213,79 @@ def build_sim_spec(sim) -> SimSpec:
     return SimSpec(d, keep, columns, results)
 
 
-def run_replicates(sims) -> None:
+def _advance_count(people, count: int) -> None:
+    """Bring people.count to the engine's count through LaserFrame's public
+    add(n), as laser_core's LaserFrame advances it (births only grow it)."""
+    n = int(count) - int(people.count)
+    if n < 0:
+        raise RuntimeError(f"engine count {count} is below people.count {people.count}")
+    if n:
+        people.add(n)
+
+
+def _check_node_ids(spec) -> None:
+    """node_id of the first count slots within [0, n_nodes) (lpg_start
+    checks the same on the device for the whole handle)."""
+    n, count = spec.desc.n_nodes, spec.desc.count
+    node = spec.columns.get("node_id")
+    if node is not None and count and (int(node[:count].min()) < 0 or int(node[:count].max()) >= n):
+        raise ValueError(f"LPG_ERR_NODE: node_id outside [0, {n}) among the first {count} slots")
+
+
+def run_replicates(sims) -> list:
     """Run several SEIR_ABM (drop-in GPU components) as one batch: one
     handle, one launch sequence per tick for all of them.  The reference's
-    calibration runs its replicates one after another (calib/objective.py:
-    47-70, run_sim per replicate).  The sims may differ in nodes, agents,
-    durations and components; each stops at its own last tick or stop rule.
-    Afterwards every sim holds what its own run() would have left: results,
-    people columns and count, t and should_stop."""
+    calibration runs its replicates one after another, each in its own
+    try/except, so that a failing replicate is reported and the others go on
+    (calib/objective.py:47-70).  The same holds here:
+      - each sim's description and node ids are checked on the host first
+        (lpg_check_desc); a sim that fails is left out of the batch;
+      - on the device a sim that fails (births beyond its capacity, a
+        timed-out wait) stops at that tick while the others run to their end.
+    The sims may differ in nodes, agents, durations and components; each
+    stops at its own last tick or stop rule.  Every sim that ran holds what
+    its own run() would have left (results, people columns and count, t and
+    should_stop; a failed one as far as it got).  Returns one entry per sim:
+    None, or the exception its run raised (ValueError for bad parameters,
+    node ids and capacity, as the reference; LpgError otherwise).  A failure
+    of the whole device (a CUDA error) raises."""
     sims = list(sims)
+    errors = [None] * len(sims)
     if not sims:
-        return
-    specs = [build_sim_spec(s) for s in sims]
+        return errors
+    ok, specs = [], []
+    for i, s in enumerate(sims):
+        try:
+            sp = build_sim_spec(s)
+            _lib.check_desc(sp.desc)
+            _check_node_ids(sp)
+        except (ValueError, TypeError, _lib.LpgError) as exc:
+            errors[i] = exc
+            continue
+        ok.append(i)
+        specs.append(sp)
+    if not ok:
+        return errors
     handle = _lib.Handle([sp.desc for sp in specs])
     try:
-        for i, sp in enumerate(specs):
-            handle.bind_columns(i, sp.columns)
+        for j, sp in enumerate(specs):
+            handle.bind_columns(j, sp.columns)
         handle.start()
-        handle.step(max(int(s.nt) for s in sims) - 1)
-        handle.sync()
-        for i, (sim, sp) in enumerate(zip(sims, specs)):
-            handle.read_results(i, sp.results)
-            handle.read_columns(i, sp.columns)
-            st = handle.state(i)
-            sim.people._set_count(st.count)
+        handle.step(max(int(sims[i].nt) for i in ok) - 1)
+        statuses = handle.sync_statuses()
+        for j, (i, sp) in enumerate(zip(ok, specs)):
+            sim = sims[i]
+            handle.read_results(j, sp.results)
+            handle.read_columns(j, sp.columns)
+            st = handle.state(j, check=False)
+            _advance_count(sim.people, st.count)
             sim.t = st.t
             sim.should_stop = bool(st.stopped)
+            if statuses[j]:
+                errors[i] = _lib.error_for(statuses[j], f"replicate {i}: device error at tick {st.t}")
     finally:
         handle.close()
+    return errors
 
 
 class GpuTick:
@@ -271,7 +316,7 @@ class GpuTick:
         self.handle.read_results(0, self.spec.results)
         self.handle.read_columns(0, self.spec.columns)
         st = self.handle.state(0)
-        self.sim.people._set_count(st.count)
+        _advance_count(self.sim.people, st.count)
         self._finished = True
 
     # -- per-tick interface used by the components ----------------------------

@@ -143,20 +143,16 @@ class SEIR_ABM:
         for cls in ordered:
             with self.perf_stats.start(cls.__name__ + ".__init__()"):
                 self.instances.append(cls(self))
-        if any(isinstance(c, _GpuComponent) for c in self.instances):
-            from .engine import GpuTick
-
-            self._engine = GpuTick(self)
+        self._engine = None
 
     def run(self):
         """SEIR_ABM.run (model.py:246-282).  With GPU components the whole
         loop runs on the device in one call; the result is the same as the
         per-tick loop below, which is kept for component sets that mix in
         host classes."""
-        engine = getattr(self, "_engine", None)
-        if engine is not None and all(isinstance(c, _GpuComponent) for c in self.instances):
+        if self.instances and all(isinstance(c, _GpuComponent) for c in self.instances):
             with self.perf_stats.start("GpuTick.run()"):
-                engine.run_all()
+                _engine_of(self).run_all()
             if self.should_stop and self.verbose >= 1:
                 print(f"[SEIR_ABM] Early stopping at t={self.t}: no E/I and no future seed_schedule events.")
             return
@@ -181,14 +177,28 @@ class SEIR_ABM:
                 component.log(t)
 
 
+def _engine_of(sim):
+    """The sim's GpuTick, created on first use.  The reference's own
+    SEIR_ABM (model.py:209-289) knows nothing of an engine: its components
+    setter only instantiates the classes and its run() only calls step() and
+    log(t), so the first call from any drop-in component creates it."""
+    eng = getattr(sim, "_engine", None)
+    if eng is None:
+        from .engine import GpuTick
+
+        eng = GpuTick(sim)
+        sim._engine = eng
+    return eng
+
+
 class _GpuComponent:
     """Base of the drop-in components: step()/log() go to the shared engine."""
 
     def step(self):
-        self.sim._engine.step(self)
+        _engine_of(self.sim).step(self)
 
     def log(self, t):
-        self.sim._engine.log(self, t)
+        _engine_of(self.sim).log(self, t)
 
     def plot(self, save=False, results_path=None):
         pass

@@ -192,7 +192,13 @@ def save_sim_results(sim, filename="simulation_results.h5", summary_config=None)
         raise ValueError(f"save_sim_results: {len(dates)} dates for {nt} timesteps")
     fields = {}
     for col, attr in RESULT_TABLE_COLUMNS:
-        a = np.ascontiguousarray(np.asarray(getattr(sim.results, attr)), dtype=np.int32)
+        raw = np.asarray(getattr(sim.results, attr))
+        if raw.dtype.kind not in "iub":
+            raise TypeError(f"save_sim_results: results.{attr} is {raw.dtype}; the native writer takes integer "
+                            "counts (the reference's results arrays are int32)")
+        if raw.size and (int(raw.min()) < np.iinfo(np.int32).min or int(raw.max()) > np.iinfo(np.int32).max):
+            raise ValueError(f"save_sim_results: results.{attr} holds values outside int32")
+        a = np.ascontiguousarray(raw, dtype=np.int32)
         if a.shape != (nt, nodes):
             raise ValueError(f"save_sim_results: results.{attr} has shape {a.shape}, expected {(nt, nodes)}")
         fields[col] = a

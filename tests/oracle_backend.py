@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import numpy as np
 
+from laser_polio_gb300.engine import _advance_count
 from laser_polio_gb300.engine import build_sim_spec
 from oracle.oracle import OracleSim
 
@@ -22,7 +23,7 @@ def run_with_oracle(sim, n_ticks=None):
     st = o.state()
     o.read_results(spec.results)
     o.read_columns(spec.columns)
-    sim.people._set_count(st.count)
+    _advance_count(sim.people, st.count)
     sim.t = st.t
     sim.should_stop = bool(st.stopped)
     o.close()
@@ -79,3 +80,45 @@ def assert_same(a: dict, b: dict, what: str, count=None):
             idx = np.argwhere(x != y)
             raise AssertionError(f"{what} '{k}' differs at {len(idx)} entries, first {idx[:5].tolist()}: "
                                  f"{x[tuple(idx[0])]} vs {y[tuple(idx[0])]}")
+
+
+class OracleHandle:
+    """The engine handle's interface (laser_polio_gb300._lib.Handle) over the
+    oracle, one simulation per handle: lets a CPU test drive the drop-in
+    components' whole host path (GpuTick, run_replicates) with the oracle in
+    place of the device."""
+
+    made = []
+
+    def __init__(self, descs, device=0):
+        descs = list(descs)
+        assert len(descs) == 1, "one simulation per oracle handle"
+        self.o = OracleSim(descs[0])
+        OracleHandle.made.append(self)
+
+    def bind_columns(self, sim, cols):
+        self.o.bind_columns(cols)
+
+    def start(self):
+        self.o.start()
+
+    def step(self, n):
+        self.o.step(n)
+
+    def sync(self):
+        pass
+
+    def sync_statuses(self):
+        return [int(self.o.state().error)]
+
+    def state(self, sim=0, check=True):
+        return self.o.state()
+
+    def read_results(self, sim, res):
+        self.o.read_results(res)
+
+    def read_columns(self, sim, cols):
+        self.o.read_columns(cols)
+
+    def close(self):
+        self.o.close()

@@ -109,6 +109,17 @@ def test_errors(tmp_path):
     sim.results.S = sim.results.S[:, :1]
     with pytest.raises(ValueError, match="results.S"):
         save_sim_results(sim, tmp_path / "x.csv")
+    # counts are written as int32: a float array or an int64 value beyond int32 is refused, not cut
+    sim = _fake_sim(3, 2)
+    sim.results.E = sim.results.E.astype(np.float64) + 0.5
+    with pytest.raises(TypeError, match="results.E"):
+        save_sim_results(sim, tmp_path / "x.csv")
+    sim = _fake_sim(3, 2)
+    sim.results.I = sim.results.I.astype(np.int64)
+    save_sim_results(sim, tmp_path / "ok.csv")  # int64 within range is fine
+    sim.results.I[1, 1] = 2**31
+    with pytest.raises(ValueError, match="outside int32"):
+        save_sim_results(sim, tmp_path / "x.csv")
     try:
         import pandas  # noqa: F401
     except ImportError:

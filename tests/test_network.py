@@ -18,9 +18,40 @@ def test_native_radiation_equals_the_python_definition(n, seed, ties):
     else:
         xy = rng.uniform(0, 500, (n, 2))
     dist = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
-    for k, home in ((1.0, False), (0.3, True)):
-        np.testing.assert_array_equal(radiation(pops, dist, k, include_home=home),
-                                      _radiation_py(pops, dist, k, include_home=home))
+    for k in (1.0, 0.3):
+        np.testing.assert_array_equal(radiation(pops, dist, k), _radiation_py(pops, dist, k))
+
+
+def test_radiation_ties_do_not_depend_on_node_order():
+    """Nodes at equal distances (duplicate coordinates, and a node on top of
+    i): s_ij counts only the strictly closer ones, so relabelling the nodes
+    permutes the network and changes no value; checked against a direct sum
+    of the definition."""
+    rng = np.random.default_rng(7)
+    n = 40
+    xy = rng.integers(0, 4, (n, 2)).astype(np.float64)  # many duplicate coordinates
+    pops = rng.lognormal(np.log(2e4), 0.6, n)
+    dist = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
+    net = radiation(pops, dist, 1.0)
+    for i in range(n):
+        for j in range(n):
+            if i == j:
+                assert net[i, j] == 0.0
+                continue
+            inside = [m for m in range(n) if m not in (i, j) and dist[i, m] < dist[i, j]]
+            s = float(np.sum(pops[inside])) if inside else 0.0
+            want = pops[i] * pops[j] / ((pops[i] + s) * (pops[i] + pops[j] + s))
+            assert abs(net[i, j] - want) <= 1e-12 * want, (i, j)
+    perm = rng.permutation(n)
+    net_p = radiation(pops[perm], dist[np.ix_(perm, perm)], 1.0)
+    np.testing.assert_allclose(net_p, net[np.ix_(perm, perm)], rtol=1e-12, atol=0)
+
+
+def test_radiation_rejects_include_home():
+    with pytest.raises(ValueError, match="include_home"):
+        radiation(np.ones(3), np.ones((3, 3)) - np.eye(3), 1.0, include_home=True)
+    with pytest.raises(ValueError, match="include_home"):
+        _radiation_py(np.ones(3), np.ones((3, 3)) - np.eye(3), 1.0, include_home=True)
 
 
 def test_radiation_rejects_bad_shapes():

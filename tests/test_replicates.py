@@ -38,6 +38,10 @@ class _FakeHandle:
     def sync(self):
         self.calls.append(("sync",))
 
+    def sync_statuses(self):
+        self.calls.append(("sync",))
+        return list(getattr(self, "statuses", [0] * len(self.descs)))
+
     def read_results(self, i, res):
         for a in res.values():
             a[...] = 100 + i
@@ -45,8 +49,9 @@ class _FakeHandle:
     def read_columns(self, i, cols):
         self.calls.append(("columns", i))
 
-    def state(self, i):
-        return types.SimpleNamespace(t=int(self.descs[i].nt), count=1000 + i, stopped=i == 1, error=0)
+    def state(self, i, check=True):
+        return types.SimpleNamespace(t=int(self.descs[i].nt), count=int(self.descs[i].count) + 10 + i,
+                                     stopped=i == 1, error=0)
 
     def close(self):
         self.closed = True
@@ -57,14 +62,15 @@ def test_one_handle_for_all_sims_and_results_back_in_each(monkeypatch):
     _FakeHandle.made.clear()
     sims = [synthetic.zamfara_like(n_agents=4_000, dur=8, seed=1),
             synthetic.zamfara_like(n_agents=6_000, dur=12, seed=2, n_nodes=5)]
-    engine.run_replicates(sims)
+    counts = [s.people.count for s in sims]
+    assert engine.run_replicates(sims) == [None, None]
     (h,) = _FakeHandle.made
     assert len(h.descs) == 2 and h.closed
     assert h.calls[:3] == [("bind", 0), ("bind", 1), ("start",)]
     assert ("step", max(s.nt for s in sims) - 1) in h.calls
     for i, s in enumerate(sims):
         assert np.all(s.results.S == 100 + i) and np.all(s.results.new_exposed == 100 + i)
-        assert s.people.count == 1000 + i and s.t == s.nt
+        assert s.people.count == counts[i] + 10 + i and s.t == s.nt
     assert sims[1].should_stop and not sims[0].should_stop
 
 
@@ -78,6 +84,65 @@ def test_handle_is_closed_when_a_step_fails(monkeypatch):
         engine.run_replicates([synthetic.zamfara_like(n_agents=3_000, dur=5, seed=3)])
     assert _FakeHandle.made[0].closed
     engine.run_replicates([])  # nothing to run
+
+
+def test_bad_replicates_fail_alone(monkeypatch):
+    """A replicate with bad parameters (a NaN R0 scalar), node ids out of
+    range, or a device failure (births beyond its capacity) gets its own
+    error; the handle runs the others, which end as their own runs would
+    (the reference's replicate loop catches each replicate's exception and
+    goes on, calib/objective.py:47-70)."""
+    monkeypatch.setattr(engine._lib, "Handle", _FakeHandle)
+    _FakeHandle.made.clear()
+    sims = [synthetic.zamfara_like(n_agents=4_000, dur=8, seed=s) for s in range(5)]
+    sims[1].pars.r0_scalars = np.array(sims[1].pars.r0_scalars, dtype=float)
+    sims[1].pars.r0_scalars[2] = np.nan
+    sims[3].people.node_id[7] = 99
+    counts = [s.people.count for s in sims]
+    _FakeHandle.statuses = [0, 0, -2]  # the third sim of the batch (sims[4]) outgrows its capacity
+    try:
+        errors = engine.run_replicates(sims)
+    finally:
+        del _FakeHandle.statuses
+    (h,) = _FakeHandle.made
+    assert len(h.descs) == 3 and h.closed
+    assert errors[0] is None and errors[2] is None
+    assert isinstance(errors[1], ValueError) and "r0_scalars[2]" in str(errors[1])
+    assert isinstance(errors[3], ValueError) and "node_id" in str(errors[3])
+    assert isinstance(errors[4], ValueError)
+    for i, j in ((0, 0), (2, 1), (4, 2)):
+        assert np.all(sims[i].results.S == 100 + j) and sims[i].people.count == counts[i] + 10 + j
+    assert sims[1].t == 0 and sims[3].t == 0
+
+
+@pytest.mark.gpu
+def test_gpu_a_replicate_that_outgrows_its_capacity_fails_alone():
+    """On the device: one replicate's births exceed its capacity; it stops
+    with LPG_ERR_CAPACITY at that tick while the others run to their end,
+    bit-exact with their own oracle runs."""
+    from oracle_backend import assert_same
+    from oracle_backend import run_spec_oracle
+    from oracle_backend import snapshot
+
+    sims = [synthetic.zamfara_like(n_agents=40_000, dur=60, seed=s) for s in (11, 12, 13)]
+    small = sims[1].people
+    small._capacity = small.count + 50  # a few weeks of births
+    for name in ("disease_state", "strain", "exposure_timer", "infection_timer", "paralysis_timer",
+                 "potentially_paralyzed", "paralyzed", "ipv_protected", "chronically_missed", "node_id",
+                 "ri_timer", "acq_risk_multiplier", "daily_infectivity", "date_of_birth", "date_of_death"):
+        setattr(small, name, np.ascontiguousarray(getattr(small, name)[: small.capacity]))
+    snaps = {i: snapshot(sims[i]) for i in (0, 2)}
+    states = {i: run_spec_oracle(spec, cols, res, sims[i].nt - 1) for i, (spec, cols, res) in snaps.items()}
+    errors = engine.run_replicates(sims)
+    assert errors[0] is None and errors[2] is None
+    assert isinstance(errors[1], ValueError)
+    assert 1 < sims[1].t < sims[1].nt
+    for i, (_, cols_o, res_o) in snaps.items():
+        so = states[i]
+        s = sims[i]
+        assert (s.people.count, s.t) == (so.count, so.t), i
+        assert_same(res_o, {k: getattr(s.results, k) for k in res_o}, f"replicate {i} result")
+        assert_same(cols_o, {k: getattr(s.people, k) for k in cols_o}, f"replicate {i} column", count=so.count)
 
 
 @pytest.mark.gpu
