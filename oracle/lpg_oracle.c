@@ -910,6 +910,45 @@ int lpo_read_aggregates_fp64(lpo_sim* s, double* srisk, double* beta) {
   return 0;
 }
 
+/* Single draws of the counter-based hook, for a harness that hands them to
+ * another implementation of the same step (the reference's own code run
+ * with its random calls redirected): each returns exactly what the oracle
+ * and the engine draw for that (purpose, tick, a, b, k). */
+double lpo_u01(uint64_t seed, int32_t purpose, int32_t t, uint64_t a, uint64_t b, uint64_t k) {
+  return lpg_u01(seed, (uint32_t)purpose, t, a, b, k);
+}
+uint64_t lpo_u53(uint64_t seed, int32_t purpose, int32_t t, uint64_t a, uint64_t b, uint64_t k) {
+  return lpg_u53(seed, (uint32_t)purpose, t, a, b, k);
+}
+uint64_t lpo_raw(uint64_t seed, int32_t purpose, int32_t t, uint64_t a, uint64_t b, uint64_t k) {
+  return lpg_raw(seed, (uint32_t)purpose, t, a, b, k);
+}
+/* The node's exposure-count stream (lpo_node_tx): its first uniform (the
+ * zero-inflation test), the negative binomial drawn after it, or the
+ * Poisson count from its start. */
+double lpo_tx_u0(uint64_t seed, int32_t t, uint64_t node) {
+  lpg_stream st;
+  lpg_stream_init(&st, seed, LPG_P_TXCOUNT, t, node, 0);
+  return lpg_next(&st);
+}
+int64_t lpo_tx_negbinom(uint64_t seed, int32_t t, uint64_t node, double r, double p) {
+  lpg_stream st;
+  lpg_stream_init(&st, seed, LPG_P_TXCOUNT, t, node, 0);
+  (void)lpg_next(&st);
+  return lpg_negbinom(&st, r, p);
+}
+int64_t lpo_tx_poisson(uint64_t seed, int32_t t, uint64_t node, double lam) {
+  lpg_stream st;
+  lpg_stream_init(&st, seed, LPG_P_TXCOUNT, t, node, 0);
+  return lpg_poisson(&st, lam);
+}
+/* The infection timer a seed event e redraws for slot (lpo_seed). */
+double lpo_seed_timer(uint64_t seed, int32_t t, uint64_t slot, uint64_t e, int kind, double p1, double p2) {
+  lpg_stream st;
+  lpg_stream_init(&st, seed, LPG_P_SEEDTIMER, t, slot, e);
+  return lpg_dist_sample(&st, kind, p1, p2);
+}
+
 /* Building blocks exposed for the unit tests of the draw hook. */
 void lpo_philox(uint64_t ctr[4], uint64_t k0, uint64_t k1) { lpg_philox4x64_10(ctr, k0, k1); }
 double lpo_exp(double x) { return lpg_exp(x); }

@@ -51,6 +51,17 @@ def lib():
         L.lpo_record_aggregates.argtypes = [C.c_void_p, C.c_int]
         L.lpo_read_aggregates.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 4
         L.lpo_read_aggregates_fp64.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 2
+        for name, res in (("lpo_u01", C.c_double), ("lpo_u53", C.c_uint64), ("lpo_raw", C.c_uint64)):
+            getattr(L, name).restype = res
+            getattr(L, name).argtypes = [C.c_uint64, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, C.c_uint64]
+        L.lpo_tx_u0.restype = C.c_double
+        L.lpo_tx_u0.argtypes = [C.c_uint64, C.c_int32, C.c_uint64]
+        L.lpo_tx_negbinom.restype = C.c_int64
+        L.lpo_tx_negbinom.argtypes = [C.c_uint64, C.c_int32, C.c_uint64, C.c_double, C.c_double]
+        L.lpo_tx_poisson.restype = C.c_int64
+        L.lpo_tx_poisson.argtypes = [C.c_uint64, C.c_int32, C.c_uint64, C.c_double]
+        L.lpo_seed_timer.restype = C.c_double
+        L.lpo_seed_timer.argtypes = [C.c_uint64, C.c_int32, C.c_uint64, C.c_uint64, C.c_int, C.c_double, C.c_double]
         _lib = L
     return _lib
 
