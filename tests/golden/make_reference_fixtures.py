@@ -1,6 +1,7 @@
 """Golden outputs of the reference's own code, for the parity tests.
 
-    python tests/golden/make_reference_fixtures.py <reference checkout> [--cases busy,stop] [--native N]
+    python tests/golden/make_reference_fixtures.py <reference checkout> [--cases busy,stop]
+    python tests/golden/make_reference_fixtures.py <reference checkout> --native 200
 
 Imports the unmodified laser_polio package from <checkout>/src with the
 stand-ins and the draw hook of reference_harness.py, and writes:
@@ -12,6 +13,9 @@ stand-ins and the draw hook of reference_harness.py, and writes:
       counter-based draws: every results array, the final agent columns
       (stored as their XOR with the initial ones, which is mostly zeros),
       t, count and the stop flag, and how many draws of each kind it made.
+  reference_native.npz  (--native N) the native case's description and
+      initial table, and the new exposures per tick and node of N reference
+      runs with numpy's own generator (seeds 1 .. N), without the hook.
 
 The reference checkout is read, never written; the reference's logger writes
 its log files under a temporary working directory.
@@ -170,13 +174,91 @@ def run_replay(lp, harness, cases_mod, name, pyramid):
     return desc, cols, res, final, state, hook.calls
 
 
+NATIVE_CASE = "native"
+_NATIVE = {}
+
+
+def _native_worker_init(ref):
+    import reference_harness as harness
+
+    os.chdir(tempfile.mkdtemp())  # the reference's logger writes logs/ into the working directory
+    _NATIVE["lp"] = harness.import_reference(Path(ref) / "src")
+    _NATIVE["pyramid"] = Path(ref) / "data" / "Nigeria_age_pyramid_2024.csv"
+
+
+def _native_run(seed):
+    """One reference run of the native case with numpy's own generator
+    seeded with ``seed`` (laser_core's seed, through SEIR_ABM's init): the
+    new exposures per tick and node."""
+    import replay_cases
+    from laser_core.propertyset import PropertySet
+
+    lp = _NATIVE["lp"]
+    pars = replay_cases.make_pars(NATIVE_CASE, lp, PropertySet, _NATIVE["pyramid"])
+    pars.seed = int(seed)
+    sim = lp.SEIR_ABM(pars)
+    sim.components = replay_cases.components(lp)
+    cols = replay_cases.initial_columns(NATIVE_CASE, sim.people.count, sim.people.capacity,
+                                        np.asarray(sim.pars.init_pop), seed=1000 + sum(map(ord, NATIVE_CASE)))
+    for k, v in cols.items():
+        getattr(sim.people, k)[:] = v
+    sim.run()
+    return np.asarray(sim.results.new_exposed, np.int32)
+
+
+def native(ref, n_seeds, out_path, workers):
+    """reference_native.npz: the native case's description and initial table
+    (as in the replay file) and the reference's new exposures per tick and
+    node for seeds 1 .. n_seeds."""
+    import multiprocessing as mp
+
+    import reference_harness as harness
+    import replay_cases
+
+    cwd = os.getcwd()
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        os.chdir(tmp)
+        try:
+            lp = harness.import_reference(Path(ref) / "src")
+            from laser_core.propertyset import PropertySet
+
+            pars = replay_cases.make_pars(NATIVE_CASE, lp, PropertySet, Path(ref) / "data" / "Nigeria_age_pyramid_2024.csv")
+            sim = lp.SEIR_ABM(pars)
+            sim.components = replay_cases.components(lp)
+            cols = replay_cases.initial_columns(NATIVE_CASE, sim.people.count, sim.people.capacity,
+                                                np.asarray(sim.pars.init_pop), seed=1000 + sum(map(ord, NATIVE_CASE)))
+            for k, v in cols.items():
+                getattr(sim.people, k)[:] = v
+            pack_desc(f"{NATIVE_CASE}/desc", describe(lp, sim), out)
+            for k, v in cols.items():
+                out[f"{NATIVE_CASE}/in/{k}"] = v
+        finally:
+            os.chdir(cwd)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers, initializer=_native_worker_init, initargs=(str(ref),)) as pool:
+        runs = pool.map(_native_run, range(1, n_seeds + 1))
+    out[f"{NATIVE_CASE}/new_exposed"] = np.stack(runs)
+    out[f"{NATIVE_CASE}/seeds"] = np.arange(1, n_seeds + 1)
+    np.savez_compressed(out_path, **out)
+    tot = out[f"{NATIVE_CASE}/new_exposed"].sum(axis=(1, 2))
+    print(f"wrote {out_path}: {n_seeds} reference runs, total new exposures mean {tot.mean():.1f} "
+          f"sd {tot.std():.1f} ({Path(out_path).stat().st_size} bytes)")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("reference", help="path of the laser-polio checkout")
     ap.add_argument("--cases", default=None)
     ap.add_argument("--out", default=str(HERE / "reference_replay.npz"))
+    ap.add_argument("--native", type=int, default=0, metavar="N",
+                    help="instead: N reference runs of the native case with numpy's own generator")
+    ap.add_argument("--workers", type=int, default=os.cpu_count() or 1)
     args = ap.parse_args()
     ref = Path(args.reference).resolve()
+    if args.native:
+        native(ref, args.native, HERE / "reference_native.npz", args.workers)
+        return
     pyramid = ref / "data" / "Nigeria_age_pyramid_2024.csv"
     import reference_harness as harness
     import replay_cases

@@ -57,6 +57,10 @@ def make_pars(name, lp, property_set, pyramid_path=None):
             radiation_k_log10=-0.3, max_migr_frac=0.2, vx_prob_ri=0.5, vx_prob_ipv=0.1,
             stop_if_no_cases=False, p_paralysis=1 / 2000, dur_inf=lp.gamma(shape=4, scale=6.0),
         )
+    elif name == "native":  # the zamfara case's first 120 ticks: an outbreak growing in 14 nodes
+        p = dict(make_pars("zamfara", lp, dict, pyramid_path))
+        p.update(dur=120)
+        return property_set(p)
     elif name == "collisions":
         p.update(
             seed=77, dur=40, init_pop=np.array([3000, 1500, 800]), cbr=np.array([30.0, 30.0, 30.0]),
@@ -96,6 +100,7 @@ def initial_columns(name, count, capacity, init_pop, seed):
         rng.shuffle(node)  # slots of the nodes interleaved, as after births
     state = rng.choice(np.array([0, 1, 2, 3], np.int8), n,
                        p={"busy": [0.55, 0.03, 0.04, 0.38], "zamfara": [0.35, 0.0, 0.002, 0.648],
+                          "native": [0.35, 0.0, 0.002, 0.648],
                           "collisions": [0.97, 0.0, 0.03, 0.0], "stop": [0.6, 0.0, 0.001, 0.399]}[name])
     strain = np.where(rng.random(n) < 0.8, 0, rng.integers(1, 3, n)).astype(np.int8)
     strain[(state != 1) & (state != 2)] = 0
