@@ -224,6 +224,13 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def wait_ready(self, timeout=10.0):
+        """Block until nvidia-smi has printed its first sample: its start-up
+        takes driver locks that would otherwise land inside a timed region."""
+        t0 = time.perf_counter()
+        while self.proc is not None and not self.lines and time.perf_counter() - t0 < timeout:
+            time.sleep(0.02)
+
     def __exit__(self, *exc):
         if self.proc is not None:
             self.proc.terminate()
@@ -506,6 +513,7 @@ def batch_arm(args):
         return ms, at, launches
 
     with ClockSampler(0) as clocks:
+        clocks.wait_ready()
         ms_b, at_b, _ = timed(list(range(len(bundles))))
     ms_s, at_s = 0.0, 0.0
     for i in range(len(bundles)):
@@ -562,6 +570,7 @@ def incidence_arm(args):
     W, K = max(3, args.warmup), max(1, min(args.steps, 200))
     torch.cuda.synchronize()
     with ClockSampler(0) as clocks:
+        clocks.wait_ready()
         t0 = time.perf_counter()
         plan = ops.IncidencePlan(inp, target)
         t_setup = time.perf_counter() - t0
@@ -760,6 +769,7 @@ def main():
 
     clocks = ClockSampler(dev)
     clocks.__enter__()  # the whole device phase: end to end, timed region, full run, profiling
+    clocks.wait_ready()
 
     # ---- end to end through the C ABI from pinned host columns --------------
     e2e = None

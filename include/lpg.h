@@ -317,6 +317,77 @@ const char* lpg_last_error(const lpg_handle* h);
 void lpg_destroy(lpg_handle* h);
 
 /* ---------------------------------------------------------------------- */
+/* Initialisation of the agent table on the device.
+ *
+ * The reference fills its columns in SEIR_ABM.__init__ and in each
+ * component's constructor with numpy draws (model.py:101-175, 561-713,
+ * 816-866, 1548-1611, 1887-1894; flagged slow at :852).  lpg_init_columns
+ * fills the same columns with this project's counter-based draws, in
+ * reference slot order, on the device.  `parts` selects what to fill, in the
+ * order of the bits below; a part reads what earlier parts (of this call or
+ * an earlier one) wrote.  Each part writes the columns named beside it, over
+ * the whole capacity:
+ *   LPG_INIT_BASE        disease_state (0 for the first count slots, -1 after),
+ *                        node_id (node-contiguous from node_pop, -1 after),
+ *                        strain 0, potentially_paralyzed -1, paralyzed 0,
+ *                        ipv_protected 0, chronically_missed 0 (model.py:139-162)
+ *   LPG_INIT_MISSED      chronically_missed = 1 for missed_k agents chosen
+ *                        without replacement among the first count (:155-158)
+ *   LPG_INIT_TIMERS      exposure_timer, infection_timer, paralysis_timer (:575-587)
+ *   LPG_INIT_IMMUNITY    disease_state = 3 for immune_k[n] agents of each node,
+ *                        chosen without replacement (:589-618)
+ *   LPG_INIT_PREVALENCE  disease_state = 2 for prev_k agents chosen among all
+ *                        (prev_per_node 0, prev_k[0]) or prev_k[n] per node (:670-713)
+ *   LPG_INIT_HETEROGENEITY acq_risk_multiplier, daily_infectivity (:816-866)
+ *   LPG_INIT_AGES        date_of_birth (-age for the first count, -1 after) (:1576-1596)
+ *   LPG_INIT_DEATHS      date_of_death (age at death - age; 0 after) (:1605-1611)
+ *   LPG_INIT_RI          ri_timer (date of birth + [42, 98) days; -1 after) (:1887-1894)
+ * Selections take the agents with the smallest counter-based keys (exactly
+ * k of the group, every subset equally likely).  Column pointers are device
+ * memory of `capacity` elements; only those a requested part writes or reads
+ * need be set.  Asynchronous on `stream`; scratch comes from
+ * cudaMallocAsync on it.  Errors: lpg_op_last_error(). */
+enum {
+  LPG_INIT_BASE = 1,
+  LPG_INIT_MISSED = 2,
+  LPG_INIT_TIMERS = 4,
+  LPG_INIT_IMMUNITY = 8,
+  LPG_INIT_PREVALENCE = 16,
+  LPG_INIT_HETEROGENEITY = 32,
+  LPG_INIT_AGES = 64,
+  LPG_INIT_DEATHS = 128,
+  LPG_INIT_RI = 256
+};
+
+typedef struct {
+  int32_t n_nodes;
+  int32_t prev_per_node;     /* LPG_INIT_PREVALENCE: 1 = prev_k[n] per node, 0 = prev_k[0] among all */
+  int64_t count, capacity;
+  uint64_t seed;
+  const int64_t* node_pop;   /* [n_nodes] initial agents per node (pars.init_pop) */
+  int64_t missed_k;          /* int(missed_frac * count) */
+  const int64_t* immune_k;   /* [n_nodes] int(immunity fraction * node pop) */
+  const int64_t* prev_k;     /* [n_nodes] or [1] */
+  lpg_dist dur_exp, dur_inf, t_to_paralysis;
+  int32_t heterogeneity;     /* pars.individual_heterogeneity */
+  int32_t n_age_bins;
+  double risk_mult_var, corr_risk_inf;
+  double r0;                 /* infectivity mean = r0 / mean of 1000 infectious durations */
+  const int32_t* age_lo_days;  /* [n_age_bins] inclusive: max(min age * 365, 1) */
+  const int32_t* age_hi_days;  /* [n_age_bins] exclusive: (max age + 1) * 365 */
+  const int64_t* age_weight;   /* [n_age_bins] */
+  const int64_t* km_cumdeaths; /* cumulative deaths by age-year (utils.py:795-816) */
+  int32_t km_len, km_max_year;
+} lpg_init_desc;
+
+int lpg_init_columns(const lpg_init_desc* d, uint32_t parts, const lpg_columns* cols, void* stream);
+
+/* The mean daily infectivity the initialisation scales to,
+ * r0 / mean(dur_inf(1000)) (model.py:843; the mean of 1000 draws, as the
+ * reference estimates it), with this project's draws.  Host only. */
+double lpg_init_mean_infectivity(uint64_t seed, double r0, lpg_dist dur_inf);
+
+/* ---------------------------------------------------------------------- */
 /* Standalone ops over plain device columns (no handle).  Asynchronous on
  * `stream` (a cudaStream_t; NULL = the legacy default stream) on the
  * current device.  Errors: a negative lpg_status; the text from

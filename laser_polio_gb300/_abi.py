@@ -136,6 +136,39 @@ class lpg_columns(C.Structure):
     _fields_ = [(name, ptype) for name, ptype, _ in COLUMN_FIELDS]
 
 
+# lpg_init_columns' parts, in the order they run
+INIT_BASE, INIT_MISSED, INIT_TIMERS, INIT_IMMUNITY, INIT_PREVALENCE = 1, 2, 4, 8, 16
+INIT_HETEROGENEITY, INIT_AGES, INIT_DEATHS, INIT_RI = 32, 64, 128, 256
+
+
+class lpg_init_desc(C.Structure):
+    _fields_ = [
+        ("n_nodes", C.c_int32),
+        ("prev_per_node", C.c_int32),
+        ("count", C.c_int64),
+        ("capacity", C.c_int64),
+        ("seed", C.c_uint64),
+        ("node_pop", P_i64),
+        ("missed_k", C.c_int64),
+        ("immune_k", P_i64),
+        ("prev_k", P_i64),
+        ("dur_exp", lpg_dist),
+        ("dur_inf", lpg_dist),
+        ("t_to_paralysis", lpg_dist),
+        ("heterogeneity", C.c_int32),
+        ("n_age_bins", C.c_int32),
+        ("risk_mult_var", C.c_double),
+        ("corr_risk_inf", C.c_double),
+        ("r0", C.c_double),
+        ("age_lo_days", P_i32),
+        ("age_hi_days", P_i32),
+        ("age_weight", P_i64),
+        ("km_cumdeaths", P_i64),
+        ("km_len", C.c_int32),
+        ("km_max_year", C.c_int32),
+    ]
+
+
 RESULT_FIELDS = [
     ("S", False),
     ("E", False),

@@ -60,6 +60,9 @@ SIGNATURES = {
                                         C.c_int32, C.POINTER(C.c_double)]),
     "lpg_op_last_error": (C.c_char_p, []),
     "lpg_check_desc": (C.c_int, [C.POINTER(_abi.lpg_sim_desc)]),
+    "lpg_init_columns": (C.c_int, [C.POINTER(_abi.lpg_init_desc), C.c_uint32, C.POINTER(_abi.lpg_columns),
+                                   C.c_void_p]),
+    "lpg_init_mean_infectivity": (C.c_double, [C.c_uint64, C.c_double, _abi.lpg_dist]),
     "lpg_test_stall_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
 }
 

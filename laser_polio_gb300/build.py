@@ -17,10 +17,10 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build" / "liblpg.so"
-SOURCES = [CSRC / "lpg_engine.cu", CSRC / "lpg_ops.cu", CSRC / "lpg_adjoint.cu", CSRC / "lpg_export.cpp",
-           CSRC / "lpg_network.cpp"]
+SOURCES = [CSRC / "lpg_engine.cu", CSRC / "lpg_ops.cu", CSRC / "lpg_adjoint.cu", CSRC / "lpg_init.cu",
+           CSRC / "lpg_export.cpp", CSRC / "lpg_network.cpp"]
 DEPS = SOURCES + [CSRC / "lpg_kernels.cuh", CSRC / "lpg_engine.cuh", CSRC / "lpg_rng.h", CSRC / "lpg_detmath.h",
-                  CSRC / "lpg_ri.h", ROOT / "include" / "lpg.h"]
+                  CSRC / "lpg_ri.h", CSRC / "lpg_init.h", ROOT / "include" / "lpg.h"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler",
          "-fPIC,-ffp-contract=off,-fno-math-errno,-pthread"]

@@ -42,7 +42,17 @@ enum {
   LPG_P_SELECT = 7,     /* a = node, b = round, k = draw  */
   LPG_P_STRAIN = 8,     /* a = slot                       */
   LPG_P_SEEDPICK = 9,   /* a = slot, b = seed event       */
-  LPG_P_SEEDTIMER = 10  /* a = slot, b = seed event, k    */
+  LPG_P_SEEDTIMER = 10, /* a = slot, b = seed event, k    */
+  /* initialisation (tick 0) */
+  LPG_P_INIT_MISSED = 11,  /* a = slot: selection key          */
+  LPG_P_INIT_IMMUNE = 12,  /* a = slot: selection key          */
+  LPG_P_INIT_PREV = 13,    /* a = slot: selection key          */
+  LPG_P_INIT_TIMER = 14,   /* a = slot, b = 0 exposure, 1 infection, 2 paralysis */
+  LPG_P_INIT_HET = 15,     /* a = slot: two normals            */
+  LPG_P_INIT_AGE = 16,     /* a = slot: age bin, day           */
+  LPG_P_INIT_KM = 17,      /* a = slot: year, day of death     */
+  LPG_P_INIT_RI = 18,      /* a = slot: day of RI              */
+  LPG_P_INIT_MEANINF = 19  /* the 1000 infectious durations whose mean scales infectivity */
 };
 
 #define LPG_PHILOX_M0 0xD2E7470EE14C6C93ULL

@@ -15,7 +15,7 @@ ROOT = HERE.parent
 OUT = HERE / "_build" / "liblpg_oracle.so"
 SRC = HERE / "lpg_oracle.c"
 HEADERS = [ROOT / "include" / "lpg.h", ROOT / "laser_polio_gb300" / "csrc" / "lpg_rng.h",
-           ROOT / "laser_polio_gb300" / "csrc" / "lpg_detmath.h"]
+           ROOT / "laser_polio_gb300" / "csrc" / "lpg_detmath.h", ROOT / "laser_polio_gb300" / "csrc" / "lpg_init.h"]
 
 
 def build(force: bool = False) -> Path:

@@ -31,6 +31,7 @@
 
 #include "lpg.h"
 #include "lpg_rng.h"
+#include "lpg_init.h"
 
 #define NRES 22
 enum {
@@ -907,6 +908,128 @@ int lpo_read_aggregates_fp64(lpo_sim* s, double* srisk, double* beta) {
     if (beta)
       for (int k = 0; k < NS; ++k) beta[q * NS + k] = b[1 + k];
   }
+  return 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Initialisation (the engine's lpg_init_columns), restated for host columns:
+ * the per-slot parts with the arithmetic of lpg_init.h (each citing the
+ * reference lines it follows), the choices without replacement by sorting
+ * each group's (key, slot) pairs and taking the k smallest, which is the
+ * set the engine's radix select finds. */
+static void lpo_select(uint64_t seed, uint32_t purpose, const int64_t* start, int G, const int64_t* k, int action,
+                       const lpg_columns* c) {
+  for (int g = 0; g < G; ++g) {
+    const int64_t s0 = start[g], n = start[g + 1] - start[g];
+    const int64_t kk = k[g];
+    if (kk <= 0 || n <= 0) continue;
+    keyslot* ks = malloc((size_t)n * sizeof(keyslot));
+    for (int64_t j = 0; j < n; ++j) {
+      ks[j].key = lpg_raw(seed, purpose, 0, (uint64_t)(s0 + j), 0, 0);
+      ks[j].slot = s0 + j;
+    }
+    if (kk < n) qsort(ks, (size_t)n, sizeof(keyslot), cmp_keyslot);
+    const int64_t take = kk < n ? kk : n;
+    for (int64_t j = 0; j < take; ++j) {
+      const int64_t i = ks[j].slot;
+      if (action == 0) c->chronically_missed[i] = 1;
+      else if (action == 1) c->disease_state[i] = 3;
+      else c->disease_state[i] = 2;
+    }
+    free(ks);
+  }
+}
+
+double lpo_init_mean_infectivity(uint64_t seed, double r0, lpg_dist dur_inf) {
+  lpg_stream st;
+  lpg_stream_init(&st, seed, LPG_P_INIT_MEANINF, 0, 0, 0);
+  double sum = 0.0;
+  for (int j = 0; j < 1000; ++j) sum = sum + lpg_dist_sample(&st, dur_inf.kind, dur_inf.p1, dur_inf.p2);
+  return r0 / (sum / 1000.0);
+}
+
+int lpo_init_columns(const lpg_init_desc* d, uint32_t parts, const lpg_columns* c) {
+  const int n = d->n_nodes;
+  int64_t* start = malloc(((size_t)n + 1) * sizeof(int64_t));
+  start[0] = 0;
+  for (int i = 0; i < n; ++i) start[i + 1] = start[i] + d->node_pop[i];
+  if (start[n] != d->count) {
+    free(start);
+    return LPG_ERR_ARG;
+  }
+  double mu = 0, sigma = 0, rho = 0, srho = 0, scale = 0;
+  if (parts & LPG_INIT_HETEROGENEITY) { /* model.py:839-851 */
+    const double var = d->risk_mult_var;
+    mu = log(1.0 / sqrt(var + 1.0));
+    sigma = sqrt(log(var + 1.0));
+    rho = 2.0 * sin(LPG_PI * d->corr_risk_inf / 6.0);
+    srho = sqrt(1.0 - rho * rho);
+    const double mean = lpo_init_mean_infectivity(d->seed, d->r0, d->dur_inf);
+    scale = mean > 1e-10 ? mean : 1e-10;
+  }
+  int64_t* cum = NULL;
+  if (parts & LPG_INIT_AGES) {
+    cum = malloc((size_t)d->n_age_bins * sizeof(int64_t));
+    int64_t acc = 0;
+    for (int b = 0; b < d->n_age_bins; ++b) cum[b] = (acc += d->age_weight[b]);
+  }
+  const int64_t count = d->count;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < d->capacity; ++i) {
+    const int live = i < count;
+    if (parts & LPG_INIT_BASE) { /* model.py:139-162 */
+      int g = 0;
+      if (live) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+          int m = (lo + hi + 1) >> 1;
+          if (start[m] <= i) lo = m; else hi = m - 1;
+        }
+        g = lo;
+      }
+      c->disease_state[i] = live ? 0 : -1;
+      c->node_id[i] = live ? (int16_t)g : (int16_t)-1;
+      c->strain[i] = 0;
+      c->potentially_paralyzed[i] = -1;
+      c->paralyzed[i] = 0;
+      c->ipv_protected[i] = 0;
+      c->chronically_missed[i] = 0;
+    }
+    if (parts & LPG_INIT_TIMERS)
+      lpg_init_timers(d->seed, (uint64_t)i, d->dur_exp.kind, d->dur_exp.p1, d->dur_exp.p2, d->dur_inf.kind,
+                      d->dur_inf.p1, d->dur_inf.p2, d->t_to_paralysis.kind, d->t_to_paralysis.p1,
+                      d->t_to_paralysis.p2, &c->exposure_timer[i], &c->infection_timer[i], &c->paralysis_timer[i]);
+    if (parts & LPG_INIT_HETEROGENEITY)
+      lpg_init_het(d->seed, (uint64_t)i, d->heterogeneity != 0, mu, sigma, rho, srho, scale,
+                   &c->acq_risk_multiplier[i], &c->daily_infectivity[i]);
+    int32_t dob = -1;
+    if (parts & LPG_INIT_AGES) {
+      dob = live ? -lpg_init_age(d->seed, (uint64_t)i, d->n_age_bins, cum, d->age_lo_days, d->age_hi_days) : -1;
+      c->date_of_birth[i] = dob;
+    } else if (parts & (LPG_INIT_DEATHS | LPG_INIT_RI)) {
+      dob = c->date_of_birth[i];
+    }
+    if (parts & LPG_INIT_DEATHS) {
+      int32_t dod = 0;
+      if (live) {
+        const int64_t age = -(int64_t)dob;
+        const double u0 = lpg_u01(d->seed, LPG_P_INIT_KM, 0, (uint64_t)i, 0, 0);
+        const double u1 = lpg_u01(d->seed, LPG_P_INIT_KM, 0, (uint64_t)i, 0, 1);
+        dod = (int32_t)(lpg_km_age_at_death(d->km_cumdeaths, d->km_len, d->km_max_year, age, u0, u1) - age);
+      }
+      c->date_of_death[i] = dod;
+    }
+    if (parts & LPG_INIT_RI) c->ri_timer[i] = live ? lpg_init_ri(d->seed, (uint64_t)i, dob) : (int16_t)-1;
+  }
+  const int64_t all[2] = {0, count};
+  if (parts & LPG_INIT_MISSED) lpo_select(d->seed, LPG_P_INIT_MISSED, all, 1, &d->missed_k, 0, c);
+  if (parts & LPG_INIT_IMMUNITY) lpo_select(d->seed, LPG_P_INIT_IMMUNE, start, n, d->immune_k, 1, c);
+  if (parts & LPG_INIT_PREVALENCE) {
+    if (d->prev_per_node) lpo_select(d->seed, LPG_P_INIT_PREV, start, n, d->prev_k, 2, c);
+    else lpo_select(d->seed, LPG_P_INIT_PREV, all, 1, d->prev_k, 2, c);
+  }
+  free(cum);
+  free(start);
   return 0;
 }
 

@@ -43,6 +43,7 @@ def test_struct_layout_matches_header(tmp_path):
         "lpg_incidence_in": _abi.lpg_incidence_in,
         "lpg_incidence_grad": _abi.lpg_incidence_grad,
         "lpg_incidence_params": _abi.lpg_incidence_params,
+        "lpg_init_desc": _abi.lpg_init_desc,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "lpg.h"', "int main(void){"]
     for name, cls in structs.items():
