@@ -254,14 +254,22 @@ def ptr(arr, ctype):
 
 
 def make_columns(cols: dict) -> lpg_columns:
-    """Build an lpg_columns from a dict name -> numpy array (missing = NULL)."""
+    """Build an lpg_columns from a dict name -> column (missing = NULL): a
+    numpy array, or a CUDA tensor (a device-resident column), of the
+    reference's element type."""
     out = lpg_columns()
     for name, ptype, dtype in COLUMN_FIELDS:
         arr = cols.get(name)
-        if arr is not None:
+        if arr is None:
+            continue
+        if isinstance(arr, np.ndarray):
             if arr.dtype != dtype:
                 raise TypeError(f"column {name} must be {np.dtype(dtype).name}, got {arr.dtype}")
             setattr(out, name, ptr(arr, ptype))
+        else:
+            if str(arr.dtype).rsplit(".", 1)[-1] != np.dtype(dtype).name or not arr.is_contiguous():
+                raise TypeError(f"column {name} must be a contiguous {np.dtype(dtype).name} tensor, got {arr.dtype}")
+            setattr(out, name, C.cast(C.c_void_p(arr.data_ptr()), ptype))
     return out
 
 

@@ -103,16 +103,59 @@ class PropertySet:
 class LaserFrame:
     """Structure-of-arrays agent table (laser_core.laserframe.LaserFrame).
 
-    Columns are numpy arrays of length ``capacity``; ``count`` is the active
+    Columns are arrays of length ``capacity``; ``count`` is the active
     prefix; ``add(n)`` appends n rows and returns (start, end).  There is no
     compaction: dead agents keep their slot.
+
+    A column is either a host numpy array (an ordinary attribute, as in
+    laser_core) or device-resident: a CUDA tensor that the device
+    initialisation filled and the engine reads and writes in place.  Reading
+    a device-resident column by attribute (``people.disease_state``) copies it
+    to the host once; from then on the numpy array is the column, so callers
+    may change it in place before a run, as the reference's tests do.  The
+    engine takes each column from wherever it lives (``engine_columns``).
     """
 
     def __init__(self, capacity: int, initial_count: int = -1):
         self._capacity = int(capacity)
         self._count = self._capacity if initial_count < 0 else int(initial_count)
+        self._dev = {}
         if self._count > self._capacity:
             raise ValueError(f"initial_count {initial_count} exceeds capacity {capacity}")
+
+    def __getattr__(self, name):
+        dev = self.__dict__.get("_dev")
+        if dev is not None and name in dev:
+            host = dev.pop(name).cpu().numpy()
+            object.__setattr__(self, name, host)
+            return host
+        raise AttributeError(name)
+
+    def has_column(self, name) -> bool:
+        return name in self.__dict__.get("_dev", {}) or isinstance(self.__dict__.get(name), np.ndarray)
+
+    def device_columns(self) -> dict:
+        """The columns that live on the device, by name (CUDA tensors)."""
+        return dict(self._dev)
+
+    def set_device_column(self, name, tensor):
+        """Make ``tensor`` (CUDA, length capacity) the column ``name``; a host
+        copy of the column, if there was one, is dropped."""
+        if int(tensor.shape[0]) != self._capacity:
+            raise ValueError(f"column {name}: {tuple(tensor.shape)} elements for capacity {self._capacity}")
+        self.__dict__.pop(name, None)
+        self._dev[name] = tensor
+
+    def engine_columns(self, names) -> dict:
+        """name -> the column as it lives (CUDA tensor or numpy array) for
+        the names present, without copying anything."""
+        out = {}
+        for name in names:
+            if name in self._dev:
+                out[name] = self._dev[name]
+            elif isinstance(self.__dict__.get(name), np.ndarray):
+                out[name] = self.__dict__[name]
+        return out
 
     @property
     def capacity(self) -> int:
@@ -131,6 +174,7 @@ class LaserFrame:
         return self._count
 
     def add_scalar_property(self, name, dtype=np.uint32, default=0):
+        self._dev.pop(name, None)
         setattr(self, name, np.full(self._capacity, default, dtype=dtype))
 
     def add_vector_property(self, name, length, dtype=np.uint32, default=0):

@@ -203,13 +203,17 @@ def build_sim_spec(sim) -> SimSpec:
     p["R_preseed"] = Rres if (Rres is not None and np.any(Rres)) else None
     d, keep = make_desc(p)
 
-    columns = {}
+    # each column as it lives: a device-resident tensor, or the host array
+    people = sim.people
+    if hasattr(people, "engine_columns"):
+        columns = people.engine_columns([name for name, _, _ in _abi.COLUMN_FIELDS])
+    else:  # a LaserFrame of another package: host arrays
+        columns = {name: getattr(people, name) for name, _, _ in _abi.COLUMN_FIELDS
+                   if isinstance(getattr(people, name, None), np.ndarray)}
     for name, _, dtype in _abi.COLUMN_FIELDS:
-        a = getattr(sim.people, name, None)
-        if isinstance(a, np.ndarray):
-            if a.dtype != dtype or not a.flags["C_CONTIGUOUS"]:
-                raise TypeError(f"people.{name} must be a contiguous {np.dtype(dtype).name} array")
-            columns[name] = a
+        a = columns.get(name)
+        if isinstance(a, np.ndarray) and (a.dtype != dtype or not a.flags["C_CONTIGUOUS"]):
+            raise TypeError(f"people.{name} must be a contiguous {np.dtype(dtype).name} array")
     return SimSpec(d, keep, columns, results)
 
 
@@ -225,11 +229,17 @@ def _advance_count(people, count: int) -> None:
 
 def _check_node_ids(spec) -> None:
     """node_id of the first count slots within [0, n_nodes) (lpg_start
-    checks the same on the device for the whole handle)."""
+    checks the same on the device for the whole handle); a device-resident
+    column is checked where it lives."""
     n, count = spec.desc.n_nodes, spec.desc.count
     node = spec.columns.get("node_id")
     if node is not None and count and (int(node[:count].min()) < 0 or int(node[:count].max()) >= n):
         raise ValueError(f"LPG_ERR_NODE: node_id outside [0, {n}) among the first {count} slots")
+
+
+def host_columns(spec) -> dict:
+    """Copies of a spec's columns on the host (numpy), wherever they live."""
+    return {k: (v.copy() if isinstance(v, np.ndarray) else v.cpu().numpy().copy()) for k, v in spec.columns.items()}
 
 
 def run_replicates(sims) -> list:

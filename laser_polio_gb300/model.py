@@ -1,30 +1,37 @@
-"""SEIR_ABM driver and the five drop-in components.
+"""SEIR_ABM and the five drop-in components.
 
-Each class carries the reference's name, takes the reference's ``pars`` and
+Each class has the reference's name, takes the reference's ``pars`` and
 fills the reference's ``sim.results`` arrays; the names matter because the
-components setter orders and filters classes by ``__name__``
-(laser_polio/model.py:226-237).  Initialisation (timers, immunity, seeding,
-ages, lifespans, heterogeneity, network) runs on the host with numpy exactly
-as in the reference, because it is once per run and its random draws are
-not part of the replayed stream.  Every per-tick ``step()`` and ``log()``
-goes to the shared ``GpuTick`` engine (engine.py), which runs the whole tick
-on the GPU through the C ABI in include/lpg.h.
+components setter keeps and orders classes by ``__name__``
+(laser_polio/model.py:226-237).
+
+Construction.  SEIR_ABM and each component describe what their slice of the
+agent table holds (an init.InitSpec: population per node, how many agents
+are missed, immune, infected, the timer and heterogeneity distributions,
+the age pyramid, the lifespan table) and the device fills it
+(init.fill -> lpg_init_columns): the columns are device-resident from the
+start, and reading one by attribute brings it to the host.  Small per-run
+state (results arrays, the network, schedules, birth rates) is built on the
+host.
+
+Running.  Every per-tick ``step()`` and ``log()`` goes to the sim's GpuTick
+engine (engine.py), created on first use, which runs the whole tick on the
+GPU through the C ABI of include/lpg.h.
 """
 
 from __future__ import annotations
 
-import numbers
 import time
 from collections import defaultdict
 from copy import deepcopy
 from datetime import datetime
 
 import numpy as np
-import scipy.stats as stats
 
+from . import _abi
+from . import init as _init
 from . import pars as _pars
 from . import utils as lpu
-from .core import AliasedDistribution
 from .core import KaplanMeierEstimator
 from .core import LaserFrame
 from .core import PropertySet
@@ -35,12 +42,13 @@ from .core import radiation
 from .core import resolve_pyramid
 from .core import row_normalizer
 
-__all__ = ["RI_ABM", "SEIR_ABM", "SIA_ABM", "DiseaseState_ABM", "Transmission_ABM", "VitalDynamics_ABM"]
+__all__ = ["RI_ABM", "SEIR_ABM", "SIA_ABM", "DiseaseState_ABM", "Transmission_ABM", "VitalDynamics_ABM",
+           "populate_heterogeneous_values"]
 
 
 class TimingStats:
-    """Accumulated wall time per label, in ns (the keys the reference's
-    TimingStats uses, laser_polio/utils.py:819-945)."""
+    """Wall time per label, in ns, under the labels the reference uses
+    (laser_polio/utils.py:819-945)."""
 
     def __init__(self):
         self.stats = defaultdict(int)
@@ -61,74 +69,95 @@ class TimingStats:
         return TimingStats._Watch(self, label)
 
 
+def capacity_for(total, pars) -> int:
+    """Agent slots for a run: everyone present at the start and everyone born
+    within the run's duration plus 100 days at the (mean) crude birth rate,
+    times a margin 1 + 4/sqrt(births) that narrows as births grow; without
+    births, just the starting population (model.py:118-137)."""
+    if pars.cbr is None:
+        return int(total)
+    rate = float(np.mean(np.atleast_1d(pars.cbr)))
+    births = calc_capacity(total, pars.dur + 100, rate) - total
+    if births <= 0:
+        return int(total)
+    return int((1.0 + 4.0 / np.sqrt(births)) * (total + births))
+
+
+def _spec_of(sim) -> _init.InitSpec:
+    """The sim's initialisation description, created from its pars and
+    people when the sim was not built by this package's SEIR_ABM."""
+    spec = getattr(sim, "_init", None)
+    if spec is None:
+        pops = np.atleast_1d(sim.pars.init_pop).astype(np.int64)
+        spec = _init.InitSpec(sim.pars.seed if sim.pars.seed is not None else 0, pops, sim.people.count,
+                              sim.people.capacity)
+        sim._init = spec
+    return spec
+
+
 class SEIR_ABM:
     """Agent-based SEIR polio model (laser_polio/model.py:51-342).
 
-    Disease state codes: -1 dead/inactive, 0 S, 1 E, 2 I, 3 R.
+    Disease state codes: -1 dead or not yet born, 0 S, 1 E, 2 I, 3 R.
     """
 
     def common_init(self, pars, verbose):
+        """Parameters (defaults overridden by ``pars``; unknown keys dropped
+        with a warning), the seed, and the time axis."""
         self.perf_stats = TimingStats()
-        self.pars = deepcopy(_pars.default_pars)
+        merged = deepcopy(_pars.default_pars)
         if pars is not None:
-            unexpected = set(pars.to_dict().keys()) - set(self.pars.to_dict().keys())
-            if unexpected:
-                print(f"Warning: ignoring unexpected parameters: {list(unexpected)}")
-                filtered = {k: v for k, v in pars.items() if k in self.pars}
-                self.pars <<= filtered
-            else:
-                self.pars <<= pars
-        pars = self.pars
-        self.verbose = pars["verbose"] if "verbose" in pars else 1
-        if pars.seed is None:
-            now = datetime.now()  # noqa: DTZ005
-            pars.seed = now.microsecond ^ int(now.timestamp())
+            given = pars.to_dict() if isinstance(pars, PropertySet) else dict(pars)
+            unknown = sorted(set(given) - set(merged.keys()))
+            if unknown:
+                print(f"Warning: ignoring unexpected parameters: {unknown}")
+                given = {k: v for k, v in given.items() if k in merged}
+            merged <<= given
+        self.pars = merged
+        self.verbose = merged["verbose"] if "verbose" in merged else verbose
+        if merged.seed is None:
+            stamp = datetime.now()  # noqa: DTZ005  (a seed from the clock, as the reference does)
+            merged.seed = stamp.microsecond ^ int(stamp.timestamp())
             if self.verbose >= 1:
-                print(f"No seed provided. Using random seed of {pars.seed}.")
-        np.random.seed(int(pars.seed) & 0xFFFFFFFF)
+                print(f"No seed provided. Using random seed of {merged.seed}.")
         self.t = 0
-        self.nt = pars.dur + 1
-        self.datevec = lpu.daterange(self.pars["start_date"], days=self.nt)
+        self.nt = merged.dur + 1
+        self.datevec = lpu.daterange(merged["start_date"], days=self.nt)
         self.should_stop = False
 
     def __init__(self, pars: PropertySet = None, verbose=1):
         self.common_init(pars, verbose)
-        pars = self.pars
-        pars.init_pop = np.atleast_1d(pars.init_pop).astype(int)
-        if pars.init_sus_by_age is not None:
+        p = self.pars
+        p.init_pop = np.atleast_1d(p.init_pop).astype(int)
+        if p.init_sus_by_age is not None:
             raise NotImplementedError("init_sus_by_age (real-data initialisation through run_sim) is not supported")
-        total_pop = int(np.sum(pars.init_pop))
-        # capacity estimate with the reference's fudge factor (model.py:124-137)
-        expected_births = 0
-        if (pars.cbr is not None) and (len(np.atleast_1d(pars.cbr)) == 1):
-            expected_births = calc_capacity(pars.init_pop.sum(), pars.dur + 100, np.atleast_1d(pars.cbr)[0]) - pars.init_pop.sum()
-        elif (pars.cbr is not None) and (len(pars.cbr) > 1):
-            expected_births = calc_capacity(pars.init_pop.sum(), pars.dur + 100, np.mean(pars.cbr)) - pars.init_pop.sum()
-        fudge = 1 + 4 / np.sqrt(expected_births) if expected_births > 0 else 1
-        capacity = int(fudge * (total_pop + expected_births))
-        self.people = LaserFrame(capacity=capacity, initial_count=total_pop)
-
-        p = self.people
-        p.add_scalar_property("disease_state", dtype=np.int8, default=-1)
-        p.disease_state[: p.count] = 0
-        p.add_scalar_property("potentially_paralyzed", dtype=np.int8, default=-1)
-        p.add_scalar_property("paralyzed", dtype=np.int8, default=0)
-        p.add_scalar_property("ipv_protected", dtype=np.int8, default=0)
-        self.results = LaserFrame(capacity=1)
-        p.add_scalar_property("strain", dtype=np.int8, default=0)
-        p.add_scalar_property("chronically_missed", dtype=np.uint8, default=0)
-        n_missed = int(pars.missed_frac * p.count)
-        missed_ids = np.random.choice(p.count, size=n_missed, replace=False)
-        p.chronically_missed[missed_ids] = 1
-
-        p.add_scalar_property("node_id", dtype=np.int16, default=-1)
-        self.nodes = np.arange(len(pars.init_pop))
-        pop_by_node = pars.init_pop
-        if np.any(pop_by_node <= 0) or np.any(np.isnan(pop_by_node)):
+        pops = p.init_pop
+        if np.any(pops <= 0) or np.any(np.isnan(pops)):
             raise ValueError("pop_by_node must be positive & non-nan")
-        p.node_id[:total_pop] = np.repeat(np.arange(len(pop_by_node)), pop_by_node).astype(np.int16)
+        total = int(pops.sum())
+        self.people = LaserFrame(capacity=capacity_for(total, p), initial_count=total)
+        self.results = LaserFrame(capacity=1)
+        self.nodes = np.arange(len(pops))
+        self._init = _init.InitSpec(p.seed, pops, total, self.people.capacity)
+        self._init.missed_k = _init.missed_count(p.missed_frac, total)
+        _init.fill(self.people, self._init, _abi.INIT_BASE | _abi.INIT_MISSED)
         self._components = []
         self.instances = []
+        self._engine = None
+
+    @classmethod
+    def init_from_file(cls, people: LaserFrame, pars: PropertySet = None):
+        """A model around an agent table loaded from a snapshot
+        (model.py:177-195): the people as they are, the nodes they live in,
+        empty results and no components yet."""
+        model = cls.__new__(cls)
+        model.common_init(pars, verbose=2)
+        model.people = people
+        model.nodes = np.unique(people.node_id[: people.count])
+        model.results = LaserFrame(capacity=1)
+        model._engine = None
+        model.components = []
+        return model
 
     @property
     def components(self) -> list:
@@ -136,20 +165,19 @@ class SEIR_ABM:
 
     @components.setter
     def components(self, components: list) -> None:
-        lookup = {cls.__name__: cls for cls in components}
-        ordered = [lookup[name] for name in _pars.default_run_order if name in lookup]
-        self._components = ordered
+        by_name = {cls.__name__: cls for cls in components}
+        self._components = [by_name[name] for name in _pars.default_run_order if name in by_name]
         self.instances = []
-        for cls in ordered:
+        for cls in self._components:
             with self.perf_stats.start(cls.__name__ + ".__init__()"):
                 self.instances.append(cls(self))
         self._engine = None
 
     def run(self):
-        """SEIR_ABM.run (model.py:246-282).  With GPU components the whole
-        loop runs on the device in one call; the result is the same as the
-        per-tick loop below, which is kept for component sets that mix in
-        host classes."""
+        """SEIR_ABM.run (model.py:246-282).  With drop-in components only,
+        the whole loop runs on the device in one call, with the same result
+        as the per-tick loop below (kept for component sets that mix in host
+        classes)."""
         if self.instances and all(isinstance(c, _GpuComponent) for c in self.instances):
             with self.perf_stats.start("GpuTick.run()"):
                 _engine_of(self).run_all()
@@ -157,16 +185,13 @@ class SEIR_ABM:
                 print(f"[SEIR_ABM] Early stopping at t={self.t}: no E/I and no future seed_schedule events.")
             return
         for tick in range(self.nt):
-            if tick == 0:
-                self.log_results(tick)
-                self.t += 1
-                continue
-            for component in self.instances:
-                with self.perf_stats.start(component.__class__.__name__ + ".step()"):
-                    component.step()
+            if tick > 0:
+                for component in self.instances:
+                    with self.perf_stats.start(component.__class__.__name__ + ".step()"):
+                        component.step()
             self.log_results(tick)
             self.t += 1
-            if self.should_stop:
+            if tick > 0 and self.should_stop:
                 if self.verbose >= 1:
                     print(f"[SEIR_ABM] Early stopping at t={self.t}: no E/I and no future seed_schedule events.")
                 break
@@ -204,11 +229,18 @@ class _GpuComponent:
         pass
 
 
+def _results(sim, names, wide=False):
+    nt, nn, ns = sim.nt, len(sim.nodes), len(sim.pars.strain_ids)
+    for name in names:
+        sim.results.add_array_property(name, shape=(nt, nn, ns) if wide else (nt, nn), dtype=np.int32)
+
+
 # ---------------------------------------------------------------------------
 class DiseaseState_ABM(_GpuComponent):
-    """Timers, immunity and seeding at init (model.py:561-713); per tick the
-    E->I->R progression, paralysis, seed schedule and stop rule
-    (model.py:715-795) run in the engine's sweep."""
+    """E -> I -> R progression, paralysis, the seed schedule and the stop
+    rule (model.py:505-812).  At construction: the results arrays, the
+    timers of every slot, the immune and the initially infected agents
+    (filled on the device)."""
 
     def _common_init(self, sim):
         self.sim = sim
@@ -217,119 +249,92 @@ class DiseaseState_ABM(_GpuComponent):
         self.nodes = sim.nodes
         self.results = sim.results
         self.verbose = self.pars["verbose"] if "verbose" in self.pars else 1
+        # tick -> [(node, prevalence)]; entries by date name their node by dot_name
         self.seed_schedule = defaultdict(list)
-        if self.pars.seed_schedule is not None:
-            for entry in self.pars.seed_schedule:
-                if "date" in entry and "dot_name" in entry:
-                    d = lpu.date(entry["date"])
-                    t = (d - lpu.date(self.pars.start_date)).days
-                    lookup = self.pars.node_lookup or {}
-                    node_id = next((nid for nid, info in lookup.items() if info["dot_name"] == entry["dot_name"]), None)
-                    if node_id is not None:
-                        self.seed_schedule[t].append((node_id, entry["prevalence"]))
-                elif "timestep" in entry and "node_id" in entry:
-                    self.seed_schedule[entry["timestep"]].append((entry["node_id"], entry["prevalence"]))
+        lookup = self.pars.node_lookup or {}
+        start = lpu.date(self.pars.start_date)
+        for entry in self.pars.seed_schedule or []:
+            if "date" in entry and "dot_name" in entry:
+                node = next((nid for nid, info in lookup.items() if info["dot_name"] == entry["dot_name"]), None)
+                if node is not None:
+                    self.seed_schedule[(lpu.date(entry["date"]) - start).days].append((node, entry["prevalence"]))
+            elif "timestep" in entry and "node_id" in entry:
+                self.seed_schedule[entry["timestep"]].append((entry["node_id"], entry["prevalence"]))
 
     def _initialize_results_arrays(self):
-        nt, nn, ns = self.sim.nt, len(self.nodes), len(self.sim.pars.strain_ids)
-        r = self.results
-        for name in ("S", "E", "I", "R"):
-            r.add_array_property(name, shape=(nt, nn), dtype=np.int32)
-        r.add_array_property("E_by_strain", shape=(nt, nn, ns), dtype=np.int32)
-        r.add_array_property("I_by_strain", shape=(nt, nn, ns), dtype=np.int32)
-        for name in ("potentially_paralyzed", "paralyzed", "new_potentially_paralyzed", "new_paralyzed", "pop"):
-            r.add_array_property(name, shape=(nt, nn), dtype=np.int32)
-        r.pop[0] = self.sim.pars.init_pop
+        _results(self.sim, ("S", "E", "I", "R", "potentially_paralyzed", "paralyzed", "new_potentially_paralyzed",
+                            "new_paralyzed", "pop"))
+        _results(self.sim, ("E_by_strain", "I_by_strain"), wide=True)
+        self.results.pop[0] = self.sim.pars.init_pop
 
     def __init__(self, sim):
         self._common_init(sim)
         self._initialize_results_arrays()
         pars = self.pars
+        spec = _spec_of(sim)
+        spec.dur_exp, spec.dur_inf, spec.t_to_paralysis = (pars.dur_exp.spec(), pars.dur_inf.spec(),
+                                                           pars.t_to_paralysis.spec())
+        spec.immune_k = _init.immune_counts(pars.init_immun, pars.init_pop)
+        spec.prev_per_node, spec.prev_k = _init.prevalence_counts(pars.init_prev, pars.init_pop)
+        _init.fill(sim.people, spec, _abi.INIT_TIMERS | _abi.INIT_IMMUNITY | _abi.INIT_PREVALENCE)
+
+    @classmethod
+    def init_from_file(cls, sim):
+        """For a loaded agent table (model.py:506-524): results arrays, and
+        for the unborn slots fresh timers and heterogeneity, with their
+        paralysis and IPV flags at -1 as the reference leaves them."""
+        self = cls.__new__(cls)
+        self._common_init(sim)
+        self._initialize_results_arrays()
         p = sim.people
-        p.add_scalar_property("exposure_timer", dtype=np.int8, default=0)
-        p.add_scalar_property("infection_timer", dtype=np.int8, default=0)
-        p.add_scalar_property("paralysis_timer", dtype=np.int8, default=0)
-        p.exposure_timer[:] = np.clip(pars.dur_exp(p.capacity), 0, 127)
-        p.infection_timer[:] = np.clip(pars.dur_inf(p.capacity), 0, 127)
-        raw = pars.t_to_paralysis(p.capacity) - p.exposure_timer
-        upper = np.minimum(p.infection_timer, 127)
-        p.paralysis_timer[:] = np.clip(raw, 0, upper).astype(np.int8)
+        count, cap = p.count, getattr(p, "true_capacity", p.capacity)
+        populate_heterogeneous_values(count, cap, p.acq_risk_multiplier, p.daily_infectivity, self.pars)
+        et, it, pt = _unborn_timers(sim, count, cap)
+        p.exposure_timer[count:cap], p.infection_timer[count:cap], p.paralysis_timer[count:cap] = et, it, pt
+        p.potentially_paralyzed[count:cap] = -1
+        p.paralyzed[count:cap] = -1
+        p.ipv_protected[count:cap] = -1
+        return self
 
-        # immunity (model.py:590-618)
-        if isinstance(pars.init_immun, float):
-            immun = np.full_like(pars.init_pop, fill_value=pars.init_immun, dtype=np.float32)
-        elif isinstance(pars.init_immun, list):
-            immun = np.asarray(pars.init_immun, dtype=np.float32)
-        elif isinstance(pars.init_immun, np.ndarray):
-            immun = pars.init_immun
-        else:
-            raise ValueError(f"Unsupported init_immun type: {type(pars.init_immun)}")
-        for nid, (frac, node_pop) in enumerate(zip(immun, pars.init_pop, strict=False)):
-            assert 0.0 <= frac <= 1.0, f"Invalid immunity fraction: {frac} for node {nid}"
-            n_rec = int(frac * node_pop)
-            if n_rec > 0:
-                idx = np.where(p.node_id == nid)[0]
-                p.disease_state[np.random.choice(idx, size=n_rec, replace=False)] = 3
 
-        # initial infections (model.py:670-713)
-        infected = []
-        total = int(np.sum(pars.init_pop))
-        if isinstance(pars.init_prev, float):
-            infected = np.random.choice(total, size=int(total * pars.init_prev), replace=False)
-        elif isinstance(pars.init_prev, (int, np.integer)) and not isinstance(pars.init_prev, bool):
-            infected = np.random.choice(total, size=min(int(pars.init_prev), total), replace=False)
-        elif isinstance(pars.init_prev, (list, np.ndarray)):
-            if len(pars.init_prev) != len(pars.init_pop):
-                raise ValueError(
-                    f"Length mismatch: init_prev has {len(pars.init_prev)} entries, expected {len(pars.init_pop)} nodes."
-                )
-            node_ids = p.node_id[: p.count]
-            states = p.disease_state[: p.count]
-            infected = []
-            for node, prev in enumerate(pars.init_prev):
-                if not isinstance(prev, numbers.Real):
-                    raise ValueError(f"Unsupported value in init_prev list at node {node}: {prev}")
-                n_inf = int(pars.init_pop[node] * prev) if 0 < prev < 1 else min(int(prev), pars.init_pop[node])
-                alive = np.where((node_ids == node) & (states >= 0))[0]
-                k = min(n_inf, len(alive))
-                infected.extend(np.random.choice(alive, size=k, replace=False))
-        else:
-            raise ValueError(f"Unsupported init_prev type: {type(pars.init_prev)}")
-        p.disease_state[np.asarray(infected, dtype=np.int64)] = 2
+def _slice_of_fresh_init(pars, capacity, parts, start, end, **fields):
+    """Columns of a fresh initialisation over [start, end): the draws are
+    keyed by slot, so these are the values those slots get in a table of
+    ``end`` slots."""
+    people = LaserFrame(capacity=end, initial_count=0)
+    spec = _init.InitSpec(pars.seed if pars.seed is not None else 0, np.zeros(1, np.int64), 0, end)
+    for k, v in fields.items():
+        setattr(spec, k, v)
+    _init.fill(people, spec, parts)
+    return {name: np.asarray(getattr(people, name))[start:end] for name in _init.part_columns(parts)}
+
+
+def _unborn_timers(sim, start, end):
+    pars = sim.pars
+    cols = _slice_of_fresh_init(pars, end, _abi.INIT_TIMERS, start, end, dur_exp=pars.dur_exp.spec(),
+                                dur_inf=pars.dur_inf.spec(), t_to_paralysis=pars.t_to_paralysis.spec())
+    return cols["exposure_timer"], cols["infection_timer"], cols["paralysis_timer"]
+
+
+def populate_heterogeneous_values(start, end, acq_risk_out, infectivity_out, pars):
+    """Acquisition risk and daily infectivity of slots [start, end)
+    (model.py:816-866), correlated lognormal risk and exponential
+    infectivity, drawn on the device as the initialisation draws them."""
+    cols = _slice_of_fresh_init(pars, end, _abi.INIT_HETEROGENEITY, start, end,
+                                heterogeneity=pars.individual_heterogeneity, risk_mult_var=pars.risk_mult_var,
+                                corr_risk_inf=pars.corr_risk_inf, r0=pars.r0, dur_inf=pars.dur_inf.spec())
+    acq_risk_out[start:end] = cols["acq_risk_multiplier"]
+    infectivity_out[start:end] = cols["daily_infectivity"]
 
 
 # ---------------------------------------------------------------------------
-def populate_heterogeneous_values(start, end, acq_risk_out, infectivity_out, pars):
-    """Correlated lognormal acquisition risk and gamma infectivity through a
-    Gaussian copula (model.py:816-866)."""
-    mean_ln = 1
-    var_ln = pars.risk_mult_var
-    mu_ln = np.log(mean_ln**2 / np.sqrt(var_ln + mean_ln**2))
-    sigma_ln = np.sqrt(np.log(var_ln / mean_ln**2 + 1))
-    mean_gamma = pars.r0 / np.mean(pars.dur_inf(1000))
-    shape_gamma = 1
-    scale_gamma = max(mean_gamma / shape_gamma, 1e-10)
-    rho = 2.0 * np.sin(np.pi * pars.corr_risk_inf / 6)
-    L = np.linalg.cholesky(np.array([[1, rho], [rho, 1]]))
-    batch = 1_000_000
-    for b0 in range(start, end, batch):
-        b1 = min(b0 + batch, end)
-        z = np.random.normal(size=(b1 - b0, 2)) @ L.T
-        if pars.individual_heterogeneity:
-            acq_risk_out[b0:b1] = np.exp(mu_ln + sigma_ln * z[:, 0])
-            infectivity_out[b0:b1] = stats.gamma.ppf(stats.norm.cdf(z[:, 1]), a=shape_gamma, scale=scale_gamma)
-        else:
-            acq_risk_out[b0:b1] = 1.0
-            infectivity_out[b0:b1] = mean_gamma
-
-
 class Transmission_ABM(_GpuComponent):
-    """Heterogeneity and the mixing network at init (model.py:1153-1279);
-    per tick the infectivity reduce, mixing, draws and weighted selection
-    (model.py:1281-1459) and the SEIR counts of log() (model.py:1461-1487)
-    run in the engine."""
+    """Mixing, draws and weighted selection of the exposed, and the SEIR
+    counts (model.py:1152-1491).  At construction: the migration network,
+    the results arrays and every slot's acquisition risk and daily
+    infectivity (filled on the device)."""
 
-    def __init__(self, sim):
+    def _bind(self, sim):
         self.sim = sim
         self.people = sim.people
         self.nodes = np.arange(len(sim.pars.init_pop))
@@ -337,53 +342,71 @@ class Transmission_ABM(_GpuComponent):
         self.results = sim.results
         self.verbose = sim.pars["verbose"] if "verbose" in sim.pars else 1
         self.r0_scalars = np.array(self.pars.r0_scalars)
-        self._initialize_people_fields()
+
+    def __init__(self, sim):
+        self._bind(sim)
+        spec = _spec_of(sim)
+        p = self.pars
+        spec.heterogeneity = p.individual_heterogeneity
+        spec.risk_mult_var, spec.corr_risk_inf, spec.r0 = p.risk_mult_var, p.corr_risk_inf, p.r0
+        spec.dur_inf = p.dur_inf.spec()
+        _init.fill(sim.people, spec, _abi.INIT_HETEROGENEITY)
         self._initialize_common()
 
-    def _initialize_people_fields(self):
-        count = self.people.capacity
-        self.people.add_scalar_property("acq_risk_multiplier", dtype=np.float32, default=1.0)
-        self.people.add_scalar_property("daily_infectivity", dtype=np.float32, default=1.0)
-        populate_heterogeneous_values(0, count, self.people.acq_risk_multiplier, self.people.daily_infectivity, self.pars)
+    @classmethod
+    def init_from_file(cls, sim):
+        """For a loaded agent table (model.py:1169-1188): infectivity scaled
+        by r0 / old_r0 when the run's R0 differs from the stored one."""
+        self = cls.__new__(cls)
+        self._bind(sim)
+        old = sim.pars["old_r0"] if "old_r0" in sim.pars else sim.pars.r0
+        if sim.pars.r0 != old:
+            sim.people.daily_infectivity *= sim.pars.r0 / old
+        self._initialize_common()
+        return self
+
+    def _distances(self):
+        if self.sim.pars.distances is not None:
+            return np.asarray(self.sim.pars.distances, dtype=np.float64)
+        lookup = self.sim.pars.node_lookup
+        ids = sorted(lookup.keys())
+        lat = np.array([lookup[i]["lat"] for i in ids])
+        lon = np.array([lookup[i]["lon"] for i in ids])
+        n = len(self.sim.nodes)
+        d = np.zeros((n, n))
+        for i in range(n):
+            for j in range(i + 1, n):
+                d[i, j] = d[j, i] = distance(lat[i], lon[i], lat[j], lon[j]) or 1.0  # a zero distance counts as 1
+        return d
 
     def _initialize_common(self):
+        """The network (model.py:1213-1258): gravity scaled by the total
+        population to the power c, or radiation; then rows capped at
+        max_migr_frac."""
         self.sim.results.add_vector_property("network", length=len(self.sim.nodes), dtype=np.float32)
-        init_pops = self.sim.pars.init_pop
-        if self.sim.pars.distances is not None:
-            dist = np.asarray(self.sim.pars.distances, dtype=np.float64)
-        else:
-            lookup = self.sim.pars.node_lookup
-            ids = sorted(lookup.keys())
-            lats = np.array([lookup[i]["lat"] for i in ids])
-            lons = np.array([lookup[i]["lon"] for i in ids])
-            n = len(self.sim.nodes)
-            dist = np.zeros((n, n))
-            for i in range(n):
-                for j in range(i + 1, n):
-                    d = distance(lats[i], lons[i], lats[j], lons[j]) or 1
-                    dist[i, j] = dist[j, i] = d
+        pops = self.sim.pars.init_pop
+        dist = self._distances()
         method = self.pars.migration_method.lower()
         if method == "gravity":
-            k = self.pars.gravity_k * 10 ** (self.pars.gravity_k_exponent)
-            a, b, c = self.pars.gravity_a, self.pars.gravity_b, self.pars.gravity_c
-            net = gravity(init_pops, dist, k, a, b, c)
-            net /= np.power(init_pops.sum(), c)
+            p = self.pars
+            k = p.gravity_k * 10 ** p.gravity_k_exponent
+            net = gravity(pops, dist, k, p.gravity_a, p.gravity_b, p.gravity_c) / np.power(pops.sum(), p.gravity_c)
         elif method == "radiation":
-            net = radiation(init_pops, dist, 10**self.pars.radiation_k_log10, include_home=False)
+            net = radiation(pops, dist, 10 ** self.pars.radiation_k_log10, include_home=False)
         else:
             raise ValueError(f"Unknown migration method: {self.pars.migration_method}")
         self.network = row_normalizer(net, self.pars.max_migr_frac)
-        nt, nn, ns = self.sim.nt, len(self.nodes), len(self.pars.strain_ids)
-        self.sim.results.add_array_property("new_exposed", shape=(nt, nn), dtype=np.int32)
-        self.sim.results.add_array_property("new_exposed_by_strain", shape=(nt, nn, ns), dtype=np.int32)
+        _results(self.sim, ("new_exposed",))
+        _results(self.sim, ("new_exposed_by_strain",), wide=True)
 
 
 # ---------------------------------------------------------------------------
 class VitalDynamics_ABM(_GpuComponent):
-    """Ages, lifespans and birth rates at init (model.py:1522-1687); per tick
-    deaths and births (model.py:1689-1757) run in the engine."""
+    """Births and deaths (model.py:1521-1765).  At construction: the results
+    arrays, birth rates, the lifespan table, and every initial agent's date
+    of birth and of death (filled on the device)."""
 
-    def __init__(self, sim):
+    def _bind(self, sim):
         self.sim = sim
         self.people = sim.people
         self.nodes = sim.nodes
@@ -391,57 +414,50 @@ class VitalDynamics_ABM(_GpuComponent):
         self.pars = sim.pars
         self.step_size = self.pars.step_size_VitalDynamics_ABM
         self.verbose = sim.pars["verbose"] if "verbose" in sim.pars else 1
-        self._initialize_ages_and_births()
-        self._initialize_deaths()
+
+    def __init__(self, sim):
+        self._bind(sim)
+        spec = _spec_of(sim)
+        spec.age_lo, spec.age_hi, spec.age_weight = _init.age_bins(resolve_pyramid(self.pars.age_pyramid_path))
+        parts = _abi.INIT_AGES
+        self.death_estimator = None
+        if self.pars.cbr is not None:
+            _results(sim, ("births", "deaths"))
+            cum = lpu.create_cumulative_deaths(np.sum(self.pars.init_pop), max_age_years=100)
+            self.death_estimator = KaplanMeierEstimator(cum)
+            spec.km, spec.km_max_year = np.asarray(cum, np.int64), 100
+            parts |= _abi.INIT_DEATHS
+        _init.fill(sim.people, spec, parts)
         self._initialize_birth_rates()
 
-    def _initialize_ages_and_births(self):
-        pars = self.pars
-        p = self.people
-        p.add_scalar_property("date_of_birth", dtype=np.int32, default=-1)
-        pyramid = resolve_pyramid(pars.age_pyramid_path)
-        sampler = AliasedDistribution(pyramid[:, 2] + pyramid[:, 3])
-        samples = sampler.sample(p.count)
-        lo = np.maximum(pyramid[:, 0] * 365, 1)
-        hi = (pyramid[:, 1] + 1) * 365
-        ages = np.zeros(p.count, dtype=np.int32)
-        for i in range(len(pyramid)):
-            mask = samples == i
-            ages[mask] = np.random.randint(lo[i], hi[i], mask.sum())
-        ages[ages == 0] = 1
-        p.date_of_birth[: p.count] = -ages
-
-    def _initialize_deaths(self):
-        pars = self.pars
-        if pars.cbr is None:
-            return
-        nt, nn = self.sim.nt, len(self.nodes)
-        self.results.add_array_property("births", shape=(nt, nn), dtype=np.int32)
-        self.results.add_array_property("deaths", shape=(nt, nn), dtype=np.int32)
-        self.people.add_scalar_property("date_of_death", dtype=np.int32, default=0)
-        cum = lpu.create_cumulative_deaths(np.sum(pars.init_pop), max_age_years=100)
-        self.death_estimator = KaplanMeierEstimator(cum)
-        ages = -self.people.date_of_birth[: self.people.count]
-        lifespans = self.death_estimator.predict_age_at_death(ages, max_year=100)
-        self.people.date_of_death[: self.people.count] = lifespans - ages
+    @classmethod
+    def init_from_file(cls, sim):
+        """For a loaded agent table (model.py:1528-1537): results arrays if
+        missing, birth rates and the lifespan table."""
+        self = cls.__new__(cls)
+        self._bind(sim)
+        for name in ("births", "deaths"):
+            if not isinstance(getattr(sim.results, name, None), np.ndarray):
+                _results(sim, (name,))
+        self._initialize_birth_rates()
+        self.death_estimator = KaplanMeierEstimator(lpu.create_cumulative_deaths(np.sum(self.pars.init_pop), 100))
+        return self
 
     def _initialize_birth_rates(self):
-        pars = self.pars
+        """Per-node daily births per person: cbr / (365 * 1000)."""
         self.birth_rate = np.zeros(len(self.nodes))
-        if pars.cbr is not None:
-            cbr = np.atleast_1d(pars.cbr)
-            if len(cbr) == 1:
-                self.birth_rate[:] = cbr[0] / (365 * 1000)
-            else:
-                self.birth_rate[:] = np.array(cbr) / (365 * 1000)
+        if self.pars.cbr is not None:
+            cbr = np.atleast_1d(np.asarray(self.pars.cbr, dtype=np.float64))
+            self.birth_rate[:] = (cbr[0] if len(cbr) == 1 else cbr) / (365 * 1000)
 
 
 # ---------------------------------------------------------------------------
 class RI_ABM(_GpuComponent):
-    """RI timers at init (model.py:1887-1894); per tick the OPV/IPV dosing of
-    fast_ri (model.py:1784-1855, 1920-1985) runs in the engine."""
+    """Routine immunisation (model.py:1858-1992).  At construction: the
+    results arrays and every initial agent's RI date (filled on the
+    device)."""
 
-    def __init__(self, sim):
+    def _bind(self, sim):
         self.sim = sim
         self.step_size = sim.pars.step_size_RI_ABM
         self.people = sim.people
@@ -449,22 +465,28 @@ class RI_ABM(_GpuComponent):
         self.pars = sim.pars
         self.results = sim.results
         self.verbose = self.pars["verbose"] if "verbose" in self.pars else 1
-        self.people.add_scalar_property("ri_timer", dtype=np.int16, default=-1)
-        dob = self.people.date_of_birth[: self.people.count]
-        days = np.random.uniform(42, 98, self.people.count)
-        self.people.ri_timer[: self.people.count] = (dob + days).astype(np.int32)
-        nt, nn, ns = self.sim.nt, len(self.sim.nodes), len(self.pars.strain_ids)
-        r = self.sim.results
-        r.add_array_property("ri_vaccinated", shape=(nt, nn), dtype=np.int32)
-        r.add_array_property("ri_protected", shape=(nt, nn), dtype=np.int32)
-        r.add_array_property("ri_new_exposed_by_strain", shape=(nt, nn, ns), dtype=np.int32)
-        r.add_array_property("ipv_vaccinated", shape=(nt, nn), dtype=np.int32)
+        _results(sim, ("ri_vaccinated", "ri_protected", "ipv_vaccinated"))
+        _results(sim, ("ri_new_exposed_by_strain",), wide=True)
+
+    def __init__(self, sim):
+        self._bind(sim)
+        if not sim.people.has_column("date_of_birth"):
+            raise AttributeError("RI_ABM needs people.date_of_birth (VitalDynamics_ABM sets it)")
+        _init.fill(sim.people, _spec_of(sim), _abi.INIT_RI)
+
+    @classmethod
+    def init_from_file(cls, sim):
+        """For a loaded agent table (model.py:1872-1885): the RI dates are
+        kept; only the results arrays."""
+        self = cls.__new__(cls)
+        self._bind(sim)
+        return self
 
 
 # ---------------------------------------------------------------------------
 class SIA_ABM(_GpuComponent):
-    """Campaign schedule at init (model.py:2064-2097); per tick the dosing of
-    fast_sia (model.py:1994-2060, 2099-2156) runs in the engine."""
+    """Campaigns (model.py:2063-2163).  At construction: the results arrays
+    and the schedule with its dates parsed."""
 
     def __init__(self, sim):
         self.sim = sim
@@ -473,11 +495,13 @@ class SIA_ABM(_GpuComponent):
         self.pars = sim.pars
         self.results = sim.results
         self.verbose = sim.pars["verbose"] if "verbose" in sim.pars else 1
-        nt, nn, ns = self.sim.nt, len(self.nodes), len(self.pars.strain_ids)
-        self.results.add_array_property("sia_vaccinated", shape=(nt, nn), dtype=np.int32)
-        self.results.add_array_property("sia_protected", shape=(nt, nn), dtype=np.int32)
-        self.results.add_array_property("sia_new_exposed_by_strain", shape=(nt, nn, ns), dtype=np.int32)
-        sched = self.pars["sia_schedule"] if "sia_schedule" in self.pars else None
-        self.sia_schedule = [] if sched is None else sched
+        _results(sim, ("sia_vaccinated", "sia_protected"))
+        _results(sim, ("sia_new_exposed_by_strain",), wide=True)
+        schedule = self.pars["sia_schedule"] if "sia_schedule" in self.pars else None
+        self.sia_schedule = [] if schedule is None else schedule
         for event in self.sia_schedule:
             event["date"] = lpu.date(event["date"])
+
+    @classmethod
+    def init_from_file(cls, sim):
+        return cls(sim)

@@ -60,6 +60,9 @@ def lib():
         L.lpo_tx_negbinom.argtypes = [C.c_uint64, C.c_int32, C.c_uint64, C.c_double, C.c_double]
         L.lpo_tx_poisson.restype = C.c_int64
         L.lpo_tx_poisson.argtypes = [C.c_uint64, C.c_int32, C.c_uint64, C.c_double]
+        L.lpo_init_columns.argtypes = [C.POINTER(_abi.lpg_init_desc), C.c_uint32, C.POINTER(_abi.lpg_columns)]
+        L.lpo_init_mean_infectivity.restype = C.c_double
+        L.lpo_init_mean_infectivity.argtypes = [C.c_uint64, C.c_double, _abi.lpg_dist]
         L.lpo_seed_timer.restype = C.c_double
         L.lpo_seed_timer.argtypes = [C.c_uint64, C.c_int32, C.c_uint64, C.c_uint64, C.c_int, C.c_double, C.c_double]
         _lib = L
@@ -236,3 +239,11 @@ def fix_risk_many(r):
     c = np.empty(len(r), np.uint64)
     lib().lpo_fix_risk_many(r.ctypes.data, len(r), a.ctypes.data, b.ctypes.data, c.ctypes.data)
     return a, b, c
+
+
+def init_columns(desc, parts, cols):
+    """The oracle's restatement of lpg_init_columns over host numpy columns
+    (name -> array of length capacity)."""
+    rc = lib().lpo_init_columns(C.byref(desc), int(parts), C.byref(_abi.make_columns(cols)))
+    if rc != 0:
+        raise ValueError(f"oracle: lpo_init_columns failed ({rc})")

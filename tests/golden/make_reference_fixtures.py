@@ -2,6 +2,7 @@
 
     python tests/golden/make_reference_fixtures.py <reference checkout> [--cases busy,stop]
     python tests/golden/make_reference_fixtures.py <reference checkout> --native 200
+    python tests/golden/make_reference_fixtures.py <reference checkout> --init 16
 
 Imports the unmodified laser_polio package from <checkout>/src with the
 stand-ins and the draw hook of reference_harness.py, and writes:
@@ -16,6 +17,11 @@ stand-ins and the draw hook of reference_harness.py, and writes:
   reference_native.npz  (--native N) the native case's description and
       initial table, and the new exposures per tick and node of N reference
       runs with numpy's own generator (seeds 1 .. N), without the hook.
+  reference_init.npz  (--init N) statistics of the reference's own
+      initialisation (SEIR_ABM and the five constructors) of the init case,
+      seeds 1 .. N: per-node state counts, the missed count, histograms of
+      the timers, ages, ages at death and RI offsets, a (risk, infectivity)
+      sample, and the age pyramid it read.
 
 The reference checkout is read, never written; the reference's logger writes
 its log files under a temporary working directory.
@@ -246,6 +252,46 @@ def native(ref, n_seeds, out_path, workers):
           f"sd {tot.std():.1f} ({Path(out_path).stat().st_size} bytes)")
 
 
+INIT_CASE = "init"
+
+def _init_run(seed):
+    import replay_cases
+    from laser_core.propertyset import PropertySet
+    from replay_cases import init_statistics
+
+    lp = _NATIVE["lp"]
+    pars = replay_cases.make_pars(INIT_CASE, lp, PropertySet, _NATIVE["pyramid"])
+    pars.seed = int(seed)
+    sim = lp.SEIR_ABM(pars)
+    sim.components = replay_cases.components(lp)
+    return init_statistics(sim.people, sim.people.count, sim.people.capacity), int(sim.people.capacity)
+
+
+def init_fixture(ref, n_seeds, out_path, workers):
+    """reference_init.npz: statistics of the reference's own initialisation
+    of the init case for seeds 1 .. n_seeds, summed over seeds (histograms,
+    counts) or stacked (the risk and infectivity sample of each run), with
+    the age pyramid it read."""
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers, initializer=_native_worker_init, initargs=(str(ref),)) as pool:
+        runs = pool.map(_init_run, range(1, n_seeds + 1))
+    out = {}
+    for k in runs[0][0]:
+        vals = [r[0][k] for r in runs]
+        out[k] = np.concatenate(vals, axis=1) if k == "risk_inf" else (np.stack(vals) if k in ("state_by_node", "missed")
+                                                                       else np.sum(vals, axis=0))
+    import reference_harness  # noqa: F401
+    from laser_polio_gb300.core import load_pyramid_csv
+
+    out["pyramid"] = load_pyramid_csv(Path(ref) / "data" / "Nigeria_age_pyramid_2024.csv")
+    out["capacity"] = np.array([runs[0][1]])
+    out["seeds"] = np.arange(1, n_seeds + 1)
+    np.savez_compressed(out_path, **out)
+    print(f"wrote {out_path}: {n_seeds} reference initialisations ({Path(out_path).stat().st_size} bytes)")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("reference", help="path of the laser-polio checkout")
@@ -254,8 +300,13 @@ def main():
     ap.add_argument("--native", type=int, default=0, metavar="N",
                     help="instead: N reference runs of the native case with numpy's own generator")
     ap.add_argument("--workers", type=int, default=os.cpu_count() or 1)
+    ap.add_argument("--init", type=int, default=0, metavar="N",
+                    help="instead: statistics of N reference initialisations of the init case")
     args = ap.parse_args()
     ref = Path(args.reference).resolve()
+    if args.init:
+        init_fixture(ref, args.init, HERE / "reference_init.npz", args.workers)
+        return
     if args.native:
         native(ref, args.native, HERE / "reference_native.npz", args.workers)
         return

@@ -61,6 +61,15 @@ def make_pars(name, lp, property_set, pyramid_path=None):
         p = dict(make_pars("zamfara", lp, dict, pyramid_path))
         p.update(dur=120)
         return property_set(p)
+    elif name == "init":  # the reference's own initialisation: every init parameter exercised
+        rng = np.random.default_rng(21)
+        p.update(
+            seed=1, dur=30, init_pop=np.round(rng.lognormal(np.log(1500), 0.5, 14)).astype(int),
+            cbr=np.full(14, 37.0), init_immun=list(rng.uniform(0.2, 0.9, 14)),
+            init_prev=[10, 0, 0.01, 0, 3, 0, 0, 0, 0, 0, 0, 0, 0, 25], missed_frac=0.1,
+            r0=14, r0_scalars=np.ones(14), distances=np.ones((14, 14)) - np.eye(14), migration_method="gravity",
+            vx_prob_ri=0.5,
+        )
     elif name == "collisions":
         p.update(
             seed=77, dur=40, init_pop=np.array([3000, 1500, 800]), cbr=np.array([30.0, 30.0, 30.0]),
@@ -138,3 +147,37 @@ def initial_columns(name, count, capacity, init_pop, seed):
     cols["acq_risk_multiplier"] = np.maximum(0.5, rng.lognormal(0.0, 0.5, cap)).astype(np.float32)
     cols["daily_infectivity"] = rng.exponential(0.5, cap).astype(np.float32)
     return cols
+
+
+INIT_COLUMNS = ("disease_state", "chronically_missed", "node_id", "exposure_timer", "infection_timer",
+                "paralysis_timer", "acq_risk_multiplier", "daily_infectivity", "date_of_birth", "date_of_death",
+                "ri_timer", "strain", "potentially_paralyzed", "paralyzed", "ipv_protected")
+
+
+def init_statistics(people, count, capacity):
+    """Summaries of an initial agent table that a test can compare with
+    another: exact counts, histograms of the integer columns and a sample of
+    the (risk, infectivity) pairs."""
+    c = {k: np.asarray(getattr(people, k)) for k in INIT_COLUMNS}
+    live = slice(0, count)
+    n_nodes = int(c["node_id"][live].max()) + 1
+    out = {
+        "state_by_node": np.stack([np.bincount(c["node_id"][live][c["disease_state"][live] == s],
+                                               minlength=n_nodes) for s in range(4)]),
+        "missed": np.array([int(c["chronically_missed"][live].sum())]),
+        "et": np.bincount(c["exposure_timer"].astype(np.int64) + 128, minlength=256),
+        "it": np.bincount(c["infection_timer"].astype(np.int64) + 128, minlength=256),
+        "pt": np.bincount(c["paralysis_timer"].astype(np.int64) + 128, minlength=256),
+        "age_years": np.bincount(-c["date_of_birth"][live] // 365, minlength=101)[:101],
+        "death_age_years": np.bincount(np.minimum((c["date_of_death"][live] - c["date_of_birth"][live]) // 365,
+                                                  150), minlength=151),
+        "ri_offset": np.bincount((c["ri_timer"][live].astype(np.int64) - c["date_of_birth"][live]) % 65536,
+                                 minlength=65536)[:200],
+        "risk_inf": np.stack([c["acq_risk_multiplier"][:2000], c["daily_infectivity"][:2000]]).astype(np.float32),
+        "defaults": np.array([int((c["strain"][live] != 0).sum()), int((c["potentially_paralyzed"] != -1).sum()),
+                              int((c["paralyzed"] != 0).sum()), int((c["ipv_protected"] != 0).sum()),
+                              int((c["disease_state"][count:] != -1).sum())]),
+    }
+    return out
+
+

@@ -11,18 +11,20 @@ import numpy as np
 
 from laser_polio_gb300.engine import _advance_count
 from laser_polio_gb300.engine import build_sim_spec
+from laser_polio_gb300.engine import host_columns
 from oracle.oracle import OracleSim
 
 
 def run_with_oracle(sim, n_ticks=None):
     spec = build_sim_spec(sim)
+    cols = {k: getattr(sim.people, k) for k in spec.columns}  # host arrays (device columns copied over once)
     o = OracleSim(spec.desc, keepalive=spec)
-    o.bind_columns(spec.columns)
+    o.bind_columns(cols)
     o.start()
     o.step(sim.nt - 1 if n_ticks is None else n_ticks)
     st = o.state()
     o.read_results(spec.results)
-    o.read_columns(spec.columns)
+    o.read_columns(cols)
     _advance_count(sim.people, st.count)
     sim.t = st.t
     sim.should_stop = bool(st.stopped)
@@ -31,9 +33,10 @@ def run_with_oracle(sim, n_ticks=None):
 
 
 def snapshot(sim):
-    """Copies of the spec's columns and results (for parity comparisons)."""
+    """Copies of the spec's columns (on the host, wherever they live) and
+    results, for parity comparisons."""
     spec = build_sim_spec(sim)
-    cols = {k: v.copy() for k, v in spec.columns.items()}
+    cols = host_columns(spec)
     res = {k: v.copy() for k, v in spec.results.items()}
     return spec, cols, res
 
@@ -122,3 +125,19 @@ class OracleHandle:
 
     def close(self):
         self.o.close()
+
+
+def oracle_fill(people, spec, parts):
+    """laser_polio_gb300.init.fill with the oracle's restatement of the
+    device initialisation (lpo_init_columns, the same draws): host numpy
+    columns, for tests on a machine without a GPU."""
+    from laser_polio_gb300 import init as dinit
+    from oracle.oracle import init_columns
+
+    cols = {}
+    for name in dinit.part_columns(parts):
+        if not people.has_column(name):
+            people.add_scalar_property(name, dtype=dinit.COLUMN_DTYPES[name], default=0)
+        cols[name] = getattr(people, name)
+    desc, _keep = spec.desc()
+    init_columns(desc, parts, cols)
