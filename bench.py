@@ -22,6 +22,9 @@ reference's loops do).
             compared, every array and every slot, with the end-to-end run's.
   full_run  the whole 2555-tick run replayed on the device, and the mean
             time of each kind of tick (plain, births, RI, SIA days).
+  e2e_api   the user's path at the same scale: SEIR_ABM(pars), the five
+            components (agent table initialised on the device), run() over
+            all ticks; wall time of construction and run.
 
 python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
@@ -64,6 +67,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--no-full-run", action="store_true")
+    ap.add_argument("--no-api", action="store_true")
     ap.add_argument("--parity-ticks", type=int, default=60,
                     help="the oracle's parity leg runs min(W + K, this) ticks of the same population")
     ap.add_argument("--out", default=None)
@@ -397,6 +401,44 @@ def reference_arm(args):
         "e2e": {"value": cpu["value"], "unit": "agent-ticks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def api_run(args, dev):
+    """The user's whole path at the Nigeria scale: SEIR_ABM(pars) and the
+    five components (the agent table initialised on the device), then run()
+    over all 2555 ticks with results landing in sim.results; wall time of
+    each phase, with the device synchronised at the end of each."""
+    import torch
+
+    import laser_polio_gb300 as lp
+    from laser_polio_gb300 import synthetic
+
+    pars, immun, rng = synthetic.nigeria_like_pars(n_agents=int(args.agents), n_nodes=args.nodes, seed=args.seed)
+    prev = np.zeros(args.nodes, np.int64)
+    prev[rng.choice(args.nodes, size=2, replace=False)] = 10
+    pars.update({"init_immun": list(np.asarray(immun, float)), "init_prev": list(prev), "age_pyramid_path": None})
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim = lp.SEIR_ABM(lp.PropertySet(pars))
+    sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.RI_ABM, lp.SIA_ABM, lp.Transmission_ABM]
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    sim.run()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    births = sim.results.births.sum(axis=1).astype(np.int64)
+    cnt = int(np.sum(pars["init_pop"])) + np.cumsum(births)
+    at = float(cnt[1 : sim.t].sum())
+    out = {"value": at / (t2 - t0), "unit": "agent-ticks/s", "ticks": int(sim.t) - 1, "agents": int(cnt[0]),
+           "capacity": int(sim.people.capacity), "seconds": t2 - t0,
+           "phases_s": {"construct": t1 - t0, "run": t2 - t1},
+           "path": "SEIR_ABM(pars); sim.components = [...]; sim.run(): agent table initialised on the device, "
+                   "results copied to sim.results, columns left on the device",
+           "new_exposed_total": int(sim.results.new_exposed.sum())}
+    if sim._engine is not None:
+        sim._engine.close()
+    del sim
+    return out
 
 
 def tick_kind(params, t):
@@ -849,6 +891,11 @@ def main():
     if not args.no_full_run:
         full = full_run(desc, cols, params, dev)
 
+    # ---- the user's path: construct (device initialisation) and run -------
+    api = None
+    if not args.no_api:
+        api = api_run(args, dev)
+
     # ---- per-kernel times (profiling mode, same ticks) --------------------
     roof = None
     prof = None
@@ -966,6 +1013,7 @@ def main():
             "cpu_baseline": cpu,
             "parity": parity,
             "full_run": full,
+            "e2e_api": api,
             "clocks": summ,
             "gpu_launches": launches,
             "work_counters": work,
