@@ -1625,6 +1625,9 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
  * target needs one load to find everything about its node. */
 #define LPG_SEL_OFFS 2048 /* target offsets kept in shared memory when G < this */
 #define LPG_NODE_TX_THREADS 64
+/* six CTAs of the node step per SM (at most 170 registers a thread): one
+ * wave covers 912 nodes, so a 774-node tick needs no second wave */
+#define LPG_NODE_TX_MIN_BLOCKS 6
 
 struct SelInfo {
   uint64_t seed;
@@ -1700,7 +1703,7 @@ __device__ __forceinline__ uint64_t pre_bb_w1(const DevWorld& W, int g, int lane
   return lane < ns ? W.bb[(int64_t)lane * W.G + g] : 0;
 }
 
-__global__ void __launch_bounds__(LPG_NODE_TX_THREADS) k_node_tx(DevWorld W) {
+__global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k_node_tx(DevWorld W) {
   const int g = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __shared__ uint64_t s_mix[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS][6]; /* per warp: A, R words */
