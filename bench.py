@@ -25,6 +25,9 @@ reference's loops do).
   e2e_api   the user's path at the same scale: SEIR_ABM(pars), the five
             components (agent table initialised on the device), run() over
             all ticks; wall time of construction and run.
+  batch     the metric's second half: 64 calibration replicates (1e6-2e7
+            agents each, about 4e8 in all) over the same ticks in one handle,
+            against the same replicates run one after another.
 
 python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
@@ -68,6 +71,8 @@ def parse():
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--no-full-run", action="store_true")
     ap.add_argument("--no-api", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-reps", type=int, default=64, help="replicates of the batch leg of the default line")
     ap.add_argument("--parity-ticks", type=int, default=60,
                     help="the oracle's parity leg runs min(W + K, this) ticks of the same population")
     ap.add_argument("--out", default=None)
@@ -157,8 +162,9 @@ NCU_TRAFFIC_SOURCE = {
 #   k_sweep_rs (k_sweep_b) on RI ticks: 4 B per RI due index entry read; per visited
 #     sub-block its state, chronically-missed flags, RI timers, reference
 #     indexes and dates of birth (128 x 12 B) and the index write (4 B).
-#   k_node_tx: the network rows (nodes^2 x 8 B per simulation) and, per
-#     chunk of the population, its list entry, weight and prefix (20 B).
+#   k_node_tx: the network rows (nodes^2 x 16 B per simulation, two 8-byte
+#     fixed-point parts per entry) and, per chunk of the population, its list
+#     entry, weight and prefix (20 B).
 SWEEP_INDEX_B, SWEEP_DUE_B, SWEEP_EVT_B, SWEEP_DOD_B, QUEUE_ENTRY_B = 4.0, 128.0, 516.0, 516.0, 8.0
 DUE_ITEM_B = 8.0
 DSQ_ENTRY_B = 8.0 + 9.0 + 8.0
@@ -166,6 +172,7 @@ EVB_ENTRY_B = 8.0 + 10.0 + 5.0
 SEL_TARGET_B = 8.0 + 128.0 + 128.0 + 512.0 + 8.0
 SEL_CLAIM_B = 14.0
 NODE_TX_CHUNK_B = 20.0
+NODE_TX_NET_B = 16.0  # a network entry in its two fixed-point parts
 RI_INDEX_B, RI_DUE_B = 4.0, 128.0 * 12.0 + 4.0
 
 
@@ -184,19 +191,24 @@ def merge_selection(prof):
 
 def kernel_alg_bytes(params, ticks, cnt, work, new_exposed):
     """Algorithmic bytes of each modelled kernel over the ticks (total, all
-    launches), from the work counters of the same ticks."""
-    n = params["n_nodes"]
-    chunks = float(params["capacity"]) / 2048.0
+    launches), from the work counters of the same ticks.  ``params`` and
+    ``cnt`` may be lists (the simulations of one handle): the per-simulation
+    terms are summed; the work counters are the handle's."""
+    plist = params if isinstance(params, list) else [params]
+    clist = cnt if isinstance(params, list) else [cnt]
+    staged = sum(float(sum(sweep_b_bytes(p, t) * c[t] for t in ticks)) for p, c in zip(plist, clist))
+    node_tx = sum(len(ticks) * (p["n_nodes"] ** 2 * NODE_TX_NET_B + NODE_TX_CHUNK_B * float(p["capacity"]) / 2048.0)
+                  for p in plist)
     out = {
         "k_due": SWEEP_INDEX_B * work["sweep_index"] + DUE_ITEM_B * work["sweep_due"],
         "k_sweep_a": (DUE_ITEM_B * work["sweep_due"] + SWEEP_DUE_B * work["sweep_due"]
                       + SWEEP_EVT_B * work["sweep_evt_due"] + SWEEP_DOD_B * work["sweep_dod_due"]
                       + (QUEUE_ENTRY_B + DSQ_ENTRY_B) * work["queue_ds"]),
-        "k_sweep_b": (float(sum(sweep_b_bytes(params, t) * cnt[t] for t in ticks)) + RI_INDEX_B * work["ri_index"]
-                      + RI_DUE_B * work["ri_due"] + QUEUE_ENTRY_B * work["queue_rs"]),
+        "k_sweep_b": staged + RI_INDEX_B * work["ri_index"] + RI_DUE_B * work["ri_due"]
+                     + QUEUE_ENTRY_B * work["queue_rs"],
         "k_evb": EVB_ENTRY_B * work["queue_rs"],
         "k_select": SEL_TARGET_B * work["sel_targets"] + SEL_CLAIM_B * float(new_exposed),
-        "k_node_tx": len(ticks) * (n * n * 8.0 + NODE_TX_CHUNK_B * chunks),
+        "k_node_tx": node_tx,
     }
     return out
 
@@ -507,12 +519,14 @@ def full_run(desc, cols, params, dev):
                                  "per-kind sum exceeds the replayed total"}
 
 
-def batch_arm(args):
+def batch_measure(n_reps, seed, W, K, profile=True):
     """R calibration replicates (node counts from {14, 44, 120, 300}, 1e6-2e7
     agents each, per-replicate R0 / seasonality / gravity k, 730 ticks): the
     same ticks timed once with all replicates in one handle (one launch
     sequence per tick) and once as R plain runs one after another.  Both
-    arms time only the device ticks (CUDA events on the handle's stream)."""
+    time only the device ticks (CUDA events on the handle's stream).  A
+    profiling pass of the batch gives the kernels' shares and the dominant
+    kernel's modelled roofline."""
     import torch
 
     from laser_polio_gb300 import synthetic
@@ -520,68 +534,92 @@ def batch_arm(args):
     from laser_polio_gb300.engine import make_desc
 
     t_gen = time.perf_counter()
-    specs = synthetic.replicate_specs(args.batch, seed=args.seed, dur=730)
+    specs = synthetic.replicate_specs(n_reps, seed=seed, dur=730)
     bundles = [synthetic.bundle(**sp) for sp in specs]
     t_gen = time.perf_counter() - t_gen
     descs = [make_desc(p) for p, _ in bundles]
     nt = bundles[0][0]["nt"]
-    W = args.warmup
-    K = min(args.steps, nt - 1 - W)
+    K = max(1, min(K, nt - 1 - W))
 
-    def timed(idx):
+    def run(idx, profiling=False):
         h = Handle([descs[i][0] for i in idx])
         for j, i in enumerate(idx):
             h.bind_columns(j, bundles[i][1])
         h.start()
         h.step(W)
         h.sync()
+        if profiling:
+            h.set_profiling(True)
         stream = torch.cuda.ExternalStream(h.cuda_stream())
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
+        l0 = h.kernel_launches()
         e0.record(stream)
         h.step(K)
         e1.record(stream)
         h.sync()
         ms = e0.elapsed_time(e1)
-        at = 0.0
+        launches = h.kernel_launches() - l0
+        at, cnts, ne = 0.0, [], 0
         for j, i in enumerate(idx):
             res = result_arrays(bundles[i][0])
             h.read_results(j, res)
             cnt = counts_per_tick(bundles[i][0], res["births"])
+            cnts.append(cnt)
             at += float(cnt[W + 1 : W + K + 1].sum())
-        launches = h.kernel_launches()
+            tk = slice(W + 1, W + K + 1)
+            ne += int(res["new_exposed"][tk].sum() - res["ri_protected"][tk].sum() - res["sia_protected"][tk].sum())
+        prof = merge_selection(h.profile()) if profiling else None
+        work = h.counters() if profiling else None
         h.close()
-        return ms, at, launches
+        return ms, at, launches, prof, work, cnts, ne
 
-    with ClockSampler(0) as clocks:
-        clocks.wait_ready()
-        ms_b, at_b, _ = timed(list(range(len(bundles))))
+    ms_b, at_b, launches_b, _, _, _, _ = run(list(range(len(bundles))))
     ms_s, at_s = 0.0, 0.0
     for i in range(len(bundles)):
-        ms, at, _ = timed([i])
+        ms, at, _, _, _, _, _ = run([i])
         ms_s += ms
         at_s += at
     assert at_s == at_b
-    line = {
-        "metric": f"agent-ticks/s, {len(bundles)}-replicate calibration batch",
-        "value": at_b / (ms_b / 1e3),
-        "unit": "agent-ticks/s",
-        "n_gpus": 1,
-        "steps": K,
-        "warmup": W,
-        "ms_per_step": ms_b / K,
-        "higher_is_better": True,
-        "data": "synthetic (seeded numpy, calibration-batch shapes)",
-        "config": {"workload": f"{len(bundles)} replicates, nodes in {{14, 44, 120, 300}}, "
-                               f"{sum(p['count'] for p, _ in bundles):.3g} agents in total, "
-                               f"ticks {W + 1}-{W + K} of 730",
-                   "agents": [p["count"] for p, _ in bundles], "nodes": [p["n_nodes"] for p, _ in bundles]},
+    out = {
+        "value": at_b / (ms_b / 1e3), "unit": "agent-ticks/s", "replicates": len(bundles),
+        "agents": int(sum(p["count"] for p, _ in bundles)), "nodes": [p["n_nodes"] for p, _ in bundles],
+        "ticks": f"{W + 1}-{W + K} of 730", "ms_per_step": ms_b / K, "gpu_launches_per_tick": launches_b / K,
         "sequential": {"value": at_s / (ms_s / 1e3), "ms_total": ms_s},
-        "batched_ms_total": ms_b,
-        "speedup_vs_sequential": ms_s / ms_b,
-        "clocks": clocks.summary(),
-        "generation_s": t_gen,
+        "batched_ms_total": ms_b, "speedup_vs_sequential": ms_s / ms_b, "generation_s": t_gen,
+    }
+    if profile:
+        _, _, _, prof, work, cnts, ne = run(list(range(len(bundles))), profiling=True)
+        ticks = np.arange(W + 1, W + K + 1)
+        alg = kernel_alg_bytes([p for p, _ in bundles], ticks, cnts, work, ne)
+        tot = sum(v[0] for v in prof.values())
+        top = max(prof, key=lambda k: prof[k][0])
+        t_ms, t_n = prof[top]
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        ach = alg[top] / (t_ms / 1e3) / 1e9 if top in alg and t_ms > 0 else None
+        out["kernels"] = {k: {"ms_per_launch": v[0] / max(1, v[1]), "share": v[0] / tot} for k, v in prof.items()}
+        out["roofline"] = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                           "frac": ach / peak if ach is not None else None,
+                           "alg_bytes_per_launch": alg.get(top, 0.0) / max(1, t_n),
+                           "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    return out
+
+
+def batch_arm(args):
+    """The batch measurement alone, as its own line (see batch_measure)."""
+    with ClockSampler(0) as clocks:
+        clocks.wait_ready()
+        b = batch_measure(args.batch, args.seed, args.warmup, args.steps)
+    line = {
+        "metric": f"agent-ticks/s, {b['replicates']}-replicate calibration batch",
+        "value": b["value"], "unit": "agent-ticks/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": b["ms_per_step"], "higher_is_better": True,
+        "data": "synthetic (seeded numpy, calibration-batch shapes)",
+        "config": {"workload": f"{b['replicates']} replicates, nodes in {{14, 44, 120, 300}}, "
+                               f"{b['agents']:.3g} agents in total, ticks {b['ticks']}"},
+        "batch": b, "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
     if args.out:
@@ -809,9 +847,6 @@ def main():
     col_bytes = sum(v.nbytes for v in cols.values())
     P = min(W + K, args.parity_ticks)  # ticks of the oracle's parity leg
 
-    clocks = ClockSampler(dev)
-    clocks.__enter__()  # the whole device phase: end to end, timed region, full run, profiling
-    clocks.wait_ready()
 
     # ---- end to end through the C ABI from pinned host columns --------------
     e2e = None
@@ -852,6 +887,13 @@ def main():
             e2e_res, e2e_cols = res, out_cols
         else:
             del out_cols
+
+    # the clocks of the rest of the device phase (timed region, full run, user
+    # path, batch, profiling); started after the end-to-end leg, whose large
+    # host-to-device copies nvidia-smi's polling slows down
+    clocks = ClockSampler(dev)
+    clocks.__enter__()
+    clocks.wait_ready()
 
     # ---- device-resident timed region ------------------------------------
     h = Handle([desc], device=dev)
@@ -895,6 +937,11 @@ def main():
     api = None
     if not args.no_api:
         api = api_run(args, dev)
+
+    # ---- the calibration batch: 64 replicates in one handle vs one by one --
+    batch = None
+    if not args.no_batch and ws == 1:
+        batch = batch_measure(args.batch_reps, args.seed, W, K)
 
     # ---- per-kernel times (profiling mode, same ticks) --------------------
     roof = None
@@ -992,8 +1039,8 @@ def main():
     if rank == 0:
         summ = clocks.summary()
         summ["samples_in_timed_region"] = timed_to - timed_from
-        summ["window"] = "nvidia-smi every 100 ms over the whole device phase (end to end, timed region, " \
-                         "full run, profiling)"
+        summ["window"] = "nvidia-smi every 100 ms from the timed region to the end of the device phase " \
+                         "(timed region, full run, user path, batch, profiling)"
         line = {
             "metric": "agent-ticks/s (774 nodes, 2.2e8 agents, full agent step)",
             "value": value,
@@ -1014,6 +1061,7 @@ def main():
             "parity": parity,
             "full_run": full,
             "e2e_api": api,
+            "batch": batch,
             "clocks": summ,
             "gpu_launches": launches,
             "work_counters": work,
