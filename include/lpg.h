@@ -306,6 +306,28 @@ int lpg_read_counters(lpg_handle* h, uint64_t* out, int32_t n);
  * context stays usable.  Cached CUDA graphs are dropped. */
 int lpg_test_stall_sweep(lpg_handle* h, int32_t stages, int64_t wait_spin);
 
+/* Grid sizes (CTAs) of the tick kernels, after lpg_start: the engine's
+ * default is every CTA that fits at once (occupancy x SM count, capped);
+ * an autotuner may set others.  Results do not depend on them (every kernel
+ * is a grid-stride or work-split loop over exact integer updates), only the
+ * time does.  Setting one drops the cached CUDA graphs.  No counterpart in
+ * the reference.  lpg_set_launch returns LPG_ERR_ARG outside [1, the
+ * kernel's limit] (1024 for the two sweeps, whose per-CTA queue slabs are
+ * sized for that; 8192 for the others); lpg_get_launch returns the size, or
+ * a negative lpg_status. */
+enum {
+  LPG_LAUNCH_DUE = 0,       /* k_due */
+  LPG_LAUNCH_SWEEP_DUE = 1, /* k_sweep_due */
+  LPG_LAUNCH_SWEEP_RS = 2,  /* k_sweep_rs (and the slabs k_evb reads) */
+  LPG_LAUNCH_EVB = 3,       /* k_evb */
+  LPG_LAUNCH_SELECT = 4,    /* k_sel_locate, k_sel_rounds */
+  LPG_LAUNCH_CLAIM = 5,     /* k_sel_claim */
+  LPG_LAUNCH_NEWBORNS = 6,  /* k_newborns (CTAs per replicate) */
+  LPG_NUM_LAUNCH = 7
+};
+int lpg_set_launch(lpg_handle* h, int32_t which, int32_t blocks);
+int lpg_get_launch(lpg_handle* h, int32_t which);
+
 /* The CUDA stream the handle launches on, as an opaque pointer. */
 void* lpg_cuda_stream(lpg_handle* h);
 

@@ -136,6 +136,17 @@ class lpg_columns(C.Structure):
     _fields_ = [(name, ptype) for name, ptype, _ in COLUMN_FIELDS]
 
 
+# lpg_set_launch's tick kernels: name -> (index, largest grid, the profile entries it times)
+LAUNCH = {
+    "due": (0, 8192, ("k_due",)),
+    "sweep_due": (1, 1024, ("k_sweep_a",)),
+    "sweep_rs": (2, 1024, ("k_sweep_b",)),
+    "evb": (3, 8192, ("k_evb",)),
+    "select": (4, 8192, ("k_sel_locate", "k_sel_rounds")),
+    "claim": (5, 8192, ("k_sel_claim",)),
+    "newborns": (6, 8192, ("k_newborns",)),
+}
+
 # lpg_init_columns' parts, in the order they run
 INIT_BASE, INIT_MISSED, INIT_TIMERS, INIT_IMMUNITY, INIT_PREVALENCE = 1, 2, 4, 8, 16
 INIT_HETEROGENEITY, INIT_AGES, INIT_DEATHS, INIT_RI = 32, 64, 128, 256

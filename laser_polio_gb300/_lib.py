@@ -64,6 +64,8 @@ SIGNATURES = {
                                    C.c_void_p]),
     "lpg_init_mean_infectivity": (C.c_double, [C.c_uint64, C.c_double, _abi.lpg_dist]),
     "lpg_test_stall_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
+    "lpg_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "lpg_get_launch": (C.c_int, [C.c_void_p, C.c_int32]),
 }
 
 
@@ -170,6 +172,16 @@ class Handle:
         if st.error and check:
             self.sync()
         return st
+
+    def set_launch(self, which: int, blocks: int):
+        """Grid size of a tick kernel (lpg_set_launch; LAUNCH_* in _abi)."""
+        self._check(self.lib.lpg_set_launch(self.h, int(which), int(blocks)))
+
+    def get_launch(self, which: int) -> int:
+        rc = self.lib.lpg_get_launch(self.h, int(which))
+        if rc < 0:
+            self._check(rc)
+        return int(rc)
 
     def test_stall_sweep(self, stages: int, wait_spin: int = 0):
         """Test hook (lpg_test_stall_sweep): the staged RI/SIA sweep issues

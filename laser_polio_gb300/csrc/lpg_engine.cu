@@ -98,6 +98,8 @@ struct lpg_handle {
   int due_blocks = 0;    /* k_due */
   int select_blocks = 0; /* k_sel_locate, k_sel_rounds */
   int claim_blocks = 0;
+  int evb_blocks = 0;
+  int newborn_blocks = 0; /* per replicate */
 };
 
 static int fail(lpg_handle* h, int code, const char* fmt, ...) {
@@ -943,6 +945,8 @@ extern "C" int lpg_start(lpg_handle* h) {
   occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sel_claim, 256, 0));
   h->claim_blocks = std::min(2048, std::max(1, occ) * h->sm_count);
+  h->evb_blocks = h->sm_count * 8;
+  h->newborn_blocks = h->sm_count * 8;
   h->next_tick = 1; /* tick 0 ran above (k_end); the components run from tick 1 */
   h->started = true;
   return LPG_OK;
@@ -961,12 +965,12 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
   }
   switch (k) {
     case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
-    case 1: k_newborns<<<dim3(h->sm_count * 8, R), 256, 0, st>>>(W); break;
+    case 1: k_newborns<<<dim3(h->newborn_blocks, R), 256, 0, st>>>(W); break;
     case 2: k_due<<<h->due_blocks, 256, 0, st>>>(W); break;
     case 3: k_sweep_due<<<h->sweep0_blocks, LPG_SWEEP_BLOCK, 0, st>>>(W); break;
     case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
     case 5: k_sweep_rs<<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 6: k_evb<<<h->sm_count * 8, 256, 0, st>>>(W, h->sweep_blocks); break;
+    case 6: k_evb<<<h->evb_blocks, 256, 0, st>>>(W, h->sweep_blocks); break;
     case 7: k_node_tx<<<G, LPG_NODE_TX_THREADS, 0, st>>>(W); break;
     case 8: k_sel_locate<<<h->select_blocks, 256, 0, st>>>(W); break;
     case 9: k_sel_claim<<<h->claim_blocks, 256, 0, st>>>(W); break;
@@ -1238,6 +1242,43 @@ extern "C" int lpg_check_invariants(lpg_handle* h) {
   for (void* p : ps) dfree_one(h, p);
   if (hb) return fail(h, LPG_ERR_INTERNAL, "running totals differ from a recount (mask 0x%x)", hb);
   return LPG_OK;
+}
+
+static int* launch_slot(lpg_handle* h, int32_t which, int* limit) {
+  switch (which) {
+    case LPG_LAUNCH_DUE: *limit = 8192; return &h->due_blocks;
+    case LPG_LAUNCH_SWEEP_DUE: *limit = 1024; return &h->sweep0_blocks;
+    case LPG_LAUNCH_SWEEP_RS: *limit = 1024; return &h->sweep_blocks;
+    case LPG_LAUNCH_EVB: *limit = 8192; return &h->evb_blocks;
+    case LPG_LAUNCH_SELECT: *limit = 8192; return &h->select_blocks;
+    case LPG_LAUNCH_CLAIM: *limit = 8192; return &h->claim_blocks;
+    case LPG_LAUNCH_NEWBORNS: *limit = 8192; return &h->newborn_blocks;
+    default: return nullptr;
+  }
+}
+
+extern "C" int lpg_set_launch(lpg_handle* h, int32_t which, int32_t blocks) {
+  if (!h) return LPG_ERR_ARG;
+  if (!h->started) return fail(h, LPG_ERR_STATE, "lpg_set_launch before lpg_start");
+  int limit = 0;
+  int* slot = launch_slot(h, which, &limit);
+  if (!slot) return fail(h, LPG_ERR_ARG, "no tick kernel %d", which);
+  if (blocks < 1 || blocks > limit) return fail(h, LPG_ERR_ARG, "grid of %d CTAs outside [1, %d]", blocks, limit);
+  if (*slot != blocks) {
+    *slot = blocks;
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second.first);
+    h->graphs.clear();
+  }
+  return LPG_OK;
+}
+
+extern "C" int lpg_get_launch(lpg_handle* h, int32_t which) {
+  if (!h) return LPG_ERR_ARG;
+  if (!h->started) return fail(h, LPG_ERR_STATE, "lpg_get_launch before lpg_start");
+  int limit = 0;
+  int* slot = launch_slot(h, which, &limit);
+  if (!slot) return fail(h, LPG_ERR_ARG, "no tick kernel %d", which);
+  return *slot;
 }
 
 extern "C" int lpg_test_stall_sweep(lpg_handle* h, int32_t stages, int64_t wait_spin) {

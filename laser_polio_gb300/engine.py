@@ -242,7 +242,19 @@ def host_columns(spec) -> dict:
     return {k: (v.copy() if isinstance(v, np.ndarray) else v.cpu().numpy().copy()) for k, v in spec.columns.items()}
 
 
-def run_replicates(sims) -> list:
+def _autotune_key(handle_sims, sims):
+    import torch
+
+    from . import autotune
+
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    nodes = sum(len(s.nodes) for s in sims)
+    agents = sum(int(s.people.count) for s in sims)
+    return autotune.workload_key(props.name, props.multi_processor_count, len(sims), nodes, agents), \
+        props.multi_processor_count
+
+
+def run_replicates(sims, autotune=False) -> list:
     """Run several SEIR_ABM (drop-in GPU components) as one batch: one
     handle, one launch sequence per tick for all of them.  The reference's
     calibration runs its replicates one after another, each in its own
@@ -253,7 +265,10 @@ def run_replicates(sims) -> list:
       - on the device a sim that fails (births beyond its capacity, a
         timed-out wait) stops at that tick while the others run to their end.
     The sims may differ in nodes, agents, durations and components; each
-    stops at its own last tick or stop rule.  Every sim that ran holds what
+    stops at its own last tick or stop rule.  With ``autotune`` the tick
+    kernels' grid sizes are picked on the run's first ticks, or taken from
+    the on-disk cache for the same kind of batch (autotune.py); the results
+    are the same either way.  Every sim that ran holds what
     its own run() would have left (results, people columns and count, t and
     should_stop; a failed one as far as it got).  Returns one entry per sim:
     None, or the exception its run raised (ValueError for bad parameters,
@@ -281,7 +296,15 @@ def run_replicates(sims) -> list:
         for j, sp in enumerate(specs):
             handle.bind_columns(j, sp.columns)
         handle.start()
-        handle.step(max(int(sims[i].nt) for i in ok) - 1)
+        remaining = max(int(sims[i].nt) for i in ok) - 1
+        if autotune and remaining > 0:
+            from . import autotune as _tune
+
+            key, sm_count = _autotune_key(specs, [sims[i] for i in ok])
+            _, stepped = _tune.tune(handle, key, sm_count)
+            remaining -= stepped
+        if remaining > 0:
+            handle.step(remaining)
         statuses = handle.sync_statuses()
         for j, (i, sp) in enumerate(zip(ok, specs)):
             sim = sims[i]
