@@ -138,7 +138,7 @@ def sweep_b_bytes(params, t):
 # bytes per unit, bytes per launch besides), and where they were measured.
 NCU_TRAFFIC_PER_UNIT = {"k_select": ("sel_targets", 1071.0, 0.0)}
 NCU_TRAFFIC_SOURCE = {
-    "k_select": "ncu DRAM read+write of k_sel_locate + k_sel_claim + k_sel_rounds per target located, "
+    "k_select": "ncu DRAM read+write of k_sel_round0 + k_sel_rounds per target located, "
                 "on tick 151 of the 5e7-agent Nigeria-like case, times the targets of the timed ticks",
 }
 
@@ -155,10 +155,11 @@ NCU_TRAFFIC_SOURCE = {
 #     and state, timers and event tick written (8 B).
 #   k_evb: per queue entry the 8 B entry, then state, RI timer, flags and
 #     date of birth read (10 B) and state and timer written (5 B).
-#   k_select: per target located, the chunk prefix entry (8 B), the
-#     sub-block totals (16 x 8 B), the sub-block's 128 state bytes and 128
-#     risks (512 B), the target's hit written and read back (8 B); per agent
-#     exposed, state, strain, timers, event tick and its index (14 B).
+#   k_select: per target located, the chunk prefix entry and chunk id
+#     (12 B), the sub-block totals (16 x 8 B), the sub-block's 128 state
+#     bytes and 128 risks (512 B); per agent exposed, its reference index,
+#     state (claimed, then exposed), strain, timers, event tick and its
+#     index (15 B).
 #   k_sweep_rs (k_sweep_b) on RI ticks: 4 B per RI due index entry read; per visited
 #     sub-block its state, chronically-missed flags, RI timers, reference
 #     indexes and dates of birth (128 x 12 B) and the index write (4 B).
@@ -169,16 +170,16 @@ SWEEP_INDEX_B, SWEEP_DUE_B, SWEEP_EVT_B, SWEEP_DOD_B, QUEUE_ENTRY_B = 4.0, 128.0
 DUE_ITEM_B = 8.0
 DSQ_ENTRY_B = 8.0 + 9.0 + 8.0
 EVB_ENTRY_B = 8.0 + 10.0 + 5.0
-SEL_TARGET_B = 8.0 + 128.0 + 128.0 + 512.0 + 8.0
-SEL_CLAIM_B = 14.0
+SEL_TARGET_B = 12.0 + 128.0 + 128.0 + 512.0
+SEL_CLAIM_B = 15.0
 NODE_TX_CHUNK_B = 20.0
 NODE_TX_NET_B = 16.0  # a network entry in its two fixed-point parts
 RI_INDEX_B, RI_DUE_B = 4.0, 128.0 * 12.0 + 4.0
 
 
 def merge_selection(prof):
-    """The selection's three kernels (k_sel_locate, k_sel_claim,
-    k_sel_rounds) as one entry, k_select, per tick."""
+    """The selection's two kernels (k_sel_round0, k_sel_rounds) as one
+    entry, k_select, per tick."""
     out = {}
     for k, (ms, n) in prof.items():
         if k.startswith("k_sel_"):

@@ -306,6 +306,15 @@ int lpg_read_counters(lpg_handle* h, uint64_t* out, int32_t n);
  * context stays usable.  Cached CUDA graphs are dropped. */
 int lpg_test_stall_sweep(lpg_handle* h, int32_t stages, int64_t wait_spin);
 
+/* Test hook of the same kind for the first selection round, whose CTAs meet
+ * at a grid barrier (a cooperative launch: all of them resident): with
+ * skip != 0, CTA 0 does not arrive, and the others give up their bounded
+ * wait after `wait_spin` polls (0: the normal limit).  Every running
+ * simulation then records LPG_ERR_TIMEOUT (the barrier's count is spent),
+ * the kernel returns and the context stays usable.  Cached CUDA graphs are
+ * dropped.  No counterpart in the reference. */
+int lpg_test_stall_round0(lpg_handle* h, int32_t skip, int64_t wait_spin);
+
 /* Grid sizes (CTAs) of the tick kernels, after lpg_start: the engine's
  * default is every CTA that fits at once (occupancy x SM count, capped);
  * an autotuner may set others.  Results do not depend on them (every kernel
@@ -313,15 +322,16 @@ int lpg_test_stall_sweep(lpg_handle* h, int32_t stages, int64_t wait_spin);
  * time does.  Setting one drops the cached CUDA graphs.  No counterpart in
  * the reference.  lpg_set_launch returns LPG_ERR_ARG outside [1, the
  * kernel's limit] (1024 for the two sweeps, whose per-CTA queue slabs are
- * sized for that; 8192 for the others); lpg_get_launch returns the size, or
- * a negative lpg_status. */
+ * sized for that, and for k_sel_rounds; for k_sel_round0, a cooperative
+ * launch, the CTAs that fit on the GPU at once; 8192 for the others);
+ * lpg_get_launch returns the size, or a negative lpg_status. */
 enum {
   LPG_LAUNCH_DUE = 0,       /* k_due */
   LPG_LAUNCH_SWEEP_DUE = 1, /* k_sweep_due */
   LPG_LAUNCH_SWEEP_RS = 2,  /* k_sweep_rs (and the slabs k_evb reads) */
   LPG_LAUNCH_EVB = 3,       /* k_evb */
-  LPG_LAUNCH_SELECT = 4,    /* k_sel_locate, k_sel_rounds */
-  LPG_LAUNCH_CLAIM = 5,     /* k_sel_claim */
+  LPG_LAUNCH_SELECT = 4,    /* k_sel_round0 (cooperative: at most the CTAs resident at once) */
+  LPG_LAUNCH_ROUNDS = 5,    /* k_sel_rounds */
   LPG_LAUNCH_NEWBORNS = 6,  /* k_newborns (CTAs per replicate) */
   LPG_NUM_LAUNCH = 7
 };

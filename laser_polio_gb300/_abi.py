@@ -136,14 +136,16 @@ class lpg_columns(C.Structure):
     _fields_ = [(name, ptype) for name, ptype, _ in COLUMN_FIELDS]
 
 
-# lpg_set_launch's tick kernels: name -> (index, largest grid, the profile entries it times)
+# lpg_set_launch's tick kernels: name -> (index, largest grid, the profile
+# entries it times); None: the engine's default is the largest (the
+# cooperative k_sel_round0, whose CTAs must all be resident at once)
 LAUNCH = {
     "due": (0, 8192, ("k_due",)),
     "sweep_due": (1, 1024, ("k_sweep_a",)),
     "sweep_rs": (2, 1024, ("k_sweep_b",)),
     "evb": (3, 8192, ("k_evb",)),
-    "select": (4, 8192, ("k_sel_locate", "k_sel_rounds")),
-    "claim": (5, 8192, ("k_sel_claim",)),
+    "select": (4, None, ("k_sel_round0",)),
+    "rounds": (5, 1024, ("k_sel_rounds",)),
     "newborns": (6, 8192, ("k_newborns",)),
 }
 

@@ -64,6 +64,7 @@ SIGNATURES = {
                                    C.c_void_p]),
     "lpg_init_mean_infectivity": (C.c_double, [C.c_uint64, C.c_double, _abi.lpg_dist]),
     "lpg_test_stall_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
+    "lpg_test_stall_round0": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
     "lpg_set_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "lpg_get_launch": (C.c_int, [C.c_void_p, C.c_int32]),
 }
@@ -188,6 +189,13 @@ class Handle:
         only `stages` stages and its consumers give up after `wait_spin`
         iterations, so that a test can make the bounded wait run out."""
         self._check(self.lib.lpg_test_stall_sweep(self.h, int(stages), int(wait_spin)))
+
+    def test_stall_round0(self, skip: bool, wait_spin: int = 0):
+        """Test hook (lpg_test_stall_round0): CTA 0 of the first selection
+        round does not arrive at the round's grid barrier and the others give
+        up after `wait_spin` polls, so that a test can make that bounded wait
+        run out."""
+        self._check(self.lib.lpg_test_stall_round0(self.h, int(bool(skip)), int(wait_spin)))
 
     def read_results(self, sim: int, res: dict):
         self._check(self.lib.lpg_read_results(self.h, sim, C.byref(_abi.make_results_view(res))))

@@ -36,8 +36,8 @@ from . import _abi
 DEFAULT_MULTIPLES = {
     "due": (2, 4, 8),
     "sweep_due": (1, 2, 4),
-    "select": (1, 2, 4, 8),
-    "claim": (2, 4, 8),
+    "select": (1, 2),
+    "rounds": (1, 2, 4),
 }
 
 
@@ -57,7 +57,11 @@ def workload_key(gpu: str, sm_count: int, n_reps: int, nodes: int, agents: int) 
     return f"{gpu}|{sm_count}|reps{p2(n_reps)}|nodes{p2(nodes)}|agents{p2(agents)}"
 
 
-def candidates(sm_count: int, default: int, multiples, limit: int):
+def candidates(sm_count: int, default: int, multiples, limit):
+    """Multiples of the SM count and the default, at most ``limit`` (None:
+    the default is the largest)."""
+    if limit is None:
+        limit = default
     out = sorted({min(limit, max(1, m * sm_count)) for m in multiples} | {default})
     return out
 

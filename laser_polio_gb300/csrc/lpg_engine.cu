@@ -38,9 +38,8 @@ static bool kernel_needed(int k, uint8_t need) {
 }
 
 const char* kKernelNames[] = {"k_begin", "k_newborns", "k_due", "k_sweep_a", "k_seed",
-                              "k_sweep_b", "k_evb", "k_node_tx", "k_sel_locate", "k_sel_claim",
-                              "k_sel_rounds"};
-constexpr int kNumTickKernels = 11; /* k_sel_rounds ends the tick (results rows, next tick's setup) */
+                              "k_sweep_b", "k_evb", "k_node_tx", "k_sel_round0", "k_sel_rounds"};
+constexpr int kNumTickKernels = 10; /* k_sel_rounds ends the tick (results rows, next tick's setup) */
 constexpr int kTicksPerGraph = 8;
 
 /* Reference-ordered columns of one simulation on the device. */
@@ -83,6 +82,7 @@ struct lpg_handle {
   bool use_graphs = true;
   int32_t test_stall_after = -1; /* lpg_test_stall_sweep */
   int64_t test_wait_spin = 0;
+  int32_t test_bar_skip = 0;     /* lpg_test_stall_round0 */
   std::map<uint32_t, std::pair<cudaGraphExec_t, int>> graphs; /* by the needs of 8 ticks: graph, launches */
   bool graph_failed = false;
   std::vector<uint8_t> tick_need; /* per tick: the optional kernels some simulation needs (NEED_*) */
@@ -96,8 +96,9 @@ struct lpg_handle {
   int sweep_blocks = 0;  /* k_sweep_rs (staged through shared memory) */
   int sweep0_blocks = 0; /* k_sweep_due (direct loads, no staging) */
   int due_blocks = 0;    /* k_due */
-  int select_blocks = 0; /* k_sel_locate, k_sel_rounds */
-  int claim_blocks = 0;
+  int select_blocks = 0; /* k_sel_round0 (cooperative: at most round0_max) */
+  int round0_max = 0;    /* CTAs of k_sel_round0 that fit on the GPU at once */
+  int rounds_blocks = 0; /* k_sel_rounds */
   int evb_blocks = 0;
   int newborn_blocks = 0; /* per replicate */
 };
@@ -585,6 +586,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   W.total_chunks = chunk_total;
   W.stall_after = h->test_stall_after;
   W.wait_spin = h->test_wait_spin > 0 ? h->test_wait_spin : LPG_MBAR_SPIN;
+  W.test_bar_skip = h->test_bar_skip;
   const int64_t P = (int64_t)chunk_total * LPG_CHUNK;
   int rc = 0;
   rc |= dalloc(h, &W.ds, P);
@@ -645,6 +647,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.hits, hits);
   rc |= dalloc(h, &W.ctr, LPG_NUM_COUNTERS);
   rc |= dalloc(h, &W.end_done, 1);
+  rc |= dalloc(h, &W.grid_bar, 1);
   rc |= dalloc(h, &W.reps, R);
   if (rc) return LPG_ERR_NOMEM;
   CK(cudaMemsetAsync(W.ds, 0xff, P, st));
@@ -660,6 +663,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaMemsetAsync(W.uniq, 0, sizeof(int64_t) * G, st));
   CK(cudaMemsetAsync(W.ctr, 0, sizeof(unsigned long long) * LPG_NUM_COUNTERS, st));
   CK(cudaMemsetAsync(W.end_done, 0, 4, st));
+  CK(cudaMemsetAsync(W.grid_bar, 0, 8, st));
 
   /* 4. per-simulation static data, results, pools, chunk tables */
   std::vector<int4> h_meta(chunk_total, make_int4(-1, 0, -1, 0));
@@ -940,11 +944,13 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_due, 256, 0));
   h->due_blocks = std::max(1, occ) * h->sm_count;
   occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sel_locate, 256, 0));
-  h->select_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sel_round0, 256, 0));
+  if (occ < 1) return fail(h, LPG_ERR_CUDA, "k_sel_round0 does not fit on an SM");
+  h->round0_max = occ * h->sm_count;
+  h->select_blocks = h->round0_max;
   occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sel_claim, 256, 0));
-  h->claim_blocks = std::min(2048, std::max(1, occ) * h->sm_count);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sel_rounds, 256, 0));
+  h->rounds_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
   h->evb_blocks = h->sm_count * 8;
   h->newborn_blocks = h->sm_count * 8;
   h->next_tick = 1; /* tick 0 ran above (k_end); the components run from tick 1 */
@@ -972,9 +978,13 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 5: k_sweep_rs<<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
     case 6: k_evb<<<h->evb_blocks, 256, 0, st>>>(W, h->sweep_blocks); break;
     case 7: k_node_tx<<<G, LPG_NODE_TX_THREADS, 0, st>>>(W); break;
-    case 8: k_sel_locate<<<h->select_blocks, 256, 0, st>>>(W); break;
-    case 9: k_sel_claim<<<h->claim_blocks, 256, 0, st>>>(W); break;
-    case 10: k_sel_rounds<<<h->select_blocks, 256, 0, st>>>(W); break;
+    case 8: {
+      /* cooperative: its CTAs meet at a grid barrier, so all must be resident */
+      void* args[] = {&W};
+      CK(cudaLaunchCooperativeKernel((const void*)k_sel_round0, dim3(h->select_blocks), dim3(256), args, 0, st));
+      break;
+    }
+    case 9: k_sel_rounds<<<h->rounds_blocks, 256, 0, st>>>(W); break;
   }
   CK(cudaGetLastError());
   if (timed) CK(cudaEventRecord(e1, st));
@@ -1250,8 +1260,8 @@ static int* launch_slot(lpg_handle* h, int32_t which, int* limit) {
     case LPG_LAUNCH_SWEEP_DUE: *limit = 1024; return &h->sweep0_blocks;
     case LPG_LAUNCH_SWEEP_RS: *limit = 1024; return &h->sweep_blocks;
     case LPG_LAUNCH_EVB: *limit = 8192; return &h->evb_blocks;
-    case LPG_LAUNCH_SELECT: *limit = 8192; return &h->select_blocks;
-    case LPG_LAUNCH_CLAIM: *limit = 8192; return &h->claim_blocks;
+    case LPG_LAUNCH_SELECT: *limit = h->round0_max; return &h->select_blocks;
+    case LPG_LAUNCH_ROUNDS: *limit = 1024; return &h->rounds_blocks;
     case LPG_LAUNCH_NEWBORNS: *limit = 8192; return &h->newborn_blocks;
     default: return nullptr;
   }
@@ -1268,6 +1278,11 @@ extern "C" int lpg_set_launch(lpg_handle* h, int32_t which, int32_t blocks) {
     *slot = blocks;
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second.first);
     h->graphs.clear();
+    /* the grid barrier's count is kept a multiple of the grid size */
+    if (which == LPG_LAUNCH_SELECT) {
+      CK(cudaSetDevice(h->device));
+      CK(cudaMemsetAsync(h->W.grid_bar, 0, sizeof(unsigned long long), h->stream));
+    }
   }
   return LPG_OK;
 }
@@ -1289,6 +1304,18 @@ extern "C" int lpg_test_stall_sweep(lpg_handle* h, int32_t stages, int64_t wait_
   h->W.stall_after = h->test_stall_after;
   h->W.wait_spin = wait_spin > 0 ? wait_spin : LPG_MBAR_SPIN;
   /* graphs hold the kernels' arguments as captured: capture again */
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second.first);
+  h->graphs.clear();
+  return LPG_OK;
+}
+
+extern "C" int lpg_test_stall_round0(lpg_handle* h, int32_t skip, int64_t wait_spin) {
+  if (!h) return LPG_ERR_ARG;
+  if (wait_spin < 0 || wait_spin > LPG_MBAR_SPIN) return fail(h, LPG_ERR_ARG, "wait_spin %lld out of range", (long long)wait_spin);
+  h->test_bar_skip = skip != 0;
+  h->test_wait_spin = wait_spin;
+  h->W.test_bar_skip = h->test_bar_skip;
+  h->W.wait_spin = wait_spin > 0 ? wait_spin : LPG_MBAR_SPIN;
   for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second.first);
   h->graphs.clear();
   return LPG_OK;

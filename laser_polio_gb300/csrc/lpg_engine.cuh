@@ -217,6 +217,8 @@ typedef struct {
   uint32_t* due_n;   /* entries of due (k_due appends, k_end clears) */
   unsigned long long* ctr; /* [LPG_NUM_COUNTERS] work counters */
   uint32_t* end_done;      /* CTAs of k_end done with the tick (the last prepares the next) */
+  unsigned long long* grid_bar; /* arrivals at k_sel_round0's grid barrier (only grows) */
+  int32_t test_bar_skip;   /* test hook: CTA 0 of k_sel_round0 does not arrive at its barrier */
 } DevWorld;
 
 #endif

@@ -21,7 +21,7 @@
  *   k_node_tx    per node: population (model.py:1751-1755), mixing,
  *                seasonality, probabilities and exposure counts
  *                (model.py:1327-1407)
- *   k_sel_locate, k_sel_claim, k_sel_rounds   weighted selection rounds
+ *   k_sel_round0, k_sel_rounds               weighted selection rounds
  *                and strain assignment (tx_infect_nb, model.py:1010-1149);
  *                k_sel_rounds then ends the tick (end_tick): results rows
  *                (model.py:1461-1487 and the result writes of every
@@ -36,6 +36,14 @@
 
 #define FULLMASK 0xffffffffu
 #define LPG_NONE 0xffffffffu
+/* State byte of an agent claimed by a round-0 target of this tick while the
+ * round is still running: the round's other targets locate on the frozen
+ * CDF, so they still count it as susceptible; k_sel_round0 makes it exposed
+ * (1) after its grid barrier.  No other kernel sees it. */
+#define LPG_DS_CLAIMED 0x40u
+/* a state byte that carries selection weight: susceptible, or claimed in the
+ * running round 0 */
+__device__ __forceinline__ bool sel_open(uint32_t b) { return (b & ~LPG_DS_CLAIMED & 0xffu) == 0; }
 #define LPG_MAX_ROUNDS 1000000
 
 /* ------------------------------------------------------------------------ */
@@ -1638,7 +1646,7 @@ struct SelInfo {
   int32_t i;         /* node index in its simulation */
   int32_t t;         /* tick */
   int32_t ns;
-  int32_t pad;
+  int32_t csr;       /* which of the two chunk-list buffers holds the node's list */
 };
 
 /* Cumulative relative FOI that the strain draw compares against
@@ -1922,7 +1930,7 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
     N.i = i;
     N.t = t;
     N.ns = ns;
-    N.pad = 0;
+    N.csr = rp->csr_cur;
     reinterpret_cast<SelInfo*>(W.sel_info)[g] = N;
     W.ksel[g] = size;
   }
@@ -1961,7 +1969,7 @@ __device__ __forceinline__ uint32_t locate_in_chunk(const DevWorld& W, int64_t c
       for (int k = 0; k < 32; ++k) {
         if (hit != LPG_NONE) break;
         const uint32_t sbyte = (sw32[k >> 2] >> (8 * (k & 3))) & 0xffu;
-        if (sbyte != 0) continue;
+        if (!sel_open(sbyte)) continue;
         const uint64_t w = fix_risk(reinterpret_cast<const float*>(rv)[k]);
         if (w > v) hit = (uint32_t)(p0 + grp * 32 + k);
         else v -= w;
@@ -2013,128 +2021,220 @@ __device__ __forceinline__ uint64_t team_incl_scan(const Team& tm, uint64_t x) {
   return x;
 }
 
-/* locate() by a team: the same answer, with a (T+1)-ary search of the chunk
- * prefix and, for T >= 4, the sub-block totals and the 128 slots split over
- * the lanes (each lane a contiguous run; a team scan finds the lane that
- * holds the target).  Every lane of the team returns the hit.  All 32 lanes
- * of the warp call it together (teams without a target pass active = false)
- * so that the warp reconverges between the stages: teams that diverged in
- * the search would otherwise run the later stages one team at a time. */
-__device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& tm, const int32_t* ls,
-                                                const uint64_t* cp, int32_t n, uint64_t v, uint64_t base,
-                                                bool active = true) {
-  const int T = tm.T;
+/* Probe l of a (T+1)-ary search of [lo, lo + m): lo + (l + 1) m / (T + 1).
+ * In 32 bits: m is below 2^21 (chunks of a node, or nodes of a batch) and
+ * l + 1 at most 32; with T a constant the division is a multiply. */
+template <int T>
+__device__ __forceinline__ int32_t team_probe(int32_t lo, int32_t m, int l) {
+  return lo + (int32_t)(((uint32_t)(l + 1) * (uint32_t)m) / (uint32_t)(T + 1));
+}
+
+/* locate() by a team of T lanes: the same answer, with a (T+1)-ary search
+ * of the chunk prefix and, for T >= 4, the sub-block totals and the 128
+ * slots split over the lanes (each lane a contiguous run; a team scan finds
+ * the lane that holds the target).  Every lane of the team returns the hit.
+ * All 32 lanes of the warp call it together (teams without a target pass
+ * active = false) so that the warp reconverges between the stages: teams
+ * that diverged in the search would otherwise run the later stages one team
+ * at a time.  Each probe of the search requests the chunk id beside the
+ * prefix, and the team keeps the values at the bounds (the prefix below lo,
+ * the chunk at hi), so that the chunk and the target's offset in it are
+ * known when the search ends, without further loads.  word_out / risk_out
+ * (when given) receive the hit slot's state word (4 state bytes) and risk as
+ * read.  T is a template constant, so that every loop below has its exact
+ * trip count and no dead iterations (the kernels run once a tick and fetch
+ * their instructions cold: code that is not there costs nothing). */
+template <int T>
+__device__ __forceinline__ uint32_t locate_team_t(const DevWorld& W, const int32_t* ls, const uint64_t* cp,
+                                                  int32_t n, uint64_t v, uint64_t base, bool active,
+                                                  uint32_t* word_out, float* risk_out) {
+  const Team tm = make_team(T);
   int32_t lo = 0, hi = active ? n - 1 : 0;
+  uint64_t cp_lo = base;                    /* cp[lo - 1] (base while lo = 0) */
+  int32_t ls_hi = active ? ls[hi] : 0;      /* ls[hi] */
   while (lo < hi) {
     const int32_t m = hi - lo;
-    const int32_t p = lo + (int32_t)(((int64_t)(tm.l + 1) * m) / (T + 1));
-    const unsigned b = team_ballot(tm, cp[p] - base > v);
+    const int32_t p = team_probe<T>(lo, m, tm.l);
+    const uint64_t cpp = cp[p];
+    const int32_t lsp = ls[p];
+    const unsigned b = team_ballot(tm, cpp - base > v);
     const int c = __ffs(b) - 1; /* first probe above v; probes ascend with the lane */
+    const uint64_t cp_below = __shfl_sync(tm.mask, cpp, c < 0 ? T - 1 : (c > 0 ? c - 1 : 0), T);
+    const int32_t ls_c = __shfl_sync(tm.mask, lsp, c < 0 ? 0 : c, T);
+    const int32_t lo0 = lo;
     if (c < 0) {
-      lo = lo + (int32_t)(((int64_t)T * m) / (T + 1)) + 1;
+      lo = team_probe<T>(lo0, m, T - 1) + 1;
+      cp_lo = cp_below;
     } else {
-      const int32_t pc = lo + (int32_t)(((int64_t)(c + 1) * m) / (T + 1));
-      if (c > 0) lo = lo + (int32_t)(((int64_t)c * m) / (T + 1)) + 1;
-      hi = pc;
+      if (c > 0) {
+        lo = team_probe<T>(lo0, m, c - 1) + 1;
+        cp_lo = cp_below;
+      }
+      hi = team_probe<T>(lo0, m, c);
+      ls_hi = ls_c;
     }
   }
   __syncwarp();
   uint32_t hit = LPG_NONE;
   int64_t cid = 0;
   if (active) {
-    if (lo > 0) v -= cp[lo - 1] - base;
-    cid = ls[lo];
+    if (lo > 0) v -= cp_lo - base;
+    cid = ls_hi;
   }
-  if (T < 4) {
+  if constexpr (T < 4) {
     if (active && tm.l == 0) hit = locate_in_chunk(W, cid, v);
     __syncwarp();
-    return active ? __shfl_sync(tm.mask, hit, 0, T) : LPG_NONE;
-  }
-  /* sub-block: lanes l < min(T, 16) hold 16 / min(T, 16) consecutive totals */
-  const int TS = T < LPG_NSUB ? T : LPG_NSUB;
-  const int per = LPG_NSUB / TS;
-  int sb = -1;
-  uint64_t vl = 0;
-  if (active) {
-    uint64_t sw[LPG_NSUB];
-    uint64_t sum = 0;
+    hit = active ? __shfl_sync(tm.mask, hit, 0, T) : LPG_NONE;
+    if (word_out && hit != LPG_NONE) {
+      *word_out = __ldcg(reinterpret_cast<const uint32_t*>(W.ds + ((int64_t)hit & ~3LL)));
+      *risk_out = W.risk[hit];
+    }
+    return hit;
+  } else {
+    /* sub-block: lanes l < min(T, 16) hold 16 / min(T, 16) consecutive totals */
+    constexpr int TS = T < LPG_NSUB ? T : LPG_NSUB;
+    constexpr int PER = LPG_NSUB / TS;
+    int sb = -1;
+    uint64_t vl = 0;
+    if (active) {
+      uint64_t sw[PER];
+      uint64_t sum = 0;
 #pragma unroll
-    for (int k = 0; k < LPG_NSUB; ++k) {
-      sw[k] = 0;
-      if (k < per && tm.l < TS) {
-        sw[k] = __ldcg(&W.sub_w[cid * LPG_NSUB + tm.l * per + k]);
+      for (int k = 0; k < PER; ++k) {
+        sw[k] = tm.l < TS ? __ldcg(&W.sub_w[cid * LPG_NSUB + tm.l * PER + k]) : 0;
         sum += sw[k];
       }
-    }
-    const uint64_t incl = team_incl_scan(tm, sum);
-    const uint64_t excl = incl - sum;
-    const unsigned own = team_ballot(tm, sum > 0 && excl <= v && v < incl);
-    if (own != 0) {
-      const int ol = __ffs(own) - 1;
-      vl = v - excl;
-      if (tm.l == ol) {
+      const uint64_t incl = team_incl_scan(tm, sum);
+      const uint64_t excl = incl - sum;
+      const unsigned own = team_ballot(tm, sum > 0 && excl <= v && v < incl);
+      if (own != 0) {
+        const int ol = __ffs(own) - 1;
+        vl = v - excl;
+        if (tm.l == ol) {
 #pragma unroll
-        for (int k = 0; k < LPG_NSUB; ++k) {
-          if (sb < 0 && k < per) {
-            if (sw[k] > vl) sb = tm.l * per + k;
-            else vl -= sw[k];
+          for (int k = 0; k < PER; ++k) {
+            if (sb < 0) {
+              if (sw[k] > vl) sb = tm.l * PER + k;
+              else vl -= sw[k];
+            }
           }
         }
+        sb = __shfl_sync(tm.mask, sb, ol, T);
+        vl = __shfl_sync(tm.mask, vl, ol, T);
       }
-      sb = __shfl_sync(tm.mask, sb, ol, T);
-      vl = __shfl_sync(tm.mask, vl, ol, T);
     }
-  }
-  __syncwarp();
-  /* slots: lane l holds L = 128 / T consecutive slots */
-  const bool go = active && sb >= 0;
-  const int L = LPG_SUB / T;
-  const int64_t s0 = go ? cid * LPG_CHUNK + (int64_t)sb * LPG_SUB + (int64_t)tm.l * L : 0;
-  uint32_t dw[8];
-  float4 rv[8];
+    __syncwarp();
+    /* slots: lane l holds L = 128 / T consecutive slots (L / 4 state words) */
+    constexpr int L = LPG_SUB / T;
+    const bool go = active && sb >= 0;
+    const int64_t s0 = go ? cid * LPG_CHUNK + (int64_t)sb * LPG_SUB + (int64_t)tm.l * L : 0;
+    uint32_t dw[L / 4];
+    float4 rv[L / 4];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    if (go && k < L / 4) {
-      dw[k] = __ldcg(reinterpret_cast<const uint32_t*>(W.ds + s0) + k);
-      rv[k] = reinterpret_cast<const float4*>(W.risk + s0)[k];
-    } else {
-      dw[k] = 0xffffffffu;
-      rv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = 0; k < L / 4; ++k) {
+      if (go) {
+        dw[k] = __ldcg(reinterpret_cast<const uint32_t*>(W.ds + s0) + k);
+        rv[k] = reinterpret_cast<const float4*>(W.risk + s0)[k];
+      } else {
+        dw[k] = 0xffffffffu;
+        rv[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
     }
-  }
-  uint64_t wsum = 0;
+    uint64_t wsum = 0;
 #pragma unroll
-  for (int k = 0; k < 32; ++k) {
-    if (k < L && ((dw[k >> 2] >> (8 * (k & 3))) & 0xffu) == 0)
-      wsum += fix_risk(reinterpret_cast<const float*>(rv)[k]);
-  }
-  if (go) {
-    const uint64_t incl = team_incl_scan(tm, wsum);
-    const uint64_t excl = incl - wsum;
-    const unsigned own = team_ballot(tm, wsum > 0 && excl <= vl && vl < incl);
-    if (own != 0) {
-      const int ol = __ffs(own) - 1;
-      if (tm.l == ol) {
-        uint64_t r = vl - excl;
+    for (int k = 0; k < L; ++k)
+      if (sel_open((dw[k >> 2] >> (8 * (k & 3))) & 0xffu)) wsum += fix_risk(reinterpret_cast<const float*>(rv)[k]);
+    if (go) {
+      const uint64_t incl = team_incl_scan(tm, wsum);
+      const uint64_t excl = incl - wsum;
+      const unsigned own = team_ballot(tm, wsum > 0 && excl <= vl && vl < incl);
+      if (own != 0) {
+        const int ol = __ffs(own) - 1;
+        uint32_t word = 0;
+        float rk = 0.f;
+        if (tm.l == ol) {
+          uint64_t r = vl - excl;
 #pragma unroll
-        for (int k = 0; k < 32; ++k) {
-          if (hit == LPG_NONE && k < L && ((dw[k >> 2] >> (8 * (k & 3))) & 0xffu) == 0) {
-            const uint64_t w = fix_risk(reinterpret_cast<const float*>(rv)[k]);
-            if (w > r) hit = (uint32_t)(s0 + k);
-            else r -= w;
+          for (int k = 0; k < L; ++k) {
+            if (hit == LPG_NONE && sel_open((dw[k >> 2] >> (8 * (k & 3))) & 0xffu)) {
+              const uint64_t w = fix_risk(reinterpret_cast<const float*>(rv)[k]);
+              if (w > r) {
+                hit = (uint32_t)(s0 + k);
+                word = dw[k >> 2];
+                rk = reinterpret_cast<const float*>(rv)[k];
+              } else {
+                r -= w;
+              }
+            }
           }
         }
+        hit = __shfl_sync(tm.mask, hit, ol, T);
+        if (word_out) {
+          *word_out = __shfl_sync(tm.mask, word, ol, T);
+          *risk_out = __shfl_sync(tm.mask, rk, ol, T);
+        }
       }
-      hit = __shfl_sync(tm.mask, hit, ol, T);
     }
+    __syncwarp();
+    return hit;
   }
-  __syncwarp();
-  return hit;
 }
 
-/* The first target to claim an agent (state 0 -> 1) exposes it: strain by
- * relative FOI (model.py:1127-1145) and every susceptible total.  Returns
- * whether this target claimed it (and the weight it removed in *w_out). */
+/* locate_team_t for a team size known only at run time (uniform in the
+ * warp). */
+__device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& tm, const int32_t* ls,
+                                                const uint64_t* cp, int32_t n, uint64_t v, uint64_t base,
+                                                bool active = true, uint32_t* word_out = nullptr,
+                                                float* risk_out = nullptr) {
+  switch (tm.T) {
+    case 32: return locate_team_t<32>(W, ls, cp, n, v, base, active, word_out, risk_out);
+    case 16: return locate_team_t<16>(W, ls, cp, n, v, base, active, word_out, risk_out);
+    case 8: return locate_team_t<8>(W, ls, cp, n, v, base, active, word_out, risk_out);
+    case 4: return locate_team_t<4>(W, ls, cp, n, v, base, active, word_out, risk_out);
+    case 2: return locate_team_t<2>(W, ls, cp, n, v, base, active, word_out, risk_out);
+    default: return locate_team_t<1>(W, ls, cp, n, v, base, active, word_out, risk_out);
+  }
+}
+
+/* The exposure of an agent that a target has claimed: strain by relative
+ * FOI (model.py:1127-1145), its first step in E, and every susceptible total
+ * but the sub-block's (sub_now: that one too).  Returns its weight. */
+__device__ __forceinline__ uint64_t expose_claimed(DevWorld& W, int64_t pos, int g, const SelInfo& N, double r,
+                                                   int8_t et, float risk, bool sub_now) {
+  const int G = W.G;
+  const int64_t cid = pos / LPG_CHUNK;
+  int s = 0;
+  bool found = false;
+#pragma unroll
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k)
+    if (!found && k < N.ns && r < N.cum[k]) {
+      s = k;
+      found = true;
+    }
+  W.strain[pos] = (int8_t)s;
+  {
+    /* first step in E is at t + 1 (model.py:393-454) */
+    const int32_t e1 = N.t + 1 + (et > 0 ? et : 0);
+    W.evt[pos] = e1;
+    atomicMin(&W.sub_evt[pos >> 7], e1);
+  }
+  const uint64_t w = fix_risk(risk);
+  atomicAdd(&W.tot[(int64_t)TT_S * G + g], -1);
+  atomicAdd(&W.tot[(int64_t)(TT_E0 + s) * G + g], 1);
+  atomicAdd(&W.ev[(int64_t)(EV_TXNEW0 + s) * G + g], 1);
+  atomicAdd((unsigned long long*)&W.uniq[g], 1ULL);
+  if (w) {
+    atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
+    atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
+    if (sub_now) atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
+  }
+  return w;
+}
+
+/* The first target to claim an agent (state 0 -> 1) exposes it (rounds
+ * after the first, whose claims follow all of the round's locates).
+ * Returns whether this target claimed it (and the weight it removed in
+ * *w_out). */
 __device__ __forceinline__ bool claim(DevWorld& W, uint32_t hit, int g, const SelInfo& N, uint64_t* w_out = nullptr) {
   const int64_t pos = hit;
   /* the agent's fixed columns requested first, and its strain draw formed
@@ -2157,60 +2257,190 @@ __device__ __forceinline__ bool claim(DevWorld& W, uint32_t hit, int g, const Se
     old = prev;
   }
   if (!won) return false;
-  const int G = W.G;
-  const int64_t cid = pos / LPG_CHUNK;
-  int s = 0;
-  for (int k = 0; k < N.ns; ++k)
-    if (r < N.cum[k]) {
-      s = k;
-      break;
-    }
-  W.strain[pos] = (int8_t)s;
-  {
-    /* first step in E is at t + 1 (model.py:393-454) */
-    const int32_t e1 = N.t + 1 + (et > 0 ? et : 0);
-    W.evt[pos] = e1;
-    atomicMin(&W.sub_evt[pos >> 7], e1);
-  }
-  const uint64_t w = fix_risk(risk);
-  atomicAdd(&W.tot[(int64_t)TT_S * G + g], -1);
-  atomicAdd(&W.tot[(int64_t)(TT_E0 + s) * G + g], 1);
-  atomicAdd(&W.ev[(int64_t)(EV_TXNEW0 + s) * G + g], 1);
-  atomicAdd((unsigned long long*)&W.uniq[g], 1ULL);
-  if (w) {
-    atomicAdd((unsigned long long*)&W.sw[g], neg64(w));
-    atomicAdd((unsigned long long*)&W.chunk_w[cid], neg64(w));
-    atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
-  }
+  const uint64_t w = expose_claimed(W, pos, g, N, r, et, risk, true);
   if (w_out) *w_out = w;
   return true;
 }
 
-/* Node of target q: the last g with off[g] <= q. */
-__device__ __forceinline__ int sel_node_of(const int64_t* off, int G, int64_t q) {
-  int lo = 0, hi = G;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (off[mid] > q) hi = mid; else lo = mid + 1;
+/* A round-0 claim, made as soon as the target is located: state 0 ->
+ * LPG_DS_CLAIMED (the round's other targets still see the agent's weight),
+ * the exposure and every total but the sub-block weight, which the claimer
+ * removes after the round (claim0_finish).  word and risk are the slot's
+ * state word and risk as the locate read them (the word is the first guess
+ * of the compare-and-swap). */
+__device__ __forceinline__ bool claim0(DevWorld& W, uint32_t hit, uint32_t word, float risk, int g,
+                                       const SelInfo& N, uint64_t* w_out) {
+  const int64_t pos = hit;
+  const uint32_t ref = W.ref[pos];
+  const int8_t et = W.et[pos];
+  uint32_t* wp = reinterpret_cast<uint32_t*>(W.ds + (pos & ~3LL));
+  const int sh = (int)(pos & 3) * 8;
+  uint32_t old = word;
+  const double r = lpg_u01(N.seed, LPG_P_STRAIN, N.t, ref, 0, 0);
+  bool won = false;
+  while (((old >> sh) & 0xffu) == 0) {
+    const uint32_t nw = (old & ~(0xffu << sh)) | (LPG_DS_CLAIMED << sh);
+    const uint32_t prev = atomicCAS(wp, old, nw);
+    if (prev == old) {
+      won = true;
+      break;
+    }
+    old = prev;
   }
-  return lo - 1;
+  if (!won) return false;
+  *w_out = expose_claimed(W, pos, g, N, r, et, risk, false);
+  return true;
+}
+
+/* After round 0: the claimed agent becomes exposed (state 1) and leaves its
+ * sub-block's weight. */
+__device__ __forceinline__ void claim0_finish(DevWorld& W, uint32_t hit, uint64_t w) {
+  if (hit == LPG_NONE) return;
+  const int64_t pos = hit;
+  W.ds[pos] = 1;
+  if (w) {
+    const int64_t cid = pos / LPG_CHUNK;
+    atomicAdd((unsigned long long*)&W.sub_w[cid * LPG_NSUB + (pos % LPG_CHUNK) / LPG_SUB], neg64(w));
+  }
+}
+
+/* Grid-wide barrier of a cooperative launch (every CTA resident), on a
+ * counter that only grows: thread 0 of each CTA adds 1 and polls until the
+ * count reaches the next multiple of the grid size, at most `limit` times.
+ * Every barrier adds exactly one per CTA, so the count is a multiple of the
+ * grid size whenever none is open (the host clears it when the grid size
+ * changes).  Returns false (in every thread of the CTA) when the poll ran
+ * out. */
+__device__ bool grid_sync(unsigned long long* ctr, long long limit, bool skip_arrive = false) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    if (skip_arrive) {
+      ok = 0;
+    } else {
+      __threadfence();
+      const unsigned long long old = atomicAdd(ctr, 1ULL);
+      const unsigned long long target = (old / gridDim.x + 1) * gridDim.x;
+      const volatile unsigned long long* vc = ctr;
+      long long it = 0;
+      while (*vc < target) {
+        if (++it > limit) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+      __threadfence();
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+/* First g in [lo, hi] with off[g] > q (the answer is known to be <= hi), by
+ * a (T+1)-ary search of the team over off (shared memory). */
+template <int T>
+__device__ __forceinline__ int team_first_above(const Team& tm, const int64_t* off, int lo, int hi, int64_t q) {
+  while (lo < hi) {
+    const int m = hi - lo;
+    const unsigned b = team_ballot(tm, off[team_probe<T>(lo, m, tm.l)] > q);
+    const int c = __ffs(b) - 1;
+    const int lo0 = lo;
+    if (c < 0) {
+      lo = team_probe<T>(lo0, m, T - 1) + 1;
+    } else {
+      if (c > 0) lo = team_probe<T>(lo0, m, c - 1) + 1;
+      hi = team_probe<T>(lo0, m, c);
+    }
+  }
+  return lo;
+}
+
+/* Round 0's targets for a team size T: each located on the frozen CDF and
+ * claimed at once by the team's first lane, which keeps its first two
+ * claims in registers and stores later ones' slots in hits[q]; then the
+ * grid barrier, after which the claimers settle their agents (state 1,
+ * sub-block weight).  Returns false when the barrier's wait ran out. */
+template <int T>
+__device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs, const SelInfo* info, int64_t K) {
+  const int G = W.G;
+  const Team tm = make_team(T);
+  const int64_t nteams = ((int64_t)gridDim.x * blockDim.x) / T;
+  const int64_t q0 = (int64_t)(threadIdx.x / T) * gridDim.x + blockIdx.x;
+  uint32_t h0 = LPG_NONE, h1 = LPG_NONE;
+  uint64_t w0 = 0, w1 = 0;
+  int it = 0;
+  /* warp-uniform trip count: every lane stays until no team of its warp has a target */
+  for (int64_t q = q0; __any_sync(FULLMASK, q < K); q += nteams, ++it) {
+    const bool act = q < K;
+    SelInfo N;
+    uint64_t v = 0;
+    const int32_t* ls = W.node_chunks[0];
+    /* the node of target q: the last g with offs[g] <= q */
+    const int g = team_first_above<T>(tm, offs, 0, act ? G : 0, q) - 1;
+    if (act) {
+      N = info[g];
+      const int64_t j = q - offs[g];
+      v = lpg_scale_target(lpg_u53(N.seed, LPG_P_SELECT, N.t, (uint64_t)N.i, 0, (uint64_t)j), N.T);
+      ls = W.node_chunks[N.csr] + N.a;
+    } else {
+      N.a = 0;
+      N.n = 1;
+    }
+    uint32_t word = 0;
+    float rk = 0.f;
+    const uint32_t hit = locate_team_t<T>(W, ls, W.cpref + N.a, N.n, v, 0, act, &word, &rk);
+    if (act && tm.l == 0) {
+      uint32_t won_at = LPG_NONE;
+      uint64_t w = 0;
+      if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
+      else if (claim0(W, hit, word, rk, g, N, &w)) won_at = hit;
+      if (it == 0) {
+        h0 = won_at;
+        w0 = w;
+      } else if (it == 1) {
+        h1 = won_at;
+        w1 = w;
+      } else {
+        W.hits[q] = won_at;
+      }
+    }
+  }
+  /* every target of the round located and claimed: the claimed agents
+   * become exposed and leave their sub-blocks' weights */
+  if (!grid_sync(W.grid_bar, W.wait_spin, W.test_bar_skip && blockIdx.x == 0)) return false;
+  if (tm.l == 0) {
+    claim0_finish(W, h0, w0);
+    claim0_finish(W, h1, w1);
+    for (int64_t q = q0 + 2 * nteams; q < K; q += nteams) {
+      const uint32_t h = W.hits[q];
+      if (h != LPG_NONE) claim0_finish(W, h, fix_risk(W.risk[h]));
+    }
+  }
+  return true;
 }
 
 /* Weighted selection without replacement (tx_infect_nb, model.py:1066-1147),
- * in three kernels.  k_node_tx has left, per node with demand, its round-0
+ * in two kernels.  k_node_tx has left, per node with demand, its round-0
  * target count (ksel), its selection record and its node-local chunk
- * prefix.  Round 0 runs over all nodes at once: k_sel_locate forms the
- * target offsets in every CTA's shared memory and locates every target;
- * k_sel_claim claims them, targets going round-robin over the CTAs.  The
- * few collisions left after round 0 are redrawn per node by one CTA in
- * later rounds (k_sel_rounds), with CTA barriers only.  Round r of node n
- * draws the (n, r, j) uniforms of the oracle, so the CDF targets are the
- * same whatever runs them. */
-__global__ void __launch_bounds__(256) k_sel_locate(DevWorld W) {
+ * prefix.  Round 0 runs over all nodes at once in one cooperative launch
+ * (k_sel_round0): every CTA forms the target offsets in its shared memory;
+ * targets go round-robin over the CTAs, each located by a team of lanes on
+ * the round's frozen CDF and claimed at once (claim0: the agent keeps its
+ * weight for the round's other targets); after a grid barrier the claimers
+ * settle the sub-block weights.  The few collisions left after round 0 are
+ * redrawn per node by one CTA in later rounds (k_sel_rounds), with CTA
+ * barriers only.  Round r of node n draws the (n, r, j) uniforms of the
+ * oracle, so the CDF targets are the same whatever runs them, and which of
+ * two targets on one agent claims it changes nothing (its strain draw is
+ * keyed by the agent). */
+__global__ void __launch_bounds__(256) k_sel_round0(DevWorld W) {
   const int R = W.n_reps, G = W.G;
   int any = 0;
   for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
-  if (!any) return;
+  if (!any) return; /* the same answer in every CTA: none waits at the barrier */
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
   const SelInfo* info = reinterpret_cast<const SelInfo*>(W.sel_info);
@@ -2218,10 +2448,9 @@ __global__ void __launch_bounds__(256) k_sel_locate(DevWorld W) {
   __shared__ int64_t s_off[LPG_SEL_OFFS];
   const bool offs_in_smem = G < LPG_SEL_OFFS;
 
-  /* ---- round 0, all nodes ---- */
+  /* target offsets of all nodes; every CTA computes the same values and
+   * keeps them in shared memory when they fit */
   {
-    /* target offsets of all nodes; every CTA computes the same values and
-     * keeps them in shared memory when they fit */
     int64_t carry = 0;
     for (int base = 0; base < G; base += 4 * blockDim.x) {
       /* 4 consecutive nodes a thread: one block scan per 4 * blockDim nodes */
@@ -2238,7 +2467,7 @@ __global__ void __launch_bounds__(256) k_sel_locate(DevWorld W) {
       for (int u = 0; u < 4; ++u) {
         if (g0 + u < G) {
           if (offs_in_smem) s_off[g0 + u] = run;
-          if (!offs_in_smem || blockIdx.x == 0) W.tgt_off[g0 + u] = run; /* for the claims */
+          if (!offs_in_smem || blockIdx.x == 0) W.tgt_off[g0 + u] = run;
         }
         run += k[u];
       }
@@ -2252,70 +2481,33 @@ __global__ void __launch_bounds__(256) k_sel_locate(DevWorld W) {
     __syncthreads();
   }
   const int64_t K = s_K;
-  if (K > W.hits_cap) {
+  if (K > W.hits_cap) { /* the same in every CTA */
     if (gtid == 0) W.reps[0].error = LPG_ERR_INTERNAL;
     return;
   }
   if (gtid == 0 && K) atomicAdd(&W.ctr[LPG_CTR_SEL_TARGETS], (unsigned long long)K);
+  /* (when the offsets do not fit in shared memory, every CTA has written
+   * all of them to tgt_off itself, so it reads its own values back) */
   const int64_t* offs = offs_in_smem ? s_off : W.tgt_off;
   /* Targets go round-robin over the CTAs (target q on CTA q mod grid), so
    * that a few thousand of them still use every SM, each located by a team
-   * of T lanes: the largest power of two <= 32 with T * K <= threads. */
-  {
-    int T = 1;
-    while (T < 32 && (int64_t)(2 * T) * K <= gsz) T *= 2;
-    const Team tm = make_team(T);
-    const int64_t nteams = gsz / T;
-    /* warp-uniform trip count: every lane stays until no team of its warp has a target */
-    for (int64_t q = (int64_t)(threadIdx.x / T) * gridDim.x + blockIdx.x; __any_sync(FULLMASK, q < K); q += nteams) {
-      const bool act = q < K;
-      int g = 0;
-      SelInfo N;
-      uint64_t v = 0;
-      const int32_t* ls = W.node_chunks[0];
-      if (act) {
-        g = sel_node_of(offs, G, q);
-        N = info[g];
-        const int64_t j = q - offs[g];
-        v = lpg_scale_target(lpg_u53(N.seed, LPG_P_SELECT, N.t, (uint64_t)N.i, 0, (uint64_t)j), N.T);
-        ls = W.node_chunks[W.reps[W.node_rep[g]].csr_cur] + N.a;
-      } else {
-        N.a = 0;
-        N.n = 1;
-      }
-      const uint32_t hit = locate_team(W, tm, ls, W.cpref + N.a, N.n, v, 0, act);
-      if (act && tm.l == 0) {
-        if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
-        W.hits[q] = hit;
-      }
-    }
+   * of T lanes: the largest power of two <= 32 with T * K <= threads, and
+   * at least 8 (more targets than teams: each team takes several in turn;
+   * smaller teams would hold more slots a lane than the registers of two
+   * CTAs an SM allow). */
+  int T = 8;
+  while (T < 32 && (int64_t)(2 * T) * K <= gsz) T *= 2;
+  bool ok;
+  switch (T) {
+    case 32: ok = round0_targets<32>(W, offs, info, K); break;
+    case 16: ok = round0_targets<16>(W, offs, info, K); break;
+    default: ok = round0_targets<8>(W, offs, info, K); break;
   }
-}
-
-/* Round 0 claims (after every target of round 0 has been located): the
- * first target to reach an agent exposes it. */
-__global__ void __launch_bounds__(256) k_sel_claim(DevWorld W) {
-  const int R = W.n_reps, G = W.G;
-  int any = 0;
-  for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
-  if (!any) return;
-  const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
-  const SelInfo* info = reinterpret_cast<const SelInfo*>(W.sel_info);
-  __shared__ int64_t s_off[LPG_SEL_OFFS];
-  const bool offs_in_smem = G < LPG_SEL_OFFS;
-  if (offs_in_smem) {
-    for (int g = threadIdx.x; g <= G; g += blockDim.x) s_off[g] = __ldcg(&W.tgt_off[g]);
-    __syncthreads();
-  }
-  const int64_t* offs = offs_in_smem ? s_off : W.tgt_off;
-  const int64_t K = __ldcg(&W.tgt_off[G]);
-  if (K > W.hits_cap) return;
-  for (int64_t q = (int64_t)threadIdx.x * gridDim.x + blockIdx.x; q < K; q += gsz) {
-    const uint32_t hit = W.hits[q];
-    if (hit == LPG_NONE) continue;
-    const int g = sel_node_of(offs, G, q);
-    claim(W, hit, g, info[g]);
-  }
+  /* a CTA that never reached the barrier: the round is incomplete, and the
+   * barrier's count is no longer to be trusted, so every replicate stops */
+  if (!ok && threadIdx.x == 0)
+    for (int r = 0; r < R; ++r)
+      if (W.reps[r].active) W.reps[r].error = LPG_ERR_TIMEOUT;
 }
 
 /* Later rounds (after the round 0 claims): one CTA per node that still

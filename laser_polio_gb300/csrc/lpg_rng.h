@@ -107,7 +107,10 @@ LPG_HD uint64_t lpg_raw(uint64_t seed, uint32_t purpose, int32_t tick, uint64_t 
   c[2] = ((uint64_t)purpose << 32) | (uint64_t)(uint32_t)tick;
   c[3] = k >> 2;
   lpg_philox4x64_10(c, seed, LPG_KEY_TAG);
-  return c[k & 3];
+  /* word k mod 4 of the block, chosen without indexing the array (an
+   * indexed register array would live in local memory on the GPU) */
+  const unsigned w = (unsigned)(k & 3);
+  return w == 0 ? c[0] : w == 1 ? c[1] : w == 2 ? c[2] : c[3];
 }
 
 /* 53-bit integer and the matching uniform on [0, 1). */

@@ -19,6 +19,7 @@ def test_choice_prefers_the_default_within_the_margin():
 def test_candidates_hold_the_default_and_respect_the_limit():
     c = autotune.candidates(152, 1216, (1, 2, 8), 1024)
     assert c == sorted(set(c)) and 1216 in c and max(x for x in c if x != 1216) <= 1024 and 152 in c
+    assert autotune.candidates(152, 304, (1, 2, 4), None) == [152, 304]
 
 
 def test_keys_round_to_powers_of_two():
@@ -65,12 +66,14 @@ def test_tune_measures_applies_and_caches(tmp_path):
     h = _Handle()
     chosen, stepped = autotune.tune(h, "k1", 152, rounds=2, path=path)
     assert stepped == h.steps == 2 * 4
-    assert chosen["select"] == 608 and chosen["claim"] == 608
-    assert h.grid[_abi.LAUNCH["select"][0]] == 608
+    assert chosen["rounds"] == 608 and chosen["due"] == 608
+    # the cooperative round-0 kernel is never tried above its default (all of its CTAs must be resident)
+    assert chosen["select"] == 304
+    assert h.grid[_abi.LAUNCH["rounds"][0]] == 608
     h2 = _Handle()
     again, stepped2 = autotune.tune(h2, "k1", 152, path=path)
     assert again == chosen and stepped2 == 0 and h2.steps == 0
-    assert h2.grid[_abi.LAUNCH["select"][0]] == 608
+    assert h2.grid[_abi.LAUNCH["rounds"][0]] == 608
 
 
 @pytest.mark.gpu

@@ -9,6 +9,9 @@ traps or hangs the device.
     limit, so the wait runs out as it would if a copy never landed; the kernel
     records LPG_ERR_TIMEOUT against the simulation it was sweeping, drains
     the copies it did issue and returns, and the context stays usable.
+  - The same for the grid barrier of the first selection round
+    (lpg_test_stall_round0): one CTA held back, the others' bounded wait runs
+    out, every running simulation records LPG_ERR_TIMEOUT.
 """
 
 import numpy as np
@@ -116,5 +119,56 @@ def test_gpu_a_wait_that_runs_out_reports_timeout_on_its_simulation():
         assert_same(res_o2, res_g, "result")
         assert_same(cols_o2, cols_g, "column", count=so2.count)
         assert res_g["sia_vaccinated"][180].sum() > 0
+    finally:
+        h.close()
+
+
+@pytest.mark.gpu
+def test_gpu_a_round0_barrier_that_runs_out_stops_the_run_and_leaves_the_context_usable():
+    """The first selection round is one cooperative launch whose CTAs meet
+    at a grid barrier with a bounded wait.  With CTA 0 held back from the
+    barrier (lpg_test_stall_round0) and the limit at 4096 polls, the other
+    CTAs give up: every running simulation records LPG_ERR_TIMEOUT on the
+    first tick with transmission demand and stops there; a fresh handle on
+    the same device then runs bit-exact with the oracle."""
+    from oracle_backend import assert_same
+    from oracle.oracle import OracleSim
+
+    params, cols = synthetic.bundle(kind="zamfara", n_agents=100_000, n_nodes=8, dur=60, seed=3)
+    d, keep = make_desc(params)
+    h = _lib.Handle([d, d])
+    try:
+        h.test_stall_round0(True, 4096)
+        h.bind_columns(0, {k: v.copy() for k, v in cols.items()})
+        h.bind_columns(1, {k: v.copy() for k, v in cols.items()})
+        h.start()
+        h.step(params["nt"] - 1)
+        assert h.sync_statuses() == [-4, -4]
+        s0, s1 = h.state(0, check=False), h.state(1, check=False)
+        assert s0.error == s1.error == -4 and s0.t == s1.t and 1 < s0.t < params["nt"]
+    finally:
+        h.close()
+    o = OracleSim(d, keepalive=keep)
+    c_o = {k: v.copy() for k, v in cols.items()}
+    o.bind_columns(c_o)
+    o.start()
+    o.step(params["nt"] - 1)
+    res_o = _results(params)
+    o.read_results(res_o)
+    o.read_columns(c_o)
+    so = o.state()
+    o.close()
+    h = _lib.Handle([d])
+    try:
+        c_g = {k: v.copy() for k, v in cols.items()}
+        h.bind_columns(0, c_g)
+        h.start()
+        h.step(params["nt"] - 1)
+        assert h.sync_statuses() == [0]
+        res_g = _results(params)
+        h.read_results(0, res_g)
+        h.read_columns(0, c_g)
+        assert_same(res_o, res_g, "result")
+        assert_same(c_o, c_g, "column", count=so.count)
     finally:
         h.close()
