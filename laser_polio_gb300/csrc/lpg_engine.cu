@@ -18,6 +18,8 @@
 #include <vector>
 
 #include "lpg.h"
+#include <utility>
+
 #include "lpg_kernels.cuh"
 
 namespace {
@@ -959,6 +961,25 @@ extern "C" int lpg_start(lpg_handle* h) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* A tick kernel launched with programmatic stream serialization: its CTAs
+ * may be scheduled before the previous kernel on the stream has finished;
+ * it waits for that kernel's completion itself (pdl_begin). */
+template <typename... Exp, typename... Act>
+static cudaError_t launch_pdl(void (*k)(Exp...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Act&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Act>(args)...);
+}
+
 static int launch_one(lpg_handle* h, int k, bool timed) {
   cudaStream_t st = h->stream;
   DevWorld& W = h->W;
@@ -970,21 +991,21 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     CK(cudaEventRecord(e0, st));
   }
   switch (k) {
-    case 0: k_begin<<<R, 1024, 0, st>>>(W); break;
-    case 1: k_newborns<<<dim3(h->newborn_blocks, R), 256, 0, st>>>(W); break;
-    case 2: k_due<<<h->due_blocks, 256, 0, st>>>(W); break;
-    case 3: k_sweep_due<<<h->sweep0_blocks, LPG_SWEEP_BLOCK, 0, st>>>(W); break;
-    case 4: k_seed<<<R, 1024, 0, st>>>(W); break;
-    case 5: k_sweep_rs<<<h->sweep_blocks, LPG_SWEEP_BLOCK, LPG_SWEEP_SMEM, st>>>(W); break;
-    case 6: k_evb<<<h->evb_blocks, 256, 0, st>>>(W, h->sweep_blocks); break;
-    case 7: k_node_tx<<<G, LPG_NODE_TX_THREADS, 0, st>>>(W); break;
+    case 0: CK(launch_pdl(k_begin, dim3(R), dim3(1024), 0, st, W)); break;
+    case 1: CK(launch_pdl(k_newborns, dim3(h->newborn_blocks, R), dim3(256), 0, st, W)); break;
+    case 2: CK(launch_pdl(k_due, dim3(h->due_blocks), dim3(256), 0, st, W)); break;
+    case 3: CK(launch_pdl(k_sweep_due, dim3(h->sweep0_blocks), dim3(LPG_SWEEP_BLOCK), 0, st, W)); break;
+    case 4: CK(launch_pdl(k_seed, dim3(R), dim3(1024), 0, st, W)); break;
+    case 5: CK(launch_pdl(k_sweep_rs, dim3(h->sweep_blocks), dim3(LPG_SWEEP_BLOCK), LPG_SWEEP_SMEM, st, W)); break;
+    case 6: CK(launch_pdl(k_evb, dim3(h->evb_blocks), dim3(256), 0, st, W, h->sweep_blocks)); break;
+    case 7: CK(launch_pdl(k_node_tx, dim3(G), dim3(LPG_NODE_TX_THREADS), 0, st, W)); break;
     case 8: {
       /* cooperative: its CTAs meet at a grid barrier, so all must be resident */
       void* args[] = {&W};
       CK(cudaLaunchCooperativeKernel((const void*)k_sel_round0, dim3(h->select_blocks), dim3(256), args, 0, st));
       break;
     }
-    case 9: k_sel_rounds<<<h->rounds_blocks, 256, 0, st>>>(W); break;
+    case 9: CK(launch_pdl(k_sel_rounds, dim3(h->rounds_blocks), dim3(256), 0, st, W)); break;
   }
   CK(cudaGetLastError());
   if (timed) CK(cudaEventRecord(e1, st));

@@ -44,6 +44,18 @@
 /* a state byte that carries selection weight: susceptible, or claimed in the
  * running round 0 */
 __device__ __forceinline__ bool sel_open(uint32_t b) { return (b & ~LPG_DS_CLAIMED & 0xffu) == 0; }
+
+/* Programmatic dependent launch: the tick's kernels are launched so that
+ * the next one's CTAs may be scheduled while this one finishes.  Every tick
+ * kernel first waits until the kernel before it has completed and its
+ * writes are visible (griddepcontrol.wait: nothing of the previous kernel is
+ * read or written before it), then lets the next one be scheduled
+ * (griddepcontrol.launch_dependents).  Both are no-ops for a kernel launched
+ * without the attribute or without dependents. */
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 #define LPG_MAX_ROUNDS 1000000
 
 /* ------------------------------------------------------------------------ */
@@ -205,6 +217,7 @@ __device__ void rep_prepare(DevRep* rp) {
  * the stop rule and the cleared event counters come from the previous
  * tick's k_end). */
 __global__ void k_begin(DevWorld W) {
+  pdl_begin();
   DevRep* rp = &W.reps[blockIdx.x];
   if (!rp->active || !rp->vd_tick) return;
   const int n = rp->n_nodes, nb = rp->node_base, t = rp->cur_t, G = W.G;
@@ -355,6 +368,7 @@ __device__ __forceinline__ int32_t run_min_i32(int32_t v, uint32_t m) {
 #define LPG_NB_SMEM 4096
 #define LPG_KM_SMEM 256
 __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
+  pdl_begin();
   const DevRep* rp = &W.reps[blockIdx.y];
   if (!rp->active || !rp->vd_tick || rp->nb_total == 0) return;
   __shared__ int64_t s_end[LPG_NB_SMEM];
@@ -763,6 +777,7 @@ __device__ __forceinline__ int32_t sub8_min(int32_t x) {
  * death), one global atomic per warp. */
 #define LPG_DUE_MAX 8192
 __global__ void __launch_bounds__(256) k_due(DevWorld W) {
+  pdl_begin();
   const int lane = threadIdx.x & 31;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
@@ -891,6 +906,7 @@ __device__ __forceinline__ int32_t dense_from(const SweepPlan& P, int32_t w, int
 }
 
 __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
+  pdl_begin();
   extern __shared__ __align__(128) uint8_t sm_stage[];
   __shared__ SweepPlan P;
   __shared__ __align__(8) uint64_t full[LPG_NST];
@@ -1242,6 +1258,7 @@ __device__ __forceinline__ void ds_queue_step(DevWorld& W, uint64_t e, bool on) 
  * queued agents (ds_queue_step).  A CTA's queue slab starts at its first
  * item times 128 entries of evq. */
 __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_due(DevWorld W) {
+  pdl_begin();
   __shared__ uint32_t s_qcnt;
   const int lane = threadIdx.x & 31;
   const int64_t D = (int64_t)*(volatile uint32_t*)W.due_n;
@@ -1340,6 +1357,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_due(DevWorld W) {
  * agent.  Probability tests are integer compares of the 53-bit draw with
  * precomputed thresholds (same outcome as the double compares). */
 __global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
+  pdl_begin();
   __shared__ uint32_t s_pre[1025];
   {
     /* nothing queued unless some simulation has RI or SIA work today */
@@ -1453,6 +1471,7 @@ __global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
 /* ------------------------------------------------------------------------ */
 /* Seed schedule: one CTA per simulation, events of the tick in order. */
 __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
+  pdl_begin();
   const DevRep* rp = &W.reps[blockIdx.x];
   if (!rp->active || rp->seed_n == 0) return;
   const int t = rp->cur_t, nb = rp->node_base, G = W.G;
@@ -1712,6 +1731,7 @@ __device__ __forceinline__ uint64_t pre_bb_w1(const DevWorld& W, int g, int lane
 }
 
 __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k_node_tx(DevWorld W) {
+  pdl_begin();
   const int g = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __shared__ uint64_t s_mix[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS][6]; /* per warp: A, R words */
@@ -2437,6 +2457,7 @@ __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs,
  * two targets on one agent claims it changes nothing (its strain draw is
  * keyed by the agent). */
 __global__ void __launch_bounds__(256) k_sel_round0(DevWorld W) {
+  pdl_begin();
   const int R = W.n_reps, G = W.G;
   int any = 0;
   for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
@@ -2518,6 +2539,7 @@ __global__ void __launch_bounds__(256) k_sel_round0(DevWorld W) {
 __device__ __noinline__ void sel_rounds(DevWorld& W);
 __device__ void end_tick(DevWorld& W, int64_t g0, int64_t gstride);
 __global__ void __launch_bounds__(256) k_sel_rounds(DevWorld W) {
+  pdl_begin();
   const int R = W.n_reps;
   int any = 0;
   for (int r = 0; r < R; ++r) any |= (W.reps[r].active && W.reps[r].any_demand);
