@@ -39,9 +39,9 @@ static bool kernel_needed(int k, uint8_t need) {
   }
 }
 
-const char* kKernelNames[] = {"k_begin", "k_newborns", "k_due", "k_sweep_a", "k_seed",
-                              "k_sweep_b", "k_evb", "k_node_tx", "k_sel_round0", "k_sel_rounds"};
-constexpr int kNumTickKernels = 10; /* k_sel_rounds ends the tick (results rows, next tick's setup) */
+const char* kKernelNames[] = {"k_begin", "k_newborns", "k_due", "k_sweep_a", "k_seed", "k_sweep_b",
+                              "k_evb", "k_node_mix", "k_node_tx", "k_sel_round0", "k_sel_rounds"};
+constexpr int kNumTickKernels = 11; /* k_sel_rounds ends the tick (results rows, next tick's setup) */
 constexpr int kTicksPerGraph = 8;
 
 /* Reference-ordered columns of one simulation on the device. */
@@ -52,6 +52,7 @@ struct Staging {
   int16_t *node = nullptr, *ri = nullptr;
   float *risk = nullptr, *inf = nullptr;
   int32_t *dob = nullptr, *dod = nullptr;
+  void* base = nullptr; /* the one allocation the columns are carved from */
   bool bound = false;
 };
 
@@ -177,27 +178,104 @@ struct ScatterArgs {
   const int32_t* rank;        /* rank within node (unsorted input), or null */
 };
 
-__global__ void k_scatter(DevWorld W, ScatterArgs a) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += (int64_t)gridDim.x * blockDim.x) {
-    int n = a.s.node[i];
-    int64_t rk = a.rank ? (int64_t)a.rank[i] : i - a.node_first[n];
-    int64_t pos = (int64_t)(a.node_chunk0[n] + rk / LPG_CHUNK) * LPG_CHUNK + rk % LPG_CHUNK;
-    W.ds[pos] = a.s.ds[i];
-    W.strain[pos] = a.s.strain[i];
-    W.et[pos] = a.s.et[i];
-    W.it[pos] = a.s.it[i];
-    W.pt[pos] = a.s.pt[i];
-    W.pp[pos] = a.s.pp[i];
-    W.par[pos] = a.s.par[i];
-    W.ipv[pos] = a.s.ipv[i];
-    W.cm[pos] = a.s.cm[i];
-    W.ri[pos] = a.s.ri[i];
-    W.risk[pos] = a.s.risk[i];
-    W.inf[pos] = a.s.inf[i];
-    W.dob[pos] = a.s.dob[i];
-    W.dod[pos] = a.s.dod[i];
-    W.ref[pos] = (uint32_t)i;
+/* One agent of the reference order into its slot of the node-major layout. */
+__device__ __forceinline__ void scatter_one(const DevWorld& W, const ScatterArgs& a, int64_t i) {
+  const int n = a.s.node[i];
+  const int64_t rk = a.rank ? (int64_t)a.rank[i] : i - a.node_first[n];
+  const int64_t pos = (int64_t)a.node_chunk0[n] * LPG_CHUNK + rk; /* a node's chunks are consecutive */
+  W.ds[pos] = a.s.ds[i];
+  W.strain[pos] = a.s.strain[i];
+  W.et[pos] = a.s.et[i];
+  W.it[pos] = a.s.it[i];
+  W.pt[pos] = a.s.pt[i];
+  W.pp[pos] = a.s.pp[i];
+  W.par[pos] = a.s.par[i];
+  W.ipv[pos] = a.s.ipv[i];
+  W.cm[pos] = a.s.cm[i];
+  W.ri[pos] = a.s.ri[i];
+  W.risk[pos] = a.s.risk[i];
+  W.inf[pos] = a.s.inf[i];
+  W.dob[pos] = a.s.dob[i];
+  W.dod[pos] = a.s.dod[i];
+  W.ref[pos] = (uint32_t)i;
+}
+
+/* 16 slots of one column from 16 consecutive agents: element loads (the
+ * source run may start anywhere), packed into 16-byte stores (the slots
+ * start at a multiple of 16). */
+__device__ __forceinline__ void fill16(int8_t* __restrict__ dst, const int8_t* __restrict__ src) {
+  uint32_t w[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    w[j] = (uint32_t)(uint8_t)__ldg(src + 4 * j) | (uint32_t)(uint8_t)__ldg(src + 4 * j + 1) << 8 |
+           (uint32_t)(uint8_t)__ldg(src + 4 * j + 2) << 16 | (uint32_t)(uint8_t)__ldg(src + 4 * j + 3) << 24;
+  *reinterpret_cast<uint4*>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+__device__ __forceinline__ void fill16(uint8_t* dst, const uint8_t* src) {
+  fill16(reinterpret_cast<int8_t*>(dst), reinterpret_cast<const int8_t*>(src));
+}
+__device__ __forceinline__ void fill16(int16_t* __restrict__ dst, const int16_t* __restrict__ src) {
+  uint32_t w[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    w[j] = (uint32_t)(uint16_t)__ldg(src + 2 * j) | (uint32_t)(uint16_t)__ldg(src + 2 * j + 1) << 16;
+  reinterpret_cast<uint4*>(dst)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+  reinterpret_cast<uint4*>(dst)[1] = make_uint4(w[4], w[5], w[6], w[7]);
+}
+template <typename T>
+__device__ __forceinline__ void fill16_32(T* __restrict__ dst, const T* __restrict__ src) {
+  static_assert(sizeof(T) == 4, "32-bit columns");
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    reinterpret_cast<uint4*>(dst)[j] = make_uint4(__ldg(s + 4 * j), __ldg(s + 4 * j + 1), __ldg(s + 4 * j + 2),
+                                                  __ldg(s + 4 * j + 3));
+}
+
+/* The reference-ordered columns of sorted input into the node-major layout,
+ * slot-driven: a thread fills 16 slots of a chunk from the agents that go
+ * there (a node's agents are a contiguous run of the input and its chunks
+ * consecutive), so every store is a full 16-byte vector; the last partial
+ * group of a chunk slot by slot. */
+__global__ void k_scatter_sorted(DevWorld W, ScatterArgs a, int32_t chunk_base, int32_t used, int32_t node_base) {
+  const int64_t groups = (int64_t)used * (LPG_CHUNK / 16);
+  for (int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < groups; gi += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cid = chunk_base + gi / (LPG_CHUNK / 16);
+    const int o0 = (int)(gi % (LPG_CHUNK / 16)) * 16;
+    const int4 meta = W.cmeta[cid];
+    if (o0 >= meta.y) continue;
+    const int nl = meta.x - node_base;
+    const int64_t i0 = a.node_first[nl] + (cid - a.node_chunk0[nl]) * LPG_CHUNK + o0;
+    const int64_t p0 = cid * LPG_CHUNK + o0;
+    if (o0 + 16 <= meta.y) {
+      fill16(W.ds + p0, a.s.ds + i0);
+      fill16(W.strain + p0, a.s.strain + i0);
+      fill16(W.et + p0, a.s.et + i0);
+      fill16(W.it + p0, a.s.it + i0);
+      fill16(W.pt + p0, a.s.pt + i0);
+      fill16(W.pp + p0, a.s.pp + i0);
+      fill16(W.par + p0, a.s.par + i0);
+      fill16(W.ipv + p0, a.s.ipv + i0);
+      fill16(W.cm + p0, a.s.cm + i0);
+      fill16(W.ri + p0, a.s.ri + i0);
+      fill16_32(W.risk + p0, a.s.risk + i0);
+      fill16_32(W.inf + p0, a.s.inf + i0);
+      fill16_32(W.dob + p0, a.s.dob + i0);
+      fill16_32(W.dod + p0, a.s.dod + i0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        reinterpret_cast<uint4*>(W.ref + p0)[j] = make_uint4((uint32_t)(i0 + 4 * j), (uint32_t)(i0 + 4 * j + 1),
+                                                             (uint32_t)(i0 + 4 * j + 2), (uint32_t)(i0 + 4 * j + 3));
+    } else {
+      for (int k = 0; k < meta.y - o0; ++k) scatter_one(W, a, i0 + k);
+    }
   }
+}
+
+/* Unsorted input: agent by agent, each to the slot of its rank in its node. */
+__global__ void k_scatter(DevWorld W, ScatterArgs a) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += (int64_t)gridDim.x * blockDim.x)
+    scatter_one(W, a, i);
 }
 
 /* Columns of one simulation (rep) back in reference slot order.  Timers of
@@ -433,28 +511,38 @@ extern "C" int lpg_create(const lpg_sim_desc* sims, int32_t n_sims, int32_t devi
 }
 
 static int alloc_staging(lpg_handle* h, Staging& s, int64_t cap) {
-  int rc = 0;
-  rc |= dalloc(h, &s.ds, cap);
-  rc |= dalloc(h, &s.strain, cap);
-  rc |= dalloc(h, &s.et, cap);
-  rc |= dalloc(h, &s.it, cap);
-  rc |= dalloc(h, &s.pt, cap);
-  rc |= dalloc(h, &s.pp, cap);
-  rc |= dalloc(h, &s.par, cap);
-  rc |= dalloc(h, &s.ipv, cap);
-  rc |= dalloc(h, &s.cm, cap);
-  rc |= dalloc(h, &s.node, cap);
-  rc |= dalloc(h, &s.ri, cap);
-  rc |= dalloc(h, &s.risk, cap);
-  rc |= dalloc(h, &s.inf, cap);
-  rc |= dalloc(h, &s.dob, cap);
-  rc |= dalloc(h, &s.dod, cap);
-  return rc ? LPG_ERR_NOMEM : 0;
+  /* one allocation carved into the fifteen columns, each at a 256-byte
+   * boundary (one cudaMalloc and one cudaFree instead of fifteen) */
+  const size_t n = (size_t)std::max<int64_t>(cap, 1);
+  const size_t esz[15] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 2, 4, 4, 4, 4};
+  size_t off[15], total = 0;
+  for (int k = 0; k < 15; ++k) {
+    off[k] = total;
+    total += (esz[k] * n + 255) & ~(size_t)255;
+  }
+  uint8_t* base = nullptr;
+  if (dalloc(h, &base, total)) return LPG_ERR_NOMEM;
+  s.base = base;
+  s.ds = reinterpret_cast<int8_t*>(base + off[0]);
+  s.strain = reinterpret_cast<int8_t*>(base + off[1]);
+  s.et = reinterpret_cast<int8_t*>(base + off[2]);
+  s.it = reinterpret_cast<int8_t*>(base + off[3]);
+  s.pt = reinterpret_cast<int8_t*>(base + off[4]);
+  s.pp = reinterpret_cast<int8_t*>(base + off[5]);
+  s.par = reinterpret_cast<int8_t*>(base + off[6]);
+  s.ipv = reinterpret_cast<int8_t*>(base + off[7]);
+  s.cm = reinterpret_cast<uint8_t*>(base + off[8]);
+  s.node = reinterpret_cast<int16_t*>(base + off[9]);
+  s.ri = reinterpret_cast<int16_t*>(base + off[10]);
+  s.risk = reinterpret_cast<float*>(base + off[11]);
+  s.inf = reinterpret_cast<float*>(base + off[12]);
+  s.dob = reinterpret_cast<int32_t*>(base + off[13]);
+  s.dod = reinterpret_cast<int32_t*>(base + off[14]);
+  return 0;
 }
 
 static void free_staging(lpg_handle* h, Staging& s) {
-  void* ps[] = {s.ds, s.strain, s.et, s.it, s.pt, s.pp, s.par, s.ipv, s.cm, s.node, s.ri, s.risk, s.inf, s.dob, s.dod};
-  for (void* p : ps) dfree_one(h, p);
+  dfree_one(h, s.base);
   s = Staging();
 }
 
@@ -633,6 +721,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   rc |= dalloc(h, &W.nb_end, G);
   rc |= dalloc(h, &W.nb_li0, G);
   rc |= dalloc(h, &W.prob, (size_t)LPG_MAX_STRAINS * G);
+  rc |= dalloc(h, &W.inck, (size_t)LPG_MAX_STRAINS * G);
   rc |= dalloc(h, &W.size, G);
   rc |= dalloc(h, &W.uniq, G);
   rc |= dalloc(h, &W.ksel, G);
@@ -902,7 +991,10 @@ extern "C" int lpg_start(lpg_handle* h) {
       CK(cudaStreamSynchronize(st));
     }
     ScatterArgs a{s.stg, s.d.count, d_nc0, d_first, d_rank};
-    if (s.d.count > 0) k_scatter<<<2048, 256, 0, st>>>(W, a);
+    if (s.d.count > 0) {
+      if (a.rank) k_scatter<<<2048, 256, 0, st>>>(W, a);
+      else k_scatter_sorted<<<h->sm_count * 16, 256, 0, st>>>(W, a, hr[r].chunk_base, hr[r].used_chunks, hr[r].node_base);
+    }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     dfree_one(h, d_nc0);
@@ -998,14 +1090,15 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 4: CK(launch_pdl(k_seed, dim3(R), dim3(1024), 0, st, W)); break;
     case 5: CK(launch_pdl(k_sweep_rs, dim3(h->sweep_blocks), dim3(LPG_SWEEP_BLOCK), LPG_SWEEP_SMEM, st, W)); break;
     case 6: CK(launch_pdl(k_evb, dim3(h->evb_blocks), dim3(256), 0, st, W, h->sweep_blocks)); break;
-    case 7: CK(launch_pdl(k_node_tx, dim3(G), dim3(LPG_NODE_TX_THREADS), 0, st, W)); break;
-    case 8: {
+    case 7: CK(launch_pdl(k_node_mix, dim3(G), dim3(LPG_NODE_MIX_THREADS), 0, st, W)); break;
+    case 8: CK(launch_pdl(k_node_tx, dim3(G), dim3(LPG_NODE_TX_THREADS), 0, st, W)); break;
+    case 9: {
       /* cooperative: its CTAs meet at a grid barrier, so all must be resident */
       void* args[] = {&W};
       CK(cudaLaunchCooperativeKernel((const void*)k_sel_round0, dim3(h->select_blocks), dim3(256), args, 0, st));
       break;
     }
-    case 9: CK(launch_pdl(k_sel_rounds, dim3(h->rounds_blocks), dim3(256), 0, st, W)); break;
+    case 10: CK(launch_pdl(k_sel_rounds, dim3(h->rounds_blocks), dim3(256), 0, st, W)); break;
   }
   CK(cudaGetLastError());
   if (timed) CK(cudaEventRecord(e1, st));

@@ -203,6 +203,7 @@ typedef struct {
   int64_t* nb_end;
   int64_t* nb_li0;
   double* prob; /* [LPG_MAX_STRAINS][G] */
+  double* inck; /* [LPG_MAX_STRAINS][G] incoming infectivity of the tick (k_node_mix) */
   int64_t* size;
   int64_t* uniq;
   int64_t* ksel;

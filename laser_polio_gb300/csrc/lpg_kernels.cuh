@@ -1655,6 +1655,11 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
 /* six CTAs of the node step per SM (at most 170 registers a thread): one
  * wave covers 912 nodes, so a 774-node tick needs no second wave */
 #define LPG_NODE_TX_MIN_BLOCKS 6
+/* the mixing step: four warps of products and sums, one warp for the
+ * node's chunk prefix; six CTAs per SM (at most 68 registers a thread) */
+#define LPG_NODE_MIX_WARPS 4
+#define LPG_NODE_MIX_THREADS (32 * (LPG_NODE_MIX_WARPS + 1))
+#define LPG_NODE_MIX_MIN_BLOCKS 6
 
 struct SelInfo {
   uint64_t seed;
@@ -1717,15 +1722,105 @@ __device__ __forceinline__ void warp_chunk_prefix(const DevWorld& W, const int32
   }
 }
 
+/* Incoming infectivity of every node and strain (model.py:1327-1363: the
+ * network product), and the node's chunk prefix for the selection.  One CTA
+ * per node: four warps share the source nodes, exact integer arithmetic: B
+ * in units of 2^-40 times the network weight in its two fixed-point parts
+ * (lpg_net_split; transposed row, contiguous), the two products summed in
+ * three-word accumulators, one conversion (lpg_mix_value) into inck; an
+ * exact sum does not depend on how the threads split it.  The fifth warp
+ * forms the node-local chunk prefix (exact in integers) meanwhile. */
+__global__ void __launch_bounds__(LPG_NODE_MIX_THREADS, LPG_NODE_MIX_MIN_BLOCKS) k_node_mix(DevWorld W) {
+  pdl_begin();
+  const int g = blockIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ uint64_t s_mix[LPG_NODE_MIX_WARPS][LPG_MAX_STRAINS][6]; /* per warp: A, R words */
+  if (g >= W.G) return;
+  const DevRep* rp = &W.reps[W.node_rep[g]];
+  if (!rp->active || !(rp->comps & LPG_COMP_TX)) return;
+  const int i = g - rp->node_base, n = rp->n_nodes, ns = rp->ns, G = W.G, nb = rp->node_base;
+  if (wid == LPG_NODE_MIX_WARPS) {
+    const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+    const int32_t a = st[i], nch = st[i + 1] - st[i];
+    warp_chunk_prefix(W, W.node_chunks[rp->csr_cur] + rp->chunk_base + a, nch, W.cpref + rp->chunk_base + a);
+    return;
+  }
+  /* qrow[ii] = network[ii][i] as (hi 2^-62, lo 2^-120), lpg_net_split */
+  const ulonglong2* qrow = reinterpret_cast<const ulonglong2*>(rp->netq_t) + (int64_t)i * n;
+  constexpr int NT = 32 * LPG_NODE_MIX_WARPS;
+  constexpr int PER = 7; /* source nodes a thread takes per pass: one pass up to 896 nodes */
+  static_assert(PER * NT >= 774, "one pass for a 774-node simulation");
+  /* per strain: A = sum B hi and R = sum B lo, three words each, exact;
+   * one strain at a time (six accumulators live), the network entries of
+   * the pass loaded once for all strains */
+  /* the same number of passes for every thread (the shuffles below need
+   * all 32 lanes), loads past the last node predicated off */
+  const int npass = (n + PER * NT - 1) / (PER * NT);
+  for (int pass = 0; pass < npass; ++pass) {
+    const int ii0 = pass * PER * NT + threadIdx.x;
+    ulonglong2 w[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int ii = ii0 + u * NT;
+      w[u] = ii < n ? qrow[ii] : make_ulonglong2(0, 0);
+    }
+#pragma unroll 1
+    for (int k = 0; k < ns; ++k) {
+      uint64_t b[PER];
+#pragma unroll
+      for (int u = 0; u < PER; ++u) {
+        const int ii = ii0 + u * NT;
+        b[u] = ii < n ? W.bb[(int64_t)k * G + nb + ii] : 0;
+      }
+      uint64_t a0 = 0, a1 = 0, a2 = 0, r0 = 0, r1 = 0, r2 = 0;
+#pragma unroll
+      for (int u = 0; u < PER; ++u) {
+        acc3_mul(a0, a1, a2, b[u], w[u].x);
+        acc3_mul(r0, r1, r2, b[u], w[u].y);
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const uint64_t x0 = __shfl_down_sync(FULLMASK, a0, off), x1 = __shfl_down_sync(FULLMASK, a1, off),
+                       x2 = __shfl_down_sync(FULLMASK, a2, off);
+        acc3_add(a0, a1, a2, x0, x1, x2);
+        const uint64_t y0 = __shfl_down_sync(FULLMASK, r0, off), y1 = __shfl_down_sync(FULLMASK, r1, off),
+                       y2 = __shfl_down_sync(FULLMASK, r2, off);
+        acc3_add(r0, r1, r2, y0, y1, y2);
+      }
+      if (lane == 0) {
+        if (pass == 0) {
+          s_mix[wid][k][0] = a0;
+          s_mix[wid][k][1] = a1;
+          s_mix[wid][k][2] = a2;
+          s_mix[wid][k][3] = r0;
+          s_mix[wid][k][4] = r1;
+          s_mix[wid][k][5] = r2;
+        } else { /* a later pass (more than PER x NT nodes): added to the first */
+          acc3_add(s_mix[wid][k][0], s_mix[wid][k][1], s_mix[wid][k][2], a0, a1, a2);
+          acc3_add(s_mix[wid][k][3], s_mix[wid][k][4], s_mix[wid][k][5], r0, r1, r2);
+        }
+      }
+    }
+  }
+  /* the four mixing warps only (the fifth may have left) */
+  asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
+  if (threadIdx.x < ns) {
+    const int k = threadIdx.x;
+    uint64_t x0 = 0, x1 = 0, x2 = 0, y0 = 0, y1 = 0, y2 = 0;
+#pragma unroll
+    for (int w4 = 0; w4 < LPG_NODE_MIX_WARPS; ++w4) {
+      acc3_add(x0, x1, x2, s_mix[w4][k][0], s_mix[w4][k][1], s_mix[w4][k][2]);
+      acc3_add(y0, y1, y2, s_mix[w4][k][3], s_mix[w4][k][4], s_mix[w4][k][5]);
+    }
+    W.inck[(int64_t)k * G + g] = lpg_mix_value(x0, x1, x2, y0, y1, y2);
+  }
+}
+
 /* Node-level force of infection and exposure counts (model.py:1327-1407);
- * the same arithmetic, in the same order, as the oracle's lpo_node_tx.
- * One CTA per node.  Incoming infectivity sum_i B_i N[i][n] is exact
- * integer arithmetic: B in units of 2^-40 times the network weight in its
- * two fixed-point parts (lpg_net_split; transposed row, contiguous), the two
- * products summed in three-word accumulators, one conversion
- * (lpg_mix_value); an exact sum does not depend on how the threads split it. */
-/* Lane k < ns of the second warp: this node's incoming-infectivity total of
- * strain k (the first warp's pre_bb). */
+ * the same arithmetic, in the same order, as the oracle's lpo_node_tx,
+ * from the incoming infectivity k_node_mix formed.  One CTA per node. */
+/* Lane k < ns of the second warp: this node's infectivity total of strain k
+ * (the first warp's pre_bb). */
 __device__ __forceinline__ uint64_t pre_bb_w1(const DevWorld& W, int g, int lane, int ns) {
   return lane < ns ? W.bb[(int64_t)lane * W.G + g] : 0;
 }
@@ -1734,7 +1829,6 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
   pdl_begin();
   const int g = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __shared__ uint64_t s_mix[LPG_NODE_TX_THREADS / 32][LPG_MAX_STRAINS][6]; /* per warp: A, R words */
   __shared__ double s_gam;   /* the negative binomial's gamma variate, formed ahead by the second warp */
   __shared__ uint64_t s_gamk; /* the exposure stream's position after it */
   if (g >= W.G) return;
@@ -1742,7 +1836,6 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
   if (threadIdx.x == 0) W.ksel[g] = 0;
   if (!rp->active) return;
   const int i = g - rp->node_base, n = rp->n_nodes, ns = rp->ns, t = rp->cur_t, G = W.G;
-  const int nb = rp->node_base;
   int32_t pop_t = 0;
   if (rp->comps & LPG_COMP_VD) {
     const int32_t* pop1 = RES(rp, RS_POP, t - 1);
@@ -1759,7 +1852,7 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
   if (!(rp->comps & LPG_COMP_TX)) return;
   /* inputs of lane 0's draw, requested now so that they arrive during the
    * mixing */
-  double pre_seas = 0.0, pre_r0s = 0.0, pre_rowsum = 0.0;
+  double pre_seas = 0.0, pre_r0s = 0.0, pre_rowsum = 0.0, pre_inck = 0.0;
   uint64_t pre_bb = 0;
   uint64_t pre_sw = 0;
   int64_t pre_sc = 0;
@@ -1769,6 +1862,7 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
     pre_r0s = rp->r0s[i];
     pre_rowsum = rp->rowsum[i];
     pre_bb = W.bb[(int64_t)threadIdx.x * G + g];
+    pre_inck = W.inck[(int64_t)threadIdx.x * G + g];
   }
   if (threadIdx.x == 0) {
     pre_sw = W.sw[g];
@@ -1782,53 +1876,6 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
     }
     if (threadIdx.x < ns) rr[3 + threadIdx.x] = (double)pre_bb * 0x1.0p-40;
   }
-  /* qrow[ii] = network[ii][i] as (hi 2^-62, lo 2^-120), lpg_net_split */
-  const ulonglong2* qrow = reinterpret_cast<const ulonglong2*>(rp->netq_t) + (int64_t)i * n;
-  /* per strain: A = sum B hi and R = sum B lo, three words each, exact */
-  uint64_t a0[LPG_MAX_STRAINS] = {0, 0, 0, 0}, a1[LPG_MAX_STRAINS] = {0, 0, 0, 0}, a2[LPG_MAX_STRAINS] = {0, 0, 0, 0};
-  uint64_t r0[LPG_MAX_STRAINS] = {0, 0, 0, 0}, r1[LPG_MAX_STRAINS] = {0, 0, 0, 0}, r2[LPG_MAX_STRAINS] = {0, 0, 0, 0};
-  /* batches of 8 source nodes per thread, every load of a batch issued
-   * before any multiply (two batches for up to 1024 nodes) */
-  for (int ii0 = threadIdx.x; ii0 < n; ii0 += 8 * blockDim.x) {
-    ulonglong2 w[8];
-    uint64_t b[8][LPG_MAX_STRAINS];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int ii = ii0 + u * blockDim.x;
-      w[u] = ii < n ? qrow[ii] : make_ulonglong2(0, 0);
-#pragma unroll
-      for (int k = 0; k < LPG_MAX_STRAINS; ++k) b[u][k] = (ii < n && k < ns) ? W.bb[(int64_t)k * G + nb + ii] : 0;
-    }
-#pragma unroll
-    for (int u = 0; u < 8; ++u)
-#pragma unroll
-      for (int k = 0; k < LPG_MAX_STRAINS; ++k)
-        if (k < ns) {
-          acc3_mul(a0[k], a1[k], a2[k], b[u][k], w[u].x);
-          acc3_mul(r0[k], r1[k], r2[k], b[u][k], w[u].y);
-        }
-  }
-#pragma unroll
-  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t x0 = __shfl_down_sync(FULLMASK, a0[k], off), x1 = __shfl_down_sync(FULLMASK, a1[k], off),
-                     x2 = __shfl_down_sync(FULLMASK, a2[k], off);
-      acc3_add(a0[k], a1[k], a2[k], x0, x1, x2);
-      const uint64_t y0 = __shfl_down_sync(FULLMASK, r0[k], off), y1 = __shfl_down_sync(FULLMASK, r1[k], off),
-                     y2 = __shfl_down_sync(FULLMASK, r2[k], off);
-      acc3_add(r0[k], r1[k], r2[k], y0, y1, y2);
-    }
-    if (lane == 0) {
-      s_mix[wid][k][0] = a0[k];
-      s_mix[wid][k][1] = a1[k];
-      s_mix[wid][k][2] = a2[k];
-      s_mix[wid][k][3] = r0[k];
-      s_mix[wid][k][4] = r1[k];
-      s_mix[wid][k][5] = r2[k];
-    }
-  }
-  __syncthreads();
   if (wid == 1) {
     /* the second warp: when the node has no local infectivity (the
      * zero-inflated negative binomial, model.py:1383-1395), its gamma
@@ -1846,12 +1893,6 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
     }
     __syncwarp();
     asm volatile("bar.sync 1, 64;" ::: "memory");
-    /* then the node's chunk prefix for the selection that follows
-     * (node-local, exact in integers), while lane 0 of the first warp
-     * draws the exposure count */
-    const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
-    const int32_t a = st[i], nch = st[i + 1] - st[i];
-    warp_chunk_prefix(W, W.node_chunks[rp->csr_cur] + rp->chunk_base + a, nch, W.cpref + rp->chunk_base + a);
     return;
   }
   if (wid != 0) return;
@@ -1867,13 +1908,7 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
   double pk = 0.0;
   const double denom = (double)(pop_t > 1 ? pop_t : 1);
   if (lane < ns) {
-    uint64_t x0 = 0, x1 = 0, x2 = 0, y0 = 0, y1 = 0, y2 = 0;
-#pragma unroll
-    for (int w8 = 0; w8 < LPG_NODE_TX_THREADS / 32; ++w8) {
-      acc3_add(x0, x1, x2, s_mix[w8][lane][0], s_mix[w8][lane][1], s_mix[w8][lane][2]);
-      acc3_add(y0, y1, y2, s_mix[w8][lane][3], s_mix[w8][lane][4], s_mix[w8][lane][5]);
-    }
-    const double inck = lpg_mix_value(x0, x1, x2, y0, y1, y2);
+    const double inck = pre_inck;
     const double bpre = (double)pre_bb * 0x1.0p-40;
     double beta = bpre + (inck - bpre * pre_rowsum);
     beta = (beta * pre_seas) * pre_r0s;
@@ -2924,30 +2959,43 @@ __global__ void __launch_bounds__(LPG_SWEEP_THREADS) k_count(DevWorld W, int32_t
       if (threadIdx.x == 0) s_sw = 0;
       __syncthreads();
       const int fill = meta.y;
-      for (int o = threadIdx.x; o < fill; o += blockDim.x) {
+      /* a warp takes 32 consecutive slots (one sub-block's quarter): its
+       * counts by ballot, its sums and minimum by warp reductions, one
+       * shared-memory update per warp and quantity */
+      const int lane = threadIdx.x & 31;
+      for (int o0 = threadIdx.x & ~31; o0 < fill; o0 += blockDim.x) {
+        const int o = o0 + lane;
         const int64_t pos = cid * LPG_CHUNK + o;
-        const int8_t s = W.ds[pos];
-        if (s < 0) continue;
-        atomicMin(&s_dmin[o / LPG_SUB], W.dod[pos]);
-        const int st = W.strain[pos];
-        if (s == 0) {
-          atomicAdd(&s_tot[TT_S], 1);
-          uint64_t w = fix_risk(W.risk[pos]);
-          if (w) {
-            atomicAdd(&s_sw, (unsigned long long)w);
-            atomicAdd(&s_sub[o / LPG_SUB], (unsigned long long)w);
+        const int8_t s = o < fill ? W.ds[pos] : (int8_t)-1;
+        const bool alive = s >= 0;
+        const int st = alive ? W.strain[pos] : 0;
+        const int32_t dod = alive ? W.dod[pos] : LPG_NO_DOD;
+        const uint64_t w = s == 0 ? fix_risk(W.risk[pos]) : 0;
+        const uint64_t bw = s == 2 ? fix_beta(W.inf[pos], rp->strain_scal[st]) : 0;
+        const bool potp = alive && W.pp[pos] == 1, par = alive && W.par[pos] == 1;
+        const int32_t dmin = __reduce_min_sync(FULLMASK, dod);
+        const int nS = __popc(__ballot_sync(FULLMASK, s == 0)), nR = __popc(__ballot_sync(FULLMASK, s == 3));
+        const int nPotp = __popc(__ballot_sync(FULLMASK, potp)), nPar = __popc(__ballot_sync(FULLMASK, par));
+        uint64_t ws = w;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) ws += __shfl_xor_sync(FULLMASK, ws, off);
+        if (lane == 0) {
+          atomicMin(&s_dmin[o0 / LPG_SUB], dmin);
+          if (nS) atomicAdd(&s_tot[TT_S], nS);
+          if (nR) atomicAdd(&s_tot[TT_R], nR);
+          if (nPotp) atomicAdd(&s_tot[TT_POTP], nPotp);
+          if (nPar) atomicAdd(&s_tot[TT_P], nPar);
+          if (ws) {
+            atomicAdd(&s_sw, (unsigned long long)ws);
+            atomicAdd(&s_sub[o0 / LPG_SUB], (unsigned long long)ws);
           }
-        } else if (s == 1) {
-          atomicAdd(&s_tot[TT_E0 + st], 1);
-        } else if (s == 2) {
-          atomicAdd(&s_tot[TT_I0 + st], 1);
-          uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
-          if (bw) atomicAdd(&s_bb[st], (unsigned long long)bw);
-        } else if (s == 3) {
-          atomicAdd(&s_tot[TT_R], 1);
         }
-        if (W.pp[pos] == 1) atomicAdd(&s_tot[TT_POTP], 1);
-        if (W.par[pos] == 1) atomicAdd(&s_tot[TT_P], 1);
+        /* exposed and infectious agents are few: one update each */
+        if (s == 1) atomicAdd(&s_tot[TT_E0 + st], 1);
+        if (s == 2) {
+          atomicAdd(&s_tot[TT_I0 + st], 1);
+          if (bw) atomicAdd(&s_bb[st], (unsigned long long)bw);
+        }
       }
       __syncthreads();
       if (threadIdx.x < TT_N && s_tot[threadIdx.x]) atomicAdd(&tot_out[(int64_t)threadIdx.x * W.G + g], s_tot[threadIdx.x]);
