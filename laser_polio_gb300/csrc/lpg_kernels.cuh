@@ -1664,7 +1664,7 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
 struct SelInfo {
   uint64_t seed;
   uint64_t T;        /* remaining susceptible weight */
-  double cum[LPG_MAX_STRAINS]; /* cumulative relative FOI (model.py:1127-1135) */
+  uint64_t thr[LPG_MAX_STRAINS]; /* the cumulative relative FOI (model.py:1127-1135) as 53-bit thresholds */
   int32_t a;         /* first entry of the node's chunk list in the concatenated lists */
   int32_t n;         /* its chunks */
   int32_t i;         /* node index in its simulation */
@@ -1673,9 +1673,20 @@ struct SelInfo {
   int32_t csr;       /* which of the two chunk-list buffers holds the node's list */
 };
 
+/* A uniform r = m 2^-53 (m a 53-bit integer) is below c exactly when m is
+ * below ceil(c 2^53) (the scaling is exact); so the strain draw compares
+ * integers, with the same outcome as comparing r with c (NaN or c <= 0:
+ * never below; c >= 1: always). */
+__device__ __forceinline__ uint64_t strain_threshold(double c) {
+  const double x = c * 0x1.0p53;
+  if (!(x > 0.0)) return 0;
+  if (x >= 0x1.0p53) return (uint64_t)1 << 53;
+  return (uint64_t)ceil(x);
+}
+
 /* Cumulative relative FOI that the strain draw compares against
  * (model.py:1127-1135), formed with the same operations in the same order. */
-__device__ __forceinline__ void sel_strain_cum(const DevWorld& W, const DevRep* rp, int g, double* cum) {
+__device__ __forceinline__ void sel_strain_cum(const DevWorld& W, const DevRep* rp, int g, uint64_t* thr) {
   double p[LPG_MAX_STRAINS], q[LPG_MAX_STRAINS];
   double totalp = 0.0;
   const int ns = rp->ns;
@@ -1690,7 +1701,7 @@ __device__ __forceinline__ void sel_strain_cum(const DevWorld& W, const DevRep* 
 #pragma unroll
   for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
     if (k < ns) c = c + q[k];
-    cum[k] = c;
+    thr[k] = strain_threshold(c);
   }
 }
 
@@ -1928,14 +1939,14 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
   /* strain thresholds of the selection (sel_strain_cum's values), the
    * divisions on their own lanes */
   const double qk = pk / total_p;
-  double cum[LPG_MAX_STRAINS];
+  uint64_t thr[LPG_MAX_STRAINS];
   {
     double c = 0.0;
 #pragma unroll
     for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
       const double q = __shfl_sync(FULLMASK, qk, k);
       if (k < ns) c = c + q;
-      cum[k] = c;
+      thr[k] = strain_threshold(c);
     }
   }
   __syncwarp();
@@ -1979,7 +1990,7 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
     N.seed = rp->seed;
     N.T = Tw;
 #pragma unroll
-    for (int k = 0; k < LPG_MAX_STRAINS; ++k) N.cum[k] = cum[k];
+    for (int k = 0; k < LPG_MAX_STRAINS; ++k) N.thr[k] = thr[k];
     N.a = rp->chunk_base + st[i];
     N.n = st[i + 1] - st[i];
     N.i = i;
@@ -2254,7 +2265,7 @@ __device__ __forceinline__ uint32_t locate_team(const DevWorld& W, const Team& t
 /* The exposure of an agent that a target has claimed: strain by relative
  * FOI (model.py:1127-1145), its first step in E, and every susceptible total
  * but the sub-block's (sub_now: that one too).  Returns its weight. */
-__device__ __forceinline__ uint64_t expose_claimed(DevWorld& W, int64_t pos, int g, const SelInfo& N, double r,
+__device__ __forceinline__ uint64_t expose_claimed(DevWorld& W, int64_t pos, int g, const SelInfo& N, uint64_t r53,
                                                    int8_t et, float risk, bool sub_now) {
   const int G = W.G;
   const int64_t cid = pos / LPG_CHUNK;
@@ -2262,7 +2273,7 @@ __device__ __forceinline__ uint64_t expose_claimed(DevWorld& W, int64_t pos, int
   bool found = false;
 #pragma unroll
   for (int k = 0; k < LPG_MAX_STRAINS; ++k)
-    if (!found && k < N.ns && r < N.cum[k]) {
+    if (!found && k < N.ns && r53 < N.thr[k]) {
       s = k;
       found = true;
     }
@@ -2300,7 +2311,7 @@ __device__ __forceinline__ bool claim(DevWorld& W, uint32_t hit, int g, const Se
   uint32_t* wp = reinterpret_cast<uint32_t*>(W.ds + (pos & ~3LL));
   const int sh = (int)(pos & 3) * 8;
   uint32_t old = *(volatile uint32_t*)wp;
-  const double r = lpg_u01(N.seed, LPG_P_STRAIN, N.t, ref, 0, 0);
+  const uint64_t r53 = lpg_u53(N.seed, LPG_P_STRAIN, N.t, ref, 0, 0);
   bool won = false;
   while (((old >> sh) & 0xffu) == 0) {
     const uint32_t nw = (old & ~(0xffu << sh)) | (1u << sh);
@@ -2312,7 +2323,7 @@ __device__ __forceinline__ bool claim(DevWorld& W, uint32_t hit, int g, const Se
     old = prev;
   }
   if (!won) return false;
-  const uint64_t w = expose_claimed(W, pos, g, N, r, et, risk, true);
+  const uint64_t w = expose_claimed(W, pos, g, N, r53, et, risk, true);
   if (w_out) *w_out = w;
   return true;
 }
@@ -2331,7 +2342,7 @@ __device__ __forceinline__ bool claim0(DevWorld& W, uint32_t hit, uint32_t word,
   uint32_t* wp = reinterpret_cast<uint32_t*>(W.ds + (pos & ~3LL));
   const int sh = (int)(pos & 3) * 8;
   uint32_t old = word;
-  const double r = lpg_u01(N.seed, LPG_P_STRAIN, N.t, ref, 0, 0);
+  const uint64_t r53 = lpg_u53(N.seed, LPG_P_STRAIN, N.t, ref, 0, 0);
   bool won = false;
   while (((old >> sh) & 0xffu) == 0) {
     const uint32_t nw = (old & ~(0xffu << sh)) | (LPG_DS_CLAIMED << sh);
@@ -2343,7 +2354,7 @@ __device__ __forceinline__ bool claim0(DevWorld& W, uint32_t hit, uint32_t word,
     old = prev;
   }
   if (!won) return false;
-  *w_out = expose_claimed(W, pos, g, N, r, et, risk, false);
+  *w_out = expose_claimed(W, pos, g, N, r53, et, risk, false);
   return true;
 }
 
@@ -2416,8 +2427,9 @@ __device__ __forceinline__ int team_first_above(const Team& tm, const int64_t* o
 /* Round 0's targets for a team size T: each located on the frozen CDF and
  * claimed at once by the team's first lane, which keeps its first two
  * claims in registers and stores later ones' slots in hits[q]; then the
- * grid barrier, after which the claimers settle their agents (state 1,
- * sub-block weight).  Returns false when the barrier's wait ran out. */
+ * grid barrier, after which the claims are settled (state 1, sub-block
+ * weight): the first two by the first lane, the later ones spread over the
+ * team's lanes.  Returns false when the barrier's wait ran out. */
 template <int T>
 __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs, const SelInfo* info, int64_t K) {
   const int G = W.G;
@@ -2469,10 +2481,11 @@ __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs,
   if (tm.l == 0) {
     claim0_finish(W, h0, w0);
     claim0_finish(W, h1, w1);
-    for (int64_t q = q0 + 2 * nteams; q < K; q += nteams) {
-      const uint32_t h = W.hits[q];
-      if (h != LPG_NONE) claim0_finish(W, h, fix_risk(W.risk[h]));
-    }
+  }
+  /* the team's later claims, lane l taking its turns 2 + l, 2 + l + T, ... */
+  for (int64_t q = q0 + (2 + (int64_t)tm.l) * nteams; q < K; q += (int64_t)T * nteams) {
+    const uint32_t h = W.hits[q];
+    if (h != LPG_NONE) claim0_finish(W, h, fix_risk(W.risk[h]));
   }
   return true;
 }
@@ -2491,7 +2504,7 @@ __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs,
  * oracle, so the CDF targets are the same whatever runs them, and which of
  * two targets on one agent claims it changes nothing (its strain draw is
  * keyed by the agent). */
-__global__ void __launch_bounds__(256) k_sel_round0(DevWorld W) {
+__global__ void __launch_bounds__(256, 3) k_sel_round0(DevWorld W) {
   pdl_begin();
   const int R = W.n_reps, G = W.G;
   int any = 0;
@@ -2651,7 +2664,7 @@ __device__ __noinline__ void sel_rounds(DevWorld& W) {
             s_N.seed = rp->seed;
             s_N.t = rp->cur_t;
             s_N.ns = rp->ns;
-            sel_strain_cum(W, rp, g, s_N.cum);
+            sel_strain_cum(W, rp, g, s_N.thr);
           }
         }
       }
