@@ -136,7 +136,7 @@ def sweep_b_bytes(params, t):
 
 # DRAM bytes ncu measured per unit of counted work, by kernel: (counter,
 # bytes per unit, bytes per launch besides), and where they were measured.
-NCU_TRAFFIC_PER_UNIT = {"k_select": ("sel_targets", 1071.0, 0.0)}
+NCU_TRAFFIC_PER_UNIT = {"k_select": ("sel_targets", 950.0, 0.0)}
 NCU_TRAFFIC_SOURCE = {
     "k_select": "ncu DRAM read+write of k_sel_round0 + k_sel_rounds per target located, "
                 "on tick 151 of the 5e7-agent Nigeria-like case, times the targets of the timed ticks",
@@ -166,6 +166,12 @@ NCU_TRAFFIC_SOURCE = {
 #   k_node_mix: the network rows (nodes^2 x 16 B per simulation, two 8-byte
 #     fixed-point parts per entry) and, per chunk of the population, its list
 #     entry, weight and prefix (20 B).
+#   k_node_tx: per node its population inputs (last row, births, deaths:
+#     12 B), seasonality, R0 scalar and row sum (24 B), per strain the
+#     infectivity total and incoming infectivity (16 B x 3), susceptible
+#     weight and count (12 B) read; population, per-strain probability
+#     (4 + 8 x 3 B), count, target totals (24 B) and the selection record
+#     (96 B) written: 248 B.
 SWEEP_INDEX_B, SWEEP_DUE_B, SWEEP_EVT_B, SWEEP_DOD_B, QUEUE_ENTRY_B = 4.0, 128.0, 516.0, 516.0, 8.0
 DUE_ITEM_B = 8.0
 DSQ_ENTRY_B = 8.0 + 9.0 + 8.0
@@ -174,6 +180,7 @@ SEL_TARGET_B = 12.0 + 128.0 + 128.0 + 512.0
 SEL_CLAIM_B = 15.0
 NODE_TX_CHUNK_B = 20.0
 NODE_TX_NET_B = 16.0  # a network entry in its two fixed-point parts
+NODE_TX_NODE_B = 248.0
 RI_INDEX_B, RI_DUE_B = 4.0, 128.0 * 12.0 + 4.0
 
 
@@ -210,6 +217,7 @@ def kernel_alg_bytes(params, ticks, cnt, work, new_exposed):
         "k_evb": EVB_ENTRY_B * work["queue_rs"],
         "k_select": SEL_TARGET_B * work["sel_targets"] + SEL_CLAIM_B * float(new_exposed),
         "k_node_mix": node_mix,
+        "k_node_tx": sum(len(ticks) * p["n_nodes"] * NODE_TX_NODE_B for p in plist),
     }
     return out
 

@@ -1035,7 +1035,7 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sweep_due, LPG_SWEEP_BLOCK, 0));
   h->sweep0_blocks = std::min(1024, std::max(1, occ) * h->sm_count);
   occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_due, 256, 0));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, R > 1 && R <= LPG_DUE_FLAT ? k_due<true> : k_due<false>, 256, 0));
   h->due_blocks = std::max(1, occ) * h->sm_count;
   occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sel_round0, 256, 0));
@@ -1085,7 +1085,10 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
   switch (k) {
     case 0: CK(launch_pdl(k_begin, dim3(R), dim3(1024), 0, st, W)); break;
     case 1: CK(launch_pdl(k_newborns, dim3(h->newborn_blocks, R), dim3(256), 0, st, W)); break;
-    case 2: CK(launch_pdl(k_due, dim3(h->due_blocks), dim3(256), 0, st, W)); break;
+    case 2:
+      if (R > 1 && R <= LPG_DUE_FLAT) CK(launch_pdl(k_due<true>, dim3(h->due_blocks), dim3(256), 0, st, W));
+      else CK(launch_pdl(k_due<false>, dim3(h->due_blocks), dim3(256), 0, st, W));
+      break;
     case 3: CK(launch_pdl(k_sweep_due, dim3(h->sweep0_blocks), dim3(LPG_SWEEP_BLOCK), 0, st, W)); break;
     case 4: CK(launch_pdl(k_seed, dim3(R), dim3(1024), 0, st, W)); break;
     case 5: CK(launch_pdl(k_sweep_rs, dim3(h->sweep_blocks), dim3(LPG_SWEEP_BLOCK), LPG_SWEEP_SMEM, st, W)); break;

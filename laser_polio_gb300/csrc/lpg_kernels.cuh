@@ -776,13 +776,112 @@ __device__ __forceinline__ int32_t sub8_min(int32_t x) {
  * W.due as (sub-block | simulation << 32 | what << 48; what: 1 event, 2
  * death), one global atomic per warp. */
 #define LPG_DUE_MAX 8192
+#define LPG_DUE_FLAT 256 /* replicates whose index entries k_due scans as one range */
+/* Due flags of 16 sub-blocks (4 index entries of 4) at tick t: 2 bits each
+ * (1 event, 2 death). */
+__device__ __forceinline__ uint32_t due_flags16(const int4* e, const int4* d, int t) {
+  uint32_t fl = 0;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int32_t ee[4] = {e[u].x, e[u].y, e[u].z, e[u].w}, dd[4] = {d[u].x, d[u].y, d[u].z, d[u].w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) fl |= ((ee[j] <= t ? 1u : 0u) | (dd[j] <= t ? 2u : 0u)) << (2 * (4 * u + j));
+  }
+  return fl;
+}
+/* FLAT: the instance for a batch of replicates (the host launches it when
+ * there are 2 to LPG_DUE_FLAT of them); the other scans one replicate after
+ * another, with fewer registers. */
+template <bool FLAT>
 __global__ void __launch_bounds__(256) k_due(DevWorld W) {
   pdl_begin();
   const int lane = threadIdx.x & 31;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x;
   const int4 none = make_int4(LPG_NO_DOD, LPG_NO_DOD, LPG_NO_DOD, LPG_NO_DOD);
-  for (int r = 0; r < W.n_reps; ++r) {
+  const int R = W.n_reps;
+  if constexpr (FLAT) {
+    /* the replicates' index entries as one range (a batch of small
+     * simulations is one pass, not one pass each): per replicate its first
+     * entry in the range, sub-block base, tick and which indexes it reads */
+    __shared__ int64_t s_off[LPG_DUE_FLAT + 1], s_sb0[LPG_DUE_FLAT];
+    __shared__ int32_t s_t[LPG_DUE_FLAT];
+    __shared__ uint32_t s_what[LPG_DUE_FLAT];
+    int64_t nq = 0;
+    if (threadIdx.x < R) {
+      const DevRep* rp = &W.reps[threadIdx.x];
+      const uint32_t what = rp->active ? ((rp->comps & LPG_COMP_DS) ? 1u : 0u) | (rp->vd_tick ? 2u : 0u) : 0u;
+      if (what) nq = (int64_t)rp->used_chunks * (LPG_NSUB / 4);
+      s_sb0[threadIdx.x] = (int64_t)rp->chunk_base * LPG_NSUB;
+      s_t[threadIdx.x] = rp->cur_t;
+      s_what[threadIdx.x] = what;
+      if (blockIdx.x == 0 && nq)
+        atomicAdd(&W.ctr[LPG_CTR_SWEEP_INDEX], (unsigned long long)(nq * 4 * ((what & 1u) + (what >> 1))));
+    }
+    int64_t total;
+    const int64_t ex = block_excl_scan(nq, &total);
+    if (threadIdx.x < R) s_off[threadIdx.x] = ex;
+    if (threadIdx.x == 0) s_off[R] = total;
+    __syncthreads();
+    const int64_t nall = total;
+    for (int64_t q0 = gtid; q0 - lane < nall; q0 += 4 * gsz) {
+      int4 e[4], d[4];
+      int rr[4];
+      int64_t ql[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t q = q0 + u * gsz;
+        e[u] = none;
+        d[u] = none;
+        rr[u] = 0;
+        ql[u] = 0;
+        if (q < nall) {
+          /* the replicate whose entries hold q: the last with s_off <= q */
+          int lo = 0, hi = R;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_off[mid] <= q) lo = mid; else hi = mid - 1;
+          }
+          const int r = lo;
+          rr[u] = r;
+          ql[u] = q - s_off[r];
+          const uint32_t what = s_what[r];
+          if (what & 1u) e[u] = __ldcg(reinterpret_cast<const int4*>(W.sub_evt + s_sb0[r]) + ql[u]);
+          if (what & 2u) d[u] = __ldcg(reinterpret_cast<const int4*>(W.sub_dod + s_sb0[r]) + ql[u]);
+        }
+      }
+      uint32_t fl = 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int32_t t = s_t[rr[u]];
+        const int32_t ee[4] = {e[u].x, e[u].y, e[u].z, e[u].w}, dd[4] = {d[u].x, d[u].y, d[u].z, d[u].w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) fl |= ((ee[j] <= t ? 1u : 0u) | (dd[j] <= t ? 2u : 0u)) << (2 * (4 * u + j));
+      }
+      const uint32_t nf = __popc((fl | (fl >> 1)) & 0x55555555u);
+      uint32_t x = nf;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULLMASK, x, o);
+        if (lane >= o) x += y;
+      }
+      const uint32_t tot = __shfl_sync(FULLMASK, x, 31);
+      if (tot == 0) continue;
+      uint32_t base = 0;
+      if (lane == 31) base = atomicAdd(W.due_n, tot);
+      uint32_t at = __shfl_sync(FULLMASK, base, 31) + x - nf;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const uint32_t f = (fl >> (2 * (4 * u + j))) & 3u;
+          if (f)
+            W.due[at++] = (uint64_t)(s_sb0[rr[u]] + 4 * ql[u] + j) | ((uint64_t)rr[u] << 32) | ((uint64_t)f << 48);
+        }
+    }
+    return;
+  } else {
+  for (int r = 0; r < R; ++r) {
     const DevRep* rp = &W.reps[r];
     if (!rp->active) continue;
     const bool dsq = (rp->comps & LPG_COMP_DS) != 0, vd = rp->vd_tick != 0;
@@ -799,14 +898,7 @@ __global__ void __launch_bounds__(256) k_due(DevWorld W) {
         e[u] = (dsq && q < nq) ? __ldcg(reinterpret_cast<const int4*>(W.sub_evt + sb0) + q) : none;
         d[u] = (vd && q < nq) ? __ldcg(reinterpret_cast<const int4*>(W.sub_dod + sb0) + q) : none;
       }
-      uint32_t fl = 0; /* 2 bits per entry, 16 entries */
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int32_t ee[4] = {e[u].x, e[u].y, e[u].z, e[u].w}, dd[4] = {d[u].x, d[u].y, d[u].z, d[u].w};
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-          fl |= ((ee[j] <= t ? 1u : 0u) | (dd[j] <= t ? 2u : 0u)) << (2 * (4 * u + j));
-      }
+      const uint32_t fl = due_flags16(e, d, t);
       const uint32_t nf = __popc((fl | (fl >> 1)) & 0x55555555u);
       uint32_t x = nf;
 #pragma unroll
@@ -827,6 +919,7 @@ __global__ void __launch_bounds__(256) k_due(DevWorld W) {
           if (f) W.due[at++] = (uint64_t)(sb0 + 4 * (q0 + u * gsz) + j) | ((uint64_t)r << 32) | ((uint64_t)f << 48);
         }
     }
+  }
   }
 }
 
