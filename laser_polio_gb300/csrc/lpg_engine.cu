@@ -1093,8 +1093,14 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 4: CK(launch_pdl(k_seed, dim3(R), dim3(1024), 0, st, W)); break;
     case 5: CK(launch_pdl(k_sweep_rs, dim3(h->sweep_blocks), dim3(LPG_SWEEP_BLOCK), LPG_SWEEP_SMEM, st, W)); break;
     case 6: CK(launch_pdl(k_evb, dim3(h->evb_blocks), dim3(256), 0, st, W, h->sweep_blocks)); break;
-    case 7: CK(launch_pdl(k_node_mix, dim3(G), dim3(LPG_NODE_MIX_THREADS), 0, st, W)); break;
-    case 8: CK(launch_pdl(k_node_tx, dim3(G), dim3(LPG_NODE_TX_THREADS), 0, st, W)); break;
+    case 7:
+      if (G > LPG_NODE_BATCH_MIN_PER_SM * h->sm_count) CK(launch_pdl(k_node_mix<1>, dim3(G), dim3(64), 0, st, W));
+      else CK(launch_pdl(k_node_mix<LPG_NODE_MIX_WARPS>, dim3(G), dim3(LPG_NODE_MIX_THREADS), 0, st, W));
+      break;
+    case 8:
+      if (G > LPG_NODE_BATCH_MIN_PER_SM * h->sm_count) CK(launch_pdl(k_node_tx_lanes, dim3((G + 127) / 128), dim3(128), 0, st, W));
+      else CK(launch_pdl(k_node_tx, dim3(G), dim3(LPG_NODE_TX_THREADS), 0, st, W));
+      break;
     case 9: {
       /* cooperative: its CTAs meet at a grid barrier, so all must be resident */
       void* args[] = {&W};

@@ -1748,11 +1748,17 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
 /* six CTAs of the node step per SM (at most 170 registers a thread): one
  * wave covers 912 nodes, so a 774-node tick needs no second wave */
 #define LPG_NODE_TX_MIN_BLOCKS 6
-/* the mixing step: four warps of products and sums, one warp for the
- * node's chunk prefix; six CTAs per SM (at most 68 registers a thread) */
+/* the mixing step: MW warps of products and sums, one warp for the node's
+ * chunk prefix.  MW = 4 for a simulation of hundreds of nodes (six CTAs per
+ * SM, at most 68 registers a thread: 774 nodes in one wave); MW = 1 for a
+ * batch of thousands of small nodes, where more CTAs a wave count more than
+ * more warps a node. */
 #define LPG_NODE_MIX_WARPS 4
 #define LPG_NODE_MIX_THREADS (32 * (LPG_NODE_MIX_WARPS + 1))
 #define LPG_NODE_MIX_MIN_BLOCKS 6
+/* the node steps switch to their batch forms above this many nodes (six
+ * CTAs of the per-node kernels per SM: more would take a second wave) */
+#define LPG_NODE_BATCH_MIN_PER_SM 6
 
 struct SelInfo {
   uint64_t seed;
@@ -1834,16 +1840,17 @@ __device__ __forceinline__ void warp_chunk_prefix(const DevWorld& W, const int32
  * three-word accumulators, one conversion (lpg_mix_value) into inck; an
  * exact sum does not depend on how the threads split it.  The fifth warp
  * forms the node-local chunk prefix (exact in integers) meanwhile. */
-__global__ void __launch_bounds__(LPG_NODE_MIX_THREADS, LPG_NODE_MIX_MIN_BLOCKS) k_node_mix(DevWorld W) {
+template <int MW>
+__global__ void __launch_bounds__(32 * (MW + 1), MW == 4 ? LPG_NODE_MIX_MIN_BLOCKS : 16) k_node_mix(DevWorld W) {
   pdl_begin();
   const int g = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __shared__ uint64_t s_mix[LPG_NODE_MIX_WARPS][LPG_MAX_STRAINS][6]; /* per warp: A, R words */
+  __shared__ uint64_t s_mix[MW][LPG_MAX_STRAINS][6]; /* per warp: A, R words */
   if (g >= W.G) return;
   const DevRep* rp = &W.reps[W.node_rep[g]];
   if (!rp->active || !(rp->comps & LPG_COMP_TX)) return;
   const int i = g - rp->node_base, n = rp->n_nodes, ns = rp->ns, G = W.G, nb = rp->node_base;
-  if (wid == LPG_NODE_MIX_WARPS) {
+  if (wid == MW) {
     const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
     const int32_t a = st[i], nch = st[i + 1] - st[i];
     warp_chunk_prefix(W, W.node_chunks[rp->csr_cur] + rp->chunk_base + a, nch, W.cpref + rp->chunk_base + a);
@@ -1851,9 +1858,8 @@ __global__ void __launch_bounds__(LPG_NODE_MIX_THREADS, LPG_NODE_MIX_MIN_BLOCKS)
   }
   /* qrow[ii] = network[ii][i] as (hi 2^-62, lo 2^-120), lpg_net_split */
   const ulonglong2* qrow = reinterpret_cast<const ulonglong2*>(rp->netq_t) + (int64_t)i * n;
-  constexpr int NT = 32 * LPG_NODE_MIX_WARPS;
-  constexpr int PER = 7; /* source nodes a thread takes per pass: one pass up to 896 nodes */
-  static_assert(PER * NT >= 774, "one pass for a 774-node simulation");
+  constexpr int NT = 32 * MW;
+  constexpr int PER = 7; /* source nodes a thread takes per pass: PER x NT nodes a pass */
   /* per strain: A = sum B hi and R = sum B lo, three words each, exact;
    * one strain at a time (six accumulators live), the network entries of
    * the pass loaded once for all strains */
@@ -1912,7 +1918,7 @@ __global__ void __launch_bounds__(LPG_NODE_MIX_THREADS, LPG_NODE_MIX_MIN_BLOCKS)
     const int k = threadIdx.x;
     uint64_t x0 = 0, x1 = 0, x2 = 0, y0 = 0, y1 = 0, y2 = 0;
 #pragma unroll
-    for (int w4 = 0; w4 < LPG_NODE_MIX_WARPS; ++w4) {
+    for (int w4 = 0; w4 < MW; ++w4) {
       acc3_add(x0, x1, x2, s_mix[w4][k][0], s_mix[w4][k][1], s_mix[w4][k][2]);
       acc3_add(y0, y1, y2, s_mix[w4][k][3], s_mix[w4][k][4], s_mix[w4][k][5]);
     }
@@ -2082,6 +2088,128 @@ __global__ void __launch_bounds__(LPG_NODE_TX_THREADS, LPG_NODE_TX_MIN_BLOCKS) k
     SelInfo N;
     N.seed = rp->seed;
     N.T = Tw;
+#pragma unroll
+    for (int k = 0; k < LPG_MAX_STRAINS; ++k) N.thr[k] = thr[k];
+    N.a = rp->chunk_base + st[i];
+    N.n = st[i + 1] - st[i];
+    N.i = i;
+    N.t = t;
+    N.ns = ns;
+    N.csr = rp->csr_cur;
+    reinterpret_cast<SelInfo*>(W.sel_info)[g] = N;
+    W.ksel[g] = size;
+  }
+  if (size > 0) rp->any_demand = 1;
+}
+
+/* k_node_tx for a batch of thousands of small nodes: one node a thread,
+ * the same operations in the same order (strains one after another; the
+ * negative binomial's gamma variate drawn in line, from the same stream
+ * positions).  A double-precision warp instruction costs the same for one
+ * lane or 32, so here one serves 32 nodes: a batch's nodes take one wave
+ * where a CTA a node takes ten. */
+__global__ void __launch_bounds__(128) k_node_tx_lanes(DevWorld W) {
+  pdl_begin();
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= W.G) return;
+  DevRep* rp = &W.reps[W.node_rep[g]];
+  W.ksel[g] = 0;
+  if (!rp->active) return;
+  const int i = g - rp->node_base, n = rp->n_nodes, ns = rp->ns, t = rp->cur_t, G = W.G;
+  int32_t pop_t = 0;
+  if (rp->comps & LPG_COMP_VD) {
+    pop_t = RES(rp, RS_POP, t - 1)[i];
+    if (rp->vd_tick) pop_t = pop_t + W.ev[(int64_t)EV_BIRTHS * G + g] - W.ev[(int64_t)EV_DEATHS * G + g];
+    RES(rp, RS_POP, t)[i] = pop_t;
+  } else {
+    pop_t = RES(rp, RS_POP, t)[i];
+  }
+  W.size[g] = 0;
+  W.uniq[g] = 0;
+  if (!(rp->comps & LPG_COMP_TX)) return;
+  const double seas = rp->seas[t], r0s = rp->r0s[i], rowsum = rp->rowsum[i];
+  const uint64_t sw = W.sw[g];
+  const int64_t sc = W.tot[(int64_t)TT_S * G + g];
+  uint64_t bb[LPG_MAX_STRAINS];
+  double inc[LPG_MAX_STRAINS];
+#pragma unroll
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+    bb[k] = k < ns ? W.bb[(int64_t)k * G + g] : 0;
+    inc[k] = k < ns ? W.inck[(int64_t)k * G + g] : 0.0;
+  }
+  double* rr = rp->rec ? rp->rec + ((int64_t)t * n + i) * (3 + ns) : nullptr;
+  if (rr) {
+    rr[0] = (double)sw * 0x1.0p-24;
+    rr[1] = (double)pop_t;
+  }
+  /* incoming infectivity, beta, rate and probability of each strain
+   * (model.py:1327-1363), and their sum in strain order */
+  const double denom = (double)(pop_t > 1 ? pop_t : 1);
+  double p[LPG_MAX_STRAINS];
+  double total_p = 0.0;
+  bool local_zero = true;
+#pragma unroll
+  for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+    p[k] = 0.0;
+    if (k < ns) {
+      const double bpre = (double)bb[k] * 0x1.0p-40;
+      if (rr) rr[3 + k] = bpre;
+      if (bb[k] != 0) local_zero = false;
+      double beta = bpre + (inc[k] - bpre * rowsum);
+      beta = (beta * seas) * r0s;
+      const double rate = beta / denom;
+      double pk = -lpg_expm1(-rate);
+      if (!(pk > 0.0)) pk = 0.0;
+      p[k] = pk;
+      W.prob[(int64_t)k * G + g] = pk;
+      total_p = total_p + pk;
+    }
+  }
+  /* strain thresholds of the selection (sel_strain_cum's values) */
+  uint64_t thr[LPG_MAX_STRAINS];
+  {
+    double c = 0.0;
+#pragma unroll
+    for (int k = 0; k < LPG_MAX_STRAINS; ++k) {
+      if (k < ns) c = c + p[k] / total_p;
+      thr[k] = strain_threshold(c);
+    }
+  }
+  lpg_stream sm;
+  lpg_stream_init(&sm, rp->seed, LPG_P_TXCOUNT, t, (uint64_t)i, 0);
+  const double srisk = (double)sw * 0x1.0p-24;
+  const double exposure = srisk * total_p;
+  if (rr) rr[2] = exposure;
+  int64_t total = 0;
+  if (!(exposure > 0.0)) {
+    total = 0;
+  } else if (local_zero) {
+    if (rp->zi >= 1.0) {
+      total = 0;
+    } else {
+      double mean = exposure / (1.0 - rp->zi);
+      double r = (double)rp->nb_r;
+      double pp = r / (r + mean);
+      double u = lpg_next(&sm);
+      if (u < rp->zi) {
+        total = 0;
+      } else if (rp->nb_r >= 1) {
+        const double gam = lpg_gamma_mt(&sm, rp->nb_d, rp->nb_c, 1.0); /* lpg_negbinom_dc */
+        total = lpg_poisson(&sm, gam * ((1.0 - pp) / pp));
+      } else {
+        total = lpg_negbinom(&sm, r, pp);
+      }
+    }
+  } else {
+    total = lpg_poisson(&sm, exposure);
+  }
+  const int64_t size = total < sc ? total : sc;
+  W.size[g] = size;
+  if (size > 0 && sw > 0) {
+    const int32_t* st = W.node_chunk_start[rp->csr_cur] + rp->csr_base;
+    SelInfo N;
+    N.seed = rp->seed;
+    N.T = sw;
 #pragma unroll
     for (int k = 0; k < LPG_MAX_STRAINS; ++k) N.thr[k] = thr[k];
     N.a = rp->chunk_base + st[i];

@@ -219,6 +219,36 @@ def test_parity_batched_replicates():
     h.close()
 
 
+def test_parity_batch_of_many_small_nodes():
+    """A batch whose nodes outnumber one wave of the per-node kernels (more
+    than six a GB300 SM: 912): the node steps run in their batch forms (the
+    one-warp mixing, the lane-per-node draws), and each replicate still
+    equals its own oracle run."""
+    from laser_polio_gb300._lib import Handle
+
+    sims = [synthetic.nigeria_like(n_agents=60_000, n_nodes=120, dur=60, seed=20 + k) for k in range(8)]
+    sims.append(synthetic.zamfara_like(n_agents=40_000, dur=60, seed=29))
+    snaps_o = [snapshot(s) for s in sims]
+    snaps_g = [snapshot(s) for s in sims]
+    assert sum(spec.desc.n_nodes for spec, _, _ in snaps_g) > 912
+    states_o = [run_spec_oracle(spec, cols, res, s.nt - 1) for s, (spec, cols, res) in zip(sims, snaps_o)]
+    h = Handle([spec.desc for spec, _, _ in snaps_g])
+    for i, (_, cols, _) in enumerate(snaps_g):
+        h.bind_columns(i, cols)
+    h.start()
+    h.step(max(s.nt for s in sims) - 1)
+    h.sync()
+    for i, ((_, cols_o, res_o), (_, cols_g, res_g), so) in enumerate(zip(snaps_o, snaps_g, states_o)):
+        sg = h.state(i)
+        assert (sg.t, sg.stopped, sg.count, sg.error) == (so.t, so.stopped, so.count, so.error), i
+        h.read_results(i, res_g)
+        h.read_columns(i, cols_g)
+        assert_same(res_o, res_g, f"replicate {i} result")
+        assert_same(cols_o, cols_g, f"replicate {i} column", count=so.count)
+    assert sum(res_o["new_exposed"].sum() for _, _, res_o in snaps_o) > 0
+    h.close()
+
+
 def test_work_counters_are_consistent():
     """The device work counters (lpg_read_counters) start at zero, are reset
     by turning profiling on, and agree with the results they stand behind."""
