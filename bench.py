@@ -80,6 +80,11 @@ def parse():
                     help="instead: R calibration replicates (730 ticks) batched in one handle vs run one by one")
     ap.add_argument("--incidence", type=int, default=0, metavar="T",
                     help="instead: loss and gradient of the expected incidence over T ticks (the adjoint)")
+    ap.add_argument("--incidence-data", default="replay", choices=["replay", "synthetic"],
+                    help="the adjoint's aggregates: recorded by Nigeria-scale forward runs, or seeded numpy")
+    ap.add_argument("--continental", action="store_true",
+                    help="instead: the 4000-node, 1e9-agent workload through the user's path (365 ticks); "
+                         "with --incidence, the adjoint on seeded aggregates of its shapes")
     ap.add_argument("--export", action="store_true",
                     help="instead: save_sim_results' CSV of a Nigeria-scale results table (host only)")
     return ap.parse_args()
@@ -485,6 +490,103 @@ def api_run(args, dev):
     return out
 
 
+def continental_arm(args):
+    """The continental workload through the user's path: 4000 nodes, 1e9
+    agents (capacity +30%), node populations lognormal(ln 2.5e5, 0.9), dense
+    gravity network over a 5000 km square, RI and SIA as the Nigeria-scale
+    workload, 365 ticks.  SEIR_ABM(pars) with the five components (agent
+    table initialised on the device), then the steps of run(): start (bind
+    and layout), the first W ticks with per-kernel profiling, the remaining
+    ticks between CUDA events on the engine's stream, results and columns
+    copied into the sim.  value: agent-ticks/s of the timed ticks; e2e: all
+    ticks over the wall time of construction, start, ticks and copy-back."""
+    import torch
+
+    import laser_polio_gb300 as lp
+    from laser_polio_gb300 import synthetic
+    from laser_polio_gb300.model import _engine_of
+
+    agents = int(args.agents if args.agents != 2.2e8 else 1e9)
+    nodes = args.nodes if args.nodes != 774 else 4000
+    pars, immun, rng = synthetic.continental_pars(n_agents=agents, n_nodes=nodes, dur=365, seed=args.seed)
+    prev = np.zeros(nodes, np.int64)
+    prev[rng.choice(nodes, size=2, replace=False)] = 10
+    pars.update({"init_immun": list(np.asarray(immun, float)), "init_prev": list(prev), "age_pyramid_path": None})
+    W = max(3, args.warmup)
+    free0 = torch.cuda.mem_get_info()[0]
+    with ClockSampler(0) as clocks:
+        clocks.wait_ready()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim = lp.SEIR_ABM(lp.PropertySet(pars))
+        sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.RI_ABM, lp.SIA_ABM, lp.Transmission_ABM]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        eng = _engine_of(sim)
+        eng._ensure_started()
+        h = eng.handle
+        h.sync()
+        t2 = time.perf_counter()
+        used = free0 - torch.cuda.mem_get_info()[0]
+        stream = torch.cuda.ExternalStream(h.cuda_stream())
+        h.set_profiling(True)
+        h.step(W)
+        h.sync()
+        prof = h.profile()
+        h.set_profiling(False)
+        n_rest = sim.nt - 1 - W
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = h.kernel_launches()
+        t3 = time.perf_counter()
+        e0.record(stream)
+        h.step(n_rest)
+        e1.record(stream)
+        h.sync()
+        t4 = time.perf_counter()
+        launches = h.kernel_launches() - l0
+        ms = e0.elapsed_time(e1)
+        st = h.state(0)
+        sim.t, sim.should_stop = st.t, bool(st.stopped)
+        eng._finish()
+        torch.cuda.synchronize()
+        t5 = time.perf_counter()
+    births = sim.results.births.sum(axis=1).astype(np.int64)
+    cnt = int(np.sum(pars["init_pop"])) + np.cumsum(births)
+    at_timed = float(cnt[W + 1 : W + 1 + n_rest].sum())
+    at_all = float(cnt[1 : sim.nt].sum())
+    wall = t5 - t0
+    tot = sum(v[0] for v in prof.values()) or 1.0
+    kernels = {k: {"ms_per_launch": v[0] / max(1, v[1]), "launches": v[1], "share": v[0] / tot}
+               for k, v in prof.items() if v[1]}
+    line = {
+        "metric": f"agent-ticks/s ({nodes} nodes, {agents:.2g} agents, full agent step)",
+        "value": at_timed / (ms / 1e3), "unit": "agent-ticks/s", "n_gpus": 1, "steps": n_rest, "warmup": W,
+        "ms_per_step": ms / n_rest, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int8/int32 state, f64 node FOI",
+        "data": "synthetic (seeded, the continental workload's distributions; agent table drawn on the device)",
+        "config": {"workload": f"continental {nodes} nodes x {agents:.2g} agents, capacity +30%, "
+                               f"ticks {W + 1}-{sim.nt - 1} of a {sim.nt - 1}-tick run",
+                   "capacity": int(sim.people.capacity),
+                   "l2": "state columns far larger than L2 (no flush needed)"},
+        "e2e": {"value": at_all / wall, "unit": "agent-ticks/s", "ticks": sim.nt - 1, "seconds": wall,
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "phases_s": {"construct": t1 - t0, "start": t2 - t1, "profiled_ticks": t3 - t2,
+                             "ticks": t4 - t3, "copy_back": t5 - t4},
+                "path": "SEIR_ABM(pars); sim.components = [...]; the steps of run(), results and columns "
+                        "into the sim on the device"},
+        "device_bytes_after_start": used,
+        "gpu_launches": launches,
+        "kernels_first_ticks": kernels,
+        "new_exposed_total": int(sim.results.new_exposed.sum()),
+        "clocks": clocks.summary(),
+    }
+    eng.close()
+    del sim
+    print(json.dumps(line), flush=True)
+    if args.out:
+        Path(args.out).write_text(json.dumps(line, indent=1))
+
+
 def tick_kind(params, t):
     """plain / vd / vd+ri / sia ... : the components that act on tick t
     besides the every-tick ones."""
@@ -658,11 +760,88 @@ def batch_arm(args):
         Path(args.out).write_text(json.dumps(line, indent=1))
 
 
+def replay_inputs(args, T, dev):
+    """The expected-incidence map's inputs recorded by forward runs of the
+    engine at the Nigeria scale (args.agents agents, args.nodes nodes,
+    T ticks, births, RI and SIA on): one handle, two simulations of the same
+    agent table.  Simulation 0 runs at the base parameters (R0 14, seasonal
+    amplitude 0.4 peaking on day 180, gravity k 0.5) and records srisk,
+    beta and pop per transmission tick and node (lpg_record_aggregates):
+    these are the replayed aggregates.  Simulation 1 runs at perturbed
+    parameters (every agent's infectivity x1.1, amplitude 0.35, peak day 170,
+    k 0.6, r0 scalars x lognormal(0, 0.05)); its recorded expected exposures
+    are the target curve.  Returns (map inputs at the base parameters,
+    target [T, nodes], record of the runs), the record holding the largest
+    difference between the map's lam on simulation 0's aggregates and the
+    engine's own expected exposures, relative to the largest."""
+    import datetime
+    import torch
+
+    from laser_polio_gb300 import ops, synthetic
+    from laser_polio_gb300._lib import Handle
+    from laser_polio_gb300.core import gravity, row_normalizer
+    from laser_polio_gb300.engine import make_desc
+    from laser_polio_gb300.utils import seasonality_table
+
+    t0 = time.perf_counter()
+    pa, cols = synthetic.bundle("nigeria", n_agents=int(args.agents), n_nodes=args.nodes, dur=T, seed=args.seed)
+    G, ns, nt = pa["n_nodes"], pa["n_strains"], pa["nt"]
+    pops, dist = pa["pop0"].astype(np.float64), pa["distances"]
+    rng = np.random.default_rng(args.seed + 1)
+    dates = [datetime.date(2019, 1, 1) + datetime.timedelta(days=d) for d in range(nt)]
+    pb = dict(pa, seasonality=seasonality_table(dates, 0.35, 170),
+              r0_scalars=pa["r0_scalars"] * rng.lognormal(0.0, 0.05, G),
+              network=row_normalizer(gravity(pops, dist, 0.6, 1, 1, 2.0) / np.power(pops.sum(), 2.0), 0.2))
+    cols_b = dict(cols, daily_infectivity=(cols["daily_infectivity"] * np.float32(1.1)).astype(np.float32))
+    da, ka = make_desc(pa)
+    db, kb = make_desc(pb)
+    t_gen = time.perf_counter() - t0
+    h = Handle([da, db], device=dev)
+    try:
+        h.record_aggregates(0)
+        h.record_aggregates(1)
+        h.bind_columns(0, cols)
+        h.bind_columns(1, cols_b)
+        h.start()
+        h.sync()
+        stream = torch.cuda.ExternalStream(h.cuda_stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.step(nt - 1)
+        e1.record(stream)
+        assert h.sync_statuses() == [0, 0]
+        ms = e0.elapsed_time(e1)
+        agg = h.read_aggregates(0, nt, G, ns)
+        tgt = h.read_aggregates(1, nt, G, ns)["lam"]
+    finally:
+        h.close()
+    del cols, cols_b
+    ticks = slice(1, nt)  # no component runs on tick 0
+    doy = np.array([d.timetuple().tm_yday for d in dates], np.float64)
+    year = np.array([366.0 if (d.year % 4 == 0 and (d.year % 100 != 0 or d.year % 400 == 0)) else 365.0
+                     for d in dates])
+    inp = dict(srisk=agg["srisk"][ticks], beta=agg["beta"][ticks], pop=agg["pop"][ticks], doy=doy[ticks],
+               year=year[ticks], r0s=pa["r0_scalars"], R=1.0, amp=0.4, peak=180.0, pops=pops, dist=dist,
+               k=0.5, a=1.0, b=1.0, c=2.0, max_frac=0.2)
+    lam, _ = ops.expected_incidence(inp)
+    eng = agg["lam"][ticks]
+    rec = {"source": "recorded by the engine's forward runs (lpg_record_aggregates)",
+           "agents": int(pa["count"]), "nodes": G, "ticks": nt - 1, "simulations": 2,
+           "forward_ms": ms, "generate_s": t_gen,
+           "new_exposed_expected": float(eng.sum()), "target_expected": float(tgt[ticks].sum()),
+           "map_vs_engine_max_rel": float(np.max(np.abs(lam - eng)) / max(np.max(np.abs(eng)), 1e-300))}
+    return inp, tgt[ticks].copy(), rec
+
+
 def incidence_arm(args):
     """Loss and gradient of the expected incidence over T ticks of replayed
     Nigeria-scale aggregates (774 nodes, 3 strains), against a target curve
     from perturbed parameters: L = sum (log1p(lam) - log1p(target))^2 and its
-    gradient with respect to R, amp, peak, r0s and k, a, b, c.  One step = one
+    gradient with respect to R, amp, peak, r0s and k, a, b, c.  With
+    --incidence-data replay (the default) the aggregates and the target are
+    recorded by forward runs of the engine (replay_inputs); with synthetic,
+    seeded numpy aggregates of the same shapes stand in and the target is the
+    map at perturbed parameters.  One step = one
     evaluation on a resident plan (lpg_incidence_plan_eval: parameters up,
     loss and gradients down).  value: K evaluations between CUDA events on
     the plan's stream.  e2e: wall time from host arrays, the plan's one-time
@@ -674,11 +853,25 @@ def incidence_arm(args):
     from laser_polio_gb300 import ops, synthetic
 
     T = args.incidence
-    inp = synthetic.incidence_inputs(T=T, n_nodes=args.nodes, seed=args.seed)
-    G, S = inp["r0s"].shape[0], inp["beta"].shape[2]
-    rng = np.random.default_rng(args.seed + 1)
-    pert = dict(inp, R=1.1, amp=0.35, peak=170.0, k=0.6, r0s=inp["r0s"] * rng.lognormal(0.0, 0.05, G))
-    target, _ = ops.expected_incidence(pert)
+    replay = None
+    if args.incidence_data == "replay" and not args.continental:
+        inp, target, replay = replay_inputs(args, T, 0)
+        G, S = inp["r0s"].shape[0], inp["beta"].shape[2]
+    elif args.continental:
+        # the continental shapes: two recording runs of 1.3e9-slot tables would hold
+        # their host columns twice over, so seeded aggregates of those shapes stand in
+        inp = synthetic.incidence_inputs(T=T, n_nodes=args.nodes if args.nodes != 774 else 4000, n_agents=1e9,
+                                         seed=args.seed, mu=np.log(2.5e5), sigma=0.9, side_km=5000.0)
+        G, S = inp["r0s"].shape[0], inp["beta"].shape[2]
+        rng = np.random.default_rng(args.seed + 1)
+        pert = dict(inp, R=1.1, amp=0.35, peak=170.0, k=0.6, r0s=inp["r0s"] * rng.lognormal(0.0, 0.05, G))
+        target, _ = ops.expected_incidence(pert)
+    else:
+        inp = synthetic.incidence_inputs(T=T, n_nodes=args.nodes, seed=args.seed)
+        G, S = inp["r0s"].shape[0], inp["beta"].shape[2]
+        rng = np.random.default_rng(args.seed + 1)
+        pert = dict(inp, R=1.1, amp=0.35, peak=170.0, k=0.6, r0s=inp["r0s"] * rng.lognormal(0.0, 0.05, G))
+        target, _ = ops.expected_incidence(pert)
     W, K = max(3, args.warmup), max(1, min(args.steps, 200))
     torch.cuda.synchronize()
     with ClockSampler(0) as clocks:
@@ -746,7 +939,8 @@ def incidence_arm(args):
         "ms_per_step": dev_ms,
         "higher_is_better": True,
         "dtype": "f64",
-        "data": "synthetic (seeded numpy, replayed-aggregate shapes)",
+        "data": ("synthetic agents (seeded numpy, Nigeria-scale shapes); aggregates and target recorded by "
+                 "forward runs of the engine" if replay else "synthetic (seeded numpy, replayed-aggregate shapes)"),
         "config": {"workload": f"adjoint of expected incidence, {G} nodes, {T} ticks, {S} strains",
                    "loss": "sum (log1p(lam) - log1p(target))^2",
                    "l2": "working set (~40 MB) L2-resident by design; no flush"},
@@ -759,6 +953,7 @@ def incidence_arm(args):
         "cpu_baseline": cpu,
         "loss": res["loss"],
         "grad": {k: res["grad"][k] for k in ("R", "amp", "peak", "k", "a", "b", "c")},
+        "replay": replay,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -850,6 +1045,9 @@ def main():
         return
     if args.incidence:
         incidence_arm(args)
+        return
+    if args.continental:
+        continental_arm(args)
         return
     import torch
 

@@ -1757,8 +1757,12 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
 #define LPG_NODE_MIX_THREADS (32 * (LPG_NODE_MIX_WARPS + 1))
 #define LPG_NODE_MIX_MIN_BLOCKS 6
 /* the node steps switch to their batch forms above this many nodes (six
- * CTAs of the per-node kernels per SM: more would take a second wave) */
+ * CTAs of the per-node kernels per SM: more would take a second wave), when
+ * no simulation has more than LPG_NODE_BATCH_MAX_NODES nodes: one warp then
+ * sweeps each network row in a few passes, where rows of thousands of
+ * sources keep the per-node form's four mixing warps */
 #define LPG_NODE_BATCH_MIN_PER_SM 6
+#define LPG_NODE_BATCH_MAX_NODES 512
 
 struct SelInfo {
   uint64_t seed;

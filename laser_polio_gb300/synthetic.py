@@ -119,11 +119,17 @@ def zamfara_like(n_agents=1_000_000, dur=365, seed=42, n_nodes=14):
     return sim
 
 
-def nigeria_like_pars(n_agents=220_000_000, n_nodes=774, dur=2555, seed=42):
-    """Parameters (no agents) of the Nigeria-scale workload."""
+def nigeria_like_pars(n_agents=220_000_000, n_nodes=774, dur=2555, seed=42, mu=np.log(2.8e5), sigma=0.7,
+                      side_km=1000.0):
+    """Parameters (no agents) of the Nigeria-scale workload: node
+    populations lognormal(mu, sigma) summing to n_agents, coordinates in a
+    side_km square, CBR 37, R0 14 with amplitude 0.4 peaking on day 180, RI
+    coverage beta(6, 4), an SIA on a random 30% of nodes every 180 days
+    (ages 0-5 y, coverage beta(8, 3), efficacy 0.6), three strains; under-15
+    immunity uniform(0.4, 0.9) per node (returned beside the parameters)."""
     rng = np.random.default_rng(seed)
-    pops = _node_pops(rng, n_nodes, np.log(2.8e5), 0.7, n_agents)
-    pars = _base_pars(rng, n_nodes, pops, dur, seed, 37, 1000.0, 0.4, 180, 14)
+    pops = _node_pops(rng, n_nodes, mu, sigma, n_agents)
+    pars = _base_pars(rng, n_nodes, pops, dur, seed, 37, side_km, 0.4, 180, 14)
     sia = []
     for k, t in enumerate(range(180, dur + 1, 180)):
         nodes = np.sort(rng.choice(n_nodes, size=max(1, int(0.3 * n_nodes)), replace=False))
@@ -142,6 +148,14 @@ def nigeria_like_pars(n_agents=220_000_000, n_nodes=774, dur=2555, seed=42):
     })
     immun = rng.uniform(0.4, 0.9, n_nodes)
     return pars, immun, rng
+
+
+def continental_pars(n_agents=1_000_000_000, n_nodes=4000, dur=365, seed=42):
+    """Parameters (no agents) of the continental workload: 4000 nodes,
+    1e9 agents with node populations lognormal(ln 2.5e5, 0.9), a dense
+    gravity network from coordinates in a 5000 km square, 365 ticks; RI, SIA
+    schedule, strains and the rest as the Nigeria-scale workload."""
+    return nigeria_like_pars(n_agents, n_nodes, dur, seed, mu=np.log(2.5e5), sigma=0.9, side_km=5000.0)
 
 
 def nigeria_like(n_agents=2_000_000, n_nodes=774, dur=2555, seed=42):
@@ -203,7 +217,8 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
     may supply the column buffers (pinned host memory for the end-to-end
     measurement).  r0, amp, peak and gravity_k are the replicate-level
     parameters a calibration varies (R0, seasonal amplitude and peak day,
-    gravity k).
+    gravity k).  params["distances"] is the node distance matrix the gravity
+    network was built from (make_desc ignores it).
     """
     import concurrent.futures as cf
     import datetime as dt
@@ -264,6 +279,7 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
         "sia": sia, "vx_prob_sia": p_sia.astype(np.float32), "strain_r0_scalars": np.array([1.0, 0.25, 0.125]),
         "network": net, "r0_scalars": r0s, "seasonality": seasonality_table(datevec, float(amp), int(peak)),
         "zero_inflation": 0.0, "nb_r": 1000, "pop0": pops.astype(np.int32), "R_preseed": None,
+        "distances": dist,
     }
 
     alloc = alloc or (lambda name, n, dtype: np.empty(n, dtype=dtype))
@@ -335,11 +351,12 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
     return params, cols
 
 
-def incidence_inputs(T=365, n_nodes=774, n_strains=3, n_agents=2.2e8, seed=42):
+def incidence_inputs(T=365, n_nodes=774, n_strains=3, n_agents=2.2e8, seed=42, mu=np.log(2.8e5), sigma=0.7,
+                     side_km=1000.0):
     """Node-level aggregates of a replayed Nigeria-scale run, for the
     expected-incidence map and its adjoint (laser_polio_gb300.ops.
-    expected_incidence): node populations lognormal(ln 2.8e5, 0.7) summing
-    to n_agents on a 1000 km square, growing at CBR 37 minus a flat 10 per
+    expected_incidence): node populations lognormal(mu, sigma), by default
+    (ln 2.8e5, 0.7), summing to n_agents on a side_km (1000 km) square, growing at CBR 37 minus a flat 10 per
     1000; susceptibles 5-30% of a node carrying unit mean risk; infectivity
     by strain (1, 0.25, 0.125 of the VDPV2 level) of about 0.6 per infected
     agent-day from a few hundred infected agents, zero in 30% of node-ticks;
@@ -350,8 +367,8 @@ def incidence_inputs(T=365, n_nodes=774, n_strains=3, n_agents=2.2e8, seed=42):
     import datetime as dt
 
     rng = np.random.default_rng(seed)
-    pops = _node_pops(rng, n_nodes, np.log(2.8e5), 0.7, n_agents).astype(np.float64)
-    dist = _gravity_distances(rng, n_nodes, 1000.0)
+    pops = _node_pops(rng, n_nodes, mu, sigma, n_agents).astype(np.float64)
+    dist = _gravity_distances(rng, n_nodes, side_km)
     growth = (37.0 - 10.0) / 365000.0
     pop = pops[None, :] * (1.0 + growth) ** np.arange(T)[:, None]
     sus = rng.uniform(0.05, 0.3, n_nodes)

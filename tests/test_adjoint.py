@@ -247,6 +247,39 @@ def test_gpu_engine_records_the_aggregates_its_exposures_come_from():
     _close(lam, agg["lam"][ticks], 1e-9, "engine exposures")
 
 
+@pytest.mark.gpu
+def test_gpu_replayed_nigeria_like_runs_give_the_adjoints_inputs_and_target():
+    """The adjoint's replay as the bench runs it (bench.replay_inputs), on a
+    small Nigeria-like population: two simulations of one agent table in one
+    handle, base and perturbed parameters, both recording.  The map on the
+    base run's aggregates reproduces its exposures within 1e-9 of the
+    largest; the target (the perturbed run's exposures) differs from them;
+    the plan's loss equals the oracle's on the same inputs and target, and
+    its R gradient is negative (the target has 10% more infectivity)."""
+    import types
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import bench
+
+    args = types.SimpleNamespace(agents=4e5, nodes=40, seed=11)
+    inp, target, rec = bench.replay_inputs(args, 120, 0)
+    assert inp["srisk"].shape == (120, 40) and inp["beta"].shape == (120, 40, 3) and target.shape == (120, 40)
+    assert rec["map_vs_engine_max_rel"] < 1e-9 and rec["new_exposed_expected"] > 0
+    assert rec["target_expected"] > 0 and not np.array_equal(target, inp["srisk"])
+    plan = ops.IncidencePlan(inp, target)
+    try:
+        res = plan.evaluate(inp)
+    finally:
+        plan.close()
+    lam_o, _ = I.incidence(inp)
+    resid = np.log1p(lam_o) - np.log1p(target)
+    loss_o = float((resid**2).sum())
+    assert abs(res["loss"] - loss_o) <= 1e-11 * abs(loss_o)
+    assert res["grad"]["R"] < 0
+
+
 def test_plan_rejects_bad_arguments_before_any_device_call():
     """lpg_incidence_plan_create checks sizes and inputs on the host first
     (LPG_ERR_ARG -> ValueError), with or without a GPU."""
