@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--continental", action="store_true",
                     help="instead: the 4000-node, 1e9-agent workload through the user's path (365 ticks); "
                          "with --incidence, the adjoint on seeded aggregates of its shapes")
+    ap.add_argument("--continental-reps", type=int, default=4,
+                    help="parameter-set replicates of the continental table in one handle (1e9 agents in all)")
     ap.add_argument("--export", action="store_true",
                     help="instead: save_sim_results' CSV of a Nigeria-scale results table (host only)")
     return ap.parse_args()
@@ -168,9 +170,12 @@ NCU_TRAFFIC_SOURCE = {
 #   k_sweep_rs (k_sweep_b) on RI ticks: 4 B per RI due index entry read; per visited
 #     sub-block its state, chronically-missed flags, RI timers, reference
 #     indexes and dates of birth (128 x 12 B) and the index write (4 B).
-#   k_node_mix: the network rows (nodes^2 x 16 B per simulation, two 8-byte
-#     fixed-point parts per entry) and, per chunk of the population, its list
-#     entry, weight and prefix (20 B).
+#   k_node_mix: per tick, the network entries of the sources with infected
+#     agents (nodes x such sources x 16 B per simulation, two 8-byte
+#     fixed-point parts per entry: entries of sources without infectivity
+#     add nothing to the exact sums and are not read), the infectivity
+#     totals (nodes x strains x 8 B) and, per chunk of the population, its
+#     list entry, weight and prefix (20 B).
 #   k_node_tx: per node its population inputs (last row, births, deaths:
 #     12 B), seasonality, R0 scalar and row sum (24 B), per strain the
 #     infectivity total and incoming infectivity (16 B x 3), susceptible
@@ -202,16 +207,19 @@ def merge_selection(prof):
     return out
 
 
-def kernel_alg_bytes(params, ticks, cnt, work, new_exposed):
+def kernel_alg_bytes(params, ticks, cnt, work, new_exposed, sources):
     """Algorithmic bytes of each modelled kernel over the ticks (total, all
-    launches), from the work counters of the same ticks.  ``params`` and
-    ``cnt`` may be lists (the simulations of one handle): the per-simulation
-    terms are summed; the work counters are the handle's."""
+    launches), from the work counters of the same ticks.  ``params``,
+    ``cnt`` and ``sources`` (per tick, the nodes with infected agents: the
+    results' I row > 0) may be lists (the simulations of one handle): the
+    per-simulation terms are summed; the work counters are the handle's."""
     plist = params if isinstance(params, list) else [params]
     clist = cnt if isinstance(params, list) else [cnt]
+    slist = sources if isinstance(params, list) else [sources]
     staged = sum(float(sum(sweep_b_bytes(p, t) * c[t] for t in ticks)) for p, c in zip(plist, clist))
-    node_mix = sum(len(ticks) * (p["n_nodes"] ** 2 * NODE_TX_NET_B + NODE_TX_CHUNK_B * float(p["capacity"]) / 2048.0)
-                  for p in plist)
+    node_mix = sum(float(sum(p["n_nodes"] * (src[t] * NODE_TX_NET_B + p["n_strains"] * 8.0) for t in ticks))
+                   + len(ticks) * NODE_TX_CHUNK_B * float(p["capacity"]) / 2048.0
+                   for p, src in zip(plist, slist))
     out = {
         "k_due": SWEEP_INDEX_B * work["sweep_index"] + DUE_ITEM_B * work["sweep_due"],
         "k_sweep_a": (DUE_ITEM_B * work["sweep_due"] + SWEEP_DUE_B * work["sweep_due"]
@@ -581,10 +589,89 @@ def continental_arm(args):
         "clocks": clocks.summary(),
     }
     eng.close()
-    del sim
+    del sim, eng
+    torch.cuda.empty_cache()
+    if args.continental_reps > 1:
+        line["replicates"] = continental_replicates(agents, nodes, args.continental_reps, args.seed, W)
     print(json.dumps(line), flush=True)
     if args.out:
         Path(args.out).write_text(json.dumps(line, indent=1))
+
+
+def continental_replicates(agents, nodes, reps, seed, W):
+    """R parameter sets over one continental agent table in one handle: the
+    table (agents / R agents, the continental node layout, 365 ticks) is
+    drawn once and bound R times, each replicate with its own R0 (every
+    agent's infectivity scaled), seasonal amplitude and peak, gravity k and
+    seed.  The configuration's R x 1e9 agents would need R x 68 GB of engine
+    state (52 B per capacity slot) and do not fit in one GPU's memory, so the
+    table is 1e9 / R agents and the batch 1e9 in all.  All ticks after W are
+    timed between CUDA events, batched and then the replicates one after
+    another."""
+    import torch
+
+    from laser_polio_gb300 import synthetic
+    from laser_polio_gb300._lib import Handle
+    from laser_polio_gb300.core import gravity, row_normalizer
+    from laser_polio_gb300.engine import make_desc
+    from laser_polio_gb300.utils import seasonality_table
+    import datetime
+
+    t0 = time.perf_counter()
+    p0, cols = synthetic.bundle("continental", n_agents=agents // reps, n_nodes=nodes, dur=365, seed=seed)
+    t_gen = time.perf_counter() - t0
+    pops, dist, nt = p0["pop0"].astype(np.float64), p0["distances"], p0["nt"]
+    dates = [datetime.date(2019, 1, 1) + datetime.timedelta(days=d) for d in range(nt)]
+    sets = [(1.0, 0.4, 180, 0.5), (0.8, 0.3, 150, 0.3), (1.2, 0.5, 210, 0.8), (1.1, 0.2, 120, 0.6)]
+    rng = np.random.default_rng(seed + 7)
+    runs = []
+    for r in range(reps):
+        scale, amp, peak, k = sets[r % len(sets)]
+        p = dict(p0, seed=seed + r, seasonality=seasonality_table(dates, amp, peak),
+                 r0_scalars=p0["r0_scalars"] * rng.lognormal(0.0, 0.1, nodes),
+                 network=row_normalizer(gravity(pops, dist, k, 1, 1, 2.0) / np.power(pops.sum(), 2.0), 0.2))
+        c = cols if scale == 1.0 else dict(cols, daily_infectivity=(cols["daily_infectivity"] * np.float32(scale))
+                                                                  .astype(np.float32))
+        runs.append((p, c, make_desc(p)))
+
+    def run(idx):
+        h = Handle([runs[i][2][0] for i in idx])
+        try:
+            for j, i in enumerate(idx):
+                h.bind_columns(j, runs[i][1])
+            h.start()
+            h.step(W)
+            h.sync()
+            stream = torch.cuda.ExternalStream(h.cuda_stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            h.step(nt - 1 - W)
+            e1.record(stream)
+            h.sync()
+            ms = e0.elapsed_time(e1)
+            at, ne = 0.0, 0
+            for j, i in enumerate(idx):
+                res = result_arrays(runs[i][0])
+                h.read_results(j, res)
+                at += float(counts_per_tick(runs[i][0], res["births"])[W + 1 : nt].sum())
+                ne += int(res["new_exposed"].sum())
+        finally:
+            h.close()
+        return ms, at, ne
+
+    ms_b, at_b, ne_b = run(list(range(reps)))
+    ms_s, at_s = 0.0, 0.0
+    for i in range(reps):
+        ms, at, _ = run([i])
+        ms_s += ms
+        at_s += at
+    assert at_s == at_b
+    return {"value": at_b / (ms_b / 1e3), "unit": "agent-ticks/s", "replicates": reps,
+            "agents_each": int(p0["count"]), "agents": int(p0["count"]) * reps, "nodes_each": nodes,
+            "ticks": f"{W + 1}-{nt - 1} of {nt - 1}", "ms_per_step": ms_b / (nt - 1 - W),
+            "sequential": {"value": at_s / (ms_s / 1e3), "ms_total": ms_s}, "batched_ms_total": ms_b,
+            "speedup_vs_sequential": ms_s / ms_b, "generation_s": t_gen, "new_exposed_total": ne_b,
+            "parameter_sets": "(R0 scale, amp, peak, k) in " + str(sets[:reps]) + "; r0 scalars x lognormal(0, 0.1)"}
 
 
 def tick_kind(params, t):
@@ -695,24 +782,25 @@ def batch_measure(n_reps, seed, W, K, profile=True):
         h.sync()
         ms = e0.elapsed_time(e1)
         launches = h.kernel_launches() - l0
-        at, cnts, ne = 0.0, [], 0
+        at, cnts, ne, srcs = 0.0, [], 0, []
         for j, i in enumerate(idx):
             res = result_arrays(bundles[i][0])
             h.read_results(j, res)
             cnt = counts_per_tick(bundles[i][0], res["births"])
             cnts.append(cnt)
+            srcs.append((res["I"] > 0).sum(axis=1))
             at += float(cnt[W + 1 : W + K + 1].sum())
             tk = slice(W + 1, W + K + 1)
             ne += int(res["new_exposed"][tk].sum() - res["ri_protected"][tk].sum() - res["sia_protected"][tk].sum())
         prof = merge_selection(h.profile()) if profiling else None
         work = h.counters() if profiling else None
         h.close()
-        return ms, at, launches, prof, work, cnts, ne
+        return ms, at, launches, prof, work, cnts, ne, srcs
 
-    ms_b, at_b, launches_b, _, _, _, _ = run(list(range(len(bundles))))
+    ms_b, at_b, launches_b = run(list(range(len(bundles))))[:3]
     ms_s, at_s = 0.0, 0.0
     for i in range(len(bundles)):
-        ms, at, _, _, _, _, _ = run([i])
+        ms, at = run([i])[:2]
         ms_s += ms
         at_s += at
     assert at_s == at_b
@@ -724,9 +812,9 @@ def batch_measure(n_reps, seed, W, K, profile=True):
         "batched_ms_total": ms_b, "speedup_vs_sequential": ms_s / ms_b, "generation_s": t_gen,
     }
     if profile:
-        _, _, _, prof, work, cnts, ne = run(list(range(len(bundles))), profiling=True)
+        _, _, _, prof, work, cnts, ne, srcs = run(list(range(len(bundles))), profiling=True)
         ticks = np.arange(W + 1, W + K + 1)
-        alg = kernel_alg_bytes([p for p, _ in bundles], ticks, cnts, work, ne)
+        alg = kernel_alg_bytes([p for p, _ in bundles], ticks, cnts, work, ne, srcs)
         tot = sum(v[0] for v in prof.values())
         top = max(prof, key=lambda k: prof[k][0])
         t_ms, t_n = prof[top]
@@ -1203,7 +1291,7 @@ def main():
         # agents exposed by transmission: new exposures less the RI and SIA protections counted with them
         new_exposed = int(res["new_exposed"][ticks].sum() - res["ri_protected"][ticks].sum()
                           - res["sia_protected"][ticks].sum())
-        alg = kernel_alg_bytes(params, ticks, cnt, work, new_exposed)
+        alg = kernel_alg_bytes(params, ticks, cnt, work, new_exposed, (res["I"] > 0).sum(axis=1))
         per_kernel = {}
         for k, (tot_ms, nl) in prof.items():
             row = {"ms_per_launch": tot_ms / max(1, nl), "launches": nl, "share": share[k]}

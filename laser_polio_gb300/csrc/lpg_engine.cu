@@ -104,7 +104,8 @@ struct lpg_handle {
   int rounds_blocks = 0; /* k_sel_rounds */
   int evb_blocks = 0;
   int newborn_blocks = 0; /* per replicate */
-  bool node_batch = false; /* the node steps' batch forms (k_node_mix<1>, k_node_tx_lanes) */
+  bool node_batch_tx = false;  /* the draws one node a thread (k_node_tx_lanes) */
+  bool node_batch_mix = false; /* the mixing one warp a node (k_node_mix<1>) */
 };
 
 static int fail(lpg_handle* h, int code, const char* fmt, ...) {
@@ -674,7 +675,8 @@ extern "C" int lpg_start(lpg_handle* h) {
   DevWorld& W = h->W;
   W.n_reps = R;
   W.G = G;
-  h->node_batch = G > LPG_NODE_BATCH_MIN_PER_SM * h->sm_count && maxn <= LPG_NODE_BATCH_MAX_NODES;
+  h->node_batch_tx = G > LPG_NODE_BATCH_MIN_PER_SM * h->sm_count;
+  h->node_batch_mix = h->node_batch_tx && maxn <= LPG_NODE_BATCH_MAX_NODES;
   W.total_chunks = chunk_total;
   W.stall_after = h->test_stall_after;
   W.wait_spin = h->test_wait_spin > 0 ? h->test_wait_spin : LPG_MBAR_SPIN;
@@ -1096,11 +1098,11 @@ static int launch_one(lpg_handle* h, int k, bool timed) {
     case 5: CK(launch_pdl(k_sweep_rs, dim3(h->sweep_blocks), dim3(LPG_SWEEP_BLOCK), LPG_SWEEP_SMEM, st, W)); break;
     case 6: CK(launch_pdl(k_evb, dim3(h->evb_blocks), dim3(256), 0, st, W, h->sweep_blocks)); break;
     case 7:
-      if (h->node_batch) CK(launch_pdl(k_node_mix<1>, dim3(G), dim3(64), 0, st, W));
+      if (h->node_batch_mix) CK(launch_pdl(k_node_mix<1>, dim3(G), dim3(64), 0, st, W));
       else CK(launch_pdl(k_node_mix<LPG_NODE_MIX_WARPS>, dim3(G), dim3(LPG_NODE_MIX_THREADS), 0, st, W));
       break;
     case 8:
-      if (h->node_batch) CK(launch_pdl(k_node_tx_lanes, dim3((G + 127) / 128), dim3(128), 0, st, W));
+      if (h->node_batch_tx) CK(launch_pdl(k_node_tx_lanes, dim3((G + 127) / 128), dim3(128), 0, st, W));
       else CK(launch_pdl(k_node_tx, dim3(G), dim3(LPG_NODE_TX_THREADS), 0, st, W));
       break;
     case 9: {

@@ -1757,10 +1757,10 @@ __global__ void __launch_bounds__(1024) k_seed(DevWorld W) {
 #define LPG_NODE_MIX_THREADS (32 * (LPG_NODE_MIX_WARPS + 1))
 #define LPG_NODE_MIX_MIN_BLOCKS 6
 /* the node steps switch to their batch forms above this many nodes (six
- * CTAs of the per-node kernels per SM: more would take a second wave), when
- * no simulation has more than LPG_NODE_BATCH_MAX_NODES nodes: one warp then
- * sweeps each network row in a few passes, where rows of thousands of
- * sources keep the per-node form's four mixing warps */
+ * CTAs of the per-node kernels per SM: more would take a second wave); the
+ * mixing only when no simulation has more than LPG_NODE_BATCH_MAX_NODES
+ * nodes: one warp then sweeps each network row in a few passes, where rows
+ * of thousands of sources keep the per-node form's four mixing warps */
 #define LPG_NODE_BATCH_MIN_PER_SM 6
 #define LPG_NODE_BATCH_MAX_NODES 512
 
@@ -1863,29 +1863,45 @@ __global__ void __launch_bounds__(32 * (MW + 1), MW == 4 ? LPG_NODE_MIX_MIN_BLOC
   /* qrow[ii] = network[ii][i] as (hi 2^-62, lo 2^-120), lpg_net_split */
   const ulonglong2* qrow = reinterpret_cast<const ulonglong2*>(rp->netq_t) + (int64_t)i * n;
   constexpr int NT = 32 * MW;
-  constexpr int PER = 7; /* source nodes a thread takes per pass: PER x NT nodes a pass */
+  constexpr int PER = 6; /* source nodes a thread takes per pass: PER x NT nodes a pass */
+  if (lane == 0)
+    for (int k = 0; k < ns; ++k)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) s_mix[wid][k][q] = 0;
   /* per strain: A = sum B hi and R = sum B lo, three words each, exact;
-   * one strain at a time (six accumulators live), the network entries of
-   * the pass loaded once for all strains */
+   * one strain at a time (six accumulators live).  Sources without
+   * infectivity add nothing to an exact sum, so a network entry is loaded
+   * only where some strain's B is nonzero, and a strain whose B is zero
+   * across the warp's sources of the pass is skipped: the sums, and so the
+   * results, are those of the full product. */
   /* the same number of passes for every thread (the shuffles below need
    * all 32 lanes), loads past the last node predicated off */
   const int npass = (n + PER * NT - 1) / (PER * NT);
   for (int pass = 0; pass < npass; ++pass) {
     const int ii0 = pass * PER * NT + threadIdx.x;
-    ulonglong2 w[PER];
-#pragma unroll
-    for (int u = 0; u < PER; ++u) {
-      const int ii = ii0 + u * NT;
-      w[u] = ii < n ? qrow[ii] : make_ulonglong2(0, 0);
-    }
-#pragma unroll 1
+    unsigned need = 0; /* bit u: source ii0 + u NT has infectivity of some strain */
     for (int k = 0; k < ns; ++k) {
-      uint64_t b[PER];
 #pragma unroll
       for (int u = 0; u < PER; ++u) {
         const int ii = ii0 + u * NT;
-        b[u] = ii < n ? W.bb[(int64_t)k * G + nb + ii] : 0;
+        if (ii < n && W.bb[(int64_t)k * G + nb + ii] != 0) need |= 1u << u;
       }
+    }
+    if (!__any_sync(FULLMASK, need != 0)) continue; /* warp-uniform */
+    ulonglong2 w[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) w[u] = (need >> u) & 1 ? qrow[ii0 + u * NT] : make_ulonglong2(0, 0);
+#pragma unroll 1
+    for (int k = 0; k < ns; ++k) {
+      uint64_t b[PER];
+      bool any = false;
+#pragma unroll
+      for (int u = 0; u < PER; ++u) {
+        const int ii = ii0 + u * NT;
+        b[u] = (need >> u) & 1 ? W.bb[(int64_t)k * G + nb + ii] : 0;
+        any |= b[u] != 0;
+      }
+      if (!__any_sync(FULLMASK, any)) continue; /* warp-uniform */
       uint64_t a0 = 0, a1 = 0, a2 = 0, r0 = 0, r1 = 0, r2 = 0;
 #pragma unroll
       for (int u = 0; u < PER; ++u) {
@@ -1902,17 +1918,8 @@ __global__ void __launch_bounds__(32 * (MW + 1), MW == 4 ? LPG_NODE_MIX_MIN_BLOC
         acc3_add(r0, r1, r2, y0, y1, y2);
       }
       if (lane == 0) {
-        if (pass == 0) {
-          s_mix[wid][k][0] = a0;
-          s_mix[wid][k][1] = a1;
-          s_mix[wid][k][2] = a2;
-          s_mix[wid][k][3] = r0;
-          s_mix[wid][k][4] = r1;
-          s_mix[wid][k][5] = r2;
-        } else { /* a later pass (more than PER x NT nodes): added to the first */
-          acc3_add(s_mix[wid][k][0], s_mix[wid][k][1], s_mix[wid][k][2], a0, a1, a2);
-          acc3_add(s_mix[wid][k][3], s_mix[wid][k][4], s_mix[wid][k][5], r0, r1, r2);
-        }
+        acc3_add(s_mix[wid][k][0], s_mix[wid][k][1], s_mix[wid][k][2], a0, a1, a2);
+        acc3_add(s_mix[wid][k][3], s_mix[wid][k][4], s_mix[wid][k][5], r0, r1, r2);
       }
     }
   }

@@ -160,7 +160,17 @@ def continental_pars(n_agents=1_000_000_000, n_nodes=4000, dur=365, seed=42):
 
 def nigeria_like(n_agents=2_000_000, n_nodes=774, dur=2555, seed=42):
     """Host-initialised Nigeria-like sim (moderate sizes; tests and CPU runs)."""
-    pars, immun, rng = nigeria_like_pars(n_agents, n_nodes, dur, seed)
+    return _host_sim(*nigeria_like_pars(n_agents, n_nodes, dur, seed))
+
+
+def continental_like(n_agents=4_000_000, n_nodes=4000, dur=365, seed=42):
+    """Host-initialised sim of the continental workload's shape (4000 nodes,
+    lognormal(ln 2.5e5, 0.9) node populations, 5000 km square) at moderate
+    agent counts (tests and CPU runs)."""
+    return _host_sim(*continental_pars(n_agents, n_nodes, dur, seed))
+
+
+def _host_sim(pars, immun, rng):
     sim = M.SEIR_ABM(PropertySet(pars))
     sim.components = [M.VitalDynamics_ABM, M.DiseaseState_ABM, M.RI_ABM, M.SIA_ABM, M.Transmission_ABM]
     _age_immunity(sim, rng, immun)
@@ -212,7 +222,9 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
            alloc=None, r0=14.0, amp=0.4, peak=180, gravity_k=0.5):
     """(make_desc parameters, reference-ordered columns) of a synthetic run.
 
-    kind 'nigeria' (defaults 2.2e8 agents, 774 nodes, 2555 ticks) or
+    kind 'nigeria' (defaults 2.2e8 agents, 774 nodes, 2555 ticks),
+    'continental' (1e9 agents, 4000 nodes, 365 ticks; node populations
+    lognormal(ln 2.5e5, 0.9), 5000 km square, otherwise as 'nigeria') or
     'zamfara' (1e6 agents, 14 nodes, 365 ticks).  ``alloc(name, n, dtype)``
     may supply the column buffers (pinned host memory for the end-to-end
     measurement).  r0, amp, peak and gravity_k are the replicate-level
@@ -236,6 +248,11 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
         n_nodes = 774 if n_nodes is None else n_nodes
         dur = 2555 if dur is None else dur
         mu, sg, side, cbr = np.log(2.8e5), 0.7, 1000.0, 37
+    elif kind == "continental":
+        n_agents = int(1e9 if n_agents is None else n_agents)
+        n_nodes = 4000 if n_nodes is None else n_nodes
+        dur = 365 if dur is None else dur
+        mu, sg, side, cbr = np.log(2.5e5), 0.9, 5000.0, 37
     else:
         n_agents = int(1e6 if n_agents is None else n_agents)
         n_nodes = 14 if n_nodes is None else n_nodes
@@ -247,7 +264,7 @@ def bundle(kind="nigeria", n_agents=None, n_nodes=None, dur=None, seed=42, capac
     capacity = int(count * capacity_factor)
     nt = dur + 1
     r0 = float(r0)
-    if kind == "nigeria":
+    if kind in ("nigeria", "continental"):
         immun = rng.uniform(0.4, 0.9, n_nodes)
         p_ri = rng.beta(6, 4, n_nodes)
         p_sia = rng.beta(8, 3, n_nodes)

@@ -5,6 +5,8 @@ configurations' own shapes.
   - the Nigeria-scale shape over its whole 2555-tick run at reduced agents
     (774 nodes, 2e6 agents): every SIA day (14), every RI tick (182), every
     birth tick (365) and the chunk-list rebuilds they cause;
+  - the continental shape (4000 nodes, 5000 km gravity network) at 4e6
+    agents over 40 ticks;
   - a 64-replicate calibration batch with the batch configuration's node
     counts ({14, 44, 120, 300}), per-replicate R0, seasonality and gravity k
     and 730 ticks, at 1/50 of its agents, in one handle.
@@ -60,6 +62,46 @@ def test_parity_nigeria_shape_whole_run():
     assert len(np.flatnonzero(res["ri_vaccinated"].sum(1))) >= 5
     assert len(np.flatnonzero(res["births"].sum(1))) > 300
     assert res["new_exposed"].sum() > 0
+
+
+def test_parity_continental_shape():
+    """The continental workload's node layout (4000 nodes, populations
+    lognormal(ln 2.5e5, 0.9), dense gravity network over a 5000 km square,
+    RI and births) at 4e6 agents over 40 ticks: network rows of 4000 sources
+    in the per-node mixing form, nodes of a few dozen to ten thousand agents."""
+    from laser_polio_gb300._lib import Handle
+    from oracle.oracle import OracleSim
+
+    p, cols = synthetic.bundle("continental", n_agents=4_000_000, dur=40, seed=7)
+    assert p["n_nodes"] == 4000 and p["count"] == 4_000_000 and p["network"].shape == (4000, 4000)
+    d, keep = make_desc(p)
+    o = OracleSim(d, keepalive=keep)
+    c_o = {k: v.copy() for k, v in cols.items()}
+    o.bind_columns(c_o)
+    o.start()
+    o.step(p["nt"] - 1)
+    res_o = _results(p)
+    o.read_results(res_o)
+    o.read_columns(c_o)
+    so = o.state()
+    o.close()
+    h = Handle([d])
+    try:
+        c_g = {k: v.copy() for k, v in cols.items()}
+        h.bind_columns(0, c_g)
+        h.start()
+        h.step(p["nt"] - 1)
+        h.sync()
+        sg = h.state(0)
+        assert (sg.t, sg.stopped, sg.count, sg.error) == (so.t, so.stopped, so.count, so.error)
+        res_g = _results(p)
+        h.read_results(0, res_g)
+        h.read_columns(0, c_g)
+    finally:
+        h.close()
+    assert_same(res_o, res_g, "result")
+    assert_same(c_o, c_g, "column", count=so.count)
+    assert res_o["new_exposed"].sum() > 1000 and res_o["births"].sum() > 0 and res_o["ri_vaccinated"].sum() > 0
 
 
 def test_parity_64_replicates_of_the_batch_shapes():
