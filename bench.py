@@ -498,21 +498,11 @@ def api_run(args, dev):
     return out
 
 
-def continental_arm(args):
-    """The continental workload through the user's path: 4000 nodes, 1e9
-    agents (capacity +30%), node populations lognormal(ln 2.5e5, 0.9), dense
-    gravity network over a 5000 km square, RI and SIA as the Nigeria-scale
-    workload, 365 ticks.  SEIR_ABM(pars) with the five components (agent
-    table initialised on the device), then the steps of run(): start (bind
-    and layout), the first W ticks with per-kernel profiling, the remaining
-    ticks between CUDA events on the engine's stream, results and columns
-    copied into the sim.  value: agent-ticks/s of the timed ticks; e2e: all
-    ticks over the wall time of construction, start, ticks and copy-back."""
-    import torch
-
+def continental_sim(args):
+    """SEIR_ABM of the continental workload with the five components (agent
+    table initialised on the device), its agent and node counts."""
     import laser_polio_gb300 as lp
     from laser_polio_gb300 import synthetic
-    from laser_polio_gb300.model import _engine_of
 
     agents = int(args.agents if args.agents != 2.2e8 else 1e9)
     nodes = args.nodes if args.nodes != 774 else 4000
@@ -520,14 +510,42 @@ def continental_arm(args):
     prev = np.zeros(nodes, np.int64)
     prev[rng.choice(nodes, size=2, replace=False)] = 10
     pars.update({"init_immun": list(np.asarray(immun, float)), "init_prev": list(prev), "age_pyramid_path": None})
+    sim = lp.SEIR_ABM(lp.PropertySet(pars))
+    sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.RI_ABM, lp.SIA_ABM, lp.Transmission_ABM]
+    return sim, agents, nodes
+
+
+def desc_params(desc):
+    """The fields of a simulation description the byte model reads."""
+    return {"n_nodes": desc.n_nodes, "n_strains": desc.n_strains, "capacity": desc.capacity,
+            "vd_step": desc.vd_step, "ri_enabled": desc.ri_enabled, "ri_step": desc.ri_step,
+            "sia": [(desc.sia[i].tick,) for i in range(desc.n_sia)]}
+
+
+def continental_arm(args):
+    """The continental workload through the user's path: 4000 nodes, 1e9
+    agents (capacity as the reference sizes it for the births of the run),
+    node populations lognormal(ln 2.5e5, 0.9), dense gravity network over a
+    5000 km square, RI and SIA as the Nigeria-scale workload, 365 ticks.
+    SEIR_ABM(pars) with the five components (agent table initialised on the
+    device), then the steps of run(): start (bind and layout), W untimed
+    ticks, the remaining ticks between CUDA events on the engine's stream,
+    results and columns copied into the sim.  value: agent-ticks/s of the
+    timed ticks; e2e: all ticks over the wall time of construction, start,
+    ticks and copy-back.  A second run of the same sim in profiling mode
+    gives each kernel's share of the whole run and the top kernel's
+    algorithmic bytes against the measured HBM peak."""
+    import torch
+
+    from laser_polio_gb300.model import _engine_of
+
     W = max(3, args.warmup)
     free0 = torch.cuda.mem_get_info()[0]
     with ClockSampler(0) as clocks:
         clocks.wait_ready()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim = lp.SEIR_ABM(lp.PropertySet(pars))
-        sim.components = [lp.VitalDynamics_ABM, lp.DiseaseState_ABM, lp.RI_ABM, lp.SIA_ABM, lp.Transmission_ABM]
+        sim, agents, nodes = continental_sim(args)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         eng = _engine_of(sim)
@@ -537,11 +555,8 @@ def continental_arm(args):
         t2 = time.perf_counter()
         used = free0 - torch.cuda.mem_get_info()[0]
         stream = torch.cuda.ExternalStream(h.cuda_stream())
-        h.set_profiling(True)
         h.step(W)
         h.sync()
-        prof = h.profile()
-        h.set_profiling(False)
         n_rest = sim.nt - 1 - W
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         l0 = h.kernel_launches()
@@ -559,38 +574,76 @@ def continental_arm(args):
         torch.cuda.synchronize()
         t5 = time.perf_counter()
     births = sim.results.births.sum(axis=1).astype(np.int64)
-    cnt = int(np.sum(pars["init_pop"])) + np.cumsum(births)
+    cnt = int(eng.spec.desc.count) + np.cumsum(births)
     at_timed = float(cnt[W + 1 : W + 1 + n_rest].sum())
     at_all = float(cnt[1 : sim.nt].sum())
-    wall = t5 - t0
+    new_exposed = int(sim.results.new_exposed.sum())
+    capacity = int(sim.people.capacity)
+    eng.close()
+    del sim, eng
+    torch.cuda.empty_cache()
+
+    # profiling pass: the same run again, every kernel timed with events
+    sim, _, _ = continental_sim(args)
+    eng = _engine_of(sim)
+    eng._ensure_started()
+    h = eng.handle
+    h.set_profiling(True)
+    h.step(sim.nt - 1)
+    h.sync()
+    prof = merge_selection(h.profile())
+    work = h.counters()
+    res = result_arrays(desc_params(eng.spec.desc) | {"nt": sim.nt})
+    h.read_results(0, res)
+    params = desc_params(eng.spec.desc)
+    eng.close()
+    del sim, eng
+    torch.cuda.empty_cache()
+    ticks = np.arange(1, len(cnt))
+    ne = int(res["new_exposed"][ticks].sum() - res["ri_protected"][ticks].sum() - res["sia_protected"][ticks].sum())
+    alg = kernel_alg_bytes(params, ticks, cnt, work, ne, (res["I"] > 0).sum(axis=1))
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
     tot = sum(v[0] for v in prof.values()) or 1.0
-    kernels = {k: {"ms_per_launch": v[0] / max(1, v[1]), "launches": v[1], "share": v[0] / tot}
-               for k, v in prof.items() if v[1]}
+    kernels = {}
+    for k, (k_ms, n) in prof.items():
+        if not n:
+            continue
+        row = {"ms_per_launch": k_ms / n, "launches": n, "share": k_ms / tot}
+        if k in alg and k_ms > 0:
+            row["alg_bytes_per_launch"] = alg[k] / n
+            row["achieved_gbs"] = alg[k] / (k_ms / 1e3) / 1e9
+            row["frac"] = row["achieved_gbs"] / peak
+        kernels[k] = row
+    top = max(prof, key=lambda k: prof[k][0])
+    roof = {"kernel": top, "bound": "hbm", "achieved": kernels[top].get("achieved_gbs"), "peak": peak,
+            "unit": "GB/s", "frac": kernels[top].get("frac"), "traffic": None,
+            "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+            "alg_bytes_per_launch": kernels[top].get("alg_bytes_per_launch"),
+            "mean_launch_ms": kernels[top]["ms_per_launch"], "share_of_run": kernels[top]["share"],
+            "work": work, "kernels": kernels,
+            "window": "every tick of the run (profiling pass: events around every kernel)"}
     line = {
         "metric": f"agent-ticks/s ({nodes} nodes, {agents:.2g} agents, full agent step)",
         "value": at_timed / (ms / 1e3), "unit": "agent-ticks/s", "n_gpus": 1, "steps": n_rest, "warmup": W,
         "ms_per_step": ms / n_rest, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int8/int32 state, f64 node FOI",
         "data": "synthetic (seeded, the continental workload's distributions; agent table drawn on the device)",
-        "config": {"workload": f"continental {nodes} nodes x {agents:.2g} agents, capacity +30%, "
-                               f"ticks {W + 1}-{sim.nt - 1} of a {sim.nt - 1}-tick run",
-                   "capacity": int(sim.people.capacity),
+        "config": {"workload": f"continental {nodes} nodes x {agents:.2g} agents, capacity {capacity:.3g}, "
+                               f"ticks {W + 1}-{len(cnt) - 1} of a {len(cnt) - 1}-tick run",
                    "l2": "state columns far larger than L2 (no flush needed)"},
-        "e2e": {"value": at_all / wall, "unit": "agent-ticks/s", "ticks": sim.nt - 1, "seconds": wall,
+        "e2e": {"value": at_all / (t5 - t0), "unit": "agent-ticks/s", "ticks": len(cnt) - 1, "seconds": t5 - t0,
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
-                "phases_s": {"construct": t1 - t0, "start": t2 - t1, "profiled_ticks": t3 - t2,
+                "phases_s": {"construct": t1 - t0, "start": t2 - t1, "untimed_ticks": t3 - t2,
                              "ticks": t4 - t3, "copy_back": t5 - t4},
                 "path": "SEIR_ABM(pars); sim.components = [...]; the steps of run(), results and columns "
                         "into the sim on the device"},
+        "roofline": roof,
         "device_bytes_after_start": used,
         "gpu_launches": launches,
-        "kernels_first_ticks": kernels,
-        "new_exposed_total": int(sim.results.new_exposed.sum()),
+        "new_exposed_total": new_exposed,
         "clocks": clocks.summary(),
     }
-    eng.close()
-    del sim, eng
-    torch.cuda.empty_cache()
     if args.continental_reps > 1:
         line["replicates"] = continental_replicates(agents, nodes, args.continental_reps, args.seed, W)
     print(json.dumps(line), flush=True)
