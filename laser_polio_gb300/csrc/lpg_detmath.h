@@ -478,30 +478,6 @@ LPG_HD uint64_t lpg_fix_risk_bits(float r) {
   return q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
 }
 
-/* The same weight with single-precision additions and integer operations
- * (no conversion instruction): for 0 < r < 256, f = r * 2^24 is exact;
- * below 2^23 (r < 1/2) the sum f + 2^23 lies in [2^23, 2^24), where the
- * float spacing is 1, so the addition itself rounds f to an integer, ties
- * to even, and the sum's bits less those of 2^23 are that integer; from 2^23
- * up f is an integer already, the significand M shifted left by E - 126
- * (at most 8 places below 256).  Other inputs (zero, negative, r >= 256,
- * inf, NaN) take the integer form. */
-LPG_HD uint64_t lpg_fix_risk_fadd(float r) {
-  union {
-    float f;
-    uint32_t u;
-  } c, d;
-  c.f = r;
-  const uint32_t u = c.u;
-  if (u - 1u >= 0x437fffffu) return lpg_fix_risk_bits(r); /* +0, negative, >= 256 (0x43800000), inf, NaN */
-  const float f = r * 16777216.0f;
-  d.f = f + 8388608.0f;
-  const uint32_t lo = d.u - 0x4b000000u; /* the bits of 2^23 */
-  const uint32_t e = u >> 23;
-  const uint32_t hi = ((u & 0x7fffffu) | 0x800000u) << ((e - 126u) & 31u);
-  return e < 126u ? lo : hi;
-}
-
 /* The same weight with single-precision arithmetic: r * 2^24 is exact in
  * float (a power-of-two scaling), and rounding an exact value to the nearest
  * integer, ties to even, gives the same integer in float as in double (below

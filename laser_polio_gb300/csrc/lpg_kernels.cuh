@@ -60,7 +60,7 @@ __device__ __forceinline__ void pdl_begin() {
 
 /* ------------------------------------------------------------------------ */
 /* fixed-point weights (identical definitions in the oracle)                */
-__device__ __forceinline__ uint64_t fix_risk(float r) { return lpg_fix_risk_fadd(r); }
+__device__ __forceinline__ uint64_t fix_risk(float r) { return lpg_fix_risk_f32(r); }
 __device__ __forceinline__ uint64_t fix_beta(float inf, double scal) {
   double d = ((double)inf * scal) * 0x1.0p40;
   if (!(d > 0.0)) return 0;

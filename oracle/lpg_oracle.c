@@ -1078,32 +1078,14 @@ double lpo_exp(double x) { return lpg_exp(x); }
 double lpo_expm1(double x) { return lpg_expm1(x); }
 double lpo_mlog(double x) { return lpg_log(x); }
 double lpo_lfact(int64_t k) { return lpg_lfact(k); }
-/* fixed-point weights: the double-precision definition and the integer,
- * single-precision and addition forms (the CUDA engine uses the last), for
- * many inputs at once (test export) */
-void lpo_fix_risk_many(const float* r, int64_t n, uint64_t* by_double, uint64_t* by_bits, uint64_t* by_f32,
-                       uint64_t* by_fadd) {
+/* fixed-point weights: the double-precision definition and the integer form
+ * the CUDA engine uses, for many inputs at once (test export) */
+void lpo_fix_risk_many(const float* r, int64_t n, uint64_t* by_double, uint64_t* by_bits, uint64_t* by_f32) {
   for (int64_t i = 0; i < n; ++i) {
     by_double[i] = fix_risk(r[i]);
     by_bits[i] = lpg_fix_risk_bits(r[i]);
     by_f32[i] = lpg_fix_risk_f32(r[i]);
-    by_fadd[i] = lpg_fix_risk_fadd(r[i]);
   }
-}
-/* every one of the 2^32 float bit patterns: how many give a weight from the
- * addition form (the engine's) other than the double-precision definition */
-int64_t lpo_fix_risk_fadd_mismatches(void) {
-  int64_t bad = 0;
-#pragma omp parallel for schedule(static) reduction(+ : bad)
-  for (int64_t b = 0; b < ((int64_t)1 << 32); ++b) {
-    union {
-      uint32_t u;
-      float f;
-    } c;
-    c.u = (uint32_t)b;
-    if (lpg_fix_risk_fadd(c.f) != fix_risk(c.f)) ++bad;
-  }
-  return bad;
 }
 void lpo_poisson_many(uint64_t seed, double lam, int64_t n, int64_t* out) {
   for (int64_t i = 0; i < n; ++i) {

@@ -40,8 +40,7 @@ def lib():
             getattr(L, name).argtypes = [C.c_double]
         L.lpo_lfact.restype = C.c_double
         L.lpo_lfact.argtypes = [C.c_int64]
-        L.lpo_fix_risk_many.argtypes = [C.c_void_p, C.c_int64] + [C.c_void_p] * 4
-        L.lpo_fix_risk_fadd_mismatches.restype = C.c_int64
+        L.lpo_fix_risk_many.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
         L.lpo_poisson_many.argtypes = [C.c_uint64, C.c_double, C.c_int64, C.POINTER(C.c_int64)]
         L.lpo_gamma_many.argtypes = [C.c_uint64, C.c_double, C.c_int64, C.POINTER(C.c_double)]
         L.lpo_negbinom_many.argtypes = [C.c_uint64, C.c_double, C.c_double, C.c_int64, C.POINTER(C.c_int64)]
@@ -232,18 +231,14 @@ def count_seirp(node_id, disease_state, strain, potentially_paralyzed, paralyzed
 
 
 def fix_risk_many(r):
-    """(double-precision, integer-bits, single-precision and addition-form
-    fixed-point weights) of the float32 array r."""
+    """(double-precision, integer-bits and single-precision fixed-point
+    weights) of the float32 array r."""
     r = np.ascontiguousarray(r, dtype=np.float32)
-    a, b, c, d = (np.empty(len(r), np.uint64) for _ in range(4))
-    lib().lpo_fix_risk_many(r.ctypes.data, len(r), a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data)
-    return a, b, c, d
-
-
-def fix_risk_fadd_mismatches():
-    """Float bit patterns (all 2^32) whose addition-form weight differs from
-    the double-precision definition."""
-    return int(lib().lpo_fix_risk_fadd_mismatches())
+    a = np.empty(len(r), np.uint64)
+    b = np.empty(len(r), np.uint64)
+    c = np.empty(len(r), np.uint64)
+    lib().lpo_fix_risk_many(r.ctypes.data, len(r), a.ctypes.data, b.ctypes.data, c.ctypes.data)
+    return a, b, c
 
 
 def init_columns(desc, parts, cols):
