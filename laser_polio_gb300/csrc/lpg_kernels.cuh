@@ -2656,52 +2656,81 @@ __device__ __forceinline__ int team_first_above(const Team& tm, const int64_t* o
   return lo;
 }
 
-/* Round 0's targets for a team size T: each located on the frozen CDF and
- * claimed at once by the team's first lane, which keeps its first two
- * claims in registers and stores later ones' slots in hits[q]; then the
- * grid barrier, after which the claims are settled (state 1, sub-block
- * weight): the first two by the first lane, the later ones spread over the
- * team's lanes.  Returns false when the barrier's wait ran out. */
+/* Last g in [0, G) with off[g] <= q (off ascending from off[0] = 0, q below
+ * off[G]), by one lane. */
+__device__ __forceinline__ int node_of_target(const int64_t* off, int G, int64_t q) {
+  int lo = 0, hi = G; /* off[lo] <= q < off[hi] */
+  while (hi - lo > 1) {
+    const int m = (lo + hi) >> 1;
+    if (off[m] <= q) lo = m;
+    else hi = m;
+  }
+  return lo;
+}
+
+/* Round 0's targets for a team size T.  A team takes its targets T at a
+ * time: lane l of the team finds the node and forms the uniform of the
+ * batch's l-th target (target q0 + (b T + l) nteams), the team then locates
+ * the batch's targets one after another on the frozen CDF, and each lane
+ * claims its own target's agent (claim0), so that the per-target work that
+ * is not the search (node, uniform, claim, strain draw) runs once per lane
+ * rather than once per team.  A lane keeps its first claim in registers and
+ * stores later ones' slots in hits[q]; then the grid barrier, after which
+ * each lane settles its claims (state 1, sub-block weight).  Returns false
+ * when the barrier's wait ran out. */
 template <int T>
 __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs, const SelInfo* info, int64_t K) {
   const int G = W.G;
   const Team tm = make_team(T);
   const int64_t nteams = ((int64_t)gridDim.x * blockDim.x) / T;
   const int64_t q0 = (int64_t)(threadIdx.x / T) * gridDim.x + blockIdx.x;
-  uint32_t h0 = LPG_NONE, h1 = LPG_NONE;
-  uint64_t w0 = 0, w1 = 0;
-  int it = 0;
+  uint32_t h0 = LPG_NONE;
+  uint64_t w0 = 0;
   /* warp-uniform trip count: every lane stays until no team of its warp has a target */
-  for (int64_t q = q0; __any_sync(FULLMASK, q < K); q += nteams, ++it) {
+  int b = 0;
+  for (int64_t qb = q0; __any_sync(FULLMASK, qb < K); qb += (int64_t)T * nteams, ++b) {
+    /* this lane's target of the batch */
+    const int64_t q = qb + (int64_t)tm.l * nteams;
     const bool act = q < K;
-    SelInfo N;
+    int g = 0;
     uint64_t v = 0;
-    const int32_t* ls = W.node_chunks[0];
-    /* the node of target q: the last g with offs[g] <= q */
-    const int g = team_first_above<T>(tm, offs, 0, act ? G : 0, q) - 1;
+    int32_t la = 0, ln = 1, lcsr = 0;
     if (act) {
-      N = info[g];
-      const int64_t j = q - offs[g];
-      v = lpg_scale_target(lpg_u53(N.seed, LPG_P_SELECT, N.t, (uint64_t)N.i, 0, (uint64_t)j), N.T);
-      ls = W.node_chunks[N.csr] + N.a;
-    } else {
-      N.a = 0;
-      N.n = 1;
+      g = node_of_target(offs, G, q);
+      const SelInfo& N = info[g];
+      v = lpg_scale_target(lpg_u53(N.seed, LPG_P_SELECT, N.t, (uint64_t)N.i, 0, (uint64_t)(q - offs[g])), N.T);
+      la = N.a;
+      ln = N.n;
+      lcsr = N.csr;
     }
-    uint32_t word = 0;
-    float rk = 0.f;
-    const uint32_t hit = locate_team_t<T>(W, ls, W.cpref + N.a, N.n, v, 0, act, &word, &rk);
-    if (act && tm.l == 0) {
+    /* the batch's targets are a prefix of the team's lanes (q ascends with l) */
+    const int nk = __reduce_max_sync(FULLMASK, (unsigned)__popc(team_ballot(tm, act)));
+    uint32_t my_hit = LPG_NONE, my_word = 0;
+    float my_rk = 0.f;
+    for (int k = 0; k < nk; ++k) {
+      const bool ak = __shfl_sync(FULLMASK, (int)act, k, T) != 0;
+      const uint64_t vk = __shfl_sync(FULLMASK, v, k, T);
+      const int32_t ak_a = __shfl_sync(FULLMASK, la, k, T);
+      const int32_t ak_n = __shfl_sync(FULLMASK, ln, k, T);
+      const int32_t ak_c = __shfl_sync(FULLMASK, lcsr, k, T);
+      const int32_t* ls = W.node_chunks[ak_c] + ak_a;
+      uint32_t word = 0;
+      float rk = 0.f;
+      const uint32_t hit = locate_team_t<T>(W, ls, W.cpref + ak_a, ak ? ak_n : 1, vk, 0, ak, &word, &rk);
+      if (tm.l == k) {
+        my_hit = hit;
+        my_word = word;
+        my_rk = rk;
+      }
+    }
+    if (act) {
       uint32_t won_at = LPG_NONE;
       uint64_t w = 0;
-      if (hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
-      else if (claim0(W, hit, word, rk, g, N, &w)) won_at = hit;
-      if (it == 0) {
+      if (my_hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
+      else if (claim0(W, my_hit, my_word, my_rk, g, info[g], &w)) won_at = my_hit;
+      if (b == 0) {
         h0 = won_at;
         w0 = w;
-      } else if (it == 1) {
-        h1 = won_at;
-        w1 = w;
       } else {
         W.hits[q] = won_at;
       }
@@ -2710,12 +2739,9 @@ __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs,
   /* every target of the round located and claimed: the claimed agents
    * become exposed and leave their sub-blocks' weights */
   if (!grid_sync(W.grid_bar, W.wait_spin, W.test_bar_skip && blockIdx.x == 0)) return false;
-  if (tm.l == 0) {
-    claim0_finish(W, h0, w0);
-    claim0_finish(W, h1, w1);
-  }
-  /* the team's later claims, lane l taking its turns 2 + l, 2 + l + T, ... */
-  for (int64_t q = q0 + (2 + (int64_t)tm.l) * nteams; q < K; q += (int64_t)T * nteams) {
+  claim0_finish(W, h0, w0);
+  /* this lane's later claims: batches 1, 2, ... */
+  for (int64_t q = q0 + ((int64_t)T + tm.l) * nteams; q < K; q += (int64_t)T * nteams) {
     const uint32_t h = W.hits[q];
     if (h != LPG_NONE) claim0_finish(W, h, fix_risk(W.risk[h]));
   }
