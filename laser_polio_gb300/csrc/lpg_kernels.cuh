@@ -2656,9 +2656,10 @@ __device__ __forceinline__ int team_first_above(const Team& tm, const int64_t* o
   return lo;
 }
 
-/* Last g in [lo, hi) with off[g] <= q, given off[lo] <= q < off[hi], by
- * one lane. */
-__device__ __forceinline__ int node_of_target(const int64_t* off, int lo, int hi, int64_t q) {
+/* Last g in [0, G) with off[g] <= q (off ascending from off[0] = 0, q below
+ * off[G]), by one lane. */
+__device__ __forceinline__ int node_of_target(const int64_t* off, int G, int64_t q) {
+  int lo = 0, hi = G; /* off[lo] <= q < off[hi] */
   while (hi - lo > 1) {
     const int m = (lo + hi) >> 1;
     if (off[m] <= q) lo = m;
@@ -2668,9 +2669,8 @@ __device__ __forceinline__ int node_of_target(const int64_t* off, int lo, int hi
 }
 
 /* Round 0's targets for a team size T.  A team takes its targets T at a
- * time: the team finds the nodes of the batch's first and last targets
- * together, lane l of the team the node of the batch's l-th target (target
- * q0 + (b T + l) nteams) between them and forms its uniform, the team then locates
+ * time: lane l of the team finds the node and forms the uniform of the
+ * batch's l-th target (target q0 + (b T + l) nteams), the team then locates
  * the batch's targets one after another on the frozen CDF, and each lane
  * claims its own target's agent (claim0), so that the per-target work that
  * is not the search (node, uniform, claim, strain draw) runs once per lane
@@ -2692,24 +2692,19 @@ __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs,
     /* this lane's target of the batch */
     const int64_t q = qb + (int64_t)tm.l * nteams;
     const bool act = q < K;
-    /* the batch's targets are a prefix of the team's lanes (q ascends with l) */
-    const int nt_team = __popc(team_ballot(tm, act));
-    /* nodes of the batch's first and last targets; those of the others lie between */
-    const int g_lo = team_first_above<T>(tm, offs, 0, nt_team ? G : 0, qb) - 1;
-    const int64_t q_last = qb + (int64_t)(nt_team > 0 ? nt_team - 1 : 0) * nteams;
-    const int g_hi = team_first_above<T>(tm, offs, g_lo < 0 ? 0 : g_lo, nt_team ? G : 0, q_last) - 1;
     int g = 0;
     uint64_t v = 0;
     int32_t la = 0, ln = 1, lcsr = 0;
     if (act) {
-      g = g_lo == g_hi ? g_lo : node_of_target(offs, g_lo, g_hi + 1, q);
+      g = node_of_target(offs, G, q);
       const SelInfo& N = info[g];
       v = lpg_scale_target(lpg_u53(N.seed, LPG_P_SELECT, N.t, (uint64_t)N.i, 0, (uint64_t)(q - offs[g])), N.T);
       la = N.a;
       ln = N.n;
       lcsr = N.csr;
     }
-    const int nk = __reduce_max_sync(FULLMASK, (unsigned)nt_team);
+    /* the batch's targets are a prefix of the team's lanes (q ascends with l) */
+    const int nk = __reduce_max_sync(FULLMASK, (unsigned)__popc(team_ballot(tm, act)));
     uint32_t my_hit = LPG_NONE, my_word = 0;
     float my_rk = 0.f;
     for (int k = 0; k < nk; ++k) {
