@@ -1220,7 +1220,6 @@ __device__ __forceinline__ void ds_queue_step(DevWorld& W, uint64_t e, bool on) 
   const int64_t G = W.G;
   int g = -1, st = 0;
   int32_t dS = 0, dE = 0, dI = 0, dR = 0, dPP = 0, dP = 0, nPP = 0, nP = 0, nDead = 0;
-  uint64_t dbb = 0; /* change of the node's infectivity total of strain st, modulo 2^64 */
   if (on) {
     const int64_t pos = (int64_t)(uint32_t)e;
     const uint32_t kind = (uint32_t)(e >> 32) & 3u;
@@ -1245,7 +1244,8 @@ __device__ __forceinline__ void ds_queue_step(DevWorld& W, uint64_t e, bool on) 
           dE = -1;
         } else {
           dI = -1;
-          dbb = neg64(fix_beta(W.inf[pos], rp->strain_scal[st]));
+          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
         }
         /* timers frozen at death: brought up to the step of t - 1 (they
          * count down only where disease states are stepped) */
@@ -1279,7 +1279,8 @@ __device__ __forceinline__ void ds_queue_step(DevWorld& W, uint64_t e, bool on) 
           s = 2;
           dE -= 1;
           dI += 1;
-          dbb += fix_beta(W.inf[pos], rp->strain_scal[st]);
+          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], (unsigned long long)bw);
         }
         et = dec_i8(et);
         W.et[pos] = et;
@@ -1289,7 +1290,8 @@ __device__ __forceinline__ void ds_queue_step(DevWorld& W, uint64_t e, bool on) 
           s = 3;
           dI -= 1;
           dR += 1;
-          dbb += neg64(fix_beta(W.inf[pos], rp->strain_scal[st]));
+          const uint64_t bw = fix_beta(W.inf[pos], rp->strain_scal[st]);
+          if (bw) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], neg64(bw));
         }
         it = dec_i8(it);
         W.it[pos] = it;
@@ -1336,8 +1338,6 @@ __device__ __forceinline__ void ds_queue_step(DevWorld& W, uint64_t e, bool on) 
   const unsigned by_ns = __match_any_sync(act, g * LPG_MAX_STRAINS + st);
   warp_add(&W.tot[(int64_t)(TT_E0 + st) * G + g], by_ns, dE);
   warp_add(&W.tot[(int64_t)(TT_I0 + st) * G + g], by_ns, dI);
-  const uint64_t tbb = warp_sum_u64(by_ns, dbb);
-  if ((threadIdx.x & 31) == __ffs(by_ns) - 1 && tbb) atomicAdd((unsigned long long*)&W.bb[(int64_t)st * G + g], tbb);
 }
 
 
@@ -2560,15 +2560,14 @@ __device__ __forceinline__ bool claim(DevWorld& W, uint32_t hit, int g, const Se
   return true;
 }
 
-/* A round-0 claim: state 0 -> LPG_DS_CLAIMED (the round's other targets
- * still see the agent's weight), the agent's strain and event tick and its
- * sub-block's earliest event.  word and risk are the slot's state word and
- * risk as the locate read them (the word is the first guess of the
- * compare-and-swap).  Returns whether this target claimed it, with its
- * strain and weight: the node and chunk totals are added once per warp
- * (claim0_totals), the sub-block weight after the round (claim0_finish). */
-__device__ __forceinline__ bool claim0_agent(DevWorld& W, uint32_t hit, uint32_t word, float risk, const SelInfo& N,
-                                             int* s_out, uint64_t* w_out) {
+/* A round-0 claim, made as soon as the target is located: state 0 ->
+ * LPG_DS_CLAIMED (the round's other targets still see the agent's weight),
+ * the exposure and every total but the sub-block weight, which the claimer
+ * removes after the round (claim0_finish).  word and risk are the slot's
+ * state word and risk as the locate read them (the word is the first guess
+ * of the compare-and-swap). */
+__device__ __forceinline__ bool claim0(DevWorld& W, uint32_t hit, uint32_t word, float risk, int g,
+                                       const SelInfo& N, uint64_t* w_out) {
   const int64_t pos = hit;
   const uint32_t ref = W.ref[pos];
   const int8_t et = W.et[pos];
@@ -2587,42 +2586,8 @@ __device__ __forceinline__ bool claim0_agent(DevWorld& W, uint32_t hit, uint32_t
     old = prev;
   }
   if (!won) return false;
-  int s = 0;
-  bool found = false;
-#pragma unroll
-  for (int k = 0; k < LPG_MAX_STRAINS; ++k)
-    if (!found && k < N.ns && r53 < N.thr[k]) {
-      s = k;
-      found = true;
-    }
-  W.strain[pos] = (int8_t)s;
-  const int32_t e1 = N.t + 1 + (et > 0 ? et : 0); /* first step in E at t + 1 (model.py:393-454) */
-  W.evt[pos] = e1;
-  atomicMin(&W.sub_evt[pos >> 7], e1);
-  *s_out = s;
-  *w_out = fix_risk(risk);
+  *w_out = expose_claimed(W, pos, g, N, r53, et, risk, false);
   return true;
-}
-
-/* The totals of the agents the lanes of a warp claimed in round 0 (won):
- * S, E and new exposures by strain, unique exposures and susceptible weight
- * per node, weight per chunk, each added once per node (or chunk) of the
- * warp; the same sums as expose_claimed adds one agent at a time.  All 32
- * lanes call it. */
-__device__ __forceinline__ void claim0_totals(DevWorld& W, bool won, int g, int s, uint32_t hit, uint64_t w) {
-  const unsigned wm = __ballot_sync(FULLMASK, won);
-  if (!won) return;
-  const int64_t G = W.G;
-  const unsigned by_node = __match_any_sync(wm, g);
-  warp_add(&W.tot[(int64_t)TT_S * G + g], by_node, -1);
-  if ((threadIdx.x & 31) == __ffs(by_node) - 1) atomicAdd((unsigned long long*)&W.uniq[g], (unsigned long long)__popc(by_node));
-  warp_sub_w((unsigned long long*)&W.sw[g], by_node, w);
-  const unsigned by_ns = __match_any_sync(wm, g * LPG_MAX_STRAINS + s);
-  warp_add(&W.tot[(int64_t)(TT_E0 + s) * G + g], by_ns, 1);
-  warp_add(&W.ev[(int64_t)(EV_TXNEW0 + s) * G + g], by_ns, 1);
-  const long long cid = (long long)hit / LPG_CHUNK;
-  const unsigned by_chunk = __match_any_sync(wm, cid);
-  warp_sub_w((unsigned long long*)&W.chunk_w[cid], by_chunk, w);
 }
 
 /* After round 0: the claimed agent becomes exposed (state 1) and leaves its
@@ -2707,10 +2672,9 @@ __device__ __forceinline__ int node_of_target(const int64_t* off, int G, int64_t
  * time: lane l of the team finds the node and forms the uniform of the
  * batch's l-th target (target q0 + (b T + l) nteams), the team then locates
  * the batch's targets one after another on the frozen CDF, and each lane
- * claims its own target's agent (claim0_agent; the warp's totals once per
- * node, claim0_totals), so that the per-target work that is not the search
- * (node, uniform, claim, strain draw) runs once per lane rather than once
- * per team.  A lane keeps its first claim in registers and
+ * claims its own target's agent (claim0), so that the per-target work that
+ * is not the search (node, uniform, claim, strain draw) runs once per lane
+ * rather than once per team.  A lane keeps its first claim in registers and
  * stores later ones' slots in hits[q]; then the grid barrier, after which
  * each lane settles its claims (state 1, sub-block weight).  Returns false
  * when the barrier's wait ran out. */
@@ -2759,12 +2723,11 @@ __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs,
         my_rk = rk;
       }
     }
-    uint32_t won_at = LPG_NONE;
-    uint64_t w = 0;
-    int st = 0;
     if (act) {
+      uint32_t won_at = LPG_NONE;
+      uint64_t w = 0;
       if (my_hit == LPG_NONE) W.reps[W.node_rep[g]].error = LPG_ERR_INTERNAL;
-      else if (claim0_agent(W, my_hit, my_word, my_rk, info[g], &st, &w)) won_at = my_hit;
+      else if (claim0(W, my_hit, my_word, my_rk, g, info[g], &w)) won_at = my_hit;
       if (b == 0) {
         h0 = won_at;
         w0 = w;
@@ -2772,7 +2735,6 @@ __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs,
         W.hits[q] = won_at;
       }
     }
-    claim0_totals(W, won_at != LPG_NONE, g, st, won_at, w);
   }
   /* every target of the round located and claimed: the claimed agents
    * become exposed and leave their sub-blocks' weights */
@@ -2792,7 +2754,7 @@ __device__ __forceinline__ bool round0_targets(DevWorld& W, const int64_t* offs,
  * prefix.  Round 0 runs over all nodes at once in one cooperative launch
  * (k_sel_round0): every CTA forms the target offsets in its shared memory;
  * targets go round-robin over the CTAs, each located by a team of lanes on
- * the round's frozen CDF and claimed (claim0_agent: the agent keeps its
+ * the round's frozen CDF and claimed at once (claim0: the agent keeps its
  * weight for the round's other targets); after a grid barrier the claimers
  * settle the sub-block weights.  The few collisions left after round 0 are
  * redrawn per node by one CTA in later rounds (k_sel_rounds), with CTA
