@@ -460,6 +460,12 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
     const uint64_t wg = run_sum_u64(w, mg), wc = run_sum_u64(w, mc), wsb = run_sum_u64(w, ms);
     const int32_t ng = run_sum_i32(one, mg);
     const int32_t dmin = run_min_i32(dod, ms), rmin = run_min_i32(rdt, ms);
+    {
+      /* the RI due lists hold the initial population only: a newborn due in
+       * the run sends its simulation's later RI ticks back to the index */
+      const int32_t wmin = __reduce_min_sync(FULLMASK, rdt);
+      if (lane == 0 && wmin != LPG_NO_DOD && wmin < rp->rdt_new_min) atomicMin(&W.reps[blockIdx.y].rdt_new_min, wmin);
+    }
     if (on && hg) {
       atomicAdd(&W.tot[(int64_t)TT_S * G + g], ng);
       if (wg) atomicAdd((unsigned long long*)&W.sw[g], (unsigned long long)wg);
@@ -548,7 +554,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
 }
 
 /* per-simulation flags of the launch, cached in shared memory */
-enum { SF_WORK = 1, SF_DENSE = 2, SF_RI = 16, SF_SIA = 32 };
+enum { SF_WORK = 1, SF_DENSE = 2, SF_RI = 16, SF_SIA = 32, SF_LIST = 64 };
 
 struct SweepPlan {
   int32_t total, nreps;
@@ -984,6 +990,34 @@ __device__ __noinline__ void ri_direct(DevWorld& W, const DevRep* rp, uint64_t* 
   if (lane == 0 && n_due) atomicAdd(&W.ctr[LPG_CTR_RI_DUE], (unsigned long long)n_due);
 }
 
+/* k_sweep_rs on an RI tick without SIA, for a simulation whose RI due list
+ * holds every agent due today (no newborn has been given a due tick at or
+ * before it): the CTA's share of the tick's list entries, in proportion to
+ * its share [w_lo, w_hi) of the simulation's w_len work items, queueing the
+ * entries still alive whose due tick is today (the same test as ri_due16:
+ * the list was made at the start, and an agent's due tick does not move).
+ * The agents and the queue are those of ri_direct; the sub-block index
+ * sub_rdt is left as it was, still a lower bound.  All threads of the CTA
+ * run it. */
+__device__ __noinline__ void ri_list(DevWorld& W, const DevRep* rp, uint64_t* slab, uint32_t* s_cnt, int64_t w_lo,
+                                     int64_t w_hi, int64_t w_len, int t) {
+  const int bkt = rp->ril_base + t / rp->ri_step;
+  const int64_t e0 = W.ril_off[bkt], n = (int64_t)W.ril_off[bkt + 1] - e0;
+  const int64_t a = e0 + n * w_lo / w_len, b = e0 + n * w_hi / w_len;
+  for (int64_t i0 = a; i0 < b; i0 += blockDim.x) {
+    const int64_t i = i0 + threadIdx.x;
+    bool due = false;
+    uint32_t pos = 0;
+    if (i < b) {
+      pos = __ldcg(&W.ril_pos[i]);
+      due = W.ds[pos] >= 0 && W.rdt[pos] == t;
+    }
+    const uint32_t at = slab_reserve(s_cnt, due ? 1u : 0u);
+    if (due) slab[at] = q_entry(pos, QB_RI, 0);
+  }
+  if (threadIdx.x == 0 && b > a) atomicAdd(&W.ctr[LPG_CTR_RI_LIST], (unsigned long long)(b - a));
+}
+
 /* The first work item at or after w whose simulation is staged (dense), or w1. */
 __device__ __forceinline__ int32_t dense_from(const SweepPlan& P, int32_t w, int32_t w1) {
   while (w < w1) {
@@ -1019,7 +1053,9 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
         if (rp->ri_tick) f |= SF_RI;
         if (rp->sia_n > 0) f |= SF_SIA;
         if (f) f |= SF_WORK;
-        if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due index */
+        if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due list or the due index */
+        else if ((f & SF_RI) && rp->ril_nb > 0 && rp->cur_t < rp->rdt_new_min && rp->cur_t / rp->ri_step < rp->ril_nb)
+          f |= SF_LIST;
       }
       P.flags[r] = f;
       P.cbase[r] = rp->chunk_base;
@@ -1056,9 +1092,13 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
       (void)stage_end(P, w, w1, &r);
       const int32_t we = min(w1, P.off[r + 1]);
       if ((P.flags[r] & (SF_WORK | SF_DENSE)) == SF_WORK) {
-        const int64_t sb0 = (P.cbase[r] + (int64_t)(w - P.off[r])) * LPG_NSUB;
-        ri_direct(W, &W.reps[r], slab, &s_qcnt, sb0, (int64_t)(we - w) * LPG_NSUB, P.tick[r],
-                  reinterpret_cast<uint32_t*>(sm_stage), &s_ndue);
+        if (P.flags[r] & SF_LIST) {
+          ri_list(W, &W.reps[r], slab, &s_qcnt, w - P.off[r], we - P.off[r], P.off[r + 1] - P.off[r], P.tick[r]);
+        } else {
+          const int64_t sb0 = (P.cbase[r] + (int64_t)(w - P.off[r])) * LPG_NSUB;
+          ri_direct(W, &W.reps[r], slab, &s_qcnt, sb0, (int64_t)(we - w) * LPG_NSUB, P.tick[r],
+                    reinterpret_cast<uint32_t*>(sm_stage), &s_ndue);
+        }
       }
       w = we;
     }
@@ -3188,6 +3228,29 @@ __global__ void k_ri_index(DevWorld W, int32_t* out, int at_start, int* bad) {
       }
       m = __reduce_min_sync(FULLMASK, m);
       if (lane == 0 && q < np) atomicMin(&out[pos >> 7], m);
+    }
+  }
+}
+
+/* The RI due lists, at the start (lpg_start): the alive agents of each
+ * simulation with a due list whose RI due tick falls in the run, counted
+ * into cnt[ril_base + tick / ri_step] (fill null), or written to ril_pos at
+ * fill[ril_base + tick / ri_step] (the buckets' first entries, advanced as
+ * entries are written; their order within a bucket does not matter). */
+__global__ void k_ri_list(DevWorld W, int32_t* cnt, int32_t* fill) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < W.n_reps; ++r) {
+    const DevRep* rp = &W.reps[r];
+    if (rp->ril_nb <= 0) continue;
+    const int64_t p0 = (int64_t)rp->chunk_base * LPG_CHUNK, np = (int64_t)rp->used_chunks * LPG_CHUNK;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < np; q += stride) {
+      const int64_t pos = p0 + q;
+      if (W.ds[pos] < 0) continue;
+      const int32_t d = W.rdt[pos];
+      if (d == LPG_NO_DOD || d < 1 || d >= rp->nt) continue;
+      const int b = rp->ril_base + d / rp->ri_step;
+      if (fill) W.ril_pos[atomicAdd(&fill[b], 1)] = (uint32_t)pos;
+      else atomicAdd(&cnt[b], 1);
     }
   }
 }
