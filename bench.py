@@ -167,8 +167,8 @@ NCU_TRAFFIC_SOURCE = {
 #     bytes and 128 risks (512 B); per agent exposed, its reference index,
 #     state (claimed, then exposed), strain, timers, event tick and its
 #     index (15 B).
-#   k_sweep_rs (k_sweep_b) on RI ticks: through the RI due list, per entry
-#     its position, state byte and due tick (9 B); through the index, 4 B per
+#   k_sweep_rs (k_sweep_b) on RI ticks: through the RI due lists, 4 B per
+#     list entry read (the due ones' state bytes with the queue); through the index, 4 B per
 #     RI due index entry read and per visited sub-block its state,
 #     chronically-missed flags, RI timers, reference indexes and dates of
 #     birth (128 x 12 B) and the index write (4 B).
@@ -193,7 +193,7 @@ SEL_CLAIM_B = 15.0
 NODE_TX_CHUNK_B = 20.0
 NODE_TX_NET_B = 16.0  # a network entry in its two fixed-point parts
 NODE_TX_NODE_B = 248.0
-RI_INDEX_B, RI_DUE_B, RI_LIST_B = 4.0, 128.0 * 12.0 + 4.0, 9.0
+RI_INDEX_B, RI_DUE_B, RI_LIST_B = 4.0, 128.0 * 12.0 + 4.0, 4.0
 
 
 def merge_selection(prof):

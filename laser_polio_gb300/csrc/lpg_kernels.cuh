@@ -990,32 +990,37 @@ __device__ __noinline__ void ri_direct(DevWorld& W, const DevRep* rp, uint64_t* 
   if (lane == 0 && n_due) atomicAdd(&W.ctr[LPG_CTR_RI_DUE], (unsigned long long)n_due);
 }
 
-/* k_sweep_rs on an RI tick without SIA, for a simulation whose RI due list
- * holds every agent due today (no newborn has been given a due tick at or
- * before it): the CTA's share of the tick's list entries, in proportion to
- * its share [w_lo, w_hi) of the simulation's w_len work items, queueing the
- * entries still alive whose due tick is today (the same test as ri_due16:
- * the list was made at the start, and an agent's due tick does not move).
- * The agents and the queue are those of ri_direct; the sub-block index
- * sub_rdt is left as it was, still a lower bound.  All threads of the CTA
- * run it. */
-__device__ __noinline__ void ri_list(DevWorld& W, const DevRep* rp, uint64_t* slab, uint32_t* s_cnt, int64_t w_lo,
-                                     int64_t w_hi, int64_t w_len, int t) {
-  const int bkt = rp->ril_base + t / rp->ri_step;
-  const int64_t e0 = W.ril_off[bkt], n = (int64_t)W.ril_off[bkt + 1] - e0;
-  const int64_t a = e0 + n * w_lo / w_len, b = e0 + n * w_hi / w_len;
-  for (int64_t i0 = a; i0 < b; i0 += blockDim.x) {
-    const int64_t i = i0 + threadIdx.x;
-    bool due = false;
-    uint32_t pos = 0;
-    if (i < b) {
-      pos = __ldcg(&W.ril_pos[i]);
-      due = W.ds[pos] >= 0 && W.rdt[pos] == t;
+/* k_sweep_rs on an RI tick without SIA, for a simulation whose RI due lists
+ * hold every agent due today (no newborn has been given a due tick at or
+ * before it), over its chunks [c0, c1): one warp per chunk reads the
+ * chunk's list in order and queues the entries due today that are still
+ * alive (the test of ri_due16: an agent's due tick does not move), so the
+ * queue keeps position order.  The agents and the queue are those of
+ * ri_direct; the sub-block index sub_rdt is left as it was, still a lower
+ * bound.  All threads of the CTA run it. */
+__device__ __noinline__ void ri_list(DevWorld& W, const DevRep* rp, uint64_t* slab, uint32_t* s_cnt, int64_t c0,
+                                     int64_t c1, int t) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const uint32_t bkt = (uint32_t)(t / rp->ri_step);
+  uint32_t listed = 0;
+  for (int64_t c = c0 + (threadIdx.x >> 5); __any_sync(FULLMASK, c < c1); c += nw) {
+    const bool on_c = c < c1;
+    const int32_t e0 = on_c ? __ldcg(&W.ril_coff[c]) : 0, e1 = on_c ? __ldcg(&W.ril_coff[c + 1]) : 0;
+    listed += (uint32_t)(e1 - e0);
+    for (int32_t i0 = e0; i0 < e1; i0 += 32) { /* warp-uniform: one chunk per warp */
+      const int32_t i = i0 + lane;
+      bool due = false;
+      int64_t pos = 0;
+      if (i < e1) {
+        const uint32_t e = __ldcg(&W.ril_ent[i]);
+        pos = c * LPG_CHUNK + (e & (LPG_CHUNK - 1));
+        due = (e >> 11) == bkt && W.ds[pos] >= 0;
+      }
+      const uint32_t at = slab_reserve(s_cnt, due ? 1u : 0u);
+      if (due) slab[at] = q_entry(pos, QB_RI, 0);
     }
-    const uint32_t at = slab_reserve(s_cnt, due ? 1u : 0u);
-    if (due) slab[at] = q_entry(pos, QB_RI, 0);
   }
-  if (threadIdx.x == 0 && b > a) atomicAdd(&W.ctr[LPG_CTR_RI_LIST], (unsigned long long)(b - a));
+  if (lane == 0 && listed) atomicAdd(&W.ctr[LPG_CTR_RI_LIST], (unsigned long long)listed);
 }
 
 /* The first work item at or after w whose simulation is staged (dense), or w1. */
@@ -1054,7 +1059,7 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
         if (rp->sia_n > 0) f |= SF_SIA;
         if (f) f |= SF_WORK;
         if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due list or the due index */
-        else if ((f & SF_RI) && rp->ril_nb > 0 && rp->cur_t < rp->rdt_new_min && rp->cur_t / rp->ri_step < rp->ril_nb)
+        else if ((f & SF_RI) && rp->ril_on && rp->cur_t < rp->rdt_new_min)
           f |= SF_LIST;
       }
       P.flags[r] = f;
@@ -1093,7 +1098,8 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
       const int32_t we = min(w1, P.off[r + 1]);
       if ((P.flags[r] & (SF_WORK | SF_DENSE)) == SF_WORK) {
         if (P.flags[r] & SF_LIST) {
-          ri_list(W, &W.reps[r], slab, &s_qcnt, w - P.off[r], we - P.off[r], P.off[r + 1] - P.off[r], P.tick[r]);
+          ri_list(W, &W.reps[r], slab, &s_qcnt, P.cbase[r] + (int64_t)(w - P.off[r]), P.cbase[r] + (int64_t)(we - P.off[r]),
+                  P.tick[r]);
         } else {
           const int64_t sb0 = (P.cbase[r] + (int64_t)(w - P.off[r])) * LPG_NSUB;
           ri_direct(W, &W.reps[r], slab, &s_qcnt, sb0, (int64_t)(we - w) * LPG_NSUB, P.tick[r],
@@ -3232,26 +3238,34 @@ __global__ void k_ri_index(DevWorld W, int32_t* out, int at_start, int* bad) {
   }
 }
 
-/* The RI due lists, at the start (lpg_start): the alive agents of each
- * simulation with a due list whose RI due tick falls in the run, counted
- * into cnt[ril_base + tick / ri_step] (fill null), or written to ril_pos at
- * fill[ril_base + tick / ri_step] (the buckets' first entries, advanced as
- * entries are written; their order within a bucket does not matter). */
-__global__ void k_ri_list(DevWorld W, int32_t* cnt, int32_t* fill) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int r = 0; r < W.n_reps; ++r) {
-    const DevRep* rp = &W.reps[r];
-    if (rp->ril_nb <= 0) continue;
-    const int64_t p0 = (int64_t)rp->chunk_base * LPG_CHUNK, np = (int64_t)rp->used_chunks * LPG_CHUNK;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < np; q += stride) {
-      const int64_t pos = p0 + q;
-      if (W.ds[pos] < 0) continue;
-      const int32_t d = W.rdt[pos];
-      if (d == LPG_NO_DOD || d < 1 || d >= rp->nt) continue;
-      const int b = rp->ril_base + d / rp->ri_step;
-      if (fill) W.ril_pos[atomicAdd(&fill[b], 1)] = (uint32_t)pos;
-      else atomicAdd(&cnt[b], 1);
+/* The RI due lists, at the start (lpg_start), one warp per chunk of a
+ * simulation with lists: the chunk's alive agents whose RI due tick falls
+ * in the run, counted into cnt[chunk] (ent null), or written in position
+ * order from ril_coff[chunk] (ent: W.ril_ent). */
+__global__ void k_ri_list(DevWorld W, int32_t* cnt, uint32_t* ent) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < W.total_chunks; c += warps) {
+    const int4 m = W.cmeta[c];
+    if (m.x < 0) continue; /* warp-uniform: one chunk per warp */
+    const DevRep* rp = &W.reps[W.node_rep[m.x]];
+    if (!rp->ril_on) continue;
+    int32_t n = 0, at = ent ? W.ril_coff[c] : 0;
+    for (int o0 = 0; o0 < LPG_CHUNK; o0 += 32) {
+      const int64_t pos = c * LPG_CHUNK + o0 + lane;
+      bool in = false;
+      int32_t d = LPG_NO_DOD;
+      if (W.ds[pos] >= 0) {
+        d = W.rdt[pos];
+        in = d != LPG_NO_DOD && d >= 1 && d < rp->nt;
+      }
+      const unsigned b = __ballot_sync(FULLMASK, in);
+      if (ent && in)
+        ent[at + __popc(b & ((1u << lane) - 1u))] = ((uint32_t)(d / rp->ri_step) << 11) | (uint32_t)(o0 + lane);
+      at += __popc(b);
+      n += __popc(b);
     }
+    if (!ent && lane == 0) cnt[c] = n;
   }
 }
 
