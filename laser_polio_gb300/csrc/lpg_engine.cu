@@ -1026,6 +1026,7 @@ extern "C" int lpg_start(lpg_handle* h) {
     hr[r].vd_tick = hr[r].ri_tick = hr[r].sia_n = hr[r].seed_n = 0;
     hr[r].nb_total = 0;
     hr[r].rdt_new_min = LPG_NO_DOD;
+    hr[r].ril_maxb = -1;
     /* due ticks / step must fit the entries' 21 bits */
     hr[r].ril_on = hr[r].ri_enabled && (hr[r].comps & LPG_COMP_RI) && hr[r].ri_step > 0 && hr[r].nt > 1 &&
                    (int64_t)hr[r].nt / hr[r].ri_step < (1 << 21);

@@ -160,6 +160,8 @@ typedef struct {
   int32_t ei_sum;      /* k_end: nodes with E > 0 plus nodes with I > 0 (the next tick's stop rule) */
   int32_t ril_on;      /* the RI due lists (lpg_start) cover this simulation's initial population */
   int32_t rdt_new_min; /* earliest RI due tick given to a newborn so far (LPG_NO_DOD: none) */
+  int32_t ril_maxb;    /* latest due tick / RI step in its lists (-1: empty) */
+  int32_t pad3;
 } DevRep;
 
 /* Global device state shared by the kernels of one handle. */

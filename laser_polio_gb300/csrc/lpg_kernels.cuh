@@ -118,6 +118,14 @@ __device__ __forceinline__ unsigned long long neg64(uint64_t w) { return (unsign
 /* RI runs for the simulation: RI_ABM among the components and vx_prob_ri
  * set (model.py:1920-1923).  Only then do the timers count down. */
 __device__ __forceinline__ bool ri_runs(const DevRep* rp) { return (rp->comps & LPG_COMP_RI) && rp->ri_enabled; }
+/* On this tick RI (if it runs) can go through the RI due lists: they hold
+ * every agent due (no newborn has been given a due tick at or before it). */
+__device__ __forceinline__ bool ri_by_list(const DevRep* rp) { return rp->ril_on && rp->cur_t < rp->rdt_new_min; }
+/* An RI tick with agents to queue: through the index, or through lists
+ * that still hold agents due at or after it. */
+__device__ __forceinline__ bool ri_work(const DevRep* rp) {
+  return rp->ri_tick && !(ri_by_list(rp) && rp->cur_t / rp->ri_step > rp->ril_maxb);
+}
 /* RI due tick of an agent from its base timer u, reference index and date
  * of birth (lpg_ri.h). */
 __device__ __forceinline__ int32_t ri_due_of(const DevRep* rp, int16_t u, uint32_t ref, int32_t dob) {
@@ -1055,12 +1063,11 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
       const DevRep* rp = &W.reps[r];
       uint8_t f = 0;
       if (rp->active) {
-        if (rp->ri_tick) f |= SF_RI;
-        if (rp->sia_n > 0) f |= SF_SIA;
+        if (rp->sia_n > 0) f |= SF_SIA | (rp->ri_tick ? SF_RI : 0);
+        else if (ri_work(rp)) f |= SF_RI; /* (none when the lists have nothing due from today on) */
         if (f) f |= SF_WORK;
-        if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due list or the due index */
-        else if ((f & SF_RI) && rp->ril_on && rp->cur_t < rp->rdt_new_min)
-          f |= SF_LIST;
+        if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due lists or the due index */
+        else if ((f & SF_RI) && ri_by_list(rp)) f |= SF_LIST;
       }
       P.flags[r] = f;
       P.cbase[r] = rp->chunk_base;
@@ -1502,7 +1509,7 @@ __global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
     /* nothing queued unless some simulation has RI or SIA work today */
     int any = 0;
     for (int r = 0; r < W.n_reps && !any; ++r)
-      any = W.reps[r].active && (W.reps[r].ri_tick || W.reps[r].sia_n > 0);
+      any = W.reps[r].active && (ri_work(&W.reps[r]) || W.reps[r].sia_n > 0);
     if (!any) return;
   }
   const uint32_t n = q_prefix(W, 1, s_pre, nslabs);
@@ -3250,7 +3257,7 @@ __global__ void k_ri_list(DevWorld W, int32_t* cnt, uint32_t* ent) {
     if (m.x < 0) continue; /* warp-uniform: one chunk per warp */
     const DevRep* rp = &W.reps[W.node_rep[m.x]];
     if (!rp->ril_on) continue;
-    int32_t n = 0, at = ent ? W.ril_coff[c] : 0;
+    int32_t n = 0, at = ent ? W.ril_coff[c] : 0, maxb = -1;
     for (int o0 = 0; o0 < LPG_CHUNK; o0 += 32) {
       const int64_t pos = c * LPG_CHUNK + o0 + lane;
       bool in = false;
@@ -3260,12 +3267,19 @@ __global__ void k_ri_list(DevWorld W, int32_t* cnt, uint32_t* ent) {
         in = d != LPG_NO_DOD && d >= 1 && d < rp->nt;
       }
       const unsigned b = __ballot_sync(FULLMASK, in);
+      if (in) maxb = max(maxb, d / rp->ri_step);
       if (ent && in)
         ent[at + __popc(b & ((1u << lane) - 1u))] = ((uint32_t)(d / rp->ri_step) << 11) | (uint32_t)(o0 + lane);
       at += __popc(b);
       n += __popc(b);
     }
-    if (!ent && lane == 0) cnt[c] = n;
+    if (!ent) {
+      maxb = __reduce_max_sync(FULLMASK, maxb);
+      if (lane == 0) {
+        cnt[c] = n;
+        if (maxb >= 0) atomicMax(&W.reps[W.node_rep[m.x]].ril_maxb, maxb);
+      }
+    }
   }
 }
 
