@@ -408,6 +408,7 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
   const int64_t* nbe = end_sm ? s_end : W.nb_end + nb;
   const int64_t* km = km_sm ? s_km : rp->km;
   const bool ri_on = ri_runs(rp);
+  int32_t rdt_lo = LPG_NO_DOD; /* earliest RI due tick this thread gave a newborn */
   for (int64_t j0 = (int64_t)blockIdx.x * blockDim.x;; j0 += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = j0 + threadIdx.x;
     if (__all_sync(FULLMASK, j >= total)) break;
@@ -468,12 +469,7 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
     const uint64_t wg = run_sum_u64(w, mg), wc = run_sum_u64(w, mc), wsb = run_sum_u64(w, ms);
     const int32_t ng = run_sum_i32(one, mg);
     const int32_t dmin = run_min_i32(dod, ms), rmin = run_min_i32(rdt, ms);
-    {
-      /* the RI due lists hold the initial population only: a newborn due in
-       * the run sends its simulation's later RI ticks back to the index */
-      const int32_t wmin = __reduce_min_sync(FULLMASK, rdt);
-      if (lane == 0 && wmin != LPG_NO_DOD && wmin < rp->rdt_new_min) atomicMin(&W.reps[blockIdx.y].rdt_new_min, wmin);
-    }
+    rdt_lo = min(rdt_lo, rdt);
     if (on && hg) {
       atomicAdd(&W.tot[(int64_t)TT_S * G + g], ng);
       if (wg) atomicAdd((unsigned long long*)&W.sw[g], (unsigned long long)wg);
@@ -485,6 +481,11 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
       if (wsb) atomicAdd((unsigned long long*)&W.sub_w[ks], (unsigned long long)wsb);
     }
   }
+  /* the RI due lists hold the initial population only: a newborn due in the
+   * run sends its simulation's later RI ticks back to the index (every lane
+   * left the loop together) */
+  rdt_lo = __reduce_min_sync(FULLMASK, rdt_lo);
+  if (lane == 0 && rdt_lo != LPG_NO_DOD && rdt_lo < rp->rdt_new_min) atomicMin(&W.reps[blockIdx.y].rdt_new_min, rdt_lo);
 }
 
 /* The sweeps.
