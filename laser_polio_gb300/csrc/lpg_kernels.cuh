@@ -483,9 +483,9 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
   }
   /* the RI due lists hold the initial population only: a newborn due in the
    * run sends its simulation's later RI ticks back to the index (every lane
-   * left the loop together) */
+   * left the loop together; a due tick past the run changes nothing) */
   rdt_lo = __reduce_min_sync(FULLMASK, rdt_lo);
-  if (lane == 0 && rdt_lo != LPG_NO_DOD && rdt_lo < rp->rdt_new_min) atomicMin(&W.reps[blockIdx.y].rdt_new_min, rdt_lo);
+  if (lane == 0 && rdt_lo < rp->nt && rdt_lo < rp->rdt_new_min) atomicMin(&W.reps[blockIdx.y].rdt_new_min, rdt_lo);
 }
 
 /* The sweeps.
