@@ -386,6 +386,12 @@ static int validate_desc(const lpg_sim_desc& d, int r, std::string* msg) {
   if (d.count < 0 || d.capacity < d.count || d.capacity >= (int64_t)0xFFFFFFF0LL)
     return bad(LPG_ERR_ARG, "sim %d: count %lld / capacity %lld invalid", r, (long long)d.count, (long long)d.capacity);
   if (d.vd_step < 1 || d.ri_step < 1) return bad(LPG_ERR_ARG, "sim %d: step sizes must be >= 1", r);
+  /* an agent's RI timer comes back into the window no sooner than 65536 / step - 1 RI ticks
+   * after it was there, so no agent is due twice while the last RI tick's index is below
+   * 65536 / step; the engine gives each agent one RI due tick a run */
+  if ((d.components & LPG_COMP_RI) && d.ri_enabled && (d.nt - 1) / d.ri_step >= 65536 / d.ri_step)
+    return bad(LPG_ERR_ARG, "sim %d: RI over %d ticks with step %d: an agent's RI timer would come round twice", r,
+               d.nt - 1, d.ri_step);
   if (!d.pop0) return bad(LPG_ERR_ARG, "sim %d: pop0 is required", r);
   if ((d.components & LPG_COMP_TX) && (!d.network || !d.seasonality || !d.strain_r0_scalars || !d.r0_scalars))
     return bad(LPG_ERR_ARG, "sim %d: transmission needs network, seasonality and scalars", r);

@@ -65,3 +65,71 @@ def test_ri_base_value_closed_forms_match_tick_by_tick(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout
     assert "bad 0" in out.stdout
+
+
+GAP_SRC = r"""
+#include <stdio.h>
+#include <stdint.h>
+
+/* For every int16 base, step and first RI tick index: the RI ticks between
+ * the first two eligibilities of the reference's subtraction loop.  The
+ * engine gives each agent one due tick a run, which holds while the run's
+ * last RI tick index is below 65536 / step (lpg_check_desc refuses longer
+ * runs with RI): that needs every gap to be at least 65536 / step - 1. */
+int main(void) {
+  const int steps[] = {1, 2, 7, 14, 16, 30, 182, 365};
+  long bad = 0;
+  for (int si = 0; si < 8; ++si) {
+    const int s = steps[si];
+    for (int m_lo = 1; m_lo <= 3; ++m_lo)
+      for (int u = -32768; u <= 32767; u += (s < 7 ? 7 : 1)) {
+        int16_t x = (int16_t)u;
+        long m1 = -1, gap = -1;
+        const long limit = m_lo + 3L * (65536 / s) + 10;
+        for (long m = m_lo; m <= limit && gap < 0; ++m) {
+          const int32_t timer = (int32_t)x - s;
+          const int el = (m == 1) ? (timer <= 0 && timer >= -s) : (timer <= 0 && timer > -s);
+          if (el) {
+            if (m1 < 0) m1 = m;
+            else gap = m - m1;
+          }
+          x = (int16_t)timer;
+        }
+        if (gap < 0 || gap < 65536 / s - 1) {
+          if (bad < 5) printf("u=%d s=%d m_lo=%d gap=%ld\n", u, s, m_lo, gap);
+          ++bad;
+        }
+      }
+  }
+  printf("bad %ld\n", bad);
+  return bad != 0;
+}
+"""
+
+
+def test_no_agent_is_due_for_ri_twice_within_the_runs_the_engine_accepts(tmp_path):
+    src = tmp_path / "gap.c"
+    src.write_text(GAP_SRC)
+    exe = tmp_path / "gap"
+    subprocess.run(["gcc", "-O2", "-o", str(exe), str(src)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout
+
+
+def test_runs_where_an_ri_timer_comes_round_twice_are_refused():
+    """With step 14 the last RI tick index must stay below 65536 // 14 =
+    4681: a run of 65533 ticks after tick 0 is accepted, 65534 refused."""
+    import pytest
+
+    from laser_polio_gb300 import _lib, synthetic
+    from laser_polio_gb300.engine import make_desc
+
+    for dur, ok in ((65533, True), (65534, False)):
+        params, _ = synthetic.bundle(kind="zamfara", n_agents=2000, n_nodes=3, dur=dur, seed=1)
+        assert params["ri_enabled"] and params["ri_step"] == 14
+        desc, _keep = make_desc(params)
+        if ok:
+            _lib.check_desc(desc)
+        else:
+            with pytest.raises(ValueError, match="come round twice"):
+                _lib.check_desc(desc)
