@@ -164,3 +164,63 @@ def test_gpu_run_replicates_equals_each_oracle_run():
         cols_g = {k: getattr(s.people, k) for k in cols_o}
         assert_same(res_o, res_g, f"replicate {i} result")
         assert_same(cols_o, cols_g, f"replicate {i} column", count=so.count)
+
+
+def test_replicate_objective_reports_failures_and_averages_the_rest(monkeypatch):
+    """calibrate.replicate_objective, the reference's objective loop
+    (calib/objective.py:47-82) as one batch: every buildable replicate goes
+    to one run_replicates call; a replicate that cannot be built, whose run
+    fails or whose scoring fails is reported and left out; the value is the
+    mean of the others' scores."""
+    from laser_polio_gb300 import calibrate
+
+    batches = []
+
+    def fake_run(sims, autotune=False):
+        batches.append((list(sims), autotune))
+        return [None if s.rep != 3 else RuntimeError("device error") for s in sims]
+
+    monkeypatch.setattr(engine, "run_replicates", fake_run)
+
+    def make_sim(params, rep):
+        if rep == 1:
+            raise ValueError("bad parameters")
+        return types.SimpleNamespace(rep=rep, r0=params["r0"], pars=types.SimpleNamespace(seed=100 + rep))
+
+    def score(sim):
+        if sim.rep == 4:
+            raise KeyError("no target")
+        return -float(sim.rep) * sim.r0
+
+    logged = []
+    out = calibrate.replicate_objective(make_sim, {"r0": 2.0}, score, n_replicates=6, autotune=True,
+                                        log=logged.append)
+    assert len(batches) == 1 and [s.rep for s in batches[0][0]] == [0, 2, 3, 4, 5] and batches[0][1] is True
+    assert out["scores"] == [0.0, -4.0, -10.0] and out["seeds"] == [100, 102, 105]
+    assert out["value"] == pytest.approx(-14.0 / 3)
+    assert [r for r, _ in out["errors"]] == [1, 3, 4] and len(logged) == 3
+    none = calibrate.replicate_objective(lambda p, r: (_ for _ in ()).throw(ValueError("x")), {}, score,
+                                         n_replicates=2, log=logged.append)
+    assert np.isnan(none["value"]) and none["scores"] == [] and len(none["errors"]) == 2
+
+
+@pytest.mark.gpu
+def test_gpu_replicate_objective_scores_each_replicate_as_its_own_run():
+    """Scores of a batched trial equal those of the same replicates run one
+    by one with sim.run() (the batch changes the time, not the results)."""
+    from laser_polio_gb300 import calibrate
+
+    def make_sim(params, rep):
+        return synthetic.zamfara_like(n_agents=30_000, dur=50, seed=40 + rep)
+
+    def score(sim):
+        return float(np.log1p(np.asarray(sim.results.new_exposed, np.float64)).sum())
+
+    out = calibrate.replicate_objective(make_sim, {}, score, n_replicates=3, log=lambda m: None)
+    alone = []
+    for rep in range(3):
+        s = make_sim({}, rep)
+        s.run()
+        alone.append(score(s))
+    assert out["errors"] == [] and out["scores"] == alone
+    assert out["value"] == pytest.approx(float(np.mean(alone)))
