@@ -62,8 +62,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--agents", type=float, default=2.2e8)
-    ap.add_argument("--nodes", type=int, default=774)
+    ap.add_argument("--agents", type=float, default=None, help="agents (2.2e8; 1e9 with --continental)")
+    ap.add_argument("--nodes", type=int, default=None, help="nodes (774; 4000 with --continental)")
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--cpu-seconds", type=float, default=25.0)
     ap.add_argument("--no-e2e", action="store_true")
@@ -89,7 +89,12 @@ def parse():
                     help="parameter-set replicates of the continental table in one handle (1e9 agents in all)")
     ap.add_argument("--export", action="store_true",
                     help="instead: save_sim_results' CSV of a Nigeria-scale results table (host only)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.agents is None:
+        args.agents = 1e9 if args.continental else 2.2e8
+    if args.nodes is None:
+        args.nodes = 4000 if args.continental else 774
+    return args
 
 
 def dist_env():
@@ -506,8 +511,7 @@ def continental_sim(args):
     import laser_polio_gb300 as lp
     from laser_polio_gb300 import synthetic
 
-    agents = int(args.agents if args.agents != 2.2e8 else 1e9)
-    nodes = args.nodes if args.nodes != 774 else 4000
+    agents, nodes = int(args.agents), int(args.nodes)
     pars, immun, rng = synthetic.continental_pars(n_agents=agents, n_nodes=nodes, dur=365, seed=args.seed)
     prev = np.zeros(nodes, np.int64)
     prev[rng.choice(nodes, size=2, replace=False)] = 10
@@ -1003,8 +1007,8 @@ def incidence_arm(args):
     elif args.continental:
         # the continental shapes: two recording runs of 1.3e9-slot tables would hold
         # their host columns twice over, so seeded aggregates of those shapes stand in
-        inp = synthetic.incidence_inputs(T=T, n_nodes=args.nodes if args.nodes != 774 else 4000, n_agents=1e9,
-                                         seed=args.seed, mu=np.log(2.5e5), sigma=0.9, side_km=5000.0)
+        inp = synthetic.incidence_inputs(T=T, n_nodes=args.nodes, n_agents=args.agents, seed=args.seed,
+                                         mu=np.log(2.5e5), sigma=0.9, side_km=5000.0)
         G, S = inp["r0s"].shape[0], inp["beta"].shape[2]
         rng = np.random.default_rng(args.seed + 1)
         pert = dict(inp, R=1.1, amp=0.35, peak=170.0, k=0.6, r0s=inp["r0s"] * rng.lognormal(0.0, 0.05, G))
