@@ -29,6 +29,17 @@ reference's loops do).
             agents each, about 4e8 in all) over the same ticks in one handle,
             against the same replicates run one after another.
 
+Other lines, one per call:
+  --batch R       the batch measurement alone.
+  --incidence T   the adjoint of expected incidence over T ticks, on
+                  aggregates recorded by Nigeria-scale forward runs
+                  (--incidence-data synthetic: seeded aggregates).
+  --continental   4000 nodes, 1e9 agents, 365 ticks through SEIR_ABM, a
+                  profiling pass over the whole run and 4 parameter-set
+                  replicates of one table (with --incidence: the adjoint on
+                  aggregates of the continental shapes).
+  --export        the results CSV writer (host only).
+
 python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
 
