@@ -183,11 +183,9 @@ NCU_TRAFFIC_SOURCE = {
 #     bytes and 128 risks (512 B); per agent exposed, its reference index,
 #     state (claimed, then exposed), strain, timers, event tick and its
 #     index (15 B).
-#   k_sweep_rs (k_sweep_b) on RI ticks: through the RI due lists, 4 B per
-#     list entry read (the due ones' state bytes with the queue); through the index, 4 B per
-#     RI due index entry read and per visited sub-block its state,
-#     chronically-missed flags, RI timers, reference indexes and dates of
-#     birth (128 x 12 B) and the index write (4 B).
+#   k_sweep_rs (k_sweep_b) on RI ticks: 4 B per RI due index entry read; per visited
+#     sub-block its state, chronically-missed flags, RI timers, reference
+#     indexes and dates of birth (128 x 12 B) and the index write (4 B).
 #   k_node_mix: per tick, the network entries of the sources with infected
 #     agents (nodes x such sources x 16 B per simulation, two 8-byte
 #     fixed-point parts per entry: entries of sources without infectivity
@@ -209,7 +207,7 @@ SEL_CLAIM_B = 15.0
 NODE_TX_CHUNK_B = 20.0
 NODE_TX_NET_B = 16.0  # a network entry in its two fixed-point parts
 NODE_TX_NODE_B = 248.0
-RI_INDEX_B, RI_DUE_B, RI_LIST_B = 4.0, 128.0 * 12.0 + 4.0, 4.0
+RI_INDEX_B, RI_DUE_B = 4.0, 128.0 * 12.0 + 4.0
 
 
 def merge_selection(prof):
@@ -244,7 +242,7 @@ def kernel_alg_bytes(params, ticks, cnt, work, new_exposed, sources):
                       + SWEEP_EVT_B * work["sweep_evt_due"] + SWEEP_DOD_B * work["sweep_dod_due"]
                       + (QUEUE_ENTRY_B + DSQ_ENTRY_B) * work["queue_ds"]),
         "k_sweep_b": staged + RI_INDEX_B * work["ri_index"] + RI_DUE_B * work["ri_due"]
-                     + RI_LIST_B * work.get("ri_list", 0) + QUEUE_ENTRY_B * work["queue_rs"],
+                     + QUEUE_ENTRY_B * work["queue_rs"],
         "k_evb": EVB_ENTRY_B * work["queue_rs"],
         "k_select": SEL_TARGET_B * work["sel_targets"] + SEL_CLAIM_B * float(new_exposed),
         "k_node_mix": node_mix,

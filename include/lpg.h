@@ -290,8 +290,7 @@ enum {
   LPG_CTR_SEL_NODE_ROUNDS = 7, /* node rounds after round 0 */
   LPG_CTR_RI_INDEX = 8,      /* RI due index entries k_sweep_rs read */
   LPG_CTR_RI_DUE = 9,        /* sub-blocks it visited with an RI due tick come */
-  LPG_CTR_RI_LIST = 10,      /* RI due list entries it read (RI ticks without an SIA) */
-  LPG_NUM_COUNTERS = 11
+  LPG_NUM_COUNTERS = 10
 };
 /* Copies min(n, LPG_NUM_COUNTERS) counters to out (host memory) after the
  * handle's stream has finished; returns LPG_OK or an error code. */

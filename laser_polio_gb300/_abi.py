@@ -218,7 +218,7 @@ class lpg_sim_state(C.Structure):
 
 # lpg.h's LPG_CTR_* indices, in order
 COUNTER_NAMES = ("sweep_index", "sweep_due", "sweep_evt_due", "sweep_dod_due", "queue_ds", "queue_rs",
-                 "sel_targets", "sel_node_rounds", "ri_index", "ri_due", "ri_list")
+                 "sel_targets", "sel_node_rounds", "ri_index", "ri_due")
 
 
 class lpg_profile(C.Structure):

@@ -1024,46 +1024,14 @@ extern "C" int lpg_start(lpg_handle* h) {
   CK(cudaMemsetAsync(W.sub_rdt, 0x7f, sizeof(int32_t) * (size_t)W.total_chunks * LPG_NSUB, st));
   k_ri_index<<<std::max(1, h->sm_count * 8), 256, 0, st>>>(W, W.sub_rdt, 1, nullptr);
   CK(cudaGetLastError());
-  bool any_ril = false;
   for (int r = 0; r < R; ++r) {
     hr[r].started = 1;
     hr[r].cur_t = 0;
     hr[r].active = 1;
     hr[r].vd_tick = hr[r].ri_tick = hr[r].sia_n = hr[r].seed_n = 0;
     hr[r].nb_total = 0;
-    hr[r].rdt_new_min = LPG_NO_DOD;
-    hr[r].ril_maxb = -1;
-    /* due ticks / step must fit the entries' 21 bits */
-    hr[r].ril_on = hr[r].ri_enabled && (hr[r].comps & LPG_COMP_RI) && hr[r].ri_step > 0 && hr[r].nt > 1 &&
-                   (int64_t)hr[r].nt / hr[r].ri_step < (1 << 21);
-    any_ril = any_ril || hr[r].ril_on;
   }
   CK(cudaMemcpyAsync(W.reps, hr.data(), sizeof(DevRep) * R, cudaMemcpyHostToDevice, st));
-  /* the RI due lists: counted per chunk, offsets formed here, then filled */
-  if (any_ril) {
-    const int32_t C = W.total_chunks;
-    int32_t* d_cnt = nullptr;
-    if (dalloc(h, &d_cnt, C)) return LPG_ERR_NOMEM;
-    CK(cudaMemsetAsync(d_cnt, 0, sizeof(int32_t) * C, st));
-    const int list_blocks = std::max(1, h->sm_count * 8);
-    k_ri_list<<<list_blocks, 256, 0, st>>>(W, d_cnt, nullptr);
-    CK(cudaGetLastError());
-    std::vector<int32_t> cnt(C), off(C + 1);
-    CK(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int32_t) * C, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    int64_t e = 0;
-    for (int32_t c = 0; c < C; ++c) {
-      off[c] = (int32_t)e;
-      e += cnt[c];
-      if (e >= INT32_MAX) return fail(h, LPG_ERR_ARG, "RI due lists need more than 2^31 entries");
-    }
-    off[C] = (int32_t)e;
-    if (dalloc(h, &W.ril_ent, (size_t)e) || dupload(h, &W.ril_coff, off)) return LPG_ERR_NOMEM;
-    k_ri_list<<<list_blocks, 256, 0, st>>>(W, nullptr, W.ril_ent);
-    CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(st));
-    dfree_one(h, d_cnt);
-  }
   k_end<<<(G + 255) / 256, 256, 0, st>>>(W);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));

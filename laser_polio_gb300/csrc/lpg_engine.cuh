@@ -158,10 +158,6 @@ typedef struct {
   int32_t csr_flip;    /* the node -> chunk lists were rebuilt this tick (k_newborns fills them) */
   int32_t used_before; /* used_chunks before this tick's new chunks */
   int32_t ei_sum;      /* k_end: nodes with E > 0 plus nodes with I > 0 (the next tick's stop rule) */
-  int32_t ril_on;      /* the RI due lists (lpg_start) cover this simulation's initial population */
-  int32_t rdt_new_min; /* earliest RI due tick given to a newborn so far (LPG_NO_DOD: none) */
-  int32_t ril_maxb;    /* latest due tick / RI step in its lists (-1: empty) */
-  int32_t pad3;
 } DevRep;
 
 /* Global device state shared by the kernels of one handle. */
@@ -224,12 +220,6 @@ typedef struct {
   uint32_t* end_done;      /* CTAs of k_end done with the tick (the last prepares the next) */
   unsigned long long* grid_bar; /* arrivals at k_sel_round0's grid barrier (only grows) */
   int32_t test_bar_skip;   /* test hook: CTA 0 of k_sel_round0 does not arrive at its barrier */
-  /* RI due lists, per chunk: the initial population's alive agents whose RI
-   * due tick falls in the run, in position order, each as (due tick / RI
-   * step) << 11 | offset in the chunk; chunk c holds entries
-   * [ril_coff[c], ril_coff[c + 1]) (none for chunks made after the start) */
-  uint32_t* ril_ent;
-  int32_t* ril_coff;
 } DevWorld;
 
 #endif

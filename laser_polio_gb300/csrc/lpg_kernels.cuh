@@ -118,14 +118,6 @@ __device__ __forceinline__ unsigned long long neg64(uint64_t w) { return (unsign
 /* RI runs for the simulation: RI_ABM among the components and vx_prob_ri
  * set (model.py:1920-1923).  Only then do the timers count down. */
 __device__ __forceinline__ bool ri_runs(const DevRep* rp) { return (rp->comps & LPG_COMP_RI) && rp->ri_enabled; }
-/* On this tick RI (if it runs) can go through the RI due lists: they hold
- * every agent due (no newborn has been given a due tick at or before it). */
-__device__ __forceinline__ bool ri_by_list(const DevRep* rp) { return rp->ril_on && rp->cur_t < rp->rdt_new_min; }
-/* An RI tick with agents to queue: through the index, or through lists
- * that still hold agents due at or after it. */
-__device__ __forceinline__ bool ri_work(const DevRep* rp) {
-  return rp->ri_tick && !(ri_by_list(rp) && rp->cur_t / rp->ri_step > rp->ril_maxb);
-}
 /* RI due tick of an agent from its base timer u, reference index and date
  * of birth (lpg_ri.h). */
 __device__ __forceinline__ int32_t ri_due_of(const DevRep* rp, int16_t u, uint32_t ref, int32_t dob) {
@@ -408,7 +400,6 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
   const int64_t* nbe = end_sm ? s_end : W.nb_end + nb;
   const int64_t* km = km_sm ? s_km : rp->km;
   const bool ri_on = ri_runs(rp);
-  int32_t rdt_lo = LPG_NO_DOD; /* earliest RI due tick this thread gave a newborn */
   for (int64_t j0 = (int64_t)blockIdx.x * blockDim.x;; j0 += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = j0 + threadIdx.x;
     if (__all_sync(FULLMASK, j >= total)) break;
@@ -469,7 +460,6 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
     const uint64_t wg = run_sum_u64(w, mg), wc = run_sum_u64(w, mc), wsb = run_sum_u64(w, ms);
     const int32_t ng = run_sum_i32(one, mg);
     const int32_t dmin = run_min_i32(dod, ms), rmin = run_min_i32(rdt, ms);
-    rdt_lo = min(rdt_lo, rdt);
     if (on && hg) {
       atomicAdd(&W.tot[(int64_t)TT_S * G + g], ng);
       if (wg) atomicAdd((unsigned long long*)&W.sw[g], (unsigned long long)wg);
@@ -481,11 +471,6 @@ __global__ void __launch_bounds__(256) k_newborns(DevWorld W) {
       if (wsb) atomicAdd((unsigned long long*)&W.sub_w[ks], (unsigned long long)wsb);
     }
   }
-  /* the RI due lists hold the initial population only: a newborn due in the
-   * run sends its simulation's later RI ticks back to the index (every lane
-   * left the loop together; a due tick past the run changes nothing) */
-  rdt_lo = __reduce_min_sync(FULLMASK, rdt_lo);
-  if (lane == 0 && rdt_lo < rp->nt && rdt_lo < rp->rdt_new_min) atomicMin(&W.reps[blockIdx.y].rdt_new_min, rdt_lo);
 }
 
 /* The sweeps.
@@ -563,7 +548,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
 }
 
 /* per-simulation flags of the launch, cached in shared memory */
-enum { SF_WORK = 1, SF_DENSE = 2, SF_RI = 16, SF_SIA = 32, SF_LIST = 64 };
+enum { SF_WORK = 1, SF_DENSE = 2, SF_RI = 16, SF_SIA = 32 };
 
 struct SweepPlan {
   int32_t total, nreps;
@@ -999,39 +984,6 @@ __device__ __noinline__ void ri_direct(DevWorld& W, const DevRep* rp, uint64_t* 
   if (lane == 0 && n_due) atomicAdd(&W.ctr[LPG_CTR_RI_DUE], (unsigned long long)n_due);
 }
 
-/* k_sweep_rs on an RI tick without SIA, for a simulation whose RI due lists
- * hold every agent due today (no newborn has been given a due tick at or
- * before it), over its chunks [c0, c1): one warp per chunk reads the
- * chunk's list in order and queues the entries due today that are still
- * alive (the test of ri_due16: an agent's due tick does not move), so the
- * queue keeps position order.  The agents and the queue are those of
- * ri_direct; the sub-block index sub_rdt is left as it was, still a lower
- * bound.  All threads of the CTA run it. */
-__device__ __noinline__ void ri_list(DevWorld& W, const DevRep* rp, uint64_t* slab, uint32_t* s_cnt, int64_t c0,
-                                     int64_t c1, int t) {
-  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const uint32_t bkt = (uint32_t)(t / rp->ri_step);
-  uint32_t listed = 0;
-  for (int64_t c = c0 + (threadIdx.x >> 5); __any_sync(FULLMASK, c < c1); c += nw) {
-    const bool on_c = c < c1;
-    const int32_t e0 = on_c ? __ldcg(&W.ril_coff[c]) : 0, e1 = on_c ? __ldcg(&W.ril_coff[c + 1]) : 0;
-    listed += (uint32_t)(e1 - e0);
-    for (int32_t i0 = e0; i0 < e1; i0 += 32) { /* warp-uniform: one chunk per warp */
-      const int32_t i = i0 + lane;
-      bool due = false;
-      int64_t pos = 0;
-      if (i < e1) {
-        const uint32_t e = __ldcg(&W.ril_ent[i]);
-        pos = c * LPG_CHUNK + (e & (LPG_CHUNK - 1));
-        due = (e >> 11) == bkt && W.ds[pos] >= 0;
-      }
-      const uint32_t at = slab_reserve(s_cnt, due ? 1u : 0u);
-      if (due) slab[at] = q_entry(pos, QB_RI, 0);
-    }
-  }
-  if (lane == 0 && listed) atomicAdd(&W.ctr[LPG_CTR_RI_LIST], (unsigned long long)listed);
-}
-
 /* The first work item at or after w whose simulation is staged (dense), or w1. */
 __device__ __forceinline__ int32_t dense_from(const SweepPlan& P, int32_t w, int32_t w1) {
   while (w < w1) {
@@ -1064,11 +1016,10 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
       const DevRep* rp = &W.reps[r];
       uint8_t f = 0;
       if (rp->active) {
-        if (rp->sia_n > 0) f |= SF_SIA | (rp->ri_tick ? SF_RI : 0);
-        else if (ri_work(rp)) f |= SF_RI; /* (none when the lists have nothing due from today on) */
+        if (rp->ri_tick) f |= SF_RI;
+        if (rp->sia_n > 0) f |= SF_SIA;
         if (f) f |= SF_WORK;
-        if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due lists or the due index */
-        else if ((f & SF_RI) && ri_by_list(rp)) f |= SF_LIST;
+        if (f & SF_SIA) f |= SF_DENSE; /* RI alone: through the due index */
       }
       P.flags[r] = f;
       P.cbase[r] = rp->chunk_base;
@@ -1105,14 +1056,9 @@ __global__ void __launch_bounds__(LPG_SWEEP_BLOCK) k_sweep_rs(DevWorld W) {
       (void)stage_end(P, w, w1, &r);
       const int32_t we = min(w1, P.off[r + 1]);
       if ((P.flags[r] & (SF_WORK | SF_DENSE)) == SF_WORK) {
-        if (P.flags[r] & SF_LIST) {
-          ri_list(W, &W.reps[r], slab, &s_qcnt, P.cbase[r] + (int64_t)(w - P.off[r]), P.cbase[r] + (int64_t)(we - P.off[r]),
-                  P.tick[r]);
-        } else {
-          const int64_t sb0 = (P.cbase[r] + (int64_t)(w - P.off[r])) * LPG_NSUB;
-          ri_direct(W, &W.reps[r], slab, &s_qcnt, sb0, (int64_t)(we - w) * LPG_NSUB, P.tick[r],
-                    reinterpret_cast<uint32_t*>(sm_stage), &s_ndue);
-        }
+        const int64_t sb0 = (P.cbase[r] + (int64_t)(w - P.off[r])) * LPG_NSUB;
+        ri_direct(W, &W.reps[r], slab, &s_qcnt, sb0, (int64_t)(we - w) * LPG_NSUB, P.tick[r],
+                  reinterpret_cast<uint32_t*>(sm_stage), &s_ndue);
       }
       w = we;
     }
@@ -1510,7 +1456,7 @@ __global__ void __launch_bounds__(256) k_evb(DevWorld W, int nslabs) {
     /* nothing queued unless some simulation has RI or SIA work today */
     int any = 0;
     for (int r = 0; r < W.n_reps && !any; ++r)
-      any = W.reps[r].active && (ri_work(&W.reps[r]) || W.reps[r].sia_n > 0);
+      any = W.reps[r].active && (W.reps[r].ri_tick || W.reps[r].sia_n > 0);
     if (!any) return;
   }
   const uint32_t n = q_prefix(W, 1, s_pre, nslabs);
@@ -3242,44 +3188,6 @@ __global__ void k_ri_index(DevWorld W, int32_t* out, int at_start, int* bad) {
       }
       m = __reduce_min_sync(FULLMASK, m);
       if (lane == 0 && q < np) atomicMin(&out[pos >> 7], m);
-    }
-  }
-}
-
-/* The RI due lists, at the start (lpg_start), one warp per chunk of a
- * simulation with lists: the chunk's alive agents whose RI due tick falls
- * in the run, counted into cnt[chunk] (ent null), or written in position
- * order from ril_coff[chunk] (ent: W.ril_ent). */
-__global__ void k_ri_list(DevWorld W, int32_t* cnt, uint32_t* ent) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < W.total_chunks; c += warps) {
-    const int4 m = W.cmeta[c];
-    if (m.x < 0) continue; /* warp-uniform: one chunk per warp */
-    const DevRep* rp = &W.reps[W.node_rep[m.x]];
-    if (!rp->ril_on) continue;
-    int32_t n = 0, at = ent ? W.ril_coff[c] : 0, maxb = -1;
-    for (int o0 = 0; o0 < LPG_CHUNK; o0 += 32) {
-      const int64_t pos = c * LPG_CHUNK + o0 + lane;
-      bool in = false;
-      int32_t d = LPG_NO_DOD;
-      if (W.ds[pos] >= 0) {
-        d = W.rdt[pos];
-        in = d != LPG_NO_DOD && d >= 1 && d < rp->nt;
-      }
-      const unsigned b = __ballot_sync(FULLMASK, in);
-      if (in) maxb = max(maxb, d / rp->ri_step);
-      if (ent && in)
-        ent[at + __popc(b & ((1u << lane) - 1u))] = ((uint32_t)(d / rp->ri_step) << 11) | (uint32_t)(o0 + lane);
-      at += __popc(b);
-      n += __popc(b);
-    }
-    if (!ent) {
-      maxb = __reduce_max_sync(FULLMASK, maxb);
-      if (lane == 0) {
-        cnt[c] = n;
-        if (maxb >= 0) atomicMax(&W.reps[W.node_rep[m.x]].ril_maxb, maxb);
-      }
     }
   }
 }

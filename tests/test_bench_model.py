@@ -1,6 +1,6 @@
 """The benchmark's host-side pieces, on the CPU: the continental workload's
 synthetic shapes, the parameters the byte model reads from a simulation
-description, and the byte model itself (bench.kernel_alg_bytes)."""
+description, and the byte model's mixing term (bench.kernel_alg_bytes)."""
 
 import sys
 from pathlib import Path
@@ -61,12 +61,9 @@ def test_mixing_bytes_count_only_sources_with_infected_agents():
     ticks = np.arange(1, 4)
     cnt = np.full(5, 1000)
     work = dict.fromkeys(("sweep_index", "sweep_due", "sweep_evt_due", "sweep_dod_due", "queue_ds", "queue_rs",
-                          "sel_targets", "ri_index", "ri_due", "ri_list"), 0)
+                          "sel_targets", "ri_index", "ri_due"), 0)
     none = bench.kernel_alg_bytes(p, ticks, cnt, work, 0, np.zeros(5, int))["k_node_mix"]
     some = bench.kernel_alg_bytes(p, ticks, cnt, work, 0, np.array([0, 2, 2, 2, 0]))["k_node_mix"]
     chunks = 3 * bench.NODE_TX_CHUNK_B * 4096 / 2048
     assert none == 3 * 10 * 3 * 8.0 + chunks
     assert some - none == 3 * 10 * 2 * bench.NODE_TX_NET_B
-    # the RI due lists' entries are 4 B each
-    work["ri_list"] = 1000
-    assert bench.kernel_alg_bytes(p, ticks, cnt, work, 0, np.zeros(5, int))["k_sweep_b"] == 4000.0
